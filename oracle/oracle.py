@@ -1,0 +1,478 @@
+"""ORACLE — test infrastructure only.
+
+CPU restatement of serac::Functional's global layer for structured hexahedral
+H1 meshes on one rank (P = I): element restriction (gather / scatter-add),
+domain + boundary integrals, Jacobian-vector products, element stiffness
+assembly to CSR, Dirichlet elimination and plain FP64 Krylov / Newton
+solvers.  The element arithmetic runs in ``liboracle.so`` (sfx_oracle.cpp).
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's ``cpu_baseline`` leg
+may import this module, and only as the checker / the timed CPU baseline.
+
+Reference semantics followed:
+  * Gather / ScatterAdd: E[(e*c + comp)*npe + j] = L[vdof]   (element_restriction.cpp:443-467)
+  * byNODES vdof = comp * num_nodes + node                  (element_restriction.cpp:425-432)
+  * residual: gather -> element kernel -> scatter            (functional.hpp:446-498)
+  * Jv: same with the element Jacobian action               (functional.hpp:406-432)
+  * CSR graph: sorted unique (row, col) pairs of every element's test x trial
+    vdofs; values += K_e[trial][test]                        (dof_numbering.hpp:290-351, functional.hpp:590-644)
+  * Dirichlet: residual rows set to zero (solid_mechanics.hpp:1118-1128);
+    matrix rows and columns eliminated with a unit diagonal
+    (boundary_condition_manager.hpp:91)
+  * Krylov: textbook CG (Saad, Iterative Methods, Alg. 6.18) and restarted
+    right-preconditioned GMRES (Alg. 9.5 in its flexible form) with Jacobi
+  * Newton without line search (equation_solver.cpp:79-200, max_line_search_iterations = 0)
+
+Mesh numbering (shared with the product by specification, not by code):
+  vertices   v(i,j,k) = i + (nx+1) (j + (ny+1) k), i in [0, nx]
+  elements   e = ex + nx (ey + ny ez); local vertices lexicographic a + 2b + 4c
+  H1 nodes   (p nx + 1)(p ny + 1)(p nz + 1) grid, node I + Nx (J + Ny K);
+             element local node (kx, ky, kz) lexicographic -> (p ex + kx, p ey + ky, p ez + kz)
+  boundary   sides 1..6 = z=0, y=0, x=1, y=1, x=0, z=1; each face is
+             parametrised (s, t) so that dX/ds x dX/dt points outward; faces
+             are ordered t-major within a side; local face node ks + (p+1) kt
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+_REF = None
+
+MAT_HEAT, MAT_NEOHOOKEAN, MAT_J2, MAT_THERMAL_TEST, MAT_ELASTIC_TEST, MAT_NONLINEAR_HEAT = range(6)
+BMAT_HEAT_FLUX, BMAT_TRACTION, BMAT_PRESSURE = range(3)
+COMPONENTS = {MAT_HEAT: 1, MAT_NONLINEAR_HEAT: 1, MAT_THERMAL_TEST: 1, MAT_NEOHOOKEAN: 3, MAT_J2: 3, MAT_ELASTIC_TEST: 3}
+NPARAMS = {MAT_HEAT: 2, MAT_NEOHOOKEAN: 2, MAT_J2: 4, MAT_NONLINEAR_HEAT: 3, MAT_THERMAL_TEST: 0, MAT_ELASTIC_TEST: 0}
+BCOMPONENTS = {BMAT_HEAT_FLUX: 1, BMAT_TRACTION: 3, BMAT_PRESSURE: 3}
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def _declare(lib, prefix):
+    f = getattr(lib, prefix + "geometric_factors")
+    f.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
+    f.restype = ctypes.c_int
+    f = getattr(lib, prefix + "face_geometric_factors")
+    f.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
+    f.restype = ctypes.c_int
+    f = getattr(lib, prefix + "domain")
+    args = [ctypes.c_int] * 4 + [ctypes.c_double] + [_dp] * 5 + [_dp, ctypes.c_int, _dp]
+    if prefix == "orc_":
+        args = args + [ctypes.c_int]
+    f.argtypes = args
+    f.restype = ctypes.c_int
+    f = getattr(lib, prefix + "boundary")
+    f.argtypes = [ctypes.c_int] * 4 + [ctypes.c_double] + [_dp] * 6
+    f.restype = ctypes.c_int
+
+
+def lib():
+    """The oracle's element-kernel library (built by ``make -C oracle``)."""
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "liboracle.so")
+        if not os.path.exists(path):
+            subprocess.check_call(["make", "-s", "-C", _HERE, "liboracle.so"])
+        _LIB = ctypes.CDLL(path)
+        _declare(_LIB, "orc_")
+    return _LIB
+
+
+def ref_lib():
+    """serac's own element kernels compiled from the reference sources, or None
+    where the reference tree is not present."""
+    global _REF
+    if _REF is None:
+        path = os.path.join(_HERE, "_ref", "libserac_ref.so")
+        if not os.path.exists(path):
+            return None
+        _REF = ctypes.CDLL(path)
+        _declare(_REF, "ref_")
+    return _REF
+
+
+# --------------------------------------------------------------------- mesh
+class StructuredHexMesh:
+    """nx x ny x nz hexahedra with the given vertex coordinates ((nx+1)(ny+1)(nz+1), 3)."""
+
+    def __init__(self, nx, ny, nz, vertices):
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.vertices = np.ascontiguousarray(vertices, dtype=np.float64).reshape(-1, 3)
+        assert self.vertices.shape[0] == (nx + 1) * (ny + 1) * (nz + 1)
+        self.ne = nx * ny * nz
+
+    def elem_vertex_ids(self):
+        nx, ny, nz = self.nx, self.ny, self.nz
+        ex, ey, ez = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+        ex, ey, ez = (a.transpose(2, 1, 0).ravel() for a in (ex, ey, ez))  # e = ex + nx(ey + ny ez)
+        ids = np.empty((self.ne, 8), dtype=np.int64)
+        for c in range(2):
+            for b in range(2):
+                for a in range(2):
+                    ids[:, a + 2 * b + 4 * c] = (ex + a) + (nx + 1) * ((ey + b) + (ny + 1) * (ez + c))
+        return ids
+
+    def elem_coords(self):
+        """(ne, 3, 8) vertex coordinates, lexicographic local order."""
+        ids = self.elem_vertex_ids()
+        return np.ascontiguousarray(self.vertices[ids].transpose(0, 2, 1))
+
+    def num_nodes(self, p):
+        return (p * self.nx + 1) * (p * self.ny + 1) * (p * self.nz + 1)
+
+    def elem_nodes(self, p):
+        nx, ny, nz = self.nx, self.ny, self.nz
+        Nx, Ny = p * nx + 1, p * ny + 1
+        e = np.arange(self.ne)
+        ex, ey, ez = e % nx, (e // nx) % ny, e // (nx * ny)
+        n = p + 1
+        conn = np.empty((self.ne, n ** 3), dtype=np.int64)
+        for kz in range(n):
+            for ky in range(n):
+                for kx in range(n):
+                    conn[:, kx + n * (ky + n * kz)] = (p * ex + kx) + Nx * ((p * ey + ky) + Ny * (p * ez + kz))
+        return conn
+
+    # side -> (fixed axis, fixed index(0/1), s axis, t axis)
+    SIDES = {1: (2, 0, 1, 0), 2: (1, 0, 0, 2), 3: (0, 1, 1, 2), 4: (1, 1, 2, 0), 5: (0, 0, 2, 1), 6: (2, 1, 0, 1)}
+
+    def boundary_faces(self, p, sides):
+        """Face vertex coordinates (nf, 3, 4) and face node ids (nf, (p+1)^2)."""
+        dims = (self.nx, self.ny, self.nz)
+        Nn = (p * self.nx + 1, p * self.ny + 1, p * self.nz + 1)
+        coords, nodes = [], []
+        n = p + 1
+        for side in sides:
+            ax, hi, sa, ta = self.SIDES[side]
+            fixed_v = dims[ax] if hi else 0
+            for ft in range(dims[ta]):
+                for fs in range(dims[sa]):
+                    vids = []
+                    for b in range(2):
+                        for a in range(2):
+                            idx = [0, 0, 0]
+                            idx[ax] = fixed_v
+                            idx[sa] = fs + a
+                            idx[ta] = ft + b
+                            vids.append(idx[0] + (self.nx + 1) * (idx[1] + (self.ny + 1) * idx[2]))
+                    coords.append(self.vertices[vids].T)
+                    fn = []
+                    for kt in range(n):
+                        for ks in range(n):
+                            idx = [0, 0, 0]
+                            idx[ax] = p * fixed_v
+                            idx[sa] = p * fs + ks
+                            idx[ta] = p * ft + kt
+                            fn.append(idx[0] + Nn[0] * (idx[1] + Nn[1] * idx[2]))
+                    nodes.append(fn)
+        return np.ascontiguousarray(np.array(coords, dtype=np.float64)), np.array(nodes, dtype=np.int64)
+
+    def boundary_nodes(self, p, sides):
+        _, nodes = self.boundary_faces(p, sides)
+        return np.unique(nodes.ravel())
+
+
+def box_vertices(nx, ny, nz, perturb=0.0, seed=0):
+    """Unit-cube vertex grid; interior vertices moved by U(-perturb*h, perturb*h)
+    per coordinate with numpy's PCG64 generator seeded by ``seed``."""
+    x = np.linspace(0.0, 1.0, nx + 1)
+    y = np.linspace(0.0, 1.0, ny + 1)
+    z = np.linspace(0.0, 1.0, nz + 1)
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    V = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    if perturb > 0:
+        rng = np.random.default_rng(seed)
+        d = rng.uniform(-1.0, 1.0, size=V.shape) * perturb * np.array([1.0 / nx, 1.0 / ny, 1.0 / nz])
+        i = np.arange(V.shape[0])
+        ix, iy, iz = i % (nx + 1), (i // (nx + 1)) % (ny + 1), i // ((nx + 1) * (ny + 1))
+        interior = (ix > 0) & (ix < nx) & (iy > 0) & (iy < ny) & (iz > 0) & (iz < nz)
+        V[interior] += d[interior]
+    return V
+
+
+# ----------------------------------------------------------- element level
+def geometric_factors(Xe, Q, use_ref=False):
+    ne = Xe.shape[0]
+    nq = Q ** 3
+    Xq = np.zeros((ne, 3, nq))
+    Jq = np.zeros((ne, 3, 3, nq))
+    if use_ref:
+        rc = ref_lib().ref_geometric_factors(Q, ne, _ptr(Xe), _ptr(Xq), _ptr(Jq))
+    else:
+        rc = lib().orc_geometric_factors(Q, ne, _ptr(Xe), _ptr(Xq), _ptr(Jq))
+    assert rc == 0
+    return Xq, Jq
+
+
+def face_geometric_factors(Xf, Q, use_ref=False):
+    nf = Xf.shape[0]
+    nq = Q ** 2
+    Xq = np.zeros((nf, 3, nq))
+    Jq = np.zeros((nf, 2, 3, nq))
+    if nf:
+        if use_ref:
+            rc = ref_lib().ref_face_geometric_factors(Q, nf, _ptr(Xf), _ptr(Xq), _ptr(Jq))
+        else:
+            rc = lib().orc_face_geometric_factors(Q, nf, _ptr(Xf), _ptr(Xq), _ptr(Jq))
+        assert rc == 0
+    return Xq, Jq
+
+
+def element_kernel(mat, p, mode, uE, Xq, Jq, params=None, duE=None, state=None, update=False, t=0.0,
+                   use_ref=False, nthreads=1):
+    """mode 0 residual, 1 Jv, 2 K_e, on E-vectors (ne, c, npe)."""
+    ne = uE.shape[0]
+    c = COMPONENTS[mat]
+    nd = (p + 1) ** 3 * c
+    uE = np.ascontiguousarray(uE, dtype=np.float64)
+    if duE is not None:
+        duE = np.ascontiguousarray(duE, dtype=np.float64)
+    out = np.zeros((ne, nd, nd) if mode == 2 else (ne, nd))
+    prm = None
+    if NPARAMS[mat]:
+        prm = np.ascontiguousarray(np.broadcast_to(np.asarray(params, dtype=np.float64).reshape(-1, NPARAMS[mat]),
+                                                   (ne, NPARAMS[mat])))
+    if mat == MAT_J2 and state is None:
+        state = np.zeros((ne, (p + 1) ** 3, 10))
+    if ne == 0:
+        return out
+    if use_ref:
+        rc = ref_lib().ref_domain(mat, p, mode, ne, t, _ptr(prm), _ptr(uE), _ptr(duE), _ptr(Xq), _ptr(Jq),
+                                  _ptr(state), int(update), _ptr(out))
+    else:
+        rc = lib().orc_domain(mat, p, mode, ne, t, _ptr(prm), _ptr(uE), _ptr(duE), _ptr(Xq), _ptr(Jq),
+                              _ptr(state), int(update), _ptr(out), nthreads)
+    assert rc == 0, rc
+    return out
+
+
+def boundary_kernel(bmat, p, mode, uF, Xq, Jq, params, duF=None, t=0.0, use_ref=False):
+    nf = uF.shape[0]
+    c = BCOMPONENTS[bmat]
+    nd = (p + 1) ** 2 * c
+    out = np.zeros((nf, nd, nd) if mode == 2 else (nf, nd))
+    if nf == 0:
+        return out
+    prm = np.ascontiguousarray(np.asarray(params, dtype=np.float64).ravel())
+    uF = np.ascontiguousarray(uF, dtype=np.float64)
+    if duF is not None:
+        duF = np.ascontiguousarray(duF, dtype=np.float64)
+    fn = ref_lib().ref_boundary if use_ref else lib().orc_boundary
+    rc = fn(bmat, p, mode, nf, t, _ptr(prm), _ptr(uF), _ptr(duF), _ptr(Xq), _ptr(Jq), _ptr(out))
+    assert rc == 0, rc
+    return out
+
+
+# ------------------------------------------------------------ global layer
+def gather(uL, conn, c, nnodes):
+    """L-vector (byNODES) -> E-vector (ne, c, npe)."""
+    u = uL.reshape(c, nnodes)
+    return np.ascontiguousarray(u[:, conn].transpose(1, 0, 2)).reshape(conn.shape[0], c * conn.shape[1])
+
+
+def scatter_add(E, conn, c, nnodes):
+    out = np.zeros((c, nnodes))
+    E = E.reshape(conn.shape[0], c, conn.shape[1])
+    for k in range(c):
+        np.add.at(out[k], conn.ravel(), E[:, k, :].ravel())
+    return out.ravel()
+
+
+def elem_vdofs(conn, c, nnodes):
+    """(ne, c*npe) vdof ids, component-major per element."""
+    return (np.arange(c)[None, :, None] * nnodes + conn[:, None, :]).reshape(conn.shape[0], -1)
+
+
+class OracleFunctional:
+    """Functional<H1<p,c>(H1<p,c>)> on a structured hex mesh (P = I)."""
+
+    def __init__(self, mesh: StructuredHexMesh, p: int, c: int, use_ref: bool = False, nthreads: int = 1):
+        self.mesh, self.p, self.c, self.use_ref, self.nthreads = mesh, p, c, use_ref, nthreads
+        self.Q = p + 1
+        self.nnodes = mesh.num_nodes(p)
+        self.ndofs = self.nnodes * c
+        self.conn = mesh.elem_nodes(p)
+        self.Xq, self.Jq = geometric_factors(mesh.elem_coords(), self.Q, use_ref)
+        self.domain = []
+        self.boundary = []
+        self.state = None
+
+    def add_domain_integral(self, mat, params=None):
+        assert COMPONENTS[mat] == self.c
+        if mat == MAT_J2 and self.state is None:
+            self.state = np.zeros((self.mesh.ne, self.Q ** 3, 10))
+        self.domain.append((mat, params))
+
+    def add_boundary_integral(self, bmat, sides, params):
+        assert BCOMPONENTS[bmat] == self.c
+        Xf, fnodes = self.mesh.boundary_faces(self.p, sides)
+        Xq, Jq = face_geometric_factors(Xf, self.Q, self.use_ref)
+        self.boundary.append((bmat, params, fnodes, Xq, Jq))
+
+    def _apply(self, mode, u, du=None, update=False, t=0.0):
+        c, N = self.c, self.nnodes
+        out = np.zeros(self.ndofs)
+        uE = gather(u, self.conn, c, N)
+        duE = gather(du, self.conn, c, N) if du is not None else None
+        for mat, params in self.domain:
+            st = self.state if mat == MAT_J2 else None
+            rE = element_kernel(mat, self.p, mode, uE, self.Xq, self.Jq, params, duE, st, update, t, self.use_ref,
+                                self.nthreads)
+            out += scatter_add(rE, self.conn, c, N)
+        for bmat, params, fnodes, Xq, Jq in self.boundary:
+            uF = gather(u, fnodes, c, N)
+            duF = gather(du, fnodes, c, N) if du is not None else None
+            rF = boundary_kernel(bmat, self.p, mode, uF, Xq, Jq, params, duF, t, self.use_ref)
+            out += scatter_add(rF, fnodes, c, N)
+        return out
+
+    def residual(self, u, t=0.0, update_state=False):
+        return self._apply(0, u, update=update_state, t=t)
+
+    def jvp(self, u, du, t=0.0):
+        return self._apply(1, u, du, t=t)
+
+    def csr_graph(self):
+        vd = elem_vdofs(self.conn, self.c, self.nnodes)
+        rows = np.repeat(vd, vd.shape[1], axis=1).ravel()
+        cols = np.tile(vd, (1, vd.shape[1])).ravel()
+        key = np.unique(rows * self.ndofs + cols)
+        r, cl = key // self.ndofs, key % self.ndofs
+        row_ptr = np.zeros(self.ndofs + 1, dtype=np.int64)
+        np.add.at(row_ptr, r + 1, 1)
+        return np.cumsum(row_ptr), cl.astype(np.int64)
+
+    def assemble(self, u, t=0.0):
+        """CSR (row_ptr, col, val) of dR/du; the graph holds every element's
+        test x trial vdof pair (boundary faces add into it)."""
+        import scipy.sparse as sp
+
+        row_ptr, col = self.csr_graph()
+        n = self.ndofs
+        A = sp.csr_matrix((np.zeros(col.shape[0]), col, row_ptr), shape=(n, n))
+        uE = gather(u, self.conn, self.c, self.nnodes)
+        vd = elem_vdofs(self.conn, self.c, self.nnodes)
+        for mat, params in self.domain:
+            st = self.state if mat == MAT_J2 else None
+            K = element_kernel(mat, self.p, 2, uE, self.Xq, self.Jq, params, None, st, False, t, self.use_ref,
+                               self.nthreads)
+            # K[e][trial j][test i] -> row i, col j
+            rows = np.repeat(vd, vd.shape[1], axis=1)
+            cols = np.tile(vd, (1, vd.shape[1]))
+            A = A + sp.csr_matrix((K.transpose(0, 2, 1).ravel(), (rows.ravel(), cols.ravel())), shape=(n, n))
+        for bmat, params, fnodes, Xq, Jq in self.boundary:
+            uF = gather(u, fnodes, self.c, self.nnodes)
+            K = boundary_kernel(bmat, self.p, 2, uF, Xq, Jq, params, None, t, self.use_ref)
+            fv = elem_vdofs(fnodes, self.c, self.nnodes)
+            rows = np.repeat(fv, fv.shape[1], axis=1)
+            cols = np.tile(fv, (1, fv.shape[1]))
+            A = A + sp.csr_matrix((K.transpose(0, 2, 1).ravel(), (rows.ravel(), cols.ravel())), shape=(n, n))
+        A = A.tocsr()
+        A.sort_indices()
+        # keep exactly the element graph (explicit zeros included)
+        G = sp.csr_matrix((np.ones(col.shape[0]), col, row_ptr), shape=(n, n))
+        A = (A + 0.0 * G).tocsr()
+        A.sort_indices()
+        return A
+
+
+def eliminate_dirichlet(A, ess):
+    """Zero the rows and columns of ``ess`` and put 1 on their diagonal."""
+    import scipy.sparse as sp
+
+    n = A.shape[0]
+    keep = np.ones(n)
+    keep[ess] = 0.0
+    D = sp.diags(keep)
+    A2 = (D @ A @ D).tocsr()
+    A2 = A2 + sp.diags(1.0 - keep)
+    A2 = A2.tocsr()
+    A2.sort_indices()
+    return A2
+
+
+def cg(apply_A, b, diag, rtol=1e-10, maxiter=10000):
+    """Jacobi-preconditioned conjugate gradients; returns (x, iterations, ||r||/||b||)."""
+    x = np.zeros_like(b)
+    r = b.copy()
+    z = r / diag
+    p = z.copy()
+    rz = r @ z
+    nb = np.linalg.norm(b)
+    if nb == 0:
+        return x, 0, 0.0
+    for it in range(1, maxiter + 1):
+        Ap = apply_A(p)
+        alpha = rz / (p @ Ap)
+        x += alpha * p
+        r -= alpha * Ap
+        rn = np.linalg.norm(r) / nb
+        if rn < rtol:
+            return x, it, rn
+        z = r / diag
+        rz_new = r @ z
+        p = z + (rz_new / rz) * p
+        rz = rz_new
+    return x, maxiter, rn
+
+
+def fgmres(apply_A, b, precond, rtol=1e-8, restart=50, maxiter=2000, atol=0.0):
+    """Right-preconditioned flexible GMRES(restart) with modified Gram-Schmidt."""
+    n = b.shape[0]
+    x = np.zeros(n)
+    nb = np.linalg.norm(b)
+    if nb == 0:
+        return x, 0, 0.0
+    total = 0
+    while total < maxiter:
+        r = b - apply_A(x)
+        beta = np.linalg.norm(r)
+        if beta <= max(rtol * nb, atol):
+            return x, total, beta / nb
+        V = np.zeros((restart + 1, n))
+        Zs = np.zeros((restart, n))
+        H = np.zeros((restart + 1, restart))
+        V[0] = r / beta
+        g = np.zeros(restart + 1)
+        g[0] = beta
+        cs = np.zeros(restart)
+        sn = np.zeros(restart)
+        k = 0
+        for k in range(restart):
+            Zs[k] = precond(V[k])
+            w = apply_A(Zs[k])
+            for i in range(k + 1):
+                H[i, k] = w @ V[i]
+                w = w - H[i, k] * V[i]
+            H[k + 1, k] = np.linalg.norm(w)
+            if H[k + 1, k] > 0:
+                V[k + 1] = w / H[k + 1, k]
+            for i in range(k):
+                t = cs[i] * H[i, k] + sn[i] * H[i + 1, k]
+                H[i + 1, k] = -sn[i] * H[i, k] + cs[i] * H[i + 1, k]
+                H[i, k] = t
+            d = np.hypot(H[k, k], H[k + 1, k])
+            cs[k], sn[k] = H[k, k] / d, H[k + 1, k] / d
+            H[k, k] = d
+            H[k + 1, k] = 0.0
+            g[k + 1] = -sn[k] * g[k]
+            g[k] = cs[k] * g[k]
+            total += 1
+            if abs(g[k + 1]) <= max(rtol * nb, atol) or total >= maxiter:
+                break
+        y = np.linalg.solve(np.triu(H[: k + 1, : k + 1]), g[: k + 1])
+        x = x + y @ Zs[: k + 1]
+    r = b - apply_A(x)
+    return x, total, np.linalg.norm(r) / nb
