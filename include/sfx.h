@@ -1,0 +1,134 @@
+/*
+ * sfx — C ABI of the GB300-native weak-form engine (serac::Functional on
+ * hexahedral H1 meshes).  Plain pointers and sizes only; every array argument
+ * documented "device" is a CUDA device pointer owned by the caller, every
+ * "host" one a host pointer owned by the caller.  `stream` is a cudaStream_t
+ * (NULL = the legacy default stream).  Calls are asynchronous on `stream`
+ * unless stated otherwise.  All functions return SFX_OK (0) or a negative
+ * status; sfx_last_error() describes the last failure on the calling thread.
+ *
+ * Objects are not thread-safe (like serac::Functional, whose evaluation uses
+ * mutable scratch, functional.hpp:723-741): use one form per host thread.
+ *
+ * Reference interface each entry point replaces (serac, src/serac/...):
+ *   sfx_mesh_create_structured_hex  mesh/mesh_utils.cpp:149-153 buildCuboidMesh (+ EnsureNodes, :466)
+ *   sfx_form_create                 numerics/functional/functional.hpp:219-273 Functional ctor
+ *   sfx_form_add_domain_integral    numerics/functional/functional.hpp:286-317 AddDomainIntegral
+ *   sfx_form_add_boundary_integral  numerics/functional/functional.hpp:328-354 AddBoundaryIntegral
+ *   sfx_residual                    numerics/functional/functional.hpp:502-513 operator()(t, u)
+ *   sfx_linearize                   numerics/functional/functional.hpp:481-489 operator()(t, differentiate_wrt(u))
+ *   sfx_jvp / sfx_jvp_f32           numerics/functional/functional.hpp:556-566 Gradient::Mult / operator()
+ *   sfx_csr_* / sfx_assemble_csr    numerics/functional/functional.hpp:569-667 assemble(Gradient&)
+ *   sfx_update_qdata                numerics/functional/functional.hpp:523 updateQdata(bool)
+ *   sfx_set_qdata / sfx_get_qdata   numerics/functional/quadrature_data.hpp:111-144 QuadratureData<T>
+ */
+#ifndef SFX_H
+#define SFX_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SFX_OK 0
+#define SFX_ERR_INVALID (-1)     /* bad argument or call order */
+#define SFX_ERR_CUDA (-2)        /* a CUDA call failed */
+#define SFX_ERR_NONFINITE (-3)   /* a non-finite value was detected */
+#define SFX_ERR_TIMEOUT (-4)     /* a bounded device-side wait expired */
+#define SFX_ERR_UNSUPPORTED (-5) /* order / material / size not built */
+#define SFX_ERR_NOMEM (-6)       /* device allocation failed */
+
+/* Domain materials (q-functions instantiated in this library). Parameters per
+ * element, in this order:
+ *   SFX_MAT_HEAT            {k, f}            steady conduction, source f (heat_transfer.hpp:381-400, 488-505)
+ *   SFX_MAT_NEOHOOKEAN      {K, G}            MaterialStressFunctor<NeoHookean> (solid_material.hpp:98-127)
+ *   SFX_MAT_J2              {E, nu, sigma_y, H}  J2SmallStrain<LinearHardening>, small strain (solid_material.hpp:199-258)
+ *   SFX_MAT_THERMAL_TEST    {}                linear scalar model, all derivative blocks populated
+ *   SFX_MAT_ELASTIC_TEST    {}                linear vector model, all derivative blocks populated
+ *   SFX_MAT_NONLINEAR_HEAT  {k0, beta, f}     k(u) = k0 (1 + beta u^2)
+ */
+#define SFX_MAT_HEAT 0
+#define SFX_MAT_NEOHOOKEAN 1
+#define SFX_MAT_J2 2
+#define SFX_MAT_THERMAL_TEST 3
+#define SFX_MAT_ELASTIC_TEST 4
+#define SFX_MAT_NONLINEAR_HEAT 5
+
+/* Boundary materials: SFX_BMAT_HEAT_FLUX {q0, q1, alpha}: -(q0 + q1 x + alpha u);
+ * SFX_BMAT_TRACTION {t0[3], t1[3]}: -(t0 + t1 x); SFX_BMAT_PRESSURE {p}:
+ * p n(deformed) / |n(reference)| (solid_mechanics.hpp:1029-1099). */
+#define SFX_BMAT_HEAT_FLUX 0
+#define SFX_BMAT_TRACTION 1
+#define SFX_BMAT_PRESSURE 2
+
+/* Boundary sides of the structured box, as a bit mask (bit s-1 for side s):
+ * 1: z=0, 2: y=0, 3: x=1, 4: y=1, 5: x=0, 6: z=1. */
+
+typedef struct sfx_mesh_s* sfx_mesh;
+typedef struct sfx_form_s* sfx_form;
+
+const char* sfx_last_error(void);
+int sfx_version(void);
+
+/* Structured nx x ny x nz hexahedral mesh with trilinear geometry.
+ * vertices: host, (nx+1)(ny+1)(nz+1) x 3 doubles, vertex (i,j,k) at row
+ * i + (nx+1)(j + (ny+1)k).  The mesh copies the coordinates. */
+int sfx_mesh_create_structured_hex(int nx, int ny, int nz, const double* vertices, sfx_mesh* out);
+int sfx_mesh_destroy(sfx_mesh mesh);
+int sfx_mesh_num_elements(sfx_mesh mesh, int64_t* out);
+
+/* Functional<H1<order, components>(H1<order, components)> on `mesh`
+ * (order 1 or 2; components 1 or 3).  Q = order + 1 Gauss points per
+ * direction.  Global numbering: H1 node (I, J, K) of the
+ * (order nx + 1)(order ny + 1)(order nz + 1) grid is I + Nx (J + Ny K); the
+ * vector layout is byNODES: vdof = component * num_nodes + node. */
+int sfx_form_create(sfx_mesh mesh, int order, int components, sfx_form* out);
+int sfx_form_destroy(sfx_form form);
+int sfx_form_num_dofs(sfx_form form, int64_t* out);
+
+/* params: host; if per_element != 0, num_elements x nparams values, else
+ * nparams values used for every element.  At most one domain integral per
+ * form in this version. */
+int sfx_form_add_domain_integral(sfx_form form, int material, const double* params, int per_element);
+
+/* Boundary integral over the faces of the sides in side_mask; params: host. */
+int sfx_form_add_boundary_integral(sfx_form form, int bmaterial, int side_mask, const double* params);
+
+/* r = R(t, u) (device, num_dofs doubles each).  When sfx_update_qdata(form, 1)
+ * is in effect, quadrature-point state is committed by this call. */
+int sfx_residual(sfx_form form, double t, const double* u, double* r, void* stream);
+
+/* Record the linearisation point (t, u) for sfx_jvp / sfx_jvp_f32 /
+ * sfx_assemble_csr; also writes R(t, u) to r when r != NULL.  The form keeps
+ * its own copy of u (FP64 and FP32). */
+int sfx_linearize(sfx_form form, double t, const double* u, double* r, void* stream);
+
+/* dr = dR/du(t_lin, u_lin) du, in FP64, and in FP32 (FP32 accumulation). */
+int sfx_jvp(sfx_form form, const double* du, double* dr, void* stream);
+int sfx_jvp_f32(sfx_form form, const float* du, float* dr, void* stream);
+
+/* Sparsity of dR/du: every (test vdof, trial vdof) pair of every element,
+ * rows sorted, columns sorted within a row (dof_numbering.hpp:290-351).
+ * row_ptr: device, num_dofs + 1 int64; col: device, nnz int32. */
+int sfx_csr_nnz(sfx_form form, int64_t* nnz);
+int sfx_csr_graph(sfx_form form, int64_t* row_ptr, int32_t* col, void* stream);
+/* values: device, nnz doubles, dR/du at the linearisation point. */
+int sfx_assemble_csr(sfx_form form, double* values, void* stream);
+
+/* Diagonal of dR/du at the linearisation point (device, num_dofs doubles). */
+int sfx_assemble_diagonal(sfx_form form, double* diag, void* stream);
+
+/* Quadrature-point state (J2: 10 doubles per point: plastic strain 3x3
+ * row-major, accumulated plastic strain), host arrays
+ * [element][point][10].  flag: commit state on the next residual calls. */
+int sfx_update_qdata(sfx_form form, int flag);
+int sfx_qdata_size(sfx_form form, int64_t* num_doubles);
+int sfx_set_qdata(sfx_form form, const double* host_state);
+int sfx_get_qdata(sfx_form form, double* host_state);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SFX_H */

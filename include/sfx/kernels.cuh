@@ -1,0 +1,430 @@
+// sfx — fused element kernels for H1 hexahedra on sm_103a.
+//
+// One warp owns the quadrature points of one Q2 element (27 of 32 lanes) or
+// of four Q1 elements (8 lanes each).  Lane i holds quadrature point i and,
+// before interpolation / after integration, element node i (n = q = p + 1).
+// The sum-factorised tensor contractions of serac's hexahedron_H1.inl:169-280
+// are carried out with warp shuffles (no shared memory, no barriers):
+//   interpolate: x-pass, y-pass, z-pass produce u and grad_xi u at each point
+//   q-function : in registers, with forward-mode duals for the tangent
+//   integrate  : transposed passes; each lane ends with one nodal residual
+// Element residuals go to an E-vector; a node-owner kernel sums them into the
+// global vector in a fixed order (no floating-point atomics: deterministic).
+#pragma once
+
+#include <cstdint>
+#include <type_traits>
+
+#include "sfx/dual.hpp"
+#include "sfx/materials.hpp"
+#include "sfx/quadrature.hpp"
+#include "sfx/tensor.hpp"
+#include "sfx/tuple.hpp"
+
+namespace sfx {
+namespace kernels {
+
+enum Mode : int { RESIDUAL = 0, RESIDUAL_UPDATE = 1, JVP = 2 };
+
+/// Geometric factors per quadrature point, structure-of-arrays over all points
+/// of the mesh (index k * nq_total + e * nq + q):
+///   k = 0..8   J^{-1}  (row-major, [xi][x])
+///   k = 9      det(J) * w_q
+///   k = 10..12 X (position)
+///   k = 13..21 J = dX/dxi (row-major, [x][xi])
+constexpr int GEOM_STRIDE = 22;
+
+template <typename Real>
+struct DomainArgs {
+  const Real* u;          // L-vector (byNODES) of the trial field
+  const Real* du;         // direction for JVP
+  Real* out_e;            // E-vector [e][c][node]
+  const int32_t* conn;    // [e][node] global node ids
+  const Real* geom;       // GEOM_STRIDE x nq_total
+  double* state;          // quadrature-point state, SoA [k][e*nq+q] (doubles)
+  const double* params;   // per-element material parameters [e][nparams]
+  int64_t num_nodes;
+  int64_t num_elements;
+  double t;
+};
+
+template <int C, typename T>
+using value_t = std::conditional_t<C == 1, T, tensor<T, C>>;
+template <int C, typename T>
+using grad_t = std::conditional_t<C == 1, tensor<T, 3>, tensor<T, C, 3>>;
+
+template <int C, typename V>
+SFX_HDI auto& comp(V& v, int c) {
+  if constexpr (C == 1) {
+    (void)c;
+    return v;
+  } else {
+    return v[c];
+  }
+}
+
+// component c of a q-function source output (zero / scalar / vector)
+template <int C, typename S>
+SFX_HDI auto source_comp(const S& s, int c) {
+  if constexpr (is_zero<S>::value) {
+    (void)c;
+    return zero{};
+  } else if constexpr (C == 1 && !is_tensor<S>::value) {
+    (void)c;
+    return s;
+  } else {
+    return s[c];
+  }
+}
+// row c of a q-function flux output (zero / tensor<3> / tensor<C,3>)
+template <int C, typename F>
+SFX_HDI auto flux_row(const F& f, int c) {
+  if constexpr (is_zero<F>::value) {
+    (void)c;
+    return zero{};
+  } else if constexpr (C == 1 && F::ndim == 1) {
+    (void)c;
+    return f;
+  } else {
+    return f[c];
+  }
+}
+
+template <typename T>
+struct base_scalar {
+  using type = T;
+};
+template <typename T, int... n>
+struct base_scalar<tensor<T, n...>> {
+  using type = typename base_scalar<T>::type;
+};
+
+// whether the requested part (value for residual, directional derivative for
+// JVP) of a q-function output is structurally nonzero
+template <int MODE, typename T>
+constexpr bool has_part() {
+  using B = typename base_scalar<T>::type;
+  if constexpr (is_zero<B>::value) return false;
+  else if constexpr (MODE == JVP) return is_dual<B>::value;
+  else return true;
+}
+
+template <int MODE, typename Real, typename T>
+SFX_HDI Real part(const T& x) {
+  if constexpr (MODE == JVP) {
+    if constexpr (is_dual<T>::value) return Real(x.gradient);
+    else return Real(0);
+  } else {
+    return Real(get_value(x));
+  }
+}
+
+template <typename Real>
+SFX_HDI Real shfl(Real v, int src) {
+  return __shfl_sync(0xffffffffu, v, src);
+}
+
+/// Interpolate one nodal field held one node per lane into the value and the
+/// three parent-space derivatives at this lane's quadrature point.
+template <int Q, typename Real>
+SFX_HDI void interpolate_lane(Real U, int base, int ix, int iy, int iz, const Real (*B)[Q], const Real (*G)[Q],
+                              Real& val, Real& g0, Real& g1, Real& g2) {
+  // x-pass: A0(qx, ny, nz), A1(qx, ny, nz)
+  Real A0 = 0, A1 = 0;
+#pragma unroll
+  for (int k = 0; k < Q; k++) {
+    Real v = shfl(U, base + k + Q * (iy + Q * iz));
+    A0 += B[ix][k] * v;
+    A1 += G[ix][k] * v;
+  }
+  // y-pass: C00 (B_y B_x), C10 (B_y G_x), C01 (G_y B_x)
+  Real C00 = 0, C10 = 0, C01 = 0;
+#pragma unroll
+  for (int k = 0; k < Q; k++) {
+    int src = base + ix + Q * (k + Q * iz);
+    Real a0 = shfl(A0, src);
+    Real a1 = shfl(A1, src);
+    C00 += B[iy][k] * a0;
+    C10 += B[iy][k] * a1;
+    C01 += G[iy][k] * a0;
+  }
+  // z-pass
+  Real v = 0, gx = 0, gy = 0, gz = 0;
+#pragma unroll
+  for (int k = 0; k < Q; k++) {
+    int src = base + ix + Q * (iy + Q * k);
+    Real c00 = shfl(C00, src);
+    Real c10 = shfl(C10, src);
+    Real c01 = shfl(C01, src);
+    v += B[iz][k] * c00;
+    gx += B[iz][k] * c10;
+    gy += B[iz][k] * c01;
+    gz += G[iz][k] * c00;
+  }
+  val = v;
+  g0 = gx;
+  g1 = gy;
+  g2 = gz;
+}
+
+/// Integrate (s, f) given at this lane's quadrature point against the basis,
+/// returning the nodal residual of this lane's node.  HS / HF drop the source
+/// / flux terms when they are structurally zero.
+template <int Q, bool HS, bool HF, typename Real>
+SFX_HDI Real integrate_lane(Real s, Real f0, Real f1, Real f2, int base, int ix, int iy, int iz, const Real (*B)[Q],
+                            const Real (*G)[Q]) {
+  // x-pass over qx: a = sum B[q][nx] s + G[q][nx] f0, b = sum B f1, c = sum B f2
+  Real a = 0, b = 0, c = 0;
+#pragma unroll
+  for (int k = 0; k < Q; k++) {
+    int src = base + k + Q * (iy + Q * iz);
+    if constexpr (HS) a += B[k][ix] * shfl(s, src);
+    if constexpr (HF) {
+      a += G[k][ix] * shfl(f0, src);
+      b += B[k][ix] * shfl(f1, src);
+      c += B[k][ix] * shfl(f2, src);
+    }
+  }
+  // y-pass: d = sum B[q][ny] a + G[q][ny] b ; e = sum B[q][ny] c
+  Real d = 0, e = 0;
+#pragma unroll
+  for (int k = 0; k < Q; k++) {
+    int src = base + ix + Q * (k + Q * iz);
+    d += B[k][iy] * shfl(a, src);
+    if constexpr (HF) {
+      d += G[k][iy] * shfl(b, src);
+      e += B[k][iy] * shfl(c, src);
+    }
+  }
+  // z-pass: r = sum B[q][nz] d + G[q][nz] e
+  Real r = 0;
+#pragma unroll
+  for (int k = 0; k < Q; k++) {
+    int src = base + ix + Q * (iy + Q * k);
+    r += B[k][iz] * shfl(d, src);
+    if constexpr (HF) r += G[k][iz] * shfl(e, src);
+  }
+  return r;
+}
+
+template <typename State>
+SFX_HDI void load_state(State& s, const double* state, int64_t gq, int64_t nq_total) {
+  constexpr int n = sizeof(State) / sizeof(double);
+  double* d = reinterpret_cast<double*>(&s);
+#pragma unroll
+  for (int k = 0; k < n; k++) d[k] = state[k * nq_total + gq];
+}
+template <typename State>
+SFX_HDI void store_state(const State& s, double* state, int64_t gq, int64_t nq_total) {
+  constexpr int n = sizeof(State) / sizeof(double);
+  const double* d = reinterpret_cast<const double*>(&s);
+#pragma unroll
+  for (int k = 0; k < n; k++) state[k * nq_total + gq] = d[k];
+}
+
+/// Residual / JVP over a batch of elements.
+///   QFMaker: callable (const double* params_of_element) -> q-function for that element
+template <int P, int C, int MODE, typename Real, typename State, typename QFMaker>
+__global__ void __launch_bounds__(128) domain_kernel(DomainArgs<Real> a, QFMaker make_qf) {
+  constexpr int Q = P + 1;
+  constexpr int NQ = Q * Q * Q;
+  constexpr int EPW = 32 / NQ;  // elements per warp
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int sub = lane / NQ;
+  const int qi_raw = lane - sub * NQ;
+  const bool slot = sub < EPW;
+  const int qi = slot ? qi_raw : NQ - 1;
+  const int base = slot ? sub * NQ : 0;
+  const int64_t e = warp * EPW + (slot ? sub : 0);
+  const bool valid = slot && e < a.num_elements;
+  const int ix = qi % Q, iy = (qi / Q) % Q, iz = qi / (Q * Q);
+
+  __shared__ Real sB[Q][Q], sG[Q][Q];
+  if (threadIdx.x < Q * Q) {
+    int i = threadIdx.x / Q, j = threadIdx.x % Q;
+    sB[i][j] = Real(basis_B(P, i, j));
+    sG[i][j] = Real(basis_G(P, i, j));
+  }
+  __syncthreads();
+
+  const int64_t nq_total = a.num_elements * NQ;
+  const int64_t gq = e * NQ + qi;
+  int32_t node = valid ? a.conn[e * NQ + qi] : 0;
+
+  // interpolate u (and du) at this lane's point
+  value_t<C, Real> uv{}, dv{};
+  grad_t<C, Real> ug{}, dg{};
+#pragma unroll
+  for (int c = 0; c < C; c++) {
+    Real U = valid ? a.u[c * a.num_nodes + node] : Real(0);
+    Real g[3];
+    interpolate_lane<Q, Real>(U, base, ix, iy, iz, sB, sG, comp<C>(uv, c), g[0], g[1], g[2]);
+    for (int j = 0; j < 3; j++) comp<C>(ug, c)[j] = g[j];
+    if constexpr (MODE == JVP) {
+      Real dU = valid ? a.du[c * a.num_nodes + node] : Real(0);
+      interpolate_lane<Q, Real>(dU, base, ix, iy, iz, sB, sG, comp<C>(dv, c), g[0], g[1], g[2]);
+      for (int j = 0; j < 3; j++) comp<C>(dg, c)[j] = g[j];
+    }
+  }
+
+  // geometric factors
+  Real Ji[3][3];
+  Real dvol = 0;
+  tensor<Real, 3> X{};
+  tensor<Real, 3, 3> Jm{};
+  if (valid) {
+    const Real* g = a.geom + gq;
+#pragma unroll
+    for (int k = 0; k < 9; k++) Ji[k / 3][k % 3] = g[k * nq_total];
+    dvol = g[9 * nq_total];
+#pragma unroll
+    for (int k = 0; k < 3; k++) X[k] = g[(10 + k) * nq_total];
+#pragma unroll
+    for (int k = 0; k < 9; k++) Jm[k / 3][k % 3] = g[(13 + k) * nq_total];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 9; k++) Ji[k / 3][k % 3] = Real(k % 4 == 0);
+  }
+
+  // parent -> physical gradients (finite_element.hpp:246-273)
+  using S = std::conditional_t<MODE == JVP, dual<Real, Real>, Real>;
+  value_t<C, S> qv{};
+  grad_t<C, S> qg{};
+#pragma unroll
+  for (int c = 0; c < C; c++) {
+    if constexpr (MODE == JVP) {
+      comp<C>(qv, c) = S{comp<C>(uv, c), comp<C>(dv, c)};
+    } else {
+      comp<C>(qv, c) = comp<C>(uv, c);
+    }
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      Real gu = comp<C>(ug, c)[0] * Ji[0][j] + comp<C>(ug, c)[1] * Ji[1][j] + comp<C>(ug, c)[2] * Ji[2][j];
+      if constexpr (MODE == JVP) {
+        Real gd = comp<C>(dg, c)[0] * Ji[0][j] + comp<C>(dg, c)[1] * Ji[1][j] + comp<C>(dg, c)[2] * Ji[2][j];
+        comp<C>(qg, c)[j] = S{gu, gd};
+      } else {
+        comp<C>(qg, c)[j] = gu;
+      }
+    }
+  }
+
+  // q-function
+  const auto qf = make_qf(a.params + (valid ? e : 0) * QFMaker::nparams);
+  auto position = tuple{X, Jm};
+  auto arg = tuple{qv, qg};
+  auto call = [&]() {
+    if constexpr (std::is_same<State, Nothing>::value) {
+      return qf(a.t, position, arg);
+    } else {
+      State st{};
+      if (valid) load_state(st, a.state, gq, nq_total);
+      auto r = qf(a.t, position, st, arg);
+      if constexpr (MODE == RESIDUAL_UPDATE) {
+        if (valid) store_state(st, a.state, gq, nq_total);
+      }
+      return r;
+    }
+  };
+  auto out = call();
+  using SrcT = std::decay_t<decltype(get<0>(out))>;
+  using FluxT = std::decay_t<decltype(get<1>(out))>;
+  constexpr bool HS = has_part<MODE, SrcT>();
+  constexpr bool HF = has_part<MODE, FluxT>();
+
+  // physical -> parent (finite_element.hpp:287-322), weight folded into dvol,
+  // then integrate each component
+  Real* out_e = a.out_e + e * (C * NQ);
+#pragma unroll
+  for (int c = 0; c < C; c++) {
+    Real s = 0, f[3] = {0, 0, 0};
+    if constexpr (HS) s = dvol * part<MODE, Real>(source_comp<C>(get<0>(out), c));
+    if constexpr (HF) {
+      auto frow = flux_row<C>(get<1>(out), c);
+      Real fp[3];
+#pragma unroll
+      for (int m = 0; m < 3; m++) fp[m] = part<MODE, Real>(frow[m]);
+#pragma unroll
+      for (int k = 0; k < 3; k++) f[k] = dvol * (fp[0] * Ji[k][0] + fp[1] * Ji[k][1] + fp[2] * Ji[k][2]);
+    }
+    Real r = integrate_lane<Q, HS, HF, Real>(s, f[0], f[1], f[2], base, ix, iy, iz, sB, sG);
+    if (valid) out_e[c * NQ + qi] = r;
+  }
+}
+
+/// L[c * N + node] (+)= sum over the node's (element, local node) pairs, in
+/// element order, of E[(e * C + c) * NPE + local].  One thread per node.
+template <int C, int NPE, typename Real>
+__global__ void __launch_bounds__(256) scatter_kernel(const Real* __restrict__ E, const int32_t* __restrict__ node_ptr,
+                                                      const int32_t* __restrict__ node_ent, Real* __restrict__ out,
+                                                      int64_t num_nodes, bool accumulate) {
+  int64_t n = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (n >= num_nodes) return;
+  int32_t b = node_ptr[n], end = node_ptr[n + 1];
+  Real acc[C];
+#pragma unroll
+  for (int c = 0; c < C; c++) acc[c] = accumulate ? out[c * num_nodes + n] : Real(0);
+  for (int32_t k = b; k < end; k++) {
+    int32_t ent = node_ent[k];
+    int64_t el = ent / NPE;
+    int32_t loc = ent - int32_t(el) * NPE;
+#pragma unroll
+    for (int c = 0; c < C; c++) acc[c] += E[(el * C + c) * NPE + loc];
+  }
+#pragma unroll
+  for (int c = 0; c < C; c++) out[c * num_nodes + n] = acc[c];
+}
+
+}  // namespace kernels
+}  // namespace sfx
+
+namespace sfx {
+namespace kernels {
+
+/// Geometric factors of trilinear hexahedra at the Q^3 Gauss points
+/// (geometric_factors.cpp:17-60 computes X and J; the inverse, det(J) and the
+/// quadrature weight are folded here once instead of at every evaluation).
+/// Xe: [e][3][8] lexicographic vertex coordinates.  One thread per point.
+template <int Q>
+__global__ void __launch_bounds__(256) geometry_kernel(const double* __restrict__ Xe, double* __restrict__ g64,
+                                                       float* __restrict__ g32, int64_t ne) {
+  constexpr int NQ = Q * Q * Q;
+  const int64_t nqt = ne * NQ;
+  int64_t gq = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (gq >= nqt) return;
+  int64_t e = gq / NQ;
+  int q = int(gq - e * NQ);
+  int qx = q % Q, qy = (q / Q) % Q, qz = q / (Q * Q);
+  double s[3] = {gl_point(Q, qx), gl_point(Q, qy), gl_point(Q, qz)};
+  double w = gl_weight(Q, qx) * gl_weight(Q, qy) * gl_weight(Q, qz);
+  const double* X = Xe + e * 24;
+  tensor<double, 3> x{};
+  tensor<double, 3, 3> J{};
+  for (int v = 0; v < 8; v++) {
+    int b0 = v & 1, b1 = (v >> 1) & 1, b2 = (v >> 2) & 1;
+    double N0 = b0 ? s[0] : 1.0 - s[0], N1 = b1 ? s[1] : 1.0 - s[1], N2 = b2 ? s[2] : 1.0 - s[2];
+    double d0 = b0 ? 1.0 : -1.0, d1 = b1 ? 1.0 : -1.0, d2 = b2 ? 1.0 : -1.0;
+    double phi = N0 * N1 * N2;
+    double g[3] = {d0 * N1 * N2, N0 * d1 * N2, N0 * N1 * d2};
+    for (int i = 0; i < 3; i++) {
+      double xv = X[i * 8 + v];
+      x[i] += xv * phi;
+      for (int j = 0; j < 3; j++) J[i][j] += xv * g[j];
+    }
+  }
+  auto Ji = inv(J);
+  double dv = det(J) * w;
+  double vals[GEOM_STRIDE];
+  for (int k = 0; k < 9; k++) vals[k] = Ji[k / 3][k % 3];
+  vals[9] = dv;
+  for (int k = 0; k < 3; k++) vals[10 + k] = x[k];
+  for (int k = 0; k < 9; k++) vals[13 + k] = J[k / 3][k % 3];
+  for (int k = 0; k < GEOM_STRIDE; k++) {
+    g64[k * nqt + gq] = vals[k];
+    g32[k * nqt + gq] = float(vals[k]);
+  }
+}
+
+}  // namespace kernels
+}  // namespace sfx

@@ -1,0 +1,69 @@
+// sfx — 1-D rules and bases for tensor-product H1 elements.
+//
+// Gauss-Legendre points/weights on [0, 1] use the same tabulated digits as
+// serac (numerics/functional/polynomials.hpp:42-52, 271-282) so that both
+// codes integrate with identical rules.  Shape functions are the Lagrange
+// polynomials on the Gauss-Lobatto nodes of [0, 1] (polynomials.hpp:493-541),
+// evaluated here by the product formula.
+#pragma once
+
+#include "sfx/tensor.hpp"
+
+namespace sfx {
+
+SFX_HDI constexpr double gl_point(int q, int i) {
+  if (q == 1) return 0.5;
+  if (q == 2) return i == 0 ? 0.2113248654051871 : 0.7886751345948129;
+  if (q == 3) return i == 0 ? 0.1127016653792583 : (i == 1 ? 0.500000000000000 : 0.887298334620742);
+  if (q == 4) {
+    return i == 0 ? 0.0694318442029737 : (i == 1 ? 0.330009478207572 : (i == 2 ? 0.669990521792428 : 0.930568155797026));
+  }
+  return 0.0;
+}
+
+SFX_HDI constexpr double gl_weight(int q, int i) {
+  if (q == 1) return 1.0;
+  if (q == 2) return 0.5;
+  if (q == 3) return i == 1 ? 0.444444444444444 : 0.277777777777778;
+  if (q == 4) return (i == 0 || i == 3) ? 0.173927422568727 : 0.326072577431273;
+  return 0.0;
+}
+
+SFX_HDI constexpr double gll_node(int n, int k) {
+  if (n == 2) return k == 0 ? 0.0 : 1.0;
+  if (n == 3) return k == 0 ? 0.0 : (k == 1 ? 0.5 : 1.0);
+  if (n == 4) {
+    // 1/2 -+ 1/(2 sqrt 5)
+    return k == 0 ? 0.0 : (k == 1 ? 0.27639320225002103 : (k == 2 ? 0.72360679774997897 : 1.0));
+  }
+  return 0.0;
+}
+
+/// Lagrange polynomial k on the n Gauss-Lobatto nodes, and its derivative, at x.
+SFX_HDI constexpr void gll_basis(int n, int k, double x, double& phi, double& dphi) {
+  double v = 1.0, d = 0.0;
+  double xk = gll_node(n, k);
+  for (int j = 0; j < n; j++) {
+    if (j == k) continue;
+    double xj = gll_node(n, j);
+    double term = (x - xj) / (xk - xj);
+    d = d * term + v / (xk - xj);
+    v = v * term;
+  }
+  phi = v;
+  dphi = d;
+}
+
+/// B[q][k] = phi_k(x_q), G[q][k] = phi_k'(x_q) on the (p+1)-point rule.
+SFX_HDI constexpr double basis_B(int p, int q, int k) {
+  double phi = 0, dphi = 0;
+  gll_basis(p + 1, k, gl_point(p + 1, q), phi, dphi);
+  return phi;
+}
+SFX_HDI constexpr double basis_G(int p, int q, int k) {
+  double phi = 0, dphi = 0;
+  gll_basis(p + 1, k, gl_point(p + 1, q), phi, dphi);
+  return dphi;
+}
+
+}  // namespace sfx

@@ -1,0 +1,21 @@
+"""serac_gb300 — GB300-native (sm_103a) weak-form engine with serac::Functional's
+interface: residuals, Jacobian actions and CSR assembly of domain and boundary
+integrals on hexahedral H1 meshes, computed by the sfx CUDA library."""
+from .functional import (  # noqa: F401
+    ELASTIC_TEST,
+    HEAT,
+    HEAT_FLUX,
+    J2,
+    NEOHOOKEAN,
+    NONLINEAR_HEAT,
+    PRESSURE,
+    THERMAL_TEST,
+    TRACTION,
+    H1,
+    Functional,
+    Gradient,
+    Mesh,
+    assemble,
+    box_vertices,
+    differentiate_wrt,
+)

@@ -1,0 +1,88 @@
+"""ctypes binding of the sfx C ABI (include/sfx.h).
+
+The library is the in-tree ``serac_gb300/libsfx_gb300.so`` built by
+``serac_gb300/build.py``.  There is no fallback: if the library is missing or
+a call fails, an exception is raised.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsfx_gb300.so")
+
+SFX_OK = 0
+STATUS = {
+    -1: "SFX_ERR_INVALID",
+    -2: "SFX_ERR_CUDA",
+    -3: "SFX_ERR_NONFINITE",
+    -4: "SFX_ERR_TIMEOUT",
+    -5: "SFX_ERR_UNSUPPORTED",
+    -6: "SFX_ERR_NOMEM",
+}
+
+_c = ctypes
+_vp = _c.c_void_p
+_i64p = _c.POINTER(_c.c_int64)
+_dp = _c.POINTER(_c.c_double)
+
+# name -> (restype, argtypes); every entry point declared in include/sfx.h
+SIGNATURES = {
+    "sfx_last_error": (_c.c_char_p, []),
+    "sfx_version": (_c.c_int, []),
+    "sfx_mesh_create_structured_hex": (_c.c_int, [_c.c_int, _c.c_int, _c.c_int, _dp, _c.POINTER(_vp)]),
+    "sfx_mesh_destroy": (_c.c_int, [_vp]),
+    "sfx_mesh_num_elements": (_c.c_int, [_vp, _i64p]),
+    "sfx_form_create": (_c.c_int, [_vp, _c.c_int, _c.c_int, _c.POINTER(_vp)]),
+    "sfx_form_destroy": (_c.c_int, [_vp]),
+    "sfx_form_num_dofs": (_c.c_int, [_vp, _i64p]),
+    "sfx_form_add_domain_integral": (_c.c_int, [_vp, _c.c_int, _dp, _c.c_int]),
+    "sfx_form_add_boundary_integral": (_c.c_int, [_vp, _c.c_int, _c.c_int, _dp]),
+    "sfx_residual": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp]),
+    "sfx_linearize": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp]),
+    "sfx_jvp": (_c.c_int, [_vp, _vp, _vp, _vp]),
+    "sfx_jvp_f32": (_c.c_int, [_vp, _vp, _vp, _vp]),
+    "sfx_csr_nnz": (_c.c_int, [_vp, _i64p]),
+    "sfx_csr_graph": (_c.c_int, [_vp, _vp, _vp, _vp]),
+    "sfx_assemble_csr": (_c.c_int, [_vp, _vp, _vp]),
+    "sfx_assemble_diagonal": (_c.c_int, [_vp, _vp, _vp]),
+    "sfx_update_qdata": (_c.c_int, [_vp, _c.c_int]),
+    "sfx_qdata_size": (_c.c_int, [_vp, _i64p]),
+    "sfx_set_qdata": (_c.c_int, [_vp, _dp]),
+    "sfx_get_qdata": (_c.c_int, [_vp, _dp]),
+}
+
+_LIB = None
+
+
+class SfxError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def load():
+    """Load the library (once) and declare every entry point."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"sfx CUDA library not built: {LIB_PATH} (run serac_gb300/build.py)")
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = lib
+    return _LIB
+
+
+def check(rc):
+    if rc != SFX_OK:
+        msg = load().sfx_last_error()
+        raise SfxError(rc, msg.decode() if msg else "")
+    return rc
+
+
+def call(name, *args):
+    return check(getattr(load(), name)(*args))

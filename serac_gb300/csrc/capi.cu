@@ -1,0 +1,314 @@
+// sfx C ABI: meshes, forms, residual, linearisation and Jacobian actions.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "dispatch.hpp"
+#include "form.hpp"
+#include "sfx.h"
+#include "sfx/kernels.cuh"
+
+namespace sfx_impl {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+namespace {
+
+template <int C, int NPE, typename Real>
+int scatter(const sfx_form_s& f, const Real* E, Real* out, bool accumulate, cudaStream_t s) {
+  if (f.nnodes == 0) return SFX_OK;
+  unsigned blocks = unsigned((f.nnodes + 255) / 256);
+  sfx::kernels::scatter_kernel<C, NPE, Real>
+      <<<blocks, 256, 0, s>>>(E, f.node_ptr.p, f.node_ent.p, out, f.nnodes, accumulate);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("scatter launch: ") + cudaGetErrorString(err));
+  return SFX_OK;
+}
+
+template <typename Real>
+int scatter_dispatch(const sfx_form_s& f, const Real* E, Real* out, bool accumulate, cudaStream_t s) {
+  if (f.p == 1 && f.c == 1) return scatter<1, 8, Real>(f, E, out, accumulate, s);
+  if (f.p == 1 && f.c == 3) return scatter<3, 8, Real>(f, E, out, accumulate, s);
+  if (f.p == 2 && f.c == 1) return scatter<1, 27, Real>(f, E, out, accumulate, s);
+  if (f.p == 2 && f.c == 3) return scatter<3, 27, Real>(f, E, out, accumulate, s);
+  return fail(SFX_ERR_UNSUPPORTED, "unsupported (order, components)");
+}
+
+__global__ void f64_to_f32(const double* a, float* b, int64_t n) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = float(a[i]);
+}
+
+int check_form(sfx_form f) {
+  if (!f) return fail(SFX_ERR_INVALID, "null form");
+  return SFX_OK;
+}
+
+}  // namespace
+}  // namespace sfx_impl
+
+using namespace sfx_impl;
+
+extern "C" {
+
+const char* sfx_last_error(void) { return g_last_error.c_str(); }
+
+int sfx_version(void) { return 1; }
+
+int sfx_mesh_create_structured_hex(int nx, int ny, int nz, const double* vertices, sfx_mesh* out) {
+  if (!out) return fail(SFX_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (nx < 1 || ny < 1 || nz < 1) return fail(SFX_ERR_INVALID, "mesh dimensions must be >= 1");
+  if (!vertices) return fail(SFX_ERR_INVALID, "null vertex array");
+  int64_t nv = int64_t(nx + 1) * (ny + 1) * (nz + 1);
+  if (int64_t(nx) * ny * nz * 27 >= (int64_t(1) << 31)) return fail(SFX_ERR_UNSUPPORTED, "mesh too large for int32 tables");
+  auto* m = new (std::nothrow) sfx_mesh_s;
+  if (!m) return fail(SFX_ERR_NOMEM, "host allocation failed");
+  m->nx = nx;
+  m->ny = ny;
+  m->nz = nz;
+  m->vertices.assign(vertices, vertices + nv * 3);
+  *out = m;
+  return SFX_OK;
+}
+
+int sfx_mesh_destroy(sfx_mesh mesh) {
+  delete mesh;
+  return SFX_OK;
+}
+
+int sfx_mesh_num_elements(sfx_mesh mesh, int64_t* out) {
+  if (!mesh || !out) return fail(SFX_ERR_INVALID, "null argument");
+  *out = int64_t(mesh->nx) * mesh->ny * mesh->nz;
+  return SFX_OK;
+}
+
+int sfx_form_create(sfx_mesh mesh, int order, int components, sfx_form* out) {
+  if (!mesh || !out) return fail(SFX_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (order < 1 || order > 2) return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
+  if (components != 1 && components != 3) return fail(SFX_ERR_UNSUPPORTED, "components must be 1 or 3");
+  auto* f = new (std::nothrow) sfx_form_s;
+  if (!f) return fail(SFX_ERR_NOMEM, "host allocation failed");
+  f->mesh = *mesh;
+  f->p = order;
+  f->c = components;
+  f->Q = order + 1;
+  f->NQ = f->Q * f->Q * f->Q;
+  f->NPE = (order + 1) * (order + 1) * (order + 1);
+  const int nx = mesh->nx, ny = mesh->ny, nz = mesh->nz, p = order, n = order + 1;
+  f->ne = int64_t(nx) * ny * nz;
+  const int64_t Nx = int64_t(p) * nx + 1, Ny = int64_t(p) * ny + 1, Nz = int64_t(p) * nz + 1;
+  f->nnodes = Nx * Ny * Nz;
+  f->ndofs = f->nnodes * components;
+
+  // element -> node table (lexicographic local order) and node -> (element, local) map
+  std::vector<int32_t> conn(size_t(f->ne) * f->NPE);
+  std::vector<int32_t> count(size_t(f->nnodes) + 1, 0);
+  for (int64_t e = 0; e < f->ne; e++) {
+    int64_t ex = e % nx, ey = (e / nx) % ny, ez = e / (int64_t(nx) * ny);
+    for (int kz = 0; kz < n; kz++)
+      for (int ky = 0; ky < n; ky++)
+        for (int kx = 0; kx < n; kx++) {
+          int64_t node = (p * ex + kx) + Nx * ((p * ey + ky) + Ny * (p * ez + kz));
+          conn[size_t(e * f->NPE + kx + n * (ky + n * kz))] = int32_t(node);
+          count[size_t(node) + 1]++;
+        }
+  }
+  for (size_t i = 1; i < count.size(); i++) count[i] += count[i - 1];
+  std::vector<int32_t> ent(size_t(f->ne) * f->NPE);
+  {
+    std::vector<int32_t> fill(count.begin(), count.end() - 1);
+    for (int64_t e = 0; e < f->ne; e++)
+      for (int a = 0; a < f->NPE; a++) {
+        int32_t node = conn[size_t(e * f->NPE + a)];
+        ent[size_t(fill[size_t(node)]++)] = int32_t(e * f->NPE + a);
+      }
+  }
+  // element vertex coordinates [e][3][8]
+  std::vector<double> Xe(size_t(f->ne) * 24);
+  for (int64_t e = 0; e < f->ne; e++) {
+    int64_t ex = e % nx, ey = (e / nx) % ny, ez = e / (int64_t(nx) * ny);
+    for (int v = 0; v < 8; v++) {
+      int64_t vid = (ex + (v & 1)) + int64_t(nx + 1) * ((ey + ((v >> 1) & 1)) + int64_t(ny + 1) * (ez + ((v >> 2) & 1)));
+      for (int i = 0; i < 3; i++) Xe[size_t(e * 24 + i * 8 + v)] = mesh->vertices[size_t(vid * 3 + i)];
+    }
+  }
+  auto cleanup_fail = [&](int code, const std::string& msg) {
+    delete f;
+    return fail(code, msg);
+  };
+  cudaError_t err;
+  if ((err = f->conn.upload(conn.data(), conn.size())) != cudaSuccess ||
+      (err = f->node_ptr.upload(count.data(), count.size())) != cudaSuccess ||
+      (err = f->node_ent.upload(ent.data(), ent.size())) != cudaSuccess)
+    return cleanup_fail(SFX_ERR_CUDA, std::string("upload tables: ") + cudaGetErrorString(err));
+  const int64_t nqt = f->ne * f->NQ;
+  DeviceBuf<double> dXe;
+  if ((err = dXe.upload(Xe.data(), Xe.size())) != cudaSuccess ||
+      (err = f->geom64.alloc(size_t(nqt) * sfx::kernels::GEOM_STRIDE)) != cudaSuccess ||
+      (err = f->geom32.alloc(size_t(nqt) * sfx::kernels::GEOM_STRIDE)) != cudaSuccess ||
+      (err = f->e64.alloc(size_t(f->ne) * f->NPE * components)) != cudaSuccess ||
+      (err = f->e32.alloc(size_t(f->ne) * f->NPE * components)) != cudaSuccess ||
+      (err = f->u_lin64.alloc(size_t(f->ndofs))) != cudaSuccess ||
+      (err = f->u_lin32.alloc(size_t(f->ndofs))) != cudaSuccess)
+    return cleanup_fail(SFX_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(err));
+  unsigned blocks = unsigned((nqt + 255) / 256);
+  if (f->Q == 2) sfx::kernels::geometry_kernel<2><<<blocks, 256>>>(dXe.p, f->geom64.p, f->geom32.p, f->ne);
+  else sfx::kernels::geometry_kernel<3><<<blocks, 256>>>(dXe.p, f->geom64.p, f->geom32.p, f->ne);
+  if ((err = cudaGetLastError()) != cudaSuccess || (err = cudaDeviceSynchronize()) != cudaSuccess)
+    return cleanup_fail(SFX_ERR_CUDA, std::string("geometry kernel: ") + cudaGetErrorString(err));
+  *out = f;
+  return SFX_OK;
+}
+
+int sfx_form_destroy(sfx_form form) {
+  delete form;
+  return SFX_OK;
+}
+
+int sfx_form_num_dofs(sfx_form form, int64_t* out) {
+  if (check_form(form) || !out) return fail(SFX_ERR_INVALID, "null argument");
+  *out = form->ndofs;
+  return SFX_OK;
+}
+
+int sfx_form_add_domain_integral(sfx_form form, int material, const double* params, int per_element) {
+  if (check_form(form)) return SFX_ERR_INVALID;
+  int comps = 0, np = 0, nst = 0;
+  if (int rc = material_info(material, &comps, &np, &nst)) return rc;
+  if (comps != form->c) return fail(SFX_ERR_INVALID, "material component count does not match the trial space");
+  if (!form->domain.empty()) return fail(SFX_ERR_UNSUPPORTED, "one domain integral per form in this version");
+  if (np > 0 && !params) return fail(SFX_ERR_INVALID, "material needs parameters");
+  DomainIntegral di;
+  di.material = material;
+  di.nparams = np;
+  di.state_doubles = nst;
+  std::vector<double> prm(size_t(form->ne) * np);
+  for (int64_t e = 0; e < form->ne; e++)
+    for (int k = 0; k < np; k++) prm[size_t(e * np + k)] = per_element ? params[e * np + k] : params[k];
+  cudaError_t err = di.params.upload(prm.data(), prm.size());
+  if (err == cudaSuccess && nst > 0) {
+    size_t n = size_t(form->ne) * form->NQ * nst;
+    err = di.state.alloc(n);
+    if (err == cudaSuccess) err = cudaMemset(di.state.p, 0, n * sizeof(double));
+  }
+  if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("integral setup: ") + cudaGetErrorString(err));
+  form->domain.push_back(std::move(di));
+  return SFX_OK;
+}
+
+int sfx_residual(sfx_form form, double t, const double* u, double* r, void* stream) {
+  if (check_form(form)) return SFX_ERR_INVALID;
+  if (!u || !r) return fail(SFX_ERR_INVALID, "null vector");
+  if (form->domain.empty()) return fail(SFX_ERR_INVALID, "no integrals");
+  auto s = static_cast<cudaStream_t>(stream);
+  const int mode = form->update_qdata ? sfx::kernels::RESIDUAL_UPDATE : sfx::kernels::RESIDUAL;
+  for (size_t i = 0; i < form->domain.size(); i++) {
+    if (int rc = launch_domain(*form, form->domain[i], mode, u, nullptr, form->e64.p, t, s)) return rc;
+    if (int rc = scatter_dispatch<double>(*form, form->e64.p, r, i > 0, s)) return rc;
+  }
+  return SFX_OK;
+}
+
+int sfx_linearize(sfx_form form, double t, const double* u, double* r, void* stream) {
+  if (check_form(form)) return SFX_ERR_INVALID;
+  if (!u) return fail(SFX_ERR_INVALID, "null vector");
+  auto s = static_cast<cudaStream_t>(stream);
+  SFX_CUDA_TRY(cudaMemcpyAsync(form->u_lin64.p, u, size_t(form->ndofs) * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  unsigned blocks = unsigned((form->ndofs + 255) / 256);
+  if (form->ndofs) f64_to_f32<<<blocks, 256, 0, s>>>(form->u_lin64.p, form->u_lin32.p, form->ndofs);
+  SFX_CUDA_TRY(cudaGetLastError());
+  form->t_lin = t;
+  form->linearized = true;
+  if (r) {
+    bool saved = form->update_qdata;
+    form->update_qdata = false;
+    int rc = sfx_residual(form, t, form->u_lin64.p, r, stream);
+    form->update_qdata = saved;
+    return rc;
+  }
+  return SFX_OK;
+}
+
+int sfx_jvp(sfx_form form, const double* du, double* dr, void* stream) {
+  if (check_form(form)) return SFX_ERR_INVALID;
+  if (!du || !dr) return fail(SFX_ERR_INVALID, "null vector");
+  if (!form->linearized) return fail(SFX_ERR_INVALID, "sfx_linearize must be called before sfx_jvp");
+  auto s = static_cast<cudaStream_t>(stream);
+  for (size_t i = 0; i < form->domain.size(); i++) {
+    if (int rc = launch_domain(*form, form->domain[i], sfx::kernels::JVP, form->u_lin64.p, du, form->e64.p,
+                               form->t_lin, s))
+      return rc;
+    if (int rc = scatter_dispatch<double>(*form, form->e64.p, dr, i > 0, s)) return rc;
+  }
+  return SFX_OK;
+}
+
+int sfx_jvp_f32(sfx_form form, const float* du, float* dr, void* stream) {
+  if (check_form(form)) return SFX_ERR_INVALID;
+  if (!du || !dr) return fail(SFX_ERR_INVALID, "null vector");
+  if (!form->linearized) return fail(SFX_ERR_INVALID, "sfx_linearize must be called before sfx_jvp_f32");
+  auto s = static_cast<cudaStream_t>(stream);
+  for (size_t i = 0; i < form->domain.size(); i++) {
+    if (int rc = launch_domain_jvp_f32(*form, form->domain[i], form->u_lin32.p, du, form->e32.p, form->t_lin, s))
+      return rc;
+    if (int rc = scatter_dispatch<float>(*form, form->e32.p, dr, i > 0, s)) return rc;
+  }
+  return SFX_OK;
+}
+
+int sfx_update_qdata(sfx_form form, int flag) {
+  if (check_form(form)) return SFX_ERR_INVALID;
+  form->update_qdata = flag != 0;
+  return SFX_OK;
+}
+
+int sfx_qdata_size(sfx_form form, int64_t* num_doubles) {
+  if (check_form(form) || !num_doubles) return fail(SFX_ERR_INVALID, "null argument");
+  *num_doubles = 0;
+  for (auto& di : form->domain) *num_doubles += form->ne * form->NQ * di.state_doubles;
+  return SFX_OK;
+}
+
+static int qdata_copy(sfx_form form, double* host, bool to_device) {
+  for (auto& di : form->domain) {
+    if (!di.state_doubles) continue;
+    const int64_t nqt = form->ne * form->NQ;
+    const int k = di.state_doubles;
+    std::vector<double> soa(size_t(nqt) * k);
+    if (to_device) {
+      for (int64_t q = 0; q < nqt; q++)
+        for (int j = 0; j < k; j++) soa[size_t(j * nqt + q)] = host[q * k + j];
+      SFX_CUDA_TRY(cudaMemcpy(di.state.p, soa.data(), soa.size() * sizeof(double), cudaMemcpyHostToDevice));
+    } else {
+      SFX_CUDA_TRY(cudaMemcpy(soa.data(), di.state.p, soa.size() * sizeof(double), cudaMemcpyDeviceToHost));
+      for (int64_t q = 0; q < nqt; q++)
+        for (int j = 0; j < k; j++) host[q * k + j] = soa[size_t(j * nqt + q)];
+    }
+    host += nqt * k;
+  }
+  return SFX_OK;
+}
+
+int sfx_set_qdata(sfx_form form, const double* host_state) {
+  if (check_form(form) || !host_state) return fail(SFX_ERR_INVALID, "null argument");
+  return qdata_copy(form, const_cast<double*>(host_state), true);
+}
+
+int sfx_get_qdata(sfx_form form, double* host_state) {
+  if (check_form(form) || !host_state) return fail(SFX_ERR_INVALID, "null argument");
+  return qdata_copy(form, host_state, false);
+}
+
+}  // extern "C"

@@ -1,0 +1,130 @@
+// Instantiates the fused domain kernels for the material library and
+// dispatches on (order, material, mode, precision).
+#include <cuda_runtime.h>
+
+#include "dispatch.hpp"
+#include "form.hpp"
+#include "sfx/kernels.cuh"
+#include "sfx/materials.hpp"
+
+namespace sfx_impl {
+namespace {
+
+using namespace sfx;
+using J2 = solid_mechanics::J2SmallStrain<solid_mechanics::LinearHardening>;
+
+struct HeatMaker {
+  static constexpr int nparams = 2;
+  SFX_HD heat_transfer::HeatIntegrand operator()(const double* p) const {
+    heat_transfer::HeatIntegrand q{};
+    q.material.conductivity = p[0];
+    q.source = p[1];
+    return q;
+  }
+};
+struct NonlinearHeatMaker {
+  static constexpr int nparams = 3;
+  SFX_HD heat_transfer::NonlinearHeatIntegrand operator()(const double* p) const {
+    return heat_transfer::NonlinearHeatIntegrand{p[0], p[1], p[2]};
+  }
+};
+struct NeoHookeanMaker {
+  static constexpr int nparams = 2;
+  SFX_HD solid_mechanics::MaterialStressFunctor<solid_mechanics::NeoHookean, true> operator()(const double* p) const {
+    return {solid_mechanics::NeoHookean{1.0, p[0], p[1]}};
+  }
+};
+struct J2Maker {
+  static constexpr int nparams = 4;
+  SFX_HD solid_mechanics::MaterialStressFunctor<J2, false> operator()(const double* p) const {
+    J2 m{};
+    m.E = p[0];
+    m.nu = p[1];
+    m.hardening = solid_mechanics::LinearHardening{p[2], p[3]};
+    m.Hk = 0.0;
+    m.density = 1.0;
+    return {m};
+  }
+};
+struct ThermalTestMaker {
+  static constexpr int nparams = 0;
+  SFX_HD test_models::ThermalModel operator()(const double*) const { return {}; }
+};
+struct ElasticTestMaker {
+  static constexpr int nparams = 0;
+  SFX_HD test_models::ElasticModel operator()(const double*) const { return {}; }
+};
+
+template <int P, int C, int MODE, typename Real, typename State, typename Maker>
+int launch(const sfx_form_s& f, const DomainIntegral& di, const Real* u, const Real* du, Real* E, const Real* geom,
+           double t, cudaStream_t s) {
+  constexpr int NQ = (P + 1) * (P + 1) * (P + 1);
+  constexpr int EPW = 32 / NQ;
+  if (f.ne == 0) return SFX_OK;
+  kernels::DomainArgs<Real> a{u, du, E, f.conn.p, geom, di.state.p, di.params.p, f.nnodes, f.ne, t};
+  int64_t warps = (f.ne + EPW - 1) / EPW;
+  int64_t blocks = (warps * 32 + 127) / 128;
+  kernels::domain_kernel<P, C, MODE, Real, State, Maker><<<unsigned(blocks), 128, 0, s>>>(a, Maker{});
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("domain kernel launch: ") + cudaGetErrorString(err));
+  return SFX_OK;
+}
+
+template <int MODE, typename Real, int P>
+int dispatch_p(const sfx_form_s& f, const DomainIntegral& di, const Real* u, const Real* du, Real* E,
+               const Real* geom, double t, cudaStream_t s) {
+  switch (di.material) {
+    case SFX_MAT_HEAT: return launch<P, 1, MODE, Real, Nothing, HeatMaker>(f, di, u, du, E, geom, t, s);
+    case SFX_MAT_NONLINEAR_HEAT:
+      return launch<P, 1, MODE, Real, Nothing, NonlinearHeatMaker>(f, di, u, du, E, geom, t, s);
+    case SFX_MAT_THERMAL_TEST: return launch<P, 1, MODE, Real, Nothing, ThermalTestMaker>(f, di, u, du, E, geom, t, s);
+    case SFX_MAT_ELASTIC_TEST: return launch<P, 3, MODE, Real, Nothing, ElasticTestMaker>(f, di, u, du, E, geom, t, s);
+    case SFX_MAT_NEOHOOKEAN: return launch<P, 3, MODE, Real, Empty, NeoHookeanMaker>(f, di, u, du, E, geom, t, s);
+    case SFX_MAT_J2: return launch<P, 3, MODE, Real, J2::State, J2Maker>(f, di, u, du, E, geom, t, s);
+  }
+  return fail(SFX_ERR_UNSUPPORTED, "unknown material");
+}
+
+template <int MODE, typename Real>
+int dispatch(const sfx_form_s& f, const DomainIntegral& di, const Real* u, const Real* du, Real* E, const Real* geom,
+             double t, cudaStream_t s) {
+  if (f.p == 1) return dispatch_p<MODE, Real, 1>(f, di, u, du, E, geom, t, s);
+  if (f.p == 2) return dispatch_p<MODE, Real, 2>(f, di, u, du, E, geom, t, s);
+  return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
+}
+
+}  // namespace
+
+int material_info(int material, int* components, int* nparams, int* state_doubles) {
+  switch (material) {
+    case SFX_MAT_HEAT: *components = 1; *nparams = HeatMaker::nparams; *state_doubles = 0; return SFX_OK;
+    case SFX_MAT_NONLINEAR_HEAT: *components = 1; *nparams = NonlinearHeatMaker::nparams; *state_doubles = 0; return SFX_OK;
+    case SFX_MAT_THERMAL_TEST: *components = 1; *nparams = 0; *state_doubles = 0; return SFX_OK;
+    case SFX_MAT_ELASTIC_TEST: *components = 3; *nparams = 0; *state_doubles = 0; return SFX_OK;
+    case SFX_MAT_NEOHOOKEAN: *components = 3; *nparams = NeoHookeanMaker::nparams; *state_doubles = 0; return SFX_OK;
+    case SFX_MAT_J2:
+      *components = 3;
+      *nparams = J2Maker::nparams;
+      *state_doubles = int(sizeof(J2::State) / sizeof(double));
+      return SFX_OK;
+  }
+  return fail(SFX_ERR_UNSUPPORTED, "unknown material id");
+}
+
+int launch_domain(const sfx_form_s& f, const DomainIntegral& di, int mode, const double* u, const double* du,
+                  double* E, double t, cudaStream_t s) {
+  switch (mode) {
+    case kernels::RESIDUAL: return dispatch<kernels::RESIDUAL, double>(f, di, u, du, E, f.geom64.p, t, s);
+    case kernels::RESIDUAL_UPDATE:
+      return dispatch<kernels::RESIDUAL_UPDATE, double>(f, di, u, du, E, f.geom64.p, t, s);
+    case kernels::JVP: return dispatch<kernels::JVP, double>(f, di, u, du, E, f.geom64.p, t, s);
+  }
+  return fail(SFX_ERR_INVALID, "bad mode");
+}
+
+int launch_domain_jvp_f32(const sfx_form_s& f, const DomainIntegral& di, const float* u, const float* du, float* E,
+                          double t, cudaStream_t s) {
+  return dispatch<kernels::JVP, float>(f, di, u, du, E, f.geom32.p, t, s);
+}
+
+}  // namespace sfx_impl

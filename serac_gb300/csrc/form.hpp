@@ -1,0 +1,119 @@
+// Internal state of the sfx C ABI: meshes, forms and their device buffers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "sfx.h"
+
+namespace sfx_impl {
+
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+
+#define SFX_CUDA_TRY(call)                                                            \
+  do {                                                                                \
+    cudaError_t err_ = (call);                                                        \
+    if (err_ != cudaSuccess)                                                          \
+      return ::sfx_impl::fail(SFX_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(err_)); \
+  } while (0)
+
+/// Owning device buffer (cudaMalloc / cudaFree).
+template <typename T>
+struct DeviceBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DeviceBuf() = default;
+  DeviceBuf(const DeviceBuf&) = delete;
+  DeviceBuf& operator=(const DeviceBuf&) = delete;
+  DeviceBuf(DeviceBuf&& o) noexcept : p(o.p), n(o.n) {
+    o.p = nullptr;
+    o.n = 0;
+  }
+  DeviceBuf& operator=(DeviceBuf&& o) noexcept {
+    std::swap(p, o.p);
+    std::swap(n, o.n);
+    return *this;
+  }
+  ~DeviceBuf() { reset(); }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t count) {
+    reset();
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    else p = nullptr;
+    return e;
+  }
+  cudaError_t upload(const T* host, size_t count) {
+    cudaError_t e = alloc(count);
+    if (e != cudaSuccess || count == 0) return e;
+    return cudaMemcpy(p, host, count * sizeof(T), cudaMemcpyHostToDevice);
+  }
+};
+
+struct DomainIntegral {
+  int material = 0;
+  int nparams = 0;
+  int state_doubles = 0;  // per quadrature point
+  DeviceBuf<double> params;  // [e][nparams]
+  DeviceBuf<double> state;   // SoA [k][e*nq+q]
+};
+
+struct BoundaryIntegral {
+  int material = 0;
+  int nparams = 0;
+  int64_t num_faces = 0;
+  DeviceBuf<double> params;     // nparams (uniform)
+  DeviceBuf<int32_t> fconn;     // [f][(p+1)^2] node ids
+  DeviceBuf<double> fgeom64;    // FGEOM_STRIDE x nq_total
+  DeviceBuf<float> fgeom32;
+  DeviceBuf<int32_t> node_ptr;  // over the face nodes: compact list
+  DeviceBuf<int32_t> node_ids;  // global node of each compact entry
+  DeviceBuf<int32_t> node_ent;  // (f * npf + local) entries
+  int64_t num_face_nodes = 0;
+};
+
+}  // namespace sfx_impl
+
+struct sfx_mesh_s {
+  int nx = 0, ny = 0, nz = 0;
+  std::vector<double> vertices;
+};
+
+struct sfx_form_s {
+  sfx_mesh_s mesh;
+  int p = 0, c = 0, Q = 0, NQ = 0, NPE = 0;
+  int64_t ne = 0, nnodes = 0, ndofs = 0;
+  sfx_impl::DeviceBuf<int32_t> conn;      // [e][NPE]
+  sfx_impl::DeviceBuf<int32_t> node_ptr;  // [nnodes + 1]
+  sfx_impl::DeviceBuf<int32_t> node_ent;  // e * NPE + local, element order
+  sfx_impl::DeviceBuf<double> geom64;
+  sfx_impl::DeviceBuf<float> geom32;
+  sfx_impl::DeviceBuf<double> e64;  // E-vector scratch
+  sfx_impl::DeviceBuf<float> e32;
+  sfx_impl::DeviceBuf<double> ef64;  // face E-vector scratch
+  sfx_impl::DeviceBuf<float> ef32;
+  sfx_impl::DeviceBuf<double> u_lin64;
+  sfx_impl::DeviceBuf<float> u_lin32;
+  double t_lin = 0.0;
+  bool linearized = false;
+  bool update_qdata = false;
+  std::vector<sfx_impl::DomainIntegral> domain;
+  std::vector<sfx_impl::BoundaryIntegral> boundary;
+  // CSR graph (built on first request)
+  bool csr_built = false;
+  int64_t nnz = 0;
+  sfx_impl::DeviceBuf<int64_t> row_ptr;
+  sfx_impl::DeviceBuf<int32_t> col;
+  sfx_impl::DeviceBuf<double> ke;  // element matrices scratch
+};

@@ -1,0 +1,244 @@
+"""Python mirror of serac::Functional over the sfx C ABI.
+
+    mesh = Mesh.structured_hex(nx, ny, nz, vertices)
+    f = Functional(mesh, H1(order=2, components=3))       # Functional<H1<2,3>(H1<2,3>)>
+    f.AddDomainIntegral(NEOHOOKEAN, params=[K, G])          # functional.hpp:286-317
+    r = f(t, u)                                             # functional.hpp:502-513
+    r, dRdu = f(t, differentiate_wrt(u))                    # functional.hpp:481-489
+    dr = dRdu(du)                                           # Gradient::operator(), :562-566
+    A = assemble(dRdu)                                      # functional.hpp:569-667 (CSR)
+
+Vectors are torch CUDA tensors (float64; float32 for the FP32 Jacobian
+action).  Like serac, the returned residual is a member buffer overwritten by
+the next call (functional.hpp:740-741) unless ``out`` is given.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+
+HEAT, NEOHOOKEAN, J2, THERMAL_TEST, ELASTIC_TEST, NONLINEAR_HEAT = range(6)
+HEAT_FLUX, TRACTION, PRESSURE = range(3)
+COMPONENTS = {HEAT: 1, NONLINEAR_HEAT: 1, THERMAL_TEST: 1, NEOHOOKEAN: 3, J2: 3, ELASTIC_TEST: 3}
+NPARAMS = {HEAT: 2, NEOHOOKEAN: 2, J2: 4, NONLINEAR_HEAT: 3, THERMAL_TEST: 0, ELASTIC_TEST: 0}
+J2_STATE_DOUBLES = 10
+
+
+def _stream(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _dptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _require(t, dtype, n, name):
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if t.dtype != dtype or not t.is_contiguous() or t.numel() != n:
+        raise ValueError(f"{name} must be a contiguous {dtype} tensor with {n} entries")
+
+
+@dataclass(frozen=True)
+class H1:
+    order: int
+    components: int = 1
+
+
+class Mesh:
+    """Structured hexahedral mesh with trilinear geometry (buildCuboidMesh)."""
+
+    def __init__(self, handle, nx, ny, nz, vertices):
+        self._h = handle
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.vertices = vertices
+        self.num_elements = nx * ny * nz
+
+    @staticmethod
+    def structured_hex(nx, ny, nz, vertices=None):
+        if vertices is None:
+            vertices = box_vertices(nx, ny, nz)
+        v = np.ascontiguousarray(vertices, dtype=np.float64).reshape(-1, 3)
+        if v.shape[0] != (nx + 1) * (ny + 1) * (nz + 1):
+            raise ValueError("vertex array has the wrong size")
+        h = ctypes.c_void_p()
+        _lib.call("sfx_mesh_create_structured_hex", nx, ny, nz, v.ctypes.data_as(_lib._dp), ctypes.byref(h))
+        return Mesh(h, nx, ny, nz, v)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib._LIB is not None:
+            _lib.load().sfx_mesh_destroy(self._h)
+            self._h = None
+
+
+def box_vertices(nx, ny, nz, perturb=0.0, seed=0):
+    """Vertices of the unit cube grid; interior vertices moved uniformly by up
+    to ``perturb`` times the cell size per coordinate (numpy PCG64, ``seed``)."""
+    x = np.linspace(0.0, 1.0, nx + 1)
+    y = np.linspace(0.0, 1.0, ny + 1)
+    z = np.linspace(0.0, 1.0, nz + 1)
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    V = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    if perturb > 0:
+        rng = np.random.default_rng(seed)
+        d = rng.uniform(-1.0, 1.0, size=V.shape) * perturb * np.array([1.0 / nx, 1.0 / ny, 1.0 / nz])
+        i = np.arange(V.shape[0])
+        ix, iy, iz = i % (nx + 1), (i // (nx + 1)) % (ny + 1), i // ((nx + 1) * (ny + 1))
+        interior = (ix > 0) & (ix < nx) & (iy > 0) & (iy < ny) & (iz > 0) & (iz < nz)
+        V[interior] += d[interior]
+    return V
+
+
+class differentiate_wrt:
+    """Marks the argument to linearise about (differentiate_wrt.hpp:12-42)."""
+
+    def __init__(self, u):
+        self.u = u
+
+
+class Gradient:
+    """dR/du at the linearisation point; an operator (functional.hpp:534-708)."""
+
+    def __init__(self, form):
+        self.form = form
+
+    def mult(self, du, out=None, stream=None):
+        f = self.form
+        if du.dtype == torch.float32:
+            _require(du, torch.float32, f.ndofs, "du")
+            out = torch.empty_like(du) if out is None else out
+            _lib.call("sfx_jvp_f32", f._h, _dptr(du), _dptr(out), _stream(stream))
+            return out
+        _require(du, torch.float64, f.ndofs, "du")
+        out = torch.empty_like(du) if out is None else out
+        _lib.call("sfx_jvp", f._h, _dptr(du), _dptr(out), _stream(stream))
+        return out
+
+    Mult = mult
+
+    def __call__(self, du):
+        return self.mult(du)
+
+
+class Functional:
+    """Functional<H1<p,c>(H1<p,c>)> on a structured hex mesh."""
+
+    def __init__(self, mesh: Mesh, space: H1):
+        self.mesh = mesh
+        self.space = space
+        h = ctypes.c_void_p()
+        _lib.call("sfx_form_create", mesh._h, space.order, space.components, ctypes.byref(h))
+        self._h = h
+        n = ctypes.c_int64()
+        _lib.call("sfx_form_num_dofs", h, ctypes.byref(n))
+        self.ndofs = n.value
+        self.num_nodes = self.ndofs // space.components
+        self.gradient = Gradient(self)
+        self._out = None
+        self._materials = []
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib._LIB is not None:
+            _lib.load().sfx_form_destroy(self._h)
+            self._h = None
+
+    # --------------------------------------------------------------- setup
+    def AddDomainIntegral(self, material, params=None, per_element=False):
+        np_ = NPARAMS[material]
+        p = None
+        if np_:
+            arr = np.ascontiguousarray(np.asarray(params, dtype=np.float64).ravel())
+            expect = self.mesh.num_elements * np_ if per_element else np_
+            if arr.size != expect:
+                raise ValueError(f"expected {expect} parameters, got {arr.size}")
+            self._params_keepalive = arr
+            p = arr.ctypes.data_as(_lib._dp)
+        _lib.call("sfx_form_add_domain_integral", self._h, material, p, int(per_element))
+        self._materials.append(material)
+
+    add_domain_integral = AddDomainIntegral
+    AddVolumeIntegral = AddDomainIntegral
+
+    def AddBoundaryIntegral(self, material, sides, params):
+        mask = 0
+        for s in sides:
+            mask |= 1 << (s - 1)
+        arr = np.ascontiguousarray(np.asarray(params, dtype=np.float64).ravel())
+        _lib.call("sfx_form_add_boundary_integral", self._h, material, mask, arr.ctypes.data_as(_lib._dp))
+
+    add_boundary_integral = AddBoundaryIntegral
+    AddSurfaceIntegral = AddBoundaryIntegral
+
+    def updateQdata(self, flag: bool):
+        _lib.call("sfx_update_qdata", self._h, int(bool(flag)))
+
+    def qdata(self):
+        n = ctypes.c_int64()
+        _lib.call("sfx_qdata_size", self._h, ctypes.byref(n))
+        out = np.zeros(n.value)
+        if n.value:
+            _lib.call("sfx_get_qdata", self._h, out.ctypes.data_as(_lib._dp))
+        return out
+
+    def set_qdata(self, host):
+        a = np.ascontiguousarray(host, dtype=np.float64).ravel()
+        _lib.call("sfx_set_qdata", self._h, a.ctypes.data_as(_lib._dp))
+
+    # ----------------------------------------------------------- evaluation
+    def residual(self, t, u, out=None, stream=None):
+        _require(u, torch.float64, self.ndofs, "u")
+        out = torch.empty_like(u) if out is None else out
+        _lib.call("sfx_residual", self._h, float(t), _dptr(u), _dptr(out), _stream(stream))
+        return out
+
+    def linearize(self, t, u, out=None, stream=None):
+        _require(u, torch.float64, self.ndofs, "u")
+        _lib.call("sfx_linearize", self._h, float(t), _dptr(u), _dptr(out), _stream(stream))
+        return self.gradient
+
+    def __call__(self, t, arg, out=None):
+        if isinstance(arg, differentiate_wrt):
+            if self._out is None:
+                self._out = torch.empty(self.ndofs, dtype=torch.float64, device=arg.u.device)
+            r = self._out if out is None else out
+            self.linearize(t, arg.u, r)
+            return r, self.gradient
+        if out is None:
+            if self._out is None:
+                self._out = torch.empty(self.ndofs, dtype=torch.float64, device=arg.device)
+            out = self._out
+        return self.residual(t, arg, out)
+
+    # ------------------------------------------------------------ assembly
+    def csr_graph(self, stream=None):
+        n = ctypes.c_int64()
+        _lib.call("sfx_csr_nnz", self._h, ctypes.byref(n))
+        row_ptr = torch.empty(self.ndofs + 1, dtype=torch.int64, device="cuda")
+        col = torch.empty(n.value, dtype=torch.int32, device="cuda")
+        _lib.call("sfx_csr_graph", self._h, _dptr(row_ptr), _dptr(col), _stream(stream))
+        return row_ptr, col
+
+    def assemble_values(self, out=None, stream=None):
+        n = ctypes.c_int64()
+        _lib.call("sfx_csr_nnz", self._h, ctypes.byref(n))
+        out = torch.empty(n.value, dtype=torch.float64, device="cuda") if out is None else out
+        _lib.call("sfx_assemble_csr", self._h, _dptr(out), _stream(stream))
+        return out
+
+    def assemble_diagonal(self, out=None, stream=None):
+        out = torch.empty(self.ndofs, dtype=torch.float64, device="cuda") if out is None else out
+        _lib.call("sfx_assemble_diagonal", self._h, _dptr(out), _stream(stream))
+        return out
+
+
+def assemble(gradient: Gradient):
+    """CSR of dR/du at the linearisation point: (row_ptr int64, col int32, values float64)."""
+    f = gradient.form
+    row_ptr, col = f.csr_graph()
+    return row_ptr, col, f.assemble_values()
