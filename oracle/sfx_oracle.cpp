@@ -914,4 +914,232 @@ int orc_boundary(int mat, int p, int mode, int nf, double t, const double* param
   return 0;
 }
 
+
+// ---------------------------------------------------------------------------
+// Stored-derivative Jacobian action, the way serac applies a linearisation:
+// the q-function derivative D is computed once per quadrature point
+// (evaluation_kernel_impl with differentiation, domain_integral_kernels.hpp:
+// 152-220, D stored after physical->parent at :209-214) and every Jv then
+// runs interpolate(du) -> D . du -> integrate with sum factorisation
+// (action_of_gradient_kernel, domain_integral_kernels.hpp:277-304;
+// hexahedron_H1.inl:169-280).  This is the CPU baseline path.
+
+// D: [e][q][N][N], N = 4c, quadrature weight not included.
+int orc_linearize(int mat, int p, int ne, double t, const double* params, const double* uE, const double* Xq,
+                  const double* Jq, const double* state, double* D, int nthreads) {
+  (void)t;
+  if (p < 1 || p > 3 || mat < 0 || mat > 5) return -1;
+  const int c = components_of(mat);
+  const int np = params_of(mat);
+  Basis3 b(p);
+  const int nd = b.nd, nq = b.nq, N = 4 * c;
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+#endif
+  for (int e = 0; e < ne; e++) {
+    const double* prm = params ? params + size_t(e) * size_t(np) : nullptr;
+    const double* ue = uE + size_t(e) * nd * c;
+    for (int q = 0; q < nq; q++) {
+      const double* phi = &b.phi[size_t(q * nd)];
+      const double* dphi = &b.dphi[size_t(q * nd * 3)];
+      double uval[3] = {0, 0, 0}, ugrad[3][3] = {};
+      for (int i = 0; i < c; i++)
+        for (int a = 0; a < nd; a++) {
+          double ua = ue[i * nd + a];
+          uval[i] += ua * phi[a];
+          for (int j = 0; j < 3; j++) ugrad[i][j] += ua * dphi[a * 3 + j];
+        }
+      double J[3][3], xq[3];
+      for (int i = 0; i < 3; i++) {
+        xq[i] = Xq[(size_t(e) * 3 + i) * nq + q];
+        for (int j = 0; j < 3; j++) J[i][j] = Jq[((size_t(e) * 3 + j) * 3 + i) * nq + q];
+      }
+      J2State st{};
+      J2State* sp = nullptr;
+      if (mat == MAT_J2) {
+        if (state) std::memcpy(&st, state + (size_t(e) * nq + q) * 10, sizeof(J2State));
+        sp = &st;
+      }
+      double vals[12];
+      double* Dq = D + (size_t(e) * nq + q) * size_t(N * N);
+      if (c == 1) qp_linearise<1>(mat, prm, sp, xq, J, uval, ugrad, vals, Dq);
+      else qp_linearise<3>(mat, prm, sp, xq, J, uval, ugrad, vals, Dq);
+    }
+  }
+  return 0;
+}
+
+}  // extern "C"
+
+template <int n, int c>
+static void apply_linearization_element(const double (&B)[4][4], const double (&G)[4][4], const double (&Bw)[4][4],
+                                        const double (&Gw)[4][4], const double* D, const double* due, double* out) {
+  constexpr int q = n, nq = q * q * q, N = 4 * c;
+  double din[nq][N];
+  // interpolate each component (A10/A11, A20/A21/A22, value/gradients)
+  for (int i = 0; i < c; i++) {
+    const double* X = due + i * n * n * n;  // X[dz][dy][dx]
+    double A10[n][n][q], A11[n][n][q];
+    for (int dz = 0; dz < n; dz++)
+      for (int dy = 0; dy < n; dy++)
+        for (int qx = 0; qx < q; qx++) {
+          double s0 = 0, s1 = 0;
+          for (int dx = 0; dx < n; dx++) {
+            double v = X[(dz * n + dy) * n + dx];
+            s0 += B[qx][dx] * v;
+            s1 += G[qx][dx] * v;
+          }
+          A10[dz][dy][qx] = s0;
+          A11[dz][dy][qx] = s1;
+        }
+    double A20[n][q][q], A21[n][q][q], A22[n][q][q];
+    for (int dz = 0; dz < n; dz++)
+      for (int qy = 0; qy < q; qy++)
+        for (int qx = 0; qx < q; qx++) {
+          double s0 = 0, s1 = 0, s2 = 0;
+          for (int dy = 0; dy < n; dy++) {
+            s0 += B[qy][dy] * A10[dz][dy][qx];
+            s1 += B[qy][dy] * A11[dz][dy][qx];
+            s2 += G[qy][dy] * A10[dz][dy][qx];
+          }
+          A20[dz][qy][qx] = s0;
+          A21[dz][qy][qx] = s1;
+          A22[dz][qy][qx] = s2;
+        }
+    for (int qz = 0; qz < q; qz++)
+      for (int qy = 0; qy < q; qy++)
+        for (int qx = 0; qx < q; qx++) {
+          double v = 0, g0 = 0, g1 = 0, g2 = 0;
+          for (int dz = 0; dz < n; dz++) {
+            v += B[qz][dz] * A20[dz][qy][qx];
+            g0 += B[qz][dz] * A21[dz][qy][qx];
+            g1 += B[qz][dz] * A22[dz][qy][qx];
+            g2 += G[qz][dz] * A20[dz][qy][qx];
+          }
+          int Q = (qz * q + qy) * q + qx;
+          din[Q][i] = v;
+          din[Q][c + 3 * i + 0] = g0;
+          din[Q][c + 3 * i + 1] = g1;
+          din[Q][c + 3 * i + 2] = g2;
+        }
+  }
+  // chain rule
+  double dout[nq][N];
+  for (int Q = 0; Q < nq; Q++) {
+    const double* Dq = D + size_t(Q) * N * N;
+    for (int r = 0; r < N; r++) {
+      double acc = 0;
+      for (int s2 = 0; s2 < N; s2++) acc += Dq[r * N + s2] * din[Q][s2];
+      dout[Q][r] = acc;
+    }
+  }
+  // integrate each component with the weighted 1-D matrices
+  for (int i = 0; i < c; i++) {
+    double A20[q][q][n], A21[q][q][n], A22[q][q][n];
+    for (int qz = 0; qz < q; qz++)
+      for (int qy = 0; qy < q; qy++)
+        for (int dx = 0; dx < n; dx++) {
+          double s0 = 0, s1 = 0, s2 = 0;
+          for (int qx = 0; qx < q; qx++) {
+            int Q = (qz * q + qy) * q + qx;
+            s0 += Bw[qx][dx] * dout[Q][i] + Gw[qx][dx] * dout[Q][c + 3 * i];
+            s1 += Bw[qx][dx] * dout[Q][c + 3 * i + 1];
+            s2 += Bw[qx][dx] * dout[Q][c + 3 * i + 2];
+          }
+          A20[qz][qy][dx] = s0;
+          A21[qz][qy][dx] = s1;
+          A22[qz][qy][dx] = s2;
+        }
+    double A10[q][n][n], A11[q][n][n];
+    for (int qz = 0; qz < q; qz++)
+      for (int dy = 0; dy < n; dy++)
+        for (int dx = 0; dx < n; dx++) {
+          double s0 = 0, s1 = 0;
+          for (int qy = 0; qy < q; qy++) {
+            s0 += Bw[qy][dy] * A20[qz][qy][dx] + Gw[qy][dy] * A21[qz][qy][dx];
+            s1 += Bw[qy][dy] * A22[qz][qy][dx];
+          }
+          A10[qz][dy][dx] = s0;
+          A11[qz][dy][dx] = s1;
+        }
+    for (int dz = 0; dz < n; dz++)
+      for (int dy = 0; dy < n; dy++)
+        for (int dx = 0; dx < n; dx++) {
+          double s0 = 0;
+          for (int qz = 0; qz < q; qz++) s0 += Bw[qz][dz] * A10[qz][dy][dx] + Gw[qz][dz] * A11[qz][dy][dx];
+          out[i * n * n * n + (dz * n + dy) * n + dx] = s0;
+        }
+  }
+}
+
+extern "C" {
+
+// out E-vector = J(u) duE using the stored derivatives D of orc_linearize.
+int orc_apply_linearization(int p, int c, int ne, const double* D, const double* duE, double* out, int nthreads) {
+  if (p < 1 || p > 3 || (c != 1 && c != 3)) return -1;
+  const int n = p + 1, q = p + 1;
+  const double* pts = gl_points(q);
+  const double* wts = gl_weights(q);
+  double B[4][4] = {}, G[4][4] = {}, Bw[4][4] = {}, Gw[4][4] = {};
+  for (int i = 0; i < q; i++) {
+    lagrange(n, pts[i], B[i], G[i]);
+    for (int k = 0; k < n; k++) {
+      Bw[i][k] = B[i][k] * wts[i];
+      Gw[i][k] = G[i][k] * wts[i];
+    }
+  }
+  const int nd = n * n * n * c, nq = q * q * q, N = 4 * c;
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+#endif
+  for (int e = 0; e < ne; e++) {
+    const double* De = D + size_t(e) * nq * N * N;
+    const double* de = duE + size_t(e) * nd;
+    double* o = out + size_t(e) * nd;
+    if (p == 1 && c == 1) apply_linearization_element<2, 1>(B, G, Bw, Gw, De, de, o);
+    else if (p == 1 && c == 3) apply_linearization_element<2, 3>(B, G, Bw, Gw, De, de, o);
+    else if (p == 2 && c == 1) apply_linearization_element<3, 1>(B, G, Bw, Gw, De, de, o);
+    else if (p == 2 && c == 3) apply_linearization_element<3, 3>(B, G, Bw, Gw, De, de, o);
+    else if (p == 3 && c == 1) apply_linearization_element<4, 1>(B, G, Bw, Gw, De, de, o);
+    else apply_linearization_element<4, 3>(B, G, Bw, Gw, De, de, o);
+  }
+  return 0;
+}
+
+// E[(e c + k) npe + j] = L[k nnodes + conn[e npe + j]]   (element_restriction.cpp:443-454)
+int orc_gather(int64_t ne, int npe, int c, int64_t nnodes, const int64_t* conn, const double* L, double* E,
+               int nthreads) {
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+#endif
+  for (int64_t e = 0; e < ne; e++)
+    for (int k = 0; k < c; k++)
+      for (int j = 0; j < npe; j++) E[(e * c + k) * npe + j] = L[k * nnodes + conn[e * npe + j]];
+  return 0;
+}
+
+// L[k nnodes + n] = sum over the node's (element, local) entries of E, in
+// entry order (the node-owner form of ScatterAdd, element_restriction.cpp:456-467)
+int orc_scatter(int64_t nnodes, int npe, int c, const int64_t* node_ptr, const int64_t* node_ent, const double* E,
+                double* L, int nthreads) {
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+#endif
+  for (int64_t nd = 0; nd < nnodes; nd++)
+    for (int k = 0; k < c; k++) {
+      double acc = 0.0;
+      for (int64_t i = node_ptr[nd]; i < node_ptr[nd + 1]; i++) {
+        int64_t ent = node_ent[i];
+        int64_t e = ent / npe, j = ent % npe;
+        acc += E[(e * c + k) * npe + j];
+      }
+      L[k * nnodes + nd] = acc;
+    }
+  return 0;
+}
+
 }  // extern "C"

@@ -43,6 +43,7 @@ SIGNATURES = {
     "sfx_linearize": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp]),
     "sfx_jvp": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "sfx_jvp_f32": (_c.c_int, [_vp, _vp, _vp, _vp]),
+    "sfx_jvp_element": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "sfx_csr_nnz": (_c.c_int, [_vp, _i64p]),
     "sfx_csr_graph": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "sfx_assemble_csr": (_c.c_int, [_vp, _vp, _vp]),

@@ -268,6 +268,15 @@ int sfx_jvp_f32(sfx_form form, const float* du, float* dr, void* stream) {
   return SFX_OK;
 }
 
+int sfx_jvp_element(sfx_form form, const double* du, double* dE, void* stream) {
+  if (check_form(form)) return SFX_ERR_INVALID;
+  if (!du || !dE) return fail(SFX_ERR_INVALID, "null vector");
+  if (!form->linearized) return fail(SFX_ERR_INVALID, "sfx_linearize must be called before sfx_jvp_element");
+  if (form->domain.empty()) return fail(SFX_ERR_INVALID, "no domain integral");
+  return launch_domain(*form, form->domain[0], sfx::kernels::JVP, form->u_lin64.p, du, dE, form->t_lin,
+                       static_cast<cudaStream_t>(stream));
+}
+
 int sfx_update_qdata(sfx_form form, int flag) {
   if (check_form(form)) return SFX_ERR_INVALID;
   form->update_qdata = flag != 0;

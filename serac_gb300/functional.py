@@ -76,6 +76,41 @@ class Mesh:
             _lib.load().sfx_mesh_destroy(self._h)
             self._h = None
 
+    def node_coordinates(self, order):
+        """(num_nodes, 3) positions of the H1 nodes of the given order: the
+        trilinear image of each element's Gauss-Lobatto nodes."""
+        p = order
+        Nx, Ny, Nz = p * self.nx + 1, p * self.ny + 1, p * self.nz + 1
+        idx = np.arange(Nx * Ny * Nz)
+        I, J, K = idx % Nx, (idx // Nx) % Ny, idx // (Nx * Ny)
+        gll = {1: np.array([0.0, 1.0]), 2: np.array([0.0, 0.5, 1.0])}[p]
+        out = np.zeros((idx.size, 3))
+        ijk = []
+        for A, n in ((I, self.nx), (J, self.ny), (K, self.nz)):
+            e = np.minimum(A // p, n - 1)
+            ijk.append((e, gll[A - p * e]))
+        (ex, sx), (ey, sy), (ez, sz) = ijk
+        V = self.vertices.reshape(self.nz + 1, self.ny + 1, self.nx + 1, 3)
+        for c in range(2):
+            for b in range(2):
+                for a in range(2):
+                    w = (sx if a else 1 - sx) * (sy if b else 1 - sy) * (sz if c else 1 - sz)
+                    out += w[:, None] * V[ez + c, ey + b, ex + a]
+        return out
+
+    def boundary_nodes(self, order, sides):
+        """Sorted node ids on the given box sides (1: z=0, 2: y=0, 3: x=1,
+        4: y=1, 5: x=0, 6: z=1)."""
+        p = order
+        Nx, Ny, Nz = p * self.nx + 1, p * self.ny + 1, p * self.nz + 1
+        idx = np.arange(Nx * Ny * Nz)
+        I, J, K = idx % Nx, (idx // Nx) % Ny, idx // (Nx * Ny)
+        sel = np.zeros(idx.size, dtype=bool)
+        tests = {1: K == 0, 2: J == 0, 3: I == Nx - 1, 4: J == Ny - 1, 5: I == 0, 6: K == Nz - 1}
+        for s in sides:
+            sel |= tests[s]
+        return idx[sel]
+
 
 def box_vertices(nx, ny, nz, perturb=0.0, seed=0):
     """Vertices of the unit cube grid; interior vertices moved uniformly by up
@@ -121,6 +156,15 @@ class Gradient:
         return out
 
     Mult = mult
+
+    def element_action(self, du, out=None, stream=None):
+        """Element-level action [e][component][node] before the scatter-add."""
+        f = self.form
+        _require(du, torch.float64, f.ndofs, "du")
+        n = f.mesh.num_elements * f.space.components * (f.space.order + 1) ** 3
+        out = torch.empty(n, dtype=torch.float64, device=du.device) if out is None else out
+        _lib.call("sfx_jvp_element", f._h, _dptr(du), _dptr(out), _stream(stream))
+        return out
 
     def __call__(self, du):
         return self.mult(du)

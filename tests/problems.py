@@ -19,9 +19,9 @@ def mesh(nx, ny, nz, perturb=0.1, seed=1):
     return O.StructuredHexMesh(nx, ny, nz, O.box_vertices(nx, ny, nz, perturb, seed))
 
 
-def fields(ndofs, mat, seed=0):
+def fields(ndofs, mat, seed=0, scale=1.0):
     rng = np.random.default_rng(seed)
-    u = rng.standard_normal(ndofs) * AMPLITUDE.get(mat, 0.3)
+    u = rng.standard_normal(ndofs) * AMPLITUDE.get(mat, 0.3) * scale
     du = rng.standard_normal(ndofs)
     return u, du
 
