@@ -428,3 +428,273 @@ __global__ void __launch_bounds__(256) geometry_kernel(const double* __restrict_
 
 }  // namespace kernels
 }  // namespace sfx
+
+namespace sfx {
+namespace kernels {
+
+/// Element stiffness matrices dR_e/du_e at the linearisation point, stored
+/// K[e][trial vdof][test vdof] like serac's element_gradient_kernel
+/// (domain_integral_kernels.hpp:327-361; vdof = component * NPE + node).
+/// Lane q first linearises the q-function at its point one trial component
+/// at a time (4 directional dual evaluations seeded on the parent-space value
+/// and gradient, giving the 4C x 4 block of the derivative), then for every
+/// trial node j applies that block to (phi_j, grad_xi phi_j) at its point and
+/// integrates with the transposed sum-factorised passes, so that lane i ends
+/// with K[(cj, j)][(ci, i)].  diag_only: only the diagonal entries, written to
+/// an E-vector [e][c][node].
+template <int P, int C, typename State, typename QFMaker, bool diag_only>
+__global__ void __launch_bounds__(128) element_matrix_kernel(DomainArgs<double> a, QFMaker make_qf, int64_t e_begin,
+                                                             int64_t e_end) {
+  using Real = double;
+  constexpr int Q = P + 1;
+  constexpr int NQ = Q * Q * Q;
+  constexpr int EPW = 32 / NQ;
+  constexpr int NDOF = C * NQ;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int sub = lane / NQ;
+  const int qi_raw = lane - sub * NQ;
+  const bool slot = sub < EPW;
+  const int qi = slot ? qi_raw : NQ - 1;
+  const int base = slot ? sub * NQ : 0;
+  const int64_t e = e_begin + warp * EPW + (slot ? sub : 0);
+  const bool valid = slot && e < e_end;
+  const int ix = qi % Q, iy = (qi / Q) % Q, iz = qi / (Q * Q);
+
+  __shared__ Real sB[Q][Q], sG[Q][Q];
+  if (threadIdx.x < Q * Q) {
+    int i = threadIdx.x / Q, j = threadIdx.x % Q;
+    sB[i][j] = basis_B(P, i, j);
+    sG[i][j] = basis_G(P, i, j);
+  }
+  __syncthreads();
+
+  const int64_t nq_total = a.num_elements * NQ;
+  const int64_t gq = e * NQ + qi;
+  const int64_t el = e - e_begin;  // slot in the output chunk
+  int32_t node = valid ? a.conn[e * NQ + qi] : 0;
+
+  value_t<C, Real> uv{};
+  grad_t<C, Real> ug{};
+#pragma unroll
+  for (int c = 0; c < C; c++) {
+    Real U = valid ? a.u[c * a.num_nodes + node] : Real(0);
+    Real g[3];
+    interpolate_lane<Q, Real>(U, base, ix, iy, iz, sB, sG, comp<C>(uv, c), g[0], g[1], g[2]);
+    for (int j = 0; j < 3; j++) comp<C>(ug, c)[j] = g[j];
+  }
+
+  Real Ji[3][3];
+  Real dvol = 0;
+  tensor<Real, 3> X{};
+  tensor<Real, 3, 3> Jm{};
+  if (valid) {
+    const Real* g = a.geom + gq;
+#pragma unroll
+    for (int k = 0; k < 9; k++) Ji[k / 3][k % 3] = g[k * nq_total];
+    dvol = g[9 * nq_total];
+#pragma unroll
+    for (int k = 0; k < 3; k++) X[k] = g[(10 + k) * nq_total];
+#pragma unroll
+    for (int k = 0; k < 9; k++) Jm[k / 3][k % 3] = g[(13 + k) * nq_total];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 9; k++) Ji[k / 3][k % 3] = Real(k % 4 == 0);
+  }
+  // physical gradient of u
+  Real gx[C][3];
+#pragma unroll
+  for (int c = 0; c < C; c++)
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+      gx[c][j] = comp<C>(ug, c)[0] * Ji[0][j] + comp<C>(ug, c)[1] * Ji[1][j] + comp<C>(ug, c)[2] * Ji[2][j];
+
+  const auto qf = make_qf(a.params + (valid ? e : 0) * QFMaker::nparams);
+  auto position = tuple{X, Jm};
+  State st0{};
+  if constexpr (!std::is_same<State, Nothing>::value) {
+    if (valid) load_state(st0, a.state, gq, nq_total);
+  }
+  using S = dual<Real, Real>;
+
+#pragma unroll 1
+  for (int cj = 0; cj < C; cj++) {
+    // D[out][b]: derivative of parent-space output `out` (source ci, flux ci*3+k)
+    // w.r.t. the parent-space input b of component cj (0: value, 1..3: d/dxi_k)
+    Real Ds[C][4];
+    Real Df[C][3][4];
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      value_t<C, S> qv{};
+      grad_t<C, S> qg{};
+#pragma unroll
+      for (int c = 0; c < C; c++) {
+        comp<C>(qv, c) = S{comp<C>(uv, c), Real(c == cj && b == 0)};
+#pragma unroll
+        for (int j = 0; j < 3; j++) comp<C>(qg, c)[j] = S{gx[c][j], (c == cj && b > 0) ? Ji[b - 1][j] : Real(0)};
+      }
+      auto arg = tuple{qv, qg};
+      auto call = [&]() {
+        if constexpr (std::is_same<State, Nothing>::value) {
+          return qf(a.t, position, arg);
+        } else {
+          State st = st0;
+          return qf(a.t, position, st, arg);
+        }
+      };
+      auto out = call();
+      using SrcT = std::decay_t<decltype(get<0>(out))>;
+      using FluxT = std::decay_t<decltype(get<1>(out))>;
+#pragma unroll
+      for (int ci = 0; ci < C; ci++) {
+        if constexpr (has_part<JVP, SrcT>()) Ds[ci][b] = dvol * part<JVP, Real>(source_comp<C>(get<0>(out), ci));
+        else Ds[ci][b] = 0;
+        if constexpr (has_part<JVP, FluxT>()) {
+          auto frow = flux_row<C>(get<1>(out), ci);
+          Real fp[3];
+#pragma unroll
+          for (int m = 0; m < 3; m++) fp[m] = part<JVP, Real>(frow[m]);
+#pragma unroll
+          for (int k = 0; k < 3; k++) Df[ci][k][b] = dvol * (fp[0] * Ji[k][0] + fp[1] * Ji[k][1] + fp[2] * Ji[k][2]);
+        } else {
+#pragma unroll
+          for (int k = 0; k < 3; k++) Df[ci][k][b] = 0;
+        }
+      }
+    }
+    if constexpr (diag_only) {
+      // K[(cj,i)][(cj,i)] = sum_q Psi_i(q)^T D Psi_i(q): each lane needs every
+      // point's contribution for its own node: integrate with trial node = test node
+#pragma unroll 1
+      for (int j = 0; j < NQ; j++) {
+        const int jx = j % Q, jy = (j / Q) % Q, jz = j / (Q * Q);
+        Real psi[4] = {sB[ix][jx] * sB[iy][jy] * sB[iz][jz], sG[ix][jx] * sB[iy][jy] * sB[iz][jz],
+                       sB[ix][jx] * sG[iy][jy] * sB[iz][jz], sB[ix][jx] * sB[iy][jy] * sG[iz][jz]};
+        Real s = Ds[cj][0] * psi[0] + Ds[cj][1] * psi[1] + Ds[cj][2] * psi[2] + Ds[cj][3] * psi[3];
+        Real f[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+          f[k] = Df[cj][k][0] * psi[0] + Df[cj][k][1] * psi[1] + Df[cj][k][2] * psi[2] + Df[cj][k][3] * psi[3];
+        Real r = integrate_lane<Q, true, true, Real>(s, f[0], f[1], f[2], base, ix, iy, iz, sB, sG);
+        if (valid && qi == j) a.out_e[(e * C + cj) * NQ + qi] = r;  // diagonal E-vector covers all elements
+      }
+    } else {
+#pragma unroll 1
+      for (int j = 0; j < NQ; j++) {
+        const int jx = j % Q, jy = (j / Q) % Q, jz = j / (Q * Q);
+        Real psi[4] = {sB[ix][jx] * sB[iy][jy] * sB[iz][jz], sG[ix][jx] * sB[iy][jy] * sB[iz][jz],
+                       sB[ix][jx] * sG[iy][jy] * sB[iz][jz], sB[ix][jx] * sB[iy][jy] * sG[iz][jz]};
+        Real* col = a.out_e + (el * NDOF + (cj * NQ + j)) * int64_t(NDOF);
+#pragma unroll
+        for (int ci = 0; ci < C; ci++) {
+          Real s = Ds[ci][0] * psi[0] + Ds[ci][1] * psi[1] + Ds[ci][2] * psi[2] + Ds[ci][3] * psi[3];
+          Real f[3];
+#pragma unroll
+          for (int k = 0; k < 3; k++)
+            f[k] = Df[ci][k][0] * psi[0] + Df[ci][k][1] * psi[1] + Df[ci][k][2] * psi[2] + Df[ci][k][3] * psi[3];
+          Real r = integrate_lane<Q, true, true, Real>(s, f[0], f[1], f[2], base, ix, iy, iz, sB, sG);
+          if (valid) col[ci * NQ + qi] = r;
+        }
+      }
+    }
+  }
+}
+
+/// CSR graph of a structured-mesh H1 form: row (comp, node) holds, for every
+/// component, the box of nodes covered by the elements that contain the node
+/// (the union of their nodes is the product of three 1-D index ranges).
+struct GridShape {
+  int p;
+  int64_t N[3];   // nodes per direction
+  int64_t ne[3];  // elements per direction
+};
+
+SFX_HDI void node_range(const GridShape& g, int d, int64_t I, int64_t& lo, int64_t& hi) {
+  const int p = g.p;
+  if (I % p == 0) {
+    int64_t e = I / p;
+    lo = (e > 0) ? I - p : I;
+    hi = (e < g.ne[d]) ? I + p : I;
+  } else {
+    int64_t e = I / p;
+    lo = e * p;
+    hi = e * p + p;
+  }
+}
+
+template <int C>
+__global__ void csr_row_length_kernel(GridShape g, int64_t* row_len) {
+  const int64_t nn = g.N[0] * g.N[1] * g.N[2];
+  int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (r >= nn * C) return;
+  int64_t node = r % nn;
+  int64_t I = node % g.N[0], J = (node / g.N[0]) % g.N[1], K = node / (g.N[0] * g.N[1]);
+  int64_t l0, h0, l1, h1, l2, h2;
+  node_range(g, 0, I, l0, h0);
+  node_range(g, 1, J, l1, h1);
+  node_range(g, 2, K, l2, h2);
+  row_len[r + 1] = int64_t(C) * (h0 - l0 + 1) * (h1 - l1 + 1) * (h2 - l2 + 1);
+  if (r == 0) row_len[0] = 0;
+}
+
+template <int C>
+__global__ void csr_fill_kernel(GridShape g, const int64_t* __restrict__ row_ptr, int32_t* __restrict__ col) {
+  const int64_t nn = g.N[0] * g.N[1] * g.N[2];
+  int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (r >= nn * C) return;
+  int64_t node = r % nn;
+  int64_t I = node % g.N[0], J = (node / g.N[0]) % g.N[1], K = node / (g.N[0] * g.N[1]);
+  int64_t l0, h0, l1, h1, l2, h2;
+  node_range(g, 0, I, l0, h0);
+  node_range(g, 1, J, l1, h1);
+  node_range(g, 2, K, l2, h2);
+  int64_t k = row_ptr[r];
+  for (int c = 0; c < C; c++)
+    for (int64_t z = l2; z <= h2; z++)
+      for (int64_t y = l1; y <= h1; y++)
+        for (int64_t x = l0; x <= h0; x++) col[k++] = int32_t(c * nn + x + g.N[0] * (y + g.N[1] * z));
+}
+
+/// values[row] = sum over the row node's elements (element order) of the
+/// element-matrix entries; one thread per row, so the order of the additions
+/// is fixed.  Ke: [e][trial vdof][test vdof].
+template <int P, int C>
+__global__ void csr_assemble_kernel(GridShape g, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ conn,
+                                    const int32_t* __restrict__ node_ptr, const int32_t* __restrict__ node_ent,
+                                    const double* __restrict__ Ke, int64_t e_begin, int64_t e_end,
+                                    double* __restrict__ values, bool accumulate) {
+  constexpr int NPE = (P + 1) * (P + 1) * (P + 1);
+  constexpr int NDOF = C * NPE;
+  const int64_t nn = g.N[0] * g.N[1] * g.N[2];
+  int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (r >= nn * C) return;
+  const int ci = int(r / nn);
+  const int64_t node = r - ci * nn;
+  int64_t I = node % g.N[0], J = (node / g.N[0]) % g.N[1], K = node / (g.N[0] * g.N[1]);
+  int64_t l0, h0, l1, h1, l2, h2;
+  node_range(g, 0, I, l0, h0);
+  node_range(g, 1, J, l1, h1);
+  node_range(g, 2, K, l2, h2);
+  const int64_t w0 = h0 - l0 + 1, w1 = h1 - l1 + 1, w2 = h2 - l2 + 1;
+  const int64_t scalar_len = w0 * w1 * w2;
+  double* row = values + row_ptr[r];
+  if (!accumulate)
+    for (int64_t k = 0; k < C * scalar_len; k++) row[k] = 0.0;
+  for (int32_t t = node_ptr[node]; t < node_ptr[node + 1]; t++) {
+    const int32_t ent = node_ent[t];
+    const int64_t e = ent / NPE;
+    if (e < e_begin || e >= e_end) continue;
+    const int a = ent - int(e) * NPE;
+    const double* Kcol = Ke + (e - e_begin) * NDOF * NDOF + (ci * NPE + a);  // stride NDOF over trial vdofs
+    for (int b = 0; b < NPE; b++) {
+      const int64_t nb = conn[e * NPE + b];
+      const int64_t x = nb % g.N[0], y = (nb / g.N[0]) % g.N[1], z = nb / (g.N[0] * g.N[1]);
+      const int64_t pos = ((z - l2) * w1 + (y - l1)) * w0 + (x - l0);
+#pragma unroll
+      for (int cj = 0; cj < C; cj++) row[cj * scalar_len + pos] += Kcol[int64_t(cj * NPE + b) * NDOF];
+    }
+  }
+}
+
+}  // namespace kernels
+}  // namespace sfx

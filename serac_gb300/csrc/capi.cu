@@ -55,6 +55,11 @@ int check_form(sfx_form f) {
 }
 
 }  // namespace
+
+int scatter_evector(const sfx_form_s& f, const double* E, double* out, bool accumulate, cudaStream_t s) {
+  return scatter_dispatch<double>(f, E, out, accumulate, s);
+}
+
 }  // namespace sfx_impl
 
 using namespace sfx_impl;

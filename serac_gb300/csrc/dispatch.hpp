@@ -12,6 +12,13 @@ int material_info(int material, int* components, int* nparams, int* state_double
 // mode: 0 residual, 1 residual committing state, 2 Jacobian action (FP64)
 int launch_domain(const sfx_form_s& f, const DomainIntegral& di, int mode, const double* u, const double* du,
                   double* E, double t, cudaStream_t s);
+// element matrices K[e - e0][trial][test] of elements [e0, e1) at the
+// linearisation point, or (diag_only) their diagonals as an E-vector over all elements
+int launch_element_matrix(const sfx_form_s& f, const DomainIntegral& di, bool diag_only, double* out, int64_t e0,
+                          int64_t e1, cudaStream_t s);
+// scatter-add of an E-vector [e][c][node] into an L-vector
+int scatter_evector(const sfx_form_s& f, const double* E, double* out, bool accumulate, cudaStream_t s);
+
 int launch_domain_jvp_f32(const sfx_form_s& f, const DomainIntegral& di, const float* u, const float* du, float* E,
                           double t, cudaStream_t s);
 

@@ -93,7 +93,47 @@ int dispatch(const sfx_form_s& f, const DomainIntegral& di, const Real* u, const
   return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
 }
 
+template <int P, int C, typename State, typename Maker>
+int launch_em(const sfx_form_s& f, const DomainIntegral& di, bool diag_only, double* out, int64_t e0, int64_t e1,
+              cudaStream_t s) {
+  constexpr int NQ = (P + 1) * (P + 1) * (P + 1);
+  constexpr int EPW = 32 / NQ;
+  if (e1 <= e0) return SFX_OK;
+  kernels::DomainArgs<double> a{f.u_lin64.p, nullptr, out, f.conn.p, f.geom64.p, di.state.p, di.params.p,
+                                f.nnodes, f.ne, f.t_lin};
+  int64_t warps = (e1 - e0 + EPW - 1) / EPW;
+  int64_t blocks = (warps * 32 + 127) / 128;
+  if (diag_only)
+    kernels::element_matrix_kernel<P, C, State, Maker, true><<<unsigned(blocks), 128, 0, s>>>(a, Maker{}, e0, e1);
+  else
+    kernels::element_matrix_kernel<P, C, State, Maker, false><<<unsigned(blocks), 128, 0, s>>>(a, Maker{}, e0, e1);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("element matrix launch: ") + cudaGetErrorString(err));
+  return SFX_OK;
+}
+
+template <int P>
+int dispatch_em(const sfx_form_s& f, const DomainIntegral& di, bool diag_only, double* out, int64_t e0, int64_t e1,
+                cudaStream_t s) {
+  switch (di.material) {
+    case SFX_MAT_HEAT: return launch_em<P, 1, Nothing, HeatMaker>(f, di, diag_only, out, e0, e1, s);
+    case SFX_MAT_NONLINEAR_HEAT: return launch_em<P, 1, Nothing, NonlinearHeatMaker>(f, di, diag_only, out, e0, e1, s);
+    case SFX_MAT_THERMAL_TEST: return launch_em<P, 1, Nothing, ThermalTestMaker>(f, di, diag_only, out, e0, e1, s);
+    case SFX_MAT_ELASTIC_TEST: return launch_em<P, 3, Nothing, ElasticTestMaker>(f, di, diag_only, out, e0, e1, s);
+    case SFX_MAT_NEOHOOKEAN: return launch_em<P, 3, Empty, NeoHookeanMaker>(f, di, diag_only, out, e0, e1, s);
+    case SFX_MAT_J2: return launch_em<P, 3, J2::State, J2Maker>(f, di, diag_only, out, e0, e1, s);
+  }
+  return fail(SFX_ERR_UNSUPPORTED, "unknown material");
+}
+
 }  // namespace
+
+int launch_element_matrix(const sfx_form_s& f, const DomainIntegral& di, bool diag_only, double* out, int64_t e0,
+                          int64_t e1, cudaStream_t s) {
+  if (f.p == 1) return dispatch_em<1>(f, di, diag_only, out, e0, e1, s);
+  if (f.p == 2) return dispatch_em<2>(f, di, diag_only, out, e0, e1, s);
+  return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
+}
 
 int material_info(int material, int* components, int* nparams, int* state_doubles) {
   switch (material) {
