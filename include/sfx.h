@@ -105,6 +105,17 @@ int sfx_residual(sfx_form form, double t, const double* u, double* r, void* stre
  * its own copy of u (FP64 and FP32). */
 int sfx_linearize(sfx_form form, double t, const double* u, double* r, void* stream);
 
+/* How sfx_jvp applies the linearisation:
+ *   SFX_JVP_STORED_TANGENT (default): sfx_linearize evaluates the q-function
+ *     derivative at every quadrature point once and stores it (FP64 and FP32
+ *     copies, serac's own scheme: domain_integral_kernels.hpp:209-214, 277-304);
+ *     each Jacobian action then only interpolates du, applies it and integrates.
+ *   SFX_JVP_RECOMPUTE: nothing is stored; every Jacobian action re-evaluates
+ *     the q-function on directional dual numbers (less memory, more FP64 work). */
+#define SFX_JVP_STORED_TANGENT 0
+#define SFX_JVP_RECOMPUTE 1
+int sfx_form_set_jvp_mode(sfx_form form, int mode);
+
 /* dr = dR/du(t_lin, u_lin) du, in FP64, and in FP32 (FP32 accumulation). */
 int sfx_jvp(sfx_form form, const double* du, double* dr, void* stream);
 int sfx_jvp_f32(sfx_form form, const float* du, float* dr, void* stream);

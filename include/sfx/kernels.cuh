@@ -698,3 +698,266 @@ __global__ void csr_assemble_kernel(GridShape g, const int64_t* __restrict__ row
 
 }  // namespace kernels
 }  // namespace sfx
+
+namespace sfx {
+namespace kernels {
+
+template <typename State, typename QF, typename Pos, typename Arg>
+SFX_HDI auto invoke_qf(const QF& qf, double t, const Pos& pos, State& st, const Arg& arg) {
+  if constexpr (std::is_same<State, Nothing>::value) {
+    (void)st;
+    return qf(t, pos, arg);
+  } else {
+    return qf(t, pos, st, arg);
+  }
+}
+
+/// Whether the q-function's source output depends on the trial field (the
+/// stored derivative then has source rows).
+template <int C, typename State, typename QF>
+constexpr bool tangent_has_source() {
+  using S = dual<double, double>;
+  using Out = decltype(invoke_qf<State>(std::declval<const QF&>(), 0.0,
+                                        std::declval<tuple<tensor<double, 3>, tensor<double, 3, 3>>>(),
+                                        std::declval<State&>(), std::declval<tuple<value_t<C, S>, grad_t<C, S>>>()));
+  using SrcT = std::decay_t<decltype(get<0>(std::declval<Out>()))>;
+  return has_part<JVP, SrcT>();
+}
+
+/// Shape of the stored q-function derivative per quadrature point:
+/// rows = parent-space outputs (source components if the source depends on the
+/// trial field, then the C x 3 flux), cols = parent-space inputs (values if the
+/// q-function reads them, then the C x 3 gradient).
+template <int C, bool HS, bool VI>
+struct TangentShape {
+  static constexpr int rows = (HS ? C : 0) + 3 * C;
+  static constexpr int cols = (VI ? C : 0) + 3 * C;
+  static constexpr int size = rows * cols;
+};
+
+/// Linearise the q-function at every quadrature point (the derivative serac
+/// stores in evaluation_kernel_impl, domain_integral_kernels.hpp:209-214, after
+/// physical_to_parent, with det(J) w folded in) and, optionally, write the
+/// element residuals of the same evaluation.  D is stored structure-of-arrays
+/// D[(row * cols + col) * nq_total + point] in FP64 and FP32.
+template <int P, int C, typename State, typename QFMaker>
+__global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QFMaker make_qf, double* __restrict__ D64,
+                                                        float* __restrict__ D32, double* __restrict__ res_e) {
+  using Real = double;
+  constexpr int Q = P + 1;
+  constexpr int NQ = Q * Q * Q;
+  constexpr int EPW = 32 / NQ;
+  constexpr bool VI = QFMaker::value_input;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int sub = lane / NQ;
+  const int qi_raw = lane - sub * NQ;
+  const bool slot = sub < EPW;
+  const int qi = slot ? qi_raw : NQ - 1;
+  const int base = slot ? sub * NQ : 0;
+  const int64_t e = warp * EPW + (slot ? sub : 0);
+  const bool valid = slot && e < a.num_elements;
+  const int ix = qi % Q, iy = (qi / Q) % Q, iz = qi / (Q * Q);
+
+  __shared__ Real sB[Q][Q], sG[Q][Q];
+  if (threadIdx.x < Q * Q) {
+    int i = threadIdx.x / Q, j = threadIdx.x % Q;
+    sB[i][j] = basis_B(P, i, j);
+    sG[i][j] = basis_G(P, i, j);
+  }
+  __syncthreads();
+
+  const int64_t nq_total = a.num_elements * NQ;
+  const int64_t gq = e * NQ + qi;
+  int32_t node = valid ? a.conn[e * NQ + qi] : 0;
+
+  value_t<C, Real> uv{};
+  grad_t<C, Real> ug{};
+#pragma unroll
+  for (int c = 0; c < C; c++) {
+    Real U = valid ? a.u[c * a.num_nodes + node] : Real(0);
+    Real g[3];
+    interpolate_lane<Q, Real>(U, base, ix, iy, iz, sB, sG, comp<C>(uv, c), g[0], g[1], g[2]);
+    for (int j = 0; j < 3; j++) comp<C>(ug, c)[j] = g[j];
+  }
+  Real Ji[3][3];
+  Real dvol = 0;
+  tensor<Real, 3> X{};
+  tensor<Real, 3, 3> Jm{};
+  if (valid) {
+    const Real* g = a.geom + gq;
+#pragma unroll
+    for (int k = 0; k < 9; k++) Ji[k / 3][k % 3] = g[k * nq_total];
+    dvol = g[9 * nq_total];
+#pragma unroll
+    for (int k = 0; k < 3; k++) X[k] = g[(10 + k) * nq_total];
+#pragma unroll
+    for (int k = 0; k < 9; k++) Jm[k / 3][k % 3] = g[(13 + k) * nq_total];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 9; k++) Ji[k / 3][k % 3] = Real(k % 4 == 0);
+  }
+  Real gx[C][3];
+#pragma unroll
+  for (int c = 0; c < C; c++)
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+      gx[c][j] = comp<C>(ug, c)[0] * Ji[0][j] + comp<C>(ug, c)[1] * Ji[1][j] + comp<C>(ug, c)[2] * Ji[2][j];
+
+  const auto qf = make_qf(a.params + (valid ? e : 0) * QFMaker::nparams);
+  auto position = tuple{X, Jm};
+  State st0{};
+  if constexpr (!std::is_same<State, Nothing>::value) {
+    if (valid) load_state(st0, a.state, gq, nq_total);
+  }
+  using S = dual<Real, Real>;
+  constexpr int NCOLS = (VI ? C : 0) + 3 * C;
+
+  Real res_s[C] = {}, res_f[C][3] = {};
+  bool have_res = false;
+#pragma unroll 1
+  for (int k = 0; k < NCOLS; k++) {
+    // seed: value of component k (k < C when VI), else gradient entry (c, b)
+    const int kk = VI ? k : k + C;
+    const int seed_c = kk < C ? kk : (kk - C) / 3;
+    const int seed_b = kk < C ? -1 : (kk - C) % 3;
+    value_t<C, S> qv{};
+    grad_t<C, S> qg{};
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+      comp<C>(qv, c) = S{comp<C>(uv, c), Real(c == seed_c && seed_b < 0)};
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+        comp<C>(qg, c)[j] = S{gx[c][j], (c == seed_c && seed_b >= 0) ? Ji[seed_b][j] : Real(0)};
+    }
+    auto arg = tuple{qv, qg};
+    auto call = [&]() {
+      if constexpr (std::is_same<State, Nothing>::value) {
+        return qf(a.t, position, arg);
+      } else {
+        State st = st0;
+        return qf(a.t, position, st, arg);
+      }
+    };
+    auto out = call();
+    using SrcT = std::decay_t<decltype(get<0>(out))>;
+    using FluxT = std::decay_t<decltype(get<1>(out))>;
+    constexpr bool HS = has_part<JVP, SrcT>();
+    using Shape = TangentShape<C, HS, VI>;
+    int row = 0;
+#pragma unroll
+    for (int ci = 0; ci < C; ci++) {
+      if constexpr (HS) {
+        Real v = dvol * part<JVP, Real>(source_comp<C>(get<0>(out), ci));
+        if (valid) {
+          D64[(int64_t(ci) * Shape::cols + k) * nq_total + gq] = v;
+          D32[(int64_t(ci) * Shape::cols + k) * nq_total + gq] = float(v);
+        }
+      }
+    }
+    row = HS ? C : 0;
+#pragma unroll
+    for (int ci = 0; ci < C; ci++) {
+      Real fp[3] = {0, 0, 0}, fv[3] = {0, 0, 0};
+      if constexpr (has_part<JVP, FluxT>()) {
+        auto frow = flux_row<C>(get<1>(out), ci);
+#pragma unroll
+        for (int m = 0; m < 3; m++) fp[m] = part<JVP, Real>(frow[m]);
+      }
+      if constexpr (has_part<RESIDUAL, FluxT>()) {
+        auto frow = flux_row<C>(get<1>(out), ci);
+#pragma unroll
+        for (int m = 0; m < 3; m++) fv[m] = part<RESIDUAL, Real>(frow[m]);
+      }
+#pragma unroll
+      for (int kd = 0; kd < 3; kd++) {
+        Real v = dvol * (fp[0] * Ji[kd][0] + fp[1] * Ji[kd][1] + fp[2] * Ji[kd][2]);
+        if (valid) {
+          D64[(int64_t(row + 3 * ci + kd) * Shape::cols + k) * nq_total + gq] = v;
+          D32[(int64_t(row + 3 * ci + kd) * Shape::cols + k) * nq_total + gq] = float(v);
+        }
+        if (!have_res) res_f[ci][kd] = dvol * (fv[0] * Ji[kd][0] + fv[1] * Ji[kd][1] + fv[2] * Ji[kd][2]);
+      }
+      if constexpr (has_part<RESIDUAL, SrcT>()) {
+        if (!have_res) res_s[ci] = dvol * part<RESIDUAL, Real>(source_comp<C>(get<0>(out), ci));
+      }
+    }
+    have_res = true;
+  }
+  if (res_e != nullptr) {
+    // element residuals of the linearisation point (value part of the evaluation)
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+      Real r = integrate_lane<Q, true, true, Real>(res_s[c], res_f[c][0], res_f[c][1], res_f[c][2], base, ix, iy, iz,
+                                                   sB, sG);
+      if (valid) res_e[(e * C + c) * NQ + qi] = r;
+    }
+  }
+}
+
+/// Jacobian action from the stored derivative (serac's action_of_gradient_kernel,
+/// domain_integral_kernels.hpp:277-304): interpolate du, apply D, integrate.
+template <int P, int C, bool HS, bool VI, typename Real>
+__global__ void __launch_bounds__(128) jvp_stored_kernel(const Real* __restrict__ du, const Real* __restrict__ D,
+                                                         const int32_t* __restrict__ conn, Real* __restrict__ out_e,
+                                                         int64_t num_nodes, int64_t num_elements) {
+  constexpr int Q = P + 1;
+  constexpr int NQ = Q * Q * Q;
+  constexpr int EPW = 32 / NQ;
+  using Shape = TangentShape<C, HS, VI>;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int sub = lane / NQ;
+  const int qi_raw = lane - sub * NQ;
+  const bool slot = sub < EPW;
+  const int qi = slot ? qi_raw : NQ - 1;
+  const int base = slot ? sub * NQ : 0;
+  const int64_t e = warp * EPW + (slot ? sub : 0);
+  const bool valid = slot && e < num_elements;
+  const int ix = qi % Q, iy = (qi / Q) % Q, iz = qi / (Q * Q);
+
+  __shared__ Real sB[Q][Q], sG[Q][Q];
+  if (threadIdx.x < Q * Q) {
+    int i = threadIdx.x / Q, j = threadIdx.x % Q;
+    sB[i][j] = Real(basis_B(P, i, j));
+    sG[i][j] = Real(basis_G(P, i, j));
+  }
+  __syncthreads();
+
+  const int64_t nq_total = num_elements * NQ;
+  const int64_t gq = e * NQ + qi;
+  const int32_t node = valid ? conn[e * NQ + qi] : 0;
+
+  Real din[Shape::cols];
+#pragma unroll
+  for (int c = 0; c < C; c++) {
+    Real U = valid ? du[c * num_nodes + node] : Real(0);
+    Real v, g0, g1, g2;
+    interpolate_lane<Q, Real>(U, base, ix, iy, iz, sB, sG, v, g0, g1, g2);
+    if constexpr (VI) din[c] = v;
+    constexpr int off = VI ? C : 0;
+    din[off + 3 * c + 0] = g0;
+    din[off + 3 * c + 1] = g1;
+    din[off + 3 * c + 2] = g2;
+  }
+  Real dout[Shape::rows];
+  const Real* Dq = D + (valid ? gq : 0);
+#pragma unroll
+  for (int r = 0; r < Shape::rows; r++) {
+    Real acc = 0;
+#pragma unroll
+    for (int k = 0; k < Shape::cols; k++) acc += (valid ? Dq[(int64_t(r) * Shape::cols + k) * nq_total] : Real(0)) * din[k];
+    dout[r] = acc;
+  }
+  constexpr int roff = HS ? C : 0;
+#pragma unroll
+  for (int c = 0; c < C; c++) {
+    Real s = HS ? dout[HS ? c : 0] : Real(0);
+    Real r = integrate_lane<Q, HS, true, Real>(s, dout[roff + 3 * c], dout[roff + 3 * c + 1], dout[roff + 3 * c + 2],
+                                               base, ix, iy, iz, sB, sG);
+    if (valid) out_e[(e * C + c) * NQ + qi] = r;
+  }
+}
+
+}  // namespace kernels
+}  // namespace sfx

@@ -41,6 +41,7 @@ SIGNATURES = {
     "sfx_form_add_boundary_integral": (_c.c_int, [_vp, _c.c_int, _c.c_int, _dp]),
     "sfx_residual": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp]),
     "sfx_linearize": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp]),
+    "sfx_form_set_jvp_mode": (_c.c_int, [_vp, _c.c_int]),
     "sfx_jvp": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "sfx_jvp_f32": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "sfx_jvp_element": (_c.c_int, [_vp, _vp, _vp, _vp]),

@@ -236,6 +236,14 @@ int sfx_linearize(sfx_form form, double t, const double* u, double* r, void* str
   SFX_CUDA_TRY(cudaGetLastError());
   form->t_lin = t;
   form->linearized = true;
+  if (form->jvp_mode == SFX_JVP_STORED_TANGENT) {
+    for (size_t i = 0; i < form->domain.size(); i++) {
+      if (int rc = launch_linearize(*form, form->domain[i], r ? form->e64.p : nullptr, s)) return rc;
+      if (r)
+        if (int rc = scatter_dispatch<double>(*form, form->e64.p, r, i > 0, s)) return rc;
+    }
+    return SFX_OK;
+  }
   if (r) {
     bool saved = form->update_qdata;
     form->update_qdata = false;
@@ -246,16 +254,26 @@ int sfx_linearize(sfx_form form, double t, const double* u, double* r, void* str
   return SFX_OK;
 }
 
+int sfx_form_set_jvp_mode(sfx_form form, int mode) {
+  if (check_form(form)) return SFX_ERR_INVALID;
+  if (mode != SFX_JVP_STORED_TANGENT && mode != SFX_JVP_RECOMPUTE) return fail(SFX_ERR_INVALID, "unknown jvp mode");
+  if (mode != form->jvp_mode) form->linearized = false;
+  form->jvp_mode = mode;
+  return SFX_OK;
+}
+
 int sfx_jvp(sfx_form form, const double* du, double* dr, void* stream) {
   if (check_form(form)) return SFX_ERR_INVALID;
   if (!du || !dr) return fail(SFX_ERR_INVALID, "null vector");
   if (!form->linearized) return fail(SFX_ERR_INVALID, "sfx_linearize must be called before sfx_jvp");
   auto s = static_cast<cudaStream_t>(stream);
   for (size_t i = 0; i < form->domain.size(); i++) {
-    if (int rc = launch_domain(*form, form->domain[i], sfx::kernels::JVP, form->u_lin64.p, du, form->e64.p,
-                               form->t_lin, s))
-      return rc;
-    if (int rc = scatter_dispatch<double>(*form, form->e64.p, dr, i > 0, s)) return rc;
+    int rc = form->jvp_mode == SFX_JVP_STORED_TANGENT
+                 ? launch_jvp_stored(*form, form->domain[i], du, form->e64.p, s)
+                 : launch_domain(*form, form->domain[i], sfx::kernels::JVP, form->u_lin64.p, du, form->e64.p,
+                                 form->t_lin, s);
+    if (rc) return rc;
+    if (int rc2 = scatter_dispatch<double>(*form, form->e64.p, dr, i > 0, s)) return rc2;
   }
   return SFX_OK;
 }
@@ -266,9 +284,11 @@ int sfx_jvp_f32(sfx_form form, const float* du, float* dr, void* stream) {
   if (!form->linearized) return fail(SFX_ERR_INVALID, "sfx_linearize must be called before sfx_jvp_f32");
   auto s = static_cast<cudaStream_t>(stream);
   for (size_t i = 0; i < form->domain.size(); i++) {
-    if (int rc = launch_domain_jvp_f32(*form, form->domain[i], form->u_lin32.p, du, form->e32.p, form->t_lin, s))
-      return rc;
-    if (int rc = scatter_dispatch<float>(*form, form->e32.p, dr, i > 0, s)) return rc;
+    int rc = form->jvp_mode == SFX_JVP_STORED_TANGENT
+                 ? launch_jvp_stored_f32(*form, form->domain[i], du, form->e32.p, s)
+                 : launch_domain_jvp_f32(*form, form->domain[i], form->u_lin32.p, du, form->e32.p, form->t_lin, s);
+    if (rc) return rc;
+    if (int rc2 = scatter_dispatch<float>(*form, form->e32.p, dr, i > 0, s)) return rc2;
   }
   return SFX_OK;
 }
@@ -278,8 +298,9 @@ int sfx_jvp_element(sfx_form form, const double* du, double* dE, void* stream) {
   if (!du || !dE) return fail(SFX_ERR_INVALID, "null vector");
   if (!form->linearized) return fail(SFX_ERR_INVALID, "sfx_linearize must be called before sfx_jvp_element");
   if (form->domain.empty()) return fail(SFX_ERR_INVALID, "no domain integral");
-  return launch_domain(*form, form->domain[0], sfx::kernels::JVP, form->u_lin64.p, du, dE, form->t_lin,
-                       static_cast<cudaStream_t>(stream));
+  auto s = static_cast<cudaStream_t>(stream);
+  if (form->jvp_mode == SFX_JVP_STORED_TANGENT) return launch_jvp_stored(*form, form->domain[0], du, dE, s);
+  return launch_domain(*form, form->domain[0], sfx::kernels::JVP, form->u_lin64.p, du, dE, form->t_lin, s);
 }
 
 int sfx_update_qdata(sfx_form form, int flag) {

@@ -19,6 +19,11 @@ int launch_element_matrix(const sfx_form_s& f, const DomainIntegral& di, bool di
 // scatter-add of an E-vector [e][c][node] into an L-vector
 int scatter_evector(const sfx_form_s& f, const double* E, double* out, bool accumulate, cudaStream_t s);
 
+// stored-tangent path: linearise (store D, optionally element residuals) and apply D
+int launch_linearize(const sfx_form_s& f, DomainIntegral& di, double* res_e, cudaStream_t s);
+int launch_jvp_stored(const sfx_form_s& f, const DomainIntegral& di, const double* du, double* E, cudaStream_t s);
+int launch_jvp_stored_f32(const sfx_form_s& f, const DomainIntegral& di, const float* du, float* E, cudaStream_t s);
+
 int launch_domain_jvp_f32(const sfx_form_s& f, const DomainIntegral& di, const float* u, const float* du, float* E,
                           double t, cudaStream_t s);
 

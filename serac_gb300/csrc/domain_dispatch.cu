@@ -15,6 +15,7 @@ using J2 = solid_mechanics::J2SmallStrain<solid_mechanics::LinearHardening>;
 
 struct HeatMaker {
   static constexpr int nparams = 2;
+  static constexpr bool value_input = false;
   SFX_HD heat_transfer::HeatIntegrand operator()(const double* p) const {
     heat_transfer::HeatIntegrand q{};
     q.material.conductivity = p[0];
@@ -24,18 +25,21 @@ struct HeatMaker {
 };
 struct NonlinearHeatMaker {
   static constexpr int nparams = 3;
+  static constexpr bool value_input = true;
   SFX_HD heat_transfer::NonlinearHeatIntegrand operator()(const double* p) const {
     return heat_transfer::NonlinearHeatIntegrand{p[0], p[1], p[2]};
   }
 };
 struct NeoHookeanMaker {
   static constexpr int nparams = 2;
+  static constexpr bool value_input = false;
   SFX_HD solid_mechanics::MaterialStressFunctor<solid_mechanics::NeoHookean, true> operator()(const double* p) const {
     return {solid_mechanics::NeoHookean{1.0, p[0], p[1]}};
   }
 };
 struct J2Maker {
   static constexpr int nparams = 4;
+  static constexpr bool value_input = false;
   SFX_HD solid_mechanics::MaterialStressFunctor<J2, false> operator()(const double* p) const {
     J2 m{};
     m.E = p[0];
@@ -48,12 +52,28 @@ struct J2Maker {
 };
 struct ThermalTestMaker {
   static constexpr int nparams = 0;
+  static constexpr bool value_input = true;
   SFX_HD test_models::ThermalModel operator()(const double*) const { return {}; }
 };
 struct ElasticTestMaker {
   static constexpr int nparams = 0;
+  static constexpr bool value_input = true;
   SFX_HD test_models::ElasticModel operator()(const double*) const { return {}; }
 };
+
+// Calls fn.template operator()<C, State, Maker>() for the form's material.
+template <typename Fn>
+int visit_material(int material, Fn&& fn) {
+  switch (material) {
+    case SFX_MAT_HEAT: return fn.template operator()<1, Nothing, HeatMaker>();
+    case SFX_MAT_NONLINEAR_HEAT: return fn.template operator()<1, Nothing, NonlinearHeatMaker>();
+    case SFX_MAT_THERMAL_TEST: return fn.template operator()<1, Nothing, ThermalTestMaker>();
+    case SFX_MAT_ELASTIC_TEST: return fn.template operator()<3, Nothing, ElasticTestMaker>();
+    case SFX_MAT_NEOHOOKEAN: return fn.template operator()<3, Empty, NeoHookeanMaker>();
+    case SFX_MAT_J2: return fn.template operator()<3, J2::State, J2Maker>();
+  }
+  return fail(SFX_ERR_UNSUPPORTED, "unknown material");
+}
 
 template <int P, int C, int MODE, typename Real, typename State, typename Maker>
 int launch(const sfx_form_s& f, const DomainIntegral& di, const Real* u, const Real* du, Real* E, const Real* geom,
@@ -126,7 +146,83 @@ int dispatch_em(const sfx_form_s& f, const DomainIntegral& di, bool diag_only, d
   return fail(SFX_ERR_UNSUPPORTED, "unknown material");
 }
 
+template <int P>
+struct LinearizeFn {
+  const sfx_form_s& f;
+  DomainIntegral& di;
+  double* res_e;
+  cudaStream_t s;
+  template <int C, typename State, typename Maker>
+  int operator()() {
+    constexpr int NQ = (P + 1) * (P + 1) * (P + 1);
+    constexpr int EPW = 32 / NQ;
+    using QF = decltype(Maker{}(nullptr));
+    constexpr bool HS = kernels::tangent_has_source<C, State, QF>();
+    using Shape = kernels::TangentShape<C, HS, Maker::value_input>;
+    const size_t n = size_t(f.ne) * NQ * Shape::size;
+    if (di.D64.n != n) {
+      cudaError_t err = di.D64.alloc(n);
+      if (err == cudaSuccess) err = di.D32.alloc(n);
+      if (err != cudaSuccess) return fail(SFX_ERR_NOMEM, std::string("tangent storage: ") + cudaGetErrorString(err));
+    }
+    di.tangent_rows = Shape::rows;
+    di.tangent_cols = Shape::cols;
+    if (f.ne == 0) return SFX_OK;
+    kernels::DomainArgs<double> a{f.u_lin64.p, nullptr, nullptr, f.conn.p, f.geom64.p, di.state.p, di.params.p,
+                                  f.nnodes, f.ne, f.t_lin};
+    int64_t warps = (f.ne + EPW - 1) / EPW;
+    int64_t blocks = (warps * 32 + 127) / 128;
+    kernels::linearize_kernel<P, C, State, Maker><<<unsigned(blocks), 128, 0, s>>>(a, Maker{}, di.D64.p, di.D32.p, res_e);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("linearize launch: ") + cudaGetErrorString(err));
+    return SFX_OK;
+  }
+};
+
+template <int P, typename Real>
+struct StoredJvpFn {
+  const sfx_form_s& f;
+  const DomainIntegral& di;
+  const Real* du;
+  const Real* D;
+  Real* E;
+  cudaStream_t s;
+  template <int C, typename State, typename Maker>
+  int operator()() {
+    constexpr int NQ = (P + 1) * (P + 1) * (P + 1);
+    constexpr int EPW = 32 / NQ;
+    using QF = decltype(Maker{}(nullptr));
+    constexpr bool HS = kernels::tangent_has_source<C, State, QF>();
+    if (f.ne == 0) return SFX_OK;
+    int64_t warps = (f.ne + EPW - 1) / EPW;
+    int64_t blocks = (warps * 32 + 127) / 128;
+    kernels::jvp_stored_kernel<P, C, HS, Maker::value_input, Real>
+        <<<unsigned(blocks), 128, 0, s>>>(du, D, f.conn.p, E, f.nnodes, f.ne);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("stored jvp launch: ") + cudaGetErrorString(err));
+    return SFX_OK;
+  }
+};
+
 }  // namespace
+
+int launch_linearize(const sfx_form_s& f, DomainIntegral& di, double* res_e, cudaStream_t s) {
+  if (f.p == 1) return visit_material(di.material, LinearizeFn<1>{f, di, res_e, s});
+  if (f.p == 2) return visit_material(di.material, LinearizeFn<2>{f, di, res_e, s});
+  return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
+}
+
+int launch_jvp_stored(const sfx_form_s& f, const DomainIntegral& di, const double* du, double* E, cudaStream_t s) {
+  if (f.p == 1) return visit_material(di.material, StoredJvpFn<1, double>{f, di, du, di.D64.p, E, s});
+  if (f.p == 2) return visit_material(di.material, StoredJvpFn<2, double>{f, di, du, di.D64.p, E, s});
+  return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
+}
+
+int launch_jvp_stored_f32(const sfx_form_s& f, const DomainIntegral& di, const float* du, float* E, cudaStream_t s) {
+  if (f.p == 1) return visit_material(di.material, StoredJvpFn<1, float>{f, di, du, di.D32.p, E, s});
+  if (f.p == 2) return visit_material(di.material, StoredJvpFn<2, float>{f, di, du, di.D32.p, E, s});
+  return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
+}
 
 int launch_element_matrix(const sfx_form_s& f, const DomainIntegral& di, bool diag_only, double* out, int64_t e0,
                           int64_t e1, cudaStream_t s) {

@@ -67,6 +67,10 @@ struct DomainIntegral {
   int state_doubles = 0;  // per quadrature point
   DeviceBuf<double> params;  // [e][nparams]
   DeviceBuf<double> state;   // SoA [k][e*nq+q]
+  // stored q-function derivative (stored-tangent Jacobian action)
+  DeviceBuf<double> D64;
+  DeviceBuf<float> D32;
+  int tangent_rows = 0, tangent_cols = 0;
 };
 
 struct BoundaryIntegral {
@@ -108,6 +112,7 @@ struct sfx_form_s {
   double t_lin = 0.0;
   bool linearized = false;
   bool update_qdata = false;
+  int jvp_mode = SFX_JVP_STORED_TANGENT;
   std::vector<sfx_impl::DomainIntegral> domain;
   std::vector<sfx_impl::BoundaryIntegral> boundary;
   // CSR graph (built on first request)

@@ -219,6 +219,14 @@ class Functional:
     add_boundary_integral = AddBoundaryIntegral
     AddSurfaceIntegral = AddBoundaryIntegral
 
+    STORED_TANGENT, RECOMPUTE = 0, 1
+
+    def set_jvp_mode(self, mode):
+        """STORED_TANGENT (default): the q-function derivative is stored at each
+        quadrature point by linearize(); RECOMPUTE: every Jacobian action
+        re-evaluates the q-function on dual numbers."""
+        _lib.call("sfx_form_set_jvp_mode", self._h, int(mode))
+
     def updateQdata(self, flag: bool):
         _lib.call("sfx_update_qdata", self._h, int(bool(flag)))
 

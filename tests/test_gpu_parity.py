@@ -43,9 +43,11 @@ def _pair(mat, p, dims=(4, 3, 2), perturb=0.1, per_element=False, seed=0):
     return orc, f
 
 
+@pytest.mark.parametrize("mode", [0, 1], ids=["stored", "recompute"])
 @pytest.mark.parametrize("mat,p", CASES)
-def test_residual_and_jvp_fp64(cuda, mat, p):
+def test_residual_and_jvp_fp64(cuda, mat, p, mode):
     orc, f = _pair(mat, p)
+    f.set_jvp_mode(mode)
     u, du = fields(orc.ndofs, mat, seed=3)
     ut = torch.tensor(u, device=cuda)
     dut = torch.tensor(du, device=cuda)
@@ -67,9 +69,11 @@ def sg_wrt(u):
     return sg.differentiate_wrt(u)
 
 
+@pytest.mark.parametrize("mode", [0, 1], ids=["stored", "recompute"])
 @pytest.mark.parametrize("mat", [O.MAT_HEAT, O.MAT_NEOHOOKEAN, O.MAT_J2])
-def test_per_element_parameters(cuda, mat):
+def test_per_element_parameters(cuda, mat, mode):
     orc, f = _pair(mat, 2, dims=(3, 3, 3), per_element=True, seed=5)
+    f.set_jvp_mode(mode)
     u, du = fields(orc.ndofs, mat, seed=9)
     ut = torch.tensor(u, device=cuda)
     f.linearize(0.0, ut)
@@ -77,8 +81,10 @@ def test_per_element_parameters(cuda, mat):
     assert rel(f.gradient(torch.tensor(du, device=cuda)).cpu().numpy(), orc.jvp(u, du)) <= TOL64
 
 
-def test_bitwise_reproducible(cuda):
+@pytest.mark.parametrize("mode", [0, 1], ids=["stored", "recompute"])
+def test_bitwise_reproducible(cuda, mode):
     orc, f = _pair(O.MAT_NEOHOOKEAN, 2, dims=(6, 5, 4))
+    f.set_jvp_mode(mode)
     u, du = fields(orc.ndofs, O.MAT_NEOHOOKEAN, seed=11, scale=0.25)
     ut = torch.tensor(u, device=cuda)
     dut = torch.tensor(du, device=cuda)
@@ -93,8 +99,10 @@ def test_bitwise_reproducible(cuda):
     assert torch.equal(ra, rb)
 
 
-def test_j2_state_update_matches_oracle(cuda):
+@pytest.mark.parametrize("mode", [0, 1], ids=["stored", "recompute"])
+def test_j2_state_update_matches_oracle(cuda, mode):
     orc, f = _pair(O.MAT_J2, 1, dims=(3, 2, 2))
+    f.set_jvp_mode(mode)
     u, du = fields(orc.ndofs, O.MAT_J2, seed=13)
     ut = torch.tensor(u, device=cuda)
     # commit plastic state at u, then evaluate at 1.5 u with that state
