@@ -219,14 +219,18 @@ def run_sfx(args, rank, world):
             torch.distributed.barrier()
 
     for _ in range(args.warmup):
-        grad.mult(du, dr)
-        if not args.kernels_only:
+        if not (args.kernels_only and args.precision == "f32"):
+            grad.mult(du, dr)
+        if not args.kernels_only or args.precision == "f32":
             grad.mult(du32, dr32)
     torch.cuda.synchronize()
     if args.kernels_only:
-        # only the FP64 Jacobian actions (for profiler captures)
+        # only the Jacobian actions of one precision (for profiler captures)
         for _ in range(args.steps):
-            grad.mult(du, dr)
+            if args.precision == "f32":
+                grad.mult(du32, dr32)
+            else:
+                grad.mult(du, dr)
         torch.cuda.synchronize()
         if rank == 0:
             print(json.dumps({"kernels_only": True, "steps": args.steps, "finite": bool(torch.isfinite(dr).all())}))
@@ -304,7 +308,9 @@ def run_sfx(args, rank, world):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     prof = load_profile_numbers()
     traffic = prof.get("dram_bytes_per_launch")
-    flops_per_elem = prof.get("fp64_flops_per_element")
+    # algorithmic FP64 work of the stored-tangent action per element: per point,
+    # interpolate grad du (3 x 24 FMA), apply the 9x9 tangent (81), integrate (3 x 27)
+    flops_per_elem = 2 * (72 + 81 + 81) * (ORDER + 1) ** 3
     fp64_peak = measure_fp64_peak(dev)
     roofline = {
         "bound": "hbm",
@@ -323,7 +329,7 @@ def run_sfx(args, rank, world):
         ach = flops_per_elem * ne / t_k / 1e12
         compute = {"bound": "fp64", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach / fp64_peak,
                    "flops_per_element": flops_per_elem,
-                   "peak_source": "cuBLAS DGEMM 8192^3 measured in this run"}
+                   "peak_source": "cuBLAS DGEMM 4096^3 measured in this run"}
 
     result = {
         "metric": METRIC,
@@ -383,7 +389,7 @@ def measure_fp64_peak(dev):
 def load_profile_numbers():
     """Per-launch DRAM traffic and FP64 operation count of the element kernel,
     read from the committed ncu summary (profiles/), if present."""
-    path = os.path.join(ROOT, "profiles", "jvp_neohookean_q2.json")
+    path = os.path.join(ROOT, "profiles", "jvp_stored_f64_neohookean_q2_32cubed.json")
     try:
         return json.load(open(path))
     except (OSError, ValueError):
@@ -431,7 +437,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["sfx", "reference"], default="sfx")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--kernels-only", action="store_true", help="run only the FP64 Jacobian actions (profiling)")
+    ap.add_argument("--kernels-only", action="store_true", help="run only the Jacobian actions (profiling)")
+    ap.add_argument("--precision", choices=["f64", "f32"], default="f64", help="precision of --kernels-only")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
