@@ -243,8 +243,8 @@ __global__ void __launch_bounds__(128) domain_kernel(DomainArgs<Real> a, QFMaker
   __shared__ Real sB[Q][Q], sG[Q][Q];
   if (threadIdx.x < Q * Q) {
     int i = threadIdx.x / Q, j = threadIdx.x % Q;
-    sB[i][j] = Real(basis_B(P, i, j));
-    sG[i][j] = Real(basis_G(P, i, j));
+    sB[i][j] = Real(basis_table<P>().B[i][j]);
+    sG[i][j] = Real(basis_table<P>().G[i][j]);
   }
   __syncthreads();
 
@@ -464,8 +464,8 @@ __global__ void __launch_bounds__(128) element_matrix_kernel(DomainArgs<double> 
   __shared__ Real sB[Q][Q], sG[Q][Q];
   if (threadIdx.x < Q * Q) {
     int i = threadIdx.x / Q, j = threadIdx.x % Q;
-    sB[i][j] = basis_B(P, i, j);
-    sG[i][j] = basis_G(P, i, j);
+    sB[i][j] = basis_table<P>().B[i][j];
+    sG[i][j] = basis_table<P>().G[i][j];
   }
   __syncthreads();
 
@@ -762,8 +762,8 @@ __global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QF
   __shared__ Real sB[Q][Q], sG[Q][Q];
   if (threadIdx.x < Q * Q) {
     int i = threadIdx.x / Q, j = threadIdx.x % Q;
-    sB[i][j] = basis_B(P, i, j);
-    sG[i][j] = basis_G(P, i, j);
+    sB[i][j] = basis_table<P>().B[i][j];
+    sG[i][j] = basis_table<P>().G[i][j];
   }
   __syncthreads();
 
@@ -919,8 +919,8 @@ __global__ void __launch_bounds__(128) jvp_stored_kernel(const Real* __restrict_
   __shared__ Real sB[Q][Q], sG[Q][Q];
   if (threadIdx.x < Q * Q) {
     int i = threadIdx.x / Q, j = threadIdx.x % Q;
-    sB[i][j] = Real(basis_B(P, i, j));
-    sG[i][j] = Real(basis_G(P, i, j));
+    sB[i][j] = Real(basis_table<P>().B[i][j]);
+    sG[i][j] = Real(basis_table<P>().G[i][j]);
   }
   __syncthreads();
 

@@ -66,4 +66,39 @@ SFX_HDI constexpr double basis_G(int p, int q, int k) {
   return dphi;
 }
 
+/// B and G of the (p+1)-point rule, evaluated at compile time.
+template <int P>
+struct BasisTable {
+  double B[P + 1][P + 1];
+  double G[P + 1][P + 1];
+};
+
+template <int P>
+constexpr BasisTable<P> make_basis_table() {
+  BasisTable<P> t{};
+  for (int q = 0; q <= P; q++)
+    for (int k = 0; k <= P; k++) {
+      double phi = 0, dphi = 0;
+      gll_basis(P + 1, k, gl_point(P + 1, q), phi, dphi);
+      t.B[q][k] = phi;
+      t.G[q][k] = dphi;
+    }
+  return t;
+}
+
+#if defined(__CUDACC__)
+/// Device copies of the tables (constant memory, no runtime FP64 work).
+static __constant__ BasisTable<1> kBasis1 = make_basis_table<1>();
+static __constant__ BasisTable<2> kBasis2 = make_basis_table<2>();
+static __constant__ BasisTable<3> kBasis3 = make_basis_table<3>();
+template <int P>
+__device__ inline const BasisTable<P>& basis_table();
+template <>
+__device__ inline const BasisTable<1>& basis_table<1>() { return kBasis1; }
+template <>
+__device__ inline const BasisTable<2>& basis_table<2>() { return kBasis2; }
+template <>
+__device__ inline const BasisTable<3>& basis_table<3>() { return kBasis3; }
+#endif
+
 }  // namespace sfx

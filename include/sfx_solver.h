@@ -1,0 +1,82 @@
+/*
+ * sfx — device-resident Newton-Krylov solver over an sfx form (C ABI).
+ *
+ * Replaces serac's solver stack for the quasi-static physics solve
+ * (src/serac/numerics/equation_solver.cpp and solver_config.hpp):
+ *   sfx_solver_default_options  solver_config.hpp:342-400 LinearSolverOptions / NonlinearSolverOptions
+ *   sfx_solver_create           equation_solver.cpp:820-950 buildNonlinearSolver / buildLinearSolverAndPreconditioner
+ *   sfx_solver_set_essential    physics/boundary_conditions/boundary_condition_manager.hpp:91 (essential dofs)
+ *   sfx_solver_solve            equation_solver.cpp:79-200 NewtonSolver::Mult (quasiStaticSolve, solid_mechanics.hpp:1620-1630)
+ *   sfx_solver_solve_linear     one linearised solve (warmStartDisplacement, solid_mechanics.hpp:1727-1770)
+ * The Chebyshev, flexible-GMRES and mixed-precision options have no
+ * counterpart in serac (its LinearSolver enum is CG / GMRES / direct / PETSc).
+ */
+#ifndef SFX_SOLVER_H
+#define SFX_SOLVER_H
+
+#include <stdint.h>
+
+#include "sfx.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SFX_ERR_NOT_CONVERGED (-7)
+
+#define SFX_KRYLOV_GMRES 0  /* restarted GMRES(restart), right preconditioned */
+#define SFX_KRYLOV_CG 1     /* conjugate gradients (symmetric positive definite) */
+#define SFX_KRYLOV_FGMRES 2 /* flexible GMRES (preconditioner may vary per step) */
+
+#define SFX_PREC_NONE 0
+#define SFX_PREC_JACOBI 1
+#define SFX_PREC_JACOBI_CHEBYSHEV 2
+
+typedef struct {
+  int max_newton_iterations; /* 20 */
+  double newton_rel_tol;     /* 1e-8: ||r|| <= rel ||r0|| */
+  double newton_abs_tol;     /* 1e-12 */
+  int krylov;                /* SFX_KRYLOV_* (GMRES) */
+  int restart;               /* 50 */
+  int max_krylov_iterations; /* 300 per linear solve */
+  double krylov_rel_tol;     /* 1e-8 */
+  double krylov_abs_tol;     /* 1e-12 */
+  int precond;               /* SFX_PREC_* (Jacobi-Chebyshev) */
+  int chebyshev_degree;      /* 3: Chebyshev polynomial degree (degree-1 Jacobian actions) */
+  double chebyshev_ratio;    /* 30: interval [lmax / ratio, 1.1 lmax] of D^-1 J */
+  int power_iterations;      /* 10: lmax estimate per linearisation */
+  int mixed_precision;       /* 1: FP64 flexible GMRES outside, FP32 GMRES + FP32 Jacobi-Chebyshev inside */
+  int inner_iterations;      /* 20: FP32 inner GMRES steps per outer step */
+  double inner_rel_tol;      /* 1e-3 */
+  int print_level;           /* 0 */
+} sfx_solver_options;
+
+typedef struct {
+  int newton_iterations;
+  int krylov_iterations; /* outer (FP64) Krylov steps over the whole solve */
+  int inner_iterations;  /* inner FP32 Krylov steps (mixed precision) */
+  int converged;
+  double initial_residual;
+  double final_residual;
+  double last_krylov_rel;
+} sfx_solver_stats;
+
+typedef struct sfx_solver_s* sfx_solver;
+
+int sfx_solver_default_options(sfx_solver_options* opt);
+int sfx_solver_create(sfx_form form, const sfx_solver_options* opt, sfx_solver* out);
+int sfx_solver_destroy(sfx_solver solver);
+/* Essential (Dirichlet) vdofs, host array; their values are taken from u. */
+int sfx_solver_set_essential(sfx_solver solver, const int64_t* dofs, int64_t n);
+/* Newton solve of R(t, u) = 0 in place (u: device, num_dofs doubles). */
+int sfx_solver_solve(sfx_solver solver, double t, double* u, void* stream);
+/* x = J(t, u_lin)^-1 rhs with the essential rows/columns eliminated. */
+int sfx_solver_solve_linear(sfx_solver solver, double t, const double* u_lin, const double* rhs, double* x,
+                            void* stream);
+int sfx_solver_get_stats(sfx_solver solver, sfx_solver_stats* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SFX_SOLVER_H */

@@ -476,3 +476,24 @@ def fgmres(apply_A, b, precond, rtol=1e-8, restart=50, maxiter=2000, atol=0.0):
         x = x + y @ Zs[: k + 1]
     r = b - apply_A(x)
     return x, total, np.linalg.norm(r) / nb
+
+
+def newton(f, u0, ess, rel_tol=1e-12, abs_tol=1e-14, max_iter=30, t=0.0):
+    """Plain Newton with direct linear solves of the Dirichlet-eliminated
+    Jacobian (equation_solver.cpp:79-200 without line search).  Returns
+    (u, iterations, final ||r||)."""
+    import scipy.sparse.linalg as spla
+
+    u = np.array(u0, dtype=np.float64, copy=True)
+    r = f.residual(u, t=t)
+    r[ess] = 0.0
+    r0 = np.linalg.norm(r)
+    it = 0
+    for it in range(max_iter):
+        if np.linalg.norm(r) <= max(rel_tol * r0, abs_tol):
+            break
+        A = eliminate_dirichlet(f.assemble(u, t=t), ess)
+        u -= spla.spsolve(A.tocsc(), r)
+        r = f.residual(u, t=t)
+        r[ess] = 0.0
+    return u, it, np.linalg.norm(r)

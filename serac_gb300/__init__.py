@@ -19,3 +19,4 @@ from .functional import (  # noqa: F401
     box_vertices,
     differentiate_wrt,
 )
+from .solver import CG, FGMRES, GMRES, JACOBI, JACOBI_CHEBYSHEV, NewtonSolver, SolverOptions  # noqa: F401,E402

@@ -53,6 +53,14 @@ SIGNATURES = {
     "sfx_qdata_size": (_c.c_int, [_vp, _i64p]),
     "sfx_set_qdata": (_c.c_int, [_vp, _dp]),
     "sfx_get_qdata": (_c.c_int, [_vp, _dp]),
+    # include/sfx_solver.h (struct arguments passed by address)
+    "sfx_solver_default_options": (_c.c_int, [_vp]),
+    "sfx_solver_create": (_c.c_int, [_vp, _vp, _c.POINTER(_vp)]),
+    "sfx_solver_destroy": (_c.c_int, [_vp]),
+    "sfx_solver_set_essential": (_c.c_int, [_vp, _i64p, _c.c_int64]),
+    "sfx_solver_solve": (_c.c_int, [_vp, _c.c_double, _vp, _vp]),
+    "sfx_solver_solve_linear": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp, _vp]),
+    "sfx_solver_get_stats": (_c.c_int, [_vp, _vp]),
 }
 
 _LIB = None

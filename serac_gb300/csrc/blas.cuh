@@ -1,0 +1,146 @@
+// Deterministic vector kernels for the Krylov solvers: every reduction is a
+// fixed-shape two-pass tree (per-block partial sums in a fixed order, then one
+// block reducing the partials in a fixed order), so results are bit-identical
+// from run to run.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace sfx_blas {
+
+constexpr int kBlock = 256;
+constexpr int kMaxPartials = 1024;  // blocks of the first pass
+
+template <typename T>
+__device__ inline T block_reduce(T v, T* sh) {
+  const int t = threadIdx.x;
+  sh[t] = v;
+  __syncthreads();
+  for (int s = kBlock / 2; s > 0; s >>= 1) {
+    if (t < s) sh[t] += sh[t + s];
+    __syncthreads();
+  }
+  T r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+// partial[j * gridDim.x + b] = sum over the block's fixed chunk of x_j . y
+// for j in [0, m); x_j = X + j * ldx.  Accumulates in Acc.
+template <typename T, typename Acc>
+__global__ void __launch_bounds__(kBlock) multi_dot_partial(const T* __restrict__ X, int64_t ldx, int m,
+                                                            const T* __restrict__ y, int64_t n,
+                                                            Acc* __restrict__ partial) {
+  __shared__ Acc sh[kBlock];
+  const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  const int64_t b0 = int64_t(blockIdx.x) * chunk;
+  const int64_t b1 = b0 + chunk < n ? b0 + chunk : n;
+  for (int j = 0; j < m; j++) {
+    const T* x = X + j * ldx;
+    Acc acc = 0;
+    for (int64_t i = b0 + threadIdx.x; i < b1; i += kBlock) acc += Acc(x[i]) * Acc(y[i]);
+    Acc s = block_reduce(acc, sh);
+    if (threadIdx.x == 0) partial[int64_t(j) * gridDim.x + blockIdx.x] = s;
+  }
+}
+
+template <typename Acc>
+__global__ void __launch_bounds__(kBlock) reduce_partials(const Acc* __restrict__ partial, int nb, int m,
+                                                          Acc* __restrict__ out) {
+  __shared__ Acc sh[kBlock];
+  for (int j = 0; j < m; j++) {
+    Acc acc = 0;
+    for (int i = threadIdx.x; i < nb; i += kBlock) acc += partial[int64_t(j) * nb + i];
+    Acc s = block_reduce(acc, sh);
+    if (threadIdx.x == 0) out[j] = s;
+  }
+}
+
+// y = a x + b y
+template <typename T>
+__global__ void axpby(int64_t n, T a, const T* __restrict__ x, T b, T* __restrict__ y) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = a * x[i] + b * y[i];
+}
+
+// w -= sum_j h[j] V_j   (h on the device)
+template <typename T>
+__global__ void multi_axpy_sub(int64_t n, int m, const T* __restrict__ V, int64_t ldv, const T* __restrict__ h,
+                               T* __restrict__ w) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T acc = w[i];
+  for (int j = 0; j < m; j++) acc -= h[j] * V[j * ldv + i];
+  w[i] = acc;
+}
+
+// x += sum_j y[j] Z_j  (y on the device)
+template <typename T>
+__global__ void multi_axpy_add(int64_t n, int m, const T* __restrict__ Z, int64_t ldz, const T* __restrict__ y,
+                               T* __restrict__ x) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T acc = x[i];
+  for (int j = 0; j < m; j++) acc += y[j] * Z[j * ldz + i];
+  x[i] = acc;
+}
+
+template <typename T>
+__global__ void scale(int64_t n, T a, T* __restrict__ x) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) x[i] *= a;
+}
+
+// z = x / d (elementwise)
+template <typename T>
+__global__ void diag_solve(int64_t n, const T* __restrict__ x, const T* __restrict__ d, T* __restrict__ z) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) z[i] = x[i] / d[i];
+}
+
+// d = a d + b (r / D)
+template <typename T>
+__global__ void cheb_update(int64_t n, T a, T b, const T* __restrict__ r, const T* __restrict__ D, T* __restrict__ d,
+                            T* __restrict__ z) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T v = a * d[i] + b * (r[i] / D[i]);
+  d[i] = v;
+  z[i] += v;
+}
+
+template <typename S, typename T>
+__global__ void convert(int64_t n, const S* __restrict__ x, T* __restrict__ y) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = T(x[i]);
+}
+
+// x[idx[k]] = v[k] or value
+template <typename T>
+__global__ void set_entries(int64_t m, const int64_t* __restrict__ idx, T value, T* __restrict__ x) {
+  int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < m) x[idx[k]] = value;
+}
+template <typename T>
+__global__ void copy_entries(int64_t m, const int64_t* __restrict__ idx, const T* __restrict__ src, T* __restrict__ x) {
+  int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < m) x[idx[k]] = src[idx[k]];
+}
+
+// r = b - r (in place on r)
+template <typename T>
+__global__ void rsub(int64_t n, const T* __restrict__ b, T* __restrict__ r) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) r[i] = b[i] - r[i];
+}
+
+// nonzero count of non-finite entries (flag)
+template <typename T>
+__global__ void nonfinite_flag(int64_t n, const T* __restrict__ x, int* __restrict__ flag) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n && !isfinite(double(x[i]))) *flag = 1;
+}
+
+}  // namespace sfx_blas

@@ -1,0 +1,510 @@
+// Device-resident Newton-Krylov solver over an sfx form.
+//
+// Newton (serac's NewtonSolver without line search, equation_solver.cpp:79-200):
+//   r = R(u), r[ess] = 0; until ||r|| <= max(rel ||r0||, abs):
+//     linearise at u (stored tangent), solve J du = r, u -= du
+// Krylov: right-preconditioned restarted GMRES(m) / flexible GMRES (Saad,
+// Iterative Methods, Alg. 6.9 / 9.5) with classical Gram-Schmidt applied
+// twice, or Jacobi-preconditioned CG (Alg. 6.18) for symmetric problems.
+// Preconditioners: Jacobi, Jacobi-Chebyshev (Chebyshev iteration on D^-1 J
+// over [lmax/ratio, 1.1 lmax], lmax from a power iteration), and, in the
+// mixed-precision mode, an inner FP32 GMRES(k) on the FP32 stored tangent with
+// FP32 Jacobi-Chebyshev inside FP64 flexible GMRES.
+// Dirichlet rows/columns: J[ess, :] = J[:, ess] = I on the essential set,
+// residual entries zeroed (solid_mechanics.hpp:1118-1139).
+// Vectors and reductions stay on the device; the host reads back only the
+// Gram-Schmidt coefficients of each Krylov step (deterministic tree sums).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <functional>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "blas.cuh"
+#include "form.hpp"
+#include "sfx.h"
+#include "sfx_solver.h"
+
+using namespace sfx_impl;
+
+namespace {
+
+inline unsigned nblocks(int64_t n, int b = 256) { return unsigned((n + b - 1) / b); }
+
+template <typename T>
+struct Vec {
+  DeviceBuf<T> buf;
+  T* p() const { return buf.p; }
+};
+
+template <typename T, typename Acc>
+struct Reducer {
+  DeviceBuf<Acc> partial;
+  DeviceBuf<Acc> out;
+  std::vector<Acc> host;
+  int nb = 0;
+  cudaError_t init(int64_t n, int max_m) {
+    nb = int(std::min<int64_t>(sfx_blas::kMaxPartials, std::max<int64_t>(1, (n + 4095) / 4096)));
+    cudaError_t e = partial.alloc(size_t(nb) * max_m);
+    if (e == cudaSuccess) e = out.alloc(size_t(max_m));
+    host.resize(size_t(max_m));
+    return e;
+  }
+  // host[j] = X_j . y for j < m (one synchronisation)
+  cudaError_t multi_dot(const T* X, int64_t ldx, int m, const T* y, int64_t n, cudaStream_t s) {
+    sfx_blas::multi_dot_partial<T, Acc><<<nb, sfx_blas::kBlock, 0, s>>>(X, ldx, m, y, n, partial.p);
+    sfx_blas::reduce_partials<Acc><<<1, sfx_blas::kBlock, 0, s>>>(partial.p, nb, m, out.p);
+    cudaError_t e = cudaMemcpyAsync(host.data(), out.p, sizeof(Acc) * m, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return e;
+  }
+  Acc dot(const T* x, const T* y, int64_t n, cudaStream_t s, cudaError_t* err) {
+    *err = multi_dot(x, 0, 1, y, n, s);
+    return host[0];
+  }
+};
+
+}  // namespace
+
+struct sfx_solver_s {
+  sfx_form form = nullptr;
+  sfx_solver_options opt{};
+  sfx_solver_stats stats{};
+  int64_t n = 0;
+  DeviceBuf<int64_t> ess;
+  int64_t n_ess = 0;
+  // FP64 work vectors
+  DeviceBuf<double> r, du, tmp, tmp2, diag, cheb_d, cheb_r, V, Z, y;
+  // FP32 work vectors
+  DeviceBuf<float> diag32, x32, b32, tmp32, tmp32b, cheb_d32, cheb_r32, V32, y32;
+  Reducer<double, double> red;
+  Reducer<float, float> red32;
+  double lmax = 0.0, lmax32 = 0.0;
+  std::function<int(int, const char*)> log;
+};
+
+namespace {
+
+// ---------------------------------------------------------------- operators
+int apply_J64(sfx_solver s, const double* x, double* y, cudaStream_t st) {
+  // y = J (x with essential entries zeroed); y[ess] = x[ess]
+  if (s->n_ess) {
+    SFX_CUDA_TRY(cudaMemcpyAsync(s->tmp2.p, x, sizeof(double) * s->n, cudaMemcpyDeviceToDevice, st));
+    sfx_blas::set_entries<double><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, 0.0, s->tmp2.p);
+    if (int rc = sfx_jvp(s->form, s->tmp2.p, y, st)) return rc;
+    sfx_blas::copy_entries<double><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, x, y);
+  } else {
+    if (int rc = sfx_jvp(s->form, x, y, st)) return rc;
+  }
+  return SFX_OK;
+}
+
+int apply_J32(sfx_solver s, const float* x, float* y, cudaStream_t st) {
+  if (s->n_ess) {
+    SFX_CUDA_TRY(cudaMemcpyAsync(s->tmp32b.p, x, sizeof(float) * s->n, cudaMemcpyDeviceToDevice, st));
+    sfx_blas::set_entries<float><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, 0.0f, s->tmp32b.p);
+    if (int rc = sfx_jvp_f32(s->form, s->tmp32b.p, y, st)) return rc;
+    sfx_blas::copy_entries<float><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, x, y);
+  } else {
+    if (int rc = sfx_jvp_f32(s->form, x, y, st)) return rc;
+  }
+  return SFX_OK;
+}
+
+// power iteration for the largest eigenvalue of D^-1 J
+template <typename T, typename Acc>
+int estimate_lmax(sfx_solver s, int (*apply)(sfx_solver, const T*, T*, cudaStream_t), const T* D, T* x, T* y,
+                  Reducer<T, Acc>& red, double* lmax, cudaStream_t st) {
+  const int64_t n = s->n;
+  // deterministic start vector: all ones
+  {
+    std::vector<T> ones(size_t(n), T(1));
+    SFX_CUDA_TRY(cudaMemcpyAsync(x, ones.data(), sizeof(T) * n, cudaMemcpyHostToDevice, st));
+    SFX_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  cudaError_t err;
+  double lam = 0.0;
+  for (int it = 0; it < s->opt.power_iterations; it++) {
+    double nx = std::sqrt(double(red.dot(x, x, n, st, &err)));
+    SFX_CUDA_TRY(err);
+    sfx_blas::scale<T><<<nblocks(n), 256, 0, st>>>(n, T(1.0 / nx), x);
+    if (int rc = apply(s, x, y, st)) return rc;
+    sfx_blas::diag_solve<T><<<nblocks(n), 256, 0, st>>>(n, y, D, y);
+    lam = double(red.dot(x, y, n, st, &err));
+    SFX_CUDA_TRY(err);
+    std::swap(x, y);
+  }
+  *lmax = lam;
+  return SFX_OK;
+}
+
+// z = Chebyshev(D^-1 J) approximation of J^-1 b, degree k, starting from 0
+template <typename T, typename Acc>
+int chebyshev(sfx_solver s, int (*apply)(sfx_solver, const T*, T*, cudaStream_t), const T* D, double lmax,
+              const T* b, T* z, T* d, T* res, cudaStream_t st) {
+  const int64_t n = s->n;
+  const double hi = 1.1 * lmax, lo = lmax / s->opt.chebyshev_ratio;
+  const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo);
+  const double sigma = theta / delta;
+  double rho = 1.0 / sigma;
+  // d = D^-1 b / theta ; z = d
+  sfx_blas::diag_solve<T><<<nblocks(n), 256, 0, st>>>(n, b, D, d);
+  sfx_blas::scale<T><<<nblocks(n), 256, 0, st>>>(n, T(1.0 / theta), d);
+  SFX_CUDA_TRY(cudaMemcpyAsync(z, d, sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
+  for (int k = 1; k < s->opt.chebyshev_degree; k++) {
+    if (int rc = apply(s, z, res, st)) return rc;
+    sfx_blas::rsub<T><<<nblocks(n), 256, 0, st>>>(n, b, res);  // res = b - J z
+    double rho_new = 1.0 / (2.0 * sigma - rho);
+    sfx_blas::cheb_update<T><<<nblocks(n), 256, 0, st>>>(n, T(rho_new * rho), T(2.0 * rho_new / delta), res, D, d, z);
+    rho = rho_new;
+  }
+  SFX_CUDA_TRY(cudaGetLastError());
+  return SFX_OK;
+}
+
+// Restarted right-preconditioned (flexible) GMRES on vectors of type T with
+// accumulation type Acc.  x holds the initial guess and the result.
+template <typename T, typename Acc>
+int gmres(sfx_solver s, int (*apply)(sfx_solver, const T*, T*, cudaStream_t),
+          const std::function<int(const T*, T*)>& precond, bool flexible, const T* b, T* x, T* V, T* Zs,
+          T* w, T* ydev, Reducer<T, Acc>& red, int restart, int max_iters, double rel_tol, double abs_tol,
+          int* iters_out, double* rel_out, cudaStream_t st) {
+  const int64_t n = s->n;
+  cudaError_t err;
+  const double nb = std::sqrt(double(red.dot(b, b, n, st, &err)));
+  SFX_CUDA_TRY(err);
+  *iters_out = 0;
+  if (nb == 0.0) {
+    SFX_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(T) * n, st));
+    *rel_out = 0.0;
+    return SFX_OK;
+  }
+  const double target = std::max(rel_tol * nb, abs_tol);
+  int total = 0;
+  const size_t mr = static_cast<size_t>(restart);
+  std::vector<double> H((mr + 1) * mr), cs(mr), sn(mr), g(mr + 1), yv(mr);
+  std::vector<T> yh(mr + 1);
+  double beta = 0.0;
+  while (true) {
+    // r = b - A x into V_0
+    if (int rc = apply(s, x, V, st)) return rc;
+    sfx_blas::rsub<T><<<nblocks(n), 256, 0, st>>>(n, b, V);
+    beta = std::sqrt(double(red.dot(V, V, n, st, &err)));
+    SFX_CUDA_TRY(err);
+    if (!std::isfinite(beta)) return fail(SFX_ERR_NONFINITE, "non-finite residual in GMRES");
+    if (beta <= target || total >= max_iters) break;
+    sfx_blas::scale<T><<<nblocks(n), 256, 0, st>>>(n, T(1.0 / beta), V);
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int k = 0;
+    bool done = false;
+    for (k = 0; k < restart && total < max_iters; k++) {
+      T* vk = V + int64_t(k) * n;
+      T* zk = flexible ? Zs + int64_t(k) * n : w;
+      if (int rc = precond(vk, zk)) return rc;
+      T* vnext = V + int64_t(k + 1) * n;
+      if (int rc = apply(s, zk, vnext, st)) return rc;
+      // classical Gram-Schmidt, twice
+      double* Hk = &H[size_t(k) * (restart + 1)];
+      for (int j = 0; j <= k; j++) Hk[j] = 0.0;
+      for (int pass = 0; pass < 2; pass++) {
+        SFX_CUDA_TRY(red.multi_dot(V, n, k + 1, vnext, n, st));
+        for (int j = 0; j <= k; j++) {
+          Hk[j] += double(red.host[size_t(j)]);
+          yh[size_t(j)] = T(red.host[size_t(j)]);
+        }
+        SFX_CUDA_TRY(cudaMemcpyAsync(ydev, yh.data(), sizeof(T) * (k + 1), cudaMemcpyHostToDevice, st));
+        sfx_blas::multi_axpy_sub<T><<<nblocks(n), 256, 0, st>>>(n, k + 1, V, n, ydev, vnext);
+      }
+      double hn = std::sqrt(double(red.dot(vnext, vnext, n, st, &err)));
+      SFX_CUDA_TRY(err);
+      Hk[k + 1] = hn;
+      if (hn > 0.0) sfx_blas::scale<T><<<nblocks(n), 256, 0, st>>>(n, T(1.0 / hn), vnext);
+      for (int j = 0; j < k; j++) {
+        double t = cs[size_t(j)] * Hk[j] + sn[size_t(j)] * Hk[j + 1];
+        Hk[j + 1] = -sn[size_t(j)] * Hk[j] + cs[size_t(j)] * Hk[j + 1];
+        Hk[j] = t;
+      }
+      double d = std::hypot(Hk[k], Hk[k + 1]);
+      if (d == 0.0) d = 1e-300;
+      cs[size_t(k)] = Hk[k] / d;
+      sn[size_t(k)] = Hk[k + 1] / d;
+      Hk[k] = d;
+      Hk[k + 1] = 0.0;
+      g[size_t(k + 1)] = -sn[size_t(k)] * g[size_t(k)];
+      g[size_t(k)] = cs[size_t(k)] * g[size_t(k)];
+      total++;
+      if (std::fabs(g[size_t(k + 1)]) <= target || hn == 0.0) {
+        k++;
+        done = true;
+        break;
+      }
+    }
+    if (!done) k = std::min(k, restart);
+    // back substitution H y = g
+    for (int i = k - 1; i >= 0; i--) {
+      double acc = g[size_t(i)];
+      for (int j = i + 1; j < k; j++) acc -= H[size_t(j) * (restart + 1) + i] * yv[size_t(j)];
+      yv[size_t(i)] = acc / H[size_t(i) * (restart + 1) + i];
+    }
+    for (int i = 0; i < k; i++) yh[size_t(i)] = T(yv[size_t(i)]);
+    SFX_CUDA_TRY(cudaMemcpyAsync(ydev, yh.data(), sizeof(T) * k, cudaMemcpyHostToDevice, st));
+    if (flexible) {
+      sfx_blas::multi_axpy_add<T><<<nblocks(n), 256, 0, st>>>(n, k, Zs, n, ydev, x);
+    } else {
+      // x += M (V y): form V y in w, precondition into V_k slot (free), add
+      SFX_CUDA_TRY(cudaMemsetAsync(w, 0, sizeof(T) * n, st));
+      sfx_blas::multi_axpy_add<T><<<nblocks(n), 256, 0, st>>>(n, k, V, n, ydev, w);
+      T* zz = V + int64_t(k) * n;
+      if (int rc = precond(w, zz)) return rc;
+      sfx_blas::axpby<T><<<nblocks(n), 256, 0, st>>>(n, T(1), zz, T(1), x);
+    }
+    SFX_CUDA_TRY(cudaGetLastError());
+    if (done && total >= max_iters) {
+      // fall through to the true-residual check
+    }
+  }
+  *iters_out = total;
+  *rel_out = beta / nb;
+  return SFX_OK;
+}
+
+// Jacobi-preconditioned CG (symmetric positive definite J)
+int cg(sfx_solver s, const double* b, double* x, int* iters_out, double* rel_out, cudaStream_t st) {
+  const int64_t n = s->n;
+  cudaError_t err;
+  double* r = s->V.p;
+  double* z = s->V.p + n;
+  double* p = s->V.p + 2 * n;
+  double* q = s->V.p + 3 * n;
+  SFX_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
+  SFX_CUDA_TRY(cudaMemcpyAsync(r, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  const double nb = std::sqrt(s->red.dot(b, b, n, st, &err));
+  SFX_CUDA_TRY(err);
+  *iters_out = 0;
+  *rel_out = 0.0;
+  if (nb == 0.0) return SFX_OK;
+  const double target = std::max(s->opt.krylov_rel_tol * nb, s->opt.krylov_abs_tol);
+  sfx_blas::diag_solve<double><<<nblocks(n), 256, 0, st>>>(n, r, s->diag.p, z);
+  SFX_CUDA_TRY(cudaMemcpyAsync(p, z, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  double rz = s->red.dot(r, z, n, st, &err);
+  SFX_CUDA_TRY(err);
+  double rn = nb;
+  int it = 0;
+  for (it = 1; it <= s->opt.max_krylov_iterations; it++) {
+    if (int rc = apply_J64(s, p, q, st)) return rc;
+    double pq = s->red.dot(p, q, n, st, &err);
+    SFX_CUDA_TRY(err);
+    if (!(pq > 0.0)) return fail(SFX_ERR_NONFINITE, "CG breakdown (operator not positive definite)");
+    double alpha = rz / pq;
+    sfx_blas::axpby<double><<<nblocks(n), 256, 0, st>>>(n, alpha, p, 1.0, x);
+    sfx_blas::axpby<double><<<nblocks(n), 256, 0, st>>>(n, -alpha, q, 1.0, r);
+    rn = std::sqrt(s->red.dot(r, r, n, st, &err));
+    SFX_CUDA_TRY(err);
+    if (rn <= target) break;
+    sfx_blas::diag_solve<double><<<nblocks(n), 256, 0, st>>>(n, r, s->diag.p, z);
+    double rz_new = s->red.dot(r, z, n, st, &err);
+    SFX_CUDA_TRY(err);
+    sfx_blas::axpby<double><<<nblocks(n), 256, 0, st>>>(n, 1.0, z, rz_new / rz, p);
+    rz = rz_new;
+  }
+  *iters_out = std::min(it, s->opt.max_krylov_iterations);
+  *rel_out = rn / nb;
+  return SFX_OK;
+}
+
+int ensure(DeviceBuf<double>& b, size_t n) { return b.n >= n ? SFX_OK : (b.alloc(n) == cudaSuccess ? SFX_OK : SFX_ERR_NOMEM); }
+int ensure(DeviceBuf<float>& b, size_t n) { return b.n >= n ? SFX_OK : (b.alloc(n) == cudaSuccess ? SFX_OK : SFX_ERR_NOMEM); }
+
+// one linear solve J du = r at the current linearisation
+int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
+  const int64_t n = s->n;
+  const auto& o = s->opt;
+  int iters = 0;
+  double rel = 0.0;
+  // Jacobi diagonal with unit entries on the essential set
+  if (int rc = sfx_assemble_diagonal(s->form, s->diag.p, st)) return rc;
+  if (s->n_ess) sfx_blas::set_entries<double><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, 1.0, s->diag.p);
+  if (o.krylov == SFX_KRYLOV_CG) {
+    int rc = cg(s, rhs, x, &iters, &rel, st);
+    s->stats.krylov_iterations += iters;
+    s->stats.last_krylov_rel = rel;
+    return rc;
+  }
+  const int m = o.restart;
+  if (ensure(s->V, size_t(m + 1) * n) || ensure(s->Z, size_t(m) * n))
+    return fail(SFX_ERR_NOMEM, "Krylov basis allocation failed");
+  std::function<int(const double*, double*)> prec;
+  if (o.precond == SFX_PREC_NONE) {
+    prec = [=](const double* v, double* z) -> int {
+      SFX_CUDA_TRY(cudaMemcpyAsync(z, v, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+      return SFX_OK;
+    };
+  } else if (o.precond == SFX_PREC_JACOBI) {
+    prec = [=](const double* v, double* z) -> int {
+      sfx_blas::diag_solve<double><<<nblocks(n), 256, 0, st>>>(n, v, s->diag.p, z);
+      return SFX_OK;
+    };
+  } else if (o.mixed_precision) {
+    // inner FP32 GMRES(k) with FP32 Jacobi-Chebyshev on the FP32 stored tangent
+    const int k = o.inner_iterations;
+    if (ensure(s->V32, size_t(k + 1) * n) || ensure(s->x32, n) || ensure(s->b32, n) || ensure(s->tmp32, n) ||
+        ensure(s->diag32, n) || ensure(s->cheb_d32, n) || ensure(s->cheb_r32, n) || ensure(s->y32, size_t(k + 1)) ||
+        ensure(s->tmp32b, n))
+      return fail(SFX_ERR_NOMEM, "FP32 workspace allocation failed");
+    sfx_blas::convert<double, float><<<nblocks(n), 256, 0, st>>>(n, s->diag.p, s->diag32.p);
+    if (int rc = estimate_lmax<float, float>(s, apply_J32, s->diag32.p, s->tmp32.p, s->cheb_r32.p, s->red32,
+                                             &s->lmax32, st))
+      return rc;
+    prec = [=](const double* v, double* z) -> int {
+      sfx_blas::convert<double, float><<<nblocks(n), 256, 0, st>>>(n, v, s->b32.p);
+      SFX_CUDA_TRY(cudaMemsetAsync(s->x32.p, 0, sizeof(float) * n, st));
+      std::function<int(const float*, float*)> inner_prec = [=](const float* a, float* b) -> int {
+        return chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, a, b, s->cheb_d32.p, s->cheb_r32.p, st);
+      };
+      int it = 0;
+      double rel_in = 0.0;
+      if (int rc = gmres<float, float>(s, apply_J32, inner_prec, false, s->b32.p, s->x32.p, s->V32.p, nullptr,
+                                       s->tmp32.p, s->y32.p, s->red32, k, k, o.inner_rel_tol, 0.0, &it, &rel_in, st))
+        return rc;
+      s->stats.inner_iterations += it;
+      sfx_blas::convert<float, double><<<nblocks(n), 256, 0, st>>>(n, s->x32.p, z);
+      return SFX_OK;
+    };
+  } else {
+    if (ensure(s->cheb_d, n) || ensure(s->cheb_r, n)) return fail(SFX_ERR_NOMEM, "workspace allocation failed");
+    if (int rc = estimate_lmax<double, double>(s, apply_J64, s->diag.p, s->tmp.p, s->cheb_r.p, s->red, &s->lmax, st))
+      return rc;
+    prec = [=](const double* v, double* z) -> int {
+      return chebyshev<double, double>(s, apply_J64, s->diag.p, s->lmax, v, z, s->cheb_d.p, s->cheb_r.p, st);
+    };
+  }
+  SFX_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
+  const bool flexible = o.mixed_precision != 0 || o.krylov == SFX_KRYLOV_FGMRES;
+  int rc = gmres<double, double>(s, apply_J64, prec, flexible, rhs, x, s->V.p, s->Z.p, s->tmp.p, s->y.p, s->red, m,
+                                 o.max_krylov_iterations, o.krylov_rel_tol, o.krylov_abs_tol, &iters, &rel, st);
+  s->stats.krylov_iterations += iters;
+  s->stats.last_krylov_rel = rel;
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sfx_solver_default_options(sfx_solver_options* o) {
+  if (!o) return fail(SFX_ERR_INVALID, "null options");
+  *o = sfx_solver_options{};
+  o->max_newton_iterations = 20;
+  o->newton_rel_tol = 1e-8;
+  o->newton_abs_tol = 1e-12;
+  o->krylov = SFX_KRYLOV_GMRES;
+  o->restart = 50;
+  o->max_krylov_iterations = 300;
+  o->krylov_rel_tol = 1e-8;
+  o->krylov_abs_tol = 1e-12;
+  o->precond = SFX_PREC_JACOBI_CHEBYSHEV;
+  o->chebyshev_degree = 3;
+  o->chebyshev_ratio = 30.0;
+  o->power_iterations = 10;
+  o->mixed_precision = 0;
+  o->inner_iterations = 20;
+  o->inner_rel_tol = 1e-3;
+  o->print_level = 0;
+  return SFX_OK;
+}
+
+int sfx_solver_create(sfx_form form, const sfx_solver_options* opt, sfx_solver* out) {
+  if (!form || !out) return fail(SFX_ERR_INVALID, "null argument");
+  *out = nullptr;
+  auto* s = new (std::nothrow) sfx_solver_s;
+  if (!s) return fail(SFX_ERR_NOMEM, "host allocation failed");
+  s->form = form;
+  if (opt) s->opt = *opt;
+  else sfx_solver_default_options(&s->opt);
+  if (s->opt.restart < 1 || s->opt.chebyshev_degree < 1 || s->opt.inner_iterations < 1) {
+    delete s;
+    return fail(SFX_ERR_INVALID, "bad solver options");
+  }
+  sfx_form_num_dofs(form, &s->n);
+  const size_t n = size_t(s->n);
+  if (s->r.alloc(n) || s->du.alloc(n) || s->tmp.alloc(n) || s->tmp2.alloc(n) || s->diag.alloc(n) ||
+      s->y.alloc(size_t(s->opt.restart + 1)) || s->V.alloc(4 * n) ||
+      s->red.init(s->n, std::max(s->opt.restart, s->opt.inner_iterations) + 1) != cudaSuccess ||
+      s->red32.init(s->n, s->opt.inner_iterations + 1) != cudaSuccess) {
+    delete s;
+    return fail(SFX_ERR_NOMEM, "solver workspace allocation failed");
+  }
+  *out = s;
+  return SFX_OK;
+}
+
+int sfx_solver_destroy(sfx_solver s) {
+  delete s;
+  return SFX_OK;
+}
+
+int sfx_solver_set_essential(sfx_solver s, const int64_t* dofs, int64_t n) {
+  if (!s || (n > 0 && !dofs)) return fail(SFX_ERR_INVALID, "null argument");
+  for (int64_t i = 0; i < n; i++)
+    if (dofs[i] < 0 || dofs[i] >= s->n) return fail(SFX_ERR_INVALID, "essential dof out of range");
+  s->n_ess = n;
+  if (n == 0) return SFX_OK;
+  if (s->ess.upload(dofs, size_t(n)) != cudaSuccess) return fail(SFX_ERR_CUDA, "upload essential dofs");
+  return SFX_OK;
+}
+
+int sfx_solver_solve_linear(sfx_solver s, double t, const double* u_lin, const double* rhs, double* x, void* stream) {
+  if (!s || !u_lin || !rhs || !x) return fail(SFX_ERR_INVALID, "null argument");
+  auto st = static_cast<cudaStream_t>(stream);
+  s->stats = sfx_solver_stats{};
+  if (int rc = sfx_linearize(s->form, t, u_lin, nullptr, st)) return rc;
+  return linear_solve(s, rhs, x, st);
+}
+
+int sfx_solver_solve(sfx_solver s, double t, double* u, void* stream) {
+  if (!s || !u) return fail(SFX_ERR_INVALID, "null argument");
+  auto st = static_cast<cudaStream_t>(stream);
+  const int64_t n = s->n;
+  s->stats = sfx_solver_stats{};
+  cudaError_t err;
+  // r = R(u), zero on the essential set
+  if (int rc = sfx_residual(s->form, t, u, s->r.p, st)) return rc;
+  if (s->n_ess) sfx_blas::set_entries<double><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, 0.0, s->r.p);
+  double r0 = std::sqrt(s->red.dot(s->r.p, s->r.p, n, st, &err));
+  SFX_CUDA_TRY(err);
+  if (!std::isfinite(r0)) return fail(SFX_ERR_NONFINITE, "non-finite initial residual");
+  s->stats.initial_residual = r0;
+  double rn = r0;
+  const double target = std::max(s->opt.newton_rel_tol * r0, s->opt.newton_abs_tol);
+  int it = 0;
+  for (it = 0; it < s->opt.max_newton_iterations && rn > target; it++) {
+    if (int rc = sfx_linearize(s->form, t, u, nullptr, st)) return rc;
+    if (int rc = linear_solve(s, s->r.p, s->du.p, st)) return rc;
+    sfx_blas::axpby<double><<<nblocks(n), 256, 0, st>>>(n, -1.0, s->du.p, 1.0, u);
+    if (int rc = sfx_residual(s->form, t, u, s->r.p, st)) return rc;
+    if (s->n_ess) sfx_blas::set_entries<double><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, 0.0, s->r.p);
+    rn = std::sqrt(s->red.dot(s->r.p, s->r.p, n, st, &err));
+    SFX_CUDA_TRY(err);
+    if (!std::isfinite(rn)) return fail(SFX_ERR_NONFINITE, "non-finite residual in Newton");
+    if (s->opt.print_level > 0)
+      std::fprintf(stderr, "newton %d  |r| = %.6e  rel = %.3e  krylov %d\n", it + 1, rn, rn / (r0 > 0 ? r0 : 1.0),
+                   s->stats.krylov_iterations);
+  }
+  s->stats.newton_iterations = it;
+  s->stats.final_residual = rn;
+  s->stats.converged = rn <= target ? 1 : 0;
+  return s->stats.converged ? SFX_OK : fail(SFX_ERR_NOT_CONVERGED, "Newton did not converge");
+}
+
+int sfx_solver_get_stats(sfx_solver s, sfx_solver_stats* out) {
+  if (!s || !out) return fail(SFX_ERR_INVALID, "null argument");
+  *out = s->stats;
+  return SFX_OK;
+}
+
+}  // extern "C"
