@@ -738,8 +738,9 @@ struct TangentShape {
 /// Linearise the q-function at every quadrature point (the derivative serac
 /// stores in evaluation_kernel_impl, domain_integral_kernels.hpp:209-214, after
 /// physical_to_parent, with det(J) w folded in) and, optionally, write the
-/// element residuals of the same evaluation.  D is stored structure-of-arrays
-/// D[(row * cols + col) * nq_total + point] in FP64 and FP32.
+/// element residuals of the same evaluation.  D is stored element-major,
+/// D[((e * rows + row) * cols + col) * NQ + q], in FP64 and FP32, so that one
+/// element's tangent is one contiguous block.
 template <int P, int C, typename State, typename QFMaker>
 __global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QFMaker make_qf, double* __restrict__ D64,
                                                         float* __restrict__ D32, double* __restrict__ res_e) {
@@ -850,8 +851,8 @@ __global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QF
       if constexpr (HS) {
         Real v = dvol * part<JVP, Real>(source_comp<C>(get<0>(out), ci));
         if (valid) {
-          D64[(int64_t(ci) * Shape::cols + k) * nq_total + gq] = v;
-          D32[(int64_t(ci) * Shape::cols + k) * nq_total + gq] = float(v);
+          D64[(e * Shape::size + int64_t(ci) * Shape::cols + k) * NQ + qi] = v;
+          D32[(e * Shape::size + int64_t(ci) * Shape::cols + k) * NQ + qi] = float(v);
         }
       }
     }
@@ -873,8 +874,8 @@ __global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QF
       for (int kd = 0; kd < 3; kd++) {
         Real v = dvol * (fp[0] * Ji[kd][0] + fp[1] * Ji[kd][1] + fp[2] * Ji[kd][2]);
         if (valid) {
-          D64[(int64_t(row + 3 * ci + kd) * Shape::cols + k) * nq_total + gq] = v;
-          D32[(int64_t(row + 3 * ci + kd) * Shape::cols + k) * nq_total + gq] = float(v);
+          D64[(e * Shape::size + int64_t(row + 3 * ci + kd) * Shape::cols + k) * NQ + qi] = v;
+          D32[(e * Shape::size + int64_t(row + 3 * ci + kd) * Shape::cols + k) * NQ + qi] = float(v);
         }
         if (!have_res) res_f[ci][kd] = dvol * (fv[0] * Ji[kd][0] + fv[1] * Ji[kd][1] + fv[2] * Ji[kd][2]);
       }
@@ -941,12 +942,12 @@ __global__ void __launch_bounds__(128) jvp_stored_kernel(const Real* __restrict_
     din[off + 3 * c + 2] = g2;
   }
   Real dout[Shape::rows];
-  const Real* Dq = D + (valid ? gq : 0);
+  const Real* Dq = D + (valid ? e * Shape::size * NQ + qi : 0);
 #pragma unroll
   for (int r = 0; r < Shape::rows; r++) {
     Real acc = 0;
 #pragma unroll
-    for (int k = 0; k < Shape::cols; k++) acc += (valid ? Dq[(int64_t(r) * Shape::cols + k) * nq_total] : Real(0)) * din[k];
+    for (int k = 0; k < Shape::cols; k++) acc += (valid ? Dq[(r * Shape::cols + k) * NQ] : Real(0)) * din[k];
     dout[r] = acc;
   }
   constexpr int roff = HS ? C : 0;
@@ -956,6 +957,85 @@ __global__ void __launch_bounds__(128) jvp_stored_kernel(const Real* __restrict_
     Real r = integrate_lane<Q, HS, true, Real>(s, dout[roff + 3 * c], dout[roff + 3 * c + 1], dout[roff + 3 * c + 2],
                                                base, ix, iy, iz, sB, sG);
     if (valid) out_e[(e * C + c) * NQ + qi] = r;
+  }
+}
+
+}  // namespace kernels
+}  // namespace sfx
+
+namespace sfx {
+namespace kernels {
+
+/// Diagonal of the element Jacobians from the stored tangent, as an E-vector
+/// [e][c][node]: K[(c,i)][(c,i)] = sum_q sum_{a,b} Psi_a(i,q) D[(c,a)][(c,b)](q) Psi_b(i,q)
+/// with Psi_0 = phi and Psi_{1..3} = d phi / d xi_k.  Each (a, b) term is a
+/// product of 1-D factors, so the sum over the points runs as three
+/// sum-factorised passes (x, y, z) of 3 FMA per lane.
+template <int P, int C, bool HS, bool VI>
+__global__ void __launch_bounds__(128) diag_from_tangent_kernel(const double* __restrict__ D, double* __restrict__ out_e,
+                                                                int64_t num_elements) {
+  using Real = double;
+  constexpr int Q = P + 1;
+  constexpr int NQ = Q * Q * Q;
+  constexpr int EPW = 32 / NQ;
+  using Shape = TangentShape<C, HS, VI>;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int sub = lane / NQ;
+  const int qi_raw = lane - sub * NQ;
+  const bool slot = sub < EPW;
+  const int qi = slot ? qi_raw : NQ - 1;
+  const int base = slot ? sub * NQ : 0;
+  const int64_t e = warp * EPW + (slot ? sub : 0);
+  const bool valid = slot && e < num_elements;
+  const int ix = qi % Q, iy = (qi / Q) % Q, iz = qi / (Q * Q);
+
+  __shared__ Real sB[Q][Q], sG[Q][Q];
+  if (threadIdx.x < Q * Q) {
+    int i = threadIdx.x / Q, j = threadIdx.x % Q;
+    sB[i][j] = basis_table<P>().B[i][j];
+    sG[i][j] = basis_table<P>().G[i][j];
+  }
+  __syncthreads();
+  const int64_t nq_total = num_elements * NQ;
+  const int64_t gq = e * NQ + qi;
+
+#pragma unroll
+  for (int c = 0; c < C; c++) {
+    Real acc_node = 0;
+#pragma unroll
+    for (int a = (HS ? 0 : 1); a < 4; a++) {
+#pragma unroll
+      for (int b = (VI ? 0 : 1); b < 4; b++) {
+        const int row = (a == 0) ? c : (HS ? C : 0) + 3 * c + (a - 1);
+        const int col = (b == 0) ? c : (VI ? C : 0) + 3 * c + (b - 1);
+        Real d = valid ? D[(e * Shape::size + int64_t(row) * Shape::cols + col) * NQ + qi] : Real(0);
+        // x-pass: T1(ix', qy, qz) = sum_qx d(qx,qy,qz) fa_x(qx,ix') fb_x(qx,ix')
+        Real t1 = 0;
+#pragma unroll
+        for (int k = 0; k < Q; k++) {
+          Real fa = (a == 1) ? sG[k][ix] : sB[k][ix];
+          Real fb = (b == 1) ? sG[k][ix] : sB[k][ix];
+          t1 += fa * fb * shfl(d, base + k + Q * (iy + Q * iz));
+        }
+        Real t2 = 0;
+#pragma unroll
+        for (int k = 0; k < Q; k++) {
+          Real fa = (a == 2) ? sG[k][iy] : sB[k][iy];
+          Real fb = (b == 2) ? sG[k][iy] : sB[k][iy];
+          t2 += fa * fb * shfl(t1, base + ix + Q * (k + Q * iz));
+        }
+        Real t3 = 0;
+#pragma unroll
+        for (int k = 0; k < Q; k++) {
+          Real fa = (a == 3) ? sG[k][iz] : sB[k][iz];
+          Real fb = (b == 3) ? sG[k][iz] : sB[k][iz];
+          t3 += fa * fb * shfl(t2, base + ix + Q * (iy + Q * k));
+        }
+        acc_node += t3;
+      }
+    }
+    if (valid) out_e[(e * C + c) * NQ + qi] = acc_node;
   }
 }
 

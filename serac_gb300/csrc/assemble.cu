@@ -126,7 +126,11 @@ int sfx_assemble_diagonal(sfx_form form, double* diag, void* stream) {
   if (form->domain.empty()) return fail(SFX_ERR_INVALID, "no domain integral");
   auto s = static_cast<cudaStream_t>(stream);
   for (size_t i = 0; i < form->domain.size(); i++) {
-    if (int rc = launch_element_matrix(*form, form->domain[i], true, form->e64.p, 0, form->ne, s)) return rc;
+    const auto& di = form->domain[i];
+    const bool stored = form->jvp_mode == SFX_JVP_STORED_TANGENT && di.D64.p != nullptr;
+    int rc0 = stored ? launch_diag_from_tangent(*form, di, form->e64.p, s)
+                     : launch_element_matrix(*form, di, true, form->e64.p, 0, form->ne, s);
+    if (rc0) return rc0;
     if (int rc = scatter_evector(*form, form->e64.p, diag, i > 0, s)) return rc;
   }
   return SFX_OK;

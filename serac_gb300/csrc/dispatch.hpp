@@ -22,6 +22,8 @@ int scatter_evector(const sfx_form_s& f, const double* E, double* out, bool accu
 // stored-tangent path: linearise (store D, optionally element residuals) and apply D
 int launch_linearize(const sfx_form_s& f, DomainIntegral& di, double* res_e, cudaStream_t s);
 int launch_jvp_stored(const sfx_form_s& f, const DomainIntegral& di, const double* du, double* E, cudaStream_t s);
+// diagonal of the element Jacobians from the stored tangent (E-vector)
+int launch_diag_from_tangent(const sfx_form_s& f, const DomainIntegral& di, double* E, cudaStream_t s);
 int launch_jvp_stored_f32(const sfx_form_s& f, const DomainIntegral& di, const float* du, float* E, cudaStream_t s);
 
 int launch_domain_jvp_f32(const sfx_form_s& f, const DomainIntegral& di, const float* u, const float* du, float* E,

@@ -204,7 +204,35 @@ struct StoredJvpFn {
   }
 };
 
+template <int P>
+struct DiagFn {
+  const sfx_form_s& f;
+  const DomainIntegral& di;
+  double* E;
+  cudaStream_t s;
+  template <int C, typename State, typename Maker>
+  int operator()() {
+    constexpr int NQ = (P + 1) * (P + 1) * (P + 1);
+    constexpr int EPW = 32 / NQ;
+    using QF = decltype(Maker{}(nullptr));
+    constexpr bool HS = kernels::tangent_has_source<C, State, QF>();
+    if (f.ne == 0) return SFX_OK;
+    int64_t warps = (f.ne + EPW - 1) / EPW;
+    int64_t blocks = (warps * 32 + 127) / 128;
+    kernels::diag_from_tangent_kernel<P, C, HS, Maker::value_input><<<unsigned(blocks), 128, 0, s>>>(di.D64.p, E, f.ne);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("diagonal launch: ") + cudaGetErrorString(err));
+    return SFX_OK;
+  }
+};
+
 }  // namespace
+
+int launch_diag_from_tangent(const sfx_form_s& f, const DomainIntegral& di, double* E, cudaStream_t s) {
+  if (f.p == 1) return visit_material(di.material, DiagFn<1>{f, di, E, s});
+  if (f.p == 2) return visit_material(di.material, DiagFn<2>{f, di, E, s});
+  return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
+}
 
 int launch_linearize(const sfx_form_s& f, DomainIntegral& di, double* res_e, cudaStream_t s) {
   if (f.p == 1) return visit_material(di.material, LinearizeFn<1>{f, di, res_e, s});
