@@ -136,6 +136,34 @@ int sfx_assemble_csr(sfx_form form, double* values, void* stream);
 /* Diagonal of dR/du at the linearisation point (device, num_dofs doubles). */
 int sfx_assemble_diagonal(sfx_form form, double* diag, void* stream);
 
+/* Device-side layout of a form, for the header-only C++ front-end
+ * (include/sfx/functional.hpp) that instantiates the element kernels for
+ * user q-functions in the caller's translation unit.  It corresponds to the
+ * members serac's Functional keeps for its integrals (element restriction
+ * tables, geometric factors and E-vector scratch: functional.hpp:723-741,
+ * geometric_factors.hpp).  Pointers stay valid until the form is destroyed;
+ * row_ptr is NULL until the CSR graph has been built (sfx_csr_nnz). */
+typedef struct {
+  int order, components;
+  int64_t num_elements, num_nodes, num_dofs;
+  const int32_t* conn;     /* [e][(order+1)^3] node ids */
+  const int32_t* node_ptr; /* [num_nodes + 1] node -> (element, local) entries */
+  const int32_t* node_ent; /* e * (order+1)^3 + local, element order */
+  const double* geom;      /* 22 x num_elements (order+1)^3 point factors (sfx/kernels.cuh GEOM_STRIDE) */
+  const float* geom_f32;
+  double* evector;         /* scratch [e][component][node] */
+  float* evector_f32;
+  const int64_t* row_ptr;  /* CSR rows (num_dofs + 1) or NULL */
+  int nx, ny, nz;
+} sfx_form_layout;
+int sfx_form_get_layout(sfx_form form, sfx_form_layout* out);
+
+/* out = (accumulate ? out : 0) + scatter-add of the E-vector E [e][component][node]
+ * (ElementRestriction::ScatterAdd, element_restriction.cpp:456-467), node-owner
+ * order, deterministic. */
+int sfx_scatter_add(sfx_form form, const double* E, double* out, int accumulate, void* stream);
+int sfx_scatter_add_f32(sfx_form form, const float* E, float* out, int accumulate, void* stream);
+
 /* Quadrature-point state (J2: 10 doubles per point: plastic strain 3x3
  * row-major, accumulated plastic strain), host arrays
  * [element][point][10].  flag: commit state on the next residual calls. */

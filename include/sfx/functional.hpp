@@ -1,0 +1,404 @@
+// sfx — serac::Functional's C++ interface for user q-functions (header-only;
+// compile the including translation unit with nvcc, link libsfx_gb300.so).
+//
+//   sfx::Mesh mesh = sfx::Mesh::StructuredHex(nx, ny, nz, vertices);
+//   sfx::Functional<sfx::H1<2, 3>(sfx::H1<2, 3>)> residual(mesh);
+//   residual.AddDomainIntegral(sfx::Dimension<3>{}, sfx::DependsOn<0>{}, MyQFunction{...});
+//   const double* r = residual(t, u);                          // device pointers
+//   auto [r2, dRdu] = residual(t, sfx::differentiate_wrt(u));
+//   dRdu.Mult(du, dr);                                         // FP64; MultF32 for the FP32 action
+//   sfx::CSRMatrix K = sfx::assemble(dRdu);
+//
+// Mirrors functional.hpp:189-745 (Functional), :286-317 (AddDomainIntegral),
+// :446-513 (operator()), :534-708 (Gradient, assemble), :523 (updateQdata)
+// and quadrature_data.hpp:111-144 (QuadratureData).  The q-function is a
+// callable object whose operator() is a template usable on the device
+// (`SFX_HD`), called as qf(t, tuple{X, dX_dxi}, [state&,] tuple{u, du_dX}),
+// the way serac's GPU-ready materials are functors (solid_mechanics.hpp:809-850).
+// Its kernels are instantiated here, in the caller's translation unit, from
+// sfx/kernels.cuh; mesh tables, geometric factors and the scatter-add come
+// from the C ABI.
+//
+// Scope of this version: one trial space equal to the test space (DependsOn<0>),
+// domain integrals over the whole mesh; boundary integrals through the C ABI
+// material library (sfx_form_add_boundary_integral).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "sfx.h"
+#include "sfx/kernels.cuh"
+
+namespace sfx {
+
+template <int p, int c = 1>
+struct H1 {
+  static constexpr int order = p;
+  static constexpr int components = c;
+};
+template <int d>
+struct Dimension {};
+template <int... i>
+struct DependsOn {};
+
+struct differentiate_wrt_this {
+  const double* u;
+};
+inline differentiate_wrt_this differentiate_wrt(const double* u) { return {u}; }
+
+inline void check(int rc) {
+  if (rc != SFX_OK) throw std::runtime_error(std::string("sfx: ") + sfx_last_error());
+}
+inline void check_cuda(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+struct DeviceArray {
+  T* p = nullptr;
+  size_t n = 0;
+  DeviceArray() = default;
+  explicit DeviceArray(size_t count) { resize(count); }
+  DeviceArray(const DeviceArray&) = delete;
+  DeviceArray& operator=(const DeviceArray&) = delete;
+  ~DeviceArray() {
+    if (p) cudaFree(p);
+  }
+  void resize(size_t count) {
+    if (count == n) return;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    if (count) check_cuda(cudaMalloc(&p, count * sizeof(T)), "cudaMalloc");
+    n = count;
+  }
+};
+
+class Mesh {
+ public:
+  static Mesh StructuredHex(int nx, int ny, int nz, const double* vertices) {
+    Mesh m;
+    sfx_mesh h = nullptr;
+    check(sfx_mesh_create_structured_hex(nx, ny, nz, vertices, &h));
+    m.h_ = std::shared_ptr<sfx_mesh_s>(h, [](sfx_mesh x) { sfx_mesh_destroy(x); });
+    m.nx = nx;
+    m.ny = ny;
+    m.nz = nz;
+    return m;
+  }
+  sfx_mesh handle() const { return h_.get(); }
+  int nx = 0, ny = 0, nz = 0;
+
+ private:
+  std::shared_ptr<sfx_mesh_s> h_;
+};
+
+/// Quadrature-point state (quadrature_data.hpp:111-144): one State per point,
+/// stored on the device structure-of-arrays (doubles).
+template <typename State>
+class QuadratureData {
+ public:
+  QuadratureData(int64_t num_elements, int points_per_element, const State& init = State{})
+      : num_points_(num_elements * points_per_element) {
+    constexpr int k = int(sizeof(State) / sizeof(double));
+    static_assert(sizeof(State) % sizeof(double) == 0, "state must be made of doubles");
+    data_.resize(size_t(num_points_) * k);
+    std::vector<double> host(size_t(num_points_) * k);
+    const double* s = reinterpret_cast<const double*>(&init);
+    for (int j = 0; j < k; j++)
+      for (int64_t q = 0; q < num_points_; q++) host[size_t(j * num_points_ + q)] = s[j];
+    check_cuda(cudaMemcpy(data_.p, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice), "qdata");
+  }
+  double* device() { return data_.p; }
+  int64_t num_points() const { return num_points_; }
+  State get(int64_t point) const {
+    constexpr int k = int(sizeof(State) / sizeof(double));
+    State out{};
+    double* d = reinterpret_cast<double*>(&out);
+    for (int j = 0; j < k; j++)
+      check_cuda(cudaMemcpy(d + j, data_.p + j * num_points_ + point, sizeof(double), cudaMemcpyDeviceToHost), "qdata");
+    return out;
+  }
+
+ private:
+  int64_t num_points_;
+  DeviceArray<double> data_;
+};
+
+struct CSRMatrix {
+  int64_t rows = 0, nnz = 0;
+  std::shared_ptr<DeviceArray<int64_t>> row_ptr;
+  std::shared_ptr<DeviceArray<int32_t>> col;
+  std::shared_ptr<DeviceArray<double>> values;
+};
+
+namespace detail {
+
+// adapts a user q-function object to the kernels' per-element "maker" interface
+template <typename QF>
+struct UserMaker {
+  QF qf;
+  static constexpr int nparams = 0;
+  static constexpr bool value_input = true;
+  SFX_HD QF operator()(const double*) const { return qf; }
+};
+
+inline unsigned warp_blocks(int64_t ne, int epw) {
+  const int64_t warps = (ne + epw - 1) / epw;
+  return unsigned((warps * 32 + 127) / 128);
+}
+
+struct IntegralBase {
+  virtual ~IntegralBase() = default;
+  virtual void residual(const sfx_form_layout& L, double t, const double* u, double* E, bool update,
+                        cudaStream_t s) = 0;
+  virtual void linearize(const sfx_form_layout& L, double t, const double* u, double* E, cudaStream_t s) = 0;
+  virtual void jvp(const sfx_form_layout& L, const double* du, double* E, cudaStream_t s) = 0;
+  virtual void jvp_f32(const sfx_form_layout& L, const float* du, float* E, cudaStream_t s) = 0;
+  virtual void diagonal(const sfx_form_layout& L, double* E, cudaStream_t s) = 0;
+  virtual void element_matrices(const sfx_form_layout& L, double t, const double* u, double* K, int64_t e0,
+                                int64_t e1, cudaStream_t s) = 0;
+};
+
+template <int P, int C, typename QF, typename State>
+struct DomainIntegral : IntegralBase {
+  using Maker = UserMaker<QF>;
+  static constexpr int NQ = (P + 1) * (P + 1) * (P + 1);
+  static constexpr int EPW = 32 / NQ;
+  static constexpr bool HS = kernels::tangent_has_source<C, State, QF>();
+  using Shape = kernels::TangentShape<C, HS, true>;
+  Maker maker;
+  std::shared_ptr<QuadratureData<State>> qdata;
+  DeviceArray<double> D64;
+  DeviceArray<float> D32;
+
+  DomainIntegral(const QF& qf, std::shared_ptr<QuadratureData<State>> q) : maker{qf}, qdata(std::move(q)) {}
+
+  double* state_ptr() { return qdata ? qdata->device() : nullptr; }
+
+  kernels::DomainArgs<double> args(const sfx_form_layout& L, double t, const double* u, const double* du, double* E) {
+    return {u, du, E, L.conn, L.geom, state_ptr(), nullptr, L.num_nodes, L.num_elements, t};
+  }
+  void residual(const sfx_form_layout& L, double t, const double* u, double* E, bool update, cudaStream_t s) override {
+    auto a = args(L, t, u, nullptr, E);
+    if (update)
+      kernels::domain_kernel<P, C, kernels::RESIDUAL_UPDATE, double, State, Maker>
+          <<<warp_blocks(L.num_elements, EPW), 128, 0, s>>>(a, maker);
+    else
+      kernels::domain_kernel<P, C, kernels::RESIDUAL, double, State, Maker>
+          <<<warp_blocks(L.num_elements, EPW), 128, 0, s>>>(a, maker);
+    check_cuda(cudaGetLastError(), "residual kernel");
+  }
+  void linearize(const sfx_form_layout& L, double t, const double* u, double* E, cudaStream_t s) override {
+    const size_t n = size_t(L.num_elements) * NQ * Shape::size;
+    D64.resize(n);
+    D32.resize(n);
+    auto a = args(L, t, u, nullptr, nullptr);
+    kernels::linearize_kernel<P, C, State, Maker>
+        <<<warp_blocks(L.num_elements, EPW), 128, 0, s>>>(a, maker, D64.p, D32.p, E);
+    check_cuda(cudaGetLastError(), "linearize kernel");
+  }
+  void jvp(const sfx_form_layout& L, const double* du, double* E, cudaStream_t s) override {
+    kernels::jvp_stored_kernel<P, C, HS, true, double>
+        <<<warp_blocks(L.num_elements, EPW), 128, 0, s>>>(du, D64.p, L.conn, E, L.num_nodes, L.num_elements);
+    check_cuda(cudaGetLastError(), "jvp kernel");
+  }
+  void jvp_f32(const sfx_form_layout& L, const float* du, float* E, cudaStream_t s) override {
+    kernels::jvp_stored_kernel<P, C, HS, true, float>
+        <<<warp_blocks(L.num_elements, EPW), 128, 0, s>>>(du, D32.p, L.conn, E, L.num_nodes, L.num_elements);
+    check_cuda(cudaGetLastError(), "jvp kernel (FP32)");
+  }
+  void diagonal(const sfx_form_layout& L, double* E, cudaStream_t s) override {
+    kernels::diag_from_tangent_kernel<P, C, HS, true>
+        <<<warp_blocks(L.num_elements, EPW), 128, 0, s>>>(D64.p, E, L.num_elements);
+    check_cuda(cudaGetLastError(), "diagonal kernel");
+  }
+  void element_matrices(const sfx_form_layout& L, double t, const double* u, double* K, int64_t e0, int64_t e1,
+                        cudaStream_t s) override {
+    auto a = args(L, t, u, nullptr, K);
+    kernels::element_matrix_kernel<P, C, State, Maker, false>
+        <<<warp_blocks(e1 - e0, EPW), 128, 0, s>>>(a, maker, e0, e1);
+    check_cuda(cudaGetLastError(), "element matrix kernel");
+  }
+};
+
+}  // namespace detail
+
+template <typename Signature>
+class Functional;
+
+/// Functional<H1<p,c>(H1<p,c>)>: residual, linearisation and assembly of the
+/// domain integrals added to it.  Vectors are device pointers (byNODES).
+template <int p, int c>
+class Functional<H1<p, c>(H1<p, c>)> {
+ public:
+  class Gradient {
+   public:
+    explicit Gradient(Functional* f) : f_(f) {}
+    /// df = dR/du(t_lin, u_lin) dx  (functional.hpp:556-559)
+    void Mult(const double* dx, double* df, cudaStream_t s = nullptr) const { f_->jvp(dx, df, s); }
+    /// FP32 action on the FP32 copy of the stored tangent
+    void MultF32(const float* dx, float* df, cudaStream_t s = nullptr) const { f_->jvp_f32(dx, df, s); }
+    /// returns a member buffer overwritten by the next call (functional.hpp:562-566)
+    const double* operator()(const double* dx) {
+      Mult(dx, f_->df_.p);
+      return f_->df_.p;
+    }
+    void AssembleDiagonal(double* diag, cudaStream_t s = nullptr) const { f_->diagonal(diag, s); }
+    friend CSRMatrix assemble(Gradient& g) { return g.f_->assemble_csr(); }
+
+   private:
+    Functional* f_;
+  };
+
+  explicit Functional(const Mesh& mesh) : mesh_(mesh), grad_(this) {
+    sfx_form h = nullptr;
+    check(sfx_form_create(mesh.handle(), p, c, &h));
+    form_ = std::shared_ptr<sfx_form_s>(h, [](sfx_form x) { sfx_form_destroy(x); });
+    check(sfx_form_get_layout(h, &L_));
+    out_.resize(size_t(L_.num_dofs));
+    df_.resize(size_t(L_.num_dofs));
+    u_lin_.resize(size_t(L_.num_dofs));
+  }
+
+  static constexpr int points_per_element = (p + 1) * (p + 1) * (p + 1);
+  int64_t num_dofs() const { return L_.num_dofs; }
+  int64_t num_elements() const { return L_.num_elements; }
+
+  /// AddDomainIntegral(Dimension<3>, DependsOn<0>, qf[, qdata])  (functional.hpp:286-317).
+  /// A q-function that takes a state argument but gets no quadrature data
+  /// receives an Empty state (serac's EmptyQData).
+  template <typename QF>
+  void AddDomainIntegral(Dimension<3>, DependsOn<0>, const QF& qf) {
+    using Pos = tuple<tensor<double, 3>, tensor<double, 3, 3>>;
+    using Arg = tuple<kernels::value_t<c, double>, kernels::grad_t<c, double>>;
+    if constexpr (std::is_invocable<const QF&, double, Pos, Arg>::value) {
+      integrals_.emplace_back(new detail::DomainIntegral<p, c, QF, Nothing>(qf, nullptr));
+    } else {
+      integrals_.emplace_back(new detail::DomainIntegral<p, c, QF, Empty>(qf, nullptr));
+    }
+  }
+  template <typename QF, typename State>
+  void AddDomainIntegral(Dimension<3>, DependsOn<0>, const QF& qf, std::shared_ptr<QuadratureData<State>> qdata) {
+    integrals_.emplace_back(new detail::DomainIntegral<p, c, QF, State>(qf, std::move(qdata)));
+  }
+  template <typename QF>
+  void AddVolumeIntegral(DependsOn<0> d, const QF& qf) {
+    AddDomainIntegral(Dimension<3>{}, d, qf);
+  }
+
+  /// updateQdata(bool) (functional.hpp:523): commit quadrature state on residual calls
+  void updateQdata(bool flag) { update_qdata_ = flag; }
+
+  /// R(t, u) into a member buffer (functional.hpp:502-513)
+  const double* operator()(double t, const double* u, cudaStream_t s = nullptr) {
+    residual(t, u, out_.p, s);
+    return out_.p;
+  }
+  void residual(double t, const double* u, double* r, cudaStream_t s = nullptr) {
+    if (integrals_.empty()) throw std::runtime_error("sfx: no integrals");
+    for (size_t i = 0; i < integrals_.size(); i++) {
+      integrals_[i]->residual(L_, t, u, L_.evector, update_qdata_, s);
+      check(sfx_scatter_add(form_.get(), L_.evector, r, i > 0, s));
+    }
+  }
+
+  /// (R(t, u), dR/du) with the tangent linearised at u (functional.hpp:481-489)
+  std::tuple<const double*, Gradient&> operator()(double t, differentiate_wrt_this w, cudaStream_t s = nullptr) {
+    if (integrals_.empty()) throw std::runtime_error("sfx: no integrals");
+    check_cuda(cudaMemcpyAsync(u_lin_.p, w.u, sizeof(double) * size_t(L_.num_dofs), cudaMemcpyDeviceToDevice, s),
+               "copy u");
+    t_lin_ = t;
+    for (size_t i = 0; i < integrals_.size(); i++) {
+      integrals_[i]->linearize(L_, t, u_lin_.p, L_.evector, s);
+      check(sfx_scatter_add(form_.get(), L_.evector, out_.p, i > 0, s));
+    }
+    linearized_ = true;
+    return {out_.p, grad_};
+  }
+
+ private:
+  friend class Gradient;
+  void require_linearized() const {
+    if (!linearized_) throw std::runtime_error("sfx: linearise with operator()(t, differentiate_wrt(u)) first");
+  }
+  void jvp(const double* dx, double* df, cudaStream_t s) {
+    require_linearized();
+    for (size_t i = 0; i < integrals_.size(); i++) {
+      integrals_[i]->jvp(L_, dx, L_.evector, s);
+      check(sfx_scatter_add(form_.get(), L_.evector, df, i > 0, s));
+    }
+  }
+  void jvp_f32(const float* dx, float* df, cudaStream_t s) {
+    require_linearized();
+    for (size_t i = 0; i < integrals_.size(); i++) {
+      integrals_[i]->jvp_f32(L_, dx, L_.evector_f32, s);
+      check(sfx_scatter_add_f32(form_.get(), L_.evector_f32, df, i > 0, s));
+    }
+  }
+  void diagonal(double* diag, cudaStream_t s) {
+    require_linearized();
+    for (size_t i = 0; i < integrals_.size(); i++) {
+      integrals_[i]->diagonal(L_, L_.evector, s);
+      check(sfx_scatter_add(form_.get(), L_.evector, diag, i > 0, s));
+    }
+  }
+
+ public:
+  /// assemble(Gradient&) (functional.hpp:569-667): CSR on the device
+  CSRMatrix assemble_csr() {
+    require_linearized();
+    int64_t nnz = 0;
+    check(sfx_csr_nnz(form_.get(), &nnz));
+    check(sfx_form_get_layout(form_.get(), &L_));
+    CSRMatrix A;
+    A.rows = L_.num_dofs;
+    A.nnz = nnz;
+    A.row_ptr = std::make_shared<DeviceArray<int64_t>>(size_t(L_.num_dofs + 1));
+    A.col = std::make_shared<DeviceArray<int32_t>>(size_t(nnz));
+    A.values = std::make_shared<DeviceArray<double>>(size_t(nnz));
+    check(sfx_csr_graph(form_.get(), A.row_ptr->p, A.col->p, nullptr));
+    constexpr int NDOF = c * points_per_element;
+    const int64_t chunk = std::min<int64_t>(L_.num_elements, 16384);
+    DeviceArray<double> K(size_t(chunk) * NDOF * NDOF);
+    kernels::GridShape g{};
+    g.p = p;
+    g.ne[0] = L_.nx;
+    g.ne[1] = L_.ny;
+    g.ne[2] = L_.nz;
+    for (int d = 0; d < 3; d++) g.N[d] = int64_t(p) * g.ne[d] + 1;
+    bool first = true;
+    for (auto& in : integrals_) {
+      for (int64_t e0 = 0; e0 < L_.num_elements; e0 += chunk) {
+        const int64_t e1 = std::min(L_.num_elements, e0 + chunk);
+        in->element_matrices(L_, t_lin_, u_lin_.p, K.p, e0, e1, nullptr);
+        kernels::csr_assemble_kernel<p, c><<<unsigned((L_.num_dofs + 127) / 128), 128>>>(
+            g, L_.row_ptr, L_.conn, L_.node_ptr, L_.node_ent, K.p, e0, e1, A.values->p, !first);
+        check_cuda(cudaGetLastError(), "assembly kernel");
+        first = false;
+      }
+    }
+    check_cuda(cudaDeviceSynchronize(), "assembly");
+    return A;
+  }
+
+ private:
+  Mesh mesh_;
+  std::shared_ptr<sfx_form_s> form_;
+  sfx_form_layout L_{};
+  std::vector<std::unique_ptr<detail::IntegralBase>> integrals_;
+  DeviceArray<double> out_, df_, u_lin_;
+  double t_lin_ = 0.0;
+  bool linearized_ = false;
+  bool update_qdata_ = false;
+  Gradient grad_;
+};
+
+}  // namespace sfx

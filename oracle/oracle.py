@@ -361,31 +361,31 @@ class OracleFunctional:
 
         row_ptr, col = self.csr_graph()
         n = self.ndofs
-        A = sp.csr_matrix((np.zeros(col.shape[0]), col, row_ptr), shape=(n, n))
+        rows_of = np.repeat(np.arange(n, dtype=np.int64), np.diff(row_ptr))
+        graph_keys = rows_of * n + col
+        vals = np.zeros(col.shape[0])
+
+        def add(K, vd):
+            # K[e][trial j][test i] adds to row vd[e, i], column vd[e, j]
+            nd = vd.shape[1]
+            rows = np.tile(vd, (1, nd)).ravel()
+            cols = np.repeat(vd, nd, axis=1).ravel()
+            pos = np.searchsorted(graph_keys, rows * n + cols)
+            np.add.at(vals, pos, K.ravel())
+
         uE = gather(u, self.conn, self.c, self.nnodes)
         vd = elem_vdofs(self.conn, self.c, self.nnodes)
         for mat, params in self.domain:
             st = self.state if mat == MAT_J2 else None
             K = element_kernel(mat, self.p, 2, uE, self.Xq, self.Jq, params, None, st, False, t, self.use_ref,
                                self.nthreads)
-            # K[e][trial j][test i] -> row i, col j
-            rows = np.repeat(vd, vd.shape[1], axis=1)
-            cols = np.tile(vd, (1, vd.shape[1]))
-            A = A + sp.csr_matrix((K.transpose(0, 2, 1).ravel(), (rows.ravel(), cols.ravel())), shape=(n, n))
+            add(K, vd)
         for bmat, params, fnodes, Xq, Jq in self.boundary:
             uF = gather(u, fnodes, self.c, self.nnodes)
             K = boundary_kernel(bmat, self.p, 2, uF, Xq, Jq, params, None, t, self.use_ref)
-            fv = elem_vdofs(fnodes, self.c, self.nnodes)
-            rows = np.repeat(fv, fv.shape[1], axis=1)
-            cols = np.tile(fv, (1, fv.shape[1]))
-            A = A + sp.csr_matrix((K.transpose(0, 2, 1).ravel(), (rows.ravel(), cols.ravel())), shape=(n, n))
-        A = A.tocsr()
-        A.sort_indices()
-        # keep exactly the element graph (explicit zeros included)
-        G = sp.csr_matrix((np.ones(col.shape[0]), col, row_ptr), shape=(n, n))
-        A = (A + 0.0 * G).tocsr()
-        A.sort_indices()
-        return A
+            add(K, elem_vdofs(fnodes, self.c, self.nnodes))
+        # the graph holds every element pair, explicit zeros included
+        return sp.csr_matrix((vals, col, row_ptr), shape=(n, n))
 
 
 def eliminate_dirichlet(A, ess):

@@ -102,9 +102,10 @@ int sfx_csr_graph(sfx_form form, int64_t* row_ptr, int32_t* col, void* stream) {
 int sfx_assemble_csr(sfx_form form, double* values, void* stream) {
   if (!form || !values) return fail(SFX_ERR_INVALID, "null argument");
   if (!form->linearized) return fail(SFX_ERR_INVALID, "sfx_linearize must be called before sfx_assemble_csr");
-  if (form->domain.empty()) return fail(SFX_ERR_INVALID, "no domain integral");
+  if (form->domain.empty() && form->boundary.empty()) return fail(SFX_ERR_INVALID, "no integrals");
   auto s = static_cast<cudaStream_t>(stream);
   if (int rc = build_graph(form, s)) return rc;
+  if (form->domain.empty()) SFX_CUDA_TRY(cudaMemsetAsync(values, 0, sizeof(double) * size_t(form->nnz), s));
   const int64_t ndof_e = int64_t(form->NPE) * form->c;
   const int64_t chunk = std::min<int64_t>(form->ne, kChunkElements);
   if (form->ke.n < size_t(chunk * ndof_e * ndof_e)) SFX_CUDA_TRY(form->ke.alloc(size_t(chunk * ndof_e * ndof_e)));
@@ -117,14 +118,15 @@ int sfx_assemble_csr(sfx_form form, double* values, void* stream) {
       first = false;
     }
   }
-  return SFX_OK;
+  return assemble_boundary(*form, values, nullptr, s);
 }
 
 int sfx_assemble_diagonal(sfx_form form, double* diag, void* stream) {
   if (!form || !diag) return fail(SFX_ERR_INVALID, "null argument");
   if (!form->linearized) return fail(SFX_ERR_INVALID, "sfx_linearize must be called before sfx_assemble_diagonal");
-  if (form->domain.empty()) return fail(SFX_ERR_INVALID, "no domain integral");
+  if (form->domain.empty() && form->boundary.empty()) return fail(SFX_ERR_INVALID, "no integrals");
   auto s = static_cast<cudaStream_t>(stream);
+  if (form->domain.empty()) SFX_CUDA_TRY(cudaMemsetAsync(diag, 0, sizeof(double) * size_t(form->ndofs), s));
   for (size_t i = 0; i < form->domain.size(); i++) {
     const auto& di = form->domain[i];
     const bool stored = form->jvp_mode == SFX_JVP_STORED_TANGENT && di.D64.p != nullptr;
@@ -133,11 +135,7 @@ int sfx_assemble_diagonal(sfx_form form, double* diag, void* stream) {
     if (rc0) return rc0;
     if (int rc = scatter_evector(*form, form->e64.p, diag, i > 0, s)) return rc;
   }
-  return SFX_OK;
-}
-
-int sfx_form_add_boundary_integral(sfx_form, int, int, const double*) {
-  return fail(SFX_ERR_UNSUPPORTED, "boundary integrals not built yet");
+  return assemble_boundary(*form, nullptr, diag, s);
 }
 
 }  // extern "C"

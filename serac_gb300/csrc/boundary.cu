@@ -1,0 +1,248 @@
+// Boundary integrals over the sides of the structured box
+// (serac: Functional::AddBoundaryIntegral, functional.hpp:328-354;
+// boundary_integral_kernels.hpp:112-325; face restriction, element_restriction.cpp:279-388).
+//
+// Faces of side s are parametrised (s, t) so that dX/ds x dX/dt points out of
+// the box; faces are numbered t-major within a side, sides in increasing
+// order; face-local node ks + (p+1) kt.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "dispatch.hpp"
+#include "form.hpp"
+#include "sfx.h"
+#include "sfx/boundary.cuh"
+#include "sfx/materials.hpp"
+
+using namespace sfx_impl;
+
+namespace {
+
+using namespace sfx;
+
+struct Side {
+  int axis, hi, s_axis, t_axis;
+};
+// side -> (fixed axis, fixed at max?, s axis, t axis); outward normal = J_s x J_t
+constexpr Side kSides[7] = {{0, 0, 0, 0}, {2, 0, 1, 0}, {1, 0, 0, 2}, {0, 1, 1, 2},
+                            {1, 1, 2, 0}, {0, 0, 2, 1}, {2, 1, 0, 1}};
+
+template <typename Fn>
+int visit_bmaterial(const BoundaryIntegral& bi, Fn&& fn) {
+  const auto& p = bi.params;
+  switch (bi.material) {
+    case SFX_BMAT_HEAT_FLUX:
+      return fn.template operator()<1>(boundary_models::HeatFlux{p[0], p[1], p[2]});
+    case SFX_BMAT_TRACTION: {
+      boundary_models::Traction q{};
+      for (int i = 0; i < 3; i++) {
+        q.t0[i] = p[size_t(i)];
+        q.t1[i] = p[size_t(3 + i)];
+      }
+      return fn.template operator()<3>(q);
+    }
+    case SFX_BMAT_PRESSURE: return fn.template operator()<3>(boundary_models::Pressure{p[0]});
+  }
+  return fail(SFX_ERR_UNSUPPORTED, "unknown boundary material");
+}
+
+int bmaterial_info(int material, int* components, int* nparams) {
+  switch (material) {
+    case SFX_BMAT_HEAT_FLUX: *components = 1; *nparams = 3; return SFX_OK;
+    case SFX_BMAT_TRACTION: *components = 3; *nparams = 6; return SFX_OK;
+    case SFX_BMAT_PRESSURE: *components = 3; *nparams = 1; return SFX_OK;
+  }
+  return fail(SFX_ERR_UNSUPPORTED, "unknown boundary material id");
+}
+
+template <int P, int MODE, typename Real>
+struct FaceFn {
+  const sfx_form_s& f;
+  const BoundaryIntegral& bi;
+  const Real* u;
+  const Real* du;
+  Real* out;
+  double t;
+  cudaStream_t s;
+  template <int C, typename QF>
+  int operator()(const QF& qf) {
+    constexpr int NQ = (P + 1) * (P + 1);
+    constexpr int FPW = 32 / NQ;
+    if (bi.num_faces == 0) return SFX_OK;
+    Real* E = std::is_same<Real, double>::value ? reinterpret_cast<Real*>(f.ef64.p) : reinterpret_cast<Real*>(f.ef32.p);
+    kernels::FaceArgs<Real> a{u, du, E, bi.fconn.p, bi.fgeom.p, f.nnodes, bi.num_faces, t};
+    const int64_t warps = (bi.num_faces + FPW - 1) / FPW;
+    kernels::face_kernel<P, C, MODE, Real, QF><<<unsigned((warps * 32 + 127) / 128), 128, 0, s>>>(a, qf);
+    kernels::face_scatter_kernel<C, NQ, Real><<<unsigned((bi.num_face_nodes + 255) / 256), 256, 0, s>>>(
+        E, bi.node_ptr.p, bi.node_ids.p, bi.node_ent.p, out, bi.num_face_nodes, f.nnodes);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("face kernel launch: ") + cudaGetErrorString(err));
+    return SFX_OK;
+  }
+};
+
+template <int P>
+struct FaceMatrixFn {
+  sfx_form_s& f;
+  const BoundaryIntegral& bi;
+  double* values;  // CSR values (accumulate) or nullptr
+  double* diag;    // diagonal (accumulate) or nullptr
+  cudaStream_t s;
+  template <int C, typename QF>
+  int operator()(const QF& qf) {
+    constexpr int NQ = (P + 1) * (P + 1);
+    constexpr int FPW = 32 / NQ;
+    constexpr int NDOF = C * NQ;
+    if (bi.num_faces == 0) return SFX_OK;
+    const size_t need = size_t(bi.num_faces) * NDOF * NDOF;
+    if (f.kf.n < need && f.kf.alloc(need) != cudaSuccess) return fail(SFX_ERR_NOMEM, "face matrix scratch");
+    kernels::FaceArgs<double> a{f.u_lin64.p, nullptr, f.kf.p, bi.fconn.p, bi.fgeom.p, f.nnodes, bi.num_faces, f.t_lin};
+    const int64_t warps = (bi.num_faces + FPW - 1) / FPW;
+    kernels::face_matrix_kernel<P, C, QF><<<unsigned((warps * 32 + 127) / 128), 128, 0, s>>>(a, qf);
+    if (values) {
+      kernels::GridShape g{};
+      g.p = f.p;
+      g.ne[0] = f.mesh.nx;
+      g.ne[1] = f.mesh.ny;
+      g.ne[2] = f.mesh.nz;
+      for (int d = 0; d < 3; d++) g.N[d] = int64_t(f.p) * g.ne[d] + 1;
+      kernels::face_csr_kernel<P, C><<<unsigned((bi.num_face_nodes * C + 127) / 128), 128, 0, s>>>(
+          g, f.row_ptr.p, bi.fconn.p, bi.node_ptr.p, bi.node_ids.p, bi.node_ent.p, f.kf.p, values, bi.num_face_nodes);
+    }
+    if (diag) {
+      kernels::face_diag_kernel<C, NQ><<<unsigned((bi.num_face_nodes + 255) / 256), 256, 0, s>>>(
+          bi.node_ptr.p, bi.node_ids.p, bi.node_ent.p, f.kf.p, diag, bi.num_face_nodes, f.nnodes);
+    }
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("face matrix launch: ") + cudaGetErrorString(err));
+    return SFX_OK;
+  }
+};
+
+}  // namespace
+
+namespace sfx_impl {
+
+int launch_boundary(const sfx_form_s& f, int mode, const double* u, const double* du, double* out, double t,
+                    cudaStream_t s) {
+  for (const auto& bi : f.boundary) {
+    int rc = SFX_OK;
+    if (mode == 2) {
+      rc = f.p == 1 ? visit_bmaterial(bi, FaceFn<1, kernels::JVP, double>{f, bi, u, du, out, t, s})
+                    : visit_bmaterial(bi, FaceFn<2, kernels::JVP, double>{f, bi, u, du, out, t, s});
+    } else {
+      rc = f.p == 1 ? visit_bmaterial(bi, FaceFn<1, kernels::RESIDUAL, double>{f, bi, u, du, out, t, s})
+                    : visit_bmaterial(bi, FaceFn<2, kernels::RESIDUAL, double>{f, bi, u, du, out, t, s});
+    }
+    if (rc) return rc;
+  }
+  return SFX_OK;
+}
+
+int launch_boundary_jvp_f32(const sfx_form_s& f, const float* u, const float* du, float* out, double t,
+                            cudaStream_t s) {
+  for (const auto& bi : f.boundary) {
+    int rc = f.p == 1 ? visit_bmaterial(bi, FaceFn<1, kernels::JVP, float>{f, bi, u, du, out, t, s})
+                      : visit_bmaterial(bi, FaceFn<2, kernels::JVP, float>{f, bi, u, du, out, t, s});
+    if (rc) return rc;
+  }
+  return SFX_OK;
+}
+
+int assemble_boundary(sfx_form_s& f, double* values, double* diag, cudaStream_t s) {
+  for (const auto& bi : f.boundary) {
+    int rc = f.p == 1 ? visit_bmaterial(bi, FaceMatrixFn<1>{f, bi, values, diag, s})
+                      : visit_bmaterial(bi, FaceMatrixFn<2>{f, bi, values, diag, s});
+    if (rc) return rc;
+  }
+  return SFX_OK;
+}
+
+}  // namespace sfx_impl
+
+extern "C" int sfx_form_add_boundary_integral(sfx_form form, int bmaterial, int side_mask, const double* params) {
+  if (!form) return fail(SFX_ERR_INVALID, "null form");
+  int comps = 0, np = 0;
+  if (int rc = bmaterial_info(bmaterial, &comps, &np)) return rc;
+  if (comps != form->c) return fail(SFX_ERR_INVALID, "boundary material component count does not match the space");
+  if (side_mask <= 0 || side_mask >= 64) return fail(SFX_ERR_INVALID, "side mask must select sides 1..6");
+  if (!params) return fail(SFX_ERR_INVALID, "null parameters");
+  const auto& m = form->mesh;
+  const int p = form->p, n = p + 1, npf = n * n;
+  const int64_t dims[3] = {m.nx, m.ny, m.nz};
+  const int64_t N[3] = {int64_t(p) * m.nx + 1, int64_t(p) * m.ny + 1, int64_t(p) * m.nz + 1};
+  std::vector<int32_t> fconn;
+  std::vector<double> Xf;
+  for (int side = 1; side <= 6; side++) {
+    if (!(side_mask & (1 << (side - 1)))) continue;
+    const Side sd = kSides[side];
+    const int64_t fixed = sd.hi ? dims[sd.axis] : 0;
+    for (int64_t ft = 0; ft < dims[sd.t_axis]; ft++)
+      for (int64_t fs = 0; fs < dims[sd.s_axis]; fs++) {
+        for (int i = 0; i < 3; i++)
+          for (int v = 0; v < 4; v++) {
+            int64_t idx[3] = {0, 0, 0};
+            idx[sd.axis] = fixed;
+            idx[sd.s_axis] = fs + (v & 1);
+            idx[sd.t_axis] = ft + (v >> 1);
+            const int64_t vid = idx[0] + int64_t(m.nx + 1) * (idx[1] + int64_t(m.ny + 1) * idx[2]);
+            Xf.push_back(m.vertices[size_t(vid * 3 + i)]);
+          }
+        for (int kt = 0; kt < n; kt++)
+          for (int ks = 0; ks < n; ks++) {
+            int64_t idx[3] = {0, 0, 0};
+            idx[sd.axis] = p * fixed;
+            idx[sd.s_axis] = p * fs + ks;
+            idx[sd.t_axis] = p * ft + kt;
+            fconn.push_back(int32_t(idx[0] + N[0] * (idx[1] + N[1] * idx[2])));
+          }
+      }
+  }
+  BoundaryIntegral bi;
+  bi.material = bmaterial;
+  bi.params.assign(params, params + np);
+  bi.num_faces = int64_t(fconn.size()) / npf;
+  // compact face-node map: distinct nodes ascending, entries in face order
+  std::vector<int32_t> order(fconn.size());
+  for (size_t i = 0; i < order.size(); i++) order[i] = int32_t(i);
+  std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return fconn[size_t(a)] < fconn[size_t(b)]; });
+  std::vector<int32_t> ids, ptr{0}, ent;
+  for (size_t k = 0; k < order.size(); k++) {
+    const int32_t nd = fconn[size_t(order[k])];
+    if (ids.empty() || ids.back() != nd) {
+      if (!ids.empty()) ptr.push_back(int32_t(ent.size()));
+      ids.push_back(nd);
+    }
+    ent.push_back(order[k]);
+  }
+  ptr.push_back(int32_t(ent.size()));
+  bi.num_face_nodes = int64_t(ids.size());
+  const int Q = p + 1, nq = Q * Q;
+  const int64_t nqt = bi.num_faces * nq;
+  DeviceBuf<double> dXf;
+  cudaError_t err;
+  if ((err = bi.fconn.upload(fconn.data(), fconn.size())) != cudaSuccess ||
+      (err = bi.node_ptr.upload(ptr.data(), ptr.size())) != cudaSuccess ||
+      (err = bi.node_ids.upload(ids.data(), ids.size())) != cudaSuccess ||
+      (err = bi.node_ent.upload(ent.data(), ent.size())) != cudaSuccess ||
+      (err = dXf.upload(Xf.data(), Xf.size())) != cudaSuccess ||
+      (err = bi.fgeom.alloc(size_t(nqt) * kernels::FGEOM_STRIDE)) != cudaSuccess)
+    return fail(SFX_ERR_CUDA, std::string("boundary setup: ") + cudaGetErrorString(err));
+  if (nqt > 0) {
+    const unsigned blocks = unsigned((nqt + 255) / 256);
+    if (Q == 2) kernels::face_geometry_kernel<2><<<blocks, 256>>>(dXf.p, bi.fgeom.p, bi.num_faces);
+    else kernels::face_geometry_kernel<3><<<blocks, 256>>>(dXf.p, bi.fgeom.p, bi.num_faces);
+    if ((err = cudaGetLastError()) != cudaSuccess || (err = cudaDeviceSynchronize()) != cudaSuccess)
+      return fail(SFX_ERR_CUDA, std::string("face geometry: ") + cudaGetErrorString(err));
+  }
+  const size_t escr = size_t(bi.num_faces) * npf * form->c;
+  if (form->ef64.n < escr) {
+    if (form->ef64.alloc(escr) != cudaSuccess || form->ef32.alloc(escr) != cudaSuccess)
+      return fail(SFX_ERR_NOMEM, "face scratch allocation");
+  }
+  form->boundary.push_back(std::move(bi));
+  return SFX_OK;
+}

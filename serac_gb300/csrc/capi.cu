@@ -216,19 +216,21 @@ int sfx_form_add_domain_integral(sfx_form form, int material, const double* para
 int sfx_residual(sfx_form form, double t, const double* u, double* r, void* stream) {
   if (check_form(form)) return SFX_ERR_INVALID;
   if (!u || !r) return fail(SFX_ERR_INVALID, "null vector");
-  if (form->domain.empty()) return fail(SFX_ERR_INVALID, "no integrals");
+  if (form->domain.empty() && form->boundary.empty()) return fail(SFX_ERR_INVALID, "no integrals");
   auto s = static_cast<cudaStream_t>(stream);
+  if (form->domain.empty()) SFX_CUDA_TRY(cudaMemsetAsync(r, 0, sizeof(double) * size_t(form->ndofs), s));
   const int mode = form->update_qdata ? sfx::kernels::RESIDUAL_UPDATE : sfx::kernels::RESIDUAL;
   for (size_t i = 0; i < form->domain.size(); i++) {
     if (int rc = launch_domain(*form, form->domain[i], mode, u, nullptr, form->e64.p, t, s)) return rc;
     if (int rc = scatter_dispatch<double>(*form, form->e64.p, r, i > 0, s)) return rc;
   }
-  return SFX_OK;
+  return launch_boundary(*form, sfx::kernels::RESIDUAL, u, nullptr, r, t, s);
 }
 
 int sfx_linearize(sfx_form form, double t, const double* u, double* r, void* stream) {
   if (check_form(form)) return SFX_ERR_INVALID;
   if (!u) return fail(SFX_ERR_INVALID, "null vector");
+  if (form->domain.empty() && form->boundary.empty()) return fail(SFX_ERR_INVALID, "no integrals");
   auto s = static_cast<cudaStream_t>(stream);
   SFX_CUDA_TRY(cudaMemcpyAsync(form->u_lin64.p, u, size_t(form->ndofs) * sizeof(double), cudaMemcpyDeviceToDevice, s));
   unsigned blocks = unsigned((form->ndofs + 255) / 256);
@@ -237,11 +239,13 @@ int sfx_linearize(sfx_form form, double t, const double* u, double* r, void* str
   form->t_lin = t;
   form->linearized = true;
   if (form->jvp_mode == SFX_JVP_STORED_TANGENT) {
+    if (r && form->domain.empty()) SFX_CUDA_TRY(cudaMemsetAsync(r, 0, sizeof(double) * size_t(form->ndofs), s));
     for (size_t i = 0; i < form->domain.size(); i++) {
       if (int rc = launch_linearize(*form, form->domain[i], r ? form->e64.p : nullptr, s)) return rc;
       if (r)
         if (int rc = scatter_dispatch<double>(*form, form->e64.p, r, i > 0, s)) return rc;
     }
+    if (r) return launch_boundary(*form, sfx::kernels::RESIDUAL, form->u_lin64.p, nullptr, r, t, s);
     return SFX_OK;
   }
   if (r) {
@@ -267,6 +271,7 @@ int sfx_jvp(sfx_form form, const double* du, double* dr, void* stream) {
   if (!du || !dr) return fail(SFX_ERR_INVALID, "null vector");
   if (!form->linearized) return fail(SFX_ERR_INVALID, "sfx_linearize must be called before sfx_jvp");
   auto s = static_cast<cudaStream_t>(stream);
+  if (form->domain.empty()) SFX_CUDA_TRY(cudaMemsetAsync(dr, 0, sizeof(double) * size_t(form->ndofs), s));
   for (size_t i = 0; i < form->domain.size(); i++) {
     int rc = form->jvp_mode == SFX_JVP_STORED_TANGENT
                  ? launch_jvp_stored(*form, form->domain[i], du, form->e64.p, s)
@@ -275,7 +280,7 @@ int sfx_jvp(sfx_form form, const double* du, double* dr, void* stream) {
     if (rc) return rc;
     if (int rc2 = scatter_dispatch<double>(*form, form->e64.p, dr, i > 0, s)) return rc2;
   }
-  return SFX_OK;
+  return launch_boundary(*form, sfx::kernels::JVP, form->u_lin64.p, du, dr, form->t_lin, s);
 }
 
 int sfx_jvp_f32(sfx_form form, const float* du, float* dr, void* stream) {
@@ -283,6 +288,7 @@ int sfx_jvp_f32(sfx_form form, const float* du, float* dr, void* stream) {
   if (!du || !dr) return fail(SFX_ERR_INVALID, "null vector");
   if (!form->linearized) return fail(SFX_ERR_INVALID, "sfx_linearize must be called before sfx_jvp_f32");
   auto s = static_cast<cudaStream_t>(stream);
+  if (form->domain.empty()) SFX_CUDA_TRY(cudaMemsetAsync(dr, 0, sizeof(float) * size_t(form->ndofs), s));
   for (size_t i = 0; i < form->domain.size(); i++) {
     int rc = form->jvp_mode == SFX_JVP_STORED_TANGENT
                  ? launch_jvp_stored_f32(*form, form->domain[i], du, form->e32.p, s)
@@ -290,7 +296,7 @@ int sfx_jvp_f32(sfx_form form, const float* du, float* dr, void* stream) {
     if (rc) return rc;
     if (int rc2 = scatter_dispatch<float>(*form, form->e32.p, dr, i > 0, s)) return rc2;
   }
-  return SFX_OK;
+  return launch_boundary_jvp_f32(*form, form->u_lin32.p, du, dr, form->t_lin, s);
 }
 
 int sfx_jvp_element(sfx_form form, const double* du, double* dE, void* stream) {
@@ -301,6 +307,39 @@ int sfx_jvp_element(sfx_form form, const double* du, double* dE, void* stream) {
   auto s = static_cast<cudaStream_t>(stream);
   if (form->jvp_mode == SFX_JVP_STORED_TANGENT) return launch_jvp_stored(*form, form->domain[0], du, dE, s);
   return launch_domain(*form, form->domain[0], sfx::kernels::JVP, form->u_lin64.p, du, dE, form->t_lin, s);
+}
+
+int sfx_form_get_layout(sfx_form form, sfx_form_layout* out) {
+  if (check_form(form) || !out) return fail(SFX_ERR_INVALID, "null argument");
+  sfx_form_layout L{};
+  L.order = form->p;
+  L.components = form->c;
+  L.num_elements = form->ne;
+  L.num_nodes = form->nnodes;
+  L.num_dofs = form->ndofs;
+  L.conn = form->conn.p;
+  L.node_ptr = form->node_ptr.p;
+  L.node_ent = form->node_ent.p;
+  L.geom = form->geom64.p;
+  L.geom_f32 = form->geom32.p;
+  L.evector = form->e64.p;
+  L.evector_f32 = form->e32.p;
+  L.row_ptr = form->csr_built ? form->row_ptr.p : nullptr;
+  L.nx = form->mesh.nx;
+  L.ny = form->mesh.ny;
+  L.nz = form->mesh.nz;
+  *out = L;
+  return SFX_OK;
+}
+
+int sfx_scatter_add(sfx_form form, const double* E, double* out, int accumulate, void* stream) {
+  if (check_form(form) || !E || !out) return fail(SFX_ERR_INVALID, "null argument");
+  return scatter_dispatch<double>(*form, E, out, accumulate != 0, static_cast<cudaStream_t>(stream));
+}
+
+int sfx_scatter_add_f32(sfx_form form, const float* E, float* out, int accumulate, void* stream) {
+  if (check_form(form) || !E || !out) return fail(SFX_ERR_INVALID, "null argument");
+  return scatter_dispatch<float>(*form, E, out, accumulate != 0, static_cast<cudaStream_t>(stream));
 }
 
 int sfx_update_qdata(sfx_form form, int flag) {

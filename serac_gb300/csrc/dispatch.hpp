@@ -22,6 +22,14 @@ int scatter_evector(const sfx_form_s& f, const double* E, double* out, bool accu
 // stored-tangent path: linearise (store D, optionally element residuals) and apply D
 int launch_linearize(const sfx_form_s& f, DomainIntegral& di, double* res_e, cudaStream_t s);
 int launch_jvp_stored(const sfx_form_s& f, const DomainIntegral& di, const double* du, double* E, cudaStream_t s);
+// boundary integrals: add face contributions to out (mode 0 residual at u, 2 action on du)
+int launch_boundary(const sfx_form_s& f, int mode, const double* u, const double* du, double* out, double t,
+                    cudaStream_t s);
+int launch_boundary_jvp_f32(const sfx_form_s& f, const float* u, const float* du, float* out, double t,
+                            cudaStream_t s);
+// face element matrices at the linearisation point added into CSR values and/or a diagonal
+int assemble_boundary(sfx_form_s& f, double* values, double* diag, cudaStream_t s);
+
 // diagonal of the element Jacobians from the stored tangent (E-vector)
 int launch_diag_from_tangent(const sfx_form_s& f, const DomainIntegral& di, double* E, cudaStream_t s);
 int launch_jvp_stored_f32(const sfx_form_s& f, const DomainIntegral& di, const float* du, float* E, cudaStream_t s);

@@ -75,15 +75,13 @@ struct DomainIntegral {
 
 struct BoundaryIntegral {
   int material = 0;
-  int nparams = 0;
+  std::vector<double> params;   // uniform material parameters (host; the q-function is built on the host)
   int64_t num_faces = 0;
-  DeviceBuf<double> params;     // nparams (uniform)
   DeviceBuf<int32_t> fconn;     // [f][(p+1)^2] node ids
-  DeviceBuf<double> fgeom64;    // FGEOM_STRIDE x nq_total
-  DeviceBuf<float> fgeom32;
-  DeviceBuf<int32_t> node_ptr;  // over the face nodes: compact list
+  DeviceBuf<double> fgeom;      // FGEOM_STRIDE x nq_total
+  DeviceBuf<int32_t> node_ptr;  // over the distinct face nodes (compact list)
   DeviceBuf<int32_t> node_ids;  // global node of each compact entry
-  DeviceBuf<int32_t> node_ent;  // (f * npf + local) entries
+  DeviceBuf<int32_t> node_ent;  // (f * npf + local) entries, face order
   int64_t num_face_nodes = 0;
 };
 
@@ -121,4 +119,5 @@ struct sfx_form_s {
   sfx_impl::DeviceBuf<int64_t> row_ptr;
   sfx_impl::DeviceBuf<int32_t> col;
   sfx_impl::DeviceBuf<double> ke;  // element matrices scratch
+  sfx_impl::DeviceBuf<double> kf;  // face matrices scratch
 };

@@ -66,7 +66,8 @@ def test_neohookean_newton_matches_oracle(cuda, precond):
     import serac_gb300 as sg
 
     orc, f, ess, u0 = _solid()
-    kw = dict(newton_rel_tol=1e-12, newton_abs_tol=1e-16, krylov_rel_tol=1e-10, max_krylov_iterations=2000)
+    kw = dict(newton_rel_tol=1e-12, newton_abs_tol=1e-16, krylov_rel_tol=1e-10, krylov_abs_tol=1e-16,
+              max_krylov_iterations=2000)
     if precond == "jacobi":
         kw.update(precond=sg.JACOBI)
     elif precond == "mixed":
