@@ -164,6 +164,25 @@ int sfx_form_get_layout(sfx_form form, sfx_form_layout* out);
 int sfx_scatter_add(sfx_form form, const double* E, double* out, int accumulate, void* stream);
 int sfx_scatter_add_f32(sfx_form form, const float* E, float* out, int accumulate, void* stream);
 
+/* Residual of a structured mesh that allocates nothing (no counterpart in
+ * serac).  For callers that cannot allocate device memory at call time or at
+ * all (a memory manager owns every device allocation, or the device footprint
+ * must not grow after start-up): the caller passes the vertex coordinates
+ * (device, (nx+1)(ny+1)(nz+1) x 3 doubles), the field u and the output r
+ * (device, num_dofs doubles each) and the material parameters (host, as for
+ * sfx_form_add_domain_integral, uniform); the connectivity and the geometry
+ * are derived from the grid inside the kernels, and the element-residual
+ * scratch is a fixed 32 MiB device array inside this library (held on every
+ * device that loads the library until exit), so num_elements * components *
+ * (order+1)^3 must not exceed 4,194,304 (SFX_ERR_UNSUPPORTED otherwise).
+ * Materials: SFX_MAT_HEAT, SFX_MAT_NEOHOOKEAN; order 1 or 2.  The first call
+ * on a device looks up the scratch array's device address (make it before
+ * any stream capture).  Every call on a device shares the scratch array:
+ * calls that overlap on that device race and must be serialised by the
+ * caller.  Results equal sfx_residual's for the same mesh and material. */
+int sfx_residual_structured_noalloc(int nx, int ny, int nz, int order, int material, const double* params,
+                                    const double* vertices, const double* u, double* r, double t, void* stream);
+
 /* Quadrature-point state (J2: 10 doubles per point: plastic strain 3x3
  * row-major, accumulated plastic strain), host arrays
  * [element][point][10].  flag: commit state on the next residual calls. */
