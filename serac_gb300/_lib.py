@@ -50,6 +50,9 @@ SIGNATURES = {
     "sfx_assemble_csr": (_c.c_int, [_vp, _vp, _vp]),
     "sfx_assemble_diagonal": (_c.c_int, [_vp, _vp, _vp]),
     "sfx_residual_structured_noalloc": (_c.c_int, [_c.c_int] * 5 + [_dp, _vp, _vp, _vp, _c.c_double, _vp]),
+    "sfx_form_get_layout": (_c.c_int, [_vp, _vp]),
+    "sfx_scatter_add": (_c.c_int, [_vp, _vp, _vp, _c.c_int, _vp]),
+    "sfx_scatter_add_f32": (_c.c_int, [_vp, _vp, _vp, _c.c_int, _vp]),
     "sfx_update_qdata": (_c.c_int, [_vp, _c.c_int]),
     "sfx_qdata_size": (_c.c_int, [_vp, _i64p]),
     "sfx_set_qdata": (_c.c_int, [_vp, _dp]),
