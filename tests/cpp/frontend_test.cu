@@ -1,0 +1,177 @@
+// Test driver for the header-only C++ front-end (include/sfx/functional.hpp):
+// user-written q-function objects, instantiated in this translation unit,
+// through Functional<H1<p,c>(H1<p,c>)>.  Built into a shared library by
+// tests/test_gpu_frontend.py and called through ctypes; host arrays in/out.
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "sfx/functional.hpp"
+#include "sfx/materials.hpp"
+
+namespace {
+
+// a user q-function: linear scalar model with every derivative block populated
+struct UserThermal {
+  template <typename X, typename T>
+  SFX_HD auto operator()(double, const X& position, const T& temperature) const {
+    using namespace sfx;
+    auto x = get<0>(position);
+    auto u = get<0>(temperature);
+    auto g = get<1>(temperature);
+    tensor<double, 3> d01{{0.0, 1.0, 2.0}}, d10{{0.0, 2.0, 8.0}};
+    tensor<double, 3, 3> d11{};
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) d11[i][j] = double(i + j * (j + 1) + 1);
+    auto source = 1.0 * u + dot(d01, g) + 0.5 * x[0] * x[1];
+    auto flux = u * d10 + dot(d11, g);
+    return tuple{source, flux};
+  }
+};
+
+// a user q-function: compressible Neo-Hookean written out by hand
+struct UserNeoHookean {
+  double K, G;
+  template <typename X, typename D>
+  SFX_HD auto operator()(double, const X&, const D& displacement) const {
+    using namespace sfx;
+    auto H = get<1>(displacement);
+    auto F = H + Identity<3>();
+    auto J = det(F);
+    auto B = dot(F, transpose(F));
+    double lambda = K - (2.0 / 3.0) * G;
+    using std::log;
+    auto sigma = (lambda * log(J) * Identity<3>() + G * (B - Identity<3>())) / J;
+    return tuple{zero{}, dot(sigma, transpose(inv(F))) * J};
+  }
+};
+
+using J2 = sfx::solid_mechanics::J2SmallStrain<sfx::solid_mechanics::LinearHardening>;
+
+template <typename F>
+void copy_out(const double* dev, double* host, size_t n) {
+  cudaMemcpy(host, dev, n * sizeof(double), cudaMemcpyDeviceToHost);
+}
+
+struct Buffers {
+  double *u, *du, *r, *jv, *diag;
+  float *du32, *jv32;
+  size_t n;
+  Buffers(size_t n_) : n(n_) {
+    cudaMalloc(&u, n * 8);
+    cudaMalloc(&du, n * 8);
+    cudaMalloc(&r, n * 8);
+    cudaMalloc(&jv, n * 8);
+    cudaMalloc(&diag, n * 8);
+    cudaMalloc(&du32, n * 4);
+    cudaMalloc(&jv32, n * 4);
+  }
+  ~Buffers() {
+    cudaFree(u);
+    cudaFree(du);
+    cudaFree(r);
+    cudaFree(jv);
+    cudaFree(diag);
+    cudaFree(du32);
+    cudaFree(jv32);
+  }
+};
+
+// outputs: residual, residual at linearisation, jv, jv (FP32, as double), diagonal, CSR values
+template <typename FunctionalT, typename Setup>
+int run(int nx, int ny, int nz, const double* V, const double* u, const double* du, double* out_r, double* out_r2,
+        double* out_jv, double* out_jv32, double* out_diag, double* out_csr, int64_t* out_nnz, Setup&& setup) {
+  try {
+    auto mesh = sfx::Mesh::StructuredHex(nx, ny, nz, V);
+    FunctionalT f(mesh);
+    setup(f);
+    const size_t n = size_t(f.num_dofs());
+    Buffers b(n);
+    cudaMemcpy(b.u, u, n * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(b.du, du, n * 8, cudaMemcpyHostToDevice);
+    std::vector<float> du32(du, du + n);
+    cudaMemcpy(b.du32, du32.data(), n * 4, cudaMemcpyHostToDevice);
+    const double* r = f(0.0, b.u);
+    cudaMemcpy(out_r, r, n * 8, cudaMemcpyDeviceToHost);
+    auto [r2, grad] = f(0.0, sfx::differentiate_wrt(b.u));
+    cudaMemcpy(out_r2, r2, n * 8, cudaMemcpyDeviceToHost);
+    grad.Mult(b.du, b.jv);
+    cudaMemcpy(out_jv, b.jv, n * 8, cudaMemcpyDeviceToHost);
+    grad.MultF32(b.du32, b.jv32);
+    std::vector<float> jv32(n);
+    cudaMemcpy(jv32.data(), b.jv32, n * 4, cudaMemcpyDeviceToHost);
+    for (size_t i = 0; i < n; i++) out_jv32[i] = jv32[i];
+    grad.AssembleDiagonal(b.diag);
+    cudaMemcpy(out_diag, b.diag, n * 8, cudaMemcpyDeviceToHost);
+    sfx::CSRMatrix A = assemble(grad);
+    if (out_csr) cudaMemcpy(out_csr, A.values->p, size_t(A.nnz) * 8, cudaMemcpyDeviceToHost);
+    *out_nnz = A.nnz;
+    return cudaDeviceSynchronize() == cudaSuccess ? 0 : -2;
+  } catch (const std::exception&) {
+    return -1;
+  }
+}
+
+}  // namespace
+
+extern "C" int frontend_thermal(int p, int nx, int ny, int nz, const double* V, const double* u, const double* du,
+                                double* r, double* r2, double* jv, double* jv32, double* diag, double* csr,
+                                int64_t* nnz) {
+  auto setup = [](auto& f) { f.AddDomainIntegral(sfx::Dimension<3>{}, sfx::DependsOn<0>{}, UserThermal{}); };
+  if (p == 1)
+    return run<sfx::Functional<sfx::H1<1, 1>(sfx::H1<1, 1>)>>(nx, ny, nz, V, u, du, r, r2, jv, jv32, diag, csr, nnz,
+                                                              setup);
+  return run<sfx::Functional<sfx::H1<2, 1>(sfx::H1<2, 1>)>>(nx, ny, nz, V, u, du, r, r2, jv, jv32, diag, csr, nnz,
+                                                            setup);
+}
+
+extern "C" int frontend_neohookean(int p, double K, double G, int nx, int ny, int nz, const double* V, const double* u,
+                                   const double* du, double* r, double* r2, double* jv, double* jv32, double* diag,
+                                   double* csr, int64_t* nnz) {
+  auto setup = [K, G](auto& f) { f.AddDomainIntegral(sfx::Dimension<3>{}, sfx::DependsOn<0>{}, UserNeoHookean{K, G}); };
+  if (p == 1)
+    return run<sfx::Functional<sfx::H1<1, 3>(sfx::H1<1, 3>)>>(nx, ny, nz, V, u, du, r, r2, jv, jv32, diag, csr, nnz,
+                                                              setup);
+  return run<sfx::Functional<sfx::H1<2, 3>(sfx::H1<2, 3>)>>(nx, ny, nz, V, u, du, r, r2, jv, jv32, diag, csr, nnz,
+                                                            setup);
+}
+
+// J2 through the library's material functor with a QuadratureData state:
+// commit the state at u (updateQdata), then linearise at 1.5 u.
+extern "C" int frontend_j2(int nx, int ny, int nz, const double* V, const double* u, const double* du, double E,
+                           double nu, double sy, double H, double* r_commit, double* state_out, double* r, double* jv) {
+  try {
+    auto mesh = sfx::Mesh::StructuredHex(nx, ny, nz, V);
+    sfx::Functional<sfx::H1<1, 3>(sfx::H1<1, 3>)> f(mesh);
+    J2 mat{};
+    mat.E = E;
+    mat.nu = nu;
+    mat.hardening = sfx::solid_mechanics::LinearHardening{sy, H};
+    auto qdata = std::make_shared<sfx::QuadratureData<J2::State>>(f.num_elements(), f.points_per_element);
+    f.AddDomainIntegral(sfx::Dimension<3>{}, sfx::DependsOn<0>{},
+                        sfx::solid_mechanics::MaterialStressFunctor<J2, false>{mat}, qdata);
+    const size_t n = size_t(f.num_dofs());
+    Buffers b(n);
+    cudaMemcpy(b.u, u, n * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(b.du, du, n * 8, cudaMemcpyHostToDevice);
+    f.updateQdata(true);
+    f.residual(0.0, b.u, b.r);
+    f.updateQdata(false);
+    cudaMemcpy(r_commit, b.r, n * 8, cudaMemcpyDeviceToHost);
+    const int64_t npts = qdata->num_points();
+    std::vector<double> soa(size_t(npts) * 10);
+    cudaMemcpy(soa.data(), qdata->device(), soa.size() * 8, cudaMemcpyDeviceToHost);
+    for (int64_t q = 0; q < npts; q++)
+      for (int k = 0; k < 10; k++) state_out[q * 10 + k] = soa[size_t(k * npts + q)];
+    std::vector<double> u15(u, u + n);
+    for (auto& x : u15) x *= 1.5;
+    cudaMemcpy(b.u, u15.data(), n * 8, cudaMemcpyHostToDevice);
+    auto [rr, grad] = f(0.0, sfx::differentiate_wrt(b.u));
+    cudaMemcpy(r, rr, n * 8, cudaMemcpyDeviceToHost);
+    grad.Mult(b.du, b.jv);
+    cudaMemcpy(jv, b.jv, n * 8, cudaMemcpyDeviceToHost);
+    return cudaDeviceSynchronize() == cudaSuccess ? 0 : -2;
+  } catch (const std::exception&) {
+    return -1;
+  }
+}

@@ -1,0 +1,96 @@
+"""The header-only C++ front-end (include/sfx/functional.hpp) with user-written
+q-function objects compiled into a test library (tests/cpp/frontend_test.cu):
+residual, linearised residual, FP64 / FP32 Jacobian action, diagonal and CSR
+values against the oracle; quadrature-point state through QuadratureData."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.problems import PARAMS, fields, mesh, rel
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+SRC = os.path.join(HERE, "cpp", "frontend_test.cu")
+LIB = os.path.join(HERE, "cpp", "libsfx_frontend_test.so")
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+@pytest.fixture(scope="module")
+def felib():
+    from serac_gb300 import _lib, build
+
+    _lib.load()
+    headers = [os.path.join(ROOT, "include", "sfx", f) for f in os.listdir(os.path.join(ROOT, "include", "sfx"))]
+    newest = max([os.path.getmtime(SRC), os.path.getmtime(_lib.LIB_PATH)] + [os.path.getmtime(h) for h in headers])
+    if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
+        cmd = [build.nvcc(), *build.NVCC_FLAGS, "-shared", "-I", os.path.join(ROOT, "include"), "-o", LIB, SRC,
+               "-L", os.path.dirname(_lib.LIB_PATH), "-lsfx_gb300", "-Xlinker", "-rpath=" + os.path.dirname(_lib.LIB_PATH)]
+        subprocess.check_call(cmd)
+    lib = ctypes.CDLL(LIB)
+    return lib
+
+
+def _p(a):
+    return a.ctypes.data_as(_dp)
+
+
+@pytest.mark.parametrize("p", [1, 2])
+@pytest.mark.parametrize("kind", ["thermal", "neohookean"])
+def test_user_qfunction_matches_oracle(cuda, felib, kind, p):
+    dims = (3, 2, 2)
+    m = mesh(*dims, perturb=0.1, seed=2)
+    mat = O.MAT_THERMAL_TEST if kind == "thermal" else O.MAT_NEOHOOKEAN
+    orc = O.OracleFunctional(m, p, O.COMPONENTS[mat])
+    orc.add_domain_integral(mat, PARAMS[mat])
+    u, du = fields(orc.ndofs, mat, seed=8)
+    n = orc.ndofs
+    outs = [np.zeros(n) for _ in range(5)]
+    A = orc.assemble(u)
+    csr = np.zeros(A.nnz)
+    nnz = ctypes.c_int64()
+    V = np.ascontiguousarray(m.vertices)
+    if kind == "thermal":
+        rc = felib.frontend_thermal(p, *dims, _p(V), _p(u), _p(du), *[_p(o) for o in outs], _p(csr), ctypes.byref(nnz))
+    else:
+        K, G = PARAMS[mat]
+        rc = felib.frontend_neohookean(p, ctypes.c_double(K), ctypes.c_double(G), *dims, _p(V), _p(u), _p(du),
+                                       *[_p(o) for o in outs], _p(csr), ctypes.byref(nnz))
+    assert rc == 0
+    r, r2, jv, jv32, diag = outs
+    ref_r = orc.residual(u)
+    assert rel(r, ref_r) <= 1e-12
+    assert rel(r2, ref_r) <= 1e-12
+    ref_jv = orc.jvp(u, du)
+    assert rel(jv, ref_jv) <= 1e-12
+    assert rel(jv32, ref_jv) <= 1e-5
+    assert rel(diag, A.diagonal()) <= 1e-12
+    assert nnz.value == A.nnz
+    assert rel(csr, A.data) <= 1e-12
+
+
+def test_user_qfunction_with_quadrature_state(cuda, felib):
+    dims = (3, 2, 2)
+    m = mesh(*dims, perturb=0.1, seed=4)
+    orc = O.OracleFunctional(m, 1, 3)
+    prm = PARAMS[O.MAT_J2]
+    orc.add_domain_integral(O.MAT_J2, prm)
+    u, du = fields(orc.ndofs, O.MAT_J2, seed=13)
+    n = orc.ndofs
+    r_commit, r, jv = np.zeros(n), np.zeros(n), np.zeros(n)
+    state = np.zeros((m.ne, 8, 10))
+    V = np.ascontiguousarray(m.vertices)
+    rc = felib.frontend_j2(*dims, _p(V), _p(u), _p(du), *[ctypes.c_double(x) for x in prm], _p(r_commit), _p(state),
+                           _p(r), _p(jv))
+    assert rc == 0
+    assert rel(r_commit, orc.residual(u, update_state=True)) <= 1e-12
+    assert np.abs(state - orc.state).max() <= 1e-12 * max(1.0, np.abs(orc.state).max())
+    assert orc.state[..., 9].max() > 0
+    assert rel(r, orc.residual(1.5 * u)) <= 1e-12
+    assert rel(jv, orc.jvp(1.5 * u, du)) <= 1e-12
