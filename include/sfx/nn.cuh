@@ -1,0 +1,242 @@
+// sfx — kernels of the learned multilevel preconditioner: 3x3x3 convolutions
+// on node grids (channels-last BF16 activations, FP32 accumulation on the
+// tensor cores through mma.sync m16n8k16), grid transfer between levels, and
+// the backward passes used to train the network.
+//
+// A volume is an nx x ny x nz node grid with C channels (C a multiple of 16),
+// stored [z][y][x][C].  Convolutions use zero padding, stride 1:
+//   y[n][co] = act(b[co] + sum_{tap, ci} W[co][tap][ci] x[n + off(tap)][ci]),
+// tap = (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1).  Levels nest as 2m+1 -> m+1
+// nodes per direction (the Q2 node grid of an n^3 mesh is (2n+1)^3).
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace sfx {
+namespace nn {
+
+struct Grid3 {
+  int nx, ny, nz;
+  __host__ __device__ int64_t nodes() const { return int64_t(nx) * ny * nz; }
+};
+
+__device__ inline uint32_t pack_bf16x2(float a, float b) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+
+__device__ inline void mma_bf16_16816(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+enum Act : int { ACT_NONE = 0, ACT_RELU = 1 };
+
+/// Forward 3x3x3 convolution.  One warp computes 16 consecutive output nodes
+/// for all COUT channels (COUT/8 mma tiles); the K loop runs over the 27 taps
+/// and the input channels in chunks of 16.  x: [node][CIN] bf16, W: [COUT][27][CIN]
+/// bf16, bias: [COUT] f32 (may be null), y: [node][COUT] bf16.  If `y_f32` is
+/// non-null the pre-cast FP32 result is written there instead.
+template <int CIN, int COUT, int ACT>
+__global__ void __launch_bounds__(128) conv3_fwd(Grid3 g, const __nv_bfloat16* __restrict__ x,
+                                                 const __nv_bfloat16* __restrict__ W, const float* __restrict__ bias,
+                                                 __nv_bfloat16* __restrict__ y, float* __restrict__ y_f32) {
+  static_assert(CIN % 16 == 0 && COUT % 8 == 0, "channel counts");
+  constexpr int NT = COUT / 8;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int64_t n0 = warp * 16;
+  const int64_t N = g.nodes();
+  if (n0 >= N) return;
+  const int gid = lane >> 2, tig = lane & 3;
+  // the two rows (nodes) this lane feeds into the A fragment
+  int64_t rn[2] = {n0 + gid, n0 + gid + 8};
+  int rx[2], ry[2], rz[2];
+  bool rv[2];
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    rv[h] = rn[h] < N;
+    const int64_t nn = rv[h] ? rn[h] : 0;
+    rx[h] = int(nn % g.nx);
+    ry[h] = int((nn / g.nx) % g.ny);
+    rz[h] = int(nn / (int64_t(g.nx) * g.ny));
+  }
+  float acc[NT][4];
+#pragma unroll
+  for (int j = 0; j < NT; j++)
+#pragma unroll
+    for (int k = 0; k < 4; k++) acc[j][k] = 0.f;
+
+  const uint32_t* x32 = reinterpret_cast<const uint32_t*>(x);
+  const uint32_t* W32 = reinterpret_cast<const uint32_t*>(W);
+#pragma unroll 1
+  for (int tap = 0; tap < 27; tap++) {
+    const int dx = tap % 3 - 1, dy = (tap / 3) % 3 - 1, dz = tap / 9 - 1;
+    int64_t src[2];
+    bool sv[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int xx = rx[h] + dx, yy = ry[h] + dy, zz = rz[h] + dz;
+      sv[h] = rv[h] && xx >= 0 && xx < g.nx && yy >= 0 && yy < g.ny && zz >= 0 && zz < g.nz;
+      src[h] = sv[h] ? (int64_t(zz) * g.ny + yy) * g.nx + xx : 0;
+    }
+#pragma unroll
+    for (int kc = 0; kc < CIN / 16; kc++) {
+      const int c0 = kc * 16 + tig * 2;
+      uint32_t a[4];
+      a[0] = sv[0] ? x32[(src[0] * CIN + c0) >> 1] : 0u;
+      a[1] = sv[1] ? x32[(src[1] * CIN + c0) >> 1] : 0u;
+      a[2] = sv[0] ? x32[(src[0] * CIN + c0 + 8) >> 1] : 0u;
+      a[3] = sv[1] ? x32[(src[1] * CIN + c0 + 8) >> 1] : 0u;
+#pragma unroll
+      for (int j = 0; j < NT; j++) {
+        const int co = j * 8 + gid;
+        const int64_t wb = (int64_t(co) * 27 + tap) * CIN + c0;
+        uint32_t b[2] = {W32[wb >> 1], W32[(wb + 8) >> 1]};
+        mma_bf16_16816(acc[j], a, b);
+      }
+    }
+  }
+  // epilogue: rows gid / gid+8, columns j*8 + tig*2 + {0,1}
+#pragma unroll
+  for (int j = 0; j < NT; j++) {
+    const int co = j * 8 + tig * 2;
+    const float b0 = bias ? bias[co] : 0.f, b1 = bias ? bias[co + 1] : 0.f;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      if (!rv[h]) continue;
+      float v0 = acc[j][2 * h] + b0, v1 = acc[j][2 * h + 1] + b1;
+      if (ACT == ACT_RELU) {
+        v0 = v0 > 0.f ? v0 : 0.f;
+        v1 = v1 > 0.f ? v1 : 0.f;
+      }
+      if (y_f32) {
+        y_f32[rn[h] * COUT + co] = v0;
+        y_f32[rn[h] * COUT + co + 1] = v1;
+      } else {
+        reinterpret_cast<uint32_t*>(y)[(rn[h] * COUT + co) >> 1] = pack_bf16x2(v0, v1);
+      }
+    }
+  }
+}
+
+/// Weights of the data-gradient convolution: Wt[ci][tap][co] = W[co][26 - tap][ci].
+template <int CIN, int COUT>
+__global__ void flip_weights(const __nv_bfloat16* __restrict__ W, __nv_bfloat16* __restrict__ Wt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= CIN * 27 * COUT) return;
+  const int co = i % COUT, tap = (i / COUT) % 27, ci = i / (COUT * 27);
+  Wt[(int64_t(ci) * 27 + tap) * COUT + co] = W[(int64_t(co) * 27 + (26 - tap)) * CIN + ci];
+}
+
+/// Weight gradient partials: part[blk][co][tap][ci] = sum over the block's node
+/// chunk of dy[n][co] x[n + off(tap)][ci] (FP32).  grid = (chunks), threads over
+/// (co, ci) pairs and taps.  Reduced in fixed order by reduce_chunks.
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(256) conv3_wgrad_partial(Grid3 g, const __nv_bfloat16* __restrict__ x,
+                                                           const float* __restrict__ dy, int64_t chunk,
+                                                           float* __restrict__ part) {
+  const int64_t N = g.nodes();
+  const int64_t b0 = int64_t(blockIdx.x) * chunk;
+  const int64_t b1 = b0 + chunk < N ? b0 + chunk : N;
+  float* out = part + int64_t(blockIdx.x) * COUT * 27 * CIN;
+  for (int p = threadIdx.x; p < COUT * 27 * CIN; p += blockDim.x) {
+    const int ci = p % CIN, tap = (p / CIN) % 27, co = p / (CIN * 27);
+    const int ox = tap % 3 - 1, oy = (tap / 3) % 3 - 1, oz = tap / 9 - 1;
+    float acc = 0.f;
+    for (int64_t n = b0; n < b1; n++) {
+      const int xx = int(n % g.nx) + ox, yy = int((n / g.nx) % g.ny) + oy, zz = int(n / (int64_t(g.nx) * g.ny)) + oz;
+      if (xx < 0 || xx >= g.nx || yy < 0 || yy >= g.ny || zz < 0 || zz >= g.nz) continue;
+      const int64_t s = (int64_t(zz) * g.ny + yy) * g.nx + xx;
+      acc += dy[n * COUT + co] * __bfloat162float(x[s * CIN + ci]);
+    }
+    out[p] = acc;
+  }
+}
+
+/// out[i] = sum_b part[b][i] (fixed order), optionally into a bias gradient too.
+__global__ void reduce_chunks(const float* __restrict__ part, int nchunks, int64_t len, float* __restrict__ out) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= len) return;
+  float acc = 0.f;
+  for (int b = 0; b < nchunks; b++) acc += part[int64_t(b) * len + i];
+  out[i] = acc;
+}
+
+/// bias gradient db[co] = sum_n dy[n][co] (one block per channel, fixed-order tree)
+template <int COUT>
+__global__ void __launch_bounds__(256) bias_grad(const float* __restrict__ dy, int64_t N, float* __restrict__ db) {
+  __shared__ float sh[256];
+  const int co = blockIdx.x;
+  float acc = 0.f;
+  for (int64_t n = threadIdx.x; n < N; n += 256) acc += dy[n * COUT + co];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) db[co] = sh[0];
+}
+
+template <typename T>
+__device__ inline float to_f(T v) {
+  return float(v);
+}
+template <>
+__device__ inline float to_f<__nv_bfloat16>(__nv_bfloat16 v) {
+  return __bfloat162float(v);
+}
+
+/// Prolongation from the (m+1)-grid to the (2m+1)-grid by trilinear
+/// interpolation (per channel), added into fine: fine += scale * P coarse.
+template <typename T>
+__global__ void prolong_add(Grid3 fg, Grid3 cg, int C, const T* __restrict__ coarse, float* __restrict__ fine,
+                            float scale) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= fg.nodes() * C) return;
+  const int c = int(i % C);
+  const int64_t n = i / C;
+  const int x = int(n % fg.nx), y = int((n / fg.nx) % fg.ny), z = int(n / (int64_t(fg.nx) * fg.ny));
+  const int x0 = x >> 1, y0 = y >> 1, z0 = z >> 1;
+  const int x1 = x0 + (x & 1), y1 = y0 + (y & 1), z1 = z0 + (z & 1);
+  float v = 0.f;
+  const int xs[2] = {x0, x1}, ys[2] = {y0, y1}, zs[2] = {z0, z1};
+  for (int a = 0; a < 2; a++)
+    for (int b = 0; b < 2; b++)
+      for (int d = 0; d < 2; d++) {
+        const int64_t cn = (int64_t(zs[a]) * cg.ny + ys[b]) * cg.nx + xs[d];
+        v += 0.125f * to_f(coarse[cn * C + c]);
+      }
+  fine[i] += scale * v;
+}
+
+/// Restriction coarse = scale * P^T fine (scale 1/8: full weighting), any input type.
+template <typename T, typename U>
+__global__ void restrict_to(Grid3 fg, Grid3 cg, int C, const T* __restrict__ fine, U* __restrict__ coarse,
+                            float scale) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= cg.nodes() * C) return;
+  const int c = int(i % C);
+  const int64_t n = i / C;
+  const int X = int(n % cg.nx), Y = int((n / cg.nx) % cg.ny), Z = int(n / (int64_t(cg.nx) * cg.ny));
+  float v = 0.f;
+  for (int dz = -1; dz <= 1; dz++)
+    for (int dy = -1; dy <= 1; dy++)
+      for (int dx = -1; dx <= 1; dx++) {
+        const int x = 2 * X + dx, y = 2 * Y + dy, z = 2 * Z + dz;
+        if (x < 0 || x >= fg.nx || y < 0 || y >= fg.ny || z < 0 || z >= fg.nz) continue;
+        const float w = (dx ? 0.5f : 1.f) * (dy ? 0.5f : 1.f) * (dz ? 0.5f : 1.f);
+        v += w * to_f(fine[((int64_t(z) * fg.ny + y) * fg.nx + x) * C + c]);
+      }
+  coarse[i] = U(scale * v);
+}
+
+}  // namespace nn
+}  // namespace sfx

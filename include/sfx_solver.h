@@ -31,6 +31,12 @@ extern "C" {
 #define SFX_PREC_NONE 0
 #define SFX_PREC_JACOBI 1
 #define SFX_PREC_JACOBI_CHEBYSHEV 2
+/* Learned multilevel network (include/sfx_learned.h) followed by one FP32
+ * Jacobi-Chebyshev application on what it leaves of the residual; when the
+ * network's step does not reduce the residual, Jacobi-Chebyshev alone
+ * (counted in sfx_solver_stats.learned_fallbacks).  Implies flexible GMRES
+ * with FP32 inner work (mixed precision). */
+#define SFX_PREC_LEARNED 3
 
 typedef struct {
   int max_newton_iterations; /* 20 */
@@ -59,6 +65,8 @@ typedef struct {
   double initial_residual;
   double final_residual;
   double last_krylov_rel;
+  int learned_applications; /* network preconditioner applications */
+  int learned_fallbacks;    /* of which fell back to Jacobi-Chebyshev */
 } sfx_solver_stats;
 
 typedef struct sfx_solver_s* sfx_solver;
@@ -74,6 +82,10 @@ int sfx_solver_solve(sfx_solver solver, double t, double* u, void* stream);
 int sfx_solver_solve_linear(sfx_solver solver, double t, const double* u_lin, const double* rhs, double* x,
                             void* stream);
 int sfx_solver_get_stats(sfx_solver solver, sfx_solver_stats* out);
+/* Network for SFX_PREC_LEARNED: the form's node grid (order * n + 1 nodes per
+ * direction) and per-node features (device, [2][num_nodes] floats: log
+ * modulus feature, Dirichlet mask), kept by reference. */
+int sfx_solver_set_learned(sfx_solver solver, struct sfx_lnet_s* net, int nx, int ny, int nz, const float* features);
 
 #ifdef __cplusplus
 }

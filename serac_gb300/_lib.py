@@ -57,6 +57,17 @@ SIGNATURES = {
     "sfx_qdata_size": (_c.c_int, [_vp, _i64p]),
     "sfx_set_qdata": (_c.c_int, [_vp, _dp]),
     "sfx_get_qdata": (_c.c_int, [_vp, _dp]),
+    # include/sfx_learned.h
+    "sfx_lnet_create": (_c.c_int, [_c.c_uint64, _c.POINTER(_vp)]),
+    "sfx_lnet_destroy": (_c.c_int, [_vp]),
+    "sfx_lnet_num_params": (_c.c_int, [_vp, _i64p]),
+    "sfx_lnet_get_params": (_c.c_int, [_vp, _c.POINTER(_c.c_float), _c.c_int64]),
+    "sfx_lnet_set_params": (_c.c_int, [_vp, _c.POINTER(_c.c_float), _c.c_int64]),
+    "sfx_lnet_apply": (_c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _vp, _vp, _vp, _vp]),
+    "sfx_lnet_gradient": (_c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _vp, _vp, _vp, _c.POINTER(_c.c_float),
+                                     _c.POINTER(_c.c_float), _vp]),
+    "sfx_lnet_train_step": (_c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _vp, _vp, _vp, _c.c_float,
+                                       _c.POINTER(_c.c_float), _vp]),
     # include/sfx_solver.h (struct arguments passed by address)
     "sfx_solver_default_options": (_c.c_int, [_vp]),
     "sfx_solver_create": (_c.c_int, [_vp, _vp, _c.POINTER(_vp)]),
@@ -65,6 +76,7 @@ SIGNATURES = {
     "sfx_solver_solve": (_c.c_int, [_vp, _c.c_double, _vp, _vp]),
     "sfx_solver_solve_linear": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp, _vp]),
     "sfx_solver_get_stats": (_c.c_int, [_vp, _vp]),
+    "sfx_solver_set_learned": (_c.c_int, [_vp, _vp, _c.c_int, _c.c_int, _c.c_int, _vp]),
 }
 
 _LIB = None

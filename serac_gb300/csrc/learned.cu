@@ -1,0 +1,491 @@
+// Learned multilevel preconditioner: network state, forward / backward
+// orchestration and Adam (the architecture is described in include/sfx_learned.h).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <new>
+#include <random>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "form.hpp"
+#include "learned_internal.hpp"
+#include "sfx.h"
+#include "sfx/nn.cuh"
+#include "sfx_learned.h"
+
+using namespace sfx_impl;
+using sfx::nn::Grid3;
+using bf16 = __nv_bfloat16;
+
+namespace {
+
+inline unsigned nb(int64_t n, int b = 256) { return unsigned((n + b - 1) / b); }
+
+// ----------------------------------------------------------- small kernels
+__global__ void f32_to_bf16(const float* __restrict__ a, bf16* __restrict__ b, int64_t n) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = __float2bfloat16(a[i]);
+}
+// g_pre = g * (y > 0) (ReLU backward), as fp32 and bf16; relu = false copies
+__global__ void act_bwd(const float* __restrict__ g, const bf16* __restrict__ y, bool relu, float* __restrict__ gp,
+                        bf16* __restrict__ gp16, int64_t n) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float v = (!relu || __bfloat162float(y[i]) > 0.f) ? g[i] : 0.f;
+  gp[i] = v;
+  gp16[i] = __float2bfloat16(v);
+}
+__global__ void add_into(const float* __restrict__ a, float* __restrict__ b, int64_t n) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) b[i] += a[i];
+}
+// d = float(a) + float(b) ; and its bf16 copy
+__global__ void add_bf16_into(const bf16* __restrict__ a, float* __restrict__ d, bf16* __restrict__ d16, int64_t n) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float v = d[i] + __bfloat162float(a[i]);
+  d[i] = v;
+  d16[i] = __float2bfloat16(v);
+}
+// x0[n][0..15] = {r/s (3), feature, mask, 0...}
+__global__ void pack_input(const float* __restrict__ r, const float* __restrict__ feat, int64_t N, float inv_s,
+                           bf16* __restrict__ x0) {
+  int64_t n = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  float v[16] = {};
+  for (int c = 0; c < 3; c++) v[c] = r[c * N + n] * inv_s;
+  v[3] = feat[n];
+  v[4] = feat[N + n];
+  for (int c = 0; c < 16; c++) x0[n * 16 + c] = __float2bfloat16(v[c]);
+}
+// z[c N + n] = s out[n][c] (0 on masked nodes)
+__global__ void unpack_output(const float* __restrict__ out, const float* __restrict__ feat, int64_t N, float s,
+                              float* __restrict__ z) {
+  int64_t n = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const bool masked = feat[N + n] > 0.5f;
+  for (int c = 0; c < 3; c++) z[c * N + n] = masked ? 0.f : s * out[n * 16 + c];
+}
+// squared error per node and gradient of loss = sum |out - t/s|^2 / tt
+__global__ void loss_grad(const float* __restrict__ out, const float* __restrict__ t, const float* __restrict__ feat,
+                          int64_t N, float inv_s, float inv_tt, float* __restrict__ g, float* __restrict__ err) {
+  int64_t n = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const bool masked = feat[N + n] > 0.5f;
+  float e = 0.f;
+  for (int c = 0; c < 16; c++) {
+    float d = 0.f;
+    if (c < 3 && !masked) d = out[n * 16 + c] - t[c * N + n] * inv_s;
+    g[n * 16 + c] = 2.f * d * inv_tt;
+    e += d * d;
+  }
+  err[n] = e;
+}
+__global__ void target_sq(const float* __restrict__ t, const float* __restrict__ feat, int64_t N, float inv_s,
+                          float* __restrict__ out) {
+  int64_t n = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  float e = 0.f;
+  if (feat[N + n] <= 0.5f)
+    for (int c = 0; c < 3; c++) {
+      const float v = t[c * N + n] * inv_s;
+      e += v * v;
+    }
+  out[n] = e;
+}
+__global__ void square(const float* __restrict__ a, float* __restrict__ b, int64_t n) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = a[i] * a[i];
+}
+// fixed-order sum in double (single block)
+__global__ void __launch_bounds__(256) sum_f32(const float* __restrict__ a, int64_t n, float* __restrict__ out) {
+  __shared__ double sh[256];
+  double acc = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += 256) acc += a[i];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = float(sh[0]);
+}
+__global__ void adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
+                     int64_t n, float lr, float b1, float b2, float c1, float c2, float eps, float gscale) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i] * gscale;
+  m[i] = b1 * m[i] + (1.f - b1) * gi;
+  v[i] = b2 * v[i] + (1.f - b2) * gi * gi;
+  p[i] -= lr * (m[i] / c1) / (sqrtf(v[i] / c2) + eps);
+}
+
+// --------------------------------------------------------- conv dispatch
+#define SFX_PAIRS(X) X(16, 16) X(16, 32) X(32, 32) X(32, 48) X(48, 48) X(48, 32) X(32, 16)
+
+void conv_fwd(int ci, int co, bool relu, Grid3 g, const bf16* x, const bf16* W, const float* b, bf16* y, float* y32,
+              cudaStream_t s) {
+  const unsigned blocks = nb(((g.nodes() + 15) / 16) * 32, 128);
+#define SFX_CONV(CI, CO)                                                                                   \
+  if (ci == CI && co == CO) {                                                                              \
+    if (relu) sfx::nn::conv3_fwd<CI, CO, sfx::nn::ACT_RELU><<<blocks, 128, 0, s>>>(g, x, W, b, y, y32);    \
+    else sfx::nn::conv3_fwd<CI, CO, sfx::nn::ACT_NONE><<<blocks, 128, 0, s>>>(g, x, W, b, y, y32);         \
+    return;                                                                                                \
+  }
+  SFX_PAIRS(SFX_CONV)
+#undef SFX_CONV
+}
+void conv_wgrad(int ci, int co, Grid3 g, const bf16* x, const float* dy, float* part, int nchunks, int64_t chunk,
+                cudaStream_t s) {
+#define SFX_WG(CI, CO)                                                                        \
+  if (ci == CI && co == CO) {                                                                 \
+    sfx::nn::conv3_wgrad_partial<CI, CO><<<nchunks, 256, 0, s>>>(g, x, dy, chunk, part);      \
+    return;                                                                                   \
+  }
+  SFX_PAIRS(SFX_WG)
+#undef SFX_WG
+}
+void flip(int ci, int co, const bf16* W, bf16* Wt, cudaStream_t s) {
+#define SFX_FL(CI, CO)                                                              \
+  if (ci == CI && co == CO) {                                                       \
+    sfx::nn::flip_weights<CI, CO><<<nb(CI * 27 * CO), 256, 0, s>>>(W, Wt);          \
+    return;                                                                         \
+  }
+  SFX_PAIRS(SFX_FL)
+#undef SFX_FL
+}
+void bias_grad(int co, const float* dy, int64_t N, float* db, cudaStream_t s) {
+  if (co == 16) sfx::nn::bias_grad<16><<<16, 256, 0, s>>>(dy, N, db);
+  else if (co == 32) sfx::nn::bias_grad<32><<<32, 256, 0, s>>>(dy, N, db);
+  else sfx::nn::bias_grad<48><<<48, 256, 0, s>>>(dy, N, db);
+}
+
+struct Conv {
+  int ci, co;
+  bool relu;
+  int64_t off;  // offset of W in the parameter vector (b follows)
+  int64_t nw() const { return int64_t(co) * 27 * ci; }
+};
+
+enum { A0, B0L, A1, B1L, A2, B2L, A3, U2, U1, U0, OUTL, NLAYERS };
+constexpr int kMaxChunks = 64;
+
+struct Work {
+  Grid3 g[4];
+  DeviceBuf<bf16> X0, A0b, B0b, C1, A1b, B1b, C2, A2b, B2b, C3, A3b, D2b, E2, D1b, E1, D0b, E0;
+  DeviceBuf<float> D2, D1, D0, OUT;
+  DeviceBuf<float> gOUT, gE0, gD0, gE1, gD1, gE2, gD2, gA3, gC3, gB2, gA2, gC2, gB1, gA1, gC1, gB0, gA0, gpre, tmpf;
+  DeviceBuf<bf16> gpre16;
+  DeviceBuf<float> part, red, err, scal;
+};
+
+}  // namespace
+
+struct sfx_lnet_s {
+  Conv layers[NLAYERS];
+  int64_t nparams = 0;
+  DeviceBuf<float> P, G, M, V;  // master parameters, gradient, Adam moments
+  DeviceBuf<bf16> W16[NLAYERS], Wt16[NLAYERS];
+  int64_t step = 0;
+  std::map<std::tuple<int, int, int>, std::unique_ptr<Work>> work;
+};
+
+namespace {
+
+int sync_weights(sfx_lnet net, cudaStream_t s) {
+  for (int l = 0; l < NLAYERS; l++) {
+    const Conv& c = net->layers[l];
+    f32_to_bf16<<<nb(c.nw()), 256, 0, s>>>(net->P.p + c.off, net->W16[l].p, c.nw());
+    flip(c.ci, c.co, net->W16[l].p, net->Wt16[l].p, s);
+  }
+  SFX_CUDA_TRY(cudaGetLastError());
+  return SFX_OK;
+}
+
+Grid3 coarse_of(Grid3 f) { return Grid3{(f.nx + 1) / 2, (f.ny + 1) / 2, (f.nz + 1) / 2}; }
+
+int get_work(sfx_lnet net, int nx, int ny, int nz, Work** out) {
+  for (int n : {nx, ny, nz})
+    if (n < 9 || (n - 1) % 8 != 0) return fail(SFX_ERR_UNSUPPORTED, "node grid must have 8k+1 nodes per direction");
+  auto key = std::make_tuple(nx, ny, nz);
+  auto it = net->work.find(key);
+  if (it != net->work.end()) {
+    *out = it->second.get();
+    return SFX_OK;
+  }
+  auto w = std::make_unique<Work>();
+  w->g[0] = Grid3{nx, ny, nz};
+  for (int l = 1; l < 4; l++) w->g[l] = coarse_of(w->g[l - 1]);
+  const size_t N0 = size_t(w->g[0].nodes()), N1 = size_t(w->g[1].nodes()), N2 = size_t(w->g[2].nodes()),
+               N3 = size_t(w->g[3].nodes());
+  std::vector<std::pair<DeviceBuf<bf16>*, size_t>> b16 = {
+      {&w->X0, N0 * 16}, {&w->A0b, N0 * 16}, {&w->B0b, N0 * 16}, {&w->C1, N1 * 16},  {&w->A1b, N1 * 32},
+      {&w->B1b, N1 * 32}, {&w->C2, N2 * 32}, {&w->A2b, N2 * 48}, {&w->B2b, N2 * 48}, {&w->C3, N3 * 48},
+      {&w->A3b, N3 * 48}, {&w->D2b, N2 * 48}, {&w->E2, N2 * 32}, {&w->D1b, N1 * 32}, {&w->E1, N1 * 16},
+      {&w->D0b, N0 * 16}, {&w->E0, N0 * 16}};
+  bool ok = true;
+  for (auto& e : b16) ok = ok && e.first->alloc(e.second) == cudaSuccess;
+  ok = ok && w->D2.alloc(N2 * 48) == cudaSuccess && w->D1.alloc(N1 * 32) == cudaSuccess &&
+       w->D0.alloc(N0 * 16) == cudaSuccess && w->OUT.alloc(N0 * 16) == cudaSuccess;
+  const size_t big = std::max({N0 * 16, N1 * 32, N2 * 48});
+  for (auto* b : {&w->gOUT, &w->gE0, &w->gD0, &w->gE1, &w->gD1, &w->gE2, &w->gD2, &w->gA3, &w->gC3, &w->gB2, &w->gA2,
+                  &w->gC2, &w->gB1, &w->gA1, &w->gC1, &w->gB0, &w->gA0, &w->gpre, &w->tmpf})
+    ok = ok && b->alloc(big) == cudaSuccess;
+  ok = ok && w->gpre16.alloc(big) == cudaSuccess;
+  ok = ok && w->part.alloc(size_t(kMaxChunks) * 48 * 27 * 48) == cudaSuccess &&
+       w->red.alloc(size_t(48) * 27 * 48) == cudaSuccess && w->err.alloc(N0) == cudaSuccess &&
+       w->scal.alloc(4) == cudaSuccess;
+  if (!ok) return fail(SFX_ERR_NOMEM, "network workspace allocation failed");
+  *out = w.get();
+  net->work[key] = std::move(w);
+  return SFX_OK;
+}
+
+float read_scalar(const float* d, cudaStream_t s, int* rc) {
+  float h = 0.f;
+  cudaError_t e = cudaMemcpyAsync(&h, d, sizeof(float), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  *rc = e == cudaSuccess ? SFX_OK : fail(SFX_ERR_CUDA, std::string("scalar read: ") + cudaGetErrorString(e));
+  return h;
+}
+
+const float* bias_of(sfx_lnet net, int l) { return net->P.p + net->layers[l].off + net->layers[l].nw(); }
+
+void forward(sfx_lnet net, Work* w, cudaStream_t s) {
+  const Grid3* g = w->g;
+  const int64_t N0 = g[0].nodes(), N1 = g[1].nodes(), N2 = g[2].nodes(), N3 = g[3].nodes();
+  conv_fwd(16, 16, true, g[0], w->X0.p, net->W16[A0].p, bias_of(net, A0), w->A0b.p, nullptr, s);
+  conv_fwd(16, 16, true, g[0], w->A0b.p, net->W16[B0L].p, bias_of(net, B0L), w->B0b.p, nullptr, s);
+  sfx::nn::restrict_to<bf16, bf16><<<nb(N1 * 16), 256, 0, s>>>(g[0], g[1], 16, w->B0b.p, w->C1.p, 0.125f);
+  conv_fwd(16, 32, true, g[1], w->C1.p, net->W16[A1].p, bias_of(net, A1), w->A1b.p, nullptr, s);
+  conv_fwd(32, 32, true, g[1], w->A1b.p, net->W16[B1L].p, bias_of(net, B1L), w->B1b.p, nullptr, s);
+  sfx::nn::restrict_to<bf16, bf16><<<nb(N2 * 32), 256, 0, s>>>(g[1], g[2], 32, w->B1b.p, w->C2.p, 0.125f);
+  conv_fwd(32, 48, true, g[2], w->C2.p, net->W16[A2].p, bias_of(net, A2), w->A2b.p, nullptr, s);
+  conv_fwd(48, 48, true, g[2], w->A2b.p, net->W16[B2L].p, bias_of(net, B2L), w->B2b.p, nullptr, s);
+  sfx::nn::restrict_to<bf16, bf16><<<nb(N3 * 48), 256, 0, s>>>(g[2], g[3], 48, w->B2b.p, w->C3.p, 0.125f);
+  conv_fwd(48, 48, true, g[3], w->C3.p, net->W16[A3].p, bias_of(net, A3), w->A3b.p, nullptr, s);
+  // D2 = P A3 + B2 ; E2 = relu(conv(D2))
+  cudaMemsetAsync(w->D2.p, 0, sizeof(float) * N2 * 48, s);
+  sfx::nn::prolong_add<bf16><<<nb(N2 * 48), 256, 0, s>>>(g[2], g[3], 48, w->A3b.p, w->D2.p, 1.f);
+  add_bf16_into<<<nb(N2 * 48), 256, 0, s>>>(w->B2b.p, w->D2.p, w->D2b.p, N2 * 48);
+  conv_fwd(48, 32, true, g[2], w->D2b.p, net->W16[U2].p, bias_of(net, U2), w->E2.p, nullptr, s);
+  cudaMemsetAsync(w->D1.p, 0, sizeof(float) * N1 * 32, s);
+  sfx::nn::prolong_add<bf16><<<nb(N1 * 32), 256, 0, s>>>(g[1], g[2], 32, w->E2.p, w->D1.p, 1.f);
+  add_bf16_into<<<nb(N1 * 32), 256, 0, s>>>(w->B1b.p, w->D1.p, w->D1b.p, N1 * 32);
+  conv_fwd(32, 16, true, g[1], w->D1b.p, net->W16[U1].p, bias_of(net, U1), w->E1.p, nullptr, s);
+  cudaMemsetAsync(w->D0.p, 0, sizeof(float) * N0 * 16, s);
+  sfx::nn::prolong_add<bf16><<<nb(N0 * 16), 256, 0, s>>>(g[0], g[1], 16, w->E1.p, w->D0.p, 1.f);
+  add_bf16_into<<<nb(N0 * 16), 256, 0, s>>>(w->B0b.p, w->D0.p, w->D0b.p, N0 * 16);
+  conv_fwd(16, 16, true, g[0], w->D0b.p, net->W16[U0].p, bias_of(net, U0), w->E0.p, nullptr, s);
+  conv_fwd(16, 16, false, g[0], w->E0.p, net->W16[OUTL].p, bias_of(net, OUTL), nullptr, w->OUT.p, s);
+}
+
+// backward through one convolution: given the gradient of its output (post
+// activation) gy, accumulate dW, db into G and write the input gradient to gx
+// (fp32, overwritten) unless gx is null.
+void conv_bwd(sfx_lnet net, Work* w, int l, Grid3 g, const bf16* x, const bf16* y, const float* gy, float* gx,
+              cudaStream_t s) {
+  const Conv& c = net->layers[l];
+  const int64_t N = g.nodes();
+  act_bwd<<<nb(N * c.co), 256, 0, s>>>(gy, y, c.relu, w->gpre.p, w->gpre16.p, N * c.co);
+  const int64_t chunk = std::max<int64_t>(1, (N + kMaxChunks - 1) / kMaxChunks);
+  const int nch = int((N + chunk - 1) / chunk);
+  conv_wgrad(c.ci, c.co, g, x, w->gpre.p, w->part.p, nch, chunk, s);
+  sfx::nn::reduce_chunks<<<nb(c.nw()), 256, 0, s>>>(w->part.p, nch, c.nw(), w->red.p);
+  add_into<<<nb(c.nw()), 256, 0, s>>>(w->red.p, net->G.p + c.off, c.nw());
+  bias_grad(c.co, w->gpre.p, N, w->red.p, s);
+  add_into<<<1, 64, 0, s>>>(w->red.p, net->G.p + c.off + c.nw(), c.co);
+  if (gx) conv_fwd(c.co, c.ci, false, g, w->gpre16.p, net->Wt16[l].p, nullptr, nullptr, gx, s);
+}
+
+void backward(sfx_lnet net, Work* w, cudaStream_t s) {
+  const Grid3* g = w->g;
+  const int64_t N0 = g[0].nodes(), N1 = g[1].nodes(), N2 = g[2].nodes();
+  // output and up path
+  conv_bwd(net, w, OUTL, g[0], w->E0.p, nullptr, w->gOUT.p, w->gE0.p, s);
+  conv_bwd(net, w, U0, g[0], w->D0b.p, w->E0.p, w->gE0.p, w->gD0.p, s);
+  cudaMemcpyAsync(w->gB0.p, w->gD0.p, sizeof(float) * N0 * 16, cudaMemcpyDeviceToDevice, s);
+  sfx::nn::restrict_to<float, float><<<nb(N1 * 16), 256, 0, s>>>(g[0], g[1], 16, w->gD0.p, w->gE1.p, 1.f);
+  conv_bwd(net, w, U1, g[1], w->D1b.p, w->E1.p, w->gE1.p, w->gD1.p, s);
+  cudaMemcpyAsync(w->gB1.p, w->gD1.p, sizeof(float) * N1 * 32, cudaMemcpyDeviceToDevice, s);
+  sfx::nn::restrict_to<float, float><<<nb(N2 * 32), 256, 0, s>>>(g[1], g[2], 32, w->gD1.p, w->gE2.p, 1.f);
+  conv_bwd(net, w, U2, g[2], w->D2b.p, w->E2.p, w->gE2.p, w->gD2.p, s);
+  cudaMemcpyAsync(w->gB2.p, w->gD2.p, sizeof(float) * N2 * 48, cudaMemcpyDeviceToDevice, s);
+  sfx::nn::restrict_to<float, float><<<nb(g[3].nodes() * 48), 256, 0, s>>>(g[2], g[3], 48, w->gD2.p, w->gA3.p, 1.f);
+  // coarsest and down path
+  conv_bwd(net, w, A3, g[3], w->C3.p, w->A3b.p, w->gA3.p, w->gC3.p, s);
+  sfx::nn::prolong_add<float><<<nb(N2 * 48), 256, 0, s>>>(g[2], g[3], 48, w->gC3.p, w->gB2.p, 0.125f);
+  conv_bwd(net, w, B2L, g[2], w->A2b.p, w->B2b.p, w->gB2.p, w->gA2.p, s);
+  conv_bwd(net, w, A2, g[2], w->C2.p, w->A2b.p, w->gA2.p, w->gC2.p, s);
+  sfx::nn::prolong_add<float><<<nb(N1 * 32), 256, 0, s>>>(g[1], g[2], 32, w->gC2.p, w->gB1.p, 0.125f);
+  conv_bwd(net, w, B1L, g[1], w->A1b.p, w->B1b.p, w->gB1.p, w->gA1.p, s);
+  conv_bwd(net, w, A1, g[1], w->C1.p, w->A1b.p, w->gA1.p, w->gC1.p, s);
+  sfx::nn::prolong_add<float><<<nb(N0 * 16), 256, 0, s>>>(g[0], g[1], 16, w->gC1.p, w->gB0.p, 0.125f);
+  conv_bwd(net, w, B0L, g[0], w->A0b.p, w->B0b.p, w->gB0.p, w->gA0.p, s);
+  conv_bwd(net, w, A0, g[0], w->X0.p, w->A0b.p, w->gA0.p, nullptr, s);
+}
+
+// one sample: forward, loss, backward (gradient accumulated into net->G)
+int sample_grad(sfx_lnet net, Work* w, const float* r, const float* t, const float* feat, float* loss,
+                cudaStream_t s) {
+  const int64_t N = w->g[0].nodes();
+  int rc = SFX_OK;
+  square<<<nb(3 * N), 256, 0, s>>>(r, w->tmpf.p, 3 * N);
+  sum_f32<<<1, 256, 0, s>>>(w->tmpf.p, 3 * N, w->scal.p);
+  const float ss = read_scalar(w->scal.p, s, &rc);
+  if (rc) return rc;
+  const float sc = ss > 0.f ? std::sqrt(ss / float(3 * N)) : 1.f;
+  pack_input<<<nb(N), 256, 0, s>>>(r, feat, N, 1.f / sc, w->X0.p);
+  forward(net, w, s);
+  target_sq<<<nb(N), 256, 0, s>>>(t, feat, N, 1.f / sc, w->tmpf.p);
+  sum_f32<<<1, 256, 0, s>>>(w->tmpf.p, N, w->scal.p);
+  const float tt = read_scalar(w->scal.p, s, &rc);
+  if (rc) return rc;
+  const float inv_tt = tt > 0.f ? 1.f / tt : 0.f;
+  loss_grad<<<nb(N), 256, 0, s>>>(w->OUT.p, t, feat, N, 1.f / sc, inv_tt, w->gOUT.p, w->err.p);
+  sum_f32<<<1, 256, 0, s>>>(w->err.p, N, w->scal.p);
+  const float e = read_scalar(w->scal.p, s, &rc);
+  if (rc) return rc;
+  *loss = e * inv_tt;
+  backward(net, w, s);
+  SFX_CUDA_TRY(cudaGetLastError());
+  return SFX_OK;
+}
+
+}  // namespace
+
+namespace sfx_impl {
+
+int lnet_apply(sfx_lnet net, int nx, int ny, int nz, const float* r, const float* features, float* z,
+               cudaStream_t s) {
+  Work* w = nullptr;
+  if (int rc = get_work(net, nx, ny, nz, &w)) return rc;
+  const int64_t N = w->g[0].nodes();
+  int rc = SFX_OK;
+  square<<<nb(3 * N), 256, 0, s>>>(r, w->tmpf.p, 3 * N);
+  sum_f32<<<1, 256, 0, s>>>(w->tmpf.p, 3 * N, w->scal.p);
+  const float ss = read_scalar(w->scal.p, s, &rc);
+  if (rc) return rc;
+  const float sc = ss > 0.f ? std::sqrt(ss / float(3 * N)) : 1.f;
+  pack_input<<<nb(N), 256, 0, s>>>(r, features, N, 1.f / sc, w->X0.p);
+  forward(net, w, s);
+  unpack_output<<<nb(N), 256, 0, s>>>(w->OUT.p, features, N, sc, z);
+  SFX_CUDA_TRY(cudaGetLastError());
+  return SFX_OK;
+}
+
+}  // namespace sfx_impl
+
+extern "C" {
+
+int sfx_lnet_create(uint64_t seed, sfx_lnet* out) {
+  if (!out) return fail(SFX_ERR_INVALID, "null output");
+  *out = nullptr;
+  auto* net = new (std::nothrow) sfx_lnet_s;
+  if (!net) return fail(SFX_ERR_NOMEM, "host allocation failed");
+  const int spec[NLAYERS][3] = {{16, 16, 1}, {16, 16, 1}, {16, 32, 1}, {32, 32, 1}, {32, 48, 1}, {48, 48, 1},
+                                {48, 48, 1}, {48, 32, 1}, {32, 16, 1}, {16, 16, 1}, {16, 16, 0}};
+  int64_t off = 0;
+  for (int l = 0; l < NLAYERS; l++) {
+    net->layers[l] = Conv{spec[l][0], spec[l][1], spec[l][2] != 0, off};
+    off += net->layers[l].nw() + spec[l][1];
+  }
+  net->nparams = off;
+  std::vector<float> p(size_t(off), 0.f);
+  std::mt19937_64 rng(seed);
+  for (int l = 0; l < NLAYERS; l++) {
+    const Conv& c = net->layers[l];
+    std::normal_distribution<double> nd(0.0, std::sqrt(2.0 / (27.0 * c.ci)) * (c.relu ? 1.0 : 0.1));
+    for (int64_t i = 0; i < c.nw(); i++) p[size_t(c.off + i)] = float(nd(rng));
+  }
+  bool ok = net->P.upload(p.data(), p.size()) == cudaSuccess && net->G.alloc(p.size()) == cudaSuccess &&
+            net->M.alloc(p.size()) == cudaSuccess && net->V.alloc(p.size()) == cudaSuccess;
+  for (int l = 0; l < NLAYERS && ok; l++)
+    ok = net->W16[l].alloc(size_t(net->layers[l].nw())) == cudaSuccess &&
+         net->Wt16[l].alloc(size_t(net->layers[l].nw())) == cudaSuccess;
+  if (ok) ok = cudaMemset(net->M.p, 0, p.size() * 4) == cudaSuccess && cudaMemset(net->V.p, 0, p.size() * 4) == cudaSuccess;
+  if (!ok || sync_weights(net, nullptr) != SFX_OK || cudaDeviceSynchronize() != cudaSuccess) {
+    delete net;
+    return fail(SFX_ERR_NOMEM, "network allocation failed");
+  }
+  *out = net;
+  return SFX_OK;
+}
+
+int sfx_lnet_destroy(sfx_lnet net) {
+  delete net;
+  return SFX_OK;
+}
+
+int sfx_lnet_num_params(sfx_lnet net, int64_t* n) {
+  if (!net || !n) return fail(SFX_ERR_INVALID, "null argument");
+  *n = net->nparams;
+  return SFX_OK;
+}
+
+int sfx_lnet_get_params(sfx_lnet net, float* host, int64_t n) {
+  if (!net || !host || n != net->nparams) return fail(SFX_ERR_INVALID, "bad parameter buffer");
+  SFX_CUDA_TRY(cudaMemcpy(host, net->P.p, sizeof(float) * size_t(n), cudaMemcpyDeviceToHost));
+  return SFX_OK;
+}
+
+int sfx_lnet_set_params(sfx_lnet net, const float* host, int64_t n) {
+  if (!net || !host || n != net->nparams) return fail(SFX_ERR_INVALID, "bad parameter buffer");
+  SFX_CUDA_TRY(cudaMemcpy(net->P.p, host, sizeof(float) * size_t(n), cudaMemcpyHostToDevice));
+  if (int rc = sync_weights(net, nullptr)) return rc;
+  SFX_CUDA_TRY(cudaDeviceSynchronize());
+  return SFX_OK;
+}
+
+int sfx_lnet_apply(sfx_lnet net, int nx, int ny, int nz, const float* r, const float* features, float* z,
+                   void* stream) {
+  if (!net || !r || !features || !z) return fail(SFX_ERR_INVALID, "null argument");
+  return lnet_apply(net, nx, ny, nz, r, features, z, static_cast<cudaStream_t>(stream));
+}
+
+int sfx_lnet_gradient(sfx_lnet net, int nx, int ny, int nz, const float* r, const float* target,
+                      const float* features, float* loss, float* grad_host, void* stream) {
+  if (!net || !r || !target || !features || !loss || !grad_host) return fail(SFX_ERR_INVALID, "null argument");
+  auto s = static_cast<cudaStream_t>(stream);
+  Work* w = nullptr;
+  if (int rc = get_work(net, nx, ny, nz, &w)) return rc;
+  SFX_CUDA_TRY(cudaMemsetAsync(net->G.p, 0, sizeof(float) * size_t(net->nparams), s));
+  if (int rc = sample_grad(net, w, r, target, features, loss, s)) return rc;
+  SFX_CUDA_TRY(cudaMemcpyAsync(grad_host, net->G.p, sizeof(float) * size_t(net->nparams), cudaMemcpyDeviceToHost, s));
+  SFX_CUDA_TRY(cudaStreamSynchronize(s));
+  return SFX_OK;
+}
+
+int sfx_lnet_train_step(sfx_lnet net, int nx, int ny, int nz, int batch, const float* r, const float* target,
+                        const float* features, float lr, float* mean_loss, void* stream) {
+  if (!net || !r || !target || !features || batch < 1) return fail(SFX_ERR_INVALID, "bad argument");
+  auto s = static_cast<cudaStream_t>(stream);
+  Work* w = nullptr;
+  if (int rc = get_work(net, nx, ny, nz, &w)) return rc;
+  const int64_t N = w->g[0].nodes();
+  SFX_CUDA_TRY(cudaMemsetAsync(net->G.p, 0, sizeof(float) * size_t(net->nparams), s));
+  double total = 0.0;
+  for (int b = 0; b < batch; b++) {
+    float l = 0.f;
+    if (int rc = sample_grad(net, w, r + b * 3 * N, target + b * 3 * N, features + b * 2 * N, &l, s)) return rc;
+    total += l;
+  }
+  net->step++;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f - std::pow(b1, float(net->step)), c2 = 1.f - std::pow(b2, float(net->step));
+  adam<<<nb(net->nparams), 256, 0, s>>>(net->P.p, net->G.p, net->M.p, net->V.p, net->nparams, lr, b1, b2, c1, c2,
+                                        1e-8f, 1.f / float(batch));
+  if (int rc = sync_weights(net, s)) return rc;
+  SFX_CUDA_TRY(cudaStreamSynchronize(s));
+  if (mean_loss) *mean_loss = float(total / batch);
+  return SFX_OK;
+}
+
+}  // extern "C"

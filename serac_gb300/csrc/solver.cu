@@ -26,6 +26,7 @@
 
 #include "blas.cuh"
 #include "form.hpp"
+#include "learned_internal.hpp"
 #include "sfx.h"
 #include "sfx_solver.h"
 
@@ -84,7 +85,11 @@ struct sfx_solver_s {
   Reducer<double, double> red;
   Reducer<float, float> red32;
   double lmax = 0.0, lmax32 = 0.0;
-  std::function<int(int, const char*)> log;
+  // learned preconditioner
+  sfx_lnet net = nullptr;
+  int grid[3] = {0, 0, 0};
+  const float* features = nullptr;
+  DeviceBuf<float> nn_z, nn_res;
 };
 
 namespace {
@@ -349,6 +354,44 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
       sfx_blas::diag_solve<double><<<nblocks(n), 256, 0, st>>>(n, v, s->diag.p, z);
       return SFX_OK;
     };
+  } else if (o.precond == SFX_PREC_LEARNED) {
+    if (!s->net || !s->features) return fail(SFX_ERR_INVALID, "SFX_PREC_LEARNED needs sfx_solver_set_learned");
+    if (ensure(s->x32, n) || ensure(s->b32, n) || ensure(s->tmp32, n) || ensure(s->diag32, n) ||
+        ensure(s->cheb_d32, n) || ensure(s->cheb_r32, n) || ensure(s->tmp32b, n) || ensure(s->nn_z, n) ||
+        ensure(s->nn_res, n))
+      return fail(SFX_ERR_NOMEM, "FP32 workspace allocation failed");
+    sfx_blas::convert<double, float><<<nblocks(n), 256, 0, st>>>(n, s->diag.p, s->diag32.p);
+    if (int rc = estimate_lmax<float, float>(s, apply_J32, s->diag32.p, s->tmp32.p, s->cheb_r32.p, s->red32,
+                                             &s->lmax32, st))
+      return rc;
+    prec = [=](const double* v, double* z) -> int {
+      cudaError_t err;
+      sfx_blas::convert<double, float><<<nblocks(n), 256, 0, st>>>(n, v, s->b32.p);
+      if (int rc = lnet_apply(s->net, s->grid[0], s->grid[1], s->grid[2], s->b32.p, s->features, s->nn_z.p, st))
+        return rc;
+      s->stats.learned_applications++;
+      // what the network leaves of the residual: res = v - J z_nn
+      if (int rc = apply_J32(s, s->nn_z.p, s->nn_res.p, st)) return rc;
+      sfx_blas::rsub<float><<<nblocks(n), 256, 0, st>>>(n, s->b32.p, s->nn_res.p);
+      const double nr = double(s->red32.dot(s->nn_res.p, s->nn_res.p, n, st, &err));
+      SFX_CUDA_TRY(err);
+      const double nv = double(s->red32.dot(s->b32.p, s->b32.p, n, st, &err));
+      SFX_CUDA_TRY(err);
+      if (std::isfinite(nr) && nr < nv) {
+        // z = z_nn + Chebyshev(res)
+        if (int rc = chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, s->nn_res.p, s->x32.p,
+                                             s->cheb_d32.p, s->cheb_r32.p, st))
+          return rc;
+        sfx_blas::axpby<float><<<nblocks(n), 256, 0, st>>>(n, 1.0f, s->nn_z.p, 1.0f, s->x32.p);
+      } else {
+        s->stats.learned_fallbacks++;
+        if (int rc = chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, s->b32.p, s->x32.p,
+                                             s->cheb_d32.p, s->cheb_r32.p, st))
+          return rc;
+      }
+      sfx_blas::convert<float, double><<<nblocks(n), 256, 0, st>>>(n, s->x32.p, z);
+      return SFX_OK;
+    };
   } else if (o.mixed_precision) {
     // inner FP32 GMRES(k) with FP32 Jacobi-Chebyshev on the FP32 stored tangent
     const int k = o.inner_iterations;
@@ -384,7 +427,7 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
     };
   }
   SFX_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
-  const bool flexible = o.mixed_precision != 0 || o.krylov == SFX_KRYLOV_FGMRES;
+  const bool flexible = o.mixed_precision != 0 || o.krylov == SFX_KRYLOV_FGMRES || o.precond == SFX_PREC_LEARNED;
   int rc = gmres<double, double>(s, apply_J64, prec, flexible, rhs, x, s->V.p, s->Z.p, s->tmp.p, s->y.p, s->red, m,
                                  o.max_krylov_iterations, o.krylov_rel_tol, o.krylov_abs_tol, &iters, &rel, st);
   s->stats.krylov_iterations += iters;
@@ -499,6 +542,17 @@ int sfx_solver_solve(sfx_solver s, double t, double* u, void* stream) {
   s->stats.final_residual = rn;
   s->stats.converged = rn <= target ? 1 : 0;
   return s->stats.converged ? SFX_OK : fail(SFX_ERR_NOT_CONVERGED, "Newton did not converge");
+}
+
+int sfx_solver_set_learned(sfx_solver s, sfx_lnet net, int nx, int ny, int nz, const float* features) {
+  if (!s || !net || !features) return fail(SFX_ERR_INVALID, "null argument");
+  if (int64_t(nx) * ny * nz * 3 != s->n) return fail(SFX_ERR_INVALID, "node grid does not match the form (3 components)");
+  s->net = net;
+  s->grid[0] = nx;
+  s->grid[1] = ny;
+  s->grid[2] = nz;
+  s->features = features;
+  return SFX_OK;
 }
 
 int sfx_solver_get_stats(sfx_solver s, sfx_solver_stats* out) {

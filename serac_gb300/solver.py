@@ -19,7 +19,7 @@ from . import _lib
 from .functional import Functional, _dptr, _require, _stream
 
 GMRES, CG, FGMRES = 0, 1, 2
-NONE, JACOBI, JACOBI_CHEBYSHEV = 0, 1, 2
+NONE, JACOBI, JACOBI_CHEBYSHEV, LEARNED = 0, 1, 2, 3
 ERR_NOT_CONVERGED = -7
 
 
@@ -63,6 +63,8 @@ class SolverStats(ctypes.Structure):
         ("initial_residual", ctypes.c_double),
         ("final_residual", ctypes.c_double),
         ("last_krylov_rel", ctypes.c_double),
+        ("learned_applications", ctypes.c_int),
+        ("learned_fallbacks", ctypes.c_int),
     ]
 
     def as_dict(self):
@@ -87,6 +89,16 @@ class NewtonSolver:
         d = np.ascontiguousarray(np.asarray(dofs, dtype=np.int64).ravel())
         self._ess = d
         _lib.call("sfx_solver_set_essential", self._h, d.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), d.size)
+
+    def set_learned(self, net, grid, features):
+        """Use a LearnedPreconditioner (precond=LEARNED): grid = node grid
+        (nx, ny, nz), features = float32 CUDA tensor [2 * num_nodes]."""
+        if not (isinstance(features, torch.Tensor) and features.is_cuda and features.dtype == torch.float32):
+            raise TypeError("features must be a float32 CUDA tensor")
+        self._features = features
+        self._net = net
+        _lib.call("sfx_solver_set_learned", self._h, net._h, int(grid[0]), int(grid[1]), int(grid[2]),
+                  _dptr(features))
 
     def stats(self):
         st = SolverStats()

@@ -1,0 +1,116 @@
+"""Learned preconditioner kernels (BF16 tensor-core convolutions, FP32
+accumulation) against the FP64 numpy network oracle: forward output and the
+full parameter gradient; a few Adam steps reduce the loss.
+
+Tolerances: BF16 activations, weights and gradients carry ~3 significant
+digits, so the forward output is checked to 3e-2 and the gradient to 6e-2
+relative (l2) — the FP64 oracle itself is checked against finite differences
+in test_nn_oracle.py."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import nn_oracle as NN
+
+pytestmark = pytest.mark.gpu
+
+
+def _lib():
+    from serac_gb300 import _lib
+
+    return _lib
+
+
+def _net(seed=7):
+    L = _lib()
+    h = ctypes.c_void_p()
+    L.call("sfx_lnet_create", ctypes.c_uint64(seed), ctypes.byref(h))
+    n = ctypes.c_int64()
+    L.call("sfx_lnet_num_params", h, ctypes.byref(n))
+    p = np.zeros(n.value, dtype=np.float32)
+    L.call("sfx_lnet_get_params", h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), n.value)
+    return h, p
+
+
+def _smooth_field(shape, rng, ncomp):
+    """random field with some spatial correlation (sum of a few Fourier modes)"""
+    nz, ny, nx = shape
+    z, y, x = np.meshgrid(np.linspace(0, 1, nz), np.linspace(0, 1, ny), np.linspace(0, 1, nx), indexing="ij")
+    out = []
+    for _ in range(ncomp):
+        f = np.zeros(shape)
+        for _ in range(6):
+            k = rng.integers(1, 4, 3)
+            ph = rng.uniform(0, 2 * np.pi, 3)
+            f += rng.standard_normal() * np.sin(np.pi * k[0] * x + ph[0]) * np.sin(np.pi * k[1] * y + ph[1]) * \
+                np.sin(np.pi * k[2] * z + ph[2])
+        out.append(f.ravel())
+    return np.concatenate(out)
+
+
+def _sample(shape, seed):
+    rng = np.random.default_rng(seed)
+    N = int(np.prod(shape))
+    r = _smooth_field(shape, rng, 3) + 0.1 * rng.standard_normal(3 * N)
+    t = _smooth_field(shape, rng, 3)
+    feat = np.zeros(2 * N)
+    feat[:N] = _smooth_field(shape, rng, 1) * 0.5
+    feat[N:N + shape[1] * shape[2]] = 1.0  # z = 0 layer is Dirichlet
+    return r, t, feat
+
+
+@pytest.mark.parametrize("shape", [(9, 9, 9), (17, 9, 25)])
+def test_forward_matches_oracle(cuda, shape):
+    L = _lib()
+    h, p = _net()
+    r, _, feat = _sample(shape, 1)
+    z = torch.empty(r.size, dtype=torch.float32, device=cuda)
+    rt = torch.tensor(r, dtype=torch.float32, device=cuda)
+    ft = torch.tensor(feat, dtype=torch.float32, device=cuda)
+    nz, ny, nx = shape
+    L.call("sfx_lnet_apply", h, nx, ny, nz, ctypes.c_void_p(rt.data_ptr()), ctypes.c_void_p(ft.data_ptr()),
+           ctypes.c_void_p(z.data_ptr()), None)
+    ref = NN.apply(p.astype(np.float64), r, feat, shape)
+    zz = z.cpu().numpy().astype(np.float64)
+    assert np.isfinite(zz).all()
+    assert np.linalg.norm(zz - ref) / np.linalg.norm(ref) <= 3e-2
+    L.load().sfx_lnet_destroy(h)
+
+
+def test_gradient_matches_oracle(cuda):
+    L = _lib()
+    h, p = _net(seed=11)
+    shape = (17, 17, 9)
+    nz, ny, nx = shape
+    r, t, feat = _sample(shape, 2)
+    dev = [torch.tensor(a, dtype=torch.float32, device=cuda) for a in (r, t, feat)]
+    loss = ctypes.c_float()
+    g = np.zeros_like(p)
+    L.call("sfx_lnet_gradient", h, nx, ny, nz, *[ctypes.c_void_p(d.data_ptr()) for d in dev], ctypes.byref(loss),
+           g.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), None)
+    ref_loss, ref_g, _, _ = NN.loss_and_grad(p.astype(np.float64), r, t, feat, shape)
+    assert abs(loss.value - ref_loss) <= 3e-2 * ref_loss
+    assert np.linalg.norm(g - ref_g) / np.linalg.norm(ref_g) <= 6e-2
+    L.load().sfx_lnet_destroy(h)
+
+
+def test_training_reduces_loss(cuda):
+    L = _lib()
+    h, _ = _net(seed=3)
+    shape = (9, 9, 9)
+    nz, ny, nx = shape
+    samples = [_sample(shape, 100 + i) for i in range(4)]
+    R = torch.tensor(np.concatenate([s[0] for s in samples]), dtype=torch.float32, device=cuda)
+    T = torch.tensor(np.concatenate([s[1] for s in samples]), dtype=torch.float32, device=cuda)
+    F = torch.tensor(np.concatenate([s[2] for s in samples]), dtype=torch.float32, device=cuda)
+    losses = []
+    for _ in range(40):
+        lv = ctypes.c_float()
+        L.call("sfx_lnet_train_step", h, nx, ny, nz, 4, ctypes.c_void_p(R.data_ptr()), ctypes.c_void_p(T.data_ptr()),
+               ctypes.c_void_p(F.data_ptr()), ctypes.c_float(1e-3), ctypes.byref(lv), None)
+        losses.append(lv.value)
+    assert np.isfinite(losses).all()
+    assert losses[-1] < 0.5 * losses[0]
+    L.load().sfx_lnet_destroy(h)
