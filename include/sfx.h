@@ -15,6 +15,8 @@
  *   sfx_form_create                 numerics/functional/functional.hpp:219-273 Functional ctor
  *   sfx_form_add_domain_integral    numerics/functional/functional.hpp:286-317 AddDomainIntegral
  *   sfx_form_add_boundary_integral  numerics/functional/functional.hpp:328-354 AddBoundaryIntegral
+ *   sfx_form_set_shape_displacement numerics/functional/shape_aware_functional.hpp:45-172, 330-560
+ *                                   ShapeAwareFunctional (shape displacement as trial 0, held fixed)
  *   sfx_residual                    numerics/functional/functional.hpp:502-513 operator()(t, u)
  *   sfx_linearize                   numerics/functional/functional.hpp:481-489 operator()(t, differentiate_wrt(u))
  *   sfx_jvp / sfx_jvp_f32           numerics/functional/functional.hpp:556-566 Gradient::Mult / operator()
@@ -95,6 +97,15 @@ int sfx_form_add_domain_integral(sfx_form form, int material, const double* para
 
 /* Boundary integral over the faces of the sides in side_mask; params: host. */
 int sfx_form_add_boundary_integral(sfx_form form, int bmaterial, int side_mask, const double* params);
+
+/* Shape displacement p (device, 3 * num_nodes doubles, byNODES on the form's
+ * node grid; NULL = none): every integral of the form is evaluated on the
+ * configuration x = X + p as serac's ShapeAwareFunctional does — trial
+ * gradients du/dX (I + dp/dX)^-1, domain outputs scaled by det(I + dp/dX)
+ * with the flux mapped by (I + dp/dX)^-T, boundary weights by the area ratio,
+ * and the q-function position argument X + p.  The value is copied; the form
+ * must be linearised again afterwards. */
+int sfx_form_set_shape_displacement(sfx_form form, const double* shape, void* stream);
 
 /* r = R(t, u) (device, num_dofs doubles each).  When sfx_update_qdata(form, 1)
  * is in effect, quadrature-point state is committed by this call. */

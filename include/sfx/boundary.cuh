@@ -263,6 +263,59 @@ __global__ void face_geometry_kernel(const double* __restrict__ Xf, double* __re
   for (int k = 0; k < FGEOM_STRIDE; k++) g[k * nqt + gq] = vals[k];
 }
 
+/// Face geometry of the shape-displaced configuration: x' = X + p,
+/// dx'/dxi = dX/dxi + dp/dxi and weight |cross(dx'/dxi)| w, which is serac's
+/// boundary area correction (shape_aware_functional.hpp:155-172) applied to
+/// the reference weight.  p: 3-component order-P field on the node grid
+/// (byNODES), gathered through the face connectivity [f][(P+1)^2].
+template <int P>
+__global__ void face_geometry_shape_kernel(const double* __restrict__ Xf, const int32_t* __restrict__ fconn,
+                                           const double* __restrict__ shape, int64_t num_nodes,
+                                           double* __restrict__ g, int64_t nf) {
+  constexpr int Q = P + 1, NQ = Q * Q, N1 = P + 1, NPF = N1 * N1;
+  const int64_t nqt = nf * NQ;
+  int64_t gq = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (gq >= nqt) return;
+  int64_t f = gq / NQ;
+  int q = int(gq - f * NQ);
+  int qx = q % Q, qy = q / Q;
+  double s[2] = {gl_point(Q, qx), gl_point(Q, qy)};
+  double w = gl_weight(Q, qx) * gl_weight(Q, qy);
+  const double* X = Xf + f * 12;
+  double x[3] = {0, 0, 0}, J[3][2] = {};
+  for (int v = 0; v < 4; v++) {
+    int b0 = v & 1, b1 = (v >> 1) & 1;
+    double N0 = b0 ? s[0] : 1.0 - s[0], N1v = b1 ? s[1] : 1.0 - s[1];
+    double d0 = b0 ? 1.0 : -1.0, d1 = b1 ? 1.0 : -1.0;
+    for (int i = 0; i < 3; i++) {
+      double xv = X[i * 4 + v];
+      x[i] += xv * N0 * N1v;
+      J[i][0] += xv * d0 * N1v;
+      J[i][1] += xv * N0 * d1;
+    }
+  }
+  const auto& T = basis_table<P>();
+  const int32_t* cf = fconn + f * NPF;
+  for (int a = 0; a < NPF; a++) {
+    const int as = a % N1, at = a / N1;
+    const double phi = T.B[qx][as] * T.B[qy][at];
+    const double gs = T.G[qx][as] * T.B[qy][at], gt = T.B[qx][as] * T.G[qy][at];
+    const int64_t node = cf[a];
+    for (int i = 0; i < 3; i++) {
+      const double pv = shape[i * num_nodes + node];
+      x[i] += pv * phi;
+      J[i][0] += pv * gs;
+      J[i][1] += pv * gt;
+    }
+  }
+  double n0 = J[1][0] * J[2][1] - J[2][0] * J[1][1];
+  double n1 = J[2][0] * J[0][1] - J[0][0] * J[2][1];
+  double n2 = J[0][0] * J[1][1] - J[1][0] * J[0][1];
+  double vals[FGEOM_STRIDE] = {x[0], x[1], x[2], J[0][0], J[0][1], J[1][0], J[1][1], J[2][0], J[2][1],
+                               ::sqrt(n0 * n0 + n1 * n1 + n2 * n2) * w};
+  for (int k = 0; k < FGEOM_STRIDE; k++) g[k * nqt + gq] = vals[k];
+}
+
 /// out[c * N + node_ids[i]] += sum over the compact face-node entry list (in
 /// face order) of E[(f * C + c) * NPF + local].  One thread per face node.
 template <int C, int NPF, typename Real>

@@ -297,6 +297,14 @@ class Functional<H1<p, c>(H1<p, c>)> {
   /// updateQdata(bool) (functional.hpp:523): commit quadrature state on residual calls
   void updateQdata(bool flag) { update_qdata_ = flag; }
 
+  /// Shape displacement p (device, 3 * num_nodes doubles, byNODES; nullptr =
+  /// none): the integrals are evaluated on X + p as ShapeAwareFunctional does
+  /// (shape_aware_functional.hpp:45-172).  Linearise again afterwards.
+  void SetShapeDisplacement(const double* shape, cudaStream_t s = nullptr) {
+    check(sfx_form_set_shape_displacement(form_.get(), shape, s));
+    linearized_ = false;
+  }
+
   /// R(t, u) into a member buffer (functional.hpp:502-513)
   const double* operator()(double t, const double* u, cudaStream_t s = nullptr) {
     residual(t, u, out_.p, s);
@@ -399,6 +407,30 @@ class Functional<H1<p, c>(H1<p, c>)> {
   bool linearized_ = false;
   bool update_qdata_ = false;
   Gradient grad_;
+};
+
+/// ShapeAwareFunctional<H1<p,3>, H1<p,c>(H1<p,c>)> (shape_aware_functional.hpp:330-560):
+/// the shape displacement comes first after time and is held fixed by the
+/// evaluation; r = f(t, shape, u), (r, dR/du) = f(t, shape, differentiate_wrt(u)).
+template <typename Shape, typename Sig>
+class ShapeAwareFunctional;
+
+template <int p, int c>
+class ShapeAwareFunctional<H1<p, 3>, H1<p, c>(H1<p, c>)> : public Functional<H1<p, c>(H1<p, c>)> {
+  using Base = Functional<H1<p, c>(H1<p, c>)>;
+
+ public:
+  using Base::Base;
+  using Base::operator();
+  const double* operator()(double t, const double* shape, const double* u, cudaStream_t s = nullptr) {
+    Base::SetShapeDisplacement(shape, s);
+    return Base::operator()(t, u, s);
+  }
+  std::tuple<const double*, typename Base::Gradient&> operator()(double t, const double* shape,
+                                                                 differentiate_wrt_this w, cudaStream_t s = nullptr) {
+    Base::SetShapeDisplacement(shape, s);
+    return Base::operator()(t, w, s);
+  }
 };
 
 }  // namespace sfx

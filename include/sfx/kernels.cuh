@@ -426,6 +426,71 @@ __global__ void __launch_bounds__(256) geometry_kernel(const double* __restrict_
   }
 }
 
+/// Geometric factors of the shape-displaced configuration x' = X + p
+/// (serac's ShapeAwareFunctional, shape_aware_functional.hpp:45-120): p is a
+/// 3-component H1 field of order P on the form's node grid (byNODES,
+/// shape[i * num_nodes + node]); dx'/dxi = dX/dxi + dp/dxi.  Evaluating the
+/// plain element kernels with these factors gives serac's corrections
+/// du/dx' = du/dX (I + dp/dX)^-1, flux (I + dp/dX)^-T det(I + dp/dX) and
+/// source det(I + dp/dX).  One thread per quadrature point; same layout as
+/// geometry_kernel.
+template <int P>
+__global__ void __launch_bounds__(256) geometry_shape_kernel(const double* __restrict__ Xe,
+                                                             const int32_t* __restrict__ conn,
+                                                             const double* __restrict__ shape, int64_t num_nodes,
+                                                             double* __restrict__ g64, float* __restrict__ g32,
+                                                             int64_t ne) {
+  constexpr int Q = P + 1, NQ = Q * Q * Q, N1 = P + 1, NPE = N1 * N1 * N1;
+  const int64_t nqt = ne * NQ;
+  int64_t gq = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (gq >= nqt) return;
+  int64_t e = gq / NQ;
+  int q = int(gq - e * NQ);
+  int qx = q % Q, qy = (q / Q) % Q, qz = q / (Q * Q);
+  double s[3] = {gl_point(Q, qx), gl_point(Q, qy), gl_point(Q, qz)};
+  double w = gl_weight(Q, qx) * gl_weight(Q, qy) * gl_weight(Q, qz);
+  const double* X = Xe + e * 24;
+  tensor<double, 3> x{};
+  tensor<double, 3, 3> J{};
+  for (int v = 0; v < 8; v++) {
+    int b0 = v & 1, b1 = (v >> 1) & 1, b2 = (v >> 2) & 1;
+    double N0 = b0 ? s[0] : 1.0 - s[0], N1v = b1 ? s[1] : 1.0 - s[1], N2 = b2 ? s[2] : 1.0 - s[2];
+    double d0 = b0 ? 1.0 : -1.0, d1 = b1 ? 1.0 : -1.0, d2 = b2 ? 1.0 : -1.0;
+    double phi = N0 * N1v * N2;
+    double g[3] = {d0 * N1v * N2, N0 * d1 * N2, N0 * N1v * d2};
+    for (int i = 0; i < 3; i++) {
+      double xv = X[i * 8 + v];
+      x[i] += xv * phi;
+      for (int j = 0; j < 3; j++) J[i][j] += xv * g[j];
+    }
+  }
+  const auto& T = basis_table<P>();
+  const int32_t* ce = conn + e * NPE;
+  for (int a = 0; a < NPE; a++) {
+    const int ax = a % N1, ay = (a / N1) % N1, az = a / (N1 * N1);
+    const double bx = T.B[qx][ax], by = T.B[qy][ay], bz = T.B[qz][az];
+    const double phi = bx * by * bz;
+    const double g[3] = {T.G[qx][ax] * by * bz, bx * T.G[qy][ay] * bz, bx * by * T.G[qz][az]};
+    const int64_t node = ce[a];
+    for (int i = 0; i < 3; i++) {
+      const double pv = shape[i * num_nodes + node];
+      x[i] += pv * phi;
+      for (int j = 0; j < 3; j++) J[i][j] += pv * g[j];
+    }
+  }
+  auto Ji = inv(J);
+  double dv = det(J) * w;
+  double vals[GEOM_STRIDE];
+  for (int k = 0; k < 9; k++) vals[k] = Ji[k / 3][k % 3];
+  vals[9] = dv;
+  for (int k = 0; k < 3; k++) vals[10 + k] = x[k];
+  for (int k = 0; k < 9; k++) vals[13 + k] = J[k / 3][k % 3];
+  for (int k = 0; k < GEOM_STRIDE; k++) {
+    g64[k * nqt + gq] = vals[k];
+    g32[k * nqt + gq] = float(vals[k]);
+  }
+}
+
 }  // namespace kernels
 }  // namespace sfx
 

@@ -135,28 +135,110 @@ __global__ void flip_weights(const __nv_bfloat16* __restrict__ W, __nv_bfloat16*
   Wt[(int64_t(ci) * 27 + tap) * COUT + co] = W[(int64_t(co) * 27 + (26 - tap)) * CIN + ci];
 }
 
-/// Weight gradient partials: part[blk][co][tap][ci] = sum over the block's node
-/// chunk of dy[n][co] x[n + off(tap)][ci] (FP32).  grid = (chunks), threads over
-/// (co, ci) pairs and taps.  Reduced in fixed order by reduce_chunks.
+/// Weight gradient on the tensor cores:
+///   dW[co][tap][ci] = sum_n dy[n][co] x[n + off(tap)][ci]
+/// as a GEMM with M = COUT, N = CIN per tap and K = nodes.  The nodes are cut
+/// into chunks of kWgradChunk; block b takes chunks b, b + gridDim.x, ... and
+/// writes its partial sums to part[b][co][tap][ci] (reduced over blocks in
+/// fixed order by reduce_chunks).  Per chunk the block stages dy^T
+/// ([co][node], BF16) and the tap-shifted x^T ([ci][node], zero outside the
+/// grid) in shared memory; its four warps take interleaved 16-node k-steps
+/// and are summed in warp order at the end of each tap.
+constexpr int kWgradChunk = 128;
+
 template <int CIN, int COUT>
-__global__ void __launch_bounds__(256) conv3_wgrad_partial(Grid3 g, const __nv_bfloat16* __restrict__ x,
-                                                           const float* __restrict__ dy, int64_t chunk,
-                                                           float* __restrict__ part) {
+__global__ void __launch_bounds__(128) conv3_wgrad_mma(Grid3 g, const __nv_bfloat16* __restrict__ x,
+                                                       const __nv_bfloat16* __restrict__ dy, float* __restrict__ part) {
+  static_assert(CIN % 16 == 0 && COUT % 16 == 0, "channel counts");
+  constexpr int KC = kWgradChunk;
+  constexpr int LD = KC + 8;  // row pitch in BF16: 68 words, 4 mod 32 -> conflict-free fragment loads
+  constexpr int MT = COUT / 16, NT = CIN / 8, T = MT * NT;
+  __shared__ __align__(16) __nv_bfloat16 sA[COUT * LD];
+  __shared__ __align__(16) __nv_bfloat16 sB[CIN * LD];
+  __shared__ float sR[T * 4 * 32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gid = lane >> 2, tig = lane & 3;
   const int64_t N = g.nodes();
-  const int64_t b0 = int64_t(blockIdx.x) * chunk;
-  const int64_t b1 = b0 + chunk < N ? b0 + chunk : N;
-  float* out = part + int64_t(blockIdx.x) * COUT * 27 * CIN;
-  for (int p = threadIdx.x; p < COUT * 27 * CIN; p += blockDim.x) {
-    const int ci = p % CIN, tap = (p / CIN) % 27, co = p / (CIN * 27);
+  const int64_t nchunks = (N + KC - 1) / KC;
+  const bool one_chunk = int64_t(blockIdx.x) + gridDim.x >= nchunks;  // dy^T staged once for all taps
+  const __nv_bfloat16 zero = __float2bfloat16(0.f);
+#pragma unroll 1
+  for (int tap = 0; tap < 27; tap++) {
     const int ox = tap % 3 - 1, oy = (tap / 3) % 3 - 1, oz = tap / 9 - 1;
-    float acc = 0.f;
-    for (int64_t n = b0; n < b1; n++) {
-      const int xx = int(n % g.nx) + ox, yy = int((n / g.nx) % g.ny) + oy, zz = int(n / (int64_t(g.nx) * g.ny)) + oz;
-      if (xx < 0 || xx >= g.nx || yy < 0 || yy >= g.ny || zz < 0 || zz >= g.nz) continue;
-      const int64_t s = (int64_t(zz) * g.ny + yy) * g.nx + xx;
-      acc += dy[n * COUT + co] * __bfloat162float(x[s * CIN + ci]);
+    float acc[T][4];
+#pragma unroll
+    for (int t = 0; t < T; t++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) acc[t][j] = 0.f;
+#pragma unroll 1
+    for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+      const int64_t b0 = c * KC;
+      __syncthreads();  // the previous k-steps are done with sA / sB
+      if (!one_chunk || tap == 0) {
+        for (int i = threadIdx.x; i < KC * COUT; i += blockDim.x) {
+          const int k = i / COUT, co = i % COUT;
+          const int64_t n = b0 + k;
+          sA[co * LD + k] = n < N ? dy[n * COUT + co] : zero;
+        }
+      }
+      for (int i = threadIdx.x; i < KC * CIN; i += blockDim.x) {
+        const int k = i / CIN, ci = i % CIN;
+        const int64_t n = b0 + k;
+        __nv_bfloat16 v = zero;
+        if (n < N) {
+          const int xx = int(n % g.nx) + ox, yy = int((n / g.nx) % g.ny) + oy,
+                    zz = int(n / (int64_t(g.nx) * g.ny)) + oz;
+          if (xx >= 0 && xx < g.nx && yy >= 0 && yy < g.ny && zz >= 0 && zz < g.nz)
+            v = x[((int64_t(zz) * g.ny + yy) * g.nx + xx) * CIN + ci];
+        }
+        sB[ci * LD + k] = v;
+      }
+      __syncthreads();
+#pragma unroll 1
+      for (int ks = warp; ks < KC / 16; ks += 4) {
+        const int k0 = ks * 16 + tig * 2;
+        uint32_t a[MT][4];
+#pragma unroll
+        for (int mt = 0; mt < MT; mt++) {
+          const __nv_bfloat16* r0 = sA + (mt * 16 + gid) * LD + k0;
+          const __nv_bfloat16* r1 = r0 + 8 * LD;
+          a[mt][0] = *reinterpret_cast<const uint32_t*>(r0);
+          a[mt][1] = *reinterpret_cast<const uint32_t*>(r1);
+          a[mt][2] = *reinterpret_cast<const uint32_t*>(r0 + 8);
+          a[mt][3] = *reinterpret_cast<const uint32_t*>(r1 + 8);
+        }
+#pragma unroll
+        for (int nt = 0; nt < NT; nt++) {
+          const __nv_bfloat16* rb = sB + (nt * 8 + gid) * LD + k0;
+          const uint32_t b[2] = {*reinterpret_cast<const uint32_t*>(rb), *reinterpret_cast<const uint32_t*>(rb + 8)};
+#pragma unroll
+          for (int mt = 0; mt < MT; mt++) mma_bf16_16816(acc[mt * NT + nt], a[mt], b);
+        }
+      }
     }
-    out[p] = acc;
+    // sum the four warps' tiles in warp order, then store this tap's partials
+#pragma unroll 1
+    for (int w = 0; w < 4; w++) {
+      if (warp == w) {
+#pragma unroll
+        for (int t = 0; t < T; t++)
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            float* r = &sR[(t * 4 + j) * 32 + lane];
+            *r = (w == 0 ? 0.f : *r) + acc[t][j];
+          }
+      }
+      __syncthreads();
+    }
+    float* out = part + int64_t(blockIdx.x) * COUT * 27 * CIN;
+    for (int i = threadIdx.x; i < T * 128; i += blockDim.x) {
+      const int t = i >> 7, j = (i >> 5) & 3, l = i & 31;
+      const int mt = t / NT, nt = t % NT;
+      const int co = mt * 16 + (l >> 2) + (j >= 2 ? 8 : 0);
+      const int ci = nt * 8 + (l & 3) * 2 + (j & 1);
+      out[(int64_t(co) * 27 + tap) * CIN + ci] = sR[i];
+    }
+    __syncthreads();  // sR is rewritten by the next tap
   }
 }
 

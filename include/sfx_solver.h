@@ -7,7 +7,8 @@
  *   sfx_solver_create           equation_solver.cpp:820-950 buildNonlinearSolver / buildLinearSolverAndPreconditioner
  *   sfx_solver_set_essential    physics/boundary_conditions/boundary_condition_manager.hpp:91 (essential dofs)
  *   sfx_solver_solve            equation_solver.cpp:79-200 NewtonSolver::Mult (quasiStaticSolve, solid_mechanics.hpp:1620-1630)
- *   sfx_solver_solve_linear     one linearised solve (warmStartDisplacement, solid_mechanics.hpp:1727-1770)
+ *   sfx_solver_warm_start       SolidMechanics::warmStartDisplacement (solid_mechanics.hpp:1727-1770)
+ *   sfx_solver_solve_linear     one linearised solve with the essential rows eliminated
  * The Chebyshev, flexible-GMRES and mixed-precision options have no
  * counterpart in serac (its LinearSolver enum is CG / GMRES / direct / PETSc).
  */
@@ -31,11 +32,13 @@ extern "C" {
 #define SFX_PREC_NONE 0
 #define SFX_PREC_JACOBI 1
 #define SFX_PREC_JACOBI_CHEBYSHEV 2
-/* Learned multilevel network (include/sfx_learned.h) followed by one FP32
- * Jacobi-Chebyshev application on what it leaves of the residual; when the
- * network's step does not reduce the residual, Jacobi-Chebyshev alone
- * (counted in sfx_solver_stats.learned_fallbacks).  Implies flexible GMRES
- * with FP32 inner work (mixed precision). */
+/* Learned multilevel network (include/sfx_learned.h) combined with FP32
+ * Jacobi-Chebyshev on what it leaves of the residual (learned_cycle).  The
+ * network's step is scaled to minimise the residual; a step that takes less
+ * than 1 % off the residual norm is skipped (counted in
+ * sfx_solver_stats.learned_fallbacks), leaving Jacobi-Chebyshev alone.  The
+ * outer Krylov method is flexible GMRES; with mixed_precision the step
+ * preconditions an inner FP32 flexible GMRES(inner_iterations). */
 #define SFX_PREC_LEARNED 3
 
 typedef struct {
@@ -55,6 +58,7 @@ typedef struct {
   int inner_iterations;      /* 20: FP32 inner GMRES steps per outer step */
   double inner_rel_tol;      /* 1e-3 */
   int print_level;           /* 0 */
+  int learned_cycle;         /* SFX_PREC_LEARNED step: 0 network then Chebyshev; 1 Chebyshev, network, Chebyshev */
 } sfx_solver_options;
 
 typedef struct {
@@ -81,6 +85,12 @@ int sfx_solver_solve(sfx_solver solver, double t, double* u, void* stream);
 /* x = J(t, u_lin)^-1 rhs with the essential rows/columns eliminated. */
 int sfx_solver_solve_linear(sfx_solver solver, double t, const double* u_lin, const double* rhs, double* x,
                             void* stream);
+/* Load-step predictor: with d = u_target - u on the essential vdofs (0
+ * elsewhere), solve J(t, u) x = -J(t, u) d on the free rows and set
+ * u += d + x, so that u carries the new essential values and a first-order
+ * response of the free vdofs to them (only the essential entries of
+ * u_target are read).  Follow with sfx_solver_solve. */
+int sfx_solver_warm_start(sfx_solver solver, double t, double* u, const double* u_target, void* stream);
 int sfx_solver_get_stats(sfx_solver solver, sfx_solver_stats* out);
 /* Network for SFX_PREC_LEARNED: the form's node grid (order * n + 1 nodes per
  * direction) and per-node features (device, [2][num_nodes] floats: log

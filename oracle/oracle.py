@@ -183,6 +183,23 @@ class StructuredHexMesh:
         _, nodes = self.boundary_faces(p, sides)
         return np.unique(nodes.ravel())
 
+    def node_coordinates(self, p):
+        """(num_nodes, 3): the trilinear image of each element's Gauss-Lobatto
+        nodes (nodes shared between elements get the same value)."""
+        out = np.zeros((self.num_nodes(p), 3))
+        conn = self.elem_nodes(p)
+        Xe = self.elem_coords()  # (ne, 3, 8)
+        g = np.linspace(0.0, 1.0, p + 1)
+        n = p + 1
+        for kz in range(n):
+            for ky in range(n):
+                for kx in range(n):
+                    s = (g[kx], g[ky], g[kz])
+                    w = np.array([(s[0] if a else 1 - s[0]) * (s[1] if b else 1 - s[1]) * (s[2] if c else 1 - s[2])
+                                  for c in range(2) for b in range(2) for a in range(2)])
+                    out[conn[:, kx + n * (ky + n * kz)]] = np.einsum("eiv,v->ei", Xe, w)
+        return out
+
 
 def box_vertices(nx, ny, nz, perturb=0.0, seed=0):
     """Unit-cube vertex grid; interior vertices moved by U(-perturb*h, perturb*h)
@@ -203,6 +220,28 @@ def box_vertices(nx, ny, nz, perturb=0.0, seed=0):
 
 
 # ----------------------------------------------------------- element level
+def basis_1d(p):
+    """B[q, k], G[q, k]: the order-p Gauss-Lobatto Lagrange basis (nodes
+    0, 1/p, ..., 1 for p <= 2) and its derivative at the p + 1 Gauss-Legendre
+    points of [0, 1]."""
+    nodes = np.linspace(0.0, 1.0, p + 1)
+    t, _ = np.polynomial.legendre.leggauss(p + 1)
+    x = 0.5 * (t + 1.0)
+    B = np.ones((p + 1, p + 1))
+    G = np.zeros((p + 1, p + 1))
+    for k in range(p + 1):
+        others = [j for j in range(p + 1) if j != k]
+        for j in others:
+            B[:, k] *= (x - nodes[j]) / (nodes[k] - nodes[j])
+        for m in others:
+            term = np.full(p + 1, 1.0 / (nodes[k] - nodes[m]))
+            for j in others:
+                if j != m:
+                    term *= (x - nodes[j]) / (nodes[k] - nodes[j])
+            G[:, k] += term
+    return B, G
+
+
 def geometric_factors(Xe, Q, use_ref=False):
     ne = Xe.shape[0]
     nq = Q ** 3
@@ -305,8 +344,11 @@ class OracleFunctional:
         self.ndofs = self.nnodes * c
         self.conn = mesh.elem_nodes(p)
         self.Xq, self.Jq = geometric_factors(mesh.elem_coords(), self.Q, use_ref)
+        self._geom0 = (self.Xq, self.Jq)
+        self.shape = None
         self.domain = []
         self.boundary = []
+        self._fgeom0 = []
         self.state = None
 
     def add_domain_integral(self, mat, params=None):
@@ -320,6 +362,9 @@ class OracleFunctional:
         Xf, fnodes = self.mesh.boundary_faces(self.p, sides)
         Xq, Jq = face_geometric_factors(Xf, self.Q, self.use_ref)
         self.boundary.append((bmat, params, fnodes, Xq, Jq))
+        self._fgeom0.append((Xq, Jq))
+        if self.shape is not None:
+            self.set_shape(self.shape)
 
     def _apply(self, mode, u, du=None, update=False, t=0.0):
         c, N = self.c, self.nnodes
@@ -337,6 +382,50 @@ class OracleFunctional:
             rF = boundary_kernel(bmat, self.p, mode, uF, Xq, Jq, params, duF, t, self.use_ref)
             out += scatter_add(rF, fnodes, c, N)
         return out
+
+    def set_shape(self, shape):
+        """Shape displacement p (3 * nnodes, byNODES; None = none), as serac's
+        ShapeAwareFunctional (shape_aware_functional.hpp:45-172): every integral
+        is evaluated with position X + p and dx/dxi = dX/dxi + dp/dxi, which is
+        the same as mapping the trial gradient by (I + dp/dX)^-1, scaling the
+        outputs by det(I + dp/dX) (flux by (I + dp/dX)^-T) and the boundary
+        weights by the area ratio."""
+        self.shape = None if shape is None else np.array(shape, dtype=np.float64, copy=True)
+        Xq0, Jq0 = self._geom0
+        if self.shape is None:
+            self.Xq, self.Jq = Xq0, Jq0
+            for k, (Xf0, Jf0) in enumerate(self._fgeom0):
+                bmat, params, fnodes, _, _ = self.boundary[k]
+                self.boundary[k] = (bmat, params, fnodes, Xf0, Jf0)
+            return
+        B, G = basis_1d(self.p)
+        n = self.p + 1
+        P3 = self.shape.reshape(3, self.nnodes)
+        # volume: phi[q, a], dphi[j][q, a] in lexicographic (x fastest) order
+        Bz, By, Bx = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+        a_x, a_y, a_z = Bx.ravel(), By.ravel(), Bz.ravel()
+        Qz, Qy, Qx = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+        q_x, q_y, q_z = Qx.ravel(), Qy.ravel(), Qz.ravel()
+        bx, by, bz = B[q_x][:, a_x], B[q_y][:, a_y], B[q_z][:, a_z]
+        gx, gy, gz = G[q_x][:, a_x], G[q_y][:, a_y], G[q_z][:, a_z]
+        phi = bx * by * bz
+        dphi = [gx * by * bz, bx * gy * bz, bx * by * gz]
+        pE = P3[:, self.conn]  # (3, ne, npe)
+        self.Xq = Xq0 + np.einsum("iea,qa->eiq", pE, phi)
+        self.Jq = Jq0 + np.stack([np.einsum("iea,qa->eiq", pE, dphi[j]) for j in range(3)], axis=1)
+        # faces: (s, t) lexicographic, s fastest
+        Tt, Ts = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+        a_s, a_t = Ts.ravel(), Tt.ravel()
+        q_s, q_t = Ts.ravel(), Tt.ravel()
+        fphi = B[q_s][:, a_s] * B[q_t][:, a_t]
+        fds = G[q_s][:, a_s] * B[q_t][:, a_t]
+        fdt = B[q_s][:, a_s] * G[q_t][:, a_t]
+        for k, (Xf0, Jf0) in enumerate(self._fgeom0):
+            bmat, params, fnodes, _, _ = self.boundary[k]
+            pF = P3[:, fnodes]  # (3, nf, npf)
+            Xf = Xf0 + np.einsum("ifa,qa->fiq", pF, fphi)
+            Jf = Jf0 + np.stack([np.einsum("ifa,qa->fiq", pF, fds), np.einsum("ifa,qa->fiq", pF, fdt)], axis=1)
+            self.boundary[k] = (bmat, params, fnodes, Xf, Jf)
 
     def residual(self, u, t=0.0, update_state=False):
         return self._apply(0, u, update=update_state, t=t)
@@ -497,3 +586,18 @@ def newton(f, u0, ess, rel_tol=1e-12, abs_tol=1e-14, max_iter=30, t=0.0):
         r = f.residual(u, t=t)
         r[ess] = 0.0
     return u, it, np.linalg.norm(r)
+
+
+def warm_start(f, u, u_target, ess, t=0.0):
+    """Load-step predictor of SolidMechanics::warmStartDisplacement
+    (solid_mechanics.hpp:1727-1770): d = essential-value increment, solve the
+    Dirichlet-eliminated J(u) x = -J(u) d on the free rows, return u + d + x."""
+    import scipy.sparse.linalg as spla
+
+    d = np.zeros_like(u)
+    d[ess] = u_target[ess] - u[ess]
+    rhs = -f.jvp(u, d, t=t)
+    rhs[ess] = 0.0
+    x = spla.spsolve(eliminate_dirichlet(f.assemble(u, t=t), ess).tocsc(), rhs)
+    x[ess] = 0.0
+    return u + d + x

@@ -15,8 +15,9 @@ from .functional import (  # noqa: F401
     Functional,
     Gradient,
     Mesh,
+    ShapeAwareFunctional,
     assemble,
     box_vertices,
     differentiate_wrt,
 )
-from .solver import CG, FGMRES, GMRES, JACOBI, JACOBI_CHEBYSHEV, NewtonSolver, SolverOptions  # noqa: F401,E402
+from .solver import CG, FGMRES, GMRES, JACOBI, JACOBI_CHEBYSHEV, LEARNED, NONE, NewtonSolver, SolverOptions  # noqa: F401,E402

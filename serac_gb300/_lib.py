@@ -39,6 +39,7 @@ SIGNATURES = {
     "sfx_form_num_dofs": (_c.c_int, [_vp, _i64p]),
     "sfx_form_add_domain_integral": (_c.c_int, [_vp, _c.c_int, _dp, _c.c_int]),
     "sfx_form_add_boundary_integral": (_c.c_int, [_vp, _c.c_int, _c.c_int, _dp]),
+    "sfx_form_set_shape_displacement": (_c.c_int, [_vp, _vp, _vp]),
     "sfx_residual": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp]),
     "sfx_linearize": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp]),
     "sfx_form_set_jvp_mode": (_c.c_int, [_vp, _c.c_int]),
@@ -75,6 +76,7 @@ SIGNATURES = {
     "sfx_solver_set_essential": (_c.c_int, [_vp, _i64p, _c.c_int64]),
     "sfx_solver_solve": (_c.c_int, [_vp, _c.c_double, _vp, _vp]),
     "sfx_solver_solve_linear": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp, _vp]),
+    "sfx_solver_warm_start": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp]),
     "sfx_solver_get_stats": (_c.c_int, [_vp, _vp]),
     "sfx_solver_set_learned": (_c.c_int, [_vp, _vp, _c.c_int, _c.c_int, _c.c_int, _vp]),
 }

@@ -129,6 +129,14 @@ __global__ void copy_entries(int64_t m, const int64_t* __restrict__ idx, const T
   if (k < m) x[idx[k]] = src[idx[k]];
 }
 
+// x[idx[k]] = a[idx[k]] - b[idx[k]]
+template <typename T>
+__global__ void diff_entries(int64_t m, const int64_t* __restrict__ idx, const T* __restrict__ a,
+                             const T* __restrict__ b, T* __restrict__ x) {
+  int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < m) x[idx[k]] = a[idx[k]] - b[idx[k]];
+}
+
 // r = b - r (in place on r)
 template <typename T>
 __global__ void rsub(int64_t n, const T* __restrict__ b, T* __restrict__ r) {

@@ -152,6 +152,26 @@ int launch_boundary_jvp_f32(const sfx_form_s& f, const float* u, const float* du
   return SFX_OK;
 }
 
+int compute_face_geometry(sfx_form_s& f, BoundaryIntegral& bi, cudaStream_t s) {
+  const int Q = f.p + 1;
+  const int64_t nqt = bi.num_faces * Q * Q;
+  if (nqt == 0) return SFX_OK;
+  const unsigned blocks = unsigned((nqt + 255) / 256);
+  if (f.has_shape) {
+    if (f.p == 1)
+      kernels::face_geometry_shape_kernel<1><<<blocks, 256, 0, s>>>(bi.Xf.p, bi.fconn.p, f.shape.p, f.nnodes,
+                                                                    bi.fgeom.p, bi.num_faces);
+    else
+      kernels::face_geometry_shape_kernel<2><<<blocks, 256, 0, s>>>(bi.Xf.p, bi.fconn.p, f.shape.p, f.nnodes,
+                                                                    bi.fgeom.p, bi.num_faces);
+  } else {
+    if (Q == 2) kernels::face_geometry_kernel<2><<<blocks, 256, 0, s>>>(bi.Xf.p, bi.fgeom.p, bi.num_faces);
+    else kernels::face_geometry_kernel<3><<<blocks, 256, 0, s>>>(bi.Xf.p, bi.fgeom.p, bi.num_faces);
+  }
+  SFX_CUDA_TRY(cudaGetLastError());
+  return SFX_OK;
+}
+
 int assemble_boundary(sfx_form_s& f, double* values, double* diag, cudaStream_t s) {
   for (const auto& bi : f.boundary) {
     int rc = f.p == 1 ? visit_bmaterial(bi, FaceMatrixFn<1>{f, bi, values, diag, s})
@@ -222,22 +242,18 @@ extern "C" int sfx_form_add_boundary_integral(sfx_form form, int bmaterial, int 
   bi.num_face_nodes = int64_t(ids.size());
   const int Q = p + 1, nq = Q * Q;
   const int64_t nqt = bi.num_faces * nq;
-  DeviceBuf<double> dXf;
   cudaError_t err;
   if ((err = bi.fconn.upload(fconn.data(), fconn.size())) != cudaSuccess ||
       (err = bi.node_ptr.upload(ptr.data(), ptr.size())) != cudaSuccess ||
       (err = bi.node_ids.upload(ids.data(), ids.size())) != cudaSuccess ||
       (err = bi.node_ent.upload(ent.data(), ent.size())) != cudaSuccess ||
-      (err = dXf.upload(Xf.data(), Xf.size())) != cudaSuccess ||
+      (err = bi.Xf.upload(Xf.data(), Xf.size())) != cudaSuccess ||
       (err = bi.fgeom.alloc(size_t(nqt) * kernels::FGEOM_STRIDE)) != cudaSuccess)
     return fail(SFX_ERR_CUDA, std::string("boundary setup: ") + cudaGetErrorString(err));
-  if (nqt > 0) {
-    const unsigned blocks = unsigned((nqt + 255) / 256);
-    if (Q == 2) kernels::face_geometry_kernel<2><<<blocks, 256>>>(dXf.p, bi.fgeom.p, bi.num_faces);
-    else kernels::face_geometry_kernel<3><<<blocks, 256>>>(dXf.p, bi.fgeom.p, bi.num_faces);
-    if ((err = cudaGetLastError()) != cudaSuccess || (err = cudaDeviceSynchronize()) != cudaSuccess)
-      return fail(SFX_ERR_CUDA, std::string("face geometry: ") + cudaGetErrorString(err));
-  }
+  (void)nqt;
+  if (int rc = compute_face_geometry(*form, bi, nullptr)) return rc;
+  if ((err = cudaDeviceSynchronize()) != cudaSuccess)
+    return fail(SFX_ERR_CUDA, std::string("face geometry: ") + cudaGetErrorString(err));
   const size_t escr = size_t(bi.num_faces) * npf * form->c;
   if (form->ef64.n < escr) {
     if (form->ef64.alloc(escr) != cudaSuccess || form->ef32.alloc(escr) != cudaSuccess)

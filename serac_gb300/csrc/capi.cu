@@ -64,6 +64,30 @@ int scatter_evector(const sfx_form_s& f, const double* E, double* out, bool accu
 
 using namespace sfx_impl;
 
+namespace sfx_impl {
+// geometric factors of the domain (and of every boundary integral) in the
+// reference configuration, or shape-displaced by f.shape when f.has_shape
+int compute_geometry(sfx_form_s& f, cudaStream_t s) {
+  const int64_t nqt = f.ne * f.NQ;
+  const unsigned blocks = unsigned((nqt + 255) / 256);
+  if (f.has_shape) {
+    if (f.p == 1)
+      sfx::kernels::geometry_shape_kernel<1><<<blocks, 256, 0, s>>>(f.Xe.p, f.conn.p, f.shape.p, f.nnodes, f.geom64.p,
+                                                                    f.geom32.p, f.ne);
+    else
+      sfx::kernels::geometry_shape_kernel<2><<<blocks, 256, 0, s>>>(f.Xe.p, f.conn.p, f.shape.p, f.nnodes, f.geom64.p,
+                                                                    f.geom32.p, f.ne);
+  } else {
+    if (f.Q == 2) sfx::kernels::geometry_kernel<2><<<blocks, 256, 0, s>>>(f.Xe.p, f.geom64.p, f.geom32.p, f.ne);
+    else sfx::kernels::geometry_kernel<3><<<blocks, 256, 0, s>>>(f.Xe.p, f.geom64.p, f.geom32.p, f.ne);
+  }
+  for (auto& bi : f.boundary)
+    if (int rc = compute_face_geometry(f, bi, s)) return rc;
+  SFX_CUDA_TRY(cudaGetLastError());
+  return SFX_OK;
+}
+}  // namespace sfx_impl
+
 extern "C" {
 
 const char* sfx_last_error(void) { return g_last_error.c_str(); }
@@ -159,8 +183,7 @@ int sfx_form_create(sfx_mesh mesh, int order, int components, sfx_form* out) {
       (err = f->node_ent.upload(ent.data(), ent.size())) != cudaSuccess)
     return cleanup_fail(SFX_ERR_CUDA, std::string("upload tables: ") + cudaGetErrorString(err));
   const int64_t nqt = f->ne * f->NQ;
-  DeviceBuf<double> dXe;
-  if ((err = dXe.upload(Xe.data(), Xe.size())) != cudaSuccess ||
+  if ((err = f->Xe.upload(Xe.data(), Xe.size())) != cudaSuccess ||
       (err = f->geom64.alloc(size_t(nqt) * sfx::kernels::GEOM_STRIDE)) != cudaSuccess ||
       (err = f->geom32.alloc(size_t(nqt) * sfx::kernels::GEOM_STRIDE)) != cudaSuccess ||
       (err = f->e64.alloc(size_t(f->ne) * f->NPE * components)) != cudaSuccess ||
@@ -168,13 +191,27 @@ int sfx_form_create(sfx_mesh mesh, int order, int components, sfx_form* out) {
       (err = f->u_lin64.alloc(size_t(f->ndofs))) != cudaSuccess ||
       (err = f->u_lin32.alloc(size_t(f->ndofs))) != cudaSuccess)
     return cleanup_fail(SFX_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(err));
-  unsigned blocks = unsigned((nqt + 255) / 256);
-  if (f->Q == 2) sfx::kernels::geometry_kernel<2><<<blocks, 256>>>(dXe.p, f->geom64.p, f->geom32.p, f->ne);
-  else sfx::kernels::geometry_kernel<3><<<blocks, 256>>>(dXe.p, f->geom64.p, f->geom32.p, f->ne);
-  if ((err = cudaGetLastError()) != cudaSuccess || (err = cudaDeviceSynchronize()) != cudaSuccess)
+  if (int rc = sfx_impl::compute_geometry(*f, nullptr)) {
+    delete f;
+    return rc;
+  }
+  if ((err = cudaDeviceSynchronize()) != cudaSuccess)
     return cleanup_fail(SFX_ERR_CUDA, std::string("geometry kernel: ") + cudaGetErrorString(err));
   *out = f;
   return SFX_OK;
+}
+
+int sfx_form_set_shape_displacement(sfx_form form, const double* shape, void* stream) {
+  if (check_form(form)) return fail(SFX_ERR_INVALID, "null form");
+  auto st = static_cast<cudaStream_t>(stream);
+  if (shape) {
+    const size_t n = size_t(3 * form->nnodes);
+    if (form->shape.n < n && form->shape.alloc(n) != cudaSuccess) return fail(SFX_ERR_NOMEM, "shape allocation");
+    SFX_CUDA_TRY(cudaMemcpyAsync(form->shape.p, shape, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  }
+  form->has_shape = shape != nullptr;
+  form->linearized = false;  // the stored tangent belongs to the old geometry
+  return sfx_impl::compute_geometry(*form, st);
 }
 
 int sfx_form_destroy(sfx_form form) {

@@ -29,6 +29,9 @@ int launch_boundary_jvp_f32(const sfx_form_s& f, const float* u, const float* du
                             cudaStream_t s);
 // face element matrices at the linearisation point added into CSR values and/or a diagonal
 int assemble_boundary(sfx_form_s& f, double* values, double* diag, cudaStream_t s);
+// geometric factors (reference or shape-displaced configuration)
+int compute_face_geometry(sfx_form_s& f, BoundaryIntegral& bi, cudaStream_t s);
+int compute_geometry(sfx_form_s& f, cudaStream_t s);
 
 // diagonal of the element Jacobians from the stored tangent (E-vector)
 int launch_diag_from_tangent(const sfx_form_s& f, const DomainIntegral& di, double* E, cudaStream_t s);

@@ -79,6 +79,7 @@ struct BoundaryIntegral {
   int64_t num_faces = 0;
   DeviceBuf<int32_t> fconn;     // [f][(p+1)^2] node ids
   DeviceBuf<double> fgeom;      // FGEOM_STRIDE x nq_total
+  DeviceBuf<double> Xf;         // [f][3][4] face vertex coordinates (reference configuration)
   DeviceBuf<int32_t> node_ptr;  // over the distinct face nodes (compact list)
   DeviceBuf<int32_t> node_ids;  // global node of each compact entry
   DeviceBuf<int32_t> node_ent;  // (f * npf + local) entries, face order
@@ -101,6 +102,9 @@ struct sfx_form_s {
   sfx_impl::DeviceBuf<int32_t> node_ent;  // e * NPE + local, element order
   sfx_impl::DeviceBuf<double> geom64;
   sfx_impl::DeviceBuf<float> geom32;
+  sfx_impl::DeviceBuf<double> Xe;     // [e][3][8] element vertex coordinates (reference configuration)
+  sfx_impl::DeviceBuf<double> shape;  // shape displacement [3][nnodes] when has_shape
+  bool has_shape = false;
   sfx_impl::DeviceBuf<double> e64;  // E-vector scratch
   sfx_impl::DeviceBuf<float> e32;
   sfx_impl::DeviceBuf<double> ef64;  // face E-vector scratch

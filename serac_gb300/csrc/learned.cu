@@ -142,12 +142,16 @@ void conv_fwd(int ci, int co, bool relu, Grid3 g, const bf16* x, const bf16* W, 
   SFX_PAIRS(SFX_CONV)
 #undef SFX_CONV
 }
-void conv_wgrad(int ci, int co, Grid3 g, const bf16* x, const float* dy, float* part, int nchunks, int64_t chunk,
-                cudaStream_t s) {
-#define SFX_WG(CI, CO)                                                                        \
-  if (ci == CI && co == CO) {                                                                 \
-    sfx::nn::conv3_wgrad_partial<CI, CO><<<nchunks, 256, 0, s>>>(g, x, dy, chunk, part);      \
-    return;                                                                                   \
+// blocks of the weight-gradient kernel for a grid (at most 4 per SM)
+int wgrad_blocks(Grid3 g) {
+  const int64_t nchunks = (g.nodes() + sfx::nn::kWgradChunk - 1) / sfx::nn::kWgradChunk;
+  return int(std::min<int64_t>(nchunks, 4 * 152));
+}
+void conv_wgrad(int ci, int co, Grid3 g, const bf16* x, const bf16* dy, float* part, cudaStream_t s) {
+#define SFX_WG(CI, CO)                                                                          \
+  if (ci == CI && co == CO) {                                                                   \
+    sfx::nn::conv3_wgrad_mma<CI, CO><<<wgrad_blocks(g), 128, 0, s>>>(g, x, dy, part);           \
+    return;                                                                                     \
   }
   SFX_PAIRS(SFX_WG)
 #undef SFX_WG
@@ -175,7 +179,7 @@ struct Conv {
 };
 
 enum { A0, B0L, A1, B1L, A2, B2L, A3, U2, U1, U0, OUTL, NLAYERS };
-constexpr int kMaxChunks = 64;
+constexpr int kLevel[NLAYERS] = {0, 0, 1, 1, 2, 2, 3, 2, 1, 0, 0};  // grid level of each layer
 
 struct Work {
   Grid3 g[4];
@@ -239,7 +243,10 @@ int get_work(sfx_lnet net, int nx, int ny, int nz, Work** out) {
                   &w->gC2, &w->gB1, &w->gA1, &w->gC1, &w->gB0, &w->gA0, &w->gpre, &w->tmpf})
     ok = ok && b->alloc(big) == cudaSuccess;
   ok = ok && w->gpre16.alloc(big) == cudaSuccess;
-  ok = ok && w->part.alloc(size_t(kMaxChunks) * 48 * 27 * 48) == cudaSuccess &&
+  size_t npart = 0;
+  for (int l = 0; l < NLAYERS; l++)
+    npart = std::max(npart, size_t(wgrad_blocks(w->g[kLevel[l]])) * size_t(net->layers[l].nw()));
+  ok = ok && w->part.alloc(npart) == cudaSuccess &&
        w->red.alloc(size_t(48) * 27 * 48) == cudaSuccess && w->err.alloc(N0) == cudaSuccess &&
        w->scal.alloc(4) == cudaSuccess;
   if (!ok) return fail(SFX_ERR_NOMEM, "network workspace allocation failed");
@@ -295,9 +302,8 @@ void conv_bwd(sfx_lnet net, Work* w, int l, Grid3 g, const bf16* x, const bf16* 
   const Conv& c = net->layers[l];
   const int64_t N = g.nodes();
   act_bwd<<<nb(N * c.co), 256, 0, s>>>(gy, y, c.relu, w->gpre.p, w->gpre16.p, N * c.co);
-  const int64_t chunk = std::max<int64_t>(1, (N + kMaxChunks - 1) / kMaxChunks);
-  const int nch = int((N + chunk - 1) / chunk);
-  conv_wgrad(c.ci, c.co, g, x, w->gpre.p, w->part.p, nch, chunk, s);
+  const int nch = wgrad_blocks(g);
+  conv_wgrad(c.ci, c.co, g, x, w->gpre16.p, w->part.p, s);
   sfx::nn::reduce_chunks<<<nb(c.nw()), 256, 0, s>>>(w->part.p, nch, c.nw(), w->red.p);
   add_into<<<nb(c.nw()), 256, 0, s>>>(w->red.p, net->G.p + c.off, c.nw());
   bias_grad(c.co, w->gpre.p, N, w->red.p, s);

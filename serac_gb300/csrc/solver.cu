@@ -79,7 +79,7 @@ struct sfx_solver_s {
   DeviceBuf<int64_t> ess;
   int64_t n_ess = 0;
   // FP64 work vectors
-  DeviceBuf<double> r, du, tmp, tmp2, diag, cheb_d, cheb_r, V, Z, y;
+  DeviceBuf<double> r, du, tmp, tmp2, diag, cheb_d, cheb_r, V, Z, y, wx;
   // FP32 work vectors
   DeviceBuf<float> diag32, x32, b32, tmp32, tmp32b, cheb_d32, cheb_r32, V32, y32;
   Reducer<double, double> red;
@@ -89,7 +89,7 @@ struct sfx_solver_s {
   sfx_lnet net = nullptr;
   int grid[3] = {0, 0, 0};
   const float* features = nullptr;
-  DeviceBuf<float> nn_z, nn_res;
+  DeviceBuf<float> nn_z, nn_res, nn_x, Z32, x32b;
 };
 
 namespace {
@@ -356,42 +356,87 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
     };
   } else if (o.precond == SFX_PREC_LEARNED) {
     if (!s->net || !s->features) return fail(SFX_ERR_INVALID, "SFX_PREC_LEARNED needs sfx_solver_set_learned");
+    const int k = o.inner_iterations;
     if (ensure(s->x32, n) || ensure(s->b32, n) || ensure(s->tmp32, n) || ensure(s->diag32, n) ||
         ensure(s->cheb_d32, n) || ensure(s->cheb_r32, n) || ensure(s->tmp32b, n) || ensure(s->nn_z, n) ||
-        ensure(s->nn_res, n))
+        ensure(s->nn_res, n) || ensure(s->nn_x, n) ||
+        (o.mixed_precision && (ensure(s->V32, size_t(k + 1) * n) || ensure(s->Z32, size_t(k) * n) ||
+                               ensure(s->y32, size_t(k + 1)) || ensure(s->x32b, n))))
       return fail(SFX_ERR_NOMEM, "FP32 workspace allocation failed");
     sfx_blas::convert<double, float><<<nblocks(n), 256, 0, st>>>(n, s->diag.p, s->diag32.p);
     if (int rc = estimate_lmax<float, float>(s, apply_J32, s->diag32.p, s->tmp32.p, s->cheb_r32.p, s->red32,
                                              &s->lmax32, st))
       return rc;
-    prec = [=](const double* v, double* z) -> int {
+    // FP32 two-stage preconditioner z ~ J^-1 b.  Cycle 0: network, then
+    // Chebyshev on what it leaves.  Cycle 1: Chebyshev, network on the
+    // remaining residual, Chebyshev again.  The network's step, scaled to
+    // minimise the residual, is kept only when it takes at least 1 % off the
+    // residual norm; otherwise it is skipped (a fallback).
+    std::function<int(const float*, float*)> learned = [=](const float* b, float* z) -> int {
       cudaError_t err;
-      sfx_blas::convert<double, float><<<nblocks(n), 256, 0, st>>>(n, v, s->b32.p);
-      if (int rc = lnet_apply(s->net, s->grid[0], s->grid[1], s->grid[2], s->b32.p, s->features, s->nn_z.p, st))
-        return rc;
-      s->stats.learned_applications++;
-      // what the network leaves of the residual: res = v - J z_nn
-      if (int rc = apply_J32(s, s->nn_z.p, s->nn_res.p, st)) return rc;
-      sfx_blas::rsub<float><<<nblocks(n), 256, 0, st>>>(n, s->b32.p, s->nn_res.p);
-      const double nr = double(s->red32.dot(s->nn_res.p, s->nn_res.p, n, st, &err));
-      SFX_CUDA_TRY(err);
-      const double nv = double(s->red32.dot(s->b32.p, s->b32.p, n, st, &err));
-      SFX_CUDA_TRY(err);
-      if (std::isfinite(nr) && nr < nv) {
-        // z = z_nn + Chebyshev(res)
-        if (int rc = chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, s->nn_res.p, s->x32.p,
-                                             s->cheb_d32.p, s->cheb_r32.p, st))
+      // res = b - J z for the current z (z = 0: res = b)
+      const float* res = b;
+      if (o.learned_cycle == 1) {
+        if (int rc = chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, b, z, s->cheb_d32.p,
+                                             s->cheb_r32.p, st))
           return rc;
-        sfx_blas::axpby<float><<<nblocks(n), 256, 0, st>>>(n, 1.0f, s->nn_z.p, 1.0f, s->x32.p);
+        if (int rc = apply_J32(s, z, s->nn_res.p, st)) return rc;
+        sfx_blas::rsub<float><<<nblocks(n), 256, 0, st>>>(n, b, s->nn_res.p);
+        res = s->nn_res.p;
+      } else {
+        SFX_CUDA_TRY(cudaMemsetAsync(z, 0, sizeof(float) * n, st));
+      }
+      const double nv = double(s->red32.dot(res, res, n, st, &err));
+      SFX_CUDA_TRY(err);
+      if (int rc = lnet_apply(s->net, s->grid[0], s->grid[1], s->grid[2], res, s->features, s->nn_z.p, st)) return rc;
+      s->stats.learned_applications++;
+      // trial z' = z + a z_nn with a minimising |res - a J z_nn|; accepted
+      // when it takes at least 1 % off the residual norm
+      if (int rc = apply_J32(s, s->nn_z.p, s->tmp32.p, st)) return rc;
+      const double rj = double(s->red32.dot(res, s->tmp32.p, n, st, &err));
+      SFX_CUDA_TRY(err);
+      const double jj = double(s->red32.dot(s->tmp32.p, s->tmp32.p, n, st, &err));
+      SFX_CUDA_TRY(err);
+      const double a = jj > 0.0 ? rj / jj : 0.0;
+      const double nr = nv - a * rj;  // |res - a J z_nn|^2
+      const float* res2 = res;
+      if (std::isfinite(a) && std::isfinite(jj) && jj > 0.0 && nr <= 0.9801 * nv) {
+        sfx_blas::axpby<float><<<nblocks(n), 256, 0, st>>>(n, float(a), s->nn_z.p, 1.0f, z);
+        sfx_blas::axpby<float><<<nblocks(n), 256, 0, st>>>(n, 1.0f, res, float(-a), s->tmp32.p);
+        res2 = s->tmp32.p;
       } else {
         s->stats.learned_fallbacks++;
-        if (int rc = chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, s->b32.p, s->x32.p,
-                                             s->cheb_d32.p, s->cheb_r32.p, st))
-          return rc;
       }
-      sfx_blas::convert<float, double><<<nblocks(n), 256, 0, st>>>(n, s->x32.p, z);
+      // z += Chebyshev(res2)
+      if (int rc = chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, res2, s->nn_x.p, s->cheb_d32.p,
+                                           s->cheb_r32.p, st))
+        return rc;
+      sfx_blas::axpby<float><<<nblocks(n), 256, 0, st>>>(n, 1.0f, s->nn_x.p, 1.0f, z);
       return SFX_OK;
     };
+    if (o.mixed_precision) {
+      // inner FP32 flexible GMRES(k) preconditioned by the two-stage step
+      prec = [=](const double* v, double* z) -> int {
+        sfx_blas::convert<double, float><<<nblocks(n), 256, 0, st>>>(n, v, s->b32.p);
+        SFX_CUDA_TRY(cudaMemsetAsync(s->x32b.p, 0, sizeof(float) * n, st));
+        int it = 0;
+        double rel_in = 0.0;
+        if (int rc = gmres<float, float>(s, apply_J32, learned, true, s->b32.p, s->x32b.p, s->V32.p, s->Z32.p,
+                                         s->cheb_r32.p, s->y32.p, s->red32, k, k, o.inner_rel_tol, 0.0, &it, &rel_in,
+                                         st))
+          return rc;
+        s->stats.inner_iterations += it;
+        sfx_blas::convert<float, double><<<nblocks(n), 256, 0, st>>>(n, s->x32b.p, z);
+        return SFX_OK;
+      };
+    } else {
+      prec = [=](const double* v, double* z) -> int {
+        sfx_blas::convert<double, float><<<nblocks(n), 256, 0, st>>>(n, v, s->b32.p);
+        if (int rc = learned(s->b32.p, s->x32.p)) return rc;
+        sfx_blas::convert<float, double><<<nblocks(n), 256, 0, st>>>(n, s->x32.p, z);
+        return SFX_OK;
+      };
+    }
   } else if (o.mixed_precision) {
     // inner FP32 GMRES(k) with FP32 Jacobi-Chebyshev on the FP32 stored tangent
     const int k = o.inner_iterations;
@@ -458,6 +503,7 @@ int sfx_solver_default_options(sfx_solver_options* o) {
   o->inner_iterations = 20;
   o->inner_rel_tol = 1e-3;
   o->print_level = 0;
+  o->learned_cycle = 0;
   return SFX_OK;
 }
 
@@ -469,7 +515,8 @@ int sfx_solver_create(sfx_form form, const sfx_solver_options* opt, sfx_solver* 
   s->form = form;
   if (opt) s->opt = *opt;
   else sfx_solver_default_options(&s->opt);
-  if (s->opt.restart < 1 || s->opt.chebyshev_degree < 1 || s->opt.inner_iterations < 1) {
+  if (s->opt.restart < 1 || s->opt.chebyshev_degree < 1 || s->opt.inner_iterations < 1 ||
+      s->opt.learned_cycle < 0 || s->opt.learned_cycle > 1) {
     delete s;
     return fail(SFX_ERR_INVALID, "bad solver options");
   }
@@ -542,6 +589,29 @@ int sfx_solver_solve(sfx_solver s, double t, double* u, void* stream) {
   s->stats.final_residual = rn;
   s->stats.converged = rn <= target ? 1 : 0;
   return s->stats.converged ? SFX_OK : fail(SFX_ERR_NOT_CONVERGED, "Newton did not converge");
+}
+
+int sfx_solver_warm_start(sfx_solver s, double t, double* u, const double* u_target, void* stream) {
+  if (!s || !u || !u_target) return fail(SFX_ERR_INVALID, "null argument");
+  auto st = static_cast<cudaStream_t>(stream);
+  const int64_t n = s->n;
+  s->stats = sfx_solver_stats{};
+  if (s->n_ess == 0) return SFX_OK;
+  if (ensure(s->wx, size_t(n))) return fail(SFX_ERR_NOMEM, "workspace allocation failed");
+  // d: the essential-value increment, zero elsewhere
+  SFX_CUDA_TRY(cudaMemsetAsync(s->du.p, 0, sizeof(double) * n, st));
+  sfx_blas::diff_entries<double><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, u_target, u, s->du.p);
+  // rhs = -J(u) d on the free rows, 0 on the essential rows
+  if (int rc = sfx_linearize(s->form, t, u, nullptr, st)) return rc;
+  if (int rc = sfx_jvp(s->form, s->du.p, s->r.p, st)) return rc;
+  sfx_blas::scale<double><<<nblocks(n), 256, 0, st>>>(n, -1.0, s->r.p);
+  sfx_blas::set_entries<double><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, 0.0, s->r.p);
+  // x = J_ff^-1 rhs (x = 0 on the essential rows); u += d + x
+  if (int rc = linear_solve(s, s->r.p, s->wx.p, st)) return rc;
+  sfx_blas::axpby<double><<<nblocks(n), 256, 0, st>>>(n, 1.0, s->du.p, 1.0, u);
+  sfx_blas::axpby<double><<<nblocks(n), 256, 0, st>>>(n, 1.0, s->wx.p, 1.0, u);
+  SFX_CUDA_TRY(cudaGetLastError());
+  return SFX_OK;
 }
 
 int sfx_solver_set_learned(sfx_solver s, sfx_lnet net, int nx, int ny, int nz, const float* features) {

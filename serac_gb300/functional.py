@@ -227,6 +227,16 @@ class Functional:
         re-evaluates the q-function on dual numbers."""
         _lib.call("sfx_form_set_jvp_mode", self._h, int(mode))
 
+    def set_shape_displacement(self, shape, stream=None):
+        """Evaluate every integral on the configuration X + shape (float64 CUDA
+        tensor, 3 * num_nodes, byNODES; None = the reference configuration),
+        as serac's ShapeAwareFunctional.  Linearise again afterwards."""
+        if shape is None:
+            _lib.call("sfx_form_set_shape_displacement", self._h, None, _stream(stream))
+        else:
+            _require(shape, torch.float64, 3 * self.num_nodes, "shape")
+            _lib.call("sfx_form_set_shape_displacement", self._h, _dptr(shape), _stream(stream))
+
     def updateQdata(self, flag: bool):
         _lib.call("sfx_update_qdata", self._h, int(bool(flag)))
 
@@ -287,6 +297,44 @@ class Functional:
         out = torch.empty(self.ndofs, dtype=torch.float64, device="cuda") if out is None else out
         _lib.call("sfx_assemble_diagonal", self._h, _dptr(out), _stream(stream))
         return out
+
+
+class ShapeAwareFunctional:
+    """ShapeAwareFunctional<H1<p,3>, H1<p,c>(H1<p,c>)> (shape_aware_functional.hpp:330-560):
+    the shape displacement is the first argument after time and is held
+    fixed by the evaluation.
+
+        saf = ShapeAwareFunctional(mesh, H1(2, 3), H1(2, 3))
+        saf.AddDomainIntegral(NEOHOOKEAN, [K, G])
+        r = saf(t, shape, u)
+        r, dRdu = saf(t, shape, differentiate_wrt(u))
+    """
+
+    def __init__(self, mesh: Mesh, shape_space: H1, space: H1):
+        if shape_space.components != 3 or shape_space.order != space.order:
+            raise ValueError("the shape space must be H1 with 3 components and the trial space's order")
+        self.functional = Functional(mesh, space)
+        self.ndofs = self.functional.ndofs
+        self._shape_key = None
+
+    def AddDomainIntegral(self, *a, **k):
+        return self.functional.AddDomainIntegral(*a, **k)
+
+    def AddBoundaryIntegral(self, *a, **k):
+        return self.functional.AddBoundaryIntegral(*a, **k)
+
+    def updateQdata(self, flag):
+        return self.functional.updateQdata(flag)
+
+    def _use(self, shape):
+        key = (shape.data_ptr(), shape._version)
+        if key != self._shape_key:
+            self.functional.set_shape_displacement(shape)
+            self._shape_key = key
+
+    def __call__(self, t, shape, arg, out=None):
+        self._use(shape)
+        return self.functional(t, arg, out)
 
 
 def assemble(gradient: Gradient):

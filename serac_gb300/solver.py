@@ -41,6 +41,7 @@ class SolverOptions(ctypes.Structure):
         ("inner_iterations", ctypes.c_int),
         ("inner_rel_tol", ctypes.c_double),
         ("print_level", ctypes.c_int),
+        ("learned_cycle", ctypes.c_int),
     ]
 
     @classmethod
@@ -110,6 +111,15 @@ class NewtonSolver:
         rc = _lib.load().sfx_solver_solve(self._h, float(t), _dptr(u), _stream(stream))
         if rc != 0 and (raise_on_failure or rc != ERR_NOT_CONVERGED):
             _lib.check(rc)
+        return self.stats()
+
+    def warm_start(self, t, u, u_target, stream=None):
+        """Load-step predictor (SolidMechanics::warmStartDisplacement): moves
+        the essential vdofs of u to u_target's values and the free vdofs by
+        the linearised response to that change."""
+        _require(u, torch.float64, self.form.ndofs, "u")
+        _require(u_target, torch.float64, self.form.ndofs, "u_target")
+        _lib.call("sfx_solver_warm_start", self._h, float(t), _dptr(u), _dptr(u_target), _stream(stream))
         return self.stats()
 
     def solve_linear(self, t, u_lin, rhs, out=None, stream=None):

@@ -136,6 +136,24 @@ extern "C" int frontend_neohookean(int p, double K, double G, int nx, int ny, in
                                                             setup);
 }
 
+// Neo-Hookean on a shape-displaced configuration (ShapeAwareFunctional)
+extern "C" int frontend_neohookean_shape(double K, double G, int nx, int ny, int nz, const double* V,
+                                         const double* shape_host, int64_t nshape, const double* u, const double* du,
+                                         double* r, double* r2, double* jv, double* jv32, double* diag, double* csr,
+                                         int64_t* nnz) {
+  double* shape = nullptr;
+  if (cudaMalloc(&shape, size_t(nshape) * 8) != cudaSuccess) return -2;
+  cudaMemcpy(shape, shape_host, size_t(nshape) * 8, cudaMemcpyHostToDevice);
+  auto setup = [K, G, shape](auto& f) {
+    f.AddDomainIntegral(sfx::Dimension<3>{}, sfx::DependsOn<0>{}, UserNeoHookean{K, G});
+    f.SetShapeDisplacement(shape);
+  };
+  const int rc = run<sfx::ShapeAwareFunctional<sfx::H1<2, 3>, sfx::H1<2, 3>(sfx::H1<2, 3>)>>(
+      nx, ny, nz, V, u, du, r, r2, jv, jv32, diag, csr, nnz, setup);
+  cudaFree(shape);
+  return rc;
+}
+
 // J2 through the library's material functor with a QuadratureData state:
 // commit the state at u (updateQdata), then linearise at 1.5 u.
 extern "C" int frontend_j2(int nx, int ny, int nz, const double* V, const double* u, const double* du, double E,

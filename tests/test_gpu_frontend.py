@@ -75,6 +75,37 @@ def test_user_qfunction_matches_oracle(cuda, felib, kind, p):
     assert rel(csr, A.data) <= 1e-12
 
 
+def test_shape_aware_user_qfunction_matches_oracle(cuda, felib):
+    """sfx::ShapeAwareFunctional with a user Neo-Hookean q-function on a
+    non-trilinear order-2 shape displacement."""
+    dims = (3, 2, 2)
+    m = mesh(*dims, perturb=0.1, seed=2)
+    mat = O.MAT_NEOHOOKEAN
+    orc = O.OracleFunctional(m, 2, 3)
+    orc.add_domain_integral(mat, PARAMS[mat])
+    shape = np.random.default_rng(5).uniform(-0.02, 0.02, 3 * orc.nnodes)
+    orc.set_shape(shape)
+    u, du = fields(orc.ndofs, mat, seed=8)
+    n = orc.ndofs
+    outs = [np.zeros(n) for _ in range(5)]
+    A = orc.assemble(u)
+    csr = np.zeros(A.nnz)
+    nnz = ctypes.c_int64()
+    V = np.ascontiguousarray(m.vertices)
+    K, G = PARAMS[mat]
+    rc = felib.frontend_neohookean_shape(ctypes.c_double(K), ctypes.c_double(G), *dims, _p(V), _p(shape),
+                                         ctypes.c_int64(shape.size), _p(u), _p(du), *[_p(o) for o in outs], _p(csr),
+                                         ctypes.byref(nnz))
+    assert rc == 0
+    r, r2, jv, jv32, diag = outs
+    assert rel(r, orc.residual(u)) <= 1e-12
+    assert rel(r2, orc.residual(u)) <= 1e-12
+    assert rel(jv, orc.jvp(u, du)) <= 1e-12
+    assert rel(jv32, orc.jvp(u, du)) <= 1e-5
+    assert rel(diag, A.diagonal()) <= 1e-12
+    assert rel(csr, A.data) <= 1e-12
+
+
 def test_user_qfunction_with_quadrature_state(cuda, felib):
     dims = (3, 2, 2)
     m = mesh(*dims, perturb=0.1, seed=4)

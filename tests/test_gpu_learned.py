@@ -114,3 +114,43 @@ def test_training_reduces_loss(cuda):
     assert np.isfinite(losses).all()
     assert losses[-1] < 0.5 * losses[0]
     L.load().sfx_lnet_destroy(h)
+
+
+def _solve_steps(prob, opts, net=None):
+    import serac_gb300 as sg
+    from serac_gb300 import learned as LP
+
+    S = LP.SolidSetup(prob)
+    s = sg.NewtonSolver(S.f, opts)
+    s.set_essential(S.ess)
+    if net is not None:
+        s.set_learned(net, S.grid, S.features)
+    u, tot = LP.solve_load_steps(S, s)
+    assert tot["converged"] == 1
+    return u, tot
+
+
+_TIGHT = dict(newton_rel_tol=1e-10, newton_abs_tol=1e-16, krylov_rel_tol=1e-10, krylov_abs_tol=1e-18,
+              max_krylov_iterations=4000)
+
+
+@pytest.mark.parametrize("mixed", [0, 1])
+def test_corrupted_weights_fall_back_and_keep_the_answer(cuda, mixed):
+    """Network weights replaced by large noise (a host-side corruption before
+    upload): every network step is rejected, Jacobi-Chebyshev carries the
+    solve, and the converged displacement equals the plain FP64 solve's."""
+    import serac_gb300 as sg
+    from serac_gb300 import learned as LP
+
+    prob = LP.j2_problem(4, 2000, steps=2)
+    plain = sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, **_TIGHT)
+    u_ref, _ = _solve_steps(prob, plain)
+    net = LP.LearnedPreconditioner(seed=5)
+    rng = np.random.default_rng(0)
+    net.set_params(rng.standard_normal(net.num_params).astype(np.float32) * 50.0)
+    opts = sg.SolverOptions.defaults(precond=sg.LEARNED, mixed_precision=mixed, **_TIGHT)
+    u, st = _solve_steps(prob, opts, net)
+    assert st["learned_applications"] > 0
+    assert st["learned_fallbacks"] >= 0.9 * st["learned_applications"]
+    err = float(torch.linalg.norm(u - u_ref) / torch.linalg.norm(u_ref))
+    assert err <= 1e-9, err

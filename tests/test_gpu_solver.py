@@ -121,3 +121,48 @@ def test_solver_is_bitwise_reproducible(cuda):
         s.solve(0.0, u)
         outs.append(u.clone())
     assert torch.equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("precond", ["chebyshev", "mixed"])
+def test_j2_load_steps_match_oracle(cuda, precond):
+    """Small-strain J2 plasticity under compression in 4 load steps, each a
+    warm-start predictor (SolidMechanics::warmStartDisplacement) followed by
+    Newton; the plastic state is committed between steps.  The displacement
+    and the quadrature state after every step match the oracle's direct-solve
+    path to 1e-9."""
+    import serac_gb300 as sg
+
+    n, p, strain, steps = 3, 2, 0.02, 4
+    V = O.box_vertices(n, n, n, 0.1, 1)
+    m = O.StructuredHexMesh(n, n, n, V)
+    orc = O.OracleFunctional(m, p, 3)
+    orc.add_domain_integral(O.MAT_J2, [100.0, 0.3, 1.0, 1.0])
+    mesh = sg.Mesh.structured_hex(n, n, n, V)
+    f = sg.Functional(mesh, sg.H1(p, 3))
+    f.AddDomainIntegral(sg.J2, [100.0, 0.3, 1.0, 1.0])
+    N = f.num_nodes
+    bottom, top = mesh.boundary_nodes(p, [1]), mesh.boundary_nodes(p, [6])
+    ess = np.concatenate([bottom, N + bottom, 2 * N + bottom, 2 * N + top])
+    kw = dict(newton_rel_tol=1e-11, newton_abs_tol=1e-13, krylov_rel_tol=1e-11, krylov_abs_tol=1e-18,
+              max_krylov_iterations=3000)
+    if precond == "mixed":
+        kw["mixed_precision"] = 1
+    s = sg.NewtonSolver(f, sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, **kw))
+    s.set_essential(ess)
+    u = torch.zeros(f.ndofs, dtype=torch.float64, device=cuda)
+    uo = np.zeros(f.ndofs)
+    for step in range(1, steps + 1):
+        target = np.zeros(f.ndofs)
+        target[2 * N + top] = -strain * step / steps
+        s.warm_start(0.0, u, torch.tensor(target, device=cuda))
+        st = s.solve(0.0, u)
+        assert st["converged"] == 1 and st["newton_iterations"] <= 8
+        uo = O.warm_start(orc, uo, target, ess)
+        uo, _, _ = O.newton(orc, uo, ess, rel_tol=1e-12, abs_tol=1e-14)
+        assert rel(u.cpu().numpy(), uo) <= 1e-9
+        f.updateQdata(True)
+        f.residual(0.0, u)
+        f.updateQdata(False)
+        orc.residual(uo, update_state=True)
+        assert rel(f.qdata().reshape(-1, 10), orc.state.reshape(-1, 10)) <= 1e-8
+    assert orc.state[..., 9].max() > 0.01  # the load drove the material well into plasticity
