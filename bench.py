@@ -265,9 +265,11 @@ def run_sfx(args, rank, world):
 
     # ---- FP32 Jv (inner Krylov operator)
     t_fp32 = timed(lambda: grad.mult(du32, dr32), args.steps)
-    # ---- dominant kernel alone (element kernel, no scatter)
+    # ---- dominant kernels alone (element kernels, no scatter)
     dE = torch.empty(mesh.num_elements * 81, dtype=torch.float64, device=dev)
     t_elem = timed(lambda: grad.element_action(du, dE), args.steps)
+    dE32 = torch.empty(mesh.num_elements * 81, dtype=torch.float32, device=dev)
+    t_elem32 = timed(lambda: grad.element_action(du32, dE32), args.steps)
     # ---- the same Jacobian action without the stored tangent (q-function on duals every call)
     f.set_jvp_mode(f.RECOMPUTE)
     f.linearize(0.0, u)
@@ -324,6 +326,19 @@ def run_sfx(args, rank, world):
         "kernel_ms": t_k * 1e3,
         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
     }
+    alg_bytes32 = 2 * 4 * ndofs + 81 * 4 * nq
+    t_k32 = statistics.mean(t_elem32)
+    roofline32 = {
+        "bound": "hbm",
+        "kernel": "sfx::kernels::jvp_stored_tma_kernel<3,false,false,8,3> (FP32, bulk-copy staged)",
+        "achieved": alg_bytes32 / t_k32 / 1e9,
+        "peak": hbm_peak,
+        "unit": "GB/s",
+        "frac": alg_bytes32 / t_k32 / 1e9 / hbm_peak,
+        "traffic": prof.get("dram_bytes_per_launch_f32"),
+        "algorithmic_bytes": alg_bytes32,
+        "kernel_ms": t_k32 * 1e3,
+    }
     compute = None
     if flops_per_elem:
         ach = flops_per_elem * ne / t_k / 1e12
@@ -350,7 +365,7 @@ def run_sfx(args, rank, world):
         "roofline": roofline,
         "compute_roofline": compute,
         "jv_fp32": {"value": ndofs * args.steps / sum(t_fp32) / 1e9, "unit": UNIT, "dtype": "f32",
-                    "ms_per_step": statistics.mean(t_fp32) * 1e3},
+                    "ms_per_step": statistics.mean(t_fp32) * 1e3, "roofline": roofline32},
         "jv_recompute": {"value_f64": ndofs * args.steps / sum(t_recompute) / 1e9,
                          "value_f32": ndofs * args.steps / sum(t_recompute32) / 1e9, "unit": UNIT,
                          "note": "q-function re-evaluated on dual numbers in every action; no stored tangent"},
@@ -358,12 +373,79 @@ def run_sfx(args, rank, world):
         "clocks": clk,
         "finite": ok,
     }
+    if args.newton_steps > 0 and rank == 0:
+        result["newton"] = newton_leg(args.newton_steps)
     if rank == 0:
         gd, reps, thr, el = cpu_jvp_rate(V, seconds=args.cpu_seconds)
         result["cpu_baseline"] = {"value": gd, "unit": UNIT, "cores": thr, "kind": "port",
                                   "sample": f"full workload, {reps} Jacobian actions in {el:.1f} s "
                                             "(stored-derivative form, derivative computed once untimed)"}
         print(json.dumps(result))
+
+
+NEWTON_N = 32
+NEWTON_SEED = 2000  # held out from the training seeds
+WEIGHTS = os.path.join(ROOT, "serac_gb300", "weights", "lnet_j2_q2.npy")
+
+
+def newton_leg(steps):
+    """Newton time-to-1e-8 relative residual on the heterogeneous J2 problem
+    (32^3 hexes, Q2 vector, per-element lognormal E, held-out seed), over the
+    first `steps` load steps (warm-start predictor, Newton, state commit):
+    plain FP64 GMRES(50) + Jacobi-Chebyshev against FP32-inner mixed precision
+    and, when trained weights are present, the learned preconditioner on top of
+    mixed precision.  Every variant reaches the same converged answer."""
+    import torch
+
+    import serac_gb300 as sg
+    from serac_gb300 import learned as LP
+
+    prob = LP.j2_problem(NEWTON_N, NEWTON_SEED)
+    base = dict(newton_rel_tol=1e-8, krylov_rel_tol=1e-8, max_krylov_iterations=5000)
+    variants = [("plain_fp64", sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, **base)),
+                ("mixed", sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, mixed_precision=1, **base))]
+    net = None
+    if os.path.exists(WEIGHTS):
+        net = LP.LearnedPreconditioner()
+        net.load(WEIGHTS)
+        variants.append(("learned_mixed", sg.SolverOptions.defaults(precond=sg.LEARNED, mixed_precision=1, **base)))
+    out = {"metric": "Newton time-to-1e-8 relative residual", "unit": "s", "higher_is_better": False,
+           "workload": f"j2_q2_vector_{NEWTON_N}cubed_lognormal_E (seed {NEWTON_SEED}), load steps 1-{steps} of "
+                       f"{prob.steps}, strain {prob.strain}",
+           "dofs": 3 * (2 * NEWTON_N + 1) ** 3}
+    ref = None
+    for name, opts in variants:
+        S = LP.SolidSetup(prob)
+        solver = sg.NewtonSolver(S.f, opts)
+        solver.set_essential(S.ess)
+        if name.startswith("learned"):
+            solver.set_learned(net, S.grid, S.features)
+        u = torch.zeros(S.f.ndofs, dtype=torch.float64, device="cuda")
+        tot = {}
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for step in range(1, steps + 1):
+            pre = S.predictor(solver, u, step)
+            st = solver.solve(0.0, u, raise_on_failure=False)
+            for k in ("newton_iterations", "krylov_iterations", "inner_iterations", "learned_applications",
+                      "learned_fallbacks"):
+                tot[k] = tot.get(k, 0) + st[k]
+            tot["predictor_krylov_iterations"] = tot.get("predictor_krylov_iterations", 0) + pre["krylov_iterations"]
+            tot["converged"] = min(tot.get("converged", 1), st["converged"])
+            S.commit(u)
+        torch.cuda.synchronize()
+        tot["seconds"] = time.perf_counter() - t0
+        if ref is None:
+            ref = u.clone()
+        tot["rel_diff_vs_plain"] = float(torch.linalg.norm(u - ref) / torch.linalg.norm(ref))
+        out[name] = tot
+        del solver, S
+    for name in ("mixed", "learned_mixed"):
+        if name in out:
+            out[f"speedup_{name}_vs_plain"] = out["plain_fp64"]["seconds"] / out[name]["seconds"]
+    if net is None:
+        out["learned_mixed"] = {"unavailable": f"no trained weights at {os.path.relpath(WEIGHTS, ROOT)}"}
+    return out
 
 
 def measure_fp64_peak(dev):
@@ -387,13 +469,20 @@ def measure_fp64_peak(dev):
 
 
 def load_profile_numbers():
-    """Per-launch DRAM traffic and FP64 operation count of the element kernel,
-    read from the committed ncu summary (profiles/), if present."""
-    path = os.path.join(ROOT, "profiles", "jvp_stored_f64_neohookean_q2_32cubed.json")
-    try:
-        return json.load(open(path))
-    except (OSError, ValueError):
-        return {}
+    """Per-launch DRAM traffic of the FP64 and FP32 element kernels, read from
+    the committed ncu summaries (profiles/), if present."""
+    out = {}
+    for name, key in (("jvp_stored_f64_neohookean_q2_32cubed.json", "dram_bytes_per_launch"),
+                      ("jvp_stored_tma_f32_neohookean_q2_32cubed.json", "dram_bytes_per_launch_f32")):
+        try:
+            d = json.load(open(os.path.join(ROOT, "profiles", name)))
+        except (OSError, ValueError):
+            continue
+        if key == "dram_bytes_per_launch":
+            out.update(d)
+        elif "dram_bytes_per_launch" in d:
+            out[key] = d["dram_bytes_per_launch"]
+    return out
 
 
 # ------------------------------------------------------------ reference arm
@@ -439,6 +528,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--kernels-only", action="store_true", help="run only the Jacobian actions (profiling)")
     ap.add_argument("--precision", choices=["f64", "f32"], default="f64", help="precision of --kernels-only")
+    ap.add_argument("--newton-steps", type=int, default=1,
+                    help="load steps of the Newton time-to-1e-8 leg (0 = skip)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -20,7 +20,7 @@
  *   sfx_residual                    numerics/functional/functional.hpp:502-513 operator()(t, u)
  *   sfx_linearize                   numerics/functional/functional.hpp:481-489 operator()(t, differentiate_wrt(u))
  *   sfx_jvp / sfx_jvp_f32           numerics/functional/functional.hpp:556-566 Gradient::Mult / operator()
- *   sfx_jvp_element                 numerics/functional/integral.hpp:93-103 Integral::GradientMult
+ *   sfx_jvp_element(_f32)           numerics/functional/integral.hpp:93-103 Integral::GradientMult
  *   sfx_csr_* / sfx_assemble_csr    numerics/functional/functional.hpp:569-667 assemble(Gradient&)
  *   sfx_update_qdata                numerics/functional/functional.hpp:523 updateQdata(bool)
  *   sfx_set_qdata / sfx_get_qdata   numerics/functional/quadrature_data.hpp:111-144 QuadratureData<T>
@@ -107,6 +107,13 @@ int sfx_form_add_boundary_integral(sfx_form form, int bmaterial, int side_mask, 
  * must be linearised again afterwards. */
 int sfx_form_set_shape_displacement(sfx_form form, const double* shape, void* stream);
 
+/* dr = dR/dp (t, u; p) dshape: the derivative of the residual with respect to
+ * the shape displacement p set on the form (zero when none is set), applied to
+ * dshape (device, 3 * num_nodes doubles) — ShapeAwareFunctional differentiated
+ * with respect to its argument 0 (shape_aware_functional.hpp:537-541).  Domain
+ * integrals; a form with boundary integrals returns SFX_ERR_UNSUPPORTED. */
+int sfx_shape_jvp(sfx_form form, double t, const double* u, const double* dshape, double* dr, void* stream);
+
 /* r = R(t, u) (device, num_dofs doubles each).  When sfx_update_qdata(form, 1)
  * is in effect, quadrature-point state is committed by this call. */
 int sfx_residual(sfx_form form, double t, const double* u, double* r, void* stream);
@@ -135,6 +142,8 @@ int sfx_jvp_f32(sfx_form form, const float* du, float* dr, void* stream);
  * integral.hpp:93-103): dE[e][component][node] (device, num_elements *
  * components * (order+1)^3 doubles) for the domain integral. */
 int sfx_jvp_element(sfx_form form, const double* du, double* dE, void* stream);
+/* The same in FP32 on the FP32 stored tangent (dE: num_elements * c * (p+1)^3 floats). */
+int sfx_jvp_element_f32(sfx_form form, const float* du, float* dE, void* stream);
 
 /* Sparsity of dR/du: every (test vdof, trial vdof) pair of every element,
  * rows sorted, columns sorted within a row (dof_numbering.hpp:290-351).

@@ -197,7 +197,7 @@ struct DomainIntegral : IntegralBase {
     check_cuda(cudaGetLastError(), "residual kernel");
   }
   void linearize(const sfx_form_layout& L, double t, const double* u, double* E, cudaStream_t s) override {
-    const size_t n = size_t(L.num_elements) * NQ * Shape::size;
+    const size_t n = size_t(L.num_elements) * size_t(Shape::template stride<NQ>);
     D64.resize(n);
     D32.resize(n);
     auto a = args(L, t, u, nullptr, nullptr);

@@ -17,6 +17,7 @@
 
 #include "sfx/dual.hpp"
 #include "sfx/materials.hpp"
+#include "sfx/bulk.cuh"
 #include "sfx/quadrature.hpp"
 #include "sfx/tensor.hpp"
 #include "sfx/tuple.hpp"
@@ -349,6 +350,143 @@ __global__ void __launch_bounds__(128) domain_kernel(DomainArgs<Real> a, QFMaker
       for (int k = 0; k < 3; k++) f[k] = dvol * (fp[0] * Ji[k][0] + fp[1] * Ji[k][1] + fp[2] * Ji[k][2]);
     }
     Real r = integrate_lane<Q, HS, HF, Real>(s, f[0], f[1], f[2], base, ix, iy, iz, sB, sG);
+    if (valid) out_e[c * NQ + qi] = r;
+  }
+}
+
+/// Derivative of the shape-aware residual with respect to the shape
+/// displacement, applied to a direction dp (serac's ShapeAwareFunctional
+/// differentiated with respect to argument 0, shape_aware_functional.hpp:537-541):
+/// the geometry is recomputed at each point from the element's vertices Xe
+/// ([e][3][8]) and the shape field p (nullptr = 0) with dual numbers carrying
+/// dp, x' = X + p + eps dp and dx'/dxi = J + dp/dxi + eps d(dp)/dxi, so that
+/// (dx'/dxi)^-1, det(dx'/dxi), the trial gradient du/dx' and the q-function
+/// output all carry their directional derivatives; the derivative part of the
+/// integrand is integrated into out_e [e][c][node].  a.u holds u, a.geom is
+/// not used; quadrature state is read, never written.
+template <int P, int C, typename State, typename QFMaker>
+__global__ void __launch_bounds__(128) shape_jvp_kernel(DomainArgs<double> a, QFMaker make_qf,
+                                                        const double* __restrict__ Xe,
+                                                        const double* __restrict__ shape,
+                                                        const double* __restrict__ dshape) {
+  using Real = double;
+  using S = dual<Real, Real>;
+  constexpr int Q = P + 1;
+  constexpr int NQ = Q * Q * Q;
+  constexpr int EPW = 32 / NQ;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int sub = lane / NQ;
+  const int qi_raw = lane - sub * NQ;
+  const bool slot = sub < EPW;
+  const int qi = slot ? qi_raw : NQ - 1;
+  const int base = slot ? sub * NQ : 0;
+  const int64_t e = warp * EPW + (slot ? sub : 0);
+  const bool valid = slot && e < a.num_elements;
+  const int ix = qi % Q, iy = (qi / Q) % Q, iz = qi / (Q * Q);
+
+  __shared__ Real sB[Q][Q], sG[Q][Q];
+  if (threadIdx.x < Q * Q) {
+    int i = threadIdx.x / Q, j = threadIdx.x % Q;
+    sB[i][j] = basis_table<P>().B[i][j];
+    sG[i][j] = basis_table<P>().G[i][j];
+  }
+  __syncthreads();
+
+  const int64_t nq_total = a.num_elements * NQ;
+  const int64_t gq = e * NQ + qi;
+  const int32_t node = valid ? a.conn[e * NQ + qi] : 0;
+
+  // trial field, shape field and shape direction at this lane's point
+  value_t<C, Real> uv{};
+  grad_t<C, Real> ug{};
+#pragma unroll
+  for (int c = 0; c < C; c++) {
+    Real U = valid ? a.u[c * a.num_nodes + node] : Real(0);
+    Real g[3];
+    interpolate_lane<Q, Real>(U, base, ix, iy, iz, sB, sG, comp<C>(uv, c), g[0], g[1], g[2]);
+    for (int j = 0; j < 3; j++) comp<C>(ug, c)[j] = g[j];
+  }
+  tensor<S, 3> xs{};
+  tensor<S, 3, 3> Js{};
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    Real pv = 0, pg[3] = {0, 0, 0}, dv = 0, dg[3] = {0, 0, 0};
+    Real Pn = (valid && shape) ? shape[i * a.num_nodes + node] : Real(0);
+    Real dPn = valid ? dshape[i * a.num_nodes + node] : Real(0);
+    interpolate_lane<Q, Real>(Pn, base, ix, iy, iz, sB, sG, pv, pg[0], pg[1], pg[2]);
+    interpolate_lane<Q, Real>(dPn, base, ix, iy, iz, sB, sG, dv, dg[0], dg[1], dg[2]);
+    xs[i] = S{pv, dv};
+#pragma unroll
+    for (int j = 0; j < 3; j++) Js[i][j] = S{pg[j], dg[j]};
+  }
+  // reference (trilinear) geometry at the point
+  const Real sp[3] = {gl_point(Q, ix), gl_point(Q, iy), gl_point(Q, iz)};
+  const Real w = gl_weight(Q, ix) * gl_weight(Q, iy) * gl_weight(Q, iz);
+  const Real* Xv = Xe + (valid ? e : 0) * 24;
+#pragma unroll
+  for (int v = 0; v < 8; v++) {
+    const int b0 = v & 1, b1 = (v >> 1) & 1, b2 = (v >> 2) & 1;
+    const Real N0 = b0 ? sp[0] : 1.0 - sp[0], N1 = b1 ? sp[1] : 1.0 - sp[1], N2 = b2 ? sp[2] : 1.0 - sp[2];
+    const Real d0 = b0 ? 1.0 : -1.0, d1 = b1 ? 1.0 : -1.0, d2 = b2 ? 1.0 : -1.0;
+    const Real phi = N0 * N1 * N2;
+    const Real g[3] = {d0 * N1 * N2, N0 * d1 * N2, N0 * N1 * d2};
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const Real xv = Xv[i * 8 + v];
+      xs[i].value += xv * phi;
+#pragma unroll
+      for (int j = 0; j < 3; j++) Js[i][j].value += xv * g[j];
+    }
+  }
+  if (!valid) {
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) Js[i][j] = S{Real(i == j), Real(0)};
+  }
+  const auto Jinv = inv(Js);
+  const S dvol = det(Js) * w;
+
+  // trial gradient in the shape-displaced configuration: du/dxi (dx'/dxi)^-1
+  value_t<C, S> qv{};
+  grad_t<C, S> qg{};
+#pragma unroll
+  for (int c = 0; c < C; c++) {
+    comp<C>(qv, c) = S{comp<C>(uv, c), Real(0)};
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+      comp<C>(qg, c)[j] = comp<C>(ug, c)[0] * Jinv[0][j] + comp<C>(ug, c)[1] * Jinv[1][j] +
+                          comp<C>(ug, c)[2] * Jinv[2][j];
+  }
+  const auto qf = make_qf(a.params + (valid ? e : 0) * QFMaker::nparams);
+  auto position = tuple{xs, Js};
+  auto arg = tuple{qv, qg};
+  auto call = [&]() {
+    if constexpr (std::is_same<State, Nothing>::value) {
+      return qf(a.t, position, arg);
+    } else {
+      State st{};
+      if (valid) load_state(st, a.state, gq, nq_total);
+      return qf(a.t, position, st, arg);
+    }
+  };
+  auto out = call();
+  using SrcT = std::decay_t<decltype(get<0>(out))>;
+  using FluxT = std::decay_t<decltype(get<1>(out))>;
+  constexpr bool HSrc = !is_zero<typename base_scalar<SrcT>::type>::value;
+  constexpr bool HFlx = !is_zero<typename base_scalar<FluxT>::type>::value;
+  Real* out_e = a.out_e + e * (C * NQ);
+#pragma unroll
+  for (int c = 0; c < C; c++) {
+    Real src = 0, f[3] = {0, 0, 0};
+    if constexpr (HSrc) src = part<JVP, Real>(dvol * source_comp<C>(get<0>(out), c));
+    if constexpr (HFlx) {
+      auto frow = flux_row<C>(get<1>(out), c);
+#pragma unroll
+      for (int k = 0; k < 3; k++) f[k] = part<JVP, Real>(dvol * (frow[0] * Jinv[k][0] + frow[1] * Jinv[k][1] + frow[2] * Jinv[k][2]));
+    }
+    Real r = integrate_lane<Q, HSrc, HFlx, Real>(src, f[0], f[1], f[2], base, ix, iy, iz, sB, sG);
     if (valid) out_e[c * NQ + qi] = r;
   }
 }
@@ -798,14 +936,19 @@ struct TangentShape {
   static constexpr int rows = (HS ? C : 0) + 3 * C;
   static constexpr int cols = (VI ? C : 0) + 3 * C;
   static constexpr int size = rows * cols;
+  /// entries of one element's block (size x NQ) rounded up to a multiple of
+  /// 4, so that every block starts on a 16-byte (FP32) / 32-byte (FP64)
+  /// boundary and can be moved by a bulk copy
+  template <int NQ>
+  static constexpr int64_t stride = (int64_t(size) * NQ + 3) / 4 * 4;
 };
 
 /// Linearise the q-function at every quadrature point (the derivative serac
 /// stores in evaluation_kernel_impl, domain_integral_kernels.hpp:209-214, after
 /// physical_to_parent, with det(J) w folded in) and, optionally, write the
 /// element residuals of the same evaluation.  D is stored element-major,
-/// D[((e * rows + row) * cols + col) * NQ + q], in FP64 and FP32, so that one
-/// element's tangent is one contiguous block.
+/// D[e * stride + (row * cols + col) * NQ + q] (stride = TangentShape::stride),
+/// in FP64 and FP32, so that one element's tangent is one contiguous block.
 template <int P, int C, typename State, typename QFMaker>
 __global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QFMaker make_qf, double* __restrict__ D64,
                                                         float* __restrict__ D32, double* __restrict__ res_e) {
@@ -916,8 +1059,9 @@ __global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QF
       if constexpr (HS) {
         Real v = dvol * part<JVP, Real>(source_comp<C>(get<0>(out), ci));
         if (valid) {
-          D64[(e * Shape::size + int64_t(ci) * Shape::cols + k) * NQ + qi] = v;
-          D32[(e * Shape::size + int64_t(ci) * Shape::cols + k) * NQ + qi] = float(v);
+          const int64_t at = e * Shape::template stride<NQ> + (int64_t(ci) * Shape::cols + k) * NQ + qi;
+          D64[at] = v;
+          D32[at] = float(v);
         }
       }
     }
@@ -939,8 +1083,9 @@ __global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QF
       for (int kd = 0; kd < 3; kd++) {
         Real v = dvol * (fp[0] * Ji[kd][0] + fp[1] * Ji[kd][1] + fp[2] * Ji[kd][2]);
         if (valid) {
-          D64[(e * Shape::size + int64_t(row + 3 * ci + kd) * Shape::cols + k) * NQ + qi] = v;
-          D32[(e * Shape::size + int64_t(row + 3 * ci + kd) * Shape::cols + k) * NQ + qi] = float(v);
+          const int64_t at = e * Shape::template stride<NQ> + (int64_t(row + 3 * ci + kd) * Shape::cols + k) * NQ + qi;
+          D64[at] = v;
+          D32[at] = float(v);
         }
         if (!have_res) res_f[ci][kd] = dvol * (fv[0] * Ji[kd][0] + fv[1] * Ji[kd][1] + fv[2] * Ji[kd][2]);
       }
@@ -1007,7 +1152,7 @@ __global__ void __launch_bounds__(128) jvp_stored_kernel(const Real* __restrict_
     din[off + 3 * c + 2] = g2;
   }
   Real dout[Shape::rows];
-  const Real* Dq = D + (valid ? e * Shape::size * NQ + qi : 0);
+  const Real* Dq = D + (valid ? e * Shape::template stride<NQ> + qi : 0);
 #pragma unroll
   for (int r = 0; r < Shape::rows; r++) {
     Real acc = 0;
@@ -1022,6 +1167,122 @@ __global__ void __launch_bounds__(128) jvp_stored_kernel(const Real* __restrict_
     Real r = integrate_lane<Q, HS, true, Real>(s, dout[roff + 3 * c], dout[roff + 3 * c + 1], dout[roff + 3 * c + 2],
                                                base, ix, iy, iz, sB, sG);
     if (valid) out_e[(e * C + c) * NQ + qi] = r;
+  }
+}
+
+/// FP32 Jacobian action from the stored tangent for Q2 elements, with each
+/// element's tangent block (81 x 27 floats for the vector Neo-Hookean case,
+/// 8.7 KB, contiguous) staged into shared memory by bulk asynchronous copies
+/// (cp.async.bulk) on mbarriers: each warp owns a ring of STAGES buffers and
+/// keeps STAGES - 1 copies in flight while it computes, so the kernel streams
+/// the tangent at HBM rate instead of waiting on 81 dependent loads per lane.
+/// Elements are dealt to warps round-robin (persistent grid).  A wait that
+/// does not complete sets *err and the warp drains its outstanding copies
+/// (again bounded) before returning.
+template <int C, bool HS, bool VI, int WARPS, int STAGES>
+__global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float* __restrict__ du,
+                                                                    const float* __restrict__ D,
+                                                                    const int32_t* __restrict__ conn,
+                                                                    float* __restrict__ out_e, int64_t num_nodes,
+                                                                    int64_t num_elements, int* __restrict__ err) {
+  constexpr int P = 2, Q = 3, NQ = 27;
+  using Shape = TangentShape<C, HS, VI>;
+  constexpr int64_t ES = Shape::template stride<NQ>;  // floats per element block
+  constexpr uint32_t BYTES = uint32_t(ES * 4);
+  static_assert(BYTES % 16 == 0, "bulk copies move multiples of 16 bytes");
+  extern __shared__ __align__(128) unsigned char sfx_dyn_smem[];
+  float* ring = reinterpret_cast<float*>(sfx_dyn_smem);                                 // [WARPS][STAGES][ES]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sfx_dyn_smem + size_t(WARPS) * STAGES * BYTES);  // [WARPS][STAGES]
+  __shared__ float sB[Q][Q], sG[Q][Q];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (threadIdx.x < Q * Q) {
+    const int i = threadIdx.x / Q, j = threadIdx.x % Q;
+    sB[i][j] = float(basis_table<P>().B[i][j]);
+    sG[i][j] = float(basis_table<P>().G[i][j]);
+  }
+  float* my_ring = ring + size_t(wid) * STAGES * ES;
+  uint64_t* my_bars = bars + wid * STAGES;
+  if (lane == 0) {
+    for (int s = 0; s < STAGES; s++) bulk::mbar_init(&my_bars[s], 1);
+    bulk::fence_mbar_init();
+  }
+  __syncthreads();
+
+  const int64_t first = int64_t(blockIdx.x) * WARPS + wid;
+  const int64_t step = int64_t(gridDim.x) * WARPS;
+  // prologue: the first STAGES elements of this warp
+  if (lane == 0) {
+    for (int s = 0; s < STAGES; s++) {
+      const int64_t e = first + s * step;
+      if (e < num_elements) {
+        bulk::mbar_arrive_expect_tx(&my_bars[s], BYTES);
+        bulk::copy_g2s(my_ring + s * ES, D + e * ES, BYTES, &my_bars[s]);
+      }
+    }
+  }
+  __syncwarp();
+
+  const bool lane_ok = lane < NQ;
+  const int qi = lane_ok ? lane : NQ - 1;
+  const int ix = qi % Q, iy = (qi / Q) % Q, iz = qi / (Q * Q);
+  int it = 0;
+  bool failed = false;
+  for (int64_t e = first; e < num_elements; e += step, it++) {
+    const int s = it % STAGES;
+    const uint32_t parity = uint32_t(it / STAGES) & 1u;
+    // gather and interpolate du while the tangent is in flight
+    const int32_t node = lane_ok ? conn[e * NQ + qi] : 0;
+    float din[Shape::cols];
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+      const float U = lane_ok ? du[c * num_nodes + node] : 0.f;
+      float v, g0, g1, g2;
+      interpolate_lane<Q, float>(U, 0, ix, iy, iz, sB, sG, v, g0, g1, g2);
+      if constexpr (VI) din[c] = v;
+      constexpr int off = VI ? C : 0;
+      din[off + 3 * c + 0] = g0;
+      din[off + 3 * c + 1] = g1;
+      din[off + 3 * c + 2] = g2;
+    }
+    const bool ready = __all_sync(0xffffffffu, bulk::mbar_wait(&my_bars[s], parity));
+    if (!ready) {
+      failed = true;
+      break;
+    }
+    const float* Dq = my_ring + s * ES + qi;
+    float dout[Shape::rows];
+#pragma unroll
+    for (int r = 0; r < Shape::rows; r++) {
+      float acc = 0.f;
+#pragma unroll
+      for (int k = 0; k < Shape::cols; k++) acc += Dq[(r * Shape::cols + k) * NQ] * din[k];
+      dout[r] = acc;
+    }
+    __syncwarp();  // every lane has read stage s
+    if (lane == 0) {
+      const int64_t en = e + int64_t(STAGES) * step;
+      if (en < num_elements) {
+        bulk::fence_proxy_async_smem();
+        bulk::mbar_arrive_expect_tx(&my_bars[s], BYTES);
+        bulk::copy_g2s(my_ring + s * ES, D + en * ES, BYTES, &my_bars[s]);
+      }
+    }
+    constexpr int roff = HS ? C : 0;
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+      const float src = HS ? dout[HS ? c : 0] : 0.f;
+      const float r = integrate_lane<Q, HS, true, float>(src, dout[roff + 3 * c], dout[roff + 3 * c + 1],
+                                                         dout[roff + 3 * c + 2], 0, ix, iy, iz, sB, sG);
+      if (lane_ok) out_e[(e * C + c) * NQ + qi] = r;
+    }
+  }
+  if (failed) {
+    if (lane == 0) atomicExch(err, 1);
+    // drain: the copies issued for iterations it .. it + STAGES - 1
+    for (int j = 0; j < STAGES; j++) {
+      const int k = it + j;
+      if (first + int64_t(k) * step < num_elements) (void)bulk::mbar_wait(&my_bars[k % STAGES], uint32_t(k / STAGES) & 1u);
+    }
   }
 }
 
@@ -1074,7 +1335,7 @@ __global__ void __launch_bounds__(128) diag_from_tangent_kernel(const double* __
       for (int b = (VI ? 0 : 1); b < 4; b++) {
         const int row = (a == 0) ? c : (HS ? C : 0) + 3 * c + (a - 1);
         const int col = (b == 0) ? c : (VI ? C : 0) + 3 * c + (b - 1);
-        Real d = valid ? D[(e * Shape::size + int64_t(row) * Shape::cols + col) * NQ + qi] : Real(0);
+        Real d = valid ? D[e * Shape::template stride<NQ> + (int64_t(row) * Shape::cols + col) * NQ + qi] : Real(0);
         // x-pass: T1(ix', qy, qz) = sum_qx d(qx,qy,qz) fa_x(qx,ix') fb_x(qx,ix')
         Real t1 = 0;
 #pragma unroll

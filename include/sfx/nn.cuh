@@ -42,7 +42,8 @@ enum Act : int { ACT_NONE = 0, ACT_RELU = 1 };
 /// for all COUT channels (COUT/8 mma tiles); the K loop runs over the 27 taps
 /// and the input channels in chunks of 16.  x: [node][CIN] bf16, W: [COUT][27][CIN]
 /// bf16, bias: [COUT] f32 (may be null), y: [node][COUT] bf16.  If `y_f32` is
-/// non-null the pre-cast FP32 result is written there instead.
+/// non-null the pre-cast FP32 result is written there instead.  blockIdx.y
+/// selects the sample of a batch (volumes stored one after another).
 template <int CIN, int COUT, int ACT>
 __global__ void __launch_bounds__(128) conv3_fwd(Grid3 g, const __nv_bfloat16* __restrict__ x,
                                                  const __nv_bfloat16* __restrict__ W, const float* __restrict__ bias,
@@ -54,6 +55,9 @@ __global__ void __launch_bounds__(128) conv3_fwd(Grid3 g, const __nv_bfloat16* _
   const int64_t n0 = warp * 16;
   const int64_t N = g.nodes();
   if (n0 >= N) return;
+  x += int64_t(blockIdx.y) * N * CIN;
+  if (y) y += int64_t(blockIdx.y) * N * COUT;
+  if (y_f32) y_f32 += int64_t(blockIdx.y) * N * COUT;
   const int gid = lane >> 2, tig = lane & 3;
   // the two rows (nodes) this lane feeds into the A fragment
   int64_t rn[2] = {n0 + gid, n0 + gid + 8};
@@ -137,8 +141,9 @@ __global__ void flip_weights(const __nv_bfloat16* __restrict__ W, __nv_bfloat16*
 
 /// Weight gradient on the tensor cores:
 ///   dW[co][tap][ci] = sum_n dy[n][co] x[n + off(tap)][ci]
-/// as a GEMM with M = COUT, N = CIN per tap and K = nodes.  The nodes are cut
-/// into chunks of kWgradChunk; block b takes chunks b, b + gridDim.x, ... and
+/// as a GEMM with M = COUT, N = CIN per tap and K = nodes of all samples of
+/// the batch.  Each sample's nodes are cut into chunks of kWgradChunk; block b
+/// takes chunks b, b + gridDim.x, ... of the batch's chunk list and
 /// writes its partial sums to part[b][co][tap][ci] (reduced over blocks in
 /// fixed order by reduce_chunks).  Per chunk the block stages dy^T
 /// ([co][node], BF16) and the tap-shifted x^T ([ci][node], zero outside the
@@ -147,7 +152,7 @@ __global__ void flip_weights(const __nv_bfloat16* __restrict__ W, __nv_bfloat16*
 constexpr int kWgradChunk = 128;
 
 template <int CIN, int COUT>
-__global__ void __launch_bounds__(128) conv3_wgrad_mma(Grid3 g, const __nv_bfloat16* __restrict__ x,
+__global__ void __launch_bounds__(128) conv3_wgrad_mma(Grid3 g, int batch, const __nv_bfloat16* __restrict__ x,
                                                        const __nv_bfloat16* __restrict__ dy, float* __restrict__ part) {
   static_assert(CIN % 16 == 0 && COUT % 16 == 0, "channel counts");
   constexpr int KC = kWgradChunk;
@@ -159,7 +164,8 @@ __global__ void __launch_bounds__(128) conv3_wgrad_mma(Grid3 g, const __nv_bfloa
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int gid = lane >> 2, tig = lane & 3;
   const int64_t N = g.nodes();
-  const int64_t nchunks = (N + KC - 1) / KC;
+  const int64_t per_sample = (N + KC - 1) / KC;
+  const int64_t nchunks = per_sample * batch;
   const bool one_chunk = int64_t(blockIdx.x) + gridDim.x >= nchunks;  // dy^T staged once for all taps
   const __nv_bfloat16 zero = __float2bfloat16(0.f);
 #pragma unroll 1
@@ -172,13 +178,16 @@ __global__ void __launch_bounds__(128) conv3_wgrad_mma(Grid3 g, const __nv_bfloa
       for (int j = 0; j < 4; j++) acc[t][j] = 0.f;
 #pragma unroll 1
     for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
-      const int64_t b0 = c * KC;
+      const int64_t smp = c / per_sample;
+      const int64_t b0 = (c - smp * per_sample) * KC;
+      const __nv_bfloat16* xs = x + smp * N * CIN;
+      const __nv_bfloat16* dys = dy + smp * N * COUT;
       __syncthreads();  // the previous k-steps are done with sA / sB
       if (!one_chunk || tap == 0) {
         for (int i = threadIdx.x; i < KC * COUT; i += blockDim.x) {
           const int k = i / COUT, co = i % COUT;
           const int64_t n = b0 + k;
-          sA[co * LD + k] = n < N ? dy[n * COUT + co] : zero;
+          sA[co * LD + k] = n < N ? dys[n * COUT + co] : zero;
         }
       }
       for (int i = threadIdx.x; i < KC * CIN; i += blockDim.x) {
@@ -189,7 +198,7 @@ __global__ void __launch_bounds__(128) conv3_wgrad_mma(Grid3 g, const __nv_bfloa
           const int xx = int(n % g.nx) + ox, yy = int((n / g.nx) % g.ny) + oy,
                     zz = int(n / (int64_t(g.nx) * g.ny)) + oz;
           if (xx >= 0 && xx < g.nx && yy >= 0 && yy < g.ny && zz >= 0 && zz < g.nz)
-            v = x[((int64_t(zz) * g.ny + yy) * g.nx + xx) * CIN + ci];
+            v = xs[((int64_t(zz) * g.ny + yy) * g.nx + xx) * CIN + ci];
         }
         sB[ci * LD + k] = v;
       }
@@ -278,11 +287,14 @@ __device__ inline float to_f<__nv_bfloat16>(__nv_bfloat16 v) {
 
 /// Prolongation from the (m+1)-grid to the (2m+1)-grid by trilinear
 /// interpolation (per channel), added into fine: fine += scale * P coarse.
+/// blockIdx.y selects the sample.
 template <typename T>
 __global__ void prolong_add(Grid3 fg, Grid3 cg, int C, const T* __restrict__ coarse, float* __restrict__ fine,
                             float scale) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= fg.nodes() * C) return;
+  coarse += int64_t(blockIdx.y) * cg.nodes() * C;
+  fine += int64_t(blockIdx.y) * fg.nodes() * C;
   const int c = int(i % C);
   const int64_t n = i / C;
   const int x = int(n % fg.nx), y = int((n / fg.nx) % fg.ny), z = int(n / (int64_t(fg.nx) * fg.ny));
@@ -299,12 +311,15 @@ __global__ void prolong_add(Grid3 fg, Grid3 cg, int C, const T* __restrict__ coa
   fine[i] += scale * v;
 }
 
-/// Restriction coarse = scale * P^T fine (scale 1/8: full weighting), any input type.
+/// Restriction coarse = scale * P^T fine (scale 1/8: full weighting), any
+/// input type; blockIdx.y selects the sample.
 template <typename T, typename U>
 __global__ void restrict_to(Grid3 fg, Grid3 cg, int C, const T* __restrict__ fine, U* __restrict__ coarse,
                             float scale) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= cg.nodes() * C) return;
+  fine += int64_t(blockIdx.y) * fg.nodes() * C;
+  coarse += int64_t(blockIdx.y) * cg.nodes() * C;
   const int c = int(i % C);
   const int64_t n = i / C;
   const int X = int(n % cg.nx), Y = int((n / cg.nx) % cg.ny), Z = int(n / (int64_t(cg.nx) * cg.ny));

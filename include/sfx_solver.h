@@ -32,13 +32,14 @@ extern "C" {
 #define SFX_PREC_NONE 0
 #define SFX_PREC_JACOBI 1
 #define SFX_PREC_JACOBI_CHEBYSHEV 2
-/* Learned multilevel network (include/sfx_learned.h) combined with FP32
- * Jacobi-Chebyshev on what it leaves of the residual (learned_cycle).  The
- * network's step is scaled to minimise the residual; a step that takes less
- * than 1 % off the residual norm is skipped (counted in
- * sfx_solver_stats.learned_fallbacks), leaving Jacobi-Chebyshev alone.  The
- * outer Krylov method is flexible GMRES; with mixed_precision the step
- * preconditions an inner FP32 flexible GMRES(inner_iterations). */
+/* Learned multilevel network (include/sfx_learned.h) as the first stage of
+ * each outer flexible-GMRES preconditioner application: z = a NN(v) with a
+ * minimising |v - a J NN(v)|, then, on what it leaves of v, the inner FP32
+ * GMRES(inner_iterations) with FP32 Jacobi-Chebyshev (mixed_precision = 1)
+ * or one FP32 Jacobi-Chebyshev application (mixed_precision = 0, see
+ * learned_cycle).  A network step that takes less than 1 % off the residual
+ * norm is skipped (counted in sfx_solver_stats.learned_fallbacks), leaving the
+ * method without the network. */
 #define SFX_PREC_LEARNED 3
 
 typedef struct {
@@ -58,7 +59,8 @@ typedef struct {
   int inner_iterations;      /* 20: FP32 inner GMRES steps per outer step */
   double inner_rel_tol;      /* 1e-3 */
   int print_level;           /* 0 */
-  int learned_cycle;         /* SFX_PREC_LEARNED step: 0 network then Chebyshev; 1 Chebyshev, network, Chebyshev */
+  int learned_cycle;         /* SFX_PREC_LEARNED without mixed precision: 0 network then Chebyshev;
+                                1 Chebyshev, network, Chebyshev */
 } sfx_solver_options;
 
 typedef struct {

@@ -40,12 +40,14 @@ SIGNATURES = {
     "sfx_form_add_domain_integral": (_c.c_int, [_vp, _c.c_int, _dp, _c.c_int]),
     "sfx_form_add_boundary_integral": (_c.c_int, [_vp, _c.c_int, _c.c_int, _dp]),
     "sfx_form_set_shape_displacement": (_c.c_int, [_vp, _vp, _vp]),
+    "sfx_shape_jvp": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp, _vp]),
     "sfx_residual": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp]),
     "sfx_linearize": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp]),
     "sfx_form_set_jvp_mode": (_c.c_int, [_vp, _c.c_int]),
     "sfx_jvp": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "sfx_jvp_f32": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "sfx_jvp_element": (_c.c_int, [_vp, _vp, _vp, _vp]),
+    "sfx_jvp_element_f32": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "sfx_csr_nnz": (_c.c_int, [_vp, _i64p]),
     "sfx_csr_graph": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "sfx_assemble_csr": (_c.c_int, [_vp, _vp, _vp]),

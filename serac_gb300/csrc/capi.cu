@@ -178,7 +178,8 @@ int sfx_form_create(sfx_mesh mesh, int order, int components, sfx_form* out) {
     return fail(code, msg);
   };
   cudaError_t err;
-  if ((err = f->conn.upload(conn.data(), conn.size())) != cudaSuccess ||
+  if ((err = f->wait_error.init()) != cudaSuccess ||
+      (err = f->conn.upload(conn.data(), conn.size())) != cudaSuccess ||
       (err = f->node_ptr.upload(count.data(), count.size())) != cudaSuccess ||
       (err = f->node_ent.upload(ent.data(), ent.size())) != cudaSuccess)
     return cleanup_fail(SFX_ERR_CUDA, std::string("upload tables: ") + cudaGetErrorString(err));
@@ -212,6 +213,23 @@ int sfx_form_set_shape_displacement(sfx_form form, const double* shape, void* st
   form->has_shape = shape != nullptr;
   form->linearized = false;  // the stored tangent belongs to the old geometry
   return sfx_impl::compute_geometry(*form, st);
+}
+
+int sfx_shape_jvp(sfx_form form, double t, const double* u, const double* dshape, double* dr, void* stream) {
+  if (check_form(form)) return SFX_ERR_INVALID;
+  if (!u || !dshape || !dr) return fail(SFX_ERR_INVALID, "null vector");
+  if (!form->boundary.empty())
+    return fail(SFX_ERR_UNSUPPORTED, "the shape derivative covers domain integrals only in this version");
+  auto s = static_cast<cudaStream_t>(stream);
+  if (form->domain.empty()) {
+    SFX_CUDA_TRY(cudaMemsetAsync(dr, 0, sizeof(double) * size_t(form->ndofs), s));
+    return SFX_OK;
+  }
+  for (size_t i = 0; i < form->domain.size(); i++) {
+    if (int rc = sfx_impl::launch_shape_jvp(*form, form->domain[i], u, dshape, form->e64.p, t, s)) return rc;
+    if (int rc2 = scatter_dispatch<double>(*form, form->e64.p, dr, i > 0, s)) return rc2;
+  }
+  return SFX_OK;
 }
 
 int sfx_form_destroy(sfx_form form) {
@@ -324,6 +342,10 @@ int sfx_jvp_f32(sfx_form form, const float* du, float* dr, void* stream) {
   if (check_form(form)) return SFX_ERR_INVALID;
   if (!du || !dr) return fail(SFX_ERR_INVALID, "null vector");
   if (!form->linearized) return fail(SFX_ERR_INVALID, "sfx_linearize must be called before sfx_jvp_f32");
+  if (form->wait_error.raised()) {
+    form->wait_error.clear();
+    return fail(SFX_ERR_TIMEOUT, "a bulk-copy wait of an earlier FP32 Jacobian action expired");
+  }
   auto s = static_cast<cudaStream_t>(stream);
   if (form->domain.empty()) SFX_CUDA_TRY(cudaMemsetAsync(dr, 0, sizeof(float) * size_t(form->ndofs), s));
   for (size_t i = 0; i < form->domain.size(); i++) {
@@ -344,6 +366,20 @@ int sfx_jvp_element(sfx_form form, const double* du, double* dE, void* stream) {
   auto s = static_cast<cudaStream_t>(stream);
   if (form->jvp_mode == SFX_JVP_STORED_TANGENT) return launch_jvp_stored(*form, form->domain[0], du, dE, s);
   return launch_domain(*form, form->domain[0], sfx::kernels::JVP, form->u_lin64.p, du, dE, form->t_lin, s);
+}
+
+int sfx_jvp_element_f32(sfx_form form, const float* du, float* dE, void* stream) {
+  if (check_form(form)) return SFX_ERR_INVALID;
+  if (!du || !dE) return fail(SFX_ERR_INVALID, "null vector");
+  if (!form->linearized) return fail(SFX_ERR_INVALID, "sfx_linearize must be called before sfx_jvp_element_f32");
+  if (form->domain.empty()) return fail(SFX_ERR_INVALID, "no domain integral");
+  if (form->wait_error.raised()) {
+    form->wait_error.clear();
+    return fail(SFX_ERR_TIMEOUT, "a bulk-copy wait of an earlier FP32 Jacobian action expired");
+  }
+  auto s = static_cast<cudaStream_t>(stream);
+  if (form->jvp_mode == SFX_JVP_STORED_TANGENT) return launch_jvp_stored_f32(*form, form->domain[0], du, dE, s);
+  return launch_domain_jvp_f32(*form, form->domain[0], form->u_lin32.p, du, dE, form->t_lin, s);
 }
 
 int sfx_form_get_layout(sfx_form form, sfx_form_layout* out) {

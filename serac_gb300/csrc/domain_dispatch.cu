@@ -2,6 +2,10 @@
 // dispatches on (order, material, mode, precision).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <string>
+#include <type_traits>
+
 #include "dispatch.hpp"
 #include "form.hpp"
 #include "sfx/kernels.cuh"
@@ -159,7 +163,7 @@ struct LinearizeFn {
     using QF = decltype(Maker{}(nullptr));
     constexpr bool HS = kernels::tangent_has_source<C, State, QF>();
     using Shape = kernels::TangentShape<C, HS, Maker::value_input>;
-    const size_t n = size_t(f.ne) * NQ * Shape::size;
+    const size_t n = size_t(f.ne) * size_t(Shape::template stride<NQ>);
     if (di.D64.n != n) {
       cudaError_t err = di.D64.alloc(n);
       if (err == cudaSuccess) err = di.D32.alloc(n);
@@ -194,10 +198,34 @@ struct StoredJvpFn {
     using QF = decltype(Maker{}(nullptr));
     constexpr bool HS = kernels::tangent_has_source<C, State, QF>();
     if (f.ne == 0) return SFX_OK;
-    int64_t warps = (f.ne + EPW - 1) / EPW;
-    int64_t blocks = (warps * 32 + 127) / 128;
-    kernels::jvp_stored_kernel<P, C, HS, Maker::value_input, Real>
-        <<<unsigned(blocks), 128, 0, s>>>(du, D, f.conn.p, E, f.nnodes, f.ne);
+    if constexpr (P == 2 && std::is_same<Real, float>::value) {
+      // bulk-copy staged kernel: one persistent block per SM; warps and ring
+      // depth chosen so the rings fit in 220 KB of shared memory
+      using Shape = kernels::TangentShape<C, HS, Maker::value_input>;
+      constexpr size_t kSmemBudget = 220 * 1024;
+      constexpr size_t stage_bytes = size_t(Shape::template stride<NQ>) * 4 + 8;
+      constexpr int WARPS = 8 * 2 * stage_bytes <= kSmemBudget ? 8 : 4;
+      constexpr int STAGES = int(std::min<size_t>(4, kSmemBudget / (WARPS * stage_bytes)));
+      static_assert(STAGES >= 2, "tangent block too large for a two-stage ring");
+      constexpr size_t smem = size_t(WARPS) * STAGES * stage_bytes;
+      auto kern = kernels::jvp_stored_tma_kernel<C, HS, Maker::value_input, WARPS, STAGES>;
+      static bool configured = false;  // per instantiation
+      if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("bulk jvp attribute: ") + cudaGetErrorString(e));
+        configured = true;
+      }
+      int dev = 0, sms = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      const int64_t blocks = std::min<int64_t>((f.ne + WARPS - 1) / WARPS, std::max(sms, 1));
+      kern<<<unsigned(blocks), WARPS * 32, smem, s>>>(du, D, f.conn.p, E, f.nnodes, f.ne, f.wait_error.dev);
+    } else {
+      int64_t warps = (f.ne + EPW - 1) / EPW;
+      int64_t blocks = (warps * 32 + 127) / 128;
+      kernels::jvp_stored_kernel<P, C, HS, Maker::value_input, Real>
+          <<<unsigned(blocks), 128, 0, s>>>(du, D, f.conn.p, E, f.nnodes, f.ne);
+    }
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("stored jvp launch: ") + cudaGetErrorString(err));
     return SFX_OK;
@@ -227,6 +255,40 @@ struct DiagFn {
 };
 
 }  // namespace
+
+namespace {
+template <int P>
+struct ShapeJvpFn {
+  const sfx_form_s& f;
+  const DomainIntegral& di;
+  const double* u;
+  const double* dshape;
+  double* E;
+  double t;
+  cudaStream_t s;
+  template <int C, typename State, typename Maker>
+  int operator()() {
+    constexpr int NQ = (P + 1) * (P + 1) * (P + 1);
+    constexpr int EPW = 32 / NQ;
+    if (f.ne == 0) return SFX_OK;
+    kernels::DomainArgs<double> a{u, nullptr, E, f.conn.p, nullptr, di.state.p, di.params.p, f.nnodes, f.ne, t};
+    const int64_t warps = (f.ne + EPW - 1) / EPW;
+    const int64_t blocks = (warps * 32 + 127) / 128;
+    kernels::shape_jvp_kernel<P, C, State, Maker><<<unsigned(blocks), 128, 0, s>>>(
+        a, Maker{}, f.Xe.p, f.has_shape ? f.shape.p : nullptr, dshape);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("shape jvp launch: ") + cudaGetErrorString(err));
+    return SFX_OK;
+  }
+};
+}  // namespace
+
+int launch_shape_jvp(const sfx_form_s& f, const DomainIntegral& di, const double* u, const double* dshape, double* E,
+                     double t, cudaStream_t s) {
+  if (f.p == 1) return visit_material(di.material, ShapeJvpFn<1>{f, di, u, dshape, E, t, s});
+  if (f.p == 2) return visit_material(di.material, ShapeJvpFn<2>{f, di, u, dshape, E, t, s});
+  return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
+}
 
 int launch_diag_from_tangent(const sfx_form_s& f, const DomainIntegral& di, double* E, cudaStream_t s) {
   if (f.p == 1) return visit_material(di.material, DiagFn<1>{f, di, E, s});

@@ -93,8 +93,35 @@ struct sfx_mesh_s {
   std::vector<double> vertices;
 };
 
+namespace sfx_impl {
+/// An int in mapped pinned host memory that kernels can set (device pointer)
+/// and the host can read without synchronising: the error flag of the
+/// bounded waits in the bulk-copy kernels.
+struct MappedFlag {
+  int* host = nullptr;
+  int* dev = nullptr;
+  MappedFlag() = default;
+  MappedFlag(const MappedFlag&) = delete;
+  MappedFlag& operator=(const MappedFlag&) = delete;
+  ~MappedFlag() {
+    if (host) cudaFreeHost(host);
+  }
+  cudaError_t init() {
+    cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&host), sizeof(int), cudaHostAllocMapped);
+    if (e != cudaSuccess) return e;
+    *host = 0;
+    return cudaHostGetDevicePointer(reinterpret_cast<void**>(&dev), host, 0);
+  }
+  bool raised() const { return host && *static_cast<volatile int*>(host) != 0; }
+  void clear() {
+    if (host) *static_cast<volatile int*>(host) = 0;
+  }
+};
+}  // namespace sfx_impl
+
 struct sfx_form_s {
   sfx_mesh_s mesh;
+  sfx_impl::MappedFlag wait_error;  // set by a bulk-copy kernel whose bounded wait expired
   int p = 0, c = 0, Q = 0, NQ = 0, NPE = 0;
   int64_t ne = 0, nnodes = 0, ndofs = 0;
   sfx_impl::DeviceBuf<int32_t> conn;      // [e][NPE]

@@ -89,7 +89,7 @@ struct sfx_solver_s {
   sfx_lnet net = nullptr;
   int grid[3] = {0, 0, 0};
   const float* features = nullptr;
-  DeviceBuf<float> nn_z, nn_res, nn_x, Z32, x32b;
+  DeviceBuf<float> nn_z, nn_res, nn_x, x32b;
 };
 
 namespace {
@@ -359,81 +359,81 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
     const int k = o.inner_iterations;
     if (ensure(s->x32, n) || ensure(s->b32, n) || ensure(s->tmp32, n) || ensure(s->diag32, n) ||
         ensure(s->cheb_d32, n) || ensure(s->cheb_r32, n) || ensure(s->tmp32b, n) || ensure(s->nn_z, n) ||
-        ensure(s->nn_res, n) || ensure(s->nn_x, n) ||
-        (o.mixed_precision && (ensure(s->V32, size_t(k + 1) * n) || ensure(s->Z32, size_t(k) * n) ||
-                               ensure(s->y32, size_t(k + 1)) || ensure(s->x32b, n))))
+        ensure(s->nn_res, n) || ensure(s->nn_x, n) || ensure(s->x32b, n) ||
+        (o.mixed_precision && (ensure(s->V32, size_t(k + 1) * n) || ensure(s->y32, size_t(k + 1)))))
       return fail(SFX_ERR_NOMEM, "FP32 workspace allocation failed");
     sfx_blas::convert<double, float><<<nblocks(n), 256, 0, st>>>(n, s->diag.p, s->diag32.p);
     if (int rc = estimate_lmax<float, float>(s, apply_J32, s->diag32.p, s->tmp32.p, s->cheb_r32.p, s->red32,
                                              &s->lmax32, st))
       return rc;
-    // FP32 two-stage preconditioner z ~ J^-1 b.  Cycle 0: network, then
-    // Chebyshev on what it leaves.  Cycle 1: Chebyshev, network on the
-    // remaining residual, Chebyshev again.  The network's step, scaled to
-    // minimise the residual, is kept only when it takes at least 1 % off the
-    // residual norm; otherwise it is skipped (a fallback).
-    std::function<int(const float*, float*)> learned = [=](const float* b, float* z) -> int {
+    // Network step on the residual res: z += a NN(res) with a minimising
+    // |res - a J NN(res)|, kept only when it takes at least 1 % off the
+    // residual norm (otherwise skipped: a fallback).  Returns what is left
+    // of the residual (nn_res, or res itself after a fallback).
+    auto nn_step = [=](const float* res, float* z, const float** left) -> int {
       cudaError_t err;
-      // res = b - J z for the current z (z = 0: res = b)
-      const float* res = b;
-      if (o.learned_cycle == 1) {
-        if (int rc = chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, b, z, s->cheb_d32.p,
-                                             s->cheb_r32.p, st))
-          return rc;
-        if (int rc = apply_J32(s, z, s->nn_res.p, st)) return rc;
-        sfx_blas::rsub<float><<<nblocks(n), 256, 0, st>>>(n, b, s->nn_res.p);
-        res = s->nn_res.p;
-      } else {
-        SFX_CUDA_TRY(cudaMemsetAsync(z, 0, sizeof(float) * n, st));
-      }
+      *left = res;
       const double nv = double(s->red32.dot(res, res, n, st, &err));
       SFX_CUDA_TRY(err);
       if (int rc = lnet_apply(s->net, s->grid[0], s->grid[1], s->grid[2], res, s->features, s->nn_z.p, st)) return rc;
       s->stats.learned_applications++;
-      // trial z' = z + a z_nn with a minimising |res - a J z_nn|; accepted
-      // when it takes at least 1 % off the residual norm
-      if (int rc = apply_J32(s, s->nn_z.p, s->tmp32.p, st)) return rc;
-      const double rj = double(s->red32.dot(res, s->tmp32.p, n, st, &err));
+      if (int rc = apply_J32(s, s->nn_z.p, s->nn_x.p, st)) return rc;
+      const double rj = double(s->red32.dot(res, s->nn_x.p, n, st, &err));
       SFX_CUDA_TRY(err);
-      const double jj = double(s->red32.dot(s->tmp32.p, s->tmp32.p, n, st, &err));
+      const double jj = double(s->red32.dot(s->nn_x.p, s->nn_x.p, n, st, &err));
       SFX_CUDA_TRY(err);
       const double a = jj > 0.0 ? rj / jj : 0.0;
-      const double nr = nv - a * rj;  // |res - a J z_nn|^2
-      const float* res2 = res;
+      const double nr = nv - a * rj;  // |res - a J NN(res)|^2
       if (std::isfinite(a) && std::isfinite(jj) && jj > 0.0 && nr <= 0.9801 * nv) {
         sfx_blas::axpby<float><<<nblocks(n), 256, 0, st>>>(n, float(a), s->nn_z.p, 1.0f, z);
-        sfx_blas::axpby<float><<<nblocks(n), 256, 0, st>>>(n, 1.0f, res, float(-a), s->tmp32.p);
-        res2 = s->tmp32.p;
+        SFX_CUDA_TRY(cudaMemcpyAsync(s->nn_res.p, res, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+        sfx_blas::axpby<float><<<nblocks(n), 256, 0, st>>>(n, float(-a), s->nn_x.p, 1.0f, s->nn_res.p);
+        *left = s->nn_res.p;
       } else {
         s->stats.learned_fallbacks++;
       }
-      // z += Chebyshev(res2)
-      if (int rc = chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, res2, s->nn_x.p, s->cheb_d32.p,
-                                           s->cheb_r32.p, st))
-        return rc;
-      sfx_blas::axpby<float><<<nblocks(n), 256, 0, st>>>(n, 1.0f, s->nn_x.p, 1.0f, z);
       return SFX_OK;
     };
+    auto cheb32 = [=](const float* b, float* z) -> int {
+      return chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, b, z, s->cheb_d32.p, s->cheb_r32.p, st);
+    };
     if (o.mixed_precision) {
-      // inner FP32 flexible GMRES(k) preconditioned by the two-stage step
+      // network step, then inner FP32 GMRES(k) + Jacobi-Chebyshev on what it leaves
       prec = [=](const double* v, double* z) -> int {
         sfx_blas::convert<double, float><<<nblocks(n), 256, 0, st>>>(n, v, s->b32.p);
         SFX_CUDA_TRY(cudaMemsetAsync(s->x32b.p, 0, sizeof(float) * n, st));
+        const float* left = nullptr;
+        if (int rc = nn_step(s->b32.p, s->x32b.p, &left)) return rc;
+        SFX_CUDA_TRY(cudaMemsetAsync(s->x32.p, 0, sizeof(float) * n, st));
+        std::function<int(const float*, float*)> inner_prec = cheb32;
         int it = 0;
         double rel_in = 0.0;
-        if (int rc = gmres<float, float>(s, apply_J32, learned, true, s->b32.p, s->x32b.p, s->V32.p, s->Z32.p,
-                                         s->cheb_r32.p, s->y32.p, s->red32, k, k, o.inner_rel_tol, 0.0, &it, &rel_in,
-                                         st))
+        if (int rc = gmres<float, float>(s, apply_J32, inner_prec, false, left, s->x32.p, s->V32.p, nullptr,
+                                         s->tmp32.p, s->y32.p, s->red32, k, k, o.inner_rel_tol, 0.0, &it, &rel_in, st))
           return rc;
         s->stats.inner_iterations += it;
+        sfx_blas::axpby<float><<<nblocks(n), 256, 0, st>>>(n, 1.0f, s->x32.p, 1.0f, s->x32b.p);
         sfx_blas::convert<float, double><<<nblocks(n), 256, 0, st>>>(n, s->x32b.p, z);
         return SFX_OK;
       };
     } else {
+      // cycle 0: network, Chebyshev; cycle 1: Chebyshev, network, Chebyshev
       prec = [=](const double* v, double* z) -> int {
         sfx_blas::convert<double, float><<<nblocks(n), 256, 0, st>>>(n, v, s->b32.p);
-        if (int rc = learned(s->b32.p, s->x32.p)) return rc;
-        sfx_blas::convert<float, double><<<nblocks(n), 256, 0, st>>>(n, s->x32.p, z);
+        const float* res = s->b32.p;
+        if (o.learned_cycle == 1) {
+          if (int rc = cheb32(s->b32.p, s->x32b.p)) return rc;
+          if (int rc = apply_J32(s, s->x32b.p, s->tmp32.p, st)) return rc;
+          sfx_blas::rsub<float><<<nblocks(n), 256, 0, st>>>(n, s->b32.p, s->tmp32.p);
+          res = s->tmp32.p;
+        } else {
+          SFX_CUDA_TRY(cudaMemsetAsync(s->x32b.p, 0, sizeof(float) * n, st));
+        }
+        const float* left = nullptr;
+        if (int rc = nn_step(res, s->x32b.p, &left)) return rc;
+        if (int rc = cheb32(left, s->x32.p)) return rc;
+        sfx_blas::axpby<float><<<nblocks(n), 256, 0, st>>>(n, 1.0f, s->x32.p, 1.0f, s->x32b.p);
+        sfx_blas::convert<float, double><<<nblocks(n), 256, 0, st>>>(n, s->x32b.p, z);
         return SFX_OK;
       };
     }

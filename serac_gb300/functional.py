@@ -158,10 +158,16 @@ class Gradient:
     Mult = mult
 
     def element_action(self, du, out=None, stream=None):
-        """Element-level action [e][component][node] before the scatter-add."""
+        """Element-level action [e][component][node] before the scatter-add
+        (FP64, or FP32 for a float32 du)."""
         f = self.form
-        _require(du, torch.float64, f.ndofs, "du")
         n = f.mesh.num_elements * f.space.components * (f.space.order + 1) ** 3
+        if du.dtype == torch.float32:
+            _require(du, torch.float32, f.ndofs, "du")
+            out = torch.empty(n, dtype=torch.float32, device=du.device) if out is None else out
+            _lib.call("sfx_jvp_element_f32", f._h, _dptr(du), _dptr(out), _stream(stream))
+            return out
+        _require(du, torch.float64, f.ndofs, "du")
         out = torch.empty(n, dtype=torch.float64, device=du.device) if out is None else out
         _lib.call("sfx_jvp_element", f._h, _dptr(du), _dptr(out), _stream(stream))
         return out
@@ -299,6 +305,28 @@ class Functional:
         return out
 
 
+class ShapeGradient:
+    """dR/dp at (t, shape, u): the derivative of the shape-aware residual with
+    respect to the shape displacement, as an operator on shape directions."""
+
+    def __init__(self, functional, t, u):
+        self.functional = functional
+        self.t = t
+        self.u = u.clone()
+
+    def mult(self, dshape, out=None, stream=None):
+        f = self.functional
+        _require(dshape, torch.float64, 3 * f.num_nodes, "dshape")
+        out = torch.empty(f.ndofs, dtype=torch.float64, device=dshape.device) if out is None else out
+        _lib.call("sfx_shape_jvp", f._h, float(self.t), _dptr(self.u), _dptr(dshape), _dptr(out), _stream(stream))
+        return out
+
+    Mult = mult
+
+    def __call__(self, dshape):
+        return self.mult(dshape)
+
+
 class ShapeAwareFunctional:
     """ShapeAwareFunctional<H1<p,3>, H1<p,c>(H1<p,c>)> (shape_aware_functional.hpp:330-560):
     the shape displacement is the first argument after time and is held
@@ -308,6 +336,7 @@ class ShapeAwareFunctional:
         saf.AddDomainIntegral(NEOHOOKEAN, [K, G])
         r = saf(t, shape, u)
         r, dRdu = saf(t, shape, differentiate_wrt(u))
+        r, dRdp = saf(t, differentiate_wrt(shape), u)     # dRdp(dshape)
     """
 
     def __init__(self, mesh: Mesh, shape_space: H1, space: H1):
@@ -333,6 +362,10 @@ class ShapeAwareFunctional:
             self._shape_key = key
 
     def __call__(self, t, shape, arg, out=None):
+        if isinstance(shape, differentiate_wrt):
+            self._use(shape.u)
+            r = self.functional(t, arg, out)
+            return r, ShapeGradient(self.functional, t, arg)
         self._use(shape)
         return self.functional(t, arg, out)
 

@@ -81,9 +81,10 @@ def gaussian_random_field(n, ell, seed):
     return g  # [z][y][x]
 
 
-def node_features(n, order, elem_log_modulus, ess_nodes):
+def node_features(n, order, elem_log_modulus, clamped_nodes, partial_nodes=()):
     """[2][num_nodes] float32: per-node mean of the incident elements' log
-    modulus feature, and a 0/1 Dirichlet mask."""
+    modulus feature, and a constraint channel: 1 on fully clamped nodes (the
+    network's output is zero there), 0.25 on partially constrained ones."""
     N1 = order * n + 1
     acc = np.zeros((N1, N1, N1))
     cnt = np.zeros((N1, N1, N1))
@@ -95,7 +96,8 @@ def node_features(n, order, elem_log_modulus, ess_nodes):
                 cnt[dz:dz + order * n:order, dy:dy + order * n:order, dx:dx + order * n:order] += 1
     feat = np.zeros(2 * N1 ** 3, dtype=np.float32)
     feat[:N1 ** 3] = (acc / cnt).ravel()
-    feat[N1 ** 3 + np.asarray(ess_nodes, dtype=np.int64)] = 1.0
+    feat[N1 ** 3 + np.asarray(partial_nodes, dtype=np.int64)] = 0.25
+    feat[N1 ** 3 + np.asarray(clamped_nodes, dtype=np.int64)] = 1.0
     return feat
 
 
@@ -156,8 +158,7 @@ class SolidSetup:
         self.top = top
         self.N = N
         self.grid = (order * n + 1,) * 3
-        ess_nodes = np.unique(np.concatenate([bottom, top]))
-        self.features = torch.tensor(node_features(n, order, prob.log_modulus, ess_nodes), device="cuda")
+        self.features = torch.tensor(node_features(n, order, prob.log_modulus, bottom, top), device="cuda")
         self.prob = prob
 
     def load(self, u, step):
@@ -195,12 +196,45 @@ def solve_load_steps(setup, solver, u=None):
     return u, tot
 
 
-def harvest(problems, order=2, options=None, max_pairs_per_problem=64, stateful=True):
-    """Run the plain FP64 Newton-Krylov solve (Jacobi-Chebyshev GMRES) of each
-    problem over its load steps and collect every Newton step's (residual,
-    correction) pair, plus the node features.  Returns float32 CUDA tensors
+def smooth_fields(grid, count, rng, ell_range=(0.05, 0.5)):
+    """count random 3-component displacement fields on the node grid: unit
+    Gaussian random fields with a correlation length drawn from ell_range,
+    byNODES float64 [count, 3 * nodes]."""
+    nx = grid[0]
+    out = np.empty((count, 3 * nx ** 3))
+    for i in range(count):
+        ell = rng.uniform(*ell_range)
+        for c in range(3):
+            out[i, c * nx ** 3:(c + 1) * nx ** 3] = gaussian_random_field(nx, ell, int(rng.integers(2 ** 62))).ravel()
+    return out
+
+
+def probe_pairs(setup, u, count, rng):
+    """Exact (residual, correction) pairs at the linearisation u: x a smooth
+    random field with x = 0 on the essential vdofs, r = J(u) x with r = 0
+    there.  Returns float32 CUDA tensors R, X [count, 3N]."""
+    setup.f.linearize(0.0, u)
+    ess = torch.as_tensor(setup.ess, device="cuda")
+    X = torch.tensor(smooth_fields(setup.grid, count, rng), device="cuda")
+    X[:, ess] = 0
+    R = torch.empty_like(X)
+    for i in range(count):
+        setup.f.gradient.mult(X[i].contiguous(), out=R[i])
+    R[:, ess] = 0
+    return R.float(), X.float()
+
+
+def harvest(problems, order=2, options=None, probes_per_step=8, newton_pairs=True, max_newton_pairs=64, seed=0):
+    """Training pairs from the solver on each problem's load steps (warm
+    start, Newton with the FP32-inner mixed-precision solve, state commit):
+    every Newton step's (residual, correction) pair, and probes_per_step
+    probe pairs at each converged step.  Returns float32 CUDA tensors
     R, T [pairs, 3N] and F [pairs, 2N]."""
-    opts = options or SolverOptions.defaults(precond=JACOBI_CHEBYSHEV, krylov_rel_tol=1e-6, max_krylov_iterations=600)
+    from .solver import SolverOptions as _SO
+
+    opts = options or _SO.defaults(precond=JACOBI_CHEBYSHEV, mixed_precision=1, krylov_rel_tol=1e-6,
+                                   max_krylov_iterations=1000)
+    rng = np.random.default_rng(seed)
     Rs, Ts, Fs = [], [], []
     for prob in problems:
         S = SolidSetup(prob, order)
@@ -214,12 +248,12 @@ def harvest(problems, order=2, options=None, max_pairs_per_problem=64, stateful=
             r = S.f.residual(0.0, u)
             r[ess] = 0
             r0 = float(torch.linalg.norm(r))
-            for _ in range(8):
+            for _ in range(10):
                 rn = float(torch.linalg.norm(r))
                 if rn <= 1e-8 * r0 or rn <= 1e-14:
                     break
                 du = solver.solve_linear(0.0, u, r)
-                if count < max_pairs_per_problem:
+                if newton_pairs and count < max_newton_pairs:
                     Rs.append(r.float().clone())
                     Ts.append(du.float().clone())
                     Fs.append(S.features)
@@ -227,23 +261,33 @@ def harvest(problems, order=2, options=None, max_pairs_per_problem=64, stateful=
                 u -= du
                 r = S.f.residual(0.0, u)
                 r[ess] = 0
-            if stateful:
-                S.commit(u)
+            if probes_per_step:
+                R, X = probe_pairs(S, u, probes_per_step, rng)
+                Rs.extend(R)
+                Ts.extend(X)
+                Fs.extend([S.features] * probes_per_step)
+            S.commit(u)
     return torch.stack(Rs), torch.stack(Ts), torch.stack(Fs)
 
 
-def train(net, grid, R, T, F, epochs=20, batch=4, lr=1e-3, seed=0, log=None):
-    """Adam over shuffled mini-batches of harvested pairs; returns the loss history."""
+def train(net, grid, R, T, F, epochs=20, batch=4, lr=1e-3, lr_min=None, seed=0, log=None):
+    """Adam over shuffled mini-batches of the pairs, learning rate decaying
+    from lr to lr_min (default lr / 20) on a cosine; returns the mean loss
+    of every epoch."""
     rng = np.random.default_rng(seed)
     n = R.shape[0]
-    hist = []
+    lr_min = lr / 20 if lr_min is None else lr_min
+    steps = max(1, epochs * (n // batch))
+    hist, k = [], 0
     for ep in range(epochs):
         order = rng.permutation(n)
         tot = 0.0
         for i in range(0, n - batch + 1, batch):
             idx = torch.as_tensor(order[i:i + batch], device=R.device)
             Rb, Tb, Fb = R[idx].contiguous(), T[idx].contiguous(), F[idx].contiguous()
-            tot += net.train_step(grid, Rb, Tb, Fb, batch, lr)
+            lr_k = lr_min + 0.5 * (lr - lr_min) * (1.0 + np.cos(np.pi * k / steps))
+            tot += net.train_step(grid, Rb, Tb, Fb, batch, lr_k)
+            k += 1
         hist.append(tot / max(1, n // batch))
         if log:
             log(ep, hist[-1])

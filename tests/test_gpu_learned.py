@@ -96,6 +96,30 @@ def test_gradient_matches_oracle(cuda):
     L.load().sfx_lnet_destroy(h)
 
 
+def test_batched_step_matches_single_samples(cuda):
+    """A training step on a batch of 3 (lr = 0) reports the mean of the three
+    single-sample losses: every sample is scaled and normalised on its own."""
+    L = _lib()
+    h, p = _net(seed=13)
+    shape = (9, 17, 9)
+    nz, ny, nx = shape
+    samples = [_sample(shape, 40 + i) for i in range(3)]
+    singles = []
+    for r, t, feat in samples:
+        dev = [torch.tensor(a, dtype=torch.float32, device=cuda) for a in (r, t, feat)]
+        loss = ctypes.c_float()
+        g = np.zeros_like(p)
+        L.call("sfx_lnet_gradient", h, nx, ny, nz, *[ctypes.c_void_p(d.data_ptr()) for d in dev], ctypes.byref(loss),
+               g.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), None)
+        singles.append(loss.value)
+    R, T, F = (torch.tensor(np.concatenate([s[k] for s in samples]), dtype=torch.float32, device=cuda) for k in range(3))
+    lv = ctypes.c_float()
+    L.call("sfx_lnet_train_step", h, nx, ny, nz, 3, ctypes.c_void_p(R.data_ptr()), ctypes.c_void_p(T.data_ptr()),
+           ctypes.c_void_p(F.data_ptr()), ctypes.c_float(0.0), ctypes.byref(lv), None)
+    assert abs(lv.value - np.mean(singles)) <= 1e-5 * np.mean(singles)
+    L.load().sfx_lnet_destroy(h)
+
+
 def test_training_reduces_loss(cuda):
     L = _lib()
     h, _ = _net(seed=3)
