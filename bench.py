@@ -409,6 +409,10 @@ def newton_leg(steps):
         net = LP.LearnedPreconditioner()
         net.load(WEIGHTS)
         variants.append(("learned_mixed", sg.SolverOptions.defaults(precond=sg.LEARNED, mixed_precision=1, **base)))
+        # the network as the coarse stage of a two-level step (Chebyshev, network,
+        # Chebyshev) inside flexible GMRES, without the inner FP32 GMRES
+        variants.append(("learned_fgmres", sg.SolverOptions.defaults(precond=sg.LEARNED, mixed_precision=0,
+                                                                      learned_cycle=1, **base)))
     out = {"metric": "Newton time-to-1e-8 relative residual", "unit": "s", "higher_is_better": False,
            "workload": f"j2_q2_vector_{NEWTON_N}cubed_lognormal_E (seed {NEWTON_SEED}), load steps 1-{steps} of "
                        f"{prob.steps}, strain {prob.strain}",
@@ -440,11 +444,14 @@ def newton_leg(steps):
         tot["rel_diff_vs_plain"] = float(torch.linalg.norm(u - ref) / torch.linalg.norm(ref))
         out[name] = tot
         del solver, S
-    for name in ("mixed", "learned_mixed"):
+    for name in ("mixed", "learned_mixed", "learned_fgmres"):
         if name in out:
             out[f"speedup_{name}_vs_plain"] = out["plain_fp64"]["seconds"] / out[name]["seconds"]
     if net is None:
         out["learned_mixed"] = {"unavailable": f"no trained weights at {os.path.relpath(WEIGHTS, ROOT)}"}
+    else:
+        out["weights"] = {"file": os.path.relpath(WEIGHTS, ROOT), "trained_on": "J2 16^3 Q2, seeds 1000-1031 "
+                          "(python -m serac_gb300.train_lnet), applied here on the 32^3 node grid"}
     return out
 
 

@@ -1225,19 +1225,34 @@ __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float*
   const bool lane_ok = lane < NQ;
   const int qi = lane_ok ? lane : NQ - 1;
   const int ix = qi % Q, iy = (qi / Q) % Q, iz = qi / (Q * Q);
+  // gather pipeline: du of the current element and the node id of the next
+  // one are already in registers; each iteration issues the next element's du
+  // and the node id two elements ahead before computing
+  int32_t node_next = 0;
+  float du_cur[C];
+  {
+    const int32_t node0 = (lane_ok && first < num_elements) ? conn[first * NQ + qi] : 0;
+#pragma unroll
+    for (int c = 0; c < C; c++) du_cur[c] = (lane_ok && first < num_elements) ? du[c * num_nodes + node0] : 0.f;
+    const int64_t e1 = first + step;
+    node_next = (lane_ok && e1 < num_elements) ? conn[e1 * NQ + qi] : 0;
+  }
   int it = 0;
   bool failed = false;
   for (int64_t e = first; e < num_elements; e += step, it++) {
     const int s = it % STAGES;
     const uint32_t parity = uint32_t(it / STAGES) & 1u;
-    // gather and interpolate du while the tangent is in flight
-    const int32_t node = lane_ok ? conn[e * NQ + qi] : 0;
+    const int64_t e1 = e + step, e2 = e + 2 * step;
+    float du_next[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) du_next[c] = (lane_ok && e1 < num_elements) ? du[c * num_nodes + node_next] : 0.f;
+    const int32_t node_after = (lane_ok && e2 < num_elements) ? conn[e2 * NQ + qi] : 0;
+    // interpolate du while the tangent is in flight
     float din[Shape::cols];
 #pragma unroll
     for (int c = 0; c < C; c++) {
-      const float U = lane_ok ? du[c * num_nodes + node] : 0.f;
       float v, g0, g1, g2;
-      interpolate_lane<Q, float>(U, 0, ix, iy, iz, sB, sG, v, g0, g1, g2);
+      interpolate_lane<Q, float>(du_cur[c], 0, ix, iy, iz, sB, sG, v, g0, g1, g2);
       if constexpr (VI) din[c] = v;
       constexpr int off = VI ? C : 0;
       din[off + 3 * c + 0] = g0;
@@ -1275,6 +1290,10 @@ __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float*
                                                          dout[roff + 3 * c + 2], 0, ix, iy, iz, sB, sG);
       if (lane_ok) out_e[(e * C + c) * NQ + qi] = r;
     }
+    // rotate the gather pipeline (its loads had this element's work to land)
+#pragma unroll
+    for (int c = 0; c < C; c++) du_cur[c] = du_next[c];
+    node_next = node_after;
   }
   if (failed) {
     if (lane == 0) atomicExch(err, 1);

@@ -59,8 +59,8 @@ typedef struct {
   int inner_iterations;      /* 20: FP32 inner GMRES steps per outer step */
   double inner_rel_tol;      /* 1e-3 */
   int print_level;           /* 0 */
-  int learned_cycle;         /* SFX_PREC_LEARNED without mixed precision: 0 network then Chebyshev;
-                                1 Chebyshev, network, Chebyshev */
+  int learned_cycle;         /* 1: SFX_PREC_LEARNED without mixed precision: 1 Chebyshev, network on
+                                the smoothed residual, Chebyshev (two-level cycle); 0 network, Chebyshev */
 } sfx_solver_options;
 
 typedef struct {

@@ -503,7 +503,7 @@ int sfx_solver_default_options(sfx_solver_options* o) {
   o->inner_iterations = 20;
   o->inner_rel_tol = 1e-3;
   o->print_level = 0;
-  o->learned_cycle = 0;
+  o->learned_cycle = 1;
   return SFX_OK;
 }
 

@@ -270,14 +270,16 @@ def harvest(problems, order=2, options=None, probes_per_step=8, newton_pairs=Tru
     return torch.stack(Rs), torch.stack(Ts), torch.stack(Fs)
 
 
-def train(net, grid, R, T, F, epochs=20, batch=4, lr=1e-3, lr_min=None, seed=0, log=None):
-    """Adam over shuffled mini-batches of the pairs, learning rate decaying
-    from lr to lr_min (default lr / 20) on a cosine; returns the mean loss
-    of every epoch."""
+def train(net, grid, R, T, F, epochs=20, batch=8, lr=1e-3, lr_min=None, warmup=0.05, seed=0, log=None):
+    """Adam over shuffled mini-batches of the pairs; the learning rate rises
+    linearly over the first `warmup` fraction of the steps, then decays from lr
+    to lr_min (default lr / 20) on a cosine.  Returns the mean loss of every
+    epoch."""
     rng = np.random.default_rng(seed)
     n = R.shape[0]
     lr_min = lr / 20 if lr_min is None else lr_min
     steps = max(1, epochs * (n // batch))
+    n_warm = max(1, int(warmup * steps))
     hist, k = [], 0
     for ep in range(epochs):
         order = rng.permutation(n)
@@ -285,7 +287,10 @@ def train(net, grid, R, T, F, epochs=20, batch=4, lr=1e-3, lr_min=None, seed=0, 
         for i in range(0, n - batch + 1, batch):
             idx = torch.as_tensor(order[i:i + batch], device=R.device)
             Rb, Tb, Fb = R[idx].contiguous(), T[idx].contiguous(), F[idx].contiguous()
-            lr_k = lr_min + 0.5 * (lr - lr_min) * (1.0 + np.cos(np.pi * k / steps))
+            if k < n_warm:
+                lr_k = lr * (k + 1) / n_warm
+            else:
+                lr_k = lr_min + 0.5 * (lr - lr_min) * (1.0 + np.cos(np.pi * (k - n_warm) / max(1, steps - n_warm)))
             tot += net.train_step(grid, Rb, Tb, Fb, batch, lr_k)
             k += 1
         hist.append(tot / max(1, n // batch))

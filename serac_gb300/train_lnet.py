@@ -26,7 +26,7 @@ def main(argv=None):
     ap.add_argument("--probes", type=int, default=8, help="probe pairs per converged load step")
     ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--batch", type=int, default=8)
-    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--init-seed", type=int, default=0)
     ap.add_argument("--out", required=True)
     args = ap.parse_args(argv)

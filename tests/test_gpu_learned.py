@@ -178,3 +178,33 @@ def test_corrupted_weights_fall_back_and_keep_the_answer(cuda, mixed):
     assert st["learned_fallbacks"] >= 0.9 * st["learned_applications"]
     err = float(torch.linalg.norm(u - u_ref) / torch.linalg.norm(u_ref))
     assert err <= 1e-9, err
+
+
+def test_trained_network_gain(cuda):
+    """What the trained network gains over the method without it.  The network
+    is trained on the GPU by the library's own kernels (pairs harvested from
+    the solver on 12 seeded J2 problems at 8^3 Q2 hexes, 40 epochs), then used
+    on two held-out seeds inside flexible GMRES as the two-level step
+    Chebyshev -> network -> Chebyshev.  Against flexible GMRES with
+    Jacobi-Chebyshev alone it must cut the Krylov iterations by at least a
+    quarter, and both solves must reach the same answer (1e-9)."""
+    import serac_gb300 as sg
+    from serac_gb300 import learned as LP
+
+    n = 8
+    R, T, F = LP.harvest([LP.j2_problem(n, 1000 + i, steps=2) for i in range(12)], probes_per_step=8)
+    net = LP.LearnedPreconditioner(seed=0)
+    hist = LP.train(net, (2 * n + 1,) * 3, R, T, F, epochs=40, batch=8, lr=1e-3)
+    assert hist[-1] < 0.97 * hist[0]
+    base = dict(_TIGHT, krylov=sg.FGMRES)
+    plain_its = learned_its = 0
+    for seed in (2000, 2001):
+        prob = LP.j2_problem(n, seed, steps=2)
+        u0, st0 = _solve_steps(prob, sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, **base))
+        u1, st1 = _solve_steps(prob, sg.SolverOptions.defaults(precond=sg.LEARNED, learned_cycle=1, **base), net)
+        assert float(torch.linalg.norm(u1 - u0) / torch.linalg.norm(u0)) <= 1e-9
+        assert st1["learned_applications"] > 0
+        plain_its += st0["krylov_iterations"] + st0["predictor_krylov_iterations"]
+        learned_its += st1["krylov_iterations"] + st1["predictor_krylov_iterations"]
+    print(f"Krylov iterations: Jacobi-Chebyshev {plain_its}, learned two-level {learned_its}")
+    assert learned_its <= 0.75 * plain_its
