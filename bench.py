@@ -265,6 +265,9 @@ def run_sfx(args, rank, world):
 
     # ---- FP32 Jv (inner Krylov operator)
     t_fp32 = timed(lambda: grad.mult(du32, dr32), args.steps)
+    # ---- FP64 residual (q-function evaluated at every point, no derivative)
+    r_buf = torch.empty_like(du)
+    t_res = timed(lambda: f.residual(0.0, u, r_buf), args.steps)
     # ---- dominant kernels alone (element kernels, no scatter)
     dE = torch.empty(mesh.num_elements * 81, dtype=torch.float64, device=dev)
     t_elem = timed(lambda: grad.element_action(du, dE), args.steps)
@@ -366,6 +369,9 @@ def run_sfx(args, rank, world):
         "compute_roofline": compute,
         "jv_fp32": {"value": ndofs * args.steps / sum(t_fp32) / 1e9, "unit": UNIT, "dtype": "f32",
                     "ms_per_step": statistics.mean(t_fp32) * 1e3, "roofline": roofline32},
+        "residual": {"value": ndofs * args.steps / sum(t_res) / 1e9, "unit": UNIT, "dtype": "f64",
+                     "ms_per_step": statistics.mean(t_res) * 1e3,
+                     "note": "R(u): fused element kernel (Neo-Hookean q-function, FP64) + node-owner scatter"},
         "jv_recompute": {"value_f64": ndofs * args.steps / sum(t_recompute) / 1e9,
                          "value_f32": ndofs * args.steps / sum(t_recompute32) / 1e9, "unit": UNIT,
                          "note": "q-function re-evaluated on dual numbers in every action; no stored tangent"},
@@ -409,10 +415,6 @@ def newton_leg(steps):
         net = LP.LearnedPreconditioner()
         net.load(WEIGHTS)
         variants.append(("learned_mixed", sg.SolverOptions.defaults(precond=sg.LEARNED, mixed_precision=1, **base)))
-        # the network as the coarse stage of a two-level step (Chebyshev, network,
-        # Chebyshev) inside flexible GMRES, without the inner FP32 GMRES
-        variants.append(("learned_fgmres", sg.SolverOptions.defaults(precond=sg.LEARNED, mixed_precision=0,
-                                                                      learned_cycle=1, **base)))
     out = {"metric": "Newton time-to-1e-8 relative residual", "unit": "s", "higher_is_better": False,
            "workload": f"j2_q2_vector_{NEWTON_N}cubed_lognormal_E (seed {NEWTON_SEED}), load steps 1-{steps} of "
                        f"{prob.steps}, strain {prob.strain}",
@@ -444,7 +446,7 @@ def newton_leg(steps):
         tot["rel_diff_vs_plain"] = float(torch.linalg.norm(u - ref) / torch.linalg.norm(ref))
         out[name] = tot
         del solver, S
-    for name in ("mixed", "learned_mixed", "learned_fgmres"):
+    for name in ("mixed", "learned_mixed"):
         if name in out:
             out[f"speedup_{name}_vs_plain"] = out["plain_fp64"]["seconds"] / out[name]["seconds"]
     if net is None:
@@ -452,6 +454,120 @@ def newton_leg(steps):
     else:
         out["weights"] = {"file": os.path.relpath(WEIGHTS, ROOT), "trained_on": "J2 16^3 Q2, seeds 1000-1031 "
                           "(python -m serac_gb300.train_lnet), applied here on the 32^3 node grid"}
+    return out
+
+
+def _solve_step(S, opts, net=None, step=1):
+    """Warm start + Newton for one load step from rest; returns (u, stats, seconds)."""
+    import torch
+
+    import serac_gb300 as sg
+
+    solver = sg.NewtonSolver(S.f, opts)
+    solver.set_essential(S.ess)
+    if net is not None:
+        solver.set_learned(net, S.grid, S.features)
+    u = torch.zeros(S.f.ndofs, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pre = S.predictor(solver, u, step)
+    st = solver.solve(0.0, u, raise_on_failure=False)
+    torch.cuda.synchronize()
+    st = dict(st)
+    st["predictor_krylov_iterations"] = pre["krylov_iterations"]
+    st["seconds"] = time.perf_counter() - t0
+    return u, st, solver
+
+
+def _jv_rates(f, u, steps=10):
+    """FP64 and FP32 Jacobian-action GDOF/s at the linearisation u (CUDA events)."""
+    import torch
+
+    grad = f.linearize(0.0, u)
+    du = torch.randn(f.ndofs, dtype=torch.float64, device="cuda")
+    dr = torch.empty_like(du)
+    du32, dr32 = du.float(), torch.empty(f.ndofs, dtype=torch.float32, device="cuda")
+    out = {}
+    for name, a, b in (("jv_f64", du, dr), ("jv_f32", du32, dr32)):
+        for _ in range(3):
+            grad.mult(a, b)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        for _ in range(steps):
+            grad.mult(a, b)
+        e.record()
+        torch.cuda.synchronize()
+        out[name] = f.ndofs * steps / (s.elapsed_time(e) * 1e-3) / 1e9
+    return out
+
+
+def config3_leg():
+    """Mixed precision on the 64^3 Q2 heterogeneous Neo-Hookean problem
+    (6,440,067 DOF; shear modulus 0.25 exp(g), g a unit Gaussian field of
+    correlation length 0.1 (seed 2), bulk modulus 20 G; z = 0 clamped, first of
+    10 compression steps to u_z = -0.05): error of the mixed-precision
+    displacement against the FP64 solve, and both times to 1e-8."""
+    import torch
+
+    import serac_gb300 as sg
+    from serac_gb300 import learned as LP
+
+    prob = LP.neohookean_problem(64, 2, sigma_log=1.0, ell=0.1, strain=0.05, steps=10, bulk_ratio=20.0)
+    S = LP.SolidSetup(prob, 2)
+    base = dict(newton_rel_tol=1e-8, krylov_rel_tol=1e-8, max_krylov_iterations=20000)
+    u64, st64, _ = _solve_step(S, sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, **base))
+    u32, st32, _ = _solve_step(S, sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, mixed_precision=1, **base))
+    err = float(torch.linalg.norm(u32 - u64) / torch.linalg.norm(u64))
+    return {"workload": "neohookean_q2_vector_64cubed_lognormal_G (seed 2), load step 1 of 10", "dofs": S.f.ndofs,
+            "plain_fp64": st64, "mixed": st32, "rel_error_mixed_vs_fp64": err,
+            "speedup_mixed_vs_plain": st64["seconds"] / st32["seconds"]}
+
+
+def large_leg(with_plain=False):
+    """The large combined sizes: 128^3 Q1 (6,440,067 DOF, 2x2x2 Gauss) and 96^3
+    Q2 (21,567,171 DOF) heterogeneous Neo-Hookean (the 64^3 problem's material
+    distribution): time to 1e-8 for the first load step with mixed precision
+    (and learned + mixed when weights exist), Jacobian-action throughput at the
+    converged state, and the device memory the problem holds."""
+    import torch
+
+    import serac_gb300 as sg
+    from serac_gb300 import learned as LP
+
+    out = {}
+    net = None
+    if os.path.exists(WEIGHTS):
+        net = LP.LearnedPreconditioner()
+        net.load(WEIGHTS)
+    base = dict(newton_rel_tol=1e-8, krylov_rel_tol=1e-8, max_krylov_iterations=20000)
+    for order, n in ((1, 128), (2, 96)):
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        prob = LP.neohookean_problem(n, 2, sigma_log=1.0, ell=0.1, strain=0.05, steps=10, bulk_ratio=20.0)
+        S = LP.SolidSetup(prob, order)
+        rec = {"dofs": S.f.ndofs, "order": order, "hexes_per_direction": n}
+        u, st, solver = _solve_step(S, sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, mixed_precision=1,
+                                                                   **base))
+        rec["mixed"] = st
+        rec.update(_jv_rates(S.f, u))
+        torch.cuda.synchronize()
+        rec["device_bytes_held"] = free0 - torch.cuda.mem_get_info()[0]
+        del solver
+        if net is not None:
+            ul, stl, solver = _solve_step(S, sg.SolverOptions.defaults(precond=sg.LEARNED, mixed_precision=1, **base),
+                                          net)
+            stl["rel_diff_vs_mixed"] = float(torch.linalg.norm(ul - u) / torch.linalg.norm(u))
+            rec["learned_mixed"] = stl
+            del solver
+        if with_plain:
+            up, stp, solver = _solve_step(S, sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, **base))
+            stp["rel_diff_vs_mixed"] = float(torch.linalg.norm(up - u) / torch.linalg.norm(u))
+            rec["plain_fp64"] = stp
+            rec["speedup_mixed_vs_plain"] = stp["seconds"] / st["seconds"]
+            del solver
+        out[f"q{order}_{n}cubed"] = rec
+        del S
+        torch.cuda.synchronize()
     return out
 
 
@@ -537,6 +653,9 @@ def main():
     ap.add_argument("--precision", choices=["f64", "f32"], default="f64", help="precision of --kernels-only")
     ap.add_argument("--newton-steps", type=int, default=1,
                     help="load steps of the Newton time-to-1e-8 leg (0 = skip)")
+    ap.add_argument("--extra", choices=["config3", "large", "large-plain"], default=None,
+                    help="run only an extra configuration (64^3 mixed-precision error, or the large sizes) "
+                         "and print its JSON record")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -545,7 +664,14 @@ def main():
 
         backend = "nccl" if args.impl == "sfx" else "gloo"
         dist.init_process_group(backend)
-    if args.impl == "reference":
+    if args.extra is not None:
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        rec = config3_leg() if args.extra == "config3" else large_leg(with_plain=args.extra == "large-plain")
+        if rank == 0:
+            print(json.dumps({"extra": args.extra, **rec}))
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_sfx(args, rank, world)
