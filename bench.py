@@ -407,7 +407,8 @@ def newton_leg(steps):
     from serac_gb300 import learned as LP
 
     prob = LP.j2_problem(NEWTON_N, NEWTON_SEED)
-    base = dict(newton_rel_tol=1e-8, krylov_rel_tol=1e-8, max_krylov_iterations=5000)
+    base = dict(newton_rel_tol=1e-8, newton_abs_tol=0.0, krylov_rel_tol=1e-8, krylov_abs_tol=0.0,
+                max_krylov_iterations=5000)
     variants = [("plain_fp64", sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, **base)),
                 ("mixed", sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, mixed_precision=1, **base))]
     net = None
@@ -438,6 +439,7 @@ def newton_leg(steps):
                 tot[k] = tot.get(k, 0) + st[k]
             tot["predictor_krylov_iterations"] = tot.get("predictor_krylov_iterations", 0) + pre["krylov_iterations"]
             tot["converged"] = min(tot.get("converged", 1), st["converged"])
+            tot["final_rel_residual"] = st["final_residual"] / st["initial_residual"]
             S.commit(u)
         torch.cuda.synchronize()
         tot["seconds"] = time.perf_counter() - t0
@@ -514,7 +516,8 @@ def config3_leg():
 
     prob = LP.neohookean_problem(64, 2, sigma_log=1.0, ell=0.1, strain=0.05, steps=10, bulk_ratio=20.0)
     S = LP.SolidSetup(prob, 2)
-    base = dict(newton_rel_tol=1e-8, krylov_rel_tol=1e-8, max_krylov_iterations=20000)
+    base = dict(newton_rel_tol=1e-8, newton_abs_tol=0.0, krylov_rel_tol=1e-8, krylov_abs_tol=0.0,
+                max_krylov_iterations=20000)
     u64, st64, _ = _solve_step(S, sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, **base))
     u32, st32, _ = _solve_step(S, sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, mixed_precision=1, **base))
     err = float(torch.linalg.norm(u32 - u64) / torch.linalg.norm(u64))
@@ -539,7 +542,8 @@ def large_leg(with_plain=False):
     if os.path.exists(WEIGHTS):
         net = LP.LearnedPreconditioner()
         net.load(WEIGHTS)
-    base = dict(newton_rel_tol=1e-8, krylov_rel_tol=1e-8, max_krylov_iterations=20000)
+    base = dict(newton_rel_tol=1e-8, newton_abs_tol=0.0, krylov_rel_tol=1e-8, krylov_abs_tol=0.0,
+                max_krylov_iterations=20000)
     for order, n in ((1, 128), (2, 96)):
         torch.cuda.synchronize()
         free0 = torch.cuda.mem_get_info()[0]

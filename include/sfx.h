@@ -145,6 +145,12 @@ int sfx_jvp_element(sfx_form form, const double* du, double* dE, void* stream);
 /* The same in FP32 on the FP32 stored tangent (dE: num_elements * c * (p+1)^3 floats). */
 int sfx_jvp_element_f32(sfx_form form, const float* du, float* dE, void* stream);
 
+/* Self-test of the device-side bounded waits (the mbarrier waits of the
+ * bulk-copy kernels): one block waits, for at most `polls` polls, on a barrier
+ * that nothing completes; returns SFX_ERR_TIMEOUT when the bound worked, as it
+ * must, and leaves the context usable. */
+int sfx_selftest_bounded_wait(unsigned polls);
+
 /* Sparsity of dR/du: every (test vdof, trial vdof) pair of every element,
  * rows sorted, columns sorted within a row (dof_numbering.hpp:290-351).
  * row_ptr: device, num_dofs + 1 int64; col: device, nnz int32. */

@@ -44,9 +44,10 @@ __device__ inline bool mbar_test(uint64_t* bar, uint32_t parity) {
       : "memory");
   return done != 0;
 }
-/// bounded wait for the phase of parity `parity`; false if it did not complete in time
-__device__ inline bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (uint32_t k = 0; k < kMaxMbarPolls; k++)
+/// bounded wait for the phase of parity `parity`; false if it did not complete
+/// within `polls` polls
+__device__ inline bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t polls = kMaxMbarPolls) {
+  for (uint32_t k = 0; k < polls; k++)
     if (mbar_test(bar, parity)) return true;
   return false;
 }

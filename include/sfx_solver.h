@@ -84,7 +84,8 @@ int sfx_solver_destroy(sfx_solver solver);
 int sfx_solver_set_essential(sfx_solver solver, const int64_t* dofs, int64_t n);
 /* Newton solve of R(t, u) = 0 in place (u: device, num_dofs doubles). */
 int sfx_solver_solve(sfx_solver solver, double t, double* u, void* stream);
-/* x = J(t, u_lin)^-1 rhs with the essential rows/columns eliminated. */
+/* x = J(t, u_lin)^-1 rhs on the free vdofs with the essential rows/columns
+ * eliminated; the essential entries of rhs are ignored and x is 0 there. */
 int sfx_solver_solve_linear(sfx_solver solver, double t, const double* u_lin, const double* rhs, double* x,
                             void* stream);
 /* Load-step predictor: with d = u_target - u on the essential vdofs (0

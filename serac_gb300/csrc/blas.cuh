@@ -111,6 +111,18 @@ __global__ void cheb_update(int64_t n, T a, T b, const T* __restrict__ r, const 
   z[i] += v;
 }
 
+// one Chebyshev step with the residual formed in place:
+// d = a d + b ((rhs - Jz) / D), z += d
+template <typename T>
+__global__ void cheb_step(int64_t n, T a, T b, const T* __restrict__ rhs, const T* __restrict__ Jz,
+                          const T* __restrict__ D, T* __restrict__ d, T* __restrict__ z) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T v = a * d[i] + b * ((rhs[i] - Jz[i]) / D[i]);
+  d[i] = v;
+  z[i] += v;
+}
+
 template <typename S, typename T>
 __global__ void convert(int64_t n, const S* __restrict__ x, T* __restrict__ y) {
   int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;

@@ -22,6 +22,7 @@
 #include <functional>
 #include <new>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "blas.cuh"
@@ -46,13 +47,15 @@ template <typename T, typename Acc>
 struct Reducer {
   DeviceBuf<Acc> partial;
   DeviceBuf<Acc> out;
+  DeviceBuf<Acc> coef;  // Gram-Schmidt coefficients of both passes and the norm, read back together
   std::vector<Acc> host;
   int nb = 0;
   cudaError_t init(int64_t n, int max_m) {
     nb = int(std::min<int64_t>(sfx_blas::kMaxPartials, std::max<int64_t>(1, (n + 4095) / 4096)));
     cudaError_t e = partial.alloc(size_t(nb) * max_m);
     if (e == cudaSuccess) e = out.alloc(size_t(max_m));
-    host.resize(size_t(max_m));
+    if (e == cudaSuccess) e = coef.alloc(size_t(2 * max_m + 1));
+    host.resize(size_t(2 * max_m + 1));
     return e;
   }
   // host[j] = X_j . y for j < m (one synchronisation)
@@ -66,6 +69,11 @@ struct Reducer {
   Acc dot(const T* x, const T* y, int64_t n, cudaStream_t s, cudaError_t* err) {
     *err = multi_dot(x, 0, 1, y, n, s);
     return host[0];
+  }
+  // dst[j] = X_j . y on the device, no synchronisation
+  void multi_dot_to(const T* X, int64_t ldx, int m, const T* y, int64_t n, Acc* dst, cudaStream_t s) {
+    sfx_blas::multi_dot_partial<T, Acc><<<nb, sfx_blas::kBlock, 0, s>>>(X, ldx, m, y, n, partial.p);
+    sfx_blas::reduce_partials<Acc><<<1, sfx_blas::kBlock, 0, s>>>(partial.p, nb, m, dst);
   }
 };
 
@@ -96,27 +104,17 @@ namespace {
 
 // ---------------------------------------------------------------- operators
 int apply_J64(sfx_solver s, const double* x, double* y, cudaStream_t st) {
-  // y = J (x with essential entries zeroed); y[ess] = x[ess]
-  if (s->n_ess) {
-    SFX_CUDA_TRY(cudaMemcpyAsync(s->tmp2.p, x, sizeof(double) * s->n, cudaMemcpyDeviceToDevice, st));
-    sfx_blas::set_entries<double><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, 0.0, s->tmp2.p);
-    if (int rc = sfx_jvp(s->form, s->tmp2.p, y, st)) return rc;
-    sfx_blas::copy_entries<double><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, x, y);
-  } else {
-    if (int rc = sfx_jvp(s->form, x, y, st)) return rc;
-  }
+  // y = P J P x with P the projection onto the free vdofs; every vector the
+  // solvers pass in is already zero on the essential set (P x = x), so only
+  // the output rows need zeroing
+  if (int rc = sfx_jvp(s->form, x, y, st)) return rc;
+  if (s->n_ess) sfx_blas::set_entries<double><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, 0.0, y);
   return SFX_OK;
 }
 
 int apply_J32(sfx_solver s, const float* x, float* y, cudaStream_t st) {
-  if (s->n_ess) {
-    SFX_CUDA_TRY(cudaMemcpyAsync(s->tmp32b.p, x, sizeof(float) * s->n, cudaMemcpyDeviceToDevice, st));
-    sfx_blas::set_entries<float><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, 0.0f, s->tmp32b.p);
-    if (int rc = sfx_jvp_f32(s->form, s->tmp32b.p, y, st)) return rc;
-    sfx_blas::copy_entries<float><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, x, y);
-  } else {
-    if (int rc = sfx_jvp_f32(s->form, x, y, st)) return rc;
-  }
+  if (int rc = sfx_jvp_f32(s->form, x, y, st)) return rc;
+  if (s->n_ess) sfx_blas::set_entries<float><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, 0.0f, y);
   return SFX_OK;
 }
 
@@ -125,10 +123,11 @@ template <typename T, typename Acc>
 int estimate_lmax(sfx_solver s, int (*apply)(sfx_solver, const T*, T*, cudaStream_t), const T* D, T* x, T* y,
                   Reducer<T, Acc>& red, double* lmax, cudaStream_t st) {
   const int64_t n = s->n;
-  // deterministic start vector: all ones
+  // deterministic start vector: ones on the free vdofs
   {
     std::vector<T> ones(size_t(n), T(1));
     SFX_CUDA_TRY(cudaMemcpyAsync(x, ones.data(), sizeof(T) * n, cudaMemcpyHostToDevice, st));
+    if (s->n_ess) sfx_blas::set_entries<T><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, T(0), x);
     SFX_CUDA_TRY(cudaStreamSynchronize(st));
   }
   cudaError_t err;
@@ -161,10 +160,9 @@ int chebyshev(sfx_solver s, int (*apply)(sfx_solver, const T*, T*, cudaStream_t)
   sfx_blas::scale<T><<<nblocks(n), 256, 0, st>>>(n, T(1.0 / theta), d);
   SFX_CUDA_TRY(cudaMemcpyAsync(z, d, sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
   for (int k = 1; k < s->opt.chebyshev_degree; k++) {
-    if (int rc = apply(s, z, res, st)) return rc;
-    sfx_blas::rsub<T><<<nblocks(n), 256, 0, st>>>(n, b, res);  // res = b - J z
+    if (int rc = apply(s, z, res, st)) return rc;  // res = J z
     double rho_new = 1.0 / (2.0 * sigma - rho);
-    sfx_blas::cheb_update<T><<<nblocks(n), 256, 0, st>>>(n, T(rho_new * rho), T(2.0 * rho_new / delta), res, D, d, z);
+    sfx_blas::cheb_step<T><<<nblocks(n), 256, 0, st>>>(n, T(rho_new * rho), T(2.0 * rho_new / delta), b, res, D, d, z);
     rho = rho_new;
   }
   SFX_CUDA_TRY(cudaGetLastError());
@@ -213,20 +211,23 @@ int gmres(sfx_solver s, int (*apply)(sfx_solver, const T*, T*, cudaStream_t),
       if (int rc = precond(vk, zk)) return rc;
       T* vnext = V + int64_t(k + 1) * n;
       if (int rc = apply(s, zk, vnext, st)) return rc;
-      // classical Gram-Schmidt, twice
+      // classical Gram-Schmidt, twice; the coefficients stay on the device and
+      // are read back once per step together with the new vector's norm
+      static_assert(std::is_same<T, Acc>::value, "coefficients are applied in the vector type");
       double* Hk = &H[size_t(k) * (restart + 1)];
-      for (int j = 0; j <= k; j++) Hk[j] = 0.0;
-      for (int pass = 0; pass < 2; pass++) {
-        SFX_CUDA_TRY(red.multi_dot(V, n, k + 1, vnext, n, st));
-        for (int j = 0; j <= k; j++) {
-          Hk[j] += double(red.host[size_t(j)]);
-          yh[size_t(j)] = T(red.host[size_t(j)]);
-        }
-        SFX_CUDA_TRY(cudaMemcpyAsync(ydev, yh.data(), sizeof(T) * (k + 1), cudaMemcpyHostToDevice, st));
-        sfx_blas::multi_axpy_sub<T><<<nblocks(n), 256, 0, st>>>(n, k + 1, V, n, ydev, vnext);
-      }
-      double hn = std::sqrt(double(red.dot(vnext, vnext, n, st, &err)));
-      SFX_CUDA_TRY(err);
+      Acc* c1 = red.coef.p;
+      Acc* c2 = red.coef.p + (k + 1);
+      Acc* c3 = red.coef.p + 2 * (k + 1);
+      red.multi_dot_to(V, n, k + 1, vnext, n, c1, st);
+      sfx_blas::multi_axpy_sub<T><<<nblocks(n), 256, 0, st>>>(n, k + 1, V, n, c1, vnext);
+      red.multi_dot_to(V, n, k + 1, vnext, n, c2, st);
+      sfx_blas::multi_axpy_sub<T><<<nblocks(n), 256, 0, st>>>(n, k + 1, V, n, c2, vnext);
+      red.multi_dot_to(vnext, 0, 1, vnext, n, c3, st);
+      SFX_CUDA_TRY(cudaMemcpyAsync(red.host.data(), red.coef.p, sizeof(Acc) * size_t(2 * (k + 1) + 1),
+                                   cudaMemcpyDeviceToHost, st));
+      SFX_CUDA_TRY(cudaStreamSynchronize(st));
+      for (int j = 0; j <= k; j++) Hk[j] = double(red.host[size_t(j)]) + double(red.host[size_t(k + 1 + j)]);
+      double hn = std::sqrt(double(red.host[size_t(2 * (k + 1))]));
       Hk[k + 1] = hn;
       if (hn > 0.0) sfx_blas::scale<T><<<nblocks(n), 256, 0, st>>>(n, T(1.0 / hn), vnext);
       for (int j = 0; j < k; j++) {
@@ -376,6 +377,7 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
       const double nv = double(s->red32.dot(res, res, n, st, &err));
       SFX_CUDA_TRY(err);
       if (int rc = lnet_apply(s->net, s->grid[0], s->grid[1], s->grid[2], res, s->features, s->nn_z.p, st)) return rc;
+      if (s->n_ess) sfx_blas::set_entries<float><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, 0.0f, s->nn_z.p);
       s->stats.learned_applications++;
       if (int rc = apply_J32(s, s->nn_z.p, s->nn_x.p, st)) return rc;
       const double rj = double(s->red32.dot(res, s->nn_x.p, n, st, &err));
@@ -553,7 +555,9 @@ int sfx_solver_solve_linear(sfx_solver s, double t, const double* u_lin, const d
   auto st = static_cast<cudaStream_t>(stream);
   s->stats = sfx_solver_stats{};
   if (int rc = sfx_linearize(s->form, t, u_lin, nullptr, st)) return rc;
-  return linear_solve(s, rhs, x, st);
+  SFX_CUDA_TRY(cudaMemcpyAsync(s->r.p, rhs, sizeof(double) * size_t(s->n), cudaMemcpyDeviceToDevice, st));
+  if (s->n_ess) sfx_blas::set_entries<double><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, 0.0, s->r.p);
+  return linear_solve(s, s->r.p, x, st);
 }
 
 int sfx_solver_solve(sfx_solver s, double t, double* u, void* stream) {
