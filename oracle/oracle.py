@@ -49,6 +49,7 @@ BMAT_HEAT_FLUX, BMAT_TRACTION, BMAT_PRESSURE = range(3)
 COMPONENTS = {MAT_HEAT: 1, MAT_NONLINEAR_HEAT: 1, MAT_THERMAL_TEST: 1, MAT_NEOHOOKEAN: 3, MAT_J2: 3, MAT_ELASTIC_TEST: 3}
 NPARAMS = {MAT_HEAT: 2, MAT_NEOHOOKEAN: 2, MAT_J2: 4, MAT_NONLINEAR_HEAT: 3, MAT_THERMAL_TEST: 0, MAT_ELASTIC_TEST: 0}
 BCOMPONENTS = {BMAT_HEAT_FLUX: 1, BMAT_TRACTION: 3, BMAT_PRESSURE: 3}
+BNPARAMS = {BMAT_HEAT_FLUX: 3, BMAT_TRACTION: 6, BMAT_PRESSURE: 1}
 
 _dp = ctypes.POINTER(ctypes.c_double)
 
@@ -359,6 +360,7 @@ class OracleFunctional:
 
     def add_boundary_integral(self, bmat, sides, params):
         assert BCOMPONENTS[bmat] == self.c
+        assert len(np.ravel(params)) == BNPARAMS[bmat], "wrong number of boundary parameters"
         Xf, fnodes = self.mesh.boundary_faces(self.p, sides)
         Xq, Jq = face_geometric_factors(Xf, self.Q, self.use_ref)
         self.boundary.append((bmat, params, fnodes, Xq, Jq))

@@ -26,6 +26,7 @@ HEAT, NEOHOOKEAN, J2, THERMAL_TEST, ELASTIC_TEST, NONLINEAR_HEAT = range(6)
 HEAT_FLUX, TRACTION, PRESSURE = range(3)
 COMPONENTS = {HEAT: 1, NONLINEAR_HEAT: 1, THERMAL_TEST: 1, NEOHOOKEAN: 3, J2: 3, ELASTIC_TEST: 3}
 NPARAMS = {HEAT: 2, NEOHOOKEAN: 2, J2: 4, NONLINEAR_HEAT: 3, THERMAL_TEST: 0, ELASTIC_TEST: 0}
+BNPARAMS = {HEAT_FLUX: 3, TRACTION: 6, PRESSURE: 1}
 J2_STATE_DOUBLES = 10
 
 
@@ -220,6 +221,8 @@ class Functional:
         for s in sides:
             mask |= 1 << (s - 1)
         arr = np.ascontiguousarray(np.asarray(params, dtype=np.float64).ravel())
+        if material in BNPARAMS and arr.size != BNPARAMS[material]:
+            raise ValueError(f"boundary material {material} takes {BNPARAMS[material]} parameters, got {arr.size}")
         _lib.call("sfx_form_add_boundary_integral", self._h, material, mask, arr.ctypes.data_as(_lib._dp))
 
     add_boundary_integral = AddBoundaryIntegral

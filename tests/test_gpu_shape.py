@@ -23,7 +23,8 @@ def _build(mat, c, bmat=None, n=3, p=2):
     saf = sg.ShapeAwareFunctional(mesh, sg.H1(p, 3), sg.H1(p, c))
     saf.AddDomainIntegral(mat, PARAMS[mat])
     if bmat is not None:
-        bp = [0.3, -0.2, 0.5] if bmat == O.BMAT_TRACTION else [0.7]
+        bp = {O.BMAT_TRACTION: [0.3, -0.2, 0.5, 0.1, 0.0, -0.2], O.BMAT_HEAT_FLUX: [0.7, 0.2, 0.4],
+              O.BMAT_PRESSURE: [0.7]}[bmat]
         orc.add_boundary_integral(bmat, [3, 6], bp)
         saf.AddBoundaryIntegral(bmat, [3, 6], bp)
     rng = np.random.default_rng(21)

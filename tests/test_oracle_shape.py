@@ -28,7 +28,8 @@ def _pair(mat, c, n=3, p=2, bmat=None):
     for f in (f_shape, f_moved):
         f.add_domain_integral(mat, PARAMS[mat])
         if bmat is not None:
-            f.add_boundary_integral(bmat, [3, 6], [0.3, -0.2, 0.5] if bmat == O.BMAT_TRACTION else [0.7])
+            f.add_boundary_integral(bmat, [3, 6], {O.BMAT_TRACTION: [0.3, -0.2, 0.5, 0.1, 0.0, -0.2],
+                                                  O.BMAT_PRESSURE: [0.7]}[bmat])
     shape = (moved.node_coordinates(p) - base.node_coordinates(p)).T.ravel()
     f_shape.set_shape(shape)
     return f_shape, f_moved, rng
