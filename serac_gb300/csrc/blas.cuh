@@ -28,34 +28,36 @@ __device__ inline T block_reduce(T v, T* sh) {
 }
 
 // partial[j * gridDim.x + b] = sum over the block's fixed chunk of x_j . y
-// for j in [0, m); x_j = X + j * ldx.  Accumulates in Acc.
+// for j = blockIdx.y (grid: blocks x vectors); x_j = X + j * ldx.
+// Accumulates in Acc.
 template <typename T, typename Acc>
 __global__ void __launch_bounds__(kBlock) multi_dot_partial(const T* __restrict__ X, int64_t ldx, int m,
                                                             const T* __restrict__ y, int64_t n,
                                                             Acc* __restrict__ partial) {
   __shared__ Acc sh[kBlock];
+  const int j = blockIdx.y;
+  if (j >= m) return;
   const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
   const int64_t b0 = int64_t(blockIdx.x) * chunk;
   const int64_t b1 = b0 + chunk < n ? b0 + chunk : n;
-  for (int j = 0; j < m; j++) {
-    const T* x = X + j * ldx;
-    Acc acc = 0;
-    for (int64_t i = b0 + threadIdx.x; i < b1; i += kBlock) acc += Acc(x[i]) * Acc(y[i]);
-    Acc s = block_reduce(acc, sh);
-    if (threadIdx.x == 0) partial[int64_t(j) * gridDim.x + blockIdx.x] = s;
-  }
+  const T* x = X + j * ldx;
+  Acc acc = 0;
+  for (int64_t i = b0 + threadIdx.x; i < b1; i += kBlock) acc += Acc(x[i]) * Acc(y[i]);
+  Acc s = block_reduce(acc, sh);
+  if (threadIdx.x == 0) partial[int64_t(j) * gridDim.x + blockIdx.x] = s;
 }
 
+// out[j] = sum of the nb partials of vector j = blockIdx.x, fixed order
 template <typename Acc>
 __global__ void __launch_bounds__(kBlock) reduce_partials(const Acc* __restrict__ partial, int nb, int m,
                                                           Acc* __restrict__ out) {
   __shared__ Acc sh[kBlock];
-  for (int j = 0; j < m; j++) {
-    Acc acc = 0;
-    for (int i = threadIdx.x; i < nb; i += kBlock) acc += partial[int64_t(j) * nb + i];
-    Acc s = block_reduce(acc, sh);
-    if (threadIdx.x == 0) out[j] = s;
-  }
+  const int j = blockIdx.x;
+  if (j >= m) return;
+  Acc acc = 0;
+  for (int i = threadIdx.x; i < nb; i += kBlock) acc += partial[int64_t(j) * nb + i];
+  Acc s = block_reduce(acc, sh);
+  if (threadIdx.x == 0) out[j] = s;
 }
 
 // y = a x + b y
@@ -109,6 +111,17 @@ __global__ void cheb_update(int64_t n, T a, T b, const T* __restrict__ r, const 
   T v = a * d[i] + b * (r[i] / D[i]);
   d[i] = v;
   z[i] += v;
+}
+
+// first Chebyshev step from zero: d = rhs / (theta D), z = d
+template <typename T>
+__global__ void cheb_start(int64_t n, T inv_theta, const T* __restrict__ rhs, const T* __restrict__ D,
+                           T* __restrict__ d, T* __restrict__ z) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T v = rhs[i] / D[i] * inv_theta;
+  d[i] = v;
+  z[i] = v;
 }
 
 // one Chebyshev step with the residual formed in place:

@@ -60,8 +60,8 @@ struct Reducer {
   }
   // host[j] = X_j . y for j < m (one synchronisation)
   cudaError_t multi_dot(const T* X, int64_t ldx, int m, const T* y, int64_t n, cudaStream_t s) {
-    sfx_blas::multi_dot_partial<T, Acc><<<nb, sfx_blas::kBlock, 0, s>>>(X, ldx, m, y, n, partial.p);
-    sfx_blas::reduce_partials<Acc><<<1, sfx_blas::kBlock, 0, s>>>(partial.p, nb, m, out.p);
+    sfx_blas::multi_dot_partial<T, Acc><<<dim3(nb, m), sfx_blas::kBlock, 0, s>>>(X, ldx, m, y, n, partial.p);
+    sfx_blas::reduce_partials<Acc><<<m, sfx_blas::kBlock, 0, s>>>(partial.p, nb, m, out.p);
     cudaError_t e = cudaMemcpyAsync(host.data(), out.p, sizeof(Acc) * m, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     return e;
@@ -72,8 +72,8 @@ struct Reducer {
   }
   // dst[j] = X_j . y on the device, no synchronisation
   void multi_dot_to(const T* X, int64_t ldx, int m, const T* y, int64_t n, Acc* dst, cudaStream_t s) {
-    sfx_blas::multi_dot_partial<T, Acc><<<nb, sfx_blas::kBlock, 0, s>>>(X, ldx, m, y, n, partial.p);
-    sfx_blas::reduce_partials<Acc><<<1, sfx_blas::kBlock, 0, s>>>(partial.p, nb, m, dst);
+    sfx_blas::multi_dot_partial<T, Acc><<<dim3(nb, m), sfx_blas::kBlock, 0, s>>>(X, ldx, m, y, n, partial.p);
+    sfx_blas::reduce_partials<Acc><<<m, sfx_blas::kBlock, 0, s>>>(partial.p, nb, m, dst);
   }
 };
 
@@ -156,9 +156,7 @@ int chebyshev(sfx_solver s, int (*apply)(sfx_solver, const T*, T*, cudaStream_t)
   const double sigma = theta / delta;
   double rho = 1.0 / sigma;
   // d = D^-1 b / theta ; z = d
-  sfx_blas::diag_solve<T><<<nblocks(n), 256, 0, st>>>(n, b, D, d);
-  sfx_blas::scale<T><<<nblocks(n), 256, 0, st>>>(n, T(1.0 / theta), d);
-  SFX_CUDA_TRY(cudaMemcpyAsync(z, d, sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
+  sfx_blas::cheb_start<T><<<nblocks(n), 256, 0, st>>>(n, T(1.0 / theta), b, D, d, z);
   for (int k = 1; k < s->opt.chebyshev_degree; k++) {
     if (int rc = apply(s, z, res, st)) return rc;  // res = J z
     double rho_new = 1.0 / (2.0 * sigma - rho);
