@@ -95,6 +95,14 @@ __global__ void scale(int64_t n, T a, T* __restrict__ x) {
   if (i < n) x[i] *= a;
 }
 
+// x *= 1 / sqrt(*nrm2) when *nrm2 > 0 (the norm squared stays on the device)
+template <typename T, typename Acc>
+__global__ void scale_inv_sqrt(int64_t n, const Acc* __restrict__ nrm2, T* __restrict__ x) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const double v = double(*nrm2);
+  if (i < n && v > 0.0) x[i] *= T(1.0 / sqrt(v));
+}
+
 // z = x / d (elementwise)
 template <typename T>
 __global__ void diag_solve(int64_t n, const T* __restrict__ x, const T* __restrict__ d, T* __restrict__ z) {

@@ -215,9 +215,12 @@ struct StoredJvpFn {
         if (e != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("bulk jvp attribute: ") + cudaGetErrorString(e));
         configured = true;
       }
-      int dev = 0, sms = 0;
-      cudaGetDevice(&dev);
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      static int sms = 0;  // SM count, queried once (this launch may sit inside a stream capture)
+      if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      }
       const int64_t blocks = std::min<int64_t>((f.ne + WARPS - 1) / WARPS, std::max(sms, 1));
       kern<<<unsigned(blocks), WARPS * 32, smem, s>>>(du, D, f.conn.p, E, f.nnodes, f.ne, f.wait_error.dev);
     } else {

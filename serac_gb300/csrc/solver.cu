@@ -48,13 +48,21 @@ struct Reducer {
   DeviceBuf<Acc> partial;
   DeviceBuf<Acc> out;
   DeviceBuf<Acc> coef;  // Gram-Schmidt coefficients of both passes and the norm, read back together
+  Acc* pinned = nullptr;  // their host copy (page-locked, so the read-back can sit in a CUDA graph)
   std::vector<Acc> host;
   int nb = 0;
+  Reducer() = default;
+  Reducer(const Reducer&) = delete;
+  Reducer& operator=(const Reducer&) = delete;
+  ~Reducer() {
+    if (pinned) cudaFreeHost(pinned);
+  }
   cudaError_t init(int64_t n, int max_m) {
     nb = int(std::min<int64_t>(sfx_blas::kMaxPartials, std::max<int64_t>(1, (n + 4095) / 4096)));
     cudaError_t e = partial.alloc(size_t(nb) * max_m);
     if (e == cudaSuccess) e = out.alloc(size_t(max_m));
     if (e == cudaSuccess) e = coef.alloc(size_t(2 * max_m + 1));
+    if (e == cudaSuccess) e = cudaHostAlloc(reinterpret_cast<void**>(&pinned), sizeof(Acc) * size_t(2 * max_m + 1), 0);
     host.resize(size_t(2 * max_m + 1));
     return e;
   }
@@ -98,6 +106,20 @@ struct sfx_solver_s {
   int grid[3] = {0, 0, 0};
   const float* features = nullptr;
   DeviceBuf<float> nn_z, nn_res, nn_x, x32b;
+  // CUDA graphs of the inner FP32 GMRES steps (one per step index), captured
+  // on a private stream and valid for one linear solve (they hold that
+  // solve's Chebyshev coefficients)
+  cudaStream_t capture = nullptr;
+  std::vector<cudaGraphExec_t> inner_graphs;
+  void drop_graphs() {
+    for (auto& g : inner_graphs)
+      if (g) cudaGraphExecDestroy(g);
+    inner_graphs.assign(inner_graphs.size(), nullptr);
+  }
+  ~sfx_solver_s() {
+    drop_graphs();
+    if (capture) cudaStreamDestroy(capture);
+  }
 };
 
 namespace {
@@ -171,9 +193,9 @@ int chebyshev(sfx_solver s, int (*apply)(sfx_solver, const T*, T*, cudaStream_t)
 // accumulation type Acc.  x holds the initial guess and the result.
 template <typename T, typename Acc>
 int gmres(sfx_solver s, int (*apply)(sfx_solver, const T*, T*, cudaStream_t),
-          const std::function<int(const T*, T*)>& precond, bool flexible, const T* b, T* x, T* V, T* Zs,
-          T* w, T* ydev, Reducer<T, Acc>& red, int restart, int max_iters, double rel_tol, double abs_tol,
-          int* iters_out, double* rel_out, cudaStream_t st) {
+          const std::function<int(const T*, T*, cudaStream_t)>& precond, bool flexible, const T* b, T* x, T* V,
+          T* Zs, T* w, T* ydev, Reducer<T, Acc>& red, int restart, int max_iters, double rel_tol, double abs_tol,
+          int* iters_out, double* rel_out, cudaStream_t st, std::vector<cudaGraphExec_t>* graphs = nullptr) {
   const int64_t n = s->n;
   cudaError_t err;
   const double nb = std::sqrt(double(red.dot(b, b, n, st, &err)));
@@ -206,28 +228,55 @@ int gmres(sfx_solver s, int (*apply)(sfx_solver, const T*, T*, cudaStream_t),
     for (k = 0; k < restart && total < max_iters; k++) {
       T* vk = V + int64_t(k) * n;
       T* zk = flexible ? Zs + int64_t(k) * n : w;
-      if (int rc = precond(vk, zk)) return rc;
       T* vnext = V + int64_t(k + 1) * n;
-      if (int rc = apply(s, zk, vnext, st)) return rc;
-      // classical Gram-Schmidt, twice; the coefficients stay on the device and
-      // are read back once per step together with the new vector's norm
+      // one Arnoldi step: precondition, apply, classical Gram-Schmidt twice,
+      // normalise; the coefficients and the norm stay on the device and are
+      // read back once (page-locked buffer)
       static_assert(std::is_same<T, Acc>::value, "coefficients are applied in the vector type");
-      double* Hk = &H[size_t(k) * (restart + 1)];
       Acc* c1 = red.coef.p;
       Acc* c2 = red.coef.p + (k + 1);
       Acc* c3 = red.coef.p + 2 * (k + 1);
-      red.multi_dot_to(V, n, k + 1, vnext, n, c1, st);
-      sfx_blas::multi_axpy_sub<T><<<nblocks(n), 256, 0, st>>>(n, k + 1, V, n, c1, vnext);
-      red.multi_dot_to(V, n, k + 1, vnext, n, c2, st);
-      sfx_blas::multi_axpy_sub<T><<<nblocks(n), 256, 0, st>>>(n, k + 1, V, n, c2, vnext);
-      red.multi_dot_to(vnext, 0, 1, vnext, n, c3, st);
-      SFX_CUDA_TRY(cudaMemcpyAsync(red.host.data(), red.coef.p, sizeof(Acc) * size_t(2 * (k + 1) + 1),
-                                   cudaMemcpyDeviceToHost, st));
+      const size_t ncoef = size_t(2 * (k + 1) + 1);
+      auto step = [&](cudaStream_t ss) -> int {
+        if (int rc = precond(vk, zk, ss)) return rc;
+        if (int rc = apply(s, zk, vnext, ss)) return rc;
+        red.multi_dot_to(V, n, k + 1, vnext, n, c1, ss);
+        sfx_blas::multi_axpy_sub<T><<<nblocks(n), 256, 0, ss>>>(n, k + 1, V, n, c1, vnext);
+        red.multi_dot_to(V, n, k + 1, vnext, n, c2, ss);
+        sfx_blas::multi_axpy_sub<T><<<nblocks(n), 256, 0, ss>>>(n, k + 1, V, n, c2, vnext);
+        red.multi_dot_to(vnext, 0, 1, vnext, n, c3, ss);
+        sfx_blas::scale_inv_sqrt<T, Acc><<<nblocks(n), 256, 0, ss>>>(n, c3, vnext);
+        SFX_CUDA_TRY(cudaMemcpyAsync(red.pinned, red.coef.p, sizeof(Acc) * ncoef, cudaMemcpyDeviceToHost, ss));
+        SFX_CUDA_TRY(cudaGetLastError());
+        return SFX_OK;
+      };
+      if (graphs && size_t(k) < graphs->size()) {
+        cudaGraphExec_t& ge = (*graphs)[size_t(k)];
+        if (!ge) {
+          SFX_CUDA_TRY(cudaStreamBeginCapture(s->capture, cudaStreamCaptureModeThreadLocal));
+          const int rc = step(s->capture);
+          cudaGraph_t graph = nullptr;
+          const cudaError_t e = cudaStreamEndCapture(s->capture, &graph);
+          if (rc || e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc ? rc : fail(SFX_ERR_CUDA, std::string("inner step capture: ") + cudaGetErrorString(e));
+          }
+          const cudaError_t ei = cudaGraphInstantiate(&ge, graph, 0);
+          cudaGraphDestroy(graph);
+          if (ei != cudaSuccess) {
+            ge = nullptr;
+            return fail(SFX_ERR_CUDA, std::string("inner step graph: ") + cudaGetErrorString(ei));
+          }
+        }
+        SFX_CUDA_TRY(cudaGraphLaunch(ge, st));
+      } else {
+        if (int rc = step(st)) return rc;
+      }
       SFX_CUDA_TRY(cudaStreamSynchronize(st));
-      for (int j = 0; j <= k; j++) Hk[j] = double(red.host[size_t(j)]) + double(red.host[size_t(k + 1 + j)]);
-      double hn = std::sqrt(double(red.host[size_t(2 * (k + 1))]));
+      double* Hk = &H[size_t(k) * (restart + 1)];
+      for (int j = 0; j <= k; j++) Hk[j] = double(red.pinned[size_t(j)]) + double(red.pinned[size_t(k + 1 + j)]);
+      double hn = std::sqrt(double(red.pinned[size_t(2 * (k + 1))]));
       Hk[k + 1] = hn;
-      if (hn > 0.0) sfx_blas::scale<T><<<nblocks(n), 256, 0, st>>>(n, T(1.0 / hn), vnext);
       for (int j = 0; j < k; j++) {
         double t = cs[size_t(j)] * Hk[j] + sn[size_t(j)] * Hk[j + 1];
         Hk[j + 1] = -sn[size_t(j)] * Hk[j] + cs[size_t(j)] * Hk[j + 1];
@@ -264,7 +313,7 @@ int gmres(sfx_solver s, int (*apply)(sfx_solver, const T*, T*, cudaStream_t),
       SFX_CUDA_TRY(cudaMemsetAsync(w, 0, sizeof(T) * n, st));
       sfx_blas::multi_axpy_add<T><<<nblocks(n), 256, 0, st>>>(n, k, V, n, ydev, w);
       T* zz = V + int64_t(k) * n;
-      if (int rc = precond(w, zz)) return rc;
+      if (int rc = precond(w, zz, st)) return rc;
       sfx_blas::axpby<T><<<nblocks(n), 256, 0, st>>>(n, T(1), zz, T(1), x);
     }
     SFX_CUDA_TRY(cudaGetLastError());
@@ -330,6 +379,8 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
   const auto& o = s->opt;
   int iters = 0;
   double rel = 0.0;
+  // graphs of the inner steps hold the previous linearisation's Chebyshev coefficients
+  s->drop_graphs();
   // Jacobi diagonal with unit entries on the essential set
   if (int rc = sfx_assemble_diagonal(s->form, s->diag.p, st)) return rc;
   if (s->n_ess) sfx_blas::set_entries<double><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, 1.0, s->diag.p);
@@ -342,14 +393,15 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
   const int m = o.restart;
   if (ensure(s->V, size_t(m + 1) * n) || ensure(s->Z, size_t(m) * n))
     return fail(SFX_ERR_NOMEM, "Krylov basis allocation failed");
-  std::function<int(const double*, double*)> prec;
+  // the outer preconditioner runs on st (it is not captured); the stream argument is unused
+  std::function<int(const double*, double*, cudaStream_t)> prec;
   if (o.precond == SFX_PREC_NONE) {
-    prec = [=](const double* v, double* z) -> int {
+    prec = [=](const double* v, double* z, cudaStream_t) -> int {
       SFX_CUDA_TRY(cudaMemcpyAsync(z, v, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
       return SFX_OK;
     };
   } else if (o.precond == SFX_PREC_JACOBI) {
-    prec = [=](const double* v, double* z) -> int {
+    prec = [=](const double* v, double* z, cudaStream_t) -> int {
       sfx_blas::diag_solve<double><<<nblocks(n), 256, 0, st>>>(n, v, s->diag.p, z);
       return SFX_OK;
     };
@@ -394,22 +446,23 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
       }
       return SFX_OK;
     };
-    auto cheb32 = [=](const float* b, float* z) -> int {
-      return chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, b, z, s->cheb_d32.p, s->cheb_r32.p, st);
+    auto cheb32 = [=](const float* b, float* z, cudaStream_t ss) -> int {
+      return chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, b, z, s->cheb_d32.p, s->cheb_r32.p, ss);
     };
     if (o.mixed_precision) {
       // network step, then inner FP32 GMRES(k) + Jacobi-Chebyshev on what it leaves
-      prec = [=](const double* v, double* z) -> int {
+      prec = [=](const double* v, double* z, cudaStream_t) -> int {
         sfx_blas::convert<double, float><<<nblocks(n), 256, 0, st>>>(n, v, s->b32.p);
         SFX_CUDA_TRY(cudaMemsetAsync(s->x32b.p, 0, sizeof(float) * n, st));
         const float* left = nullptr;
         if (int rc = nn_step(s->b32.p, s->x32b.p, &left)) return rc;
         SFX_CUDA_TRY(cudaMemsetAsync(s->x32.p, 0, sizeof(float) * n, st));
-        std::function<int(const float*, float*)> inner_prec = cheb32;
+        std::function<int(const float*, float*, cudaStream_t)> inner_prec = cheb32;
         int it = 0;
         double rel_in = 0.0;
         if (int rc = gmres<float, float>(s, apply_J32, inner_prec, false, left, s->x32.p, s->V32.p, nullptr,
-                                         s->tmp32.p, s->y32.p, s->red32, k, k, o.inner_rel_tol, 0.0, &it, &rel_in, st))
+                                         s->tmp32.p, s->y32.p, s->red32, k, k, o.inner_rel_tol, 0.0, &it, &rel_in, st,
+                                         &s->inner_graphs))
           return rc;
         s->stats.inner_iterations += it;
         sfx_blas::axpby<float><<<nblocks(n), 256, 0, st>>>(n, 1.0f, s->x32.p, 1.0f, s->x32b.p);
@@ -418,11 +471,11 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
       };
     } else {
       // cycle 0: network, Chebyshev; cycle 1: Chebyshev, network, Chebyshev
-      prec = [=](const double* v, double* z) -> int {
+      prec = [=](const double* v, double* z, cudaStream_t) -> int {
         sfx_blas::convert<double, float><<<nblocks(n), 256, 0, st>>>(n, v, s->b32.p);
         const float* res = s->b32.p;
         if (o.learned_cycle == 1) {
-          if (int rc = cheb32(s->b32.p, s->x32b.p)) return rc;
+          if (int rc = cheb32(s->b32.p, s->x32b.p, st)) return rc;
           if (int rc = apply_J32(s, s->x32b.p, s->tmp32.p, st)) return rc;
           sfx_blas::rsub<float><<<nblocks(n), 256, 0, st>>>(n, s->b32.p, s->tmp32.p);
           res = s->tmp32.p;
@@ -431,7 +484,7 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
         }
         const float* left = nullptr;
         if (int rc = nn_step(res, s->x32b.p, &left)) return rc;
-        if (int rc = cheb32(left, s->x32.p)) return rc;
+        if (int rc = cheb32(left, s->x32.p, st)) return rc;
         sfx_blas::axpby<float><<<nblocks(n), 256, 0, st>>>(n, 1.0f, s->x32.p, 1.0f, s->x32b.p);
         sfx_blas::convert<float, double><<<nblocks(n), 256, 0, st>>>(n, s->x32b.p, z);
         return SFX_OK;
@@ -448,16 +501,18 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
     if (int rc = estimate_lmax<float, float>(s, apply_J32, s->diag32.p, s->tmp32.p, s->cheb_r32.p, s->red32,
                                              &s->lmax32, st))
       return rc;
-    prec = [=](const double* v, double* z) -> int {
+    prec = [=](const double* v, double* z, cudaStream_t) -> int {
       sfx_blas::convert<double, float><<<nblocks(n), 256, 0, st>>>(n, v, s->b32.p);
       SFX_CUDA_TRY(cudaMemsetAsync(s->x32.p, 0, sizeof(float) * n, st));
-      std::function<int(const float*, float*)> inner_prec = [=](const float* a, float* b) -> int {
-        return chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, a, b, s->cheb_d32.p, s->cheb_r32.p, st);
+      std::function<int(const float*, float*, cudaStream_t)> inner_prec = [=](const float* a, float* b,
+                                                                               cudaStream_t ss) -> int {
+        return chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, a, b, s->cheb_d32.p, s->cheb_r32.p, ss);
       };
       int it = 0;
       double rel_in = 0.0;
       if (int rc = gmres<float, float>(s, apply_J32, inner_prec, false, s->b32.p, s->x32.p, s->V32.p, nullptr,
-                                       s->tmp32.p, s->y32.p, s->red32, k, k, o.inner_rel_tol, 0.0, &it, &rel_in, st))
+                                       s->tmp32.p, s->y32.p, s->red32, k, k, o.inner_rel_tol, 0.0, &it, &rel_in, st,
+                                       &s->inner_graphs))
         return rc;
       s->stats.inner_iterations += it;
       sfx_blas::convert<float, double><<<nblocks(n), 256, 0, st>>>(n, s->x32.p, z);
@@ -467,7 +522,7 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
     if (ensure(s->cheb_d, n) || ensure(s->cheb_r, n)) return fail(SFX_ERR_NOMEM, "workspace allocation failed");
     if (int rc = estimate_lmax<double, double>(s, apply_J64, s->diag.p, s->tmp.p, s->cheb_r.p, s->red, &s->lmax, st))
       return rc;
-    prec = [=](const double* v, double* z) -> int {
+    prec = [=](const double* v, double* z, cudaStream_t) -> int {
       return chebyshev<double, double>(s, apply_J64, s->diag.p, s->lmax, v, z, s->cheb_d.p, s->cheb_r.p, st);
     };
   }
@@ -477,6 +532,11 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
                                  o.max_krylov_iterations, o.krylov_rel_tol, o.krylov_abs_tol, &iters, &rel, st);
   s->stats.krylov_iterations += iters;
   s->stats.last_krylov_rel = rel;
+  if (rc == SFX_OK && s->form->wait_error.raised()) {
+    // a bounded wait inside a replayed FP32 action expired
+    s->form->wait_error.clear();
+    return fail(SFX_ERR_TIMEOUT, "a bulk-copy wait of the FP32 Jacobian action expired");
+  }
   return rc;
 }
 
@@ -529,6 +589,11 @@ int sfx_solver_create(sfx_form form, const sfx_solver_options* opt, sfx_solver* 
     delete s;
     return fail(SFX_ERR_NOMEM, "solver workspace allocation failed");
   }
+  if (cudaStreamCreateWithFlags(&s->capture, cudaStreamNonBlocking) != cudaSuccess) {
+    delete s;
+    return fail(SFX_ERR_CUDA, "capture stream creation failed");
+  }
+  s->inner_graphs.assign(size_t(s->opt.inner_iterations), nullptr);
   *out = s;
   return SFX_OK;
 }
