@@ -394,7 +394,7 @@ NEWTON_SEED = 2000  # held out from the training seeds
 WEIGHTS = os.path.join(ROOT, "serac_gb300", "weights", "lnet_j2_q2.npy")
 
 
-def newton_leg(steps):
+def newton_leg(steps, only=None):
     """Newton time-to-1e-8 relative residual on the heterogeneous J2 problem
     (32^3 hexes, Q2 vector, per-element lognormal E, held-out seed), over the
     first `steps` load steps (warm-start predictor, Newton, state commit):
@@ -420,6 +420,8 @@ def newton_leg(steps):
            "workload": f"j2_q2_vector_{NEWTON_N}cubed_lognormal_E (seed {NEWTON_SEED}), load steps 1-{steps} of "
                        f"{prob.steps}, strain {prob.strain}",
            "dofs": 3 * (2 * NEWTON_N + 1) ** 3}
+    if only is not None:
+        variants = [v for v in variants if v[0] in only]
     ref = None
     for name, opts in variants:
         S = LP.SolidSetup(prob)
@@ -449,7 +451,7 @@ def newton_leg(steps):
         out[name] = tot
         del solver, S
     for name in ("mixed", "learned_mixed"):
-        if name in out:
+        if name in out and "plain_fp64" in out:
             out[f"speedup_{name}_vs_plain"] = out["plain_fp64"]["seconds"] / out[name]["seconds"]
     if net is None:
         out["learned_mixed"] = {"unavailable": f"no trained weights at {os.path.relpath(WEIGHTS, ROOT)}"}
@@ -657,7 +659,7 @@ def main():
     ap.add_argument("--precision", choices=["f64", "f32"], default="f64", help="precision of --kernels-only")
     ap.add_argument("--newton-steps", type=int, default=1,
                     help="load steps of the Newton time-to-1e-8 leg (0 = skip)")
-    ap.add_argument("--extra", choices=["config3", "large", "large-plain"], default=None,
+    ap.add_argument("--extra", choices=["config3", "large", "large-plain", "newton-mixed"], default=None,
                     help="run only an extra configuration (64^3 mixed-precision error, or the large sizes) "
                          "and print its JSON record")
     args = ap.parse_args()
@@ -672,7 +674,12 @@ def main():
         import torch
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
-        rec = config3_leg() if args.extra == "config3" else large_leg(with_plain=args.extra == "large-plain")
+        if args.extra == "newton-mixed":  # the mixed-precision Newton leg alone (for profiler launch lists)
+            rec = newton_leg(1, only=("mixed",))
+        elif args.extra == "config3":
+            rec = config3_leg()
+        else:
+            rec = large_leg(with_plain=args.extra == "large-plain")
         if rank == 0:
             print(json.dumps({"extra": args.extra, **rec}))
     elif args.impl == "reference":

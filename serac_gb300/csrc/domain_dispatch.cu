@@ -199,12 +199,15 @@ struct StoredJvpFn {
     constexpr bool HS = kernels::tangent_has_source<C, State, QF>();
     if (f.ne == 0) return SFX_OK;
     if constexpr (P == 2 && std::is_same<Real, float>::value) {
-      // bulk-copy staged kernel: one persistent block per SM; warps and ring
-      // depth chosen so the rings fit in 220 KB of shared memory
+      // bulk-copy staged kernel: one persistent block per SM with as many warps
+      // as fit two-deep rings in 220 KB of shared memory, rings up to 4 deep
       using Shape = kernels::TangentShape<C, HS, Maker::value_input>;
       constexpr size_t kSmemBudget = 220 * 1024;
       constexpr size_t stage_bytes = size_t(Shape::template stride<NQ>) * 4 + 8;
-      constexpr int WARPS = 8 * 2 * stage_bytes <= kSmemBudget ? 8 : 4;
+      constexpr int WARPS = 16 * 2 * stage_bytes <= kSmemBudget   ? 16
+                            : 12 * 2 * stage_bytes <= kSmemBudget ? 12
+                            : 8 * 2 * stage_bytes <= kSmemBudget  ? 8
+                                                                  : 4;
       constexpr int STAGES = int(std::min<size_t>(4, kSmemBudget / (WARPS * stage_bytes)));
       static_assert(STAGES >= 2, "tangent block too large for a two-stage ring");
       constexpr size_t smem = size_t(WARPS) * STAGES * stage_bytes;
