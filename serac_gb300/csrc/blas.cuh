@@ -95,12 +95,20 @@ __global__ void scale(int64_t n, T a, T* __restrict__ x) {
   if (i < n) x[i] *= a;
 }
 
-// x *= 1 / sqrt(*nrm2) when *nrm2 > 0 (the norm squared stays on the device)
+// x *= 1 / sqrt(*nrm2) when *nrm2 > 0 (the norm squared stays on the device;
+// one thread per block forms the factor)
 template <typename T, typename Acc>
 __global__ void scale_inv_sqrt(int64_t n, const Acc* __restrict__ nrm2, T* __restrict__ x) {
+  __shared__ T a;
+  __shared__ bool go;
+  if (threadIdx.x == 0) {
+    const double v = double(*nrm2);
+    go = v > 0.0;
+    a = go ? T(1.0 / sqrt(v)) : T(1);
+  }
+  __syncthreads();
   int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  const double v = double(*nrm2);
-  if (i < n && v > 0.0) x[i] *= T(1.0 / sqrt(v));
+  if (i < n && go) x[i] *= a;
 }
 
 // z = x / d (elementwise)
