@@ -28,6 +28,9 @@ def main(argv=None):
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--init-seed", type=int, default=0)
+    ap.add_argument("--steps", type=int, default=4, help="load steps per training problem")
+    ap.add_argument("--eval-seeds", default=None,
+                    help="first:last held-out seeds: after training, solve them with and without the network")
     ap.add_argument("--out", required=True)
     args = ap.parse_args(argv)
 
@@ -37,7 +40,7 @@ def main(argv=None):
 
     lo, hi = (int(x) for x in args.seeds.split(":"))
     t0 = time.time()
-    problems = [L.j2_problem(args.n, s) for s in range(lo, hi)]
+    problems = [L.j2_problem(args.n, s, steps=args.steps) for s in range(lo, hi)]
     R, T, F = L.harvest(problems, probes_per_step=args.probes)
     torch.cuda.synchronize()
     t_harvest = time.time() - t0
@@ -52,9 +55,58 @@ def main(argv=None):
     info = {"pairs": int(R.shape[0]), "seeds": args.seeds, "n": args.n, "epochs": args.epochs, "batch": args.batch,
             "lr": args.lr, "harvest_s": round(t_harvest, 1), "train_s": round(time.time() - t0, 1),
             "final_loss": hist[-1], "loss_history": [round(h, 4) for h in hist]}
+    if args.eval_seeds:
+        info["evaluation"] = evaluate(net, args.n, args.eval_seeds, args.steps)
     with open(os.path.splitext(args.out)[0] + ".json", "w") as fh:
         json.dump(info, fh, indent=1)
     print(json.dumps(info))
+
+
+def evaluate(net, n, seeds, steps):
+    """Held-out seeds: Krylov iterations and seconds of flexible GMRES with
+    Jacobi-Chebyshev alone against the network's two-level step
+    (Chebyshev, network, Chebyshev), and of mixed precision against learned +
+    mixed precision; every pair must reach the same answer."""
+    import torch
+
+    from . import learned as L
+    from .solver import FGMRES, JACOBI_CHEBYSHEV, LEARNED, NewtonSolver, SolverOptions
+
+    tol = dict(newton_rel_tol=1e-8, newton_abs_tol=0.0, krylov_rel_tol=1e-8, krylov_abs_tol=0.0,
+               max_krylov_iterations=20000)
+    variants = {
+        "chebyshev": (SolverOptions.defaults(precond=JACOBI_CHEBYSHEV, krylov=FGMRES, **tol), False),
+        "learned_two_level": (SolverOptions.defaults(precond=LEARNED, learned_cycle=1, **tol), True),
+        "mixed": (SolverOptions.defaults(precond=JACOBI_CHEBYSHEV, mixed_precision=1, **tol), False),
+        "learned_mixed": (SolverOptions.defaults(precond=LEARNED, mixed_precision=1, **tol), True),
+    }
+    lo, hi = (int(x) for x in seeds.split(":"))
+    totals = {k: {"krylov_iterations": 0, "seconds": 0.0} for k in variants}
+    worst_diff = 0.0
+    for seed in range(lo, hi):
+        prob = L.j2_problem(n, seed, steps=steps)
+        sols = {}
+        for name, (opts, use_net) in variants.items():
+            S = L.SolidSetup(prob)
+            solver = NewtonSolver(S.f, opts)
+            solver.set_essential(S.ess)
+            if use_net:
+                solver.set_learned(net, S.grid, S.features)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            u, tot = L.solve_load_steps(S, solver)
+            torch.cuda.synchronize()
+            totals[name]["seconds"] += time.perf_counter() - t0
+            totals[name]["krylov_iterations"] += tot["krylov_iterations"] + tot["predictor_krylov_iterations"]
+            sols[name] = u
+        ref = sols["chebyshev"]
+        for u in sols.values():
+            worst_diff = max(worst_diff, float(torch.linalg.norm(u - ref) / torch.linalg.norm(ref)))
+    return {"seeds": seeds, "n": n, "totals": totals, "max_rel_diff": worst_diff,
+            "iteration_ratio_two_level": totals["learned_two_level"]["krylov_iterations"]
+            / max(1, totals["chebyshev"]["krylov_iterations"]),
+            "time_ratio_two_level": totals["learned_two_level"]["seconds"] / totals["chebyshev"]["seconds"],
+            "time_ratio_learned_mixed": totals["learned_mixed"]["seconds"] / totals["mixed"]["seconds"]}
 
 
 if __name__ == "__main__":
