@@ -38,35 +38,86 @@ __device__ inline void mma_bf16_16816(float (&d)[4], const uint32_t (&a)[4], con
 
 enum Act : int { ACT_NONE = 0, ACT_RELU = 1 };
 
-/// Forward 3x3x3 convolution.  One warp computes 16 consecutive output nodes
-/// for all COUT channels (COUT/8 mma tiles); the K loop runs over the 27 taps
-/// and the input channels in chunks of 16.  x: [node][CIN] bf16, W: [COUT][27][CIN]
-/// bf16, bias: [COUT] f32 (may be null), y: [node][COUT] bf16.  If `y_f32` is
-/// non-null the pre-cast FP32 result is written there instead.  blockIdx.y
-/// selects the sample of a batch (volumes stored one after another).
+/// Shared-memory layout of conv3_fwd for CIN input and COUT output channels:
+/// the input rows of the block's 64 output nodes for each of the 9 (dy, dz)
+/// neighbour offsets (66 consecutive nodes each, a row stride of CIN + 8 bf16)
+/// and the whole weight tensor (per output channel 27 * CIN + 8 bf16).  The
+/// padding makes the mma fragment loads of 8 rows x 4 lanes hit 32 banks.
+template <int CIN, int COUT>
+struct ConvSmem {
+  static constexpr int NODES = 64;         // output nodes per block (4 warps x 16)
+  static constexpr int SEG = NODES + 2;    // staged source nodes per (dy, dz) offset
+  static constexpr int RS = CIN + 8;       // input row stride (bf16)
+  static constexpr int WS = 27 * CIN + 8;  // weight row stride per output channel (bf16)
+  static constexpr size_t x_elems = size_t(9) * SEG * RS;
+  static constexpr size_t w_elems = size_t(COUT) * WS;
+  static constexpr size_t bytes = (x_elems + w_elems) * 2;
+};
+
+/// Forward 3x3x3 convolution as an implicit GEMM on mma.sync m16n8k16 (BF16 in,
+/// FP32 accumulate).  A block of 4 warps computes 64 consecutive output nodes
+/// (16 per warp) for all COUT channels; the input rows they touch and the
+/// weights are first staged in shared memory (16-byte vector loads), then the
+/// K loop runs over the 27 taps and the input channels in chunks of 16.
+/// x: [node][CIN] bf16, W: [COUT][27][CIN] bf16, bias: [COUT] f32 (may be
+/// null), y: [node][COUT] bf16.  If `y_f32` is non-null the pre-cast FP32
+/// result is written there instead.  blockIdx.y selects the sample of a batch
+/// (volumes stored one after another).  Dynamic shared memory:
+/// ConvSmem<CIN, COUT>::bytes.
 template <int CIN, int COUT, int ACT>
 __global__ void __launch_bounds__(128) conv3_fwd(Grid3 g, const __nv_bfloat16* __restrict__ x,
                                                  const __nv_bfloat16* __restrict__ W, const float* __restrict__ bias,
                                                  __nv_bfloat16* __restrict__ y, float* __restrict__ y_f32) {
   static_assert(CIN % 16 == 0 && COUT % 8 == 0, "channel counts");
+  using L = ConvSmem<CIN, COUT>;
   constexpr int NT = COUT / 8;
-  const int lane = threadIdx.x & 31;
-  const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-  const int64_t n0 = warp * 16;
+  extern __shared__ __align__(16) unsigned char sfx_conv_smem[];
+  __nv_bfloat16* sx = reinterpret_cast<__nv_bfloat16*>(sfx_conv_smem);
+  __nv_bfloat16* sw = sx + L::x_elems;
   const int64_t N = g.nodes();
-  if (n0 >= N) return;
+  const int64_t n0 = int64_t(blockIdx.x) * L::NODES;
   x += int64_t(blockIdx.y) * N * CIN;
   if (y) y += int64_t(blockIdx.y) * N * COUT;
   if (y_f32) y_f32 += int64_t(blockIdx.y) * N * COUT;
+
+  // stage the weights: W[co][tap][ci] -> sw[co * WS + tap * CIN + ci]
+  {
+    constexpr int VPR = 27 * CIN / 8;  // 16-byte vectors per output channel
+    const uint4* src = reinterpret_cast<const uint4*>(W);
+    for (int i = threadIdx.x; i < COUT * VPR; i += blockDim.x) {
+      const int co = i / VPR, v = i % VPR;
+      *reinterpret_cast<uint4*>(sw + co * L::WS + v * 8) = src[i];
+    }
+  }
+  // stage the input rows: segment k = (dz + 1) * 3 + (dy + 1) holds nodes
+  // n0 - 1 + dy nx + dz nx ny + [0, SEG) (zeros outside [0, N))
+  {
+    constexpr int VPN = CIN / 8;  // 16-byte vectors per node
+    const uint4* src = reinterpret_cast<const uint4*>(x);
+    const int64_t plane = int64_t(g.nx) * g.ny;
+    for (int i = threadIdx.x; i < 9 * L::SEG * VPN; i += blockDim.x) {
+      const int k = i / (L::SEG * VPN), rem = i % (L::SEG * VPN);
+      const int j = rem / VPN, v = rem % VPN;
+      const int dy = k % 3 - 1, dz = k / 3 - 1;
+      const int64_t node = n0 - 1 + dy * int64_t(g.nx) + dz * plane + j;
+      uint4 val = make_uint4(0u, 0u, 0u, 0u);
+      if (node >= 0 && node < N) val = src[node * VPN + v];
+      *reinterpret_cast<uint4*>(sx + (size_t(k) * L::SEG + j) * L::RS + v * 8) = val;
+    }
+  }
+  __syncthreads();
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int gid = lane >> 2, tig = lane & 3;
-  // the two rows (nodes) this lane feeds into the A fragment
-  int64_t rn[2] = {n0 + gid, n0 + gid + 8};
+  // the two rows (output nodes) this lane feeds into the A fragment
+  int ln[2] = {warp * 16 + gid, warp * 16 + gid + 8};  // local index in [0, 64)
   int rx[2], ry[2], rz[2];
   bool rv[2];
 #pragma unroll
   for (int h = 0; h < 2; h++) {
-    rv[h] = rn[h] < N;
-    const int64_t nn = rv[h] ? rn[h] : 0;
+    const int64_t n = n0 + ln[h];
+    rv[h] = n < N;
+    const int64_t nn = rv[h] ? n : 0;
     rx[h] = int(nn % g.nx);
     ry[h] = int((nn / g.nx) % g.ny);
     rz[h] = int(nn / (int64_t(g.nx) * g.ny));
@@ -77,32 +128,30 @@ __global__ void __launch_bounds__(128) conv3_fwd(Grid3 g, const __nv_bfloat16* _
 #pragma unroll
     for (int k = 0; k < 4; k++) acc[j][k] = 0.f;
 
-  const uint32_t* x32 = reinterpret_cast<const uint32_t*>(x);
-  const uint32_t* W32 = reinterpret_cast<const uint32_t*>(W);
 #pragma unroll 1
   for (int tap = 0; tap < 27; tap++) {
     const int dx = tap % 3 - 1, dy = (tap / 3) % 3 - 1, dz = tap / 9 - 1;
-    int64_t src[2];
+    const int seg = (dz + 1) * 3 + (dy + 1);
+    const __nv_bfloat16* rowp[2];
     bool sv[2];
 #pragma unroll
     for (int h = 0; h < 2; h++) {
       const int xx = rx[h] + dx, yy = ry[h] + dy, zz = rz[h] + dz;
       sv[h] = rv[h] && xx >= 0 && xx < g.nx && yy >= 0 && yy < g.ny && zz >= 0 && zz < g.nz;
-      src[h] = sv[h] ? (int64_t(zz) * g.ny + yy) * g.nx + xx : 0;
+      rowp[h] = sx + (size_t(seg) * L::SEG + (ln[h] + 1 + dx)) * L::RS;
     }
 #pragma unroll
     for (int kc = 0; kc < CIN / 16; kc++) {
       const int c0 = kc * 16 + tig * 2;
       uint32_t a[4];
-      a[0] = sv[0] ? x32[(src[0] * CIN + c0) >> 1] : 0u;
-      a[1] = sv[1] ? x32[(src[1] * CIN + c0) >> 1] : 0u;
-      a[2] = sv[0] ? x32[(src[0] * CIN + c0 + 8) >> 1] : 0u;
-      a[3] = sv[1] ? x32[(src[1] * CIN + c0 + 8) >> 1] : 0u;
+      a[0] = sv[0] ? *reinterpret_cast<const uint32_t*>(rowp[0] + c0) : 0u;
+      a[1] = sv[1] ? *reinterpret_cast<const uint32_t*>(rowp[1] + c0) : 0u;
+      a[2] = sv[0] ? *reinterpret_cast<const uint32_t*>(rowp[0] + c0 + 8) : 0u;
+      a[3] = sv[1] ? *reinterpret_cast<const uint32_t*>(rowp[1] + c0 + 8) : 0u;
 #pragma unroll
       for (int j = 0; j < NT; j++) {
-        const int co = j * 8 + gid;
-        const int64_t wb = (int64_t(co) * 27 + tap) * CIN + c0;
-        uint32_t b[2] = {W32[wb >> 1], W32[(wb + 8) >> 1]};
+        const __nv_bfloat16* wr = sw + (j * 8 + gid) * L::WS + tap * CIN + c0;
+        uint32_t b[2] = {*reinterpret_cast<const uint32_t*>(wr), *reinterpret_cast<const uint32_t*>(wr + 8)};
         mma_bf16_16816(acc[j], a, b);
       }
     }
@@ -115,16 +164,17 @@ __global__ void __launch_bounds__(128) conv3_fwd(Grid3 g, const __nv_bfloat16* _
 #pragma unroll
     for (int h = 0; h < 2; h++) {
       if (!rv[h]) continue;
+      const int64_t n = n0 + ln[h];
       float v0 = acc[j][2 * h] + b0, v1 = acc[j][2 * h + 1] + b1;
       if (ACT == ACT_RELU) {
         v0 = v0 > 0.f ? v0 : 0.f;
         v1 = v1 > 0.f ? v1 : 0.f;
       }
       if (y_f32) {
-        y_f32[rn[h] * COUT + co] = v0;
-        y_f32[rn[h] * COUT + co + 1] = v1;
+        y_f32[n * COUT + co] = v0;
+        y_f32[n * COUT + co + 1] = v1;
       } else {
-        reinterpret_cast<uint32_t*>(y)[(rn[h] * COUT + co) >> 1] = pack_bf16x2(v0, v1);
+        reinterpret_cast<uint32_t*>(y)[(n * COUT + co) >> 1] = pack_bf16x2(v0, v1);
       }
     }
   }

@@ -168,14 +168,28 @@ __global__ void adam(float* __restrict__ p, const float* __restrict__ g, float* 
 // --------------------------------------------------------- conv dispatch
 #define SFX_PAIRS(X) X(16, 16) X(16, 32) X(32, 32) X(32, 48) X(48, 48) X(48, 32) X(32, 16)
 
+// launch one staged convolution (the dynamic shared-memory limit is raised
+// once per instantiation)
+template <int CI, int CO, int ACT>
+void launch_conv(Grid3 g, int batch, const bf16* x, const bf16* W, const float* b, bf16* y, float* y32,
+                 cudaStream_t s) {
+  using L = sfx::nn::ConvSmem<CI, CO>;
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(sfx::nn::conv3_fwd<CI, CO, ACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(L::bytes));
+    configured = true;
+  }
+  const dim3 blocks(unsigned((g.nodes() + L::NODES - 1) / L::NODES), unsigned(batch));
+  sfx::nn::conv3_fwd<CI, CO, ACT><<<blocks, 128, L::bytes, s>>>(g, x, W, b, y, y32);
+}
+
 void conv_fwd(int ci, int co, bool relu, Grid3 g, int batch, const bf16* x, const bf16* W, const float* b, bf16* y,
               float* y32, cudaStream_t s) {
-  const dim3 blocks(nb(((g.nodes() + 15) / 16) * 32, 128), unsigned(batch));
-#define SFX_CONV(CI, CO)                                                                                   \
-  if (ci == CI && co == CO) {                                                                              \
-    if (relu) sfx::nn::conv3_fwd<CI, CO, sfx::nn::ACT_RELU><<<blocks, 128, 0, s>>>(g, x, W, b, y, y32);    \
-    else sfx::nn::conv3_fwd<CI, CO, sfx::nn::ACT_NONE><<<blocks, 128, 0, s>>>(g, x, W, b, y, y32);         \
-    return;                                                                                                \
+#define SFX_CONV(CI, CO)                                                           \
+  if (ci == CI && co == CO) {                                                      \
+    if (relu) launch_conv<CI, CO, sfx::nn::ACT_RELU>(g, batch, x, W, b, y, y32, s); \
+    else launch_conv<CI, CO, sfx::nn::ACT_NONE>(g, batch, x, W, b, y, y32, s);      \
+    return;                                                                        \
   }
   SFX_PAIRS(SFX_CONV)
 #undef SFX_CONV
