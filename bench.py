@@ -193,6 +193,23 @@ class _mesh_proxy:
 
 
 # ----------------------------------------------------------------- GPU arm
+def max_over_ranks(seconds, world, device):
+    """The slowest rank's time (replicas run the same workload independently)."""
+    if world <= 1:
+        return seconds
+    import torch
+
+    t = torch.tensor([seconds], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world, dofs, steps, seconds):
+    """Whole-job GDOF/s: every replica applied the operator `steps` times to
+    `dofs` unknowns in at most `seconds`."""
+    return world * dofs * steps / seconds / 1e9
+
+
 def run_sfx(args, rank, world):
     import torch
 
@@ -257,11 +274,8 @@ def run_sfx(args, rank, world):
     torch.cuda.synchronize()
     clk = clocks.stop(dev.index)
     total = sum(t_fp64)
-    if world > 1:
-        tt = torch.tensor([total], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total = tt.item()
-    value = world * ndofs * args.steps / total / 1e9
+    total = max_over_ranks(total, world, dev)
+    value = replica_throughput(world, ndofs, args.steps, total)
 
     # ---- FP32 Jv (inner Krylov operator)
     t_fp32 = timed(lambda: grad.mult(du32, dr32), args.steps)
