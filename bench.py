@@ -591,6 +591,38 @@ def large_leg(with_plain=False):
     return out
 
 
+def lnet_leg():
+    """The learned preconditioner's kernels: one inference pass and one
+    training step (batch 8) on the node grids of the 16^3 and 32^3 Q2 meshes."""
+    import torch
+
+    from serac_gb300 import learned as LP
+
+    net = LP.LearnedPreconditioner(seed=0)
+    out = {}
+    for nodes in (33, 65):
+        grid = (nodes,) * 3
+        n = nodes ** 3
+        r = torch.randn(3 * n, device="cuda")
+        feat = torch.zeros(2 * n, device="cuda")
+        R = torch.randn(8, 3 * n, device="cuda")
+        T = torch.randn(8, 3 * n, device="cuda")
+        F = torch.zeros(8, 2 * n, device="cuda")
+        rec = {}
+        for name, fn, reps in (("apply_ms", lambda: net.apply(grid, r, feat), 20),
+                               ("train_step_batch8_ms", lambda: net.train_step(grid, R, T, F, 8, 0.0), 5)):
+            for _ in range(3):
+                fn()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                fn()
+            torch.cuda.synchronize()
+            rec[name] = (time.perf_counter() - t0) / reps * 1e3
+        out[f"grid_{nodes}"] = rec
+    return out
+
+
 def measure_fp64_peak(dev):
     import torch
 
@@ -673,7 +705,7 @@ def main():
     ap.add_argument("--precision", choices=["f64", "f32"], default="f64", help="precision of --kernels-only")
     ap.add_argument("--newton-steps", type=int, default=1,
                     help="load steps of the Newton time-to-1e-8 leg (0 = skip)")
-    ap.add_argument("--extra", choices=["config3", "large", "large-plain", "newton-mixed"], default=None,
+    ap.add_argument("--extra", choices=["config3", "large", "large-plain", "newton-mixed", "lnet"], default=None,
                     help="run only an extra configuration (64^3 mixed-precision error, or the large sizes) "
                          "and print its JSON record")
     args = ap.parse_args()
@@ -690,6 +722,8 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         if args.extra == "newton-mixed":  # the mixed-precision Newton leg alone (for profiler launch lists)
             rec = newton_leg(1, only=("mixed",))
+        elif args.extra == "lnet":
+            rec = lnet_leg()
         elif args.extra == "config3":
             rec = config3_leg()
         else:

@@ -1,11 +1,16 @@
 """Learned multilevel preconditioner (include/sfx_learned.h): network wrapper,
-seeded heterogeneous material fields, training-data harvest from the plain
-solver and training on the GPU with the library's own BF16 kernels.
+seeded heterogeneous material fields, training-data harvest from the solver
+and training on the GPU with the library's own BF16 kernels.
 
+    problems = [j2_problem(16, seed) for seed in range(1000, 1032)]
+    R, T, F = harvest(problems)                     # (residual, correction) pairs + node features
     net = LearnedPreconditioner(seed=0)
-    data = harvest(problem_factory, seeds)          # (residual, Newton correction) pairs
-    train(net, data, epochs=...)
-    solver.set_learned(net, grid, features)         # SolverOptions(precond=LEARNED)
+    train(net, (33, 33, 33), R, T, F, epochs=40)
+    S = SolidSetup(j2_problem(16, 2000))
+    solver = NewtonSolver(S.f, SolverOptions.defaults(precond=LEARNED, mixed_precision=1))
+    solver.set_essential(S.ess)
+    solver.set_learned(net, S.grid, S.features)
+    u, stats = solve_load_steps(S, solver)
 """
 from __future__ import annotations
 
@@ -16,8 +21,8 @@ import numpy as np
 import torch
 
 from . import _lib
-from .functional import H1, Functional, Mesh, box_vertices, differentiate_wrt
-from .solver import JACOBI_CHEBYSHEV, NewtonSolver, SolverOptions
+from .functional import H1, Functional, Mesh, box_vertices
+from .solver import JACOBI_CHEBYSHEV, NewtonSolver, SolverOptions  # noqa: F401 (re-exported for callers)
 
 
 class LearnedPreconditioner:
