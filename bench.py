@@ -347,7 +347,7 @@ def run_sfx(args, rank, world):
     t_k32 = statistics.mean(t_elem32)
     roofline32 = {
         "bound": "hbm",
-        "kernel": "sfx::kernels::jvp_stored_tma_kernel<3,false,false,8,3> (FP32, bulk-copy staged)",
+        "kernel": "sfx::kernels::jvp_stored_tma_kernel<3,false,false,12,2> (FP32, bulk-copy staged)",
         "achieved": alg_bytes32 / t_k32 / 1e9,
         "peak": hbm_peak,
         "unit": "GB/s",
