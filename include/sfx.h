@@ -110,8 +110,8 @@ int sfx_form_set_shape_displacement(sfx_form form, const double* shape, void* st
 /* dr = dR/dp (t, u; p) dshape: the derivative of the residual with respect to
  * the shape displacement p set on the form (zero when none is set), applied to
  * dshape (device, 3 * num_nodes doubles) — ShapeAwareFunctional differentiated
- * with respect to its argument 0 (shape_aware_functional.hpp:537-541).  Domain
- * integrals; a form with boundary integrals returns SFX_ERR_UNSUPPORTED. */
+ * with respect to its argument 0 (shape_aware_functional.hpp:537-541), for
+ * its domain and boundary integrals. */
 int sfx_shape_jvp(sfx_form form, double t, const double* u, const double* dshape, double* dr, void* stream);
 
 /* r = R(t, u) (device, num_dofs doubles each).  When sfx_update_qdata(form, 1)

@@ -143,6 +143,104 @@ __global__ void __launch_bounds__(128) face_kernel(FaceArgs<Real> a, QF qf) {
   }
 }
 
+/// Derivative of a shape-aware boundary integral with respect to the shape
+/// displacement, applied to dp (serac's ShapeAwareBoundaryIntegrandWrapper,
+/// shape_aware_functional.hpp:475-498, differentiated with respect to the
+/// shape): x' = X + p + eps dp and dx'/d(s,t) = J + dp/d(s,t) + eps d(dp)/d(s,t)
+/// on dual numbers, so the q-function value and the area weight
+/// |dx'/ds x dx'/dt| w carry the directional derivative; its derivative part
+/// is integrated into out_e [f][c][node].  Xf: [f][3][4] face vertices,
+/// shape (nullptr = 0) and dshape: byNODES 3-component fields of order P.
+template <int P, int C, typename QF>
+__global__ void __launch_bounds__(128) face_shape_jvp_kernel(FaceArgs<double> a, QF qf,
+                                                             const double* __restrict__ Xf,
+                                                             const double* __restrict__ shape,
+                                                             const double* __restrict__ dshape) {
+  using Real = double;
+  using S = dual<Real, Real>;
+  constexpr int Q = P + 1;
+  constexpr int NQ = Q * Q;
+  constexpr int FPW = 32 / NQ;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int sub = lane / NQ;
+  const int qi_raw = lane - sub * NQ;
+  const bool slot = sub < FPW;
+  const int qi = slot ? qi_raw : NQ - 1;
+  const int base = slot ? sub * NQ : 0;
+  const int64_t f = warp * FPW + (slot ? sub : 0);
+  const bool valid = slot && f < a.num_faces;
+  const int ix = qi % Q, iy = qi / Q;
+
+  __shared__ Real sB[Q][Q], sG[Q][Q];
+  if (threadIdx.x < Q * Q) {
+    int i = threadIdx.x / Q, j = threadIdx.x % Q;
+    sB[i][j] = basis_table<P>().B[i][j];
+    sG[i][j] = basis_table<P>().G[i][j];
+  }
+  __syncthreads();
+  const int32_t node = valid ? a.fconn[f * NQ + qi] : 0;
+
+  fvalue_t<C, S> qv{};
+  fgrad_t<C, S> qg{};
+#pragma unroll
+  for (int c = 0; c < C; c++) {
+    Real U = valid ? a.u[c * a.num_nodes + node] : Real(0);
+    Real v, gs, gt;
+    face_interpolate<Q, Real>(U, base, ix, iy, sB, sG, v, gs, gt);
+    comp<C>(qv, c) = S{v, Real(0)};
+    comp<C>(qg, c)[0] = S{gs, Real(0)};
+    comp<C>(qg, c)[1] = S{gt, Real(0)};
+  }
+  // shape field and direction at the point
+  tensor<S, 3> X{};
+  tensor<S, 3, 2> J{};
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    Real pv, ps, pt, dv, ds, dt;
+    const Real Pn = (valid && shape) ? shape[i * a.num_nodes + node] : Real(0);
+    const Real dPn = valid ? dshape[i * a.num_nodes + node] : Real(0);
+    face_interpolate<Q, Real>(Pn, base, ix, iy, sB, sG, pv, ps, pt);
+    face_interpolate<Q, Real>(dPn, base, ix, iy, sB, sG, dv, ds, dt);
+    X[i] = S{pv, dv};
+    J[i][0] = S{ps, ds};
+    J[i][1] = S{pt, dt};
+  }
+  // reference (bilinear) face geometry
+  const Real sp[2] = {gl_point(Q, ix), gl_point(Q, iy)};
+  const Real w = gl_weight(Q, ix) * gl_weight(Q, iy);
+  const Real* Xv = Xf + (valid ? f : 0) * 12;
+#pragma unroll
+  for (int v = 0; v < 4; v++) {
+    const int b0 = v & 1, b1 = (v >> 1) & 1;
+    const Real N0 = b0 ? sp[0] : 1.0 - sp[0], N1 = b1 ? sp[1] : 1.0 - sp[1];
+    const Real d0 = b0 ? 1.0 : -1.0, d1 = b1 ? 1.0 : -1.0;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const Real xv = Xv[i * 4 + v];
+      X[i].value += xv * N0 * N1;
+      J[i][0].value += xv * d0 * N1;
+      J[i][1].value += xv * N0 * d1;
+    }
+  }
+  const S n0 = J[1][0] * J[2][1] - J[2][0] * J[1][1];
+  const S n1 = J[2][0] * J[0][1] - J[0][0] * J[2][1];
+  const S n2 = J[0][0] * J[1][1] - J[1][0] * J[0][1];
+  const S n2sum = n0 * n0 + n1 * n1 + n2 * n2;
+  const Real nrm = ::sqrt(n2sum.value);
+  const S weight = S{nrm * w, valid && nrm > 0 ? 0.5 * n2sum.gradient / nrm * w : Real(0)};
+  auto out = qf(a.t, tuple{X, J}, tuple{qv, qg});
+  using OutT = std::decay_t<decltype(out)>;
+  constexpr bool HS = !is_zero<typename base_scalar<OutT>::type>::value;
+#pragma unroll
+  for (int c = 0; c < C; c++) {
+    Real s = 0;
+    if constexpr (HS) s = part<JVP, Real>(weight * source_comp<C>(out, c));
+    Real r = face_integrate<Q, Real>(s, base, ix, iy, sB);
+    if (valid) a.out_e[(f * C + c) * NQ + qi] = r;
+  }
+}
+
 /// Face element matrices K[f][trial vdof][test vdof] (as the domain ones),
 /// by directional duals seeded on each parent-space input of each trial
 /// component, then one face integration per trial node.

@@ -10,6 +10,8 @@
 // The q-function call convention is serac's: qf(t, tuple{X, dX_dxi}, [state&,] tuple{value, gradient}).
 #pragma once
 
+#include <type_traits>
+
 #include "sfx/dual.hpp"
 #include "sfx/tensor.hpp"
 #include "sfx/tuple.hpp"
@@ -230,7 +232,8 @@ struct Traction {
   SFX_HDI auto operator()(double, const X& position, const T& displacement) const {
     auto x = get<0>(position);
     auto u = get<0>(displacement);
-    tensor<double, 3> tr{};
+    using XT = std::decay_t<decltype(x[0])>;  // double, or a dual under a shape derivative
+    tensor<XT, 3> tr{};
     for (int i = 0; i < 3; i++) tr[i] = t0[i] + t1[i] * x[0];
     return 0.0 * u - tr;
   }

@@ -126,6 +126,43 @@ struct FaceMatrixFn {
 
 namespace sfx_impl {
 
+template <int P>
+struct ShapeFaceFn {
+  const sfx_form_s& f;
+  const BoundaryIntegral& bi;
+  const double* u;
+  const double* dshape;
+  double* out;
+  double t;
+  cudaStream_t s;
+  template <int C, typename QF>
+  int operator()(const QF& qf) {
+    constexpr int NQ = (P + 1) * (P + 1);
+    constexpr int FPW = 32 / NQ;
+    if (bi.num_faces == 0) return SFX_OK;
+    kernels::FaceArgs<double> a{u, nullptr, f.ef64.p, bi.fconn.p, bi.fgeom.p, f.nnodes, bi.num_faces, t};
+    const int64_t warps = (bi.num_faces + FPW - 1) / FPW;
+    kernels::face_shape_jvp_kernel<P, C, QF><<<unsigned((warps * 32 + 127) / 128), 128, 0, s>>>(
+        a, qf, bi.Xf.p, f.has_shape ? f.shape.p : nullptr, dshape);
+    kernels::face_scatter_kernel<C, NQ, double><<<unsigned((bi.num_face_nodes + 255) / 256), 256, 0, s>>>(
+        f.ef64.p, bi.node_ptr.p, bi.node_ids.p, bi.node_ent.p, out, bi.num_face_nodes, f.nnodes);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("face shape jvp launch: ") + cudaGetErrorString(err));
+    return SFX_OK;
+  }
+};
+
+// out += d(boundary residual)/dp dshape for every boundary integral of the form
+int launch_boundary_shape_jvp(const sfx_form_s& f, const double* u, const double* dshape, double* out, double t,
+                              cudaStream_t s) {
+  for (const auto& bi : f.boundary) {
+    const int rc = f.p == 1 ? visit_bmaterial(bi, ShapeFaceFn<1>{f, bi, u, dshape, out, t, s})
+                            : visit_bmaterial(bi, ShapeFaceFn<2>{f, bi, u, dshape, out, t, s});
+    if (rc) return rc;
+  }
+  return SFX_OK;
+}
+
 int launch_boundary(const sfx_form_s& f, int mode, const double* u, const double* du, double* out, double t,
                     cudaStream_t s) {
   for (const auto& bi : f.boundary) {

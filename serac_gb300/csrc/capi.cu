@@ -218,18 +218,13 @@ int sfx_form_set_shape_displacement(sfx_form form, const double* shape, void* st
 int sfx_shape_jvp(sfx_form form, double t, const double* u, const double* dshape, double* dr, void* stream) {
   if (check_form(form)) return SFX_ERR_INVALID;
   if (!u || !dshape || !dr) return fail(SFX_ERR_INVALID, "null vector");
-  if (!form->boundary.empty())
-    return fail(SFX_ERR_UNSUPPORTED, "the shape derivative covers domain integrals only in this version");
   auto s = static_cast<cudaStream_t>(stream);
-  if (form->domain.empty()) {
-    SFX_CUDA_TRY(cudaMemsetAsync(dr, 0, sizeof(double) * size_t(form->ndofs), s));
-    return SFX_OK;
-  }
+  if (form->domain.empty()) SFX_CUDA_TRY(cudaMemsetAsync(dr, 0, sizeof(double) * size_t(form->ndofs), s));
   for (size_t i = 0; i < form->domain.size(); i++) {
     if (int rc = sfx_impl::launch_shape_jvp(*form, form->domain[i], u, dshape, form->e64.p, t, s)) return rc;
     if (int rc2 = scatter_dispatch<double>(*form, form->e64.p, dr, i > 0, s)) return rc2;
   }
-  return SFX_OK;
+  return sfx_impl::launch_boundary_shape_jvp(*form, u, dshape, dr, t, s);
 }
 
 int sfx_form_destroy(sfx_form form) {

@@ -32,6 +32,9 @@ int assemble_boundary(sfx_form_s& f, double* values, double* diag, cudaStream_t 
 // derivative of the domain residual with respect to the shape displacement, applied to dshape
 int launch_shape_jvp(const sfx_form_s& f, const DomainIntegral& di, const double* u, const double* dshape, double* E,
                      double t, cudaStream_t s);
+// out += derivative of the boundary residual with respect to the shape displacement, applied to dshape
+int launch_boundary_shape_jvp(const sfx_form_s& f, const double* u, const double* dshape, double* out, double t,
+                              cudaStream_t s);
 // geometric factors (reference or shape-displaced configuration)
 int compute_face_geometry(sfx_form_s& f, BoundaryIntegral& bi, cudaStream_t s);
 int compute_geometry(sfx_form_s& f, cudaStream_t s);
