@@ -52,11 +52,12 @@ typedef struct {
   double krylov_rel_tol;     /* 1e-8 */
   double krylov_abs_tol;     /* 1e-12 */
   int precond;               /* SFX_PREC_* (Jacobi-Chebyshev) */
-  int chebyshev_degree;      /* 3: Chebyshev polynomial degree (degree-1 Jacobian actions) */
+  int chebyshev_degree;      /* 3: Chebyshev polynomial degree (degree-1 Jacobian actions); higher degrees
+                                amplify the modes above the power-iteration estimate of lmax */
   double chebyshev_ratio;    /* 30: interval [lmax / ratio, 1.1 lmax] of D^-1 J */
   int power_iterations;      /* 10: lmax estimate per linearisation */
   int mixed_precision;       /* 1: FP64 flexible GMRES outside, FP32 GMRES + FP32 Jacobi-Chebyshev inside */
-  int inner_iterations;      /* 20: FP32 inner GMRES steps per outer step */
+  int inner_iterations;      /* 40: FP32 inner GMRES steps per outer step */
   double inner_rel_tol;      /* 1e-3 */
   int print_level;           /* 0 */
   int learned_cycle;         /* 1: SFX_PREC_LEARNED without mixed precision: 1 Chebyshev, network on

@@ -560,7 +560,7 @@ int sfx_solver_default_options(sfx_solver_options* o) {
   o->chebyshev_ratio = 30.0;
   o->power_iterations = 10;
   o->mixed_precision = 0;
-  o->inner_iterations = 20;
+  o->inner_iterations = 40;
   o->inner_rel_tol = 1e-3;
   o->print_level = 0;
   o->learned_cycle = 1;
