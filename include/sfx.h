@@ -184,6 +184,25 @@ typedef struct {
 } sfx_form_layout;
 int sfx_form_get_layout(sfx_form form, sfx_form_layout* out);
 
+/* Face sets for boundary integrals whose q-functions the caller evaluates in
+ * its own kernels (the C++ front-end's AddBoundaryIntegral with user
+ * q-functions, functional.hpp:328-354): the faces of the sides in side_mask
+ * (1: z=0, 2: y=0, 3: x=1, 4: y=1, 5: x=0, 6: z=1), their geometric factors
+ * (shape-displaced with the form) and the compact face-node map of the
+ * deterministic face scatter. */
+typedef struct {
+  int64_t num_faces;
+  int nodes_per_face;       /* (order+1)^2, also the points per face */
+  const int32_t* fconn;     /* [face][nodes_per_face] node ids, outward (s, t) order */
+  const double* fgeom;      /* 10 x num_faces * nodes_per_face point factors (sfx/boundary.cuh FGEOM_STRIDE) */
+  int64_t num_face_nodes;   /* distinct nodes of the set */
+  const int32_t* node_ptr;  /* [num_face_nodes + 1] entries per distinct node */
+  const int32_t* node_ids;  /* global node of each distinct node */
+  const int32_t* node_ent;  /* face * nodes_per_face + local, face order */
+} sfx_face_layout;
+int sfx_form_add_face_set(sfx_form form, int side_mask, int* face_set);
+int sfx_form_get_face_layout(sfx_form form, int face_set, sfx_face_layout* out);
+
 /* out = (accumulate ? out : 0) + scatter-add of the E-vector E [e][component][node]
  * (ElementRestriction::ScatterAdd, element_restriction.cpp:456-467), node-owner
  * order, deterministic. */

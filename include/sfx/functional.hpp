@@ -20,8 +20,9 @@
 // from the C ABI.
 //
 // Scope of this version: one trial space equal to the test space (DependsOn<0>),
-// domain integrals over the whole mesh; boundary integrals through the C ABI
-// material library (sfx_form_add_boundary_integral).
+// domain integrals over the whole mesh and boundary integrals over box sides,
+// both with user q-functions (the C ABI material library,
+// sfx_form_add_boundary_integral, serves callers without a compiler).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -34,6 +35,7 @@
 #include <vector>
 
 #include "sfx.h"
+#include "sfx/boundary.cuh"
 #include "sfx/kernels.cuh"
 
 namespace sfx {
@@ -229,6 +231,114 @@ struct DomainIntegral : IntegralBase {
   }
 };
 
+template <typename T>
+__global__ void to_f32_kernel(const double* __restrict__ x, float* __restrict__ y, int64_t n) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = float(x[i]);
+}
+
+/// A boundary integral of a user q-function over a face set
+/// (AddBoundaryIntegral, functional.hpp:328-354): qf(t, tuple{X, dX/d(s,t)},
+/// tuple{u, du/d(s,t)}) returns the flux per unit reference area (a scalar or
+/// a c-vector), integrated with |dX/ds x dX/dt| over the faces.  Jacobian
+/// actions re-evaluate the q-function on directional duals; the diagonal and
+/// the CSR values come from face element matrices.  Every result is added to
+/// its output through the face set's deterministic node-owner scatter.
+template <int P, int C, typename QF>
+struct BoundaryIntegral {
+  static constexpr int NQ = (P + 1) * (P + 1);
+  static constexpr int FPW = 32 / NQ;
+  QF qf;
+  int face_set = -1;
+  sfx_face_layout F{};
+  DeviceArray<double> E;
+  DeviceArray<float> E32;
+  DeviceArray<double> K;
+
+  unsigned blocks() const { return warp_blocks(F.num_faces, FPW); }
+  unsigned scatter_blocks() const { return unsigned((F.num_face_nodes + 255) / 256); }
+  template <typename Real>
+  kernels::FaceArgs<Real> args(const sfx_form_layout& L, const Real* u, const Real* du, Real* out, double t) const {
+    return {u, du, out, F.fconn, F.fgeom, L.num_nodes, F.num_faces, t};
+  }
+  // out += R_boundary(t, u)
+  void residual(const sfx_form_layout& L, double t, const double* u, double* out, cudaStream_t s) {
+    if (F.num_faces == 0) return;
+    E.resize(size_t(F.num_faces) * C * NQ);
+    kernels::face_kernel<P, C, kernels::RESIDUAL, double, QF><<<blocks(), 128, 0, s>>>(args(L, u, (const double*)nullptr, E.p, t), qf);
+    kernels::face_scatter_kernel<C, NQ, double><<<scatter_blocks(), 256, 0, s>>>(
+        E.p, F.node_ptr, F.node_ids, F.node_ent, out, F.num_face_nodes, L.num_nodes);
+    check_cuda(cudaGetLastError(), "boundary residual kernel");
+  }
+  // out += dR_boundary/du(t, u) du (FP64 or FP32 throughout)
+  template <typename Real>
+  void jvp(const sfx_form_layout& L, double t, const Real* u, const Real* du, Real* out, cudaStream_t s) {
+    if (F.num_faces == 0) return;
+    Real* e;
+    if constexpr (std::is_same<Real, double>::value) {
+      E.resize(size_t(F.num_faces) * C * NQ);
+      e = E.p;
+    } else {
+      E32.resize(size_t(F.num_faces) * C * NQ);
+      e = E32.p;
+    }
+    kernels::face_kernel<P, C, kernels::JVP, Real, QF><<<blocks(), 128, 0, s>>>(args(L, u, du, e, t), qf);
+    kernels::face_scatter_kernel<C, NQ, Real><<<scatter_blocks(), 256, 0, s>>>(
+        e, F.node_ptr, F.node_ids, F.node_ent, out, F.num_face_nodes, L.num_nodes);
+    check_cuda(cudaGetLastError(), "boundary jvp kernel");
+  }
+  // face element matrices at (t, u), then += into the diagonal and / or the CSR values
+  void matrices(const sfx_form_layout& L, double t, const double* u, double* diag, double* values, cudaStream_t s) {
+    if (F.num_faces == 0) return;
+    K.resize(size_t(F.num_faces) * (C * NQ) * (C * NQ));
+    kernels::face_matrix_kernel<P, C, QF><<<blocks(), 128, 0, s>>>(args(L, u, (const double*)nullptr, K.p, t), qf);
+    if (diag)
+      kernels::face_diag_kernel<C, NQ><<<scatter_blocks(), 256, 0, s>>>(F.node_ptr, F.node_ids, F.node_ent, K.p, diag,
+                                                                         F.num_face_nodes, L.num_nodes);
+    if (values) {
+      kernels::GridShape g{};
+      g.p = P;
+      g.ne[0] = L.nx;
+      g.ne[1] = L.ny;
+      g.ne[2] = L.nz;
+      for (int d = 0; d < 3; d++) g.N[d] = int64_t(P) * g.ne[d] + 1;
+      kernels::face_csr_kernel<P, C><<<unsigned((F.num_face_nodes * C + 127) / 128), 128, 0, s>>>(
+          g, L.row_ptr, F.fconn, F.node_ptr, F.node_ids, F.node_ent, K.p, values, F.num_face_nodes);
+    }
+    check_cuda(cudaGetLastError(), "boundary matrix kernels");
+  }
+};
+
+struct BoundaryBase {
+  virtual ~BoundaryBase() = default;
+  virtual void residual(const sfx_form_layout& L, double t, const double* u, double* out, cudaStream_t s) = 0;
+  virtual void jvp(const sfx_form_layout& L, double t, const double* u, const double* du, double* out,
+                   cudaStream_t s) = 0;
+  virtual void jvp_f32(const sfx_form_layout& L, double t, const float* u, const float* du, float* out,
+                       cudaStream_t s) = 0;
+  virtual void matrices(const sfx_form_layout& L, double t, const double* u, double* diag, double* values,
+                        cudaStream_t s) = 0;
+};
+template <int P, int C, typename QF>
+struct BoundaryHolder : BoundaryBase {
+  BoundaryIntegral<P, C, QF> b;
+  void residual(const sfx_form_layout& L, double t, const double* u, double* out, cudaStream_t s) override {
+    b.residual(L, t, u, out, s);
+  }
+  void jvp(const sfx_form_layout& L, double t, const double* u, const double* du, double* out,
+           cudaStream_t s) override {
+    b.template jvp<double>(L, t, u, du, out, s);
+  }
+  void jvp_f32(const sfx_form_layout& L, double t, const float* u, const float* du, float* out,
+               cudaStream_t s) override {
+    b.template jvp<float>(L, t, u, du, out, s);
+  }
+  void matrices(const sfx_form_layout& L, double t, const double* u, double* diag, double* values,
+                cudaStream_t s) override {
+    b.matrices(L, t, u, diag, values, s);
+  }
+};
+
 }  // namespace detail
 
 template <typename Signature>
@@ -294,6 +404,23 @@ class Functional<H1<p, c>(H1<p, c>)> {
     AddDomainIntegral(Dimension<3>{}, d, qf);
   }
 
+  /// AddBoundaryIntegral(Dimension<2>, DependsOn<0>, qf, sides) (functional.hpp:328-354)
+  /// over the faces of the box sides in side_mask (bit s-1 for side s: 1 z=0,
+  /// 2 y=0, 3 x=1, 4 y=1, 5 x=0, 6 z=1); qf(t, tuple{X, dX/d(s,t)},
+  /// tuple{u, du/d(s,t)}) returns the boundary flux (scalar or c-vector).
+  template <typename QF>
+  void AddBoundaryIntegral(Dimension<2>, DependsOn<0>, const QF& qf, int side_mask) {
+    auto h = std::make_unique<detail::BoundaryHolder<p, c, QF>>();
+    h->b.qf = qf;
+    check(sfx_form_add_face_set(form_.get(), side_mask, &h->b.face_set));
+    check(sfx_form_get_face_layout(form_.get(), h->b.face_set, &h->b.F));
+    boundary_.push_back(std::move(h));
+  }
+  template <typename QF>
+  void AddSurfaceIntegral(DependsOn<0> d, const QF& qf, int side_mask) {
+    AddBoundaryIntegral(Dimension<2>{}, d, qf, side_mask);
+  }
+
   /// updateQdata(bool) (functional.hpp:523): commit quadrature state on residual calls
   void updateQdata(bool flag) { update_qdata_ = flag; }
 
@@ -311,22 +438,31 @@ class Functional<H1<p, c>(H1<p, c>)> {
     return out_.p;
   }
   void residual(double t, const double* u, double* r, cudaStream_t s = nullptr) {
-    if (integrals_.empty()) throw std::runtime_error("sfx: no integrals");
+    if (integrals_.empty() && boundary_.empty()) throw std::runtime_error("sfx: no integrals");
+    if (integrals_.empty()) check_cuda(cudaMemsetAsync(r, 0, sizeof(double) * size_t(L_.num_dofs), s), "memset");
     for (size_t i = 0; i < integrals_.size(); i++) {
       integrals_[i]->residual(L_, t, u, L_.evector, update_qdata_, s);
       check(sfx_scatter_add(form_.get(), L_.evector, r, i > 0, s));
     }
+    for (auto& b : boundary_) b->residual(L_, t, u, r, s);
   }
 
   /// (R(t, u), dR/du) with the tangent linearised at u (functional.hpp:481-489)
   std::tuple<const double*, Gradient&> operator()(double t, differentiate_wrt_this w, cudaStream_t s = nullptr) {
-    if (integrals_.empty()) throw std::runtime_error("sfx: no integrals");
+    if (integrals_.empty() && boundary_.empty()) throw std::runtime_error("sfx: no integrals");
     check_cuda(cudaMemcpyAsync(u_lin_.p, w.u, sizeof(double) * size_t(L_.num_dofs), cudaMemcpyDeviceToDevice, s),
                "copy u");
     t_lin_ = t;
+    if (integrals_.empty()) check_cuda(cudaMemsetAsync(out_.p, 0, sizeof(double) * size_t(L_.num_dofs), s), "memset");
     for (size_t i = 0; i < integrals_.size(); i++) {
       integrals_[i]->linearize(L_, t, u_lin_.p, L_.evector, s);
       check(sfx_scatter_add(form_.get(), L_.evector, out_.p, i > 0, s));
+    }
+    if (!boundary_.empty()) {
+      u_lin32_.resize(size_t(L_.num_dofs));
+      detail::to_f32_kernel<float><<<unsigned((L_.num_dofs + 255) / 256), 256, 0, s>>>(u_lin_.p, u_lin32_.p,
+                                                                                       L_.num_dofs);
+      for (auto& b : boundary_) b->residual(L_, t, u_lin_.p, out_.p, s);
     }
     linearized_ = true;
     return {out_.p, grad_};
@@ -339,24 +475,30 @@ class Functional<H1<p, c>(H1<p, c>)> {
   }
   void jvp(const double* dx, double* df, cudaStream_t s) {
     require_linearized();
+    if (integrals_.empty()) check_cuda(cudaMemsetAsync(df, 0, sizeof(double) * size_t(L_.num_dofs), s), "memset");
     for (size_t i = 0; i < integrals_.size(); i++) {
       integrals_[i]->jvp(L_, dx, L_.evector, s);
       check(sfx_scatter_add(form_.get(), L_.evector, df, i > 0, s));
     }
+    for (auto& b : boundary_) b->jvp(L_, t_lin_, u_lin_.p, dx, df, s);
   }
   void jvp_f32(const float* dx, float* df, cudaStream_t s) {
     require_linearized();
+    if (integrals_.empty()) check_cuda(cudaMemsetAsync(df, 0, sizeof(float) * size_t(L_.num_dofs), s), "memset");
     for (size_t i = 0; i < integrals_.size(); i++) {
       integrals_[i]->jvp_f32(L_, dx, L_.evector_f32, s);
       check(sfx_scatter_add_f32(form_.get(), L_.evector_f32, df, i > 0, s));
     }
+    for (auto& b : boundary_) b->jvp_f32(L_, t_lin_, u_lin32_.p, dx, df, s);
   }
   void diagonal(double* diag, cudaStream_t s) {
     require_linearized();
+    if (integrals_.empty()) check_cuda(cudaMemsetAsync(diag, 0, sizeof(double) * size_t(L_.num_dofs), s), "memset");
     for (size_t i = 0; i < integrals_.size(); i++) {
       integrals_[i]->diagonal(L_, L_.evector, s);
       check(sfx_scatter_add(form_.get(), L_.evector, diag, i > 0, s));
     }
+    for (auto& b : boundary_) b->matrices(L_, t_lin_, u_lin_.p, diag, nullptr, s);
   }
 
  public:
@@ -393,6 +535,8 @@ class Functional<H1<p, c>(H1<p, c>)> {
         first = false;
       }
     }
+    if (first) check_cuda(cudaMemsetAsync(A.values->p, 0, sizeof(double) * size_t(nnz), nullptr), "memset");
+    for (auto& b : boundary_) b->matrices(L_, t_lin_, u_lin_.p, nullptr, A.values->p, nullptr);
     check_cuda(cudaDeviceSynchronize(), "assembly");
     return A;
   }
@@ -402,7 +546,9 @@ class Functional<H1<p, c>(H1<p, c>)> {
   std::shared_ptr<sfx_form_s> form_;
   sfx_form_layout L_{};
   std::vector<std::unique_ptr<detail::IntegralBase>> integrals_;
+  std::vector<std::unique_ptr<detail::BoundaryBase>> boundary_;
   DeviceArray<double> out_, df_, u_lin_;
+  DeviceArray<float> u_lin32_;
   double t_lin_ = 0.0;
   bool linearized_ = false;
   bool update_qdata_ = false;

@@ -55,6 +55,8 @@ SIGNATURES = {
     "sfx_assemble_diagonal": (_c.c_int, [_vp, _vp, _vp]),
     "sfx_residual_structured_noalloc": (_c.c_int, [_c.c_int] * 5 + [_dp, _vp, _vp, _vp, _c.c_double, _vp]),
     "sfx_form_get_layout": (_c.c_int, [_vp, _vp]),
+    "sfx_form_add_face_set": (_c.c_int, [_vp, _c.c_int, _c.POINTER(_c.c_int)]),
+    "sfx_form_get_face_layout": (_c.c_int, [_vp, _c.c_int, _vp]),
     "sfx_scatter_add": (_c.c_int, [_vp, _vp, _vp, _c.c_int, _vp]),
     "sfx_scatter_add_f32": (_c.c_int, [_vp, _vp, _vp, _c.c_int, _vp]),
     "sfx_update_qdata": (_c.c_int, [_vp, _c.c_int]),

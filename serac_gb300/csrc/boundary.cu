@@ -220,13 +220,11 @@ int assemble_boundary(sfx_form_s& f, double* values, double* diag, cudaStream_t 
 
 }  // namespace sfx_impl
 
-extern "C" int sfx_form_add_boundary_integral(sfx_form form, int bmaterial, int side_mask, const double* params) {
-  if (!form) return fail(SFX_ERR_INVALID, "null form");
-  int comps = 0, np = 0;
-  if (int rc = bmaterial_info(bmaterial, &comps, &np)) return rc;
-  if (comps != form->c) return fail(SFX_ERR_INVALID, "boundary material component count does not match the space");
+namespace sfx_impl {
+// faces of the sides in side_mask: connectivity (outward (s, t) order), vertex
+// coordinates, compact face-node map, geometric factors, face scratch
+int build_faces(sfx_form_s* form, int side_mask, BoundaryIntegral& bi) {
   if (side_mask <= 0 || side_mask >= 64) return fail(SFX_ERR_INVALID, "side mask must select sides 1..6");
-  if (!params) return fail(SFX_ERR_INVALID, "null parameters");
   const auto& m = form->mesh;
   const int p = form->p, n = p + 1, npf = n * n;
   const int64_t dims[3] = {m.nx, m.ny, m.nz};
@@ -258,9 +256,6 @@ extern "C" int sfx_form_add_boundary_integral(sfx_form form, int bmaterial, int 
           }
       }
   }
-  BoundaryIntegral bi;
-  bi.material = bmaterial;
-  bi.params.assign(params, params + np);
   bi.num_faces = int64_t(fconn.size()) / npf;
   // compact face-node map: distinct nodes ascending, entries in face order
   std::vector<int32_t> order(fconn.size());
@@ -287,7 +282,6 @@ extern "C" int sfx_form_add_boundary_integral(sfx_form form, int bmaterial, int 
       (err = bi.Xf.upload(Xf.data(), Xf.size())) != cudaSuccess ||
       (err = bi.fgeom.alloc(size_t(nqt) * kernels::FGEOM_STRIDE)) != cudaSuccess)
     return fail(SFX_ERR_CUDA, std::string("boundary setup: ") + cudaGetErrorString(err));
-  (void)nqt;
   if (int rc = compute_face_geometry(*form, bi, nullptr)) return rc;
   if ((err = cudaDeviceSynchronize()) != cudaSuccess)
     return fail(SFX_ERR_CUDA, std::string("face geometry: ") + cudaGetErrorString(err));
@@ -296,6 +290,47 @@ extern "C" int sfx_form_add_boundary_integral(sfx_form form, int bmaterial, int 
     if (form->ef64.alloc(escr) != cudaSuccess || form->ef32.alloc(escr) != cudaSuccess)
       return fail(SFX_ERR_NOMEM, "face scratch allocation");
   }
+  return SFX_OK;
+}
+}  // namespace sfx_impl
+
+extern "C" int sfx_form_add_boundary_integral(sfx_form form, int bmaterial, int side_mask, const double* params) {
+  if (!form) return fail(SFX_ERR_INVALID, "null form");
+  int comps = 0, np = 0;
+  if (int rc = bmaterial_info(bmaterial, &comps, &np)) return rc;
+  if (comps != form->c) return fail(SFX_ERR_INVALID, "boundary material component count does not match the space");
+  if (!params) return fail(SFX_ERR_INVALID, "null parameters");
+  BoundaryIntegral bi;
+  bi.material = bmaterial;
+  bi.params.assign(params, params + np);
+  if (int rc = build_faces(form, side_mask, bi)) return rc;
   form->boundary.push_back(std::move(bi));
+  return SFX_OK;
+}
+
+extern "C" int sfx_form_add_face_set(sfx_form form, int side_mask, int* face_set) {
+  if (!form || !face_set) return fail(SFX_ERR_INVALID, "null argument");
+  BoundaryIntegral bi;
+  bi.material = -1;  // evaluated by the caller's kernels
+  if (int rc = build_faces(form, side_mask, bi)) return rc;
+  form->face_sets.push_back(std::move(bi));
+  *face_set = int(form->face_sets.size()) - 1;
+  return SFX_OK;
+}
+
+extern "C" int sfx_form_get_face_layout(sfx_form form, int face_set, sfx_face_layout* out) {
+  if (!form || !out) return fail(SFX_ERR_INVALID, "null argument");
+  if (face_set < 0 || size_t(face_set) >= form->face_sets.size()) return fail(SFX_ERR_INVALID, "no such face set");
+  const BoundaryIntegral& bi = form->face_sets[size_t(face_set)];
+  sfx_face_layout L{};
+  L.num_faces = bi.num_faces;
+  L.nodes_per_face = (form->p + 1) * (form->p + 1);
+  L.fconn = bi.fconn.p;
+  L.fgeom = bi.fgeom.p;
+  L.num_face_nodes = bi.num_face_nodes;
+  L.node_ptr = bi.node_ptr.p;
+  L.node_ids = bi.node_ids.p;
+  L.node_ent = bi.node_ent.p;
+  *out = L;
   return SFX_OK;
 }

@@ -83,6 +83,8 @@ int compute_geometry(sfx_form_s& f, cudaStream_t s) {
   }
   for (auto& bi : f.boundary)
     if (int rc = compute_face_geometry(f, bi, s)) return rc;
+  for (auto& bi : f.face_sets)
+    if (int rc = compute_face_geometry(f, bi, s)) return rc;
   SFX_CUDA_TRY(cudaGetLastError());
   return SFX_OK;
 }

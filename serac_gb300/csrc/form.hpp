@@ -144,6 +144,7 @@ struct sfx_form_s {
   int jvp_mode = SFX_JVP_STORED_TANGENT;
   std::vector<sfx_impl::DomainIntegral> domain;
   std::vector<sfx_impl::BoundaryIntegral> boundary;
+  std::vector<sfx_impl::BoundaryIntegral> face_sets;  // faces for integrals evaluated by the caller's kernels
   // CSR graph (built on first request)
   bool csr_built = false;
   int64_t nnz = 0;

@@ -46,6 +46,26 @@ struct UserNeoHookean {
   }
 };
 
+// user boundary q-functions: a follower pressure along the deformed normal per
+// unit reference area, and a heat flux with a Robin term
+struct UserPressure {
+  double p;
+  template <typename X, typename D>
+  SFX_HD auto operator()(double, const X& position, const D& displacement) const {
+    using namespace sfx;
+    auto n = cross(get<1>(position) + get<1>(displacement));
+    return p * (n / norm(cross(get<1>(position))));
+  }
+};
+struct UserFlux {
+  double q0, q1, alpha;
+  template <typename X, typename T>
+  SFX_HD auto operator()(double, const X& position, const T& temperature) const {
+    using namespace sfx;
+    return -1.0 * (alpha * get<0>(temperature) + (q0 + q1 * get<0>(position)[0]));
+  }
+};
+
 using J2 = sfx::solid_mechanics::J2SmallStrain<sfx::solid_mechanics::LinearHardening>;
 
 template <typename F>
@@ -133,6 +153,33 @@ extern "C" int frontend_neohookean(int p, double K, double G, int nx, int ny, in
     return run<sfx::Functional<sfx::H1<1, 3>(sfx::H1<1, 3>)>>(nx, ny, nz, V, u, du, r, r2, jv, jv32, diag, csr, nnz,
                                                               setup);
   return run<sfx::Functional<sfx::H1<2, 3>(sfx::H1<2, 3>)>>(nx, ny, nz, V, u, du, r, r2, jv, jv32, diag, csr, nnz,
+                                                            setup);
+}
+
+// Neo-Hookean with a user follower-pressure boundary integral on sides in side_mask
+extern "C" int frontend_neohookean_pressure(double K, double G, double pressure, int side_mask, int nx, int ny, int nz,
+                                            const double* V, const double* u, const double* du, double* r, double* r2,
+                                            double* jv, double* jv32, double* diag, double* csr, int64_t* nnz) {
+  auto setup = [=](auto& f) {
+    f.AddDomainIntegral(sfx::Dimension<3>{}, sfx::DependsOn<0>{}, UserNeoHookean{K, G});
+    f.AddBoundaryIntegral(sfx::Dimension<2>{}, sfx::DependsOn<0>{}, UserPressure{pressure}, side_mask);
+  };
+  return run<sfx::Functional<sfx::H1<2, 3>(sfx::H1<2, 3>)>>(nx, ny, nz, V, u, du, r, r2, jv, jv32, diag, csr, nnz,
+                                                            setup);
+}
+
+// the thermal model with a user heat-flux boundary integral
+extern "C" int frontend_thermal_flux(int p, double q0, double q1, double alpha, int side_mask, int nx, int ny, int nz,
+                                     const double* V, const double* u, const double* du, double* r, double* r2,
+                                     double* jv, double* jv32, double* diag, double* csr, int64_t* nnz) {
+  auto setup = [=](auto& f) {
+    f.AddDomainIntegral(sfx::Dimension<3>{}, sfx::DependsOn<0>{}, UserThermal{});
+    f.AddBoundaryIntegral(sfx::Dimension<2>{}, sfx::DependsOn<0>{}, UserFlux{q0, q1, alpha}, side_mask);
+  };
+  if (p == 1)
+    return run<sfx::Functional<sfx::H1<1, 1>(sfx::H1<1, 1>)>>(nx, ny, nz, V, u, du, r, r2, jv, jv32, diag, csr, nnz,
+                                                              setup);
+  return run<sfx::Functional<sfx::H1<2, 1>(sfx::H1<2, 1>)>>(nx, ny, nz, V, u, du, r, r2, jv, jv32, diag, csr, nnz,
                                                             setup);
 }
 

@@ -75,6 +75,62 @@ def test_user_qfunction_matches_oracle(cuda, felib, kind, p):
     assert rel(csr, A.data) <= 1e-12
 
 
+def _check_all(orc, u, du, outs, csr, nnz, A):
+    r, r2, jv, jv32, diag = outs
+    ref_r = orc.residual(u)
+    assert rel(r, ref_r) <= 1e-12
+    assert rel(r2, ref_r) <= 1e-12
+    ref_jv = orc.jvp(u, du)
+    assert rel(jv, ref_jv) <= 1e-12
+    assert rel(jv32, ref_jv) <= 1e-5
+    assert rel(diag, A.diagonal()) <= 1e-12
+    assert nnz.value == A.nnz
+    assert rel(csr, A.data) <= 1e-12
+
+
+def test_user_boundary_qfunction_pressure(cuda, felib):
+    """A user follower-pressure boundary q-function (AddBoundaryIntegral) on
+    two sides, with a user Neo-Hookean domain integral, against the oracle's
+    built-in pressure boundary integral (serac's boundary kernels)."""
+    dims = (3, 2, 2)
+    m = mesh(*dims, perturb=0.1, seed=2)
+    orc = O.OracleFunctional(m, 2, 3)
+    orc.add_domain_integral(O.MAT_NEOHOOKEAN, PARAMS[O.MAT_NEOHOOKEAN])
+    orc.add_boundary_integral(O.BMAT_PRESSURE, [3, 6], [0.7])
+    u, du = fields(orc.ndofs, O.MAT_NEOHOOKEAN, seed=8)
+    outs = [np.zeros(orc.ndofs) for _ in range(5)]
+    A = orc.assemble(u)
+    csr = np.zeros(A.nnz)
+    nnz = ctypes.c_int64()
+    V = np.ascontiguousarray(m.vertices)
+    K, G = PARAMS[O.MAT_NEOHOOKEAN]
+    mask = (1 << 2) | (1 << 5)
+    rc = felib.frontend_neohookean_pressure(ctypes.c_double(K), ctypes.c_double(G), ctypes.c_double(0.7), mask, *dims,
+                                            _p(V), _p(u), _p(du), *[_p(o) for o in outs], _p(csr), ctypes.byref(nnz))
+    assert rc == 0
+    _check_all(orc, u, du, outs, csr, nnz, A)
+
+
+@pytest.mark.parametrize("p", [1, 2])
+def test_user_boundary_qfunction_heat_flux(cuda, felib, p):
+    dims = (3, 2, 2)
+    m = mesh(*dims, perturb=0.1, seed=3)
+    orc = O.OracleFunctional(m, p, 1)
+    orc.add_domain_integral(O.MAT_THERMAL_TEST, PARAMS[O.MAT_THERMAL_TEST])
+    orc.add_boundary_integral(O.BMAT_HEAT_FLUX, [1, 4, 5], [0.3, 0.7, 1.1])
+    u, du = fields(orc.ndofs, O.MAT_THERMAL_TEST, seed=9)
+    outs = [np.zeros(orc.ndofs) for _ in range(5)]
+    A = orc.assemble(u)
+    csr = np.zeros(A.nnz)
+    nnz = ctypes.c_int64()
+    V = np.ascontiguousarray(m.vertices)
+    mask = (1 << 0) | (1 << 3) | (1 << 4)
+    rc = felib.frontend_thermal_flux(p, ctypes.c_double(0.3), ctypes.c_double(0.7), ctypes.c_double(1.1), mask, *dims,
+                                     _p(V), _p(u), _p(du), *[_p(o) for o in outs], _p(csr), ctypes.byref(nnz))
+    assert rc == 0
+    _check_all(orc, u, du, outs, csr, nnz, A)
+
+
 def test_shape_aware_user_qfunction_matches_oracle(cuda, felib):
     """sfx::ShapeAwareFunctional with a user Neo-Hookean q-function on a
     non-trilinear order-2 shape displacement."""
