@@ -294,6 +294,15 @@ def run_sfx(args, rank, world):
     t_recompute32 = timed(lambda: grad.mult(du32, dr32), args.steps)
     f.set_jvp_mode(f.STORED_TANGENT)
     f.linearize(0.0, u)
+    # ---- adjoint-side operators: transposed action from the same stored tangent,
+    # and the stored-energy quantity of interest (value and gradient dQ/du)
+    t_jt = timed(lambda: grad.mult_transpose(du, dr), args.steps)
+    t_jt32 = timed(lambda: grad.mult_transpose(du32, dr32), args.steps)
+    qoi = sg.QoI(mesh, sg.H1(ORDER, 3))
+    qoi.AddDomainIntegral(sg.QOI_NEOHOOKEAN_ENERGY, [K_BULK, G_SHEAR])
+    q_val = torch.empty(1, dtype=torch.float64, device=dev)
+    t_qv = timed(lambda: qoi.value(0.0, u, q_val), args.steps)
+    t_qg = timed(lambda: qoi.gradient(0.0, u, r_buf), args.steps)
 
     # ---- end to end through the C ABI with host buffers
     h_du = torch.from_numpy(np.random.default_rng(0).standard_normal(ndofs)).pin_memory()
@@ -389,6 +398,11 @@ def run_sfx(args, rank, world):
         "jv_recompute": {"value_f64": ndofs * args.steps / sum(t_recompute) / 1e9,
                          "value_f32": ndofs * args.steps / sum(t_recompute32) / 1e9, "unit": UNIT,
                          "note": "q-function re-evaluated on dual numbers in every action; no stored tangent"},
+        "adjoint": {"jv_transpose_f64": ndofs * args.steps / sum(t_jt) / 1e9,
+                    "jv_transpose_f32": ndofs * args.steps / sum(t_jt32) / 1e9, "unit": UNIT,
+                    "qoi_energy_value_ms": statistics.mean(t_qv) * 1e3,
+                    "qoi_energy_gradient_ms": statistics.mean(t_qg) * 1e3,
+                    "note": "J^T v from the stored tangent (adjoint solves); Neo-Hookean stored-energy QoI"},
         "gpu_launches": 2 * args.steps,
         "clocks": clk,
         "finite": ok,

@@ -21,6 +21,11 @@
  *   sfx_linearize                   numerics/functional/functional.hpp:481-489 operator()(t, differentiate_wrt(u))
  *   sfx_jvp / sfx_jvp_f32           numerics/functional/functional.hpp:556-566 Gradient::Mult / operator()
  *   sfx_jvp_element(_f32)           numerics/functional/integral.hpp:93-103 Integral::GradientMult
+ *   sfx_jvp_transpose(_f32)         physics/solid_mechanics.hpp:1343-1501 (the adjoint solves' transposed
+ *                                   Jacobian, formed there as the transpose of assemble(Gradient&))
+ *   sfx_qoi_*                       numerics/functional/functional_qoi.inl:58-528 Functional<double(trials...)>:
+ *                                   AddDomainIntegral :159-189, AddBoundaryIntegral :201-228, operator() :379-392,
+ *                                   Gradient::operator() :420, Gradient::assemble :422-475
  *   sfx_csr_* / sfx_assemble_csr    numerics/functional/functional.hpp:569-667 assemble(Gradient&)
  *   sfx_update_qdata                numerics/functional/functional.hpp:523 updateQdata(bool)
  *   sfx_set_qdata / sfx_get_qdata   numerics/functional/quadrature_data.hpp:111-144 QuadratureData<T>
@@ -145,6 +150,15 @@ int sfx_jvp_element(sfx_form form, const double* du, double* dE, void* stream);
 /* The same in FP32 on the FP32 stored tangent (dE: num_elements * c * (p+1)^3 floats). */
 int sfx_jvp_element_f32(sfx_form form, const float* du, float* dE, void* stream);
 
+/* dr = dR/du(t_lin, u_lin)^T v: the transposed Jacobian action for adjoint
+ * problems (serac assembles the Jacobian and transposes it,
+ * solid_mechanics.hpp:1343-1501), matrix-free: the domain part applies the
+ * stored tangent transposed (needs SFX_JVP_STORED_TANGENT), boundary
+ * integrals re-linearise their q-functions per face point.  FP64, and FP32
+ * on the FP32 tangent. */
+int sfx_jvp_transpose(sfx_form form, const double* v, double* dr, void* stream);
+int sfx_jvp_transpose_f32(sfx_form form, const float* v, float* dr, void* stream);
+
 /* Self-test of the device-side bounded waits (the mbarrier waits of the
  * bulk-copy kernels): one block waits, for at most `polls` polls, on a barrier
  * that nothing completes; returns SFX_ERR_TIMEOUT when the bound worked, as it
@@ -227,6 +241,38 @@ int sfx_scatter_add_f32(sfx_form form, const float* E, float* out, int accumulat
  * caller.  Results equal sfx_residual's for the same mesh and material. */
 int sfx_residual_structured_noalloc(int nx, int ny, int nz, int order, int material, const double* params,
                                     const double* vertices, const double* u, double* r, double t, void* stream);
+
+/* Quantities of interest: Functional<double(H1<order, components>)>
+ * (functional_qoi.inl:58-528).  A QoI form integrates scalar integrands over
+ * the domain and / or box sides; its value, its directional derivative and
+ * its gradient dQ/du are device results.  Integrand kinds (parameters, host,
+ * in this order; q is integrated with det(J) w on the domain and
+ * |dX/ds x dX/dt| w on faces):
+ *   SFX_QOI_MEASURE            {}        1: volume / area
+ *   SFX_QOI_POSITION           {a[3]}    a . X
+ *   SFX_QOI_FIELD              {w[c]}    w . u
+ *   SFX_QOI_NEOHOOKEAN_ENERGY  {K, G}    stored energy of SFX_MAT_NEOHOOKEAN (domain, c = 3);
+ *                                        its gradient is that material's residual
+ *   SFX_QOI_NORMAL_FIELD       {}        u . n, n the outward unit normal (faces, c = 3)
+ *   SFX_QOI_POLY_TEST          {}        nonlinear test integrand (sfx/qoi.cuh)
+ * A QoI form is created by sfx_qoi_create (destroyed by sfx_form_destroy) and
+ * takes sfx_form_set_shape_displacement; the residual entry points reject it. */
+#define SFX_QOI_MEASURE 0
+#define SFX_QOI_POSITION 1
+#define SFX_QOI_FIELD 2
+#define SFX_QOI_NEOHOOKEAN_ENERGY 3
+#define SFX_QOI_NORMAL_FIELD 4
+#define SFX_QOI_POLY_TEST 5
+int sfx_qoi_create(sfx_mesh mesh, int order, int components, sfx_form* out);
+int sfx_qoi_add_domain_integral(sfx_form qoi, int kind, const double* params);
+int sfx_qoi_add_boundary_integral(sfx_form qoi, int kind, int side_mask, const double* params);
+/* value: device, one double = Q(t, u) */
+int sfx_qoi_evaluate(sfx_form qoi, double t, const double* u, double* value, void* stream);
+/* grad: device, num_dofs doubles = dQ/du (t, u); value (device, one double)
+ * receives Q(t, u) unless NULL */
+int sfx_qoi_gradient(sfx_form qoi, double t, const double* u, double* value, double* grad, void* stream);
+/* out: device, one double = dQ/du (t, u) du */
+int sfx_qoi_action(sfx_form qoi, double t, const double* u, const double* du, double* out, void* stream);
 
 /* Quadrature-point state (J2: 10 doubles per point: plastic strain 3x3
  * row-major, accumulated plastic strain), host arrays

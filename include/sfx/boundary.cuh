@@ -143,6 +143,109 @@ __global__ void __launch_bounds__(128) face_kernel(FaceArgs<Real> a, QF qf) {
   }
 }
 
+/// Transpose of face_interpolate applied to (value, d/ds, d/dt) data at the
+/// points: r(node) = sum over points of B s + G_s fs + G_t ft, for this lane's
+/// node.
+template <int Q, typename Real>
+SFX_HDI Real face_integrate_full(Real s, Real fs, Real ft, int base, int ix, int iy, const Real (*B)[Q],
+                                 const Real (*G)[Q]) {
+  Real a = 0, b = 0;
+#pragma unroll
+  for (int k = 0; k < Q; k++) {
+    const int src = base + k + Q * iy;
+    a += B[k][ix] * shfl(s, src) + G[k][ix] * shfl(fs, src);
+    b += B[k][ix] * shfl(ft, src);
+  }
+  Real r = 0;
+#pragma unroll
+  for (int k = 0; k < Q; k++) {
+    const int src = base + ix + Q * k;
+    r += B[k][iy] * shfl(a, src) + G[k][iy] * shfl(b, src);
+  }
+  return r;
+}
+
+/// Transposed Jacobian action of a boundary integral, dr = J^T v at the
+/// linearisation point a.u (a.du holds v).  Per point, the derivative of the
+/// q-function output (times the area weight) with respect to each trial
+/// component's value and surface derivatives is formed by directional duals
+/// (as in face_matrix_kernel); its transpose is applied to v at the point and
+/// integrated against the face basis and its surface derivatives.
+template <int P, int C, typename Real, typename QF>
+__global__ void __launch_bounds__(128) face_jvp_transpose_kernel(FaceArgs<Real> a, QF qf) {
+  constexpr int Q = P + 1;
+  constexpr int NQ = Q * Q;
+  constexpr int FPW = 32 / NQ;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int sub = lane / NQ;
+  const int qi_raw = lane - sub * NQ;
+  const bool slot = sub < FPW;
+  const int qi = slot ? qi_raw : NQ - 1;
+  const int base = slot ? sub * NQ : 0;
+  const int64_t f = warp * FPW + (slot ? sub : 0);
+  const bool valid = slot && f < a.num_faces;
+  const int ix = qi % Q, iy = qi / Q;
+
+  __shared__ Real sB[Q][Q], sG[Q][Q];
+  if (threadIdx.x < Q * Q) {
+    int i = threadIdx.x / Q, j = threadIdx.x % Q;
+    sB[i][j] = Real(basis_table<P>().B[i][j]);
+    sG[i][j] = Real(basis_table<P>().G[i][j]);
+  }
+  __syncthreads();
+  const int64_t nq_total = a.num_faces * NQ;
+  const int64_t gq = f * NQ + qi;
+  const int32_t node = valid ? a.fconn[f * NQ + qi] : 0;
+
+  Real uv[C], ugs[C], ugt[C], vq[C];
+#pragma unroll
+  for (int c = 0; c < C; c++) {
+    const Real U = valid ? a.u[c * a.num_nodes + node] : Real(0);
+    face_interpolate<Q, Real>(U, base, ix, iy, sB, sG, uv[c], ugs[c], ugt[c]);
+    const Real V = valid ? a.du[c * a.num_nodes + node] : Real(0);
+    Real vs, vt;
+    face_interpolate<Q, Real>(V, base, ix, iy, sB, sG, vq[c], vs, vt);
+  }
+  tensor<double, 3> X{};
+  tensor<double, 3, 2> J{};
+  Real scale = 0;
+  if (valid) {
+    const double* g = a.fgeom + gq;
+#pragma unroll
+    for (int k = 0; k < 3; k++) X[k] = g[k * nq_total];
+#pragma unroll
+    for (int k = 0; k < 6; k++) J[k / 2][k % 2] = g[(3 + k) * nq_total];
+    scale = Real(g[9 * nq_total]);
+  }
+  using S = dual<Real, Real>;
+#pragma unroll 1
+  for (int cj = 0; cj < C; cj++) {
+    Real w[3];  // sum over ci of v_ci d(out_ci)/d(value, d/ds, d/dt of component cj)
+#pragma unroll
+    for (int b = 0; b < 3; b++) {
+      fvalue_t<C, S> qv{};
+      fgrad_t<C, S> qg{};
+#pragma unroll
+      for (int c = 0; c < C; c++) {
+        comp<C>(qv, c) = S{uv[c], Real(c == cj && b == 0)};
+        comp<C>(qg, c)[0] = S{ugs[c], Real(c == cj && b == 1)};
+        comp<C>(qg, c)[1] = S{ugt[c], Real(c == cj && b == 2)};
+      }
+      auto out = qf(a.t, tuple{X, J}, tuple{qv, qg});
+      using OutT = std::decay_t<decltype(out)>;
+      Real acc = 0;
+#pragma unroll
+      for (int ci = 0; ci < C; ci++) {
+        if constexpr (has_part<JVP, OutT>()) acc += part<JVP, Real>(source_comp<C>(out, ci)) * vq[ci];
+      }
+      w[b] = scale * acc;
+    }
+    const Real r = face_integrate_full<Q, Real>(w[0], w[1], w[2], base, ix, iy, sB, sG);
+    if (valid) a.out_e[(f * C + cj) * NQ + qi] = r;
+  }
+}
+
 /// Derivative of a shape-aware boundary integral with respect to the shape
 /// displacement, applied to dp (serac's ShapeAwareBoundaryIntegrandWrapper,
 /// shape_aware_functional.hpp:475-498, differentiated with respect to the

@@ -37,6 +37,7 @@
 #include "sfx.h"
 #include "sfx/boundary.cuh"
 #include "sfx/kernels.cuh"
+#include "sfx/qoi.cuh"
 
 namespace sfx {
 
@@ -164,6 +165,8 @@ struct IntegralBase {
   virtual void linearize(const sfx_form_layout& L, double t, const double* u, double* E, cudaStream_t s) = 0;
   virtual void jvp(const sfx_form_layout& L, const double* du, double* E, cudaStream_t s) = 0;
   virtual void jvp_f32(const sfx_form_layout& L, const float* du, float* E, cudaStream_t s) = 0;
+  virtual void jvp_transpose(const sfx_form_layout& L, const double* v, double* E, cudaStream_t s) = 0;
+  virtual void jvp_transpose_f32(const sfx_form_layout& L, const float* v, float* E, cudaStream_t s) = 0;
   virtual void diagonal(const sfx_form_layout& L, double* E, cudaStream_t s) = 0;
   virtual void element_matrices(const sfx_form_layout& L, double t, const double* u, double* K, int64_t e0,
                                 int64_t e1, cudaStream_t s) = 0;
@@ -216,6 +219,16 @@ struct DomainIntegral : IntegralBase {
     kernels::jvp_stored_kernel<P, C, HS, true, float>
         <<<warp_blocks(L.num_elements, EPW), 128, 0, s>>>(du, D32.p, L.conn, E, L.num_nodes, L.num_elements);
     check_cuda(cudaGetLastError(), "jvp kernel (FP32)");
+  }
+  void jvp_transpose(const sfx_form_layout& L, const double* v, double* E, cudaStream_t s) override {
+    kernels::jvp_stored_transpose_kernel<P, C, HS, true, double>
+        <<<warp_blocks(L.num_elements, EPW), 128, 0, s>>>(v, D64.p, L.conn, E, L.num_nodes, L.num_elements);
+    check_cuda(cudaGetLastError(), "transposed jvp kernel");
+  }
+  void jvp_transpose_f32(const sfx_form_layout& L, const float* v, float* E, cudaStream_t s) override {
+    kernels::jvp_stored_transpose_kernel<P, C, HS, true, float>
+        <<<warp_blocks(L.num_elements, EPW), 128, 0, s>>>(v, D32.p, L.conn, E, L.num_nodes, L.num_elements);
+    check_cuda(cudaGetLastError(), "transposed jvp kernel (FP32)");
   }
   void diagonal(const sfx_form_layout& L, double* E, cudaStream_t s) override {
     kernels::diag_from_tangent_kernel<P, C, HS, true>
@@ -287,6 +300,23 @@ struct BoundaryIntegral {
         e, F.node_ptr, F.node_ids, F.node_ent, out, F.num_face_nodes, L.num_nodes);
     check_cuda(cudaGetLastError(), "boundary jvp kernel");
   }
+  // out += dR_boundary/du(t, u)^T v (FP64 or FP32 throughout)
+  template <typename Real>
+  void jvp_transpose(const sfx_form_layout& L, double t, const Real* u, const Real* v, Real* out, cudaStream_t s) {
+    if (F.num_faces == 0) return;
+    Real* e;
+    if constexpr (std::is_same<Real, double>::value) {
+      E.resize(size_t(F.num_faces) * C * NQ);
+      e = E.p;
+    } else {
+      E32.resize(size_t(F.num_faces) * C * NQ);
+      e = E32.p;
+    }
+    kernels::face_jvp_transpose_kernel<P, C, Real, QF><<<blocks(), 128, 0, s>>>(args(L, u, v, e, t), qf);
+    kernels::face_scatter_kernel<C, NQ, Real><<<scatter_blocks(), 256, 0, s>>>(
+        e, F.node_ptr, F.node_ids, F.node_ent, out, F.num_face_nodes, L.num_nodes);
+    check_cuda(cudaGetLastError(), "boundary transposed jvp kernel");
+  }
   // face element matrices at (t, u), then += into the diagonal and / or the CSR values
   void matrices(const sfx_form_layout& L, double t, const double* u, double* diag, double* values, cudaStream_t s) {
     if (F.num_faces == 0) return;
@@ -316,6 +346,10 @@ struct BoundaryBase {
                    cudaStream_t s) = 0;
   virtual void jvp_f32(const sfx_form_layout& L, double t, const float* u, const float* du, float* out,
                        cudaStream_t s) = 0;
+  virtual void jvp_transpose(const sfx_form_layout& L, double t, const double* u, const double* v, double* out,
+                             cudaStream_t s) = 0;
+  virtual void jvp_transpose_f32(const sfx_form_layout& L, double t, const float* u, const float* v, float* out,
+                                 cudaStream_t s) = 0;
   virtual void matrices(const sfx_form_layout& L, double t, const double* u, double* diag, double* values,
                         cudaStream_t s) = 0;
 };
@@ -332,6 +366,14 @@ struct BoundaryHolder : BoundaryBase {
   void jvp_f32(const sfx_form_layout& L, double t, const float* u, const float* du, float* out,
                cudaStream_t s) override {
     b.template jvp<float>(L, t, u, du, out, s);
+  }
+  void jvp_transpose(const sfx_form_layout& L, double t, const double* u, const double* v, double* out,
+                     cudaStream_t s) override {
+    b.template jvp_transpose<double>(L, t, u, v, out, s);
+  }
+  void jvp_transpose_f32(const sfx_form_layout& L, double t, const float* u, const float* v, float* out,
+                         cudaStream_t s) override {
+    b.template jvp_transpose<float>(L, t, u, v, out, s);
   }
   void matrices(const sfx_form_layout& L, double t, const double* u, double* diag, double* values,
                 cudaStream_t s) override {
@@ -356,6 +398,12 @@ class Functional<H1<p, c>(H1<p, c>)> {
     void Mult(const double* dx, double* df, cudaStream_t s = nullptr) const { f_->jvp(dx, df, s); }
     /// FP32 action on the FP32 copy of the stored tangent
     void MultF32(const float* dx, float* df, cudaStream_t s = nullptr) const { f_->jvp_f32(dx, df, s); }
+    /// df = dR/du^T v (mfem::Operator::MultTranspose), the adjoint action, from
+    /// the stored tangent transposed; FP32 on the FP32 copy
+    void MultTranspose(const double* v, double* df, cudaStream_t s = nullptr) const { f_->jvp_transpose(v, df, s); }
+    void MultTransposeF32(const float* v, float* df, cudaStream_t s = nullptr) const {
+      f_->jvp_transpose_f32(v, df, s);
+    }
     /// returns a member buffer overwritten by the next call (functional.hpp:562-566)
     const double* operator()(const double* dx) {
       Mult(dx, f_->df_.p);
@@ -491,6 +539,24 @@ class Functional<H1<p, c>(H1<p, c>)> {
     }
     for (auto& b : boundary_) b->jvp_f32(L_, t_lin_, u_lin32_.p, dx, df, s);
   }
+  void jvp_transpose(const double* v, double* df, cudaStream_t s) {
+    require_linearized();
+    if (integrals_.empty()) check_cuda(cudaMemsetAsync(df, 0, sizeof(double) * size_t(L_.num_dofs), s), "memset");
+    for (size_t i = 0; i < integrals_.size(); i++) {
+      integrals_[i]->jvp_transpose(L_, v, L_.evector, s);
+      check(sfx_scatter_add(form_.get(), L_.evector, df, i > 0, s));
+    }
+    for (auto& b : boundary_) b->jvp_transpose(L_, t_lin_, u_lin_.p, v, df, s);
+  }
+  void jvp_transpose_f32(const float* v, float* df, cudaStream_t s) {
+    require_linearized();
+    if (integrals_.empty()) check_cuda(cudaMemsetAsync(df, 0, sizeof(float) * size_t(L_.num_dofs), s), "memset");
+    for (size_t i = 0; i < integrals_.size(); i++) {
+      integrals_[i]->jvp_transpose_f32(L_, v, L_.evector_f32, s);
+      check(sfx_scatter_add_f32(form_.get(), L_.evector_f32, df, i > 0, s));
+    }
+    for (auto& b : boundary_) b->jvp_transpose_f32(L_, t_lin_, u_lin32_.p, v, df, s);
+  }
   void diagonal(double* diag, cudaStream_t s) {
     require_linearized();
     if (integrals_.empty()) check_cuda(cudaMemsetAsync(diag, 0, sizeof(double) * size_t(L_.num_dofs), s), "memset");
@@ -552,6 +618,201 @@ class Functional<H1<p, c>(H1<p, c>)> {
   double t_lin_ = 0.0;
   bool linearized_ = false;
   bool update_qdata_ = false;
+  Gradient grad_;
+};
+
+namespace detail {
+
+// one integral of a quantity of interest: per-element / per-face values and,
+// for QOI_GRADIENT, dQ/du added into grad
+struct QoiBase {
+  virtual ~QoiBase() = default;
+  virtual int64_t count(const sfx_form_layout& L) const = 0;
+  virtual void run(int mode, const sfx_form_layout& L, sfx_form form, double t, const double* u, const double* du,
+                   double* vals, double* grad, cudaStream_t s) = 0;
+};
+
+template <int P, int C, typename QF>
+struct QoiDomain : QoiBase {
+  static constexpr int EPW = 32 / ((P + 1) * (P + 1) * (P + 1));
+  QF qf;
+  explicit QoiDomain(const QF& q) : qf(q) {}
+  int64_t count(const sfx_form_layout& L) const override { return L.num_elements; }
+  template <int MODE>
+  void launch(const sfx_form_layout& L, double t, const double* u, const double* du, double* vals, cudaStream_t s) {
+    kernels::DomainArgs<double> a{u, du, L.evector, L.conn, L.geom, nullptr, nullptr, L.num_nodes, L.num_elements, t};
+    kernels::qoi_domain_kernel<P, C, MODE, QF><<<warp_blocks(L.num_elements, EPW), 128, 0, s>>>(a, qf, vals);
+    check_cuda(cudaGetLastError(), "QoI kernel");
+  }
+  void run(int mode, const sfx_form_layout& L, sfx_form form, double t, const double* u, const double* du,
+           double* vals, double* grad, cudaStream_t s) override {
+    if (L.num_elements == 0) return;
+    if (mode == kernels::QOI_VALUE) launch<kernels::QOI_VALUE>(L, t, u, du, vals, s);
+    if (mode == kernels::QOI_ACTION) launch<kernels::QOI_ACTION>(L, t, u, du, vals, s);
+    if (mode == kernels::QOI_GRADIENT) {
+      launch<kernels::QOI_GRADIENT>(L, t, u, du, vals, s);
+      check(sfx_scatter_add(form, L.evector, grad, 1, s));
+    }
+  }
+};
+
+template <int P, int C, typename QF>
+struct QoiFaces : QoiBase {
+  static constexpr int NQ = (P + 1) * (P + 1);
+  static constexpr int FPW = 32 / NQ;
+  QF qf;
+  int face_set = -1;
+  sfx_face_layout F{};
+  DeviceArray<double> E;
+  explicit QoiFaces(const QF& q) : qf(q) {}
+  int64_t count(const sfx_form_layout&) const override { return F.num_faces; }
+  template <int MODE>
+  void launch(const sfx_form_layout& L, double t, const double* u, const double* du, double* vals, cudaStream_t s) {
+    kernels::FaceArgs<double> a{u, du, E.p, F.fconn, F.fgeom, L.num_nodes, F.num_faces, t};
+    kernels::qoi_face_kernel<P, C, MODE, QF><<<warp_blocks(F.num_faces, FPW), 128, 0, s>>>(a, qf, vals);
+    check_cuda(cudaGetLastError(), "face QoI kernel");
+  }
+  void run(int mode, const sfx_form_layout& L, sfx_form, double t, const double* u, const double* du, double* vals,
+           double* grad, cudaStream_t s) override {
+    if (F.num_faces == 0) return;
+    E.resize(size_t(F.num_faces) * C * NQ);
+    if (mode == kernels::QOI_VALUE) launch<kernels::QOI_VALUE>(L, t, u, du, vals, s);
+    if (mode == kernels::QOI_ACTION) launch<kernels::QOI_ACTION>(L, t, u, du, vals, s);
+    if (mode == kernels::QOI_GRADIENT) {
+      launch<kernels::QOI_GRADIENT>(L, t, u, du, vals, s);
+      kernels::face_scatter_kernel<C, NQ, double><<<unsigned((F.num_face_nodes + 255) / 256), 256, 0, s>>>(
+          E.p, F.node_ptr, F.node_ids, F.node_ent, grad, F.num_face_nodes, L.num_nodes);
+      check_cuda(cudaGetLastError(), "face QoI scatter");
+    }
+  }
+};
+
+}  // namespace detail
+
+/// Functional<double(H1<p,c>)>: a quantity of interest (functional_qoi.inl:58-528)
+/// over user q-functions qf(t, tuple{X, dX/dxi}, tuple{u, du/dX}) -> scalar
+/// (domain) and qf(t, tuple{X, dX/d(s,t)}, tuple{u, du/d(s,t)}) -> scalar
+/// (box sides).  Q(t, u) = operator()(t, u); (Q, dQ/du) =
+/// operator()(t, differentiate_wrt(u)) with dQ/du(dx) the directional
+/// derivative (functional_qoi.inl:420) and assemble(dQ/du) the gradient
+/// vector (:422-475, a device buffer of the functional).  Values reduce in a
+/// fixed order (deterministic).
+template <int p, int c>
+class Functional<double(H1<p, c>)> {
+ public:
+  class Gradient {
+   public:
+    explicit Gradient(Functional* f) : f_(f) {}
+    /// dQ/du(t_lin, u_lin) dx (synchronises to return a host value)
+    double operator()(const double* dx, cudaStream_t s = nullptr) const { return f_->action(dx, s); }
+    /// the same into a device double
+    void Action(const double* dx, double* value, cudaStream_t s = nullptr) const { f_->action_device(dx, value, s); }
+    /// dQ/du as a device vector (a member buffer overwritten by the next call)
+    const double* assemble(cudaStream_t s = nullptr) { return f_->gradient(s); }
+    friend const double* assemble(Gradient& g) { return g.assemble(); }
+
+   private:
+    Functional* f_;
+  };
+
+  explicit Functional(const Mesh& mesh) : mesh_(mesh), grad_(this) {
+    sfx_form h = nullptr;
+    check(sfx_qoi_create(mesh.handle(), p, c, &h));
+    form_ = std::shared_ptr<sfx_form_s>(h, [](sfx_form x) { sfx_form_destroy(x); });
+    check(sfx_form_get_layout(h, &L_));
+    g_.resize(size_t(L_.num_dofs));
+    u_lin_.resize(size_t(L_.num_dofs));
+    value_.resize(1);
+    partial_.resize(size_t(kernels::kQoiMaxPartials));
+  }
+
+  int64_t num_dofs() const { return L_.num_dofs; }
+
+  /// AddDomainIntegral (functional_qoi.inl:159-189)
+  template <typename QF>
+  void AddDomainIntegral(Dimension<3>, DependsOn<0>, const QF& qf) {
+    integrals_.emplace_back(new detail::QoiDomain<p, c, QF>(qf));
+  }
+  /// AddBoundaryIntegral over the box sides in side_mask (functional_qoi.inl:201-228)
+  template <typename QF>
+  void AddBoundaryIntegral(Dimension<2>, DependsOn<0>, const QF& qf, int side_mask) {
+    auto h = std::make_unique<detail::QoiFaces<p, c, QF>>(qf);
+    check(sfx_form_add_face_set(form_.get(), side_mask, &h->face_set));
+    check(sfx_form_get_face_layout(form_.get(), h->face_set, &h->F));
+    integrals_.push_back(std::move(h));
+  }
+  /// evaluate on X + shape (device, 3 * num_nodes doubles; nullptr = none)
+  void SetShapeDisplacement(const double* shape, cudaStream_t s = nullptr) {
+    check(sfx_form_set_shape_displacement(form_.get(), shape, s));
+  }
+
+  /// Q(t, u) into a device double
+  void Evaluate(double t, const double* u, double* value, cudaStream_t s = nullptr) {
+    run(kernels::QOI_VALUE, t, u, nullptr, nullptr, value, s);
+  }
+  /// Q(t, u) (synchronises)
+  double operator()(double t, const double* u, cudaStream_t s = nullptr) {
+    Evaluate(t, u, value_.p, s);
+    return read_value(s);
+  }
+  /// (Q(t, u), dQ/du at u)
+  std::tuple<double, Gradient&> operator()(double t, differentiate_wrt_this w, cudaStream_t s = nullptr) {
+    check_cuda(cudaMemcpyAsync(u_lin_.p, w.u, sizeof(double) * size_t(L_.num_dofs), cudaMemcpyDeviceToDevice, s),
+               "copy u");
+    t_lin_ = t;
+    linearized_ = true;
+    Evaluate(t, u_lin_.p, value_.p, s);
+    return {read_value(s), grad_};
+  }
+
+ private:
+  friend class Gradient;
+  void run(int mode, double t, const double* u, const double* du, double* grad, double* value, cudaStream_t s) {
+    if (integrals_.empty()) throw std::runtime_error("sfx: no integrals");
+    int64_t n = 0;
+    for (auto& in : integrals_) n += in->count(L_);
+    if (vals_.n < size_t(n)) vals_.resize(size_t(n));
+    if (grad) check_cuda(cudaMemsetAsync(grad, 0, sizeof(double) * size_t(L_.num_dofs), s), "memset");
+    int64_t at = 0;
+    for (auto& in : integrals_) {
+      in->run(mode, L_, form_.get(), t, u, du, vals_.p + at, grad, s);
+      at += in->count(L_);
+    }
+    if (value) {
+      if (n == 0) check_cuda(cudaMemsetAsync(value, 0, sizeof(double), s), "memset");
+      else check_cuda(kernels::qoi_sum(vals_.p, n, partial_.p, value, s), "QoI sum");
+    }
+  }
+  double read_value(cudaStream_t s) {
+    double v = 0.0;
+    check_cuda(cudaMemcpyAsync(&v, value_.p, sizeof(double), cudaMemcpyDeviceToHost, s), "read value");
+    check_cuda(cudaStreamSynchronize(s), "synchronise");
+    return v;
+  }
+  void require_linearized() const {
+    if (!linearized_) throw std::runtime_error("sfx: differentiate with operator()(t, differentiate_wrt(u)) first");
+  }
+  void action_device(const double* dx, double* value, cudaStream_t s) {
+    require_linearized();
+    run(kernels::QOI_ACTION, t_lin_, u_lin_.p, dx, nullptr, value, s);
+  }
+  double action(const double* dx, cudaStream_t s) {
+    action_device(dx, value_.p, s);
+    return read_value(s);
+  }
+  const double* gradient(cudaStream_t s) {
+    require_linearized();
+    run(kernels::QOI_GRADIENT, t_lin_, u_lin_.p, nullptr, g_.p, nullptr, s);
+    return g_.p;
+  }
+
+  Mesh mesh_;
+  std::shared_ptr<sfx_form_s> form_;
+  sfx_form_layout L_{};
+  std::vector<std::unique_ptr<detail::QoiBase>> integrals_;
+  DeviceArray<double> g_, u_lin_, value_, partial_, vals_;
+  double t_lin_ = 0.0;
+  bool linearized_ = false;
   Gradient grad_;
 };
 

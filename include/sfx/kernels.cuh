@@ -1170,6 +1170,75 @@ __global__ void __launch_bounds__(128) jvp_stored_kernel(const Real* __restrict_
   }
 }
 
+/// Transposed Jacobian action from the stored derivative, dr = J^T v (what
+/// serac's adjoint solves obtain by transposing the assembled matrix,
+/// solid_mechanics.hpp:1343-1501).  D holds, per point, the parent-space block
+/// d(outputs)/d(inputs) with det(J) w folded in, so J = B^T D B with B the
+/// interpolation to (value, parent gradient); J^T = B^T D^T B: v is
+/// interpolated onto the output side (values if the source depends on the
+/// field, then the gradient), D^T is applied, and the result is integrated
+/// on the input side (values if the q-function reads them, then the flux).
+template <int P, int C, bool HS, bool VI, typename Real>
+__global__ void __launch_bounds__(128) jvp_stored_transpose_kernel(const Real* __restrict__ v,
+                                                                   const Real* __restrict__ D,
+                                                                   const int32_t* __restrict__ conn,
+                                                                   Real* __restrict__ out_e, int64_t num_nodes,
+                                                                   int64_t num_elements) {
+  constexpr int Q = P + 1;
+  constexpr int NQ = Q * Q * Q;
+  constexpr int EPW = 32 / NQ;
+  using Shape = TangentShape<C, HS, VI>;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int sub = lane / NQ;
+  const int qi_raw = lane - sub * NQ;
+  const bool slot = sub < EPW;
+  const int qi = slot ? qi_raw : NQ - 1;
+  const int base = slot ? sub * NQ : 0;
+  const int64_t e = warp * EPW + (slot ? sub : 0);
+  const bool valid = slot && e < num_elements;
+  const int ix = qi % Q, iy = (qi / Q) % Q, iz = qi / (Q * Q);
+
+  __shared__ Real sB[Q][Q], sG[Q][Q];
+  if (threadIdx.x < Q * Q) {
+    int i = threadIdx.x / Q, j = threadIdx.x % Q;
+    sB[i][j] = Real(basis_table<P>().B[i][j]);
+    sG[i][j] = Real(basis_table<P>().G[i][j]);
+  }
+  __syncthreads();
+
+  const int32_t node = valid ? conn[e * NQ + qi] : 0;
+  constexpr int roff = HS ? C : 0;
+  Real vin[Shape::rows];
+#pragma unroll
+  for (int c = 0; c < C; c++) {
+    Real V = valid ? v[c * num_nodes + node] : Real(0);
+    Real val, g0, g1, g2;
+    interpolate_lane<Q, Real>(V, base, ix, iy, iz, sB, sG, val, g0, g1, g2);
+    if constexpr (HS) vin[c] = val;
+    vin[roff + 3 * c + 0] = g0;
+    vin[roff + 3 * c + 1] = g1;
+    vin[roff + 3 * c + 2] = g2;
+  }
+  Real vout[Shape::cols];
+  const Real* Dq = D + (valid ? e * Shape::template stride<NQ> + qi : 0);
+#pragma unroll
+  for (int k = 0; k < Shape::cols; k++) {
+    Real acc = 0;
+#pragma unroll
+    for (int r = 0; r < Shape::rows; r++) acc += (valid ? Dq[(r * Shape::cols + k) * NQ] : Real(0)) * vin[r];
+    vout[k] = acc;
+  }
+  constexpr int coff = VI ? C : 0;
+#pragma unroll
+  for (int c = 0; c < C; c++) {
+    Real s = VI ? vout[VI ? c : 0] : Real(0);
+    Real r = integrate_lane<Q, VI, true, Real>(s, vout[coff + 3 * c], vout[coff + 3 * c + 1], vout[coff + 3 * c + 2],
+                                               base, ix, iy, iz, sB, sG);
+    if (valid) out_e[(e * C + c) * NQ + qi] = r;
+  }
+}
+
 /// FP32 Jacobian action from the stored tangent for Q2 elements, with each
 /// element's tangent block (81 x 27 floats for the vector Neo-Hookean case,
 /// 8.7 KB, contiguous) staged into shared memory by bulk asynchronous copies

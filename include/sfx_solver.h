@@ -9,6 +9,8 @@
  *   sfx_solver_solve            equation_solver.cpp:79-200 NewtonSolver::Mult (quasiStaticSolve, solid_mechanics.hpp:1620-1630)
  *   sfx_solver_warm_start       SolidMechanics::warmStartDisplacement (solid_mechanics.hpp:1727-1770)
  *   sfx_solver_solve_linear     one linearised solve with the essential rows eliminated
+ *   sfx_solver_solve_adjoint    the adjoint solve J^T lambda = dQ/du of SolidMechanics::reverseAdjointTimestep
+ *                               (solid_mechanics.hpp:1343-1501), matrix-free (sfx_jvp_transpose)
  * The Chebyshev, flexible-GMRES and mixed-precision options have no
  * counterpart in serac (its LinearSolver enum is CG / GMRES / direct / PETSc).
  */
@@ -89,6 +91,13 @@ int sfx_solver_solve(sfx_solver solver, double t, double* u, void* stream);
  * eliminated; the essential entries of rhs are ignored and x is 0 there. */
 int sfx_solver_solve_linear(sfx_solver solver, double t, const double* u_lin, const double* rhs, double* x,
                             void* stream);
+/* x = J(t, u_lin)^-T rhs on the free vdofs (essential rows and columns
+ * eliminated, x = 0 there): the adjoint solve, with the solver's Krylov
+ * method and preconditioner applied to the transposed operator (the Jacobi
+ * diagonal is the same; the learned network is used as trained).  Needs the
+ * stored-tangent Jacobian mode. */
+int sfx_solver_solve_adjoint(sfx_solver solver, double t, const double* u_lin, const double* rhs, double* x,
+                             void* stream);
 /* Load-step predictor: with d = u_target - u on the essential vdofs (0
  * elsewhere), solve J(t, u) x = -J(t, u) d on the free rows and set
  * u += d + x, so that u carries the new essential values and a first-order

@@ -435,6 +435,10 @@ class OracleFunctional:
     def jvp(self, u, du, t=0.0):
         return self._apply(1, u, du, t=t)
 
+    def jvp_transpose(self, u, v, t=0.0):
+        """dR/du(u)^T v from the assembled matrix (pinned through assemble)."""
+        return self.assemble(u, t).T @ v
+
     def csr_graph(self):
         vd = elem_vdofs(self.conn, self.c, self.nnodes)
         rows = np.repeat(vd, vd.shape[1], axis=1).ravel()
@@ -477,6 +481,196 @@ class OracleFunctional:
             add(K, elem_vdofs(fnodes, self.c, self.nnodes))
         # the graph holds every element pair, explicit zeros included
         return sp.csr_matrix((vals, col, row_ptr), shape=(n, n))
+
+
+QOI_MEASURE, QOI_POSITION, QOI_FIELD, QOI_NEOHOOKEAN_ENERGY, QOI_NORMAL_FIELD, QOI_POLY_TEST = range(6)
+
+
+def _qoi_domain_point(kind, params, X, u, g, c):
+    """q and its hand-derived partials at domain points: X (P, 3), u (P, c),
+    g (P, c, 3) physical gradients -> q (P,), dq/du (P, c), dq/dg (P, c, 3).
+    Integrands as in the product's C ABI (functional_qoi.inl semantics: the
+    value is weighted by det(J) w)."""
+    P = X.shape[0]
+    q = np.zeros(P)
+    du = np.zeros((P, c))
+    dg = np.zeros((P, c, 3))
+    if kind == QOI_MEASURE:
+        q[:] = 1.0
+    elif kind == QOI_POSITION:
+        q = X @ np.asarray(params, dtype=np.float64)
+    elif kind == QOI_FIELD:
+        w = np.asarray(params, dtype=np.float64)
+        q = u @ w
+        du[:] = w
+    elif kind == QOI_NEOHOOKEAN_ENERGY:
+        # W = G/2 (|H|^2 + 2 tr H) - G ln J + lambda/2 (ln J)^2, dW/dH = G (F - F^-T) + lambda ln J F^-T
+        K, G = params
+        lam = K - 2.0 * G / 3.0
+        F = g + np.eye(3)
+        lnJ = np.log(np.linalg.det(F))
+        q = 0.5 * G * (np.einsum("pij,pij->p", g, g) + 2.0 * np.einsum("pii->p", g)) - G * lnJ + 0.5 * lam * lnJ ** 2
+        FinvT = np.linalg.inv(F).transpose(0, 2, 1)
+        dg = G * (F - FinvT) + (lam * lnJ)[:, None, None] * FinvT
+    elif kind == QOI_POLY_TEST:
+        # X0^2 + sin X1 + X0 s^3 + (1 + X2)/2 |g|^2, s = sum_c u_c
+        sm = u.sum(axis=1)
+        q = X[:, 0] ** 2 + np.sin(X[:, 1]) + X[:, 0] * sm ** 3 + 0.5 * (1.0 + X[:, 2]) * np.einsum("pcj,pcj->p", g, g)
+        du[:] = (3.0 * X[:, 0] * sm ** 2)[:, None]
+        dg = (1.0 + X[:, 2])[:, None, None] * g
+    else:
+        raise ValueError(f"QoI kind {kind} not available on the domain")
+    return q, du, dg
+
+
+def _qoi_face_point(kind, params, X, J, u, gs, c):
+    """q and partials at face points: X (P, 3), J (P, 3, 2) = dX/d(s, t),
+    u (P, c), gs (P, c) = du/ds -> q (P,), dq/du (P, c), dq/d(du/ds) (P, c)."""
+    P = X.shape[0]
+    q = np.zeros(P)
+    du = np.zeros((P, c))
+    dgs = np.zeros((P, c))
+    if kind == QOI_MEASURE:
+        q[:] = 1.0
+    elif kind == QOI_POSITION:
+        q = X @ np.asarray(params, dtype=np.float64)
+    elif kind == QOI_FIELD:
+        w = np.asarray(params, dtype=np.float64)
+        q = u @ w
+        du[:] = w
+    elif kind == QOI_NORMAL_FIELD:
+        n = np.cross(J[:, :, 0], J[:, :, 1])
+        n /= np.linalg.norm(n, axis=1)[:, None]
+        q = np.einsum("pi,pi->p", n, u)
+        du = n
+    elif kind == QOI_POLY_TEST:
+        # X0 - X1 + cos(s X1) + |du/ds|^2 / 4
+        sm = u.sum(axis=1)
+        q = X[:, 0] - X[:, 1] + np.cos(sm * X[:, 1]) + 0.25 * np.einsum("pc,pc->p", gs, gs)
+        du[:] = (-np.sin(sm * X[:, 1]) * X[:, 1])[:, None]
+        dgs = 0.5 * gs
+    else:
+        raise ValueError(f"QoI kind {kind} not available on faces")
+    return q, du, dgs
+
+
+def _tensor_basis(p):
+    """Volume phi[q, a] and dphi[j][q, a]; face fphi[q, a], fds, fdt (lexicographic, x / s fastest)."""
+    B, G = basis_1d(p)
+    n = p + 1
+    Kz, Ky, Kx = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    ax, ay, az = Kx.ravel(), Ky.ravel(), Kz.ravel()
+    bx, by, bz = B[ax][:, ax], B[ay][:, ay], B[az][:, az]
+    gx, gy, gz = G[ax][:, ax], G[ay][:, ay], G[az][:, az]
+    phi = bx * by * bz
+    dphi = [gx * by * bz, bx * gy * bz, bx * by * gz]
+    Tt, Ts = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    a_s, a_t = Ts.ravel(), Tt.ravel()
+    fphi = B[a_s][:, a_s] * B[a_t][:, a_t]
+    fds = G[a_s][:, a_s] * B[a_t][:, a_t]
+    fdt = B[a_s][:, a_s] * G[a_t][:, a_t]
+    return phi, dphi, fphi, fds, fdt
+
+
+def _gl_weights(Q, dim):
+    t, w = np.polynomial.legendre.leggauss(Q)
+    w = 0.5 * w
+    if dim == 3:
+        return (w[None, None, :] * w[None, :, None] * w[:, None, None]).ravel()
+    return (w[None, :] * w[:, None]).ravel()
+
+
+class OracleQoI:
+    """Functional<double(H1<p,c>)> (functional_qoi.inl:58-528) on a structured
+    hex mesh: Q(u) = sum over elements and points of q det(J) w (+ faces with
+    |dX/ds x dX/dt| w); dQ/du assembled from the integrands' hand-derived
+    partials like a residual (Gradient::assemble, :422-475)."""
+
+    def __init__(self, mesh: StructuredHexMesh, p: int, c: int, shape=None):
+        self.mesh, self.p, self.c = mesh, p, c
+        self.Q = p + 1
+        self.nnodes = mesh.num_nodes(p)
+        self.ndofs = self.nnodes * c
+        self.conn = mesh.elem_nodes(p)
+        self.Xq, self.Jq = geometric_factors(mesh.elem_coords(), self.Q)
+        self.domain = []
+        self.boundary = []
+        self._shape = None if shape is None else np.asarray(shape, dtype=np.float64)
+        if self._shape is not None:
+            self._apply_shape_domain()
+
+    def _apply_shape_domain(self):
+        phi, dphi, _, _, _ = _tensor_basis(self.p)
+        P3 = self._shape.reshape(3, self.nnodes)[:, self.conn]
+        self.Xq = self.Xq + np.einsum("iea,qa->eiq", P3, phi)
+        self.Jq = self.Jq + np.stack([np.einsum("iea,qa->eiq", P3, dphi[j]) for j in range(3)], axis=1)
+
+    def add_domain_integral(self, kind, params=None):
+        self.domain.append((kind, params))
+
+    def add_boundary_integral(self, kind, sides, params=None):
+        Xf, fnodes = self.mesh.boundary_faces(self.p, sides)
+        Xq, Jq = face_geometric_factors(Xf, self.Q)
+        if self._shape is not None:
+            _, _, fphi, fds, fdt = _tensor_basis(self.p)
+            P3 = self._shape.reshape(3, self.nnodes)[:, fnodes]
+            Xq = Xq + np.einsum("ifa,qa->fiq", P3, fphi)
+            Jq = Jq + np.stack([np.einsum("ifa,qa->fiq", P3, fds), np.einsum("ifa,qa->fiq", P3, fdt)], axis=1)
+        self.boundary.append((kind, params, fnodes, Xq, Jq))
+
+    def evaluate(self, u):
+        """(Q(u), dQ/du)."""
+        c, N, p = self.c, self.nnodes, self.p
+        phi, dphi, fphi, fds, fdt = _tensor_basis(p)
+        U = np.asarray(u, dtype=np.float64).reshape(c, N)
+        value = 0.0
+        grad = np.zeros((c, N))
+        if self.domain:
+            ne, nq = self.conn.shape[0], self.Q ** 3
+            w = _gl_weights(self.Q, 3)
+            J = self.Jq.transpose(0, 3, 2, 1)  # (e, q, i, j) = dX_i/dxi_j
+            Jinv = np.linalg.inv(J)
+            detJw = np.linalg.det(J) * w[None, :]
+            X = self.Xq.transpose(0, 2, 1)  # (e, q, 3)
+            uE = U[:, self.conn]  # (c, e, a)
+            uq = np.einsum("cea,qa->eqc", uE, phi)
+            gxi = np.stack([np.einsum("cea,qa->eqc", uE, dphi[j]) for j in range(3)], axis=-1)  # (e, q, c, j)
+            gX = np.einsum("eqcj,eqji->eqci", gxi, Jinv)
+            for kind, params in self.domain:
+                q, dqu, dqg = _qoi_domain_point(kind, params, X.reshape(-1, 3), uq.reshape(-1, c),
+                                                gX.reshape(-1, c, 3), c)
+                value += float(np.sum(q.reshape(ne, nq) * detJw))
+                src = dqu.reshape(ne, nq, c) * detJw[..., None]
+                flx = np.einsum("eqci,eqji->eqcj", dqg.reshape(ne, nq, c, 3), Jinv) * detJw[..., None, None]
+                gE = np.einsum("eqc,qa->cea", src, phi)
+                for j in range(3):
+                    gE += np.einsum("eqc,qa->cea", flx[..., j], dphi[j])
+                for k in range(c):
+                    np.add.at(grad[k], self.conn.ravel(), gE[k].ravel())
+        for kind, params, fnodes, Xq, Jq in self.boundary:
+            nf, nq = fnodes.shape[0], self.Q ** 2
+            if nf == 0:
+                continue
+            w = _gl_weights(self.Q, 2)
+            X = Xq.transpose(0, 2, 1).reshape(-1, 3)
+            Jf = Jq.transpose(0, 3, 2, 1).reshape(-1, 3, 2)
+            area = np.linalg.norm(np.cross(Jf[:, :, 0], Jf[:, :, 1]), axis=1).reshape(nf, nq) * w[None, :]
+            uF = U[:, fnodes]
+            uq = np.einsum("cfa,qa->fqc", uF, fphi).reshape(-1, c)
+            gs = np.einsum("cfa,qa->fqc", uF, fds).reshape(-1, c)
+            q, dqu, dqs = _qoi_face_point(kind, params, X, Jf, uq, gs, c)
+            value += float(np.sum(q.reshape(nf, nq) * area))
+            gF = np.einsum("fqc,qa->cfa", dqu.reshape(nf, nq, c) * area[..., None], fphi)
+            gF += np.einsum("fqc,qa->cfa", dqs.reshape(nf, nq, c) * area[..., None], fds)
+            for k in range(c):
+                np.add.at(grad[k], fnodes.ravel(), gF[k].ravel())
+        return value, grad.ravel()
+
+    def value(self, u):
+        return self.evaluate(u)[0]
+
+    def gradient(self, u):
+        return self.evaluate(u)[1]
 
 
 def eliminate_dirichlet(A, ess):

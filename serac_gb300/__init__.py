@@ -9,12 +9,20 @@ from .functional import (  # noqa: F401
     NEOHOOKEAN,
     NONLINEAR_HEAT,
     PRESSURE,
+    QOI_FIELD,
+    QOI_MEASURE,
+    QOI_NEOHOOKEAN_ENERGY,
+    QOI_NORMAL_FIELD,
+    QOI_POLY_TEST,
+    QOI_POSITION,
     THERMAL_TEST,
     TRACTION,
     H1,
     Functional,
     Gradient,
     Mesh,
+    QoI,
+    QoIGradient,
     ShapeAwareFunctional,
     assemble,
     box_vertices,

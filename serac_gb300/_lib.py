@@ -45,6 +45,14 @@ SIGNATURES = {
     "sfx_linearize": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp]),
     "sfx_form_set_jvp_mode": (_c.c_int, [_vp, _c.c_int]),
     "sfx_jvp": (_c.c_int, [_vp, _vp, _vp, _vp]),
+    "sfx_jvp_transpose": (_c.c_int, [_vp, _vp, _vp, _vp]),
+    "sfx_jvp_transpose_f32": (_c.c_int, [_vp, _vp, _vp, _vp]),
+    "sfx_qoi_create": (_c.c_int, [_vp, _c.c_int, _c.c_int, _vp]),
+    "sfx_qoi_add_domain_integral": (_c.c_int, [_vp, _c.c_int, _vp]),
+    "sfx_qoi_add_boundary_integral": (_c.c_int, [_vp, _c.c_int, _c.c_int, _vp]),
+    "sfx_qoi_evaluate": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp]),
+    "sfx_qoi_gradient": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp, _vp]),
+    "sfx_qoi_action": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp, _vp]),
     "sfx_jvp_f32": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "sfx_jvp_element": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "sfx_jvp_element_f32": (_c.c_int, [_vp, _vp, _vp, _vp]),
@@ -81,6 +89,7 @@ SIGNATURES = {
     "sfx_solver_set_essential": (_c.c_int, [_vp, _i64p, _c.c_int64]),
     "sfx_solver_solve": (_c.c_int, [_vp, _c.c_double, _vp, _vp]),
     "sfx_solver_solve_linear": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp, _vp]),
+    "sfx_solver_solve_adjoint": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp, _vp]),
     "sfx_solver_warm_start": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp]),
     "sfx_solver_get_stats": (_c.c_int, [_vp, _vp]),
     "sfx_solver_set_learned": (_c.c_int, [_vp, _vp, _c.c_int, _c.c_int, _c.c_int, _vp]),

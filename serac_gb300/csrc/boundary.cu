@@ -84,6 +84,32 @@ struct FaceFn {
   }
 };
 
+template <int P, typename Real>
+struct FaceTransposeFn {
+  const sfx_form_s& f;
+  const BoundaryIntegral& bi;
+  const Real* u;
+  const Real* v;
+  Real* out;
+  cudaStream_t s;
+  template <int C, typename QF>
+  int operator()(const QF& qf) {
+    constexpr int NQ = (P + 1) * (P + 1);
+    constexpr int FPW = 32 / NQ;
+    if (bi.num_faces == 0) return SFX_OK;
+    Real* E = std::is_same<Real, double>::value ? reinterpret_cast<Real*>(f.ef64.p) : reinterpret_cast<Real*>(f.ef32.p);
+    kernels::FaceArgs<Real> a{u, v, E, bi.fconn.p, bi.fgeom.p, f.nnodes, bi.num_faces, f.t_lin};
+    const int64_t warps = (bi.num_faces + FPW - 1) / FPW;
+    kernels::face_jvp_transpose_kernel<P, C, Real, QF><<<unsigned((warps * 32 + 127) / 128), 128, 0, s>>>(a, qf);
+    kernels::face_scatter_kernel<C, NQ, Real><<<unsigned((bi.num_face_nodes + 255) / 256), 256, 0, s>>>(
+        E, bi.node_ptr.p, bi.node_ids.p, bi.node_ent.p, out, bi.num_face_nodes, f.nnodes);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess)
+      return fail(SFX_ERR_CUDA, std::string("transposed face kernel launch: ") + cudaGetErrorString(err));
+    return SFX_OK;
+  }
+};
+
 template <int P>
 struct FaceMatrixFn {
   sfx_form_s& f;
@@ -184,6 +210,24 @@ int launch_boundary_jvp_f32(const sfx_form_s& f, const float* u, const float* du
   for (const auto& bi : f.boundary) {
     int rc = f.p == 1 ? visit_bmaterial(bi, FaceFn<1, kernels::JVP, float>{f, bi, u, du, out, t, s})
                       : visit_bmaterial(bi, FaceFn<2, kernels::JVP, float>{f, bi, u, du, out, t, s});
+    if (rc) return rc;
+  }
+  return SFX_OK;
+}
+
+int launch_boundary_transpose(const sfx_form_s& f, const double* v, double* out, cudaStream_t s) {
+  for (const auto& bi : f.boundary) {
+    const int rc = f.p == 1 ? visit_bmaterial(bi, FaceTransposeFn<1, double>{f, bi, f.u_lin64.p, v, out, s})
+                            : visit_bmaterial(bi, FaceTransposeFn<2, double>{f, bi, f.u_lin64.p, v, out, s});
+    if (rc) return rc;
+  }
+  return SFX_OK;
+}
+
+int launch_boundary_transpose_f32(const sfx_form_s& f, const float* v, float* out, cudaStream_t s) {
+  for (const auto& bi : f.boundary) {
+    const int rc = f.p == 1 ? visit_bmaterial(bi, FaceTransposeFn<1, float>{f, bi, f.u_lin32.p, v, out, s})
+                            : visit_bmaterial(bi, FaceTransposeFn<2, float>{f, bi, f.u_lin32.p, v, out, s});
     if (rc) return rc;
   }
   return SFX_OK;
@@ -299,6 +343,7 @@ extern "C" int sfx_form_add_boundary_integral(sfx_form form, int bmaterial, int 
   int comps = 0, np = 0;
   if (int rc = bmaterial_info(bmaterial, &comps, &np)) return rc;
   if (comps != form->c) return fail(SFX_ERR_INVALID, "boundary material component count does not match the space");
+  if (form->qoi) return fail(SFX_ERR_INVALID, "a quantity of interest takes sfx_qoi_add_boundary_integral");
   if (!params) return fail(SFX_ERR_INVALID, "null parameters");
   BoundaryIntegral bi;
   bi.material = bmaterial;

@@ -85,6 +85,8 @@ int compute_geometry(sfx_form_s& f, cudaStream_t s) {
     if (int rc = compute_face_geometry(f, bi, s)) return rc;
   for (auto& bi : f.face_sets)
     if (int rc = compute_face_geometry(f, bi, s)) return rc;
+  for (auto& bi : f.qoi_boundary)
+    if (int rc = compute_face_geometry(f, bi, s)) return rc;
   SFX_CUDA_TRY(cudaGetLastError());
   return SFX_OK;
 }
@@ -245,6 +247,7 @@ int sfx_form_add_domain_integral(sfx_form form, int material, const double* para
   int comps = 0, np = 0, nst = 0;
   if (int rc = material_info(material, &comps, &np, &nst)) return rc;
   if (comps != form->c) return fail(SFX_ERR_INVALID, "material component count does not match the trial space");
+  if (form->qoi) return fail(SFX_ERR_INVALID, "a quantity of interest takes sfx_qoi_add_domain_integral");
   if (!form->domain.empty()) return fail(SFX_ERR_UNSUPPORTED, "one domain integral per form in this version");
   if (np > 0 && !params) return fail(SFX_ERR_INVALID, "material needs parameters");
   DomainIntegral di;
@@ -353,6 +356,36 @@ int sfx_jvp_f32(sfx_form form, const float* du, float* dr, void* stream) {
     if (int rc2 = scatter_dispatch<float>(*form, form->e32.p, dr, i > 0, s)) return rc2;
   }
   return launch_boundary_jvp_f32(*form, form->u_lin32.p, du, dr, form->t_lin, s);
+}
+
+int sfx_jvp_transpose(sfx_form form, const double* v, double* dr, void* stream) {
+  if (check_form(form)) return SFX_ERR_INVALID;
+  if (!v || !dr) return fail(SFX_ERR_INVALID, "null vector");
+  if (!form->linearized) return fail(SFX_ERR_INVALID, "sfx_linearize must be called before sfx_jvp_transpose");
+  if (!form->domain.empty() && form->jvp_mode != SFX_JVP_STORED_TANGENT)
+    return fail(SFX_ERR_UNSUPPORTED, "the transposed action needs the stored tangent (SFX_JVP_STORED_TANGENT)");
+  auto s = static_cast<cudaStream_t>(stream);
+  if (form->domain.empty()) SFX_CUDA_TRY(cudaMemsetAsync(dr, 0, sizeof(double) * size_t(form->ndofs), s));
+  for (size_t i = 0; i < form->domain.size(); i++) {
+    if (int rc = launch_jvp_transpose(*form, form->domain[i], v, form->e64.p, s)) return rc;
+    if (int rc2 = scatter_dispatch<double>(*form, form->e64.p, dr, i > 0, s)) return rc2;
+  }
+  return launch_boundary_transpose(*form, v, dr, s);
+}
+
+int sfx_jvp_transpose_f32(sfx_form form, const float* v, float* dr, void* stream) {
+  if (check_form(form)) return SFX_ERR_INVALID;
+  if (!v || !dr) return fail(SFX_ERR_INVALID, "null vector");
+  if (!form->linearized) return fail(SFX_ERR_INVALID, "sfx_linearize must be called before sfx_jvp_transpose_f32");
+  if (!form->domain.empty() && form->jvp_mode != SFX_JVP_STORED_TANGENT)
+    return fail(SFX_ERR_UNSUPPORTED, "the transposed action needs the stored tangent (SFX_JVP_STORED_TANGENT)");
+  auto s = static_cast<cudaStream_t>(stream);
+  if (form->domain.empty()) SFX_CUDA_TRY(cudaMemsetAsync(dr, 0, sizeof(float) * size_t(form->ndofs), s));
+  for (size_t i = 0; i < form->domain.size(); i++) {
+    if (int rc = launch_jvp_transpose_f32(*form, form->domain[i], v, form->e32.p, s)) return rc;
+    if (int rc2 = scatter_dispatch<float>(*form, form->e32.p, dr, i > 0, s)) return rc2;
+  }
+  return launch_boundary_transpose_f32(*form, v, dr, s);
 }
 
 int sfx_jvp_element(sfx_form form, const double* du, double* dE, void* stream) {

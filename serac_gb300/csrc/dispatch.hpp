@@ -38,6 +38,16 @@ int launch_boundary_shape_jvp(const sfx_form_s& f, const double* u, const double
 // geometric factors (reference or shape-displaced configuration)
 int compute_face_geometry(sfx_form_s& f, BoundaryIntegral& bi, cudaStream_t s);
 int compute_geometry(sfx_form_s& f, cudaStream_t s);
+// faces of the box sides in side_mask: tables, vertex coordinates, factors, scratch
+int build_faces(sfx_form_s* form, int side_mask, BoundaryIntegral& bi);
+
+// transposed Jacobian actions: domain from the stored tangent (E-vector),
+// boundary added into out
+int launch_jvp_transpose(const sfx_form_s& f, const DomainIntegral& di, const double* v, double* E, cudaStream_t s);
+int launch_jvp_transpose_f32(const sfx_form_s& f, const DomainIntegral& di, const float* v, float* E,
+                             cudaStream_t s);
+int launch_boundary_transpose(const sfx_form_s& f, const double* v, double* out, cudaStream_t s);
+int launch_boundary_transpose_f32(const sfx_form_s& f, const float* v, float* out, cudaStream_t s);
 
 // diagonal of the element Jacobians from the stored tangent (E-vector)
 int launch_diag_from_tangent(const sfx_form_s& f, const DomainIntegral& di, double* E, cudaStream_t s);

@@ -238,6 +238,30 @@ struct StoredJvpFn {
   }
 };
 
+template <int P, typename Real>
+struct StoredJvpTransposeFn {
+  const sfx_form_s& f;
+  const Real* v;
+  const Real* D;
+  Real* E;
+  cudaStream_t s;
+  template <int C, typename State, typename Maker>
+  int operator()() {
+    constexpr int NQ = (P + 1) * (P + 1) * (P + 1);
+    constexpr int EPW = 32 / NQ;
+    using QF = decltype(Maker{}(nullptr));
+    constexpr bool HS = kernels::tangent_has_source<C, State, QF>();
+    if (f.ne == 0) return SFX_OK;
+    const int64_t warps = (f.ne + EPW - 1) / EPW;
+    const int64_t blocks = (warps * 32 + 127) / 128;
+    kernels::jvp_stored_transpose_kernel<P, C, HS, Maker::value_input, Real>
+        <<<unsigned(blocks), 128, 0, s>>>(v, D, f.conn.p, E, f.nnodes, f.ne);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("transposed jvp launch: ") + cudaGetErrorString(err));
+    return SFX_OK;
+  }
+};
+
 template <int P>
 struct DiagFn {
   const sfx_form_s& f;
@@ -317,6 +341,19 @@ int launch_jvp_stored(const sfx_form_s& f, const DomainIntegral& di, const doubl
 int launch_jvp_stored_f32(const sfx_form_s& f, const DomainIntegral& di, const float* du, float* E, cudaStream_t s) {
   if (f.p == 1) return visit_material(di.material, StoredJvpFn<1, float>{f, di, du, di.D32.p, E, s});
   if (f.p == 2) return visit_material(di.material, StoredJvpFn<2, float>{f, di, du, di.D32.p, E, s});
+  return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
+}
+
+int launch_jvp_transpose(const sfx_form_s& f, const DomainIntegral& di, const double* v, double* E, cudaStream_t s) {
+  if (f.p == 1) return visit_material(di.material, StoredJvpTransposeFn<1, double>{f, v, di.D64.p, E, s});
+  if (f.p == 2) return visit_material(di.material, StoredJvpTransposeFn<2, double>{f, v, di.D64.p, E, s});
+  return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
+}
+
+int launch_jvp_transpose_f32(const sfx_form_s& f, const DomainIntegral& di, const float* v, float* E,
+                             cudaStream_t s) {
+  if (f.p == 1) return visit_material(di.material, StoredJvpTransposeFn<1, float>{f, v, di.D32.p, E, s});
+  if (f.p == 2) return visit_material(di.material, StoredJvpTransposeFn<2, float>{f, v, di.D32.p, E, s});
   return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
 }
 

@@ -86,6 +86,13 @@ struct BoundaryIntegral {
   int64_t num_face_nodes = 0;
 };
 
+/// A domain quantity-of-interest integral (Functional<double(...)>): a
+/// built-in integrand kind with uniform parameters.
+struct QoiIntegral {
+  int kind = 0;
+  std::vector<double> params;
+};
+
 }  // namespace sfx_impl
 
 struct sfx_mesh_s {
@@ -145,6 +152,13 @@ struct sfx_form_s {
   std::vector<sfx_impl::DomainIntegral> domain;
   std::vector<sfx_impl::BoundaryIntegral> boundary;
   std::vector<sfx_impl::BoundaryIntegral> face_sets;  // faces for integrals evaluated by the caller's kernels
+  // quantity of interest (test space QOI): integrals and the per-element /
+  // per-face value scratch of its deterministic sum
+  bool qoi = false;
+  std::vector<sfx_impl::QoiIntegral> qoi_domain;
+  std::vector<sfx_impl::BoundaryIntegral> qoi_boundary;  // material = QoI kind
+  sfx_impl::DeviceBuf<double> qoi_vals;
+  sfx_impl::DeviceBuf<double> qoi_partial;
   // CSR graph (built on first request)
   bool csr_built = false;
   int64_t nnz = 0;

@@ -94,6 +94,7 @@ struct sfx_solver_s {
   int64_t n = 0;
   DeviceBuf<int64_t> ess;
   int64_t n_ess = 0;
+  bool transpose = false;  // linear solves with J^T (adjoint problems)
   // FP64 work vectors
   DeviceBuf<double> r, du, tmp, tmp2, diag, cheb_d, cheb_r, V, Z, y, wx;
   // FP32 work vectors
@@ -129,13 +130,13 @@ int apply_J64(sfx_solver s, const double* x, double* y, cudaStream_t st) {
   // y = P J P x with P the projection onto the free vdofs; every vector the
   // solvers pass in is already zero on the essential set (P x = x), so only
   // the output rows need zeroing
-  if (int rc = sfx_jvp(s->form, x, y, st)) return rc;
+  if (int rc = s->transpose ? sfx_jvp_transpose(s->form, x, y, st) : sfx_jvp(s->form, x, y, st)) return rc;
   if (s->n_ess) sfx_blas::set_entries<double><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, 0.0, y);
   return SFX_OK;
 }
 
 int apply_J32(sfx_solver s, const float* x, float* y, cudaStream_t st) {
-  if (int rc = sfx_jvp_f32(s->form, x, y, st)) return rc;
+  if (int rc = s->transpose ? sfx_jvp_transpose_f32(s->form, x, y, st) : sfx_jvp_f32(s->form, x, y, st)) return rc;
   if (s->n_ess) sfx_blas::set_entries<float><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, 0.0f, y);
   return SFX_OK;
 }
@@ -621,6 +622,21 @@ int sfx_solver_solve_linear(sfx_solver s, double t, const double* u_lin, const d
   SFX_CUDA_TRY(cudaMemcpyAsync(s->r.p, rhs, sizeof(double) * size_t(s->n), cudaMemcpyDeviceToDevice, st));
   if (s->n_ess) sfx_blas::set_entries<double><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, 0.0, s->r.p);
   return linear_solve(s, s->r.p, x, st);
+}
+
+int sfx_solver_solve_adjoint(sfx_solver s, double t, const double* u_lin, const double* rhs, double* x,
+                             void* stream) {
+  if (!s || !u_lin || !rhs || !x) return fail(SFX_ERR_INVALID, "null argument");
+  auto st = static_cast<cudaStream_t>(stream);
+  s->stats = sfx_solver_stats{};
+  if (int rc = sfx_linearize(s->form, t, u_lin, nullptr, st)) return rc;
+  SFX_CUDA_TRY(cudaMemcpyAsync(s->r.p, rhs, sizeof(double) * size_t(s->n), cudaMemcpyDeviceToDevice, st));
+  if (s->n_ess) sfx_blas::set_entries<double><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, 0.0, s->r.p);
+  s->transpose = true;
+  const int rc = linear_solve(s, s->r.p, x, st);
+  s->transpose = false;
+  s->drop_graphs();  // the captured inner steps apply J^T
+  return rc;
 }
 
 int sfx_solver_solve(sfx_solver s, double t, double* u, void* stream) {

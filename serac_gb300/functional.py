@@ -158,6 +158,22 @@ class Gradient:
 
     Mult = mult
 
+    def mult_transpose(self, v, out=None, stream=None):
+        """dR/du^T v (mfem::Operator::MultTranspose): the adjoint action, from
+        the stored tangent transposed (FP64, or FP32 for a float32 v)."""
+        f = self.form
+        if v.dtype == torch.float32:
+            _require(v, torch.float32, f.ndofs, "v")
+            out = torch.empty_like(v) if out is None else out
+            _lib.call("sfx_jvp_transpose_f32", f._h, _dptr(v), _dptr(out), _stream(stream))
+            return out
+        _require(v, torch.float64, f.ndofs, "v")
+        out = torch.empty_like(v) if out is None else out
+        _lib.call("sfx_jvp_transpose", f._h, _dptr(v), _dptr(out), _stream(stream))
+        return out
+
+    MultTranspose = mult_transpose
+
     def element_action(self, du, out=None, stream=None):
         """Element-level action [e][component][node] before the scatter-add
         (FP64, or FP32 for a float32 du)."""
@@ -373,8 +389,132 @@ class ShapeAwareFunctional:
         return self.functional(t, arg, out)
 
 
-def assemble(gradient: Gradient):
-    """CSR of dR/du at the linearisation point: (row_ptr int64, col int32, values float64)."""
+QOI_MEASURE, QOI_POSITION, QOI_FIELD, QOI_NEOHOOKEAN_ENERGY, QOI_NORMAL_FIELD, QOI_POLY_TEST = range(6)
+
+
+def _qoi_nparams(kind, c, boundary):
+    n = {QOI_MEASURE: 0, QOI_POSITION: 3, QOI_FIELD: c, QOI_POLY_TEST: 0}
+    if not boundary and c == 3:
+        n[QOI_NEOHOOKEAN_ENERGY] = 2
+    if boundary and c == 3:
+        n[QOI_NORMAL_FIELD] = 0
+    if kind not in n:
+        raise ValueError(f"QoI kind {kind} is not available {'on faces' if boundary else 'on the domain'} "
+                         f"for {c} components")
+    return n[kind]
+
+
+class QoIGradient:
+    """dQ/du at (t, u) of a quantity of interest (functional_qoi.inl:407-477):
+    ``g(du)`` is the directional derivative (Gradient::operator(), :420) and
+    ``assemble(g)`` the gradient vector (Gradient::assemble, :422-475)."""
+
+    def __init__(self, qoi, t, u):
+        self.qoi = qoi
+        self.t = t
+        self.u = u.clone()
+
+    def action(self, du, out=None, stream=None):
+        """dQ/du du as a one-element float64 CUDA tensor."""
+        q = self.qoi
+        _require(du, torch.float64, q.ndofs, "du")
+        out = torch.empty(1, dtype=torch.float64, device=du.device) if out is None else out
+        _lib.call("sfx_qoi_action", q._h, float(self.t), _dptr(self.u), _dptr(du), _dptr(out), _stream(stream))
+        return out
+
+    def __call__(self, du):
+        return float(self.action(du).item())
+
+    def assemble(self, out=None, stream=None):
+        q = self.qoi
+        out = torch.empty(q.ndofs, dtype=torch.float64, device=self.u.device) if out is None else out
+        _lib.call("sfx_qoi_gradient", q._h, float(self.t), _dptr(self.u), None, _dptr(out), _stream(stream))
+        return out
+
+
+class QoI:
+    """Functional<double(H1<p,c>)>: a quantity of interest (functional_qoi.inl:58-528).
+
+        q = QoI(mesh, H1(2, 3))
+        q.AddDomainIntegral(QOI_NEOHOOKEAN_ENERGY, [K, G])    # :159-189
+        q.AddBoundaryIntegral(QOI_NORMAL_FIELD, sides=[6])    # :201-228
+        value = q(t, u)                                       # :379-392
+        value, dQdu = q(t, differentiate_wrt(u))
+        dQdu(du); assemble(dQdu)                              # :420, :422-475
+    """
+
+    def __init__(self, mesh: Mesh, space: H1):
+        self.mesh = mesh
+        self.space = space
+        h = ctypes.c_void_p()
+        _lib.call("sfx_qoi_create", mesh._h, space.order, space.components, ctypes.byref(h))
+        self._h = h
+        n = ctypes.c_int64()
+        _lib.call("sfx_form_num_dofs", h, ctypes.byref(n))
+        self.ndofs = n.value
+        self.num_nodes = self.ndofs // space.components
+        self._keep = []
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib._LIB is not None:
+            _lib.load().sfx_form_destroy(self._h)
+            self._h = None
+
+    def _params(self, kind, params, boundary):
+        n = _qoi_nparams(kind, self.space.components, boundary)
+        if n == 0:
+            return None
+        arr = np.ascontiguousarray(np.asarray(params, dtype=np.float64).ravel())
+        if arr.size != n:
+            raise ValueError(f"QoI kind {kind} takes {n} parameters, got {arr.size}")
+        self._keep.append(arr)
+        return arr.ctypes.data_as(_lib._dp)
+
+    def AddDomainIntegral(self, kind, params=None):
+        _lib.call("sfx_qoi_add_domain_integral", self._h, int(kind), self._params(kind, params, False))
+
+    def AddBoundaryIntegral(self, kind, sides, params=None):
+        mask = 0
+        for s_ in sides:
+            mask |= 1 << (s_ - 1)
+        _lib.call("sfx_qoi_add_boundary_integral", self._h, int(kind), mask, self._params(kind, params, True))
+
+    AddVolumeIntegral = AddDomainIntegral
+    AddSurfaceIntegral = AddBoundaryIntegral
+
+    def set_shape_displacement(self, shape, stream=None):
+        """Evaluate on the configuration X + shape (as Functional.set_shape_displacement)."""
+        if shape is None:
+            _lib.call("sfx_form_set_shape_displacement", self._h, None, _stream(stream))
+        else:
+            _require(shape, torch.float64, 3 * self.num_nodes, "shape")
+            _lib.call("sfx_form_set_shape_displacement", self._h, _dptr(shape), _stream(stream))
+
+    def value(self, t, u, out=None, stream=None):
+        """Q(t, u) as a one-element float64 CUDA tensor (no host synchronisation)."""
+        _require(u, torch.float64, self.ndofs, "u")
+        out = torch.empty(1, dtype=torch.float64, device=u.device) if out is None else out
+        _lib.call("sfx_qoi_evaluate", self._h, float(t), _dptr(u), _dptr(out), _stream(stream))
+        return out
+
+    def gradient(self, t, u, out=None, value=None, stream=None):
+        """dQ/du (t, u) as a CUDA tensor; value (one-element tensor) receives Q."""
+        _require(u, torch.float64, self.ndofs, "u")
+        out = torch.empty_like(u) if out is None else out
+        _lib.call("sfx_qoi_gradient", self._h, float(t), _dptr(u), _dptr(value), _dptr(out), _stream(stream))
+        return out
+
+    def __call__(self, t, arg):
+        if isinstance(arg, differentiate_wrt):
+            return float(self.value(t, arg.u).item()), QoIGradient(self, t, arg.u)
+        return float(self.value(t, arg).item())
+
+
+def assemble(gradient):
+    """CSR of dR/du at the linearisation point, (row_ptr int64, col int32,
+    values float64); for a QoI gradient, the vector dQ/du."""
+    if isinstance(gradient, QoIGradient):
+        return gradient.assemble()
     f = gradient.form
     row_ptr, col = f.csr_graph()
     return row_ptr, col, f.assemble_values()

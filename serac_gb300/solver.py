@@ -128,3 +128,14 @@ class NewtonSolver:
         out = torch.empty_like(rhs) if out is None else out
         _lib.call("sfx_solver_solve_linear", self._h, float(t), _dptr(u_lin), _dptr(rhs), _dptr(out), _stream(stream))
         return out
+
+    def solve_adjoint(self, t, u_lin, rhs, out=None, stream=None):
+        """lambda = J(t, u_lin)^-T rhs on the free vdofs (0 on the essential
+        set): the adjoint solve of SolidMechanics::reverseAdjointTimestep
+        (solid_mechanics.hpp:1343-1501), matrix-free with the transposed action."""
+        _require(u_lin, torch.float64, self.form.ndofs, "u_lin")
+        _require(rhs, torch.float64, self.form.ndofs, "rhs")
+        out = torch.empty_like(rhs) if out is None else out
+        _lib.call("sfx_solver_solve_adjoint", self._h, float(t), _dptr(u_lin), _dptr(rhs), _dptr(out),
+                  _stream(stream))
+        return out

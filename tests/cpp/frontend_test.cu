@@ -240,3 +240,134 @@ extern "C" int frontend_j2(int nx, int ny, int nz, const double* V, const double
     return -1;
   }
 }
+
+namespace {
+
+// user QoI integrands (scalar field): X0^2 + sin X1 + X0 u^3 + (1 + X2)/2 |grad u|^2
+// on the domain and X0 - X1 + cos(u X1) + (du/ds)^2 / 4 on faces
+struct UserPolyQoI {
+  template <typename X, typename T>
+  SFX_HD auto operator()(double, const X& position, const T& temperature) const {
+    using namespace sfx;
+    using std::sin;
+    auto x = get<0>(position);
+    auto u = get<0>(temperature);
+    auto g = get<1>(temperature);
+    return x[0] * x[0] + sin(x[1]) + x[0] * u * u * u + 0.5 * (1.0 + x[2]) * dot(g, g);
+  }
+};
+struct UserPolyFaceQoI {
+  template <typename X, typename T>
+  SFX_HD auto operator()(double, const X& position, const T& temperature) const {
+    using namespace sfx;
+    using std::cos;
+    auto x = get<0>(position);
+    auto u = get<0>(temperature);
+    auto g = get<1>(temperature);
+    return x[0] - x[1] + cos(u * x[1]) + 0.25 * g[0] * g[0];
+  }
+};
+// user QoI integrands (vector field): Neo-Hookean stored energy written from
+// F = I + H, and the normal displacement u . n on faces
+struct UserEnergyQoI {
+  double K, G;
+  template <typename X, typename D>
+  SFX_HD auto operator()(double, const X&, const D& displacement) const {
+    using namespace sfx;
+    using std::log;
+    auto H = get<1>(displacement);
+    auto F = H + Identity<3>();
+    auto lnJ = log(det(F));
+    auto trC = F[0][0] * F[0][0];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++)
+        if (i + j > 0) trC = trC + F[i][j] * F[i][j];
+    double lambda = K - (2.0 / 3.0) * G;
+    return 0.5 * G * (trC - 3.0) - G * lnJ + 0.5 * lambda * lnJ * lnJ;
+  }
+};
+struct UserNormalQoI {
+  template <typename X, typename D>
+  SFX_HD auto operator()(double, const X& position, const D& displacement) const {
+    using namespace sfx;
+    auto n = cross(get<1>(position));
+    return dot(get<0>(displacement), n / norm(n));
+  }
+};
+
+template <typename QoIT, typename Setup>
+int run_qoi(int nx, int ny, int nz, const double* V, const double* u, const double* du, double* value,
+            double* value2, double* action, double* grad, Setup&& setup) {
+  try {
+    auto mesh = sfx::Mesh::StructuredHex(nx, ny, nz, V);
+    QoIT q(mesh);
+    setup(q);
+    const size_t n = size_t(q.num_dofs());
+    Buffers b(n);
+    cudaMemcpy(b.u, u, n * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(b.du, du, n * 8, cudaMemcpyHostToDevice);
+    *value = q(0.0, b.u);
+    auto [v2, g] = q(0.0, sfx::differentiate_wrt(b.u));
+    *value2 = v2;
+    *action = g(b.du);
+    const double* gv = assemble(g);
+    cudaMemcpy(grad, gv, n * 8, cudaMemcpyDeviceToHost);
+    return cudaDeviceSynchronize() == cudaSuccess ? 0 : -2;
+  } catch (const std::exception&) {
+    return -1;
+  }
+}
+
+}  // namespace
+
+// scalar QoI: the polynomial integrand on the domain and on the sides in side_mask
+extern "C" int frontend_qoi_poly(int p, int side_mask, int nx, int ny, int nz, const double* V, const double* u,
+                                 const double* du, double* value, double* value2, double* action, double* grad) {
+  auto setup = [=](auto& q) {
+    q.AddDomainIntegral(sfx::Dimension<3>{}, sfx::DependsOn<0>{}, UserPolyQoI{});
+    q.AddBoundaryIntegral(sfx::Dimension<2>{}, sfx::DependsOn<0>{}, UserPolyFaceQoI{}, side_mask);
+  };
+  if (p == 1)
+    return run_qoi<sfx::Functional<double(sfx::H1<1, 1>)>>(nx, ny, nz, V, u, du, value, value2, action, grad, setup);
+  return run_qoi<sfx::Functional<double(sfx::H1<2, 1>)>>(nx, ny, nz, V, u, du, value, value2, action, grad, setup);
+}
+
+// vector QoI: stored energy on the domain plus u . n on the sides in side_mask (Q2)
+extern "C" int frontend_qoi_energy(double K, double G, int side_mask, int nx, int ny, int nz, const double* V,
+                                   const double* u, const double* du, double* value, double* value2, double* action,
+                                   double* grad) {
+  auto setup = [=](auto& q) {
+    q.AddDomainIntegral(sfx::Dimension<3>{}, sfx::DependsOn<0>{}, UserEnergyQoI{K, G});
+    q.AddBoundaryIntegral(sfx::Dimension<2>{}, sfx::DependsOn<0>{}, UserNormalQoI{}, side_mask);
+  };
+  return run_qoi<sfx::Functional<double(sfx::H1<2, 3>)>>(nx, ny, nz, V, u, du, value, value2, action, grad, setup);
+}
+
+// transposed actions of the user Neo-Hookean + follower pressure functional (Q2)
+extern "C" int frontend_neohookean_pressure_transpose(double K, double G, double pressure, int side_mask, int nx,
+                                                      int ny, int nz, const double* V, const double* u,
+                                                      const double* v, double* jt, double* jt32) {
+  try {
+    auto mesh = sfx::Mesh::StructuredHex(nx, ny, nz, V);
+    sfx::Functional<sfx::H1<2, 3>(sfx::H1<2, 3>)> f(mesh);
+    f.AddDomainIntegral(sfx::Dimension<3>{}, sfx::DependsOn<0>{}, UserNeoHookean{K, G});
+    f.AddBoundaryIntegral(sfx::Dimension<2>{}, sfx::DependsOn<0>{}, UserPressure{pressure}, side_mask);
+    const size_t n = size_t(f.num_dofs());
+    Buffers b(n);
+    cudaMemcpy(b.u, u, n * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(b.du, v, n * 8, cudaMemcpyHostToDevice);
+    std::vector<float> v32(v, v + n);
+    cudaMemcpy(b.du32, v32.data(), n * 4, cudaMemcpyHostToDevice);
+    auto [r, grad] = f(0.0, sfx::differentiate_wrt(b.u));
+    (void)r;
+    grad.MultTranspose(b.du, b.jv);
+    cudaMemcpy(jt, b.jv, n * 8, cudaMemcpyDeviceToHost);
+    grad.MultTransposeF32(b.du32, b.jv32);
+    std::vector<float> out32(n);
+    cudaMemcpy(out32.data(), b.jv32, n * 4, cudaMemcpyDeviceToHost);
+    for (size_t i = 0; i < n; i++) jt32[i] = out32[i];
+    return cudaDeviceSynchronize() == cudaSuccess ? 0 : -2;
+  } catch (const std::exception&) {
+    return -1;
+  }
+}

@@ -181,3 +181,85 @@ def test_user_qfunction_with_quadrature_state(cuda, felib):
     assert orc.state[..., 9].max() > 0
     assert rel(r, orc.residual(1.5 * u)) <= 1e-12
     assert rel(jv, orc.jvp(1.5 * u, du)) <= 1e-12
+
+
+def _qoi_call(_fn):
+    value, value2, action = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    return value, value2, action, [ctypes.byref(value), ctypes.byref(value2), ctypes.byref(action)]
+
+
+@pytest.mark.parametrize("p", [1, 2])
+def test_user_qoi_scalar(cuda, felib, p):
+    """Functional<double(H1<p,1>)> with user domain and face integrands
+    against the oracle's QOI_POLY_TEST (same mathematics, written separately)."""
+    dims = (3, 2, 2)
+    m = mesh(*dims, perturb=0.1, seed=4)
+    sides = [1, 3, 6]
+    orc = O.OracleQoI(m, p, 1)
+    orc.add_domain_integral(O.QOI_POLY_TEST)
+    orc.add_boundary_integral(O.QOI_POLY_TEST, sides)
+    rng = np.random.default_rng(40 + p)
+    u = rng.standard_normal(orc.ndofs) * 0.1
+    du = rng.standard_normal(orc.ndofs)
+    grad = np.zeros(orc.ndofs)
+    value, value2, action, refs = _qoi_call(None)
+    mask = sum(1 << (s - 1) for s in sides)
+    V = np.ascontiguousarray(m.vertices)
+    rc = felib.frontend_qoi_poly(p, mask, *dims, _p(V), _p(u), _p(du), *refs, _p(grad))
+    assert rc == 0
+    ref_v, ref_g = orc.evaluate(u)
+    assert abs(value.value - ref_v) <= 1e-12 * abs(ref_v)
+    assert value2.value == value.value
+    assert rel(grad, ref_g) <= 1e-12
+    assert abs(action.value - ref_g @ du) <= 1e-12 * np.abs(ref_g).sum() * np.abs(du).max()
+
+
+def test_user_qoi_vector_energy(cuda, felib):
+    """A user stored-energy integrand plus u . n on faces (Q2 vector): the
+    gradient matches the oracle (whose energy gradient is the pinned
+    Neo-Hookean residual)."""
+    dims = (3, 2, 2)
+    m = mesh(*dims, perturb=0.1, seed=6)
+    K, G = PARAMS[O.MAT_NEOHOOKEAN]
+    sides = [2, 6]
+    orc = O.OracleQoI(m, 2, 3)
+    orc.add_domain_integral(O.QOI_NEOHOOKEAN_ENERGY, [K, G])
+    orc.add_boundary_integral(O.QOI_NORMAL_FIELD, sides)
+    rng = np.random.default_rng(44)
+    u = rng.standard_normal(orc.ndofs) * 0.01
+    du = rng.standard_normal(orc.ndofs)
+    grad = np.zeros(orc.ndofs)
+    value, value2, action, refs = _qoi_call(None)
+    mask = sum(1 << (s - 1) for s in sides)
+    V = np.ascontiguousarray(m.vertices)
+    rc = felib.frontend_qoi_energy(ctypes.c_double(K), ctypes.c_double(G), mask, *dims, _p(V), _p(u), _p(du), *refs,
+                                   _p(grad))
+    assert rc == 0
+    ref_v, ref_g = orc.evaluate(u)
+    # tr(F^T F) - 3 in the user integrand cancels: its value carries ~1e-16 / |H|^2 relative rounding
+    assert abs(value.value - ref_v) <= 1e-10 * abs(ref_v)
+    assert rel(grad, ref_g) <= 1e-12
+    assert abs(action.value - ref_g @ du) <= 1e-12 * np.abs(ref_g).sum() * np.abs(du).max()
+
+
+def test_user_transpose_action(cuda, felib):
+    """Gradient::MultTranspose / MultTransposeF32 of a user Neo-Hookean +
+    follower-pressure functional against the oracle's assembled transpose."""
+    dims = (3, 2, 2)
+    m = mesh(*dims, perturb=0.1, seed=2)
+    orc = O.OracleFunctional(m, 2, 3)
+    orc.add_domain_integral(O.MAT_NEOHOOKEAN, PARAMS[O.MAT_NEOHOOKEAN])
+    orc.add_boundary_integral(O.BMAT_PRESSURE, [3, 6], [0.7])
+    u, v = fields(orc.ndofs, O.MAT_NEOHOOKEAN, seed=8)
+    jt = np.zeros(orc.ndofs)
+    jt32 = np.zeros(orc.ndofs)
+    K, G = PARAMS[O.MAT_NEOHOOKEAN]
+    mask = (1 << 2) | (1 << 5)
+    V = np.ascontiguousarray(m.vertices)
+    rc = felib.frontend_neohookean_pressure_transpose(ctypes.c_double(K), ctypes.c_double(G), ctypes.c_double(0.7),
+                                                      mask, *dims, _p(V), _p(u), _p(v), _p(jt), _p(jt32))
+    assert rc == 0
+    ref = orc.jvp_transpose(u, v)
+    assert rel(jt, ref) <= 1e-12
+    assert rel(jt32, ref) <= 1e-5
+    assert rel(ref, orc.jvp(u, v)) > 1e-6  # the follower pressure makes J non-symmetric
