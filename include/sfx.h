@@ -23,6 +23,8 @@
  *   sfx_jvp_element(_f32)           numerics/functional/integral.hpp:93-103 Integral::GradientMult
  *   sfx_jvp_transpose(_f32)         physics/solid_mechanics.hpp:1343-1501 (the adjoint solves' transposed
  *                                   Jacobian, formed there as the transpose of assemble(Gradient&))
+ *   sfx_shape_vjp                   physics/solid_mechanics.hpp:1421-1431, 1495-1503 (assemble(dR/dshape)
+ *                                   followed by MultTranspose(adjoint))
  *   sfx_qoi_*                       numerics/functional/functional_qoi.inl:58-528 Functional<double(trials...)>:
  *                                   AddDomainIntegral :159-189, AddBoundaryIntegral :201-228, operator() :379-392,
  *                                   Gradient::operator() :420, Gradient::assemble :422-475
@@ -118,6 +120,13 @@ int sfx_form_set_shape_displacement(sfx_form form, const double* shape, void* st
  * with respect to its argument 0 (shape_aware_functional.hpp:537-541), for
  * its domain and boundary integrals. */
 int sfx_shape_jvp(sfx_form form, double t, const double* u, const double* dshape, double* dr, void* stream);
+
+/* out = (dR/dp (t, u; p))^T lam (device, 3 * num_nodes doubles): the shape
+ * sensitivity of an adjoint problem, which serac forms by assembling dR/dp
+ * and applying its transpose (SolidMechanics::computeTimestepShapeSensitivity,
+ * solid_mechanics.hpp:1421-1431; computeDualShapeSensitivity, :1495-1503),
+ * matrix-free over the domain and boundary integrals. */
+int sfx_shape_vjp(sfx_form form, double t, const double* u, const double* lam, double* out, void* stream);
 
 /* r = R(t, u) (device, num_dofs doubles each).  When sfx_update_qdata(form, 1)
  * is in effect, quadrature-point state is committed by this call. */
@@ -273,6 +282,10 @@ int sfx_qoi_evaluate(sfx_form qoi, double t, const double* u, double* value, voi
 int sfx_qoi_gradient(sfx_form qoi, double t, const double* u, double* value, double* grad, void* stream);
 /* out: device, one double = dQ/du (t, u) du */
 int sfx_qoi_action(sfx_form qoi, double t, const double* u, const double* du, double* out, void* stream);
+/* out: device, 3 * num_nodes doubles = dQ/dp (t, u; p), the partial derivative
+ * of the QoI with respect to the shape displacement (the shape-aware QoI
+ * differentiated with respect to its shape argument, shape_aware_functional.hpp) */
+int sfx_qoi_shape_gradient(sfx_form qoi, double t, const double* u, double* out, void* stream);
 
 /* Quadrature-point state (J2: 10 doubles per point: plastic strain 3x3
  * row-major, accumulated plastic strain), host arrays

@@ -1247,8 +1247,9 @@ __global__ void __launch_bounds__(128) jvp_stored_transpose_kernel(const Real* _
 /// the tangent at HBM rate instead of waiting on 81 dependent loads per lane.
 /// Elements are dealt to warps round-robin (persistent grid).  A wait that
 /// does not complete sets *err and the warp drains its outstanding copies
-/// (again bounded) before returning.
-template <int C, bool HS, bool VI, int WARPS, int STAGES>
+/// (again bounded) before returning.  TRANSPOSE applies the block transposed
+/// (J^T v, as jvp_stored_transpose_kernel) with the same staging.
+template <int C, bool HS, bool VI, int WARPS, int STAGES, bool TRANSPOSE = false>
 __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float* __restrict__ du,
                                                                     const float* __restrict__ D,
                                                                     const int32_t* __restrict__ conn,
@@ -1256,6 +1257,12 @@ __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float*
                                                                     int64_t num_elements, int* __restrict__ err) {
   constexpr int P = 2, Q = 3, NQ = 27;
   using Shape = TangentShape<C, HS, VI>;
+  // input side (interpolated direction) and output side (integrated) of the
+  // block: D[out][in] for J, D^T for J^T
+  constexpr bool IN_VALUE = TRANSPOSE ? HS : VI;
+  constexpr bool OUT_VALUE = TRANSPOSE ? VI : HS;
+  constexpr int NIN = TRANSPOSE ? Shape::rows : Shape::cols;
+  constexpr int NOUT = TRANSPOSE ? Shape::cols : Shape::rows;
   constexpr int64_t ES = Shape::template stride<NQ>;  // floats per element block
   constexpr uint32_t BYTES = uint32_t(ES * 4);
   static_assert(BYTES % 16 == 0, "bulk copies move multiples of 16 bytes");
@@ -1317,13 +1324,13 @@ __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float*
     for (int c = 0; c < C; c++) du_next[c] = (lane_ok && e1 < num_elements) ? du[c * num_nodes + node_next] : 0.f;
     const int32_t node_after = (lane_ok && e2 < num_elements) ? conn[e2 * NQ + qi] : 0;
     // interpolate du while the tangent is in flight
-    float din[Shape::cols];
+    float din[NIN];
 #pragma unroll
     for (int c = 0; c < C; c++) {
       float v, g0, g1, g2;
       interpolate_lane<Q, float>(du_cur[c], 0, ix, iy, iz, sB, sG, v, g0, g1, g2);
-      if constexpr (VI) din[c] = v;
-      constexpr int off = VI ? C : 0;
+      if constexpr (IN_VALUE) din[c] = v;
+      constexpr int off = IN_VALUE ? C : 0;
       din[off + 3 * c + 0] = g0;
       din[off + 3 * c + 1] = g1;
       din[off + 3 * c + 2] = g2;
@@ -1334,12 +1341,13 @@ __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float*
       break;
     }
     const float* Dq = my_ring + s * ES + qi;
-    float dout[Shape::rows];
+    float dout[NOUT];
 #pragma unroll
-    for (int r = 0; r < Shape::rows; r++) {
+    for (int r = 0; r < NOUT; r++) {
       float acc = 0.f;
 #pragma unroll
-      for (int k = 0; k < Shape::cols; k++) acc += Dq[(r * Shape::cols + k) * NQ] * din[k];
+      for (int k = 0; k < NIN; k++)
+        acc += Dq[(TRANSPOSE ? k * Shape::cols + r : r * Shape::cols + k) * NQ] * din[k];
       dout[r] = acc;
     }
     __syncwarp();  // every lane has read stage s
@@ -1351,12 +1359,12 @@ __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float*
         bulk::copy_g2s(my_ring + s * ES, D + en * ES, BYTES, &my_bars[s]);
       }
     }
-    constexpr int roff = HS ? C : 0;
+    constexpr int roff = OUT_VALUE ? C : 0;
 #pragma unroll
     for (int c = 0; c < C; c++) {
-      const float src = HS ? dout[HS ? c : 0] : 0.f;
-      const float r = integrate_lane<Q, HS, true, float>(src, dout[roff + 3 * c], dout[roff + 3 * c + 1],
-                                                         dout[roff + 3 * c + 2], 0, ix, iy, iz, sB, sG);
+      const float src = OUT_VALUE ? dout[OUT_VALUE ? c : 0] : 0.f;
+      const float r = integrate_lane<Q, OUT_VALUE, true, float>(src, dout[roff + 3 * c], dout[roff + 3 * c + 1],
+                                                                dout[roff + 3 * c + 2], 0, ix, iy, iz, sB, sG);
       if (lane_ok) out_e[(e * C + c) * NQ + qi] = r;
     }
     // rotate the gather pipeline (its loads had this element's work to land)

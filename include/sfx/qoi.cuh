@@ -38,7 +38,7 @@ struct Measure {
 struct PositionMoment {
   double a[3];
   template <typename Pos, typename Arg>
-  SFX_HDI double operator()(double, const Pos& pos, const Arg&) const {
+  SFX_HDI auto operator()(double, const Pos& pos, const Arg&) const {
     const auto& X = get<0>(pos);
     return a[0] * X[0] + a[1] * X[1] + a[2] * X[2];
   }
@@ -98,12 +98,13 @@ struct NeoHookeanEnergy {
 struct NormalField {
   template <typename Pos, typename Arg>
   SFX_HDI auto operator()(double, const Pos& pos, const Arg& arg) const {
+    using std::sqrt;
     const auto& J = get<1>(pos);
     const auto& u = get<0>(arg);
-    const double n0 = J[1][0] * J[2][1] - J[2][0] * J[1][1];
-    const double n1 = J[2][0] * J[0][1] - J[0][0] * J[2][1];
-    const double n2 = J[0][0] * J[1][1] - J[1][0] * J[0][1];
-    const double inv = 1.0 / ::sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+    const auto n0 = J[1][0] * J[2][1] - J[2][0] * J[1][1];
+    const auto n1 = J[2][0] * J[0][1] - J[0][0] * J[2][1];
+    const auto n2 = J[0][0] * J[1][1] - J[1][0] * J[0][1];
+    const auto inv = 1.0 / sqrt(n0 * n0 + n1 * n1 + n2 * n2);
     return (n0 * inv) * u[0] + (n1 * inv) * u[1] + (n2 * inv) * u[2];
   }
 };

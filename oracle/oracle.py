@@ -435,6 +435,23 @@ class OracleFunctional:
     def jvp(self, u, du, t=0.0):
         return self._apply(1, u, du, t=t)
 
+    def shape_vjp_fd(self, u, lam, base_shape=None, h=1e-6, t=0.0):
+        """(dR/dp)^T lam by central differences over every shape dof (small
+        meshes only); the shape is restored afterwards."""
+        saved = self.shape
+        p0 = np.zeros(3 * self.nnodes) if base_shape is None else np.asarray(base_shape, dtype=np.float64)
+        out = np.zeros(3 * self.nnodes)
+        for k in range(out.size):
+            d = np.zeros_like(p0)
+            d[k] = h
+            self.set_shape(p0 + d)
+            rp = self.residual(u, t)
+            self.set_shape(p0 - d)
+            rm = self.residual(u, t)
+            out[k] = lam @ (rp - rm) / (2 * h)
+        self.set_shape(saved)
+        return out
+
     def jvp_transpose(self, u, v, t=0.0):
         """dR/du(u)^T v from the assembled matrix (pinned through assemble)."""
         return self.assemble(u, t).T @ v
@@ -595,6 +612,7 @@ class OracleQoI:
         self.Xq, self.Jq = geometric_factors(mesh.elem_coords(), self.Q)
         self.domain = []
         self.boundary = []
+        self._bsides = []
         self._shape = None if shape is None else np.asarray(shape, dtype=np.float64)
         if self._shape is not None:
             self._apply_shape_domain()
@@ -610,6 +628,7 @@ class OracleQoI:
 
     def add_boundary_integral(self, kind, sides, params=None):
         Xf, fnodes = self.mesh.boundary_faces(self.p, sides)
+        self._bsides.append(list(sides))
         Xq, Jq = face_geometric_factors(Xf, self.Q)
         if self._shape is not None:
             _, _, fphi, fds, fdt = _tensor_basis(self.p)
@@ -668,6 +687,24 @@ class OracleQoI:
 
     def value(self, u):
         return self.evaluate(u)[0]
+
+    def shape_gradient_fd(self, u, base_shape=None, h=1e-6):
+        """dQ/dp by central differences over every shape dof (small meshes only)."""
+        p0 = np.zeros(3 * self.nnodes) if base_shape is None else np.asarray(base_shape, dtype=np.float64)
+        out = np.zeros(3 * self.nnodes)
+
+        def q_at(shape):
+            other = OracleQoI(self.mesh, self.p, self.c, shape=shape)
+            other.domain = list(self.domain)
+            for (kind, params, _, _, _), sides in zip(self.boundary, self._bsides):
+                other.add_boundary_integral(kind, sides, params)
+            return other.value(u)
+
+        for k in range(out.size):
+            d = np.zeros_like(p0)
+            d[k] = h
+            out[k] = (q_at(p0 + d) - q_at(p0 - d)) / (2 * h)
+        return out
 
     def gradient(self, u):
         return self.evaluate(u)[1]

@@ -24,6 +24,7 @@ from .functional import (  # noqa: F401
     QoI,
     QoIGradient,
     ShapeAwareFunctional,
+    ShapeGradient,
     assemble,
     box_vertices,
     differentiate_wrt,

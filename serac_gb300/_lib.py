@@ -53,6 +53,8 @@ SIGNATURES = {
     "sfx_qoi_evaluate": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp]),
     "sfx_qoi_gradient": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp, _vp]),
     "sfx_qoi_action": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp, _vp]),
+    "sfx_qoi_shape_gradient": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp]),
+    "sfx_shape_vjp": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp, _vp]),
     "sfx_jvp_f32": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "sfx_jvp_element": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "sfx_jvp_element_f32": (_c.c_int, [_vp, _vp, _vp, _vp]),

@@ -16,6 +16,7 @@
 #include "sfx.h"
 #include "sfx/boundary.cuh"
 #include "sfx/materials.hpp"
+#include "sfx/sensitivity.cuh"
 
 using namespace sfx_impl;
 
@@ -177,6 +178,43 @@ struct ShapeFaceFn {
     return SFX_OK;
   }
 };
+
+template <int P>
+struct ShapeFaceVjpFn {
+  const sfx_form_s& f;
+  const BoundaryIntegral& bi;
+  const double* u;
+  const double* lam;
+  double* out;
+  double t;
+  cudaStream_t s;
+  template <int C, typename QF>
+  int operator()(const QF& qf) {
+    constexpr int NQ = (P + 1) * (P + 1);
+    constexpr int FPW = 32 / NQ;
+    if (bi.num_faces == 0) return SFX_OK;
+    kernels::FaceArgs<double> a{u, nullptr, f.efshape.p, bi.fconn.p, bi.fgeom.p, f.nnodes, bi.num_faces, t};
+    const int64_t warps = (bi.num_faces + FPW - 1) / FPW;
+    kernels::face_shape_adjoint_kernel<P, C, kernels::SHAPE_VJP, QF><<<unsigned((warps * 32 + 127) / 128), 128, 0, s>>>(
+        a, qf, bi.Xf.p, f.has_shape ? f.shape.p : nullptr, lam);
+    kernels::face_scatter_kernel<3, NQ, double><<<unsigned((bi.num_face_nodes + 255) / 256), 256, 0, s>>>(
+        f.efshape.p, bi.node_ptr.p, bi.node_ids.p, bi.node_ent.p, out, bi.num_face_nodes, f.nnodes);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("face shape vjp launch: ") + cudaGetErrorString(err));
+    return SFX_OK;
+  }
+};
+
+// out += (d(boundary residual)/dp)^T lam for every boundary integral of the form
+int launch_boundary_shape_vjp(const sfx_form_s& f, const double* u, const double* lam, double* out, double t,
+                              cudaStream_t s) {
+  for (const auto& bi : f.boundary) {
+    const int rc = f.p == 1 ? visit_bmaterial(bi, ShapeFaceVjpFn<1>{f, bi, u, lam, out, t, s})
+                            : visit_bmaterial(bi, ShapeFaceVjpFn<2>{f, bi, u, lam, out, t, s});
+    if (rc) return rc;
+  }
+  return SFX_OK;
+}
 
 // out += d(boundary residual)/dp dshape for every boundary integral of the form
 int launch_boundary_shape_jvp(const sfx_form_s& f, const double* u, const double* dshape, double* out, double t,

@@ -60,6 +60,23 @@ int scatter_evector(const sfx_form_s& f, const double* E, double* out, bool accu
   return scatter_dispatch<double>(f, E, out, accumulate, s);
 }
 
+int scatter_evector3(const sfx_form_s& f, const double* E, double* out, bool accumulate, cudaStream_t s) {
+  if (f.p == 1) return scatter<3, 8, double>(f, E, out, accumulate, s);
+  if (f.p == 2) return scatter<3, 27, double>(f, E, out, accumulate, s);
+  return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
+}
+
+int ensure_shape_scratch(sfx_form_s& f) {
+  const size_t ne = size_t(f.ne) * size_t(f.NPE) * 3;
+  if (f.eshape.n < ne && f.eshape.alloc(ne) != cudaSuccess) return fail(SFX_ERR_NOMEM, "shape scratch");
+  size_t nf = 0;
+  const size_t npf = size_t(f.p + 1) * size_t(f.p + 1) * 3;
+  for (const auto& bi : f.boundary) nf = std::max(nf, size_t(bi.num_faces) * npf);
+  for (const auto& bi : f.qoi_boundary) nf = std::max(nf, size_t(bi.num_faces) * npf);
+  if (f.efshape.n < nf && f.efshape.alloc(nf) != cudaSuccess) return fail(SFX_ERR_NOMEM, "face shape scratch");
+  return SFX_OK;
+}
+
 }  // namespace sfx_impl
 
 using namespace sfx_impl;
@@ -231,6 +248,20 @@ int sfx_shape_jvp(sfx_form form, double t, const double* u, const double* dshape
   return sfx_impl::launch_boundary_shape_jvp(*form, u, dshape, dr, t, s);
 }
 
+int sfx_shape_vjp(sfx_form form, double t, const double* u, const double* lam, double* out, void* stream) {
+  if (check_form(form)) return SFX_ERR_INVALID;
+  if (!u || !lam || !out) return fail(SFX_ERR_INVALID, "null vector");
+  if (form->qoi) return fail(SFX_ERR_INVALID, "a quantity of interest takes sfx_qoi_shape_gradient");
+  if (int rc = ensure_shape_scratch(*form)) return rc;
+  auto s = static_cast<cudaStream_t>(stream);
+  if (form->domain.empty()) SFX_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double) * size_t(3 * form->nnodes), s));
+  for (size_t i = 0; i < form->domain.size(); i++) {
+    if (int rc = sfx_impl::launch_shape_vjp(*form, form->domain[i], u, lam, form->eshape.p, t, s)) return rc;
+    if (int rc2 = scatter_evector3(*form, form->eshape.p, out, i > 0, s)) return rc2;
+  }
+  return sfx_impl::launch_boundary_shape_vjp(*form, u, lam, out, t, s);
+}
+
 int sfx_form_destroy(sfx_form form) {
   delete form;
   return SFX_OK;
@@ -379,6 +410,10 @@ int sfx_jvp_transpose_f32(sfx_form form, const float* v, float* dr, void* stream
   if (!form->linearized) return fail(SFX_ERR_INVALID, "sfx_linearize must be called before sfx_jvp_transpose_f32");
   if (!form->domain.empty() && form->jvp_mode != SFX_JVP_STORED_TANGENT)
     return fail(SFX_ERR_UNSUPPORTED, "the transposed action needs the stored tangent (SFX_JVP_STORED_TANGENT)");
+  if (form->wait_error.raised()) {
+    form->wait_error.clear();
+    return fail(SFX_ERR_TIMEOUT, "a bulk-copy wait of an earlier FP32 Jacobian action expired");
+  }
   auto s = static_cast<cudaStream_t>(stream);
   if (form->domain.empty()) SFX_CUDA_TRY(cudaMemsetAsync(dr, 0, sizeof(float) * size_t(form->ndofs), s));
   for (size_t i = 0; i < form->domain.size(); i++) {

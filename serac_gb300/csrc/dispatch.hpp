@@ -35,6 +35,16 @@ int launch_shape_jvp(const sfx_form_s& f, const DomainIntegral& di, const double
 // out += derivative of the boundary residual with respect to the shape displacement, applied to dshape
 int launch_boundary_shape_jvp(const sfx_form_s& f, const double* u, const double* dshape, double* out, double t,
                               cudaStream_t s);
+// shape sensitivities: (dR/dp)^T lam of the domain integral as an E-vector
+// [e][3][node]; the boundary integrals' part added into out (3 x num_nodes)
+int launch_shape_vjp(const sfx_form_s& f, const DomainIntegral& di, const double* u, const double* lam, double* E,
+                     double t, cudaStream_t s);
+int launch_boundary_shape_vjp(const sfx_form_s& f, const double* u, const double* lam, double* out, double t,
+                              cudaStream_t s);
+// scatter-add of a 3-component E-vector [e][3][node] (shape space)
+int scatter_evector3(const sfx_form_s& f, const double* E, double* out, bool accumulate, cudaStream_t s);
+// E-vector scratch of the shape-space kernels (elements and the largest face set)
+int ensure_shape_scratch(sfx_form_s& f);
 // geometric factors (reference or shape-displaced configuration)
 int compute_face_geometry(sfx_form_s& f, BoundaryIntegral& bi, cudaStream_t s);
 int compute_geometry(sfx_form_s& f, cudaStream_t s);

@@ -10,6 +10,7 @@
 #include "form.hpp"
 #include "sfx/kernels.cuh"
 #include "sfx/materials.hpp"
+#include "sfx/sensitivity.cuh"
 
 namespace sfx_impl {
 namespace {
@@ -183,6 +184,40 @@ struct LinearizeFn {
   }
 };
 
+// Bulk-copy staged FP32 action for Q2 (J, or J^T when TRANSPOSE): one
+// persistent block per SM with as many warps as fit two-deep rings in 220 KB
+// of shared memory, rings up to 4 deep.
+template <int C, bool HS, bool VI, bool TRANSPOSE>
+int launch_tma(const sfx_form_s& f, const float* du, const float* D, float* E, cudaStream_t s) {
+  constexpr int NQ = 27;
+  using Shape = kernels::TangentShape<C, HS, VI>;
+  constexpr size_t kSmemBudget = 220 * 1024;
+  constexpr size_t stage_bytes = size_t(Shape::template stride<NQ>) * 4 + 8;
+  constexpr int WARPS = 16 * 2 * stage_bytes <= kSmemBudget   ? 16
+                        : 12 * 2 * stage_bytes <= kSmemBudget ? 12
+                        : 8 * 2 * stage_bytes <= kSmemBudget  ? 8
+                                                              : 4;
+  constexpr int STAGES = int(std::min<size_t>(4, kSmemBudget / (WARPS * stage_bytes)));
+  static_assert(STAGES >= 2, "tangent block too large for a two-stage ring");
+  constexpr size_t smem = size_t(WARPS) * STAGES * stage_bytes;
+  auto kern = kernels::jvp_stored_tma_kernel<C, HS, VI, WARPS, STAGES, TRANSPOSE>;
+  static bool configured = false;  // per instantiation
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("bulk jvp attribute: ") + cudaGetErrorString(e));
+    configured = true;
+  }
+  static int sms = 0;  // SM count, queried once (this launch may sit inside a stream capture)
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  const int64_t blocks = std::min<int64_t>((f.ne + WARPS - 1) / WARPS, std::max(sms, 1));
+  kern<<<unsigned(blocks), WARPS * 32, smem, s>>>(du, D, f.conn.p, E, f.nnodes, f.ne, f.wait_error.dev);
+  return SFX_OK;
+}
+
 template <int P, typename Real>
 struct StoredJvpFn {
   const sfx_form_s& f;
@@ -199,33 +234,7 @@ struct StoredJvpFn {
     constexpr bool HS = kernels::tangent_has_source<C, State, QF>();
     if (f.ne == 0) return SFX_OK;
     if constexpr (P == 2 && std::is_same<Real, float>::value) {
-      // bulk-copy staged kernel: one persistent block per SM with as many warps
-      // as fit two-deep rings in 220 KB of shared memory, rings up to 4 deep
-      using Shape = kernels::TangentShape<C, HS, Maker::value_input>;
-      constexpr size_t kSmemBudget = 220 * 1024;
-      constexpr size_t stage_bytes = size_t(Shape::template stride<NQ>) * 4 + 8;
-      constexpr int WARPS = 16 * 2 * stage_bytes <= kSmemBudget   ? 16
-                            : 12 * 2 * stage_bytes <= kSmemBudget ? 12
-                            : 8 * 2 * stage_bytes <= kSmemBudget  ? 8
-                                                                  : 4;
-      constexpr int STAGES = int(std::min<size_t>(4, kSmemBudget / (WARPS * stage_bytes)));
-      static_assert(STAGES >= 2, "tangent block too large for a two-stage ring");
-      constexpr size_t smem = size_t(WARPS) * STAGES * stage_bytes;
-      auto kern = kernels::jvp_stored_tma_kernel<C, HS, Maker::value_input, WARPS, STAGES>;
-      static bool configured = false;  // per instantiation
-      if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        if (e != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("bulk jvp attribute: ") + cudaGetErrorString(e));
-        configured = true;
-      }
-      static int sms = 0;  // SM count, queried once (this launch may sit inside a stream capture)
-      if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-      }
-      const int64_t blocks = std::min<int64_t>((f.ne + WARPS - 1) / WARPS, std::max(sms, 1));
-      kern<<<unsigned(blocks), WARPS * 32, smem, s>>>(du, D, f.conn.p, E, f.nnodes, f.ne, f.wait_error.dev);
+      if (int rc = launch_tma<C, HS, Maker::value_input, false>(f, du, D, E, s)) return rc;
     } else {
       int64_t warps = (f.ne + EPW - 1) / EPW;
       int64_t blocks = (warps * 32 + 127) / 128;
@@ -252,10 +261,14 @@ struct StoredJvpTransposeFn {
     using QF = decltype(Maker{}(nullptr));
     constexpr bool HS = kernels::tangent_has_source<C, State, QF>();
     if (f.ne == 0) return SFX_OK;
-    const int64_t warps = (f.ne + EPW - 1) / EPW;
-    const int64_t blocks = (warps * 32 + 127) / 128;
-    kernels::jvp_stored_transpose_kernel<P, C, HS, Maker::value_input, Real>
-        <<<unsigned(blocks), 128, 0, s>>>(v, D, f.conn.p, E, f.nnodes, f.ne);
+    if constexpr (P == 2 && std::is_same<Real, float>::value) {
+      if (int rc = launch_tma<C, HS, Maker::value_input, true>(f, v, D, E, s)) return rc;
+    } else {
+      const int64_t warps = (f.ne + EPW - 1) / EPW;
+      const int64_t blocks = (warps * 32 + 127) / 128;
+      kernels::jvp_stored_transpose_kernel<P, C, HS, Maker::value_input, Real>
+          <<<unsigned(blocks), 128, 0, s>>>(v, D, f.conn.p, E, f.nnodes, f.ne);
+    }
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("transposed jvp launch: ") + cudaGetErrorString(err));
     return SFX_OK;
@@ -312,6 +325,40 @@ struct ShapeJvpFn {
   }
 };
 }  // namespace
+
+namespace {
+template <int P>
+struct ShapeVjpFn {
+  const sfx_form_s& f;
+  const DomainIntegral& di;
+  const double* u;
+  const double* lam;
+  double* E;
+  double t;
+  cudaStream_t s;
+  template <int C, typename State, typename Maker>
+  int operator()() {
+    constexpr int NQ = (P + 1) * (P + 1) * (P + 1);
+    constexpr int EPW = 32 / NQ;
+    if (f.ne == 0) return SFX_OK;
+    kernels::DomainArgs<double> a{u, nullptr, nullptr, f.conn.p, nullptr, di.state.p, di.params.p, f.nnodes, f.ne, t};
+    const int64_t warps = (f.ne + EPW - 1) / EPW;
+    const int64_t blocks = (warps * 32 + 127) / 128;
+    kernels::shape_adjoint_kernel<P, C, kernels::SHAPE_VJP, State, Maker><<<unsigned(blocks), 128, 0, s>>>(
+        a, Maker{}, f.Xe.p, f.has_shape ? f.shape.p : nullptr, lam, E);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("shape vjp launch: ") + cudaGetErrorString(err));
+    return SFX_OK;
+  }
+};
+}  // namespace
+
+int launch_shape_vjp(const sfx_form_s& f, const DomainIntegral& di, const double* u, const double* lam, double* E,
+                     double t, cudaStream_t s) {
+  if (f.p == 1) return visit_material(di.material, ShapeVjpFn<1>{f, di, u, lam, E, t, s});
+  if (f.p == 2) return visit_material(di.material, ShapeVjpFn<2>{f, di, u, lam, E, t, s});
+  return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
+}
 
 int launch_shape_jvp(const sfx_form_s& f, const DomainIntegral& di, const double* u, const double* dshape, double* E,
                      double t, cudaStream_t s) {

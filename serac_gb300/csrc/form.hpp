@@ -159,6 +159,9 @@ struct sfx_form_s {
   std::vector<sfx_impl::BoundaryIntegral> qoi_boundary;  // material = QoI kind
   sfx_impl::DeviceBuf<double> qoi_vals;
   sfx_impl::DeviceBuf<double> qoi_partial;
+  // shape-sensitivity E-vectors [e][3][node] and [face][3][node]
+  sfx_impl::DeviceBuf<double> eshape;
+  sfx_impl::DeviceBuf<double> efshape;
   // CSR graph (built on first request)
   bool csr_built = false;
   int64_t nnz = 0;

@@ -13,6 +13,7 @@
 #include "form.hpp"
 #include "sfx.h"
 #include "sfx/qoi.cuh"
+#include "sfx/sensitivity.cuh"
 
 using namespace sfx_impl;
 
@@ -124,6 +125,74 @@ struct FaceQoiFn {
   }
 };
 
+// adapts a QoI integrand to the per-element maker interface of the shape kernels
+template <typename QF>
+struct QoiMaker {
+  QF qf;
+  static constexpr int nparams = 0;
+  SFX_HD QF operator()(const double*) const { return qf; }
+};
+
+template <int P, int C>
+struct DomainQoiShapeFn {
+  const sfx_form_s& f;
+  const double* u;
+  double t;
+  cudaStream_t s;
+  template <typename QF>
+  int operator()(const QF& qf) {
+    constexpr int NQ = (P + 1) * (P + 1) * (P + 1);
+    constexpr int EPW = 32 / NQ;
+    if (f.ne == 0) return SFX_OK;
+    kernels::DomainArgs<double> a{u, nullptr, nullptr, f.conn.p, nullptr, nullptr, nullptr, f.nnodes, f.ne, t};
+    const int64_t warps = (f.ne + EPW - 1) / EPW;
+    kernels::shape_adjoint_kernel<P, C, kernels::SHAPE_QOI, Nothing, QoiMaker<QF>>
+        <<<unsigned((warps * 32 + 127) / 128), 128, 0, s>>>(a, QoiMaker<QF>{qf}, f.Xe.p,
+                                                            f.has_shape ? f.shape.p : nullptr, nullptr, f.eshape.p);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("QoI shape launch: ") + cudaGetErrorString(err));
+    return SFX_OK;
+  }
+};
+
+template <int P, int C>
+struct FaceQoiShapeFn {
+  const sfx_form_s& f;
+  const BoundaryIntegral& bi;
+  const double* u;
+  double* out;
+  double t;
+  cudaStream_t s;
+  template <typename QF>
+  int operator()(const QF& qf) {
+    constexpr int NQ = (P + 1) * (P + 1);
+    constexpr int FPW = 32 / NQ;
+    if (bi.num_faces == 0) return SFX_OK;
+    kernels::FaceArgs<double> a{u, nullptr, f.efshape.p, bi.fconn.p, bi.fgeom.p, f.nnodes, bi.num_faces, t};
+    const int64_t warps = (bi.num_faces + FPW - 1) / FPW;
+    kernels::face_shape_adjoint_kernel<P, C, kernels::SHAPE_QOI, QF><<<unsigned((warps * 32 + 127) / 128), 128, 0, s>>>(
+        a, qf, bi.Xf.p, f.has_shape ? f.shape.p : nullptr, nullptr);
+    kernels::face_scatter_kernel<3, NQ, double><<<unsigned((bi.num_face_nodes + 255) / 256), 256, 0, s>>>(
+        f.efshape.p, bi.node_ptr.p, bi.node_ids.p, bi.node_ent.p, out, bi.num_face_nodes, f.nnodes);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("face QoI shape launch: ") + cudaGetErrorString(err));
+    return SFX_OK;
+  }
+};
+
+template <int P, int C>
+int run_shape(sfx_form_s& f, double t, const double* u, double* out, cudaStream_t s) {
+  if (int rc = ensure_shape_scratch(f)) return rc;
+  SFX_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double) * size_t(3 * f.nnodes), s));
+  for (const auto& qi : f.qoi_domain) {
+    if (int rc = visit_domain_qoi<C>(qi, DomainQoiShapeFn<P, C>{f, u, t, s})) return rc;
+    if (int rc = scatter_evector3(f, f.eshape.p, out, true, s)) return rc;
+  }
+  for (const auto& bi : f.qoi_boundary)
+    if (int rc = visit_face_qoi<C>(bi, FaceQoiShapeFn<P, C>{f, bi, u, out, t, s})) return rc;
+  return SFX_OK;
+}
+
 int check_qoi(sfx_form f) {
   if (!f) return fail(SFX_ERR_INVALID, "null form");
   if (!f->qoi) return fail(SFX_ERR_INVALID, "not a quantity of interest (create it with sfx_qoi_create)");
@@ -222,6 +291,19 @@ int sfx_qoi_gradient(sfx_form qoi, double t, const double* u, double* value, dou
   if (int rc = check_qoi(qoi)) return rc;
   if (!u || !grad) return fail(SFX_ERR_INVALID, "null argument");
   return dispatch<kernels::QOI_GRADIENT>(*qoi, t, u, nullptr, grad, value, static_cast<cudaStream_t>(stream));
+}
+
+int sfx_qoi_shape_gradient(sfx_form qoi, double t, const double* u, double* out, void* stream) {
+  if (int rc = check_qoi(qoi)) return rc;
+  if (!u || !out) return fail(SFX_ERR_INVALID, "null argument");
+  if (qoi->qoi_domain.empty() && qoi->qoi_boundary.empty()) return fail(SFX_ERR_INVALID, "no integrals");
+  auto s = static_cast<cudaStream_t>(stream);
+  sfx_form_s& f = *qoi;
+  if (f.p == 1 && f.c == 1) return run_shape<1, 1>(f, t, u, out, s);
+  if (f.p == 1 && f.c == 3) return run_shape<1, 3>(f, t, u, out, s);
+  if (f.p == 2 && f.c == 1) return run_shape<2, 1>(f, t, u, out, s);
+  if (f.p == 2 && f.c == 3) return run_shape<2, 3>(f, t, u, out, s);
+  return fail(SFX_ERR_UNSUPPORTED, "unsupported (order, components)");
 }
 
 int sfx_qoi_action(sfx_form qoi, double t, const double* u, const double* du, double* out, void* stream) {

@@ -342,6 +342,17 @@ class ShapeGradient:
 
     Mult = mult
 
+    def mult_transpose(self, lam, out=None, stream=None):
+        """(dR/dp)^T lam (3 * num_nodes): the adjoint shape sensitivity
+        (computeTimestepShapeSensitivity, solid_mechanics.hpp:1421-1431)."""
+        f = self.functional
+        _require(lam, torch.float64, f.ndofs, "lam")
+        out = torch.empty(3 * f.num_nodes, dtype=torch.float64, device=lam.device) if out is None else out
+        _lib.call("sfx_shape_vjp", f._h, float(self.t), _dptr(self.u), _dptr(lam), _dptr(out), _stream(stream))
+        return out
+
+    MultTranspose = mult_transpose
+
     def __call__(self, dshape):
         return self.mult(dshape)
 
@@ -489,6 +500,14 @@ class QoI:
         else:
             _require(shape, torch.float64, 3 * self.num_nodes, "shape")
             _lib.call("sfx_form_set_shape_displacement", self._h, _dptr(shape), _stream(stream))
+
+    def shape_gradient(self, t, u, out=None, stream=None):
+        """dQ/dp (3 * num_nodes): the partial derivative with respect to the
+        shape displacement at the current shape."""
+        _require(u, torch.float64, self.ndofs, "u")
+        out = torch.empty(3 * self.num_nodes, dtype=torch.float64, device=u.device) if out is None else out
+        _lib.call("sfx_qoi_shape_gradient", self._h, float(t), _dptr(u), _dptr(out), _stream(stream))
+        return out
 
     def value(self, t, u, out=None, stream=None):
         """Q(t, u) as a one-element float64 CUDA tensor (no host synchronisation)."""

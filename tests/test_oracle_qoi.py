@@ -96,3 +96,25 @@ def test_jvp_transpose_is_the_adjoint():
     assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
     A = f.assemble(u)
     assert abs(A - A.T).max() > 1e-3  # the operator really is non-symmetric
+
+
+@pytest.mark.parametrize("p", [1, 2])
+def test_shape_gradient_of_measures(p):
+    """d(volume)/dp and d(area)/dp by finite differences: a uniform dilation
+    p = eps X changes the volume at rate 3 V and the area at rate 2 A, a
+    translation changes neither."""
+    m = mesh(2, 2, 1, perturb=0.2, seed=3)
+    X = m.node_coordinates(p)
+    dil = np.concatenate([X[:, 0], X[:, 1], X[:, 2]])
+    trans = np.concatenate([np.full(len(X), 0.3), np.full(len(X), -0.1), np.full(len(X), 0.2)])
+    u = np.zeros(m.num_nodes(p))
+    vol = O.OracleQoI(m, p, 1)
+    vol.add_domain_integral(O.QOI_MEASURE)
+    gv = vol.shape_gradient_fd(u)
+    assert abs(gv @ dil - 3.0) <= 1e-7
+    assert abs(gv @ trans) <= 1e-7
+    area = O.OracleQoI(m, p, 1)
+    area.add_boundary_integral(O.QOI_MEASURE, ALL_SIDES)
+    ga = area.shape_gradient_fd(u)
+    assert abs(ga @ dil - 12.0) <= 1e-7
+    assert abs(ga @ trans) <= 1e-7
