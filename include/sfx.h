@@ -13,6 +13,7 @@
  * Reference interface each entry point replaces (serac, src/serac/...):
  *   sfx_mesh_create_structured_hex  mesh/mesh_utils.cpp:149-153 buildCuboidMesh (+ EnsureNodes, :466)
  *   sfx_form_create                 numerics/functional/functional.hpp:219-273 Functional ctor
+ *   sfx_form_create_from_table      the same over an mfem element-dof table (element_restriction.cpp:216-277)
  *   sfx_form_add_domain_integral    numerics/functional/functional.hpp:286-317 AddDomainIntegral
  *   sfx_form_add_boundary_integral  numerics/functional/functional.hpp:328-354 AddBoundaryIntegral
  *   sfx_form_set_shape_displacement numerics/functional/shape_aware_functional.hpp:45-172, 330-560
@@ -94,6 +95,23 @@ int sfx_mesh_num_elements(sfx_mesh mesh, int64_t* out);
  * (order nx + 1)(order ny + 1)(order nz + 1) grid is I + Nx (J + Ny K); the
  * vector layout is byNODES: vdof = component * num_nodes + node. */
 int sfx_form_create(sfx_mesh mesh, int order, int components, sfx_form* out);
+
+/* The same for any conforming hexahedral mesh, from an imported element-dof
+ * table (the one mfem's ParFiniteElementSpace holds for serac's H1 spaces,
+ * element_restriction.cpp:216-277, after its native -> lexicographic
+ * permutation): elem_nodes (host, num_elements x (order+1)^3 int32) gives
+ * each element's scalar node ids in lexicographic local order (x fastest),
+ * the caller's own numbering in [0, num_nodes) (vdof = component *
+ * num_nodes + node); elem_vertices (host, num_elements x 8 x 3 doubles) the
+ * element's corner coordinates in lexicographic corner order (trilinear
+ * geometry, positively oriented).  Every operator of this header works on
+ * such a form; boundaries are given as face lists
+ * (sfx_form_add_boundary_integral_faces), the CSR graph is the union of the
+ * element node sets per node (columns sorted), and results follow the
+ * caller's numbering.  For order <= 2 every edge and face carries at most
+ * one node, so no orientation data is needed. */
+int sfx_form_create_from_table(int order, int components, int64_t num_elements, int64_t num_nodes,
+                               const int32_t* elem_nodes, const double* elem_vertices, sfx_form* out);
 int sfx_form_destroy(sfx_form form);
 int sfx_form_num_dofs(sfx_form form, int64_t* out);
 
@@ -104,6 +122,12 @@ int sfx_form_add_domain_integral(sfx_form form, int material, const double* para
 
 /* Boundary integral over the faces of the sides in side_mask; params: host. */
 int sfx_form_add_boundary_integral(sfx_form form, int bmaterial, int side_mask, const double* params);
+/* The same over an explicit face list (host arrays of num_faces entries):
+ * face_elem[k] an element, face_side[k] its local side (1: zeta=0, 2: eta=0,
+ * 3: xi=1, 4: eta=1, 5: xi=0, 6: zeta=1 in the element's lexicographic frame),
+ * like mfem's boundary elements of an attribute. */
+int sfx_form_add_boundary_integral_faces(sfx_form form, int bmaterial, int64_t num_faces, const int32_t* face_elem,
+                                         const int32_t* face_side, const double* params);
 
 /* Shape displacement p (device, 3 * num_nodes doubles, byNODES on the form's
  * node grid; NULL = none): every integral of the form is evaluated on the
@@ -224,6 +248,8 @@ typedef struct {
   const int32_t* node_ent;  /* face * nodes_per_face + local, face order */
 } sfx_face_layout;
 int sfx_form_add_face_set(sfx_form form, int side_mask, int* face_set);
+int sfx_form_add_face_set_faces(sfx_form form, int64_t num_faces, const int32_t* face_elem, const int32_t* face_side,
+                                int* face_set);
 int sfx_form_get_face_layout(sfx_form form, int face_set, sfx_face_layout* out);
 
 /* out = (accumulate ? out : 0) + scatter-add of the E-vector E [e][component][node]
@@ -275,6 +301,10 @@ int sfx_residual_structured_noalloc(int nx, int ny, int nz, int order, int mater
 int sfx_qoi_create(sfx_mesh mesh, int order, int components, sfx_form* out);
 int sfx_qoi_add_domain_integral(sfx_form qoi, int kind, const double* params);
 int sfx_qoi_add_boundary_integral(sfx_form qoi, int kind, int side_mask, const double* params);
+int sfx_qoi_create_from_table(int order, int components, int64_t num_elements, int64_t num_nodes,
+                              const int32_t* elem_nodes, const double* elem_vertices, sfx_form* out);
+int sfx_qoi_add_boundary_integral_faces(sfx_form qoi, int kind, int64_t num_faces, const int32_t* face_elem,
+                                        const int32_t* face_side, const double* params);
 /* value: device, one double = Q(t, u) */
 int sfx_qoi_evaluate(sfx_form qoi, double t, const double* u, double* value, void* stream);
 /* grad: device, num_dofs doubles = dQ/du (t, u); value (device, one double)

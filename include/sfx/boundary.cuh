@@ -564,27 +564,22 @@ __global__ void face_diag_kernel(const int32_t* __restrict__ node_ptr, const int
 
 /// CSR values of the face contributions: one thread per (component, face
 /// node) row adds its faces' element-matrix entries in face order.
-template <int P, int C>
-__global__ void face_csr_kernel(GridShape g, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ fconn,
+template <int P, int C, typename Graph>
+__global__ void face_csr_kernel(Graph g, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ fconn,
                                 const int32_t* __restrict__ node_ptr, const int32_t* __restrict__ node_ids,
                                 const int32_t* __restrict__ node_ent, const double* __restrict__ Kf,
                                 double* __restrict__ values, int64_t num_face_nodes) {
   constexpr int NPF = (P + 1) * (P + 1);
   constexpr int NDOF = C * NPF;
-  const int64_t nn = g.N[0] * g.N[1] * g.N[2];
+  const int64_t nn = g.num_nodes();
   int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= num_face_nodes * C) return;
   const int ci = int(t / num_face_nodes);
   const int64_t i = t - ci * num_face_nodes;
   const int64_t node = node_ids[i];
   const int64_t r = ci * nn + node;
-  int64_t I = node % g.N[0], J = (node / g.N[0]) % g.N[1], K = node / (g.N[0] * g.N[1]);
-  int64_t l0, h0, l1, h1, l2, h2;
-  node_range(g, 0, I, l0, h0);
-  node_range(g, 1, J, l1, h1);
-  node_range(g, 2, K, l2, h2);
-  const int64_t w0 = h0 - l0 + 1, w1 = h1 - l1 + 1, w2 = h2 - l2 + 1;
-  const int64_t scalar_len = w0 * w1 * w2;
+  const auto grow = g.row(node);
+  const int64_t scalar_len = grow.len;
   double* row = values + row_ptr[r];
   for (int32_t k = node_ptr[i]; k < node_ptr[i + 1]; k++) {
     const int32_t ent = node_ent[k];
@@ -592,9 +587,7 @@ __global__ void face_csr_kernel(GridShape g, const int64_t* __restrict__ row_ptr
     const int a = ent - int(f) * NPF;
     const double* Kcol = Kf + f * NDOF * NDOF + (ci * NPF + a);
     for (int b = 0; b < NPF; b++) {
-      const int64_t nb = fconn[f * NPF + b];
-      const int64_t x = nb % g.N[0], y = (nb / g.N[0]) % g.N[1], z = nb / (g.N[0] * g.N[1]);
-      const int64_t pos = ((z - l2) * w1 + (y - l1)) * w0 + (x - l0);
+      const int64_t pos = g.pos(grow, fconn[f * NPF + b]);
 #pragma unroll
       for (int cj = 0; cj < C; cj++) row[cj * scalar_len + pos] += Kcol[int64_t(cj * NPF + b) * NDOF];
     }

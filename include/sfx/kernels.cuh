@@ -810,76 +810,105 @@ struct GridShape {
   int p;
   int64_t N[3];   // nodes per direction
   int64_t ne[3];  // elements per direction
+  struct Row {
+    int64_t lo[3], w[3], len;
+  };
+  SFX_HDI int64_t num_nodes() const { return N[0] * N[1] * N[2]; }
+  SFX_HDI void range(int d, int64_t I, int64_t& lo, int64_t& hi) const {
+    if (I % p == 0) {
+      const int64_t e = I / p;
+      lo = (e > 0) ? I - p : I;
+      hi = (e < ne[d]) ? I + p : I;
+    } else {
+      const int64_t e = I / p;
+      lo = e * p;
+      hi = e * p + p;
+    }
+  }
+  SFX_HDI Row row(int64_t node) const {
+    const int64_t I[3] = {node % N[0], (node / N[0]) % N[1], node / (N[0] * N[1])};
+    Row r{};
+    for (int d = 0; d < 3; d++) {
+      int64_t hi = 0;
+      range(d, I[d], r.lo[d], hi);
+      r.w[d] = hi - r.lo[d] + 1;
+    }
+    r.len = r.w[0] * r.w[1] * r.w[2];
+    return r;
+  }
+  /// k-th scalar column of the row (ascending node ids)
+  SFX_HDI int64_t column(const Row& r, int64_t k) const {
+    const int64_t x = r.lo[0] + k % r.w[0], y = r.lo[1] + (k / r.w[0]) % r.w[1], z = r.lo[2] + k / (r.w[0] * r.w[1]);
+    return x + N[0] * (y + N[1] * z);
+  }
+  /// position of node nb among the row's scalar columns
+  SFX_HDI int64_t pos(const Row& r, int64_t nb) const {
+    const int64_t x = nb % N[0], y = (nb / N[0]) % N[1], z = nb / (N[0] * N[1]);
+    return ((z - r.lo[2]) * r.w[1] + (y - r.lo[1])) * r.w[0] + (x - r.lo[0]);
+  }
 };
 
-SFX_HDI void node_range(const GridShape& g, int d, int64_t I, int64_t& lo, int64_t& hi) {
-  const int p = g.p;
-  if (I % p == 0) {
-    int64_t e = I / p;
-    lo = (e > 0) ? I - p : I;
-    hi = (e < g.ne[d]) ? I + p : I;
-  } else {
-    int64_t e = I / p;
-    lo = e * p;
-    hi = e * p + p;
+/// CSR graph of a form built from an imported element table: the sorted
+/// scalar adjacency (the union of the nodes of a node's elements) per node,
+/// columns located by binary search.
+struct TableGraph {
+  const int64_t* sptr;  // [num_nodes + 1]
+  const int32_t* scol;  // ascending within each row
+  int64_t nn;
+  struct Row {
+    int64_t begin, len;
+  };
+  SFX_HDI int64_t num_nodes() const { return nn; }
+  SFX_HDI Row row(int64_t node) const { return {sptr[node], sptr[node + 1] - sptr[node]}; }
+  SFX_HDI int64_t column(const Row& r, int64_t k) const { return scol[r.begin + k]; }
+  SFX_HDI int64_t pos(const Row& r, int64_t nb) const {
+    int64_t lo = 0, hi = r.len - 1;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (scol[r.begin + mid] < nb) lo = mid + 1;
+      else hi = mid;
+    }
+    return lo;
   }
-}
+};
 
-template <int C>
-__global__ void csr_row_length_kernel(GridShape g, int64_t* row_len) {
-  const int64_t nn = g.N[0] * g.N[1] * g.N[2];
+template <int C, typename Graph>
+__global__ void csr_row_length_kernel(Graph g, int64_t* row_len) {
+  const int64_t nn = g.num_nodes();
   int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (r >= nn * C) return;
-  int64_t node = r % nn;
-  int64_t I = node % g.N[0], J = (node / g.N[0]) % g.N[1], K = node / (g.N[0] * g.N[1]);
-  int64_t l0, h0, l1, h1, l2, h2;
-  node_range(g, 0, I, l0, h0);
-  node_range(g, 1, J, l1, h1);
-  node_range(g, 2, K, l2, h2);
-  row_len[r + 1] = int64_t(C) * (h0 - l0 + 1) * (h1 - l1 + 1) * (h2 - l2 + 1);
+  row_len[r + 1] = int64_t(C) * g.row(r % nn).len;
   if (r == 0) row_len[0] = 0;
 }
 
-template <int C>
-__global__ void csr_fill_kernel(GridShape g, const int64_t* __restrict__ row_ptr, int32_t* __restrict__ col) {
-  const int64_t nn = g.N[0] * g.N[1] * g.N[2];
+template <int C, typename Graph>
+__global__ void csr_fill_kernel(Graph g, const int64_t* __restrict__ row_ptr, int32_t* __restrict__ col) {
+  const int64_t nn = g.num_nodes();
   int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (r >= nn * C) return;
-  int64_t node = r % nn;
-  int64_t I = node % g.N[0], J = (node / g.N[0]) % g.N[1], K = node / (g.N[0] * g.N[1]);
-  int64_t l0, h0, l1, h1, l2, h2;
-  node_range(g, 0, I, l0, h0);
-  node_range(g, 1, J, l1, h1);
-  node_range(g, 2, K, l2, h2);
+  const auto row = g.row(r % nn);
   int64_t k = row_ptr[r];
   for (int c = 0; c < C; c++)
-    for (int64_t z = l2; z <= h2; z++)
-      for (int64_t y = l1; y <= h1; y++)
-        for (int64_t x = l0; x <= h0; x++) col[k++] = int32_t(c * nn + x + g.N[0] * (y + g.N[1] * z));
+    for (int64_t j = 0; j < row.len; j++) col[k++] = int32_t(c * nn + g.column(row, j));
 }
 
 /// values[row] = sum over the row node's elements (element order) of the
 /// element-matrix entries; one thread per row, so the order of the additions
 /// is fixed.  Ke: [e][trial vdof][test vdof].
-template <int P, int C>
-__global__ void csr_assemble_kernel(GridShape g, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ conn,
+template <int P, int C, typename Graph>
+__global__ void csr_assemble_kernel(Graph g, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ conn,
                                     const int32_t* __restrict__ node_ptr, const int32_t* __restrict__ node_ent,
                                     const double* __restrict__ Ke, int64_t e_begin, int64_t e_end,
                                     double* __restrict__ values, bool accumulate) {
   constexpr int NPE = (P + 1) * (P + 1) * (P + 1);
   constexpr int NDOF = C * NPE;
-  const int64_t nn = g.N[0] * g.N[1] * g.N[2];
+  const int64_t nn = g.num_nodes();
   int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (r >= nn * C) return;
   const int ci = int(r / nn);
   const int64_t node = r - ci * nn;
-  int64_t I = node % g.N[0], J = (node / g.N[0]) % g.N[1], K = node / (g.N[0] * g.N[1]);
-  int64_t l0, h0, l1, h1, l2, h2;
-  node_range(g, 0, I, l0, h0);
-  node_range(g, 1, J, l1, h1);
-  node_range(g, 2, K, l2, h2);
-  const int64_t w0 = h0 - l0 + 1, w1 = h1 - l1 + 1, w2 = h2 - l2 + 1;
-  const int64_t scalar_len = w0 * w1 * w2;
+  const auto grow = g.row(node);
+  const int64_t scalar_len = grow.len;
   double* row = values + row_ptr[r];
   if (!accumulate)
     for (int64_t k = 0; k < C * scalar_len; k++) row[k] = 0.0;
@@ -890,9 +919,7 @@ __global__ void csr_assemble_kernel(GridShape g, const int64_t* __restrict__ row
     const int a = ent - int(e) * NPE;
     const double* Kcol = Ke + (e - e_begin) * NDOF * NDOF + (ci * NPE + a);  // stride NDOF over trial vdofs
     for (int b = 0; b < NPE; b++) {
-      const int64_t nb = conn[e * NPE + b];
-      const int64_t x = nb % g.N[0], y = (nb / g.N[0]) % g.N[1], z = nb / (g.N[0] * g.N[1]);
-      const int64_t pos = ((z - l2) * w1 + (y - l1)) * w0 + (x - l0);
+      const int64_t pos = g.pos(grow, conn[e * NPE + b]);
 #pragma unroll
       for (int cj = 0; cj < C; cj++) row[cj * scalar_len + pos] += Kcol[int64_t(cj * NPE + b) * NDOF];
     }

@@ -202,6 +202,65 @@ class StructuredHexMesh:
         return out
 
 
+class TableHexMesh:
+    """A conforming hexahedral mesh given by an element-node table of one
+    order (lexicographic local node order, x fastest) and element corner
+    coordinates (ne, 8, 3), as imported from an H1 element-dof table
+    (element_restriction.cpp:216-277).  Faces are (element, local side)
+    pairs with the sides parametrised in the element's own frame like the
+    structured mesh's box sides."""
+
+    SIDES = StructuredHexMesh.SIDES
+
+    def __init__(self, order, elem_nodes, elem_vertices, num_nodes=None):
+        self.order = order
+        self.table = np.ascontiguousarray(elem_nodes, dtype=np.int64).reshape(-1, (order + 1) ** 3)
+        self.corners = np.ascontiguousarray(elem_vertices, dtype=np.float64).reshape(-1, 8, 3)
+        self.ne = self.table.shape[0]
+        self.nn = int(self.table.max()) + 1 if num_nodes is None else int(num_nodes)
+
+    def num_nodes(self, p):
+        assert p == self.order
+        return self.nn
+
+    def elem_nodes(self, p):
+        assert p == self.order
+        return self.table
+
+    def elem_coords(self):
+        return np.ascontiguousarray(self.corners.transpose(0, 2, 1))
+
+    def boundary_faces(self, p, faces):
+        """faces: (elem array, side array) -> face vertex coordinates (nf, 3, 4), face nodes (nf, (p+1)^2)."""
+        assert p == self.order
+        elems, sides = (np.asarray(a, dtype=np.int64).ravel() for a in faces)
+        n = p + 1
+        coords, nodes = [], []
+        for e, side in zip(elems, sides):
+            ax, hi, sa, ta = self.SIDES[int(side)]
+            cs = []
+            for b in range(2):
+                for a in range(2):
+                    bb = [0, 0, 0]
+                    bb[ax], bb[sa], bb[ta] = hi, a, b
+                    cs.append(self.corners[e, bb[0] + 2 * bb[1] + 4 * bb[2]])
+            coords.append(np.array(cs).T)
+            fn = []
+            for kt in range(n):
+                for ks in range(n):
+                    idx = [0, 0, 0]
+                    idx[ax], idx[sa], idx[ta] = (p if hi else 0), ks, kt
+                    fn.append(self.table[e, idx[0] + n * (idx[1] + n * idx[2])])
+            nodes.append(fn)
+        nf = len(nodes)
+        return (np.ascontiguousarray(np.array(coords, dtype=np.float64).reshape(nf, 3, 4)),
+                np.array(nodes, dtype=np.int64).reshape(nf, n * n))
+
+    def boundary_nodes(self, p, faces):
+        _, nodes = self.boundary_faces(p, faces)
+        return np.unique(nodes.ravel())
+
+
 def box_vertices(nx, ny, nz, perturb=0.0, seed=0):
     """Unit-cube vertex grid; interior vertices moved by U(-perturb*h, perturb*h)
     per coordinate with numpy's PCG64 generator seeded by ``seed``."""

@@ -25,6 +25,7 @@ from .functional import (  # noqa: F401
     QoIGradient,
     ShapeAwareFunctional,
     ShapeGradient,
+    TableMesh,
     assemble,
     box_vertices,
     differentiate_wrt,

@@ -48,6 +48,11 @@ SIGNATURES = {
     "sfx_jvp_transpose": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "sfx_jvp_transpose_f32": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "sfx_qoi_create": (_c.c_int, [_vp, _c.c_int, _c.c_int, _vp]),
+    "sfx_form_create_from_table": (_c.c_int, [_c.c_int, _c.c_int, _c.c_int64, _c.c_int64, _vp, _vp, _vp]),
+    "sfx_qoi_create_from_table": (_c.c_int, [_c.c_int, _c.c_int, _c.c_int64, _c.c_int64, _vp, _vp, _vp]),
+    "sfx_form_add_boundary_integral_faces": (_c.c_int, [_vp, _c.c_int, _c.c_int64, _vp, _vp, _vp]),
+    "sfx_form_add_face_set_faces": (_c.c_int, [_vp, _c.c_int64, _vp, _vp, _vp]),
+    "sfx_qoi_add_boundary_integral_faces": (_c.c_int, [_vp, _c.c_int, _c.c_int64, _vp, _vp, _vp]),
     "sfx_qoi_add_domain_integral": (_c.c_int, [_vp, _c.c_int, _vp]),
     "sfx_qoi_add_boundary_integral": (_c.c_int, [_vp, _c.c_int, _c.c_int, _vp]),
     "sfx_qoi_evaluate": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp]),

@@ -8,9 +8,11 @@
 
 #include <algorithm>
 #include <string>
+#include <vector>
 
 #include "dispatch.hpp"
 #include "form.hpp"
+#include "graph.hpp"
 #include "sfx.h"
 #include "sfx/kernels.cuh"
 
@@ -18,24 +20,59 @@ using namespace sfx_impl;
 
 namespace {
 
-sfx::kernels::GridShape grid_shape(const sfx_form_s& f) {
-  sfx::kernels::GridShape g{};
-  g.p = f.p;
-  g.ne[0] = f.mesh.nx;
-  g.ne[1] = f.mesh.ny;
-  g.ne[2] = f.mesh.nz;
-  for (int d = 0; d < 3; d++) g.N[d] = int64_t(f.p) * g.ne[d] + 1;
-  return g;
+// scalar adjacency of an imported element table: for every node, the sorted
+// union of the nodes of its elements (host build, uploaded once)
+int build_table_adjacency(sfx_form f) {
+  const int64_t nn = f->nnodes;
+  const int NPE = f->NPE;
+  std::vector<int32_t> count(size_t(nn) + 1, 0);
+  for (int32_t node : f->conn_host) count[size_t(node) + 1]++;
+  for (size_t i = 1; i < count.size(); i++) count[i] += count[i - 1];
+  std::vector<int32_t> elems(f->conn_host.size());
+  {
+    std::vector<int32_t> fill(count.begin(), count.end() - 1);
+    for (size_t k = 0; k < f->conn_host.size(); k++) elems[size_t(fill[size_t(f->conn_host[k])]++)] = int32_t(k / NPE);
+  }
+  std::vector<int64_t> sptr(size_t(nn) + 1, 0);
+  std::vector<int32_t> scol;
+  scol.reserve(size_t(nn) * 27);
+  std::vector<int64_t> mark(size_t(nn), -1);
+  std::vector<int32_t> row;
+  for (int64_t n = 0; n < nn; n++) {
+    row.clear();
+    for (int32_t t = count[size_t(n)]; t < count[size_t(n) + 1]; t++) {
+      const int64_t e = elems[size_t(t)];
+      for (int b = 0; b < NPE; b++) {
+        const int32_t m = f->conn_host[size_t(e * NPE + b)];
+        if (mark[size_t(m)] != n) {
+          mark[size_t(m)] = n;
+          row.push_back(m);
+        }
+      }
+    }
+    std::sort(row.begin(), row.end());
+    scol.insert(scol.end(), row.begin(), row.end());
+    sptr[size_t(n) + 1] = int64_t(scol.size());
+  }
+  cudaError_t err;
+  if ((err = f->sptr.upload(sptr.data(), sptr.size())) != cudaSuccess ||
+      (err = f->scol.upload(scol.data(), scol.size())) != cudaSuccess)
+    return fail(SFX_ERR_CUDA, std::string("graph upload: ") + cudaGetErrorString(err));
+  return SFX_OK;
 }
 
 int build_graph(sfx_form f, cudaStream_t s) {
   if (f->csr_built) return SFX_OK;
-  const auto g = grid_shape(*f);
+  if (f->general && !f->sptr.p)
+    if (int rc = build_table_adjacency(f)) return rc;
   const int64_t rows = f->ndofs;
   SFX_CUDA_TRY(f->row_ptr.alloc(size_t(rows + 1)));
   const unsigned blocks = unsigned((rows + 255) / 256);
-  if (f->c == 1) sfx::kernels::csr_row_length_kernel<1><<<blocks, 256, 0, s>>>(g, f->row_ptr.p);
-  else sfx::kernels::csr_row_length_kernel<3><<<blocks, 256, 0, s>>>(g, f->row_ptr.p);
+  with_graph(*f, [&](auto g) {
+    if (f->c == 1) sfx::kernels::csr_row_length_kernel<1><<<blocks, 256, 0, s>>>(g, f->row_ptr.p);
+    else sfx::kernels::csr_row_length_kernel<3><<<blocks, 256, 0, s>>>(g, f->row_ptr.p);
+    return SFX_OK;
+  });
   SFX_CUDA_TRY(cudaGetLastError());
   size_t tmp_bytes = 0;
   SFX_CUDA_TRY(cub::DeviceScan::InclusiveSum(nullptr, tmp_bytes, f->row_ptr.p, f->row_ptr.p, rows + 1, s));
@@ -47,8 +84,11 @@ int build_graph(sfx_form f, cudaStream_t s) {
   SFX_CUDA_TRY(cudaStreamSynchronize(s));
   if (nnz >= (int64_t(1) << 62)) return fail(SFX_ERR_UNSUPPORTED, "nnz overflow");
   SFX_CUDA_TRY(f->col.alloc(size_t(nnz)));
-  if (f->c == 1) sfx::kernels::csr_fill_kernel<1><<<blocks, 256, 0, s>>>(g, f->row_ptr.p, f->col.p);
-  else sfx::kernels::csr_fill_kernel<3><<<blocks, 256, 0, s>>>(g, f->row_ptr.p, f->col.p);
+  with_graph(*f, [&](auto g) {
+    if (f->c == 1) sfx::kernels::csr_fill_kernel<1><<<blocks, 256, 0, s>>>(g, f->row_ptr.p, f->col.p);
+    else sfx::kernels::csr_fill_kernel<3><<<blocks, 256, 0, s>>>(g, f->row_ptr.p, f->col.p);
+    return SFX_OK;
+  });
   SFX_CUDA_TRY(cudaGetLastError());
   f->nnz = nnz;
   f->csr_built = true;
@@ -58,10 +98,12 @@ int build_graph(sfx_form f, cudaStream_t s) {
 template <int P, int C>
 int assemble_chunk(sfx_form f, const double* Ke, int64_t e0, int64_t e1, double* values, bool accumulate,
                    cudaStream_t s) {
-  const auto g = grid_shape(*f);
   const unsigned blocks = unsigned((f->ndofs + 127) / 128);
-  sfx::kernels::csr_assemble_kernel<P, C><<<blocks, 128, 0, s>>>(g, f->row_ptr.p, f->conn.p, f->node_ptr.p,
-                                                                 f->node_ent.p, Ke, e0, e1, values, accumulate);
+  with_graph(*f, [&](auto g) {
+    sfx::kernels::csr_assemble_kernel<P, C><<<blocks, 128, 0, s>>>(g, f->row_ptr.p, f->conn.p, f->node_ptr.p,
+                                                                   f->node_ent.p, Ke, e0, e1, values, accumulate);
+    return SFX_OK;
+  });
   SFX_CUDA_TRY(cudaGetLastError());
   return SFX_OK;
 }

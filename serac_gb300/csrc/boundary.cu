@@ -13,6 +13,7 @@
 
 #include "dispatch.hpp"
 #include "form.hpp"
+#include "graph.hpp"
 #include "sfx.h"
 #include "sfx/boundary.cuh"
 #include "sfx/materials.hpp"
@@ -130,14 +131,12 @@ struct FaceMatrixFn {
     const int64_t warps = (bi.num_faces + FPW - 1) / FPW;
     kernels::face_matrix_kernel<P, C, QF><<<unsigned((warps * 32 + 127) / 128), 128, 0, s>>>(a, qf);
     if (values) {
-      kernels::GridShape g{};
-      g.p = f.p;
-      g.ne[0] = f.mesh.nx;
-      g.ne[1] = f.mesh.ny;
-      g.ne[2] = f.mesh.nz;
-      for (int d = 0; d < 3; d++) g.N[d] = int64_t(f.p) * g.ne[d] + 1;
-      kernels::face_csr_kernel<P, C><<<unsigned((bi.num_face_nodes * C + 127) / 128), 128, 0, s>>>(
-          g, f.row_ptr.p, bi.fconn.p, bi.node_ptr.p, bi.node_ids.p, bi.node_ent.p, f.kf.p, values, bi.num_face_nodes);
+      with_graph(f, [&](auto g) {
+        kernels::face_csr_kernel<P, C><<<unsigned((bi.num_face_nodes * C + 127) / 128), 128, 0, s>>>(
+            g, f.row_ptr.p, bi.fconn.p, bi.node_ptr.p, bi.node_ids.p, bi.node_ent.p, f.kf.p, values,
+            bi.num_face_nodes);
+        return SFX_OK;
+      });
     }
     if (diag) {
       kernels::face_diag_kernel<C, NQ><<<unsigned((bi.num_face_nodes + 255) / 256), 256, 0, s>>>(
@@ -305,7 +304,12 @@ int assemble_boundary(sfx_form_s& f, double* values, double* diag, cudaStream_t 
 namespace sfx_impl {
 // faces of the sides in side_mask: connectivity (outward (s, t) order), vertex
 // coordinates, compact face-node map, geometric factors, face scratch
+int finish_faces(sfx_form_s* form, const std::vector<int32_t>& fconn, const std::vector<double>& Xf,
+                 BoundaryIntegral& bi);
+
 int build_faces(sfx_form_s* form, int side_mask, BoundaryIntegral& bi) {
+  if (form->general)
+    return fail(SFX_ERR_INVALID, "side masks need a structured mesh; give faces as (element, side) pairs");
   if (side_mask <= 0 || side_mask >= 64) return fail(SFX_ERR_INVALID, "side mask must select sides 1..6");
   const auto& m = form->mesh;
   const int p = form->p, n = p + 1, npf = n * n;
@@ -338,6 +342,61 @@ int build_faces(sfx_form_s* form, int side_mask, BoundaryIntegral& bi) {
           }
       }
   }
+  return finish_faces(form, fconn, Xf, bi);
+}
+
+// faces (element, local side) of an imported element table: the face nodes
+// and vertices in the element's own frame, parametrised like the box sides
+// (J_s x J_t points out of the element for a positively oriented element)
+int build_faces_list(sfx_form_s* form, int64_t n, const int32_t* face_elem, const int32_t* face_side,
+                     BoundaryIntegral& bi) {
+  if (n > 0 && (!face_elem || !face_side)) return fail(SFX_ERR_INVALID, "null face list");
+  if (form->conn_host.empty()) {  // structured form: host copies of its tables, once
+    form->conn_host.resize(size_t(form->ne) * form->NPE);
+    form->Xe_host.resize(size_t(form->ne) * 24);
+    SFX_CUDA_TRY(cudaMemcpy(form->conn_host.data(), form->conn.p, form->conn_host.size() * sizeof(int32_t),
+                            cudaMemcpyDeviceToHost));
+    SFX_CUDA_TRY(cudaMemcpy(form->Xe_host.data(), form->Xe.p, form->Xe_host.size() * sizeof(double),
+                            cudaMemcpyDeviceToHost));
+  }
+  const int p = form->p, nn1 = p + 1;
+  std::vector<int32_t> fconn;
+  std::vector<double> Xf;
+  fconn.reserve(size_t(n) * nn1 * nn1);
+  Xf.reserve(size_t(n) * 12);
+  for (int64_t k = 0; k < n; k++) {
+    const int64_t e = face_elem[k];
+    const int side = face_side[k];
+    if (e < 0 || e >= form->ne) return fail(SFX_ERR_INVALID, "face element out of range");
+    if (side < 1 || side > 6) return fail(SFX_ERR_INVALID, "face side must be 1..6");
+    const Side sd = kSides[side];
+    for (int i = 0; i < 3; i++)
+      for (int v = 0; v < 4; v++) {
+        int b[3] = {0, 0, 0};
+        b[sd.axis] = sd.hi;
+        b[sd.s_axis] = v & 1;
+        b[sd.t_axis] = v >> 1;
+        const int corner = b[0] + 2 * b[1] + 4 * b[2];
+        Xf.push_back(form->Xe_host[size_t(e * 24 + i * 8 + corner)]);
+      }
+    for (int kt = 0; kt < nn1; kt++)
+      for (int ks = 0; ks < nn1; ks++) {
+        int idx[3] = {0, 0, 0};
+        idx[sd.axis] = sd.hi ? p : 0;
+        idx[sd.s_axis] = ks;
+        idx[sd.t_axis] = kt;
+        const int local = idx[0] + nn1 * (idx[1] + nn1 * idx[2]);
+        fconn.push_back(form->conn_host[size_t(e * form->NPE + local)]);
+      }
+  }
+  return finish_faces(form, fconn, Xf, bi);
+}
+
+// compact face-node map, device tables, geometric factors and face scratch of
+// the faces fconn [f][(p+1)^2] with vertices Xf [f][3][4]
+int finish_faces(sfx_form_s* form, const std::vector<int32_t>& fconn, const std::vector<double>& Xf,
+                 BoundaryIntegral& bi) {
+  const int p = form->p, npf = (p + 1) * (p + 1);
   bi.num_faces = int64_t(fconn.size()) / npf;
   // compact face-node map: distinct nodes ascending, entries in face order
   std::vector<int32_t> order(fconn.size());
@@ -388,6 +447,34 @@ extern "C" int sfx_form_add_boundary_integral(sfx_form form, int bmaterial, int 
   bi.params.assign(params, params + np);
   if (int rc = build_faces(form, side_mask, bi)) return rc;
   form->boundary.push_back(std::move(bi));
+  return SFX_OK;
+}
+
+extern "C" int sfx_form_add_boundary_integral_faces(sfx_form form, int bmaterial, int64_t num_faces,
+                                                    const int32_t* face_elem, const int32_t* face_side,
+                                                    const double* params) {
+  if (!form) return fail(SFX_ERR_INVALID, "null form");
+  int comps = 0, np = 0;
+  if (int rc = bmaterial_info(bmaterial, &comps, &np)) return rc;
+  if (comps != form->c) return fail(SFX_ERR_INVALID, "boundary material component count does not match the space");
+  if (form->qoi) return fail(SFX_ERR_INVALID, "a quantity of interest takes sfx_qoi_add_boundary_integral_faces");
+  if (!params) return fail(SFX_ERR_INVALID, "null parameters");
+  BoundaryIntegral bi;
+  bi.material = bmaterial;
+  bi.params.assign(params, params + np);
+  if (int rc = build_faces_list(form, num_faces, face_elem, face_side, bi)) return rc;
+  form->boundary.push_back(std::move(bi));
+  return SFX_OK;
+}
+
+extern "C" int sfx_form_add_face_set_faces(sfx_form form, int64_t num_faces, const int32_t* face_elem,
+                                           const int32_t* face_side, int* face_set) {
+  if (!form || !face_set) return fail(SFX_ERR_INVALID, "null argument");
+  BoundaryIntegral bi;
+  bi.material = -1;
+  if (int rc = build_faces_list(form, num_faces, face_elem, face_side, bi)) return rc;
+  form->face_sets.push_back(std::move(bi));
+  *face_set = int(form->face_sets.size()) - 1;
   return SFX_OK;
 }
 

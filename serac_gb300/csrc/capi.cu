@@ -107,6 +107,45 @@ int compute_geometry(sfx_form_s& f, cudaStream_t s) {
   SFX_CUDA_TRY(cudaGetLastError());
   return SFX_OK;
 }
+// sizes, node -> element map, device tables and geometric factors of a new
+// form from its element table conn [e][NPE] and vertex coordinates Xe [e][3][8]
+int init_form(sfx_form_s* f, int order, int components, int64_t ne, int64_t nnodes, const std::vector<int32_t>& conn,
+              const std::vector<double>& Xe) {
+  f->p = order;
+  f->c = components;
+  f->Q = order + 1;
+  f->NQ = f->Q * f->Q * f->Q;
+  f->NPE = (order + 1) * (order + 1) * (order + 1);
+  f->ne = ne;
+  f->nnodes = nnodes;
+  f->ndofs = nnodes * components;
+  std::vector<int32_t> count(size_t(nnodes) + 1, 0);
+  for (int32_t node : conn) count[size_t(node) + 1]++;
+  for (size_t i = 1; i < count.size(); i++) count[i] += count[i - 1];
+  std::vector<int32_t> ent(conn.size());
+  {
+    std::vector<int32_t> fill(count.begin(), count.end() - 1);
+    for (size_t k = 0; k < conn.size(); k++) ent[size_t(fill[size_t(conn[k])]++)] = int32_t(k);
+  }
+  cudaError_t err;
+  if ((err = f->wait_error.init()) != cudaSuccess || (err = f->conn.upload(conn.data(), conn.size())) != cudaSuccess ||
+      (err = f->node_ptr.upload(count.data(), count.size())) != cudaSuccess ||
+      (err = f->node_ent.upload(ent.data(), ent.size())) != cudaSuccess)
+    return fail(SFX_ERR_CUDA, std::string("upload tables: ") + cudaGetErrorString(err));
+  const int64_t nqt = f->ne * f->NQ;
+  if ((err = f->Xe.upload(Xe.data(), Xe.size())) != cudaSuccess ||
+      (err = f->geom64.alloc(size_t(nqt) * sfx::kernels::GEOM_STRIDE)) != cudaSuccess ||
+      (err = f->geom32.alloc(size_t(nqt) * sfx::kernels::GEOM_STRIDE)) != cudaSuccess ||
+      (err = f->e64.alloc(size_t(f->ne) * f->NPE * components)) != cudaSuccess ||
+      (err = f->e32.alloc(size_t(f->ne) * f->NPE * components)) != cudaSuccess ||
+      (err = f->u_lin64.alloc(size_t(f->ndofs))) != cudaSuccess ||
+      (err = f->u_lin32.alloc(size_t(f->ndofs))) != cudaSuccess)
+    return fail(SFX_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(err));
+  if (int rc = compute_geometry(*f, nullptr)) return rc;
+  if ((err = cudaDeviceSynchronize()) != cudaSuccess)
+    return fail(SFX_ERR_CUDA, std::string("geometry kernel: ") + cudaGetErrorString(err));
+  return SFX_OK;
+}
 }  // namespace sfx_impl
 
 extern "C" {
@@ -151,74 +190,64 @@ int sfx_form_create(sfx_mesh mesh, int order, int components, sfx_form* out) {
   auto* f = new (std::nothrow) sfx_form_s;
   if (!f) return fail(SFX_ERR_NOMEM, "host allocation failed");
   f->mesh = *mesh;
-  f->p = order;
-  f->c = components;
-  f->Q = order + 1;
-  f->NQ = f->Q * f->Q * f->Q;
-  f->NPE = (order + 1) * (order + 1) * (order + 1);
   const int nx = mesh->nx, ny = mesh->ny, nz = mesh->nz, p = order, n = order + 1;
-  f->ne = int64_t(nx) * ny * nz;
   const int64_t Nx = int64_t(p) * nx + 1, Ny = int64_t(p) * ny + 1, Nz = int64_t(p) * nz + 1;
-  f->nnodes = Nx * Ny * Nz;
-  f->ndofs = f->nnodes * components;
-
-  // element -> node table (lexicographic local order) and node -> (element, local) map
-  std::vector<int32_t> conn(size_t(f->ne) * f->NPE);
-  std::vector<int32_t> count(size_t(f->nnodes) + 1, 0);
-  for (int64_t e = 0; e < f->ne; e++) {
+  const int64_t ne = int64_t(nx) * ny * nz, npe = int64_t(n) * n * n;
+  // element -> node table (lexicographic local order)
+  std::vector<int32_t> conn(size_t(ne * npe));
+  for (int64_t e = 0; e < ne; e++) {
     int64_t ex = e % nx, ey = (e / nx) % ny, ez = e / (int64_t(nx) * ny);
     for (int kz = 0; kz < n; kz++)
       for (int ky = 0; ky < n; ky++)
         for (int kx = 0; kx < n; kx++) {
           int64_t node = (p * ex + kx) + Nx * ((p * ey + ky) + Ny * (p * ez + kz));
-          conn[size_t(e * f->NPE + kx + n * (ky + n * kz))] = int32_t(node);
-          count[size_t(node) + 1]++;
+          conn[size_t(e * npe + kx + n * (ky + n * kz))] = int32_t(node);
         }
   }
-  for (size_t i = 1; i < count.size(); i++) count[i] += count[i - 1];
-  std::vector<int32_t> ent(size_t(f->ne) * f->NPE);
-  {
-    std::vector<int32_t> fill(count.begin(), count.end() - 1);
-    for (int64_t e = 0; e < f->ne; e++)
-      for (int a = 0; a < f->NPE; a++) {
-        int32_t node = conn[size_t(e * f->NPE + a)];
-        ent[size_t(fill[size_t(node)]++)] = int32_t(e * f->NPE + a);
-      }
-  }
   // element vertex coordinates [e][3][8]
-  std::vector<double> Xe(size_t(f->ne) * 24);
-  for (int64_t e = 0; e < f->ne; e++) {
+  std::vector<double> Xe(size_t(ne) * 24);
+  for (int64_t e = 0; e < ne; e++) {
     int64_t ex = e % nx, ey = (e / nx) % ny, ez = e / (int64_t(nx) * ny);
     for (int v = 0; v < 8; v++) {
       int64_t vid = (ex + (v & 1)) + int64_t(nx + 1) * ((ey + ((v >> 1) & 1)) + int64_t(ny + 1) * (ez + ((v >> 2) & 1)));
       for (int i = 0; i < 3; i++) Xe[size_t(e * 24 + i * 8 + v)] = mesh->vertices[size_t(vid * 3 + i)];
     }
   }
-  auto cleanup_fail = [&](int code, const std::string& msg) {
-    delete f;
-    return fail(code, msg);
-  };
-  cudaError_t err;
-  if ((err = f->wait_error.init()) != cudaSuccess ||
-      (err = f->conn.upload(conn.data(), conn.size())) != cudaSuccess ||
-      (err = f->node_ptr.upload(count.data(), count.size())) != cudaSuccess ||
-      (err = f->node_ent.upload(ent.data(), ent.size())) != cudaSuccess)
-    return cleanup_fail(SFX_ERR_CUDA, std::string("upload tables: ") + cudaGetErrorString(err));
-  const int64_t nqt = f->ne * f->NQ;
-  if ((err = f->Xe.upload(Xe.data(), Xe.size())) != cudaSuccess ||
-      (err = f->geom64.alloc(size_t(nqt) * sfx::kernels::GEOM_STRIDE)) != cudaSuccess ||
-      (err = f->geom32.alloc(size_t(nqt) * sfx::kernels::GEOM_STRIDE)) != cudaSuccess ||
-      (err = f->e64.alloc(size_t(f->ne) * f->NPE * components)) != cudaSuccess ||
-      (err = f->e32.alloc(size_t(f->ne) * f->NPE * components)) != cudaSuccess ||
-      (err = f->u_lin64.alloc(size_t(f->ndofs))) != cudaSuccess ||
-      (err = f->u_lin32.alloc(size_t(f->ndofs))) != cudaSuccess)
-    return cleanup_fail(SFX_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(err));
-  if (int rc = sfx_impl::compute_geometry(*f, nullptr)) {
+  if (int rc = sfx_impl::init_form(f, order, components, ne, Nx * Ny * Nz, conn, Xe)) {
     delete f;
     return rc;
   }
-  if ((err = cudaDeviceSynchronize()) != cudaSuccess)
-    return cleanup_fail(SFX_ERR_CUDA, std::string("geometry kernel: ") + cudaGetErrorString(err));
+  *out = f;
+  return SFX_OK;
+}
+
+int sfx_form_create_from_table(int order, int components, int64_t num_elements, int64_t num_nodes,
+                               const int32_t* elem_nodes, const double* elem_vertices, sfx_form* out) {
+  if (!out) return fail(SFX_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (order < 1 || order > 2) return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
+  if (components != 1 && components != 3) return fail(SFX_ERR_UNSUPPORTED, "components must be 1 or 3");
+  if (num_elements < 1 || num_nodes < 1) return fail(SFX_ERR_INVALID, "empty element table");
+  if (!elem_nodes || !elem_vertices) return fail(SFX_ERR_INVALID, "null table");
+  const int64_t npe = int64_t(order + 1) * (order + 1) * (order + 1);
+  if (num_elements * npe >= (int64_t(1) << 31) || num_nodes * components >= (int64_t(1) << 31))
+    return fail(SFX_ERR_UNSUPPORTED, "table too large for int32 indices");
+  std::vector<int32_t> conn(elem_nodes, elem_nodes + num_elements * npe);
+  for (int32_t nd : conn)
+    if (nd < 0 || nd >= num_nodes) return fail(SFX_ERR_INVALID, "element node id out of range");
+  std::vector<double> Xe(size_t(num_elements) * 24);
+  for (int64_t e = 0; e < num_elements; e++)
+    for (int v = 0; v < 8; v++)
+      for (int i = 0; i < 3; i++) Xe[size_t(e * 24 + i * 8 + v)] = elem_vertices[size_t((e * 8 + v) * 3 + i)];
+  auto* f = new (std::nothrow) sfx_form_s;
+  if (!f) return fail(SFX_ERR_NOMEM, "host allocation failed");
+  f->general = true;
+  if (int rc = sfx_impl::init_form(f, order, components, num_elements, num_nodes, conn, Xe)) {
+    delete f;
+    return rc;
+  }
+  f->conn_host = std::move(conn);
+  f->Xe_host = std::move(Xe);
   *out = f;
   return SFX_OK;
 }

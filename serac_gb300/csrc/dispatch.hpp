@@ -50,6 +50,9 @@ int compute_face_geometry(sfx_form_s& f, BoundaryIntegral& bi, cudaStream_t s);
 int compute_geometry(sfx_form_s& f, cudaStream_t s);
 // faces of the box sides in side_mask: tables, vertex coordinates, factors, scratch
 int build_faces(sfx_form_s* form, int side_mask, BoundaryIntegral& bi);
+// faces given as (element, local side 1..6) pairs, in the element's own frame
+int build_faces_list(sfx_form_s* form, int64_t n, const int32_t* face_elem, const int32_t* face_side,
+                     BoundaryIntegral& bi);
 
 // transposed Jacobian actions: domain from the stored tangent (E-vector),
 // boundary added into out

@@ -149,6 +149,13 @@ struct sfx_form_s {
   bool linearized = false;
   bool update_qdata = false;
   int jvp_mode = SFX_JVP_STORED_TANGENT;
+  // forms built from an imported element table (sfx_form_create_from_table):
+  // host copies of the tables and the scalar adjacency of the CSR graph
+  bool general = false;
+  std::vector<int32_t> conn_host;  // [e][NPE]
+  std::vector<double> Xe_host;     // [e][3][8]
+  sfx_impl::DeviceBuf<int64_t> sptr;
+  sfx_impl::DeviceBuf<int32_t> scol;
   std::vector<sfx_impl::DomainIntegral> domain;
   std::vector<sfx_impl::BoundaryIntegral> boundary;
   std::vector<sfx_impl::BoundaryIntegral> face_sets;  // faces for integrals evaluated by the caller's kernels

@@ -281,6 +281,28 @@ int sfx_qoi_add_boundary_integral(sfx_form qoi, int kind, int side_mask, const d
   return SFX_OK;
 }
 
+int sfx_qoi_create_from_table(int order, int components, int64_t num_elements, int64_t num_nodes,
+                              const int32_t* elem_nodes, const double* elem_vertices, sfx_form* out) {
+  if (int rc = sfx_form_create_from_table(order, components, num_elements, num_nodes, elem_nodes, elem_vertices, out))
+    return rc;
+  (*out)->qoi = true;
+  return SFX_OK;
+}
+
+int sfx_qoi_add_boundary_integral_faces(sfx_form qoi, int kind, int64_t num_faces, const int32_t* face_elem,
+                                        const int32_t* face_side, const double* params) {
+  if (int rc = check_qoi(qoi)) return rc;
+  const int np = qoi_nparams(kind, qoi->c, true);
+  if (np < 0) return fail(SFX_ERR_UNSUPPORTED, "QoI kind not available on faces for this space");
+  if (np > 0 && !params) return fail(SFX_ERR_INVALID, "QoI kind needs parameters");
+  BoundaryIntegral bi;
+  bi.material = kind;
+  if (np > 0) bi.params.assign(params, params + np);
+  if (int rc = build_faces_list(qoi, num_faces, face_elem, face_side, bi)) return rc;
+  qoi->qoi_boundary.push_back(std::move(bi));
+  return SFX_OK;
+}
+
 int sfx_qoi_evaluate(sfx_form qoi, double t, const double* u, double* value, void* stream) {
   if (int rc = check_qoi(qoi)) return rc;
   if (!u || !value) return fail(SFX_ERR_INVALID, "null argument");

@@ -699,6 +699,7 @@ int sfx_solver_warm_start(sfx_solver s, double t, double* u, const double* u_tar
 
 int sfx_solver_set_learned(sfx_solver s, sfx_lnet net, int nx, int ny, int nz, const float* features) {
   if (!s || !net || !features) return fail(SFX_ERR_INVALID, "null argument");
+  if (s->form->general) return fail(SFX_ERR_UNSUPPORTED, "the learned preconditioner needs a structured node grid");
   if (int64_t(nx) * ny * nz * 3 != s->n) return fail(SFX_ERR_INVALID, "node grid does not match the form (3 components)");
   s->net = net;
   s->grid[0] = nx;

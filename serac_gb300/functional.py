@@ -113,6 +113,40 @@ class Mesh:
         return idx[sel]
 
 
+class TableMesh:
+    """A conforming hexahedral mesh as an element-node table of one order
+    (an H1 element-dof table, lexicographic local order, the caller's node
+    numbering) with element corner coordinates (num_elements, 8, 3); forms
+    on it are built by sfx_form_create_from_table.  Boundaries are face
+    lists (element, local side 1..6)."""
+
+    def __init__(self, order, elem_nodes, elem_vertices, num_nodes=None):
+        self.order = order
+        self.table = np.ascontiguousarray(elem_nodes, dtype=np.int32).reshape(-1, (order + 1) ** 3)
+        self.corners = np.ascontiguousarray(elem_vertices, dtype=np.float64).reshape(-1, 8, 3)
+        self.num_elements = self.table.shape[0]
+        self.num_nodes = int(self.table.max()) + 1 if num_nodes is None else int(num_nodes)
+
+    def create(self, space, qoi=False):
+        if space.order != self.order:
+            raise ValueError("the space order must be the table's order")
+        h = ctypes.c_void_p()
+        _lib.call("sfx_qoi_create_from_table" if qoi else "sfx_form_create_from_table", self.order,
+                  space.components, ctypes.c_int64(self.num_elements), ctypes.c_int64(self.num_nodes),
+                  self.table.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), self.corners.ctypes.data_as(_lib._dp),
+                  ctypes.byref(h))
+        return h
+
+
+def _face_arrays(faces):
+    elems, sides = faces
+    e = np.ascontiguousarray(np.asarray(elems, dtype=np.int32).ravel())
+    s_ = np.ascontiguousarray(np.asarray(sides, dtype=np.int32).ravel())
+    if e.size != s_.size:
+        raise ValueError("face element and side arrays differ in length")
+    return e, s_
+
+
 def box_vertices(nx, ny, nz, perturb=0.0, seed=0):
     """Vertices of the unit cube grid; interior vertices moved uniformly by up
     to ``perturb`` times the cell size per coordinate (numpy PCG64, ``seed``)."""
@@ -196,11 +230,14 @@ class Gradient:
 class Functional:
     """Functional<H1<p,c>(H1<p,c>)> on a structured hex mesh."""
 
-    def __init__(self, mesh: Mesh, space: H1):
+    def __init__(self, mesh, space: H1):
         self.mesh = mesh
         self.space = space
-        h = ctypes.c_void_p()
-        _lib.call("sfx_form_create", mesh._h, space.order, space.components, ctypes.byref(h))
+        if isinstance(mesh, TableMesh):
+            h = mesh.create(space)
+        else:
+            h = ctypes.c_void_p()
+            _lib.call("sfx_form_create", mesh._h, space.order, space.components, ctypes.byref(h))
         self._h = h
         n = ctypes.c_int64()
         _lib.call("sfx_form_num_dofs", h, ctypes.byref(n))
@@ -232,13 +269,21 @@ class Functional:
     add_domain_integral = AddDomainIntegral
     AddVolumeIntegral = AddDomainIntegral
 
-    def AddBoundaryIntegral(self, material, sides, params):
-        mask = 0
-        for s in sides:
-            mask |= 1 << (s - 1)
+    def AddBoundaryIntegral(self, material, sides=None, params=None, faces=None):
+        """Over the box sides (structured meshes) or a face list
+        faces = (element array, local side array)."""
         arr = np.ascontiguousarray(np.asarray(params, dtype=np.float64).ravel())
         if material in BNPARAMS and arr.size != BNPARAMS[material]:
             raise ValueError(f"boundary material {material} takes {BNPARAMS[material]} parameters, got {arr.size}")
+        if faces is not None:
+            e, s_ = _face_arrays(faces)
+            _lib.call("sfx_form_add_boundary_integral_faces", self._h, material, ctypes.c_int64(e.size),
+                      e.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), s_.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                      arr.ctypes.data_as(_lib._dp))
+            return
+        mask = 0
+        for s in sides:
+            mask |= 1 << (s - 1)
         _lib.call("sfx_form_add_boundary_integral", self._h, material, mask, arr.ctypes.data_as(_lib._dp))
 
     add_boundary_integral = AddBoundaryIntegral
@@ -454,11 +499,14 @@ class QoI:
         dQdu(du); assemble(dQdu)                              # :420, :422-475
     """
 
-    def __init__(self, mesh: Mesh, space: H1):
+    def __init__(self, mesh, space: H1):
         self.mesh = mesh
         self.space = space
-        h = ctypes.c_void_p()
-        _lib.call("sfx_qoi_create", mesh._h, space.order, space.components, ctypes.byref(h))
+        if isinstance(mesh, TableMesh):
+            h = mesh.create(space, qoi=True)
+        else:
+            h = ctypes.c_void_p()
+            _lib.call("sfx_qoi_create", mesh._h, space.order, space.components, ctypes.byref(h))
         self._h = h
         n = ctypes.c_int64()
         _lib.call("sfx_form_num_dofs", h, ctypes.byref(n))
@@ -484,11 +532,19 @@ class QoI:
     def AddDomainIntegral(self, kind, params=None):
         _lib.call("sfx_qoi_add_domain_integral", self._h, int(kind), self._params(kind, params, False))
 
-    def AddBoundaryIntegral(self, kind, sides, params=None):
+    def AddBoundaryIntegral(self, kind, sides=None, params=None, faces=None):
+        prm = self._params(kind, params, True)
+        if faces is not None:
+            e, s2 = _face_arrays(faces)
+            self._keep += [e, s2]
+            _lib.call("sfx_qoi_add_boundary_integral_faces", self._h, int(kind), ctypes.c_int64(e.size),
+                      e.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), s2.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                      prm)
+            return
         mask = 0
         for s_ in sides:
             mask |= 1 << (s_ - 1)
-        _lib.call("sfx_qoi_add_boundary_integral", self._h, int(kind), mask, self._params(kind, params, True))
+        _lib.call("sfx_qoi_add_boundary_integral", self._h, int(kind), mask, prm)
 
     AddVolumeIntegral = AddDomainIntegral
     AddSurfaceIntegral = AddBoundaryIntegral
