@@ -438,7 +438,8 @@ def newton_leg(steps, only=None):
     base = dict(newton_rel_tol=1e-8, newton_abs_tol=0.0, krylov_rel_tol=1e-8, krylov_abs_tol=0.0,
                 max_krylov_iterations=5000)
     variants = [("plain_fp64", sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, **base)),
-                ("mixed", sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, mixed_precision=1, **base))]
+                ("mixed", sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, mixed_precision=1, **base)),
+                ("mixed_f16", sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, mixed_precision=1, **base))]
     net = None
     if os.path.exists(WEIGHTS):
         net = LP.LearnedPreconditioner()
@@ -453,6 +454,8 @@ def newton_leg(steps, only=None):
     ref = None
     for name, opts in variants:
         S = LP.SolidSetup(prob)
+        if name.endswith("f16"):  # FP16 copy of the tangent for the inner FP32 operator
+            S.f.set_tangent_storage(S.f.TANGENT_F16)
         solver = sg.NewtonSolver(S.f, opts)
         solver.set_essential(S.ess)
         if name.startswith("learned"):
@@ -478,7 +481,7 @@ def newton_leg(steps, only=None):
         tot["rel_diff_vs_plain"] = float(torch.linalg.norm(u - ref) / torch.linalg.norm(ref))
         out[name] = tot
         del solver, S
-    for name in ("mixed", "learned_mixed"):
+    for name in ("mixed", "mixed_f16", "learned_mixed"):
         if name in out and "plain_fp64" in out:
             out[f"speedup_{name}_vs_plain"] = out["plain_fp64"]["seconds"] / out[name]["seconds"]
     if net is None:
@@ -719,7 +722,8 @@ def main():
     ap.add_argument("--precision", choices=["f64", "f32"], default="f64", help="precision of --kernels-only")
     ap.add_argument("--newton-steps", type=int, default=1,
                     help="load steps of the Newton time-to-1e-8 leg (0 = skip)")
-    ap.add_argument("--extra", choices=["config3", "large", "large-plain", "newton-mixed", "lnet"], default=None,
+    ap.add_argument("--extra", choices=["config3", "large", "large-plain", "newton-mixed", "newton-f16", "lnet"],
+                    default=None,
                     help="run only an extra configuration (64^3 mixed-precision error, or the large sizes) "
                          "and print its JSON record")
     args = ap.parse_args()
@@ -736,6 +740,8 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         if args.extra == "newton-mixed":  # the mixed-precision Newton leg alone (for profiler launch lists)
             rec = newton_leg(1, only=("mixed",))
+        elif args.extra == "newton-f16":  # mixed precision with the FP32 and the FP16 inner tangent
+            rec = newton_leg(1, only=("mixed", "mixed_f16"))
         elif args.extra == "lnet":
             rec = lnet_leg()
         elif args.extra == "config3":

@@ -172,6 +172,15 @@ int sfx_linearize(sfx_form form, double t, const double* u, double* r, void* str
 #define SFX_JVP_RECOMPUTE 1
 int sfx_form_set_jvp_mode(sfx_form form, int mode);
 
+/* Storage of the tangent copy that the FP32 action streams (the inner
+ * Krylov operator of the mixed-precision solver): SFX_TANGENT_F32 (default)
+ * or SFX_TANGENT_F16 (half the bytes, about 3 significant digits per entry,
+ * FP32 accumulation; order 2).  The FP64 tangent is unaffected.  Takes effect
+ * at the next sfx_linearize. */
+#define SFX_TANGENT_F32 0
+#define SFX_TANGENT_F16 1
+int sfx_form_set_tangent_storage(sfx_form form, int storage);
+
 /* dr = dR/du(t_lin, u_lin) du, in FP64, and in FP32 (FP32 accumulation). */
 int sfx_jvp(sfx_form form, const double* du, double* dr, void* stream);
 int sfx_jvp_f32(sfx_form form, const float* du, float* dr, void* stream);

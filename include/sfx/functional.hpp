@@ -207,7 +207,7 @@ struct DomainIntegral : IntegralBase {
     D32.resize(n);
     auto a = args(L, t, u, nullptr, nullptr);
     kernels::linearize_kernel<P, C, State, Maker>
-        <<<warp_blocks(L.num_elements, EPW), 128, 0, s>>>(a, maker, D64.p, D32.p, E);
+        <<<warp_blocks(L.num_elements, EPW), 128, 0, s>>>(a, maker, D64.p, D32.p, nullptr, E);
     check_cuda(cudaGetLastError(), "linearize kernel");
   }
   void jvp(const sfx_form_layout& L, const double* du, double* E, cudaStream_t s) override {

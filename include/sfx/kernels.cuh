@@ -12,6 +12,8 @@
 // global vector in a fixed order (no floating-point atomics: deterministic).
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include <cstdint>
 #include <type_traits>
 
@@ -968,17 +970,29 @@ struct TangentShape {
   /// boundary and can be moved by a bulk copy
   template <int NQ>
   static constexpr int64_t stride = (int64_t(size) * NQ + 3) / 4 * 4;
+  /// the same for the FP16 copy (multiples of 8 halves = 16 bytes)
+  template <int NQ>
+  static constexpr int64_t stride16 = (int64_t(size) * NQ + 7) / 8 * 8;
+  /// entries per element block in storage type TS
+  template <int NQ, typename TS>
+  static constexpr int64_t stride_of = sizeof(TS) == 2 ? stride16<NQ> : stride<NQ>;
 };
+
+/// storage -> FP32 for the tangent copies of the FP32 Jacobian action
+SFX_HDI float tangent_to_f32(float x) { return x; }
+SFX_HDI float tangent_to_f32(__half x) { return __half2float(x); }
 
 /// Linearise the q-function at every quadrature point (the derivative serac
 /// stores in evaluation_kernel_impl, domain_integral_kernels.hpp:209-214, after
 /// physical_to_parent, with det(J) w folded in) and, optionally, write the
 /// element residuals of the same evaluation.  D is stored element-major,
 /// D[e * stride + (row * cols + col) * NQ + q] (stride = TangentShape::stride),
-/// in FP64 and FP32, so that one element's tangent is one contiguous block.
+/// in FP64 and FP32 (or FP16 with its own stride16), so that one element's
+/// tangent is one contiguous block; D32 / D16 may be null.
 template <int P, int C, typename State, typename QFMaker>
 __global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QFMaker make_qf, double* __restrict__ D64,
-                                                        float* __restrict__ D32, double* __restrict__ res_e) {
+                                                        float* __restrict__ D32, __half* __restrict__ D16,
+                                                        double* __restrict__ res_e) {
   using Real = double;
   constexpr int Q = P + 1;
   constexpr int NQ = Q * Q * Q;
@@ -1086,9 +1100,10 @@ __global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QF
       if constexpr (HS) {
         Real v = dvol * part<JVP, Real>(source_comp<C>(get<0>(out), ci));
         if (valid) {
-          const int64_t at = e * Shape::template stride<NQ> + (int64_t(ci) * Shape::cols + k) * NQ + qi;
-          D64[at] = v;
-          D32[at] = float(v);
+          const int64_t in_block = (int64_t(ci) * Shape::cols + k) * NQ + qi;
+          D64[e * Shape::template stride<NQ> + in_block] = v;
+          if (D32) D32[e * Shape::template stride<NQ> + in_block] = float(v);
+          if (D16) D16[e * Shape::template stride16<NQ> + in_block] = __float2half_rn(float(v));
         }
       }
     }
@@ -1110,9 +1125,10 @@ __global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QF
       for (int kd = 0; kd < 3; kd++) {
         Real v = dvol * (fp[0] * Ji[kd][0] + fp[1] * Ji[kd][1] + fp[2] * Ji[kd][2]);
         if (valid) {
-          const int64_t at = e * Shape::template stride<NQ> + (int64_t(row + 3 * ci + kd) * Shape::cols + k) * NQ + qi;
-          D64[at] = v;
-          D32[at] = float(v);
+          const int64_t in_block = (int64_t(row + 3 * ci + kd) * Shape::cols + k) * NQ + qi;
+          D64[e * Shape::template stride<NQ> + in_block] = v;
+          if (D32) D32[e * Shape::template stride<NQ> + in_block] = float(v);
+          if (D16) D16[e * Shape::template stride16<NQ> + in_block] = __float2half_rn(float(v));
         }
         if (!have_res) res_f[ci][kd] = dvol * (fv[0] * Ji[kd][0] + fv[1] * Ji[kd][1] + fv[2] * Ji[kd][2]);
       }
@@ -1276,9 +1292,9 @@ __global__ void __launch_bounds__(128) jvp_stored_transpose_kernel(const Real* _
 /// does not complete sets *err and the warp drains its outstanding copies
 /// (again bounded) before returning.  TRANSPOSE applies the block transposed
 /// (J^T v, as jvp_stored_transpose_kernel) with the same staging.
-template <int C, bool HS, bool VI, int WARPS, int STAGES, bool TRANSPOSE = false>
+template <int C, bool HS, bool VI, int WARPS, int STAGES, bool TRANSPOSE = false, typename TS = float>
 __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float* __restrict__ du,
-                                                                    const float* __restrict__ D,
+                                                                    const TS* __restrict__ D,
                                                                     const int32_t* __restrict__ conn,
                                                                     float* __restrict__ out_e, int64_t num_nodes,
                                                                     int64_t num_elements, int* __restrict__ err) {
@@ -1290,11 +1306,11 @@ __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float*
   constexpr bool OUT_VALUE = TRANSPOSE ? VI : HS;
   constexpr int NIN = TRANSPOSE ? Shape::rows : Shape::cols;
   constexpr int NOUT = TRANSPOSE ? Shape::cols : Shape::rows;
-  constexpr int64_t ES = Shape::template stride<NQ>;  // floats per element block
-  constexpr uint32_t BYTES = uint32_t(ES * 4);
+  constexpr int64_t ES = Shape::template stride_of<NQ, TS>;  // entries per element block
+  constexpr uint32_t BYTES = uint32_t(ES * sizeof(TS));
   static_assert(BYTES % 16 == 0, "bulk copies move multiples of 16 bytes");
   extern __shared__ __align__(128) unsigned char sfx_dyn_smem[];
-  float* ring = reinterpret_cast<float*>(sfx_dyn_smem);                                 // [WARPS][STAGES][ES]
+  TS* ring = reinterpret_cast<TS*>(sfx_dyn_smem);                                       // [WARPS][STAGES][ES]
   uint64_t* bars = reinterpret_cast<uint64_t*>(sfx_dyn_smem + size_t(WARPS) * STAGES * BYTES);  // [WARPS][STAGES]
   __shared__ float sB[Q][Q], sG[Q][Q];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -1303,7 +1319,7 @@ __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float*
     sB[i][j] = float(basis_table<P>().B[i][j]);
     sG[i][j] = float(basis_table<P>().G[i][j]);
   }
-  float* my_ring = ring + size_t(wid) * STAGES * ES;
+  TS* my_ring = ring + size_t(wid) * STAGES * ES;
   uint64_t* my_bars = bars + wid * STAGES;
   if (lane == 0) {
     for (int s = 0; s < STAGES; s++) bulk::mbar_init(&my_bars[s], 1);
@@ -1367,14 +1383,14 @@ __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float*
       failed = true;
       break;
     }
-    const float* Dq = my_ring + s * ES + qi;
+    const TS* Dq = my_ring + s * ES + qi;
     float dout[NOUT];
 #pragma unroll
     for (int r = 0; r < NOUT; r++) {
       float acc = 0.f;
 #pragma unroll
       for (int k = 0; k < NIN; k++)
-        acc += Dq[(TRANSPOSE ? k * Shape::cols + r : r * Shape::cols + k) * NQ] * din[k];
+        acc += tangent_to_f32(Dq[(TRANSPOSE ? k * Shape::cols + r : r * Shape::cols + k) * NQ]) * din[k];
       dout[r] = acc;
     }
     __syncwarp();  // every lane has read stage s

@@ -381,6 +381,17 @@ int sfx_form_set_jvp_mode(sfx_form form, int mode) {
   return SFX_OK;
 }
 
+int sfx_form_set_tangent_storage(sfx_form form, int storage) {
+  if (check_form(form)) return SFX_ERR_INVALID;
+  if (storage != SFX_TANGENT_F32 && storage != SFX_TANGENT_F16) return fail(SFX_ERR_INVALID, "unknown tangent storage");
+  if (storage == SFX_TANGENT_F16 && form->p != 2)
+    return fail(SFX_ERR_UNSUPPORTED, "the FP16 tangent copy is built for order 2");
+  const bool want = storage == SFX_TANGENT_F16;
+  if (want != form->tangent16) form->linearized = false;
+  form->tangent16 = want;
+  return SFX_OK;
+}
+
 int sfx_jvp(sfx_form form, const double* du, double* dr, void* stream) {
   if (check_form(form)) return SFX_ERR_INVALID;
   if (!du || !dr) return fail(SFX_ERR_INVALID, "null vector");

@@ -165,11 +165,19 @@ struct LinearizeFn {
     constexpr bool HS = kernels::tangent_has_source<C, State, QF>();
     using Shape = kernels::TangentShape<C, HS, Maker::value_input>;
     const size_t n = size_t(f.ne) * size_t(Shape::template stride<NQ>);
-    if (di.D64.n != n) {
-      cudaError_t err = di.D64.alloc(n);
-      if (err == cudaSuccess) err = di.D32.alloc(n);
-      if (err != cudaSuccess) return fail(SFX_ERR_NOMEM, std::string("tangent storage: ") + cudaGetErrorString(err));
+    const size_t n16 = size_t(f.ne) * size_t(Shape::template stride16<NQ>);
+    cudaError_t err = cudaSuccess;
+    if (di.D64.n != n) err = di.D64.alloc(n);
+    if (err == cudaSuccess) {
+      if (f.tangent16) {
+        di.D32.reset();
+        if (di.D16.n != n16) err = di.D16.alloc(n16);
+      } else {
+        di.D16.reset();
+        if (di.D32.n != n) err = di.D32.alloc(n);
+      }
     }
+    if (err != cudaSuccess) return fail(SFX_ERR_NOMEM, std::string("tangent storage: ") + cudaGetErrorString(err));
     di.tangent_rows = Shape::rows;
     di.tangent_cols = Shape::cols;
     if (f.ne == 0) return SFX_OK;
@@ -177,8 +185,9 @@ struct LinearizeFn {
                                   f.nnodes, f.ne, f.t_lin};
     int64_t warps = (f.ne + EPW - 1) / EPW;
     int64_t blocks = (warps * 32 + 127) / 128;
-    kernels::linearize_kernel<P, C, State, Maker><<<unsigned(blocks), 128, 0, s>>>(a, Maker{}, di.D64.p, di.D32.p, res_e);
-    cudaError_t err = cudaGetLastError();
+    kernels::linearize_kernel<P, C, State, Maker><<<unsigned(blocks), 128, 0, s>>>(a, Maker{}, di.D64.p, di.D32.p,
+                                                                                   di.D16.p, res_e);
+    err = cudaGetLastError();
     if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("linearize launch: ") + cudaGetErrorString(err));
     return SFX_OK;
   }
@@ -187,12 +196,12 @@ struct LinearizeFn {
 // Bulk-copy staged FP32 action for Q2 (J, or J^T when TRANSPOSE): one
 // persistent block per SM with as many warps as fit two-deep rings in 220 KB
 // of shared memory, rings up to 4 deep.
-template <int C, bool HS, bool VI, bool TRANSPOSE>
-int launch_tma(const sfx_form_s& f, const float* du, const float* D, float* E, cudaStream_t s) {
+template <int C, bool HS, bool VI, bool TRANSPOSE, typename TS>
+int launch_tma(const sfx_form_s& f, const float* du, const TS* D, float* E, cudaStream_t s) {
   constexpr int NQ = 27;
   using Shape = kernels::TangentShape<C, HS, VI>;
   constexpr size_t kSmemBudget = 220 * 1024;
-  constexpr size_t stage_bytes = size_t(Shape::template stride<NQ>) * 4 + 8;
+  constexpr size_t stage_bytes = size_t(Shape::template stride_of<NQ, TS>) * sizeof(TS) + 8;
   constexpr int WARPS = 16 * 2 * stage_bytes <= kSmemBudget   ? 16
                         : 12 * 2 * stage_bytes <= kSmemBudget ? 12
                         : 8 * 2 * stage_bytes <= kSmemBudget  ? 8
@@ -200,7 +209,7 @@ int launch_tma(const sfx_form_s& f, const float* du, const float* D, float* E, c
   constexpr int STAGES = int(std::min<size_t>(4, kSmemBudget / (WARPS * stage_bytes)));
   static_assert(STAGES >= 2, "tangent block too large for a two-stage ring");
   constexpr size_t smem = size_t(WARPS) * STAGES * stage_bytes;
-  auto kern = kernels::jvp_stored_tma_kernel<C, HS, VI, WARPS, STAGES, TRANSPOSE>;
+  auto kern = kernels::jvp_stored_tma_kernel<C, HS, VI, WARPS, STAGES, TRANSPOSE, TS>;
   static bool configured = false;  // per instantiation
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
@@ -234,7 +243,9 @@ struct StoredJvpFn {
     constexpr bool HS = kernels::tangent_has_source<C, State, QF>();
     if (f.ne == 0) return SFX_OK;
     if constexpr (P == 2 && std::is_same<Real, float>::value) {
-      if (int rc = launch_tma<C, HS, Maker::value_input, false>(f, du, D, E, s)) return rc;
+      const int rc = f.tangent16 ? launch_tma<C, HS, Maker::value_input, false, __half>(f, du, di.D16.p, E, s)
+                                 : launch_tma<C, HS, Maker::value_input, false, float>(f, du, D, E, s);
+      if (rc) return rc;
     } else {
       int64_t warps = (f.ne + EPW - 1) / EPW;
       int64_t blocks = (warps * 32 + 127) / 128;
@@ -250,6 +261,7 @@ struct StoredJvpFn {
 template <int P, typename Real>
 struct StoredJvpTransposeFn {
   const sfx_form_s& f;
+  const DomainIntegral& di;
   const Real* v;
   const Real* D;
   Real* E;
@@ -262,7 +274,9 @@ struct StoredJvpTransposeFn {
     constexpr bool HS = kernels::tangent_has_source<C, State, QF>();
     if (f.ne == 0) return SFX_OK;
     if constexpr (P == 2 && std::is_same<Real, float>::value) {
-      if (int rc = launch_tma<C, HS, Maker::value_input, true>(f, v, D, E, s)) return rc;
+      const int rc = f.tangent16 ? launch_tma<C, HS, Maker::value_input, true, __half>(f, v, di.D16.p, E, s)
+                                 : launch_tma<C, HS, Maker::value_input, true, float>(f, v, D, E, s);
+      if (rc) return rc;
     } else {
       const int64_t warps = (f.ne + EPW - 1) / EPW;
       const int64_t blocks = (warps * 32 + 127) / 128;
@@ -392,15 +406,15 @@ int launch_jvp_stored_f32(const sfx_form_s& f, const DomainIntegral& di, const f
 }
 
 int launch_jvp_transpose(const sfx_form_s& f, const DomainIntegral& di, const double* v, double* E, cudaStream_t s) {
-  if (f.p == 1) return visit_material(di.material, StoredJvpTransposeFn<1, double>{f, v, di.D64.p, E, s});
-  if (f.p == 2) return visit_material(di.material, StoredJvpTransposeFn<2, double>{f, v, di.D64.p, E, s});
+  if (f.p == 1) return visit_material(di.material, StoredJvpTransposeFn<1, double>{f, di, v, di.D64.p, E, s});
+  if (f.p == 2) return visit_material(di.material, StoredJvpTransposeFn<2, double>{f, di, v, di.D64.p, E, s});
   return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
 }
 
 int launch_jvp_transpose_f32(const sfx_form_s& f, const DomainIntegral& di, const float* v, float* E,
                              cudaStream_t s) {
-  if (f.p == 1) return visit_material(di.material, StoredJvpTransposeFn<1, float>{f, v, di.D32.p, E, s});
-  if (f.p == 2) return visit_material(di.material, StoredJvpTransposeFn<2, float>{f, v, di.D32.p, E, s});
+  if (f.p == 1) return visit_material(di.material, StoredJvpTransposeFn<1, float>{f, di, v, di.D32.p, E, s});
+  if (f.p == 2) return visit_material(di.material, StoredJvpTransposeFn<2, float>{f, di, v, di.D32.p, E, s});
   return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
 }
 

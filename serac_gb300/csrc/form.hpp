@@ -1,6 +1,7 @@
 // Internal state of the sfx C ABI: meshes, forms and their device buffers.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -70,6 +71,7 @@ struct DomainIntegral {
   // stored q-function derivative (stored-tangent Jacobian action)
   DeviceBuf<double> D64;
   DeviceBuf<float> D32;
+  DeviceBuf<__half> D16;  // FP16 copy for the FP32 action when the form stores it (tangent16)
   int tangent_rows = 0, tangent_cols = 0;
 };
 
@@ -149,6 +151,7 @@ struct sfx_form_s {
   bool linearized = false;
   bool update_qdata = false;
   int jvp_mode = SFX_JVP_STORED_TANGENT;
+  bool tangent16 = false;  // the FP32 action streams an FP16 copy of the tangent
   // forms built from an imported element table (sfx_form_create_from_table):
   // host copies of the tables and the scalar adjacency of the CSR graph
   bool general = false;

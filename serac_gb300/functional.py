@@ -297,6 +297,13 @@ class Functional:
         re-evaluates the q-function on dual numbers."""
         _lib.call("sfx_form_set_jvp_mode", self._h, int(mode))
 
+    TANGENT_F32, TANGENT_F16 = 0, 1
+
+    def set_tangent_storage(self, storage):
+        """Storage of the tangent copy streamed by the FP32 action (the inner
+        Krylov operator): TANGENT_F32 (default) or TANGENT_F16 (order 2)."""
+        _lib.call("sfx_form_set_tangent_storage", self._h, int(storage))
+
     def set_shape_displacement(self, shape, stream=None):
         """Evaluate every integral on the configuration X + shape (float64 CUDA
         tensor, 3 * num_nodes, byNODES; None = the reference configuration),
