@@ -44,3 +44,43 @@ def test_invalid_arguments_fail_loudly():
     assert lib.sfx_residual(None, 0.0, None, None, None) == -1
     with pytest.raises(_lib.SfxError):
         _lib.call("sfx_form_create", None, 2, 3, ctypes.byref(h))
+
+
+def test_new_entry_points_validate_before_touching_a_device():
+    """QoI, adjoint, sensitivity, element-table and tangent-storage entry
+    points reject bad arguments on the host (no GPU needed)."""
+    import numpy as np
+
+    from serac_gb300 import _lib
+
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    i32 = ctypes.POINTER(ctypes.c_int32)
+    dp = ctypes.POINTER(ctypes.c_double)
+    table = np.zeros((1, 8), dtype=np.int32)
+    corners = np.zeros((1, 8, 3))
+    # order 3 is not built; node id out of range; empty table; null tables
+    assert lib.sfx_form_create_from_table(3, 1, 1, 8, table.ctypes.data_as(i32), corners.ctypes.data_as(dp),
+                                          ctypes.byref(h)) == -5
+    bad = table.copy()
+    bad[0, 3] = 9
+    assert lib.sfx_form_create_from_table(1, 1, 1, 8, bad.ctypes.data_as(i32), corners.ctypes.data_as(dp),
+                                          ctypes.byref(h)) == -1
+    assert b"out of range" in lib.sfx_last_error()
+    assert lib.sfx_form_create_from_table(1, 1, 0, 8, table.ctypes.data_as(i32), corners.ctypes.data_as(dp),
+                                          ctypes.byref(h)) == -1
+    assert lib.sfx_form_create_from_table(1, 1, 1, 8, None, None, ctypes.byref(h)) == -1
+    assert lib.sfx_qoi_create_from_table(2, 2, 1, 27, None, None, ctypes.byref(h)) == -5
+    for call in (lambda: lib.sfx_jvp_transpose(None, None, None, None),
+                 lambda: lib.sfx_jvp_transpose_f32(None, None, None, None),
+                 lambda: lib.sfx_qoi_add_domain_integral(None, 0, None),
+                 lambda: lib.sfx_qoi_evaluate(None, 0.0, None, None, None),
+                 lambda: lib.sfx_qoi_gradient(None, 0.0, None, None, None, None),
+                 lambda: lib.sfx_qoi_action(None, 0.0, None, None, None, None),
+                 lambda: lib.sfx_qoi_shape_gradient(None, 0.0, None, None, None),
+                 lambda: lib.sfx_shape_vjp(None, 0.0, None, None, None, None),
+                 lambda: lib.sfx_form_set_tangent_storage(None, 1),
+                 lambda: lib.sfx_form_add_boundary_integral_faces(None, 0, 0, None, None, None),
+                 lambda: lib.sfx_form_add_face_set_faces(None, 0, None, None, None),
+                 lambda: lib.sfx_solver_solve_adjoint(None, 0.0, None, None, None, None)):
+        assert call() == -1
