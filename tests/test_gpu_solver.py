@@ -1,6 +1,6 @@
 """Device Newton-Krylov solver against the oracle's Newton with direct solves.
 
-Converged solutions agree to 1e-9 relative (spec parity target for the
+Converged solutions agree to 1e-9 relative (the parity target for a converged
 Newton solution); every Krylov / preconditioner combination must reach the
 same answer, including the FP32-inner mixed-precision mode.
 """
