@@ -77,6 +77,10 @@ def _declare(lib, prefix):
     f = getattr(lib, prefix + "boundary")
     f.argtypes = [ctypes.c_int] * 4 + [ctypes.c_double] + [_dp] * 6
     f.restype = ctypes.c_int
+    if prefix == "ref_" and hasattr(lib, "ref_qoi"):
+        f = lib.ref_qoi
+        f.argtypes = [ctypes.c_int] * 6 + [ctypes.c_double] + [_dp] * 5
+        f.restype = ctypes.c_int
 
 
 def lib():
@@ -743,6 +747,43 @@ class OracleQoI:
             for k in range(c):
                 np.add.at(grad[k], fnodes.ravel(), gF[k].ravel())
         return value, grad.ravel()
+
+    def evaluate_reference(self, u):
+        """(Q(u), dQ/du) from serac's own QoI element kernels (evaluation_kernel_impl
+        and element_gradient_kernel with the QOI test space, compiled into
+        oracle/_ref), on the same geometric factors; None where the reference
+        library is absent.  Integrands that depend on the field only."""
+        R = ref_lib()
+        if R is None or not hasattr(R, "ref_qoi"):
+            return None
+        c, N, p = self.c, self.nnodes, self.p
+        value = 0.0
+        grad = np.zeros(c * N)
+        nd = c * (p + 1) ** 3
+        uE = gather(u, self.conn, c, N)
+        for kind, params in self.domain:
+            prm = np.ascontiguousarray(np.asarray([0.0] if params is None else params, dtype=np.float64).ravel())
+            ne = self.conn.shape[0]
+            vals = np.zeros(ne)
+            assert R.ref_qoi(kind, 0, p, c, 0, ne, 0.0, _ptr(prm), _ptr(uE), _ptr(self.Xq), _ptr(self.Jq),
+                             _ptr(vals)) == 0
+            ge = np.zeros((ne, nd))
+            assert R.ref_qoi(kind, 0, p, c, 1, ne, 0.0, _ptr(prm), _ptr(uE), _ptr(self.Xq), _ptr(self.Jq),
+                             _ptr(ge)) == 0
+            value += float(vals.sum())
+            grad += scatter_add(ge, self.conn, c, N)
+        for kind, params, fnodes, Xq, Jq in self.boundary:
+            prm = np.ascontiguousarray(np.asarray([0.0] if params is None else params, dtype=np.float64).ravel())
+            nf = fnodes.shape[0]
+            uF = gather(u, fnodes, c, N)
+            vals = np.zeros(nf)
+            Xq, Jq = np.ascontiguousarray(Xq), np.ascontiguousarray(Jq)
+            assert R.ref_qoi(kind, 1, p, c, 0, nf, 0.0, _ptr(prm), _ptr(uF), _ptr(Xq), _ptr(Jq), _ptr(vals)) == 0
+            gf = np.zeros((nf, c * (p + 1) ** 2))
+            assert R.ref_qoi(kind, 1, p, c, 1, nf, 0.0, _ptr(prm), _ptr(uF), _ptr(Xq), _ptr(Jq), _ptr(gf)) == 0
+            value += float(vals.sum())
+            grad += scatter_add(gf, fnodes, c, N)
+        return value, grad
 
     def value(self, u):
         return self.evaluate(u)[0]

@@ -179,6 +179,219 @@ struct PressureBQF {
   }
 };
 
+// -------------------------------------------- quantities of interest
+// Integrand ids shared with oracle.py (OracleQoI) and the product's C ABI.
+enum QoiKind : int {
+  QOI_FIELD             = 2,  // w . u
+  QOI_NEOHOOKEAN_ENERGY = 3,  // Neo-Hookean stored energy (domain, 3 components)
+  QOI_NORMAL_FIELD      = 4,  // u . n (faces, 3 components)
+  QOI_POLY_TEST         = 5,  // nonlinear test integrand
+};
+
+template <int c, typename U>
+auto component_sum(const U& u)
+{
+  if constexpr (c == 1) {
+    return u;
+  } else {
+    auto s = u[0];
+    for (int i = 1; i < c; i++) s = s + u[i];
+    return s;
+  }
+}
+
+template <int c>
+struct FieldQoI {
+  double w[3];
+  template <typename X, typename T>
+  auto operator()(double, X, T field) const
+  {
+    auto u = get<0>(field);
+    if constexpr (c == 1) {
+      return w[0] * u;
+    } else {
+      auto s = w[0] * u[0];
+      for (int i = 1; i < c; i++) s = s + w[i] * u[i];
+      return s;
+    }
+  }
+};
+
+// W = G/2 (|H|^2 + 2 tr H) - G ln J + lambda/2 (ln J)^2 with ln J = log1p(det(I + H) - 1)
+struct NeoHookeanEnergyQoI {
+  double K, G;
+  template <typename X, typename T>
+  auto operator()(double, X, T displacement) const
+  {
+    auto H      = get<1>(displacement);
+    using std::log1p;
+    auto   lnJ    = log1p(detApIm1(H));
+    double lambda = K - (2.0 / 3.0) * G;
+    return 0.5 * G * (squared_norm(H) + 2.0 * tr(H)) - G * lnJ + 0.5 * lambda * lnJ * lnJ;
+  }
+};
+
+// X0^2 + sin X1 + X0 s^3 + (1 + X2)/2 |grad u|^2, s = sum of the components of u
+template <int c>
+struct PolyQoI {
+  template <typename X, typename T>
+  auto operator()(double, X position, T field) const
+  {
+    using std::sin;
+    auto x = get<0>(position);
+    auto s = component_sum<c>(get<0>(field));
+    return x[0] * x[0] + sin(x[1]) + x[0] * s * s * s + 0.5 * (1.0 + x[2]) * squared_norm(get<1>(field));
+  }
+};
+
+// faces: u . n and X0 - X1 + cos(s X1) + |du/ds|^2 / 4 (du/ds: the first parent direction)
+struct NormalFieldQoI {
+  template <typename X, typename T>
+  auto operator()(double, X position, T displacement) const
+  {
+    auto n = cross(get<1>(position));
+    return dot(get<0>(displacement), n / norm(n));
+  }
+};
+
+template <int c>
+struct PolyFaceQoI {
+  template <typename X, typename T>
+  auto operator()(double, X position, T field) const
+  {
+    using std::cos;
+    auto x  = get<0>(position);
+    auto s  = component_sum<c>(get<0>(field));
+    auto du = get<1>(field);
+    if constexpr (c == 1) {
+      return x[0] - x[1] + cos(s * x[1]) + 0.25 * du[0] * du[0];
+    } else {
+      auto g = du[0][0] * du[0][0];
+      for (int i = 1; i < c; i++) g = g + du[i][0] * du[i][0];
+      return x[0] - x[1] + cos(s * x[1]) + 0.25 * g;
+    }
+  }
+};
+
+// per-element values (mode 0) or element gradients dQ_e/du_e (mode 1) of a QoI
+template <int p, int c, typename QF>
+struct QoiDomainRunner {
+  using space   = H1<p, c>;
+  using element = finite_element<CUBE, space>;
+  using test    = finite_element<CUBE, QOI>;
+  static constexpr int Q  = p + 1;
+  static constexpr int nq = Q * Q * Q;
+  static constexpr int nd = element::ndof * c;
+  using deriv_t           = decltype(domain_integral::get_derivative_type<0, 3, space>(QF{}, Nothing{}));
+
+  static void run(int mode, const QF& qf, int ne, double t, const double* uE, const double* X, const double* J,
+                  double* out)
+  {
+    std::vector<deriv_t> derivs(nq);
+    axom::Array<Nothing, 2>     arr;
+    axom::ArrayView<Nothing, 2> view(arr);
+    tuple<element>              trial_elements{};
+    int                         elements[1] = {0};
+    for (int e = 0; e < ne; e++) {
+      std::vector<const double*> inputs{uE + size_t(e) * nd};
+      const double*              Xe = X + size_t(e) * 3 * nq;
+      const double*              Je = J + size_t(e) * 9 * nq;
+      double                     value = 0.0;
+      if (mode == 0) {
+        domain_integral::evaluation_kernel_impl<NO_DIFFERENTIATION, Q, CUBE>(
+            trial_elements, test{}, t, inputs, &value, Xe, Je, qf, view, derivs.data(), elements, 1, false,
+            camp::int_seq<int, 0>{});
+        out[e] = value;
+      } else {
+        domain_integral::evaluation_kernel_impl<0, Q, CUBE>(trial_elements, test{}, t, inputs, &value, Xe, Je, qf,
+                                                            view, derivs.data(), elements, 1, false,
+                                                            camp::int_seq<int, 0>{});
+        double* ge = out + size_t(e) * nd;
+        std::memset(ge, 0, sizeof(double) * nd);
+        ExecArrayView<double, 3, ExecutionSpace::CPU> gview(ge, {1, 1, nd});
+        domain_integral::element_gradient_kernel<CUBE, QOI, space, Q>(gview, derivs.data(), elements, 1);
+      }
+    }
+  }
+};
+
+template <int p, int c, typename QF>
+struct QoiFaceRunner {
+  using space   = H1<p, c>;
+  using element = finite_element<SQUARE, space>;
+  using test    = finite_element<SQUARE, QOI>;
+  static constexpr int Q  = p + 1;
+  static constexpr int nq = Q * Q;
+  static constexpr int nd = element::ndof * c;
+  using deriv_t           = decltype(boundary_integral::get_derivative_type<0, 2, space>(QF{}));
+
+  static void run(int mode, const QF& qf, int nf, double t, const double* uF, const double* X, const double* J,
+                  double* out)
+  {
+    std::vector<deriv_t>       derivs(size_t(nf) * nq);
+    std::vector<const double*> inputs{uF};
+    std::vector<int>           elements(static_cast<size_t>(nf));
+    for (int e = 0; e < nf; e++) elements[size_t(e)] = e;
+    tuple<element> trial_elements{};
+    if (mode == 0) {
+      std::memset(out, 0, sizeof(double) * size_t(nf));
+      boundary_integral::evaluation_kernel_impl<NO_DIFFERENTIATION, Q, SQUARE>(
+          trial_elements, test{}, t, inputs, out, X, J, qf, derivs.data(), elements.data(), uint32_t(nf),
+          camp::int_seq<int, 0>{});
+      return;
+    }
+    std::vector<double> values(size_t(nf), 0.0);
+    boundary_integral::evaluation_kernel_impl<0, Q, SQUARE>(trial_elements, test{}, t, inputs, values.data(), X, J,
+                                                            qf, derivs.data(), elements.data(), uint32_t(nf),
+                                                            camp::int_seq<int, 0>{});
+    std::memset(out, 0, sizeof(double) * size_t(nf) * nd);
+    ExecArrayView<double, 3, ExecutionSpace::CPU> view(out, {nf, 1, nd});
+    boundary_integral::element_gradient_kernel<SQUARE, QOI, space, Q>(view, derivs.data(), elements.data(),
+                                                                      size_t(nf));
+  }
+};
+
+template <int p, int c>
+int dispatch_qoi(int kind, int boundary, int mode, int n, double t, const double* params, const double* u,
+                 const double* X, const double* J, double* out)
+{
+  if (boundary) {
+    if (kind == QOI_FIELD) {
+      FieldQoI<c> q{{params[0], c > 1 ? params[1] : 0.0, c > 2 ? params[2] : 0.0}};
+      QoiFaceRunner<p, c, FieldQoI<c>>::run(mode, q, n, t, u, X, J, out);
+      return 0;
+    }
+    if (kind == QOI_POLY_TEST) {
+      QoiFaceRunner<p, c, PolyFaceQoI<c>>::run(mode, PolyFaceQoI<c>{}, n, t, u, X, J, out);
+      return 0;
+    }
+    if constexpr (c == 3) {
+      if (kind == QOI_NORMAL_FIELD) {
+        QoiFaceRunner<p, c, NormalFieldQoI>::run(mode, NormalFieldQoI{}, n, t, u, X, J, out);
+        return 0;
+      }
+    }
+    return -1;
+  }
+  if (kind == QOI_FIELD) {
+    FieldQoI<c> q{{params[0], c > 1 ? params[1] : 0.0, c > 2 ? params[2] : 0.0}};
+    QoiDomainRunner<p, c, FieldQoI<c>>::run(mode, q, n, t, u, X, J, out);
+    return 0;
+  }
+  if (kind == QOI_POLY_TEST) {
+    QoiDomainRunner<p, c, PolyQoI<c>>::run(mode, PolyQoI<c>{}, n, t, u, X, J, out);
+    return 0;
+  }
+  if constexpr (c == 3) {
+    if (kind == QOI_NEOHOOKEAN_ENERGY) {
+      QoiDomainRunner<p, c, NeoHookeanEnergyQoI>::run(mode, NeoHookeanEnergyQoI{params[0], params[1]}, n, t, u, X,
+                                                      J, out);
+      return 0;
+    }
+  }
+  return -1;
+}
+
 // ------------------------------------------------------------ domain kernels
 template <int p, int c, typename QF, typename State>
 struct DomainRunner {
@@ -474,6 +687,24 @@ int ref_boundary(int mat, int p, int mode, int nf, double t, const double* param
   try {
     if (p == 1) return dispatch_boundary<1>(mat, mode, nf, t, params, uF, duF, Xq, Jq, out);
     if (p == 2) return dispatch_boundary<2>(mat, mode, nf, t, params, uF, duF, Xq, Jq, out);
+  } catch (const std::exception&) {
+    return -2;
+  }
+  return -1;
+}
+
+// Quantities of interest (functional_qoi.inl; finite_element<g, QOI>,
+// detail/qoi.inl): mode 0 per-element (per-face) values [n], mode 1 element
+// gradients dQ_e/du_e [n][c * nodes].  boundary != 0: faces (Xq [n][3][nq],
+// Jq [n][2][3][nq]).  Integrands that depend on the field only.
+int ref_qoi(int kind, int boundary, int p, int c, int mode, int n, double t, const double* params, const double* u,
+            const double* Xq, const double* Jq, double* out)
+{
+  try {
+    if (p == 1 && c == 1) return dispatch_qoi<1, 1>(kind, boundary, mode, n, t, params, u, Xq, Jq, out);
+    if (p == 1 && c == 3) return dispatch_qoi<1, 3>(kind, boundary, mode, n, t, params, u, Xq, Jq, out);
+    if (p == 2 && c == 1) return dispatch_qoi<2, 1>(kind, boundary, mode, n, t, params, u, Xq, Jq, out);
+    if (p == 2 && c == 3) return dispatch_qoi<2, 3>(kind, boundary, mode, n, t, params, u, Xq, Jq, out);
   } catch (const std::exception&) {
     return -2;
   }

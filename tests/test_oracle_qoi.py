@@ -118,3 +118,29 @@ def test_shape_gradient_of_measures(p):
     ga = area.shape_gradient_fd(u)
     assert abs(ga @ dil - 12.0) <= 1e-7
     assert abs(ga @ trans) <= 1e-7
+
+
+@pytest.mark.parametrize("p", [1, 2])
+@pytest.mark.parametrize("c", [1, 3])
+def test_qoi_matches_reference_kernels(p, c):
+    """Values and gradients against serac's own QoI element kernels
+    (evaluation_kernel_impl / element_gradient_kernel with the QOI test space,
+    compiled from the reference sources into oracle/_ref)."""
+    if O.ref_lib() is None or not hasattr(O.ref_lib(), "ref_qoi"):
+        pytest.skip("reference kernels not built here")
+    m = mesh(3, 2, 2, perturb=0.15, seed=6)
+    rng = np.random.default_rng(7)
+    u = rng.standard_normal(m.num_nodes(p) * c) * (0.01 if c == 3 else 0.1)
+    w = np.arange(1, c + 1, dtype=np.float64)
+    q = O.OracleQoI(m, p, c)
+    q.add_domain_integral(O.QOI_POLY_TEST)
+    q.add_domain_integral(O.QOI_FIELD, w)
+    q.add_boundary_integral(O.QOI_POLY_TEST, [1, 3, 6])
+    q.add_boundary_integral(O.QOI_FIELD, [2], w)
+    if c == 3:
+        q.add_domain_integral(O.QOI_NEOHOOKEAN_ENERGY, [5.0, 0.25])
+        q.add_boundary_integral(O.QOI_NORMAL_FIELD, [4, 5])
+    v, g = q.evaluate(u)
+    rv, rg = q.evaluate_reference(u)
+    assert abs(v - rv) <= 1e-13 * abs(v)
+    assert rel(g, rg) <= 1e-13
