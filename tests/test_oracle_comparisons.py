@@ -1,0 +1,57 @@
+"""serac's functional_comparisons.cpp checks Functional against hand-assembled
+mass / diffusion / load integrators at 1e-14.  mfem is absent here, so the
+comparison is restated analytically: on an unperturbed box every element is
+the same axis-aligned brick, its diffusion stiffness is the Kronecker sum
+k (Kx (x) My (x) Mz + Mx (x) Ky (x) Mz + Mx (x) My (x) Kz) of 1-D matrices built
+from the same Gauss-Legendre points and Gauss-Lobatto basis, and the source
+load is -f (Mx (x) My (x) Mz) 1.  The oracle's heat material (pinned against
+the reference kernels) must reproduce both, element by element and assembled."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.problems import rel
+
+
+def _one_d(p, h):
+    B, G = O.basis_1d(p)
+    _, w = np.polynomial.legendre.leggauss(p + 1)
+    w = 0.5 * w
+    M = (B * (w * h)[:, None]).T @ B
+    K = (G * (w / h)[:, None]).T @ G
+    return M, K
+
+
+@pytest.mark.parametrize("p", [1, 2])
+def test_heat_matches_kronecker_integrators(p):
+    nx, ny, nz = 3, 2, 4
+    m = O.StructuredHexMesh(nx, ny, nz, O.box_vertices(nx, ny, nz, perturb=0.0))
+    k, f = 1.7, 2.1
+    hx, hy, hz = 1.0 / nx, 1.0 / ny, 1.0 / nz
+    Mx, Kx = _one_d(p, hx)
+    My, Ky = _one_d(p, hy)
+    Mz, Kz = _one_d(p, hz)
+    Ke = k * (np.kron(Mz, np.kron(My, Kx)) + np.kron(Mz, np.kron(Ky, Mx)) + np.kron(Kz, np.kron(My, Mx)))
+    Me = np.kron(Mz, np.kron(My, Mx))
+
+    orc = O.OracleFunctional(m, p, 1)
+    orc.add_domain_integral(O.MAT_HEAT, [k, f])
+    rng = np.random.default_rng(0)
+    u = rng.standard_normal(orc.ndofs)
+    # element matrices
+    uE = O.gather(u, orc.conn, 1, orc.nnodes)
+    K = O.element_kernel(O.MAT_HEAT, p, 2, uE, orc.Xq, orc.Jq, [k, f])
+    for e in (0, m.ne // 2, m.ne - 1):
+        assert np.abs(K[e] - Ke).max() <= 1e-13 * np.abs(Ke).max()
+    # assembled residual R = K u - f M 1 and the assembled matrix
+    Kg = np.zeros((orc.ndofs, orc.ndofs))
+    load = np.zeros(orc.ndofs)
+    for e in range(m.ne):
+        idx = orc.conn[e]
+        Kg[np.ix_(idx, idx)] += Ke
+        load[idx] += Me.sum(axis=1)
+    assert rel(orc.residual(u), Kg @ u - f * load) <= 1e-13
+    assert rel(orc.assemble(u).toarray(), Kg) <= 1e-13
+    # Jacobian action of the linear form is the matrix (check_gradient.hpp semantics)
+    du = rng.standard_normal(orc.ndofs)
+    assert rel(orc.jvp(u, du), Kg @ du) <= 1e-13
