@@ -55,3 +55,24 @@ def test_heat_matches_kronecker_integrators(p):
     # Jacobian action of the linear form is the matrix (check_gradient.hpp semantics)
     du = rng.standard_normal(orc.ndofs)
     assert rel(orc.jvp(u, du), Kg @ du) <= 1e-13
+
+
+@pytest.mark.parametrize("p", [1, 2])
+@pytest.mark.parametrize("mat", [O.MAT_HEAT, O.MAT_NEOHOOKEAN])
+def test_patch_test_perturbed_mesh(p, mat):
+    """Patch tests (solid_statics_patch.cpp, thermal_statics_patch.cpp) on a
+    perturbed mesh: a field affine in X is reproduced exactly by the trilinear
+    geometry and the H1 basis, its gradient is uniform, so the residual of a
+    source-free material vanishes at every interior node."""
+    m = O.StructuredHexMesh(3, 3, 3, O.box_vertices(3, 3, 3, perturb=0.25, seed=4))
+    c = O.COMPONENTS[mat]
+    f = O.OracleFunctional(m, p, c)
+    f.add_domain_integral(mat, [1.3, 0.0] if mat == O.MAT_HEAT else [5.0, 0.25])
+    X = m.node_coordinates(p)
+    G = np.array([[0.01, 0.02, -0.01], [0.0, -0.015, 0.01], [0.005, 0.0, 0.02]])[:c]
+    u = (X @ G.T + np.array([0.3, -0.2, 0.1])[:c]).T.ravel()
+    r = f.residual(u).reshape(c, -1)
+    interior = np.setdiff1d(np.arange(f.nnodes), m.boundary_nodes(p, [1, 2, 3, 4, 5, 6]))
+    scale = np.abs(r).max()
+    assert scale > 1e-6
+    assert np.abs(r[:, interior]).max() <= 1e-13 * scale
