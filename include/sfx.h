@@ -236,7 +236,10 @@ typedef struct {
   double* evector;         /* scratch [e][component][node] */
   float* evector_f32;
   const int64_t* row_ptr;  /* CSR rows (num_dofs + 1) or NULL */
-  int nx, ny, nz;
+  int nx, ny, nz;          /* structured forms: elements per direction (0 for table forms) */
+  int general;             /* 1 for forms built by sfx_form_create_from_table */
+  const int64_t* graph_ptr; /* table forms: sorted scalar adjacency [num_nodes + 1] (NULL until the CSR graph is built) */
+  const int32_t* graph_col;
 } sfx_form_layout;
 int sfx_form_get_layout(sfx_form form, sfx_form_layout* out);
 

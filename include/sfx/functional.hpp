@@ -96,11 +96,49 @@ class Mesh {
     m.nz = nz;
     return m;
   }
+  /// Any conforming hexahedral mesh as an element-node table of one order
+  /// (host arrays: elem_nodes [ne][(order+1)^3] lexicographic, the caller's
+  /// node numbering; elem_vertices [ne][8][3]), e.g. an mfem element-dof table;
+  /// forms on it are built by sfx_form_create_from_table.
+  static Mesh FromTable(int order, int64_t num_elements, int64_t num_nodes, const int32_t* elem_nodes,
+                        const double* elem_vertices) {
+    Mesh m;
+    const int64_t npe = int64_t(order + 1) * (order + 1) * (order + 1);
+    m.table_ = std::make_shared<Table>();
+    m.table_->order = order;
+    m.table_->num_elements = num_elements;
+    m.table_->num_nodes = num_nodes;
+    m.table_->nodes.assign(elem_nodes, elem_nodes + num_elements * npe);
+    m.table_->vertices.assign(elem_vertices, elem_vertices + num_elements * 24);
+    return m;
+  }
   sfx_mesh handle() const { return h_.get(); }
+  bool is_table() const { return table_ != nullptr; }
+  /// a new form (or QoI) of order p with c components on this mesh
+  sfx_form create(int p, int c, bool qoi) const {
+    sfx_form h = nullptr;
+    if (table_) {
+      if (p != table_->order) throw std::runtime_error("sfx: the space order must be the element table's order");
+      check(qoi ? sfx_qoi_create_from_table(p, c, table_->num_elements, table_->num_nodes, table_->nodes.data(),
+                                            table_->vertices.data(), &h)
+                : sfx_form_create_from_table(p, c, table_->num_elements, table_->num_nodes, table_->nodes.data(),
+                                             table_->vertices.data(), &h));
+    } else {
+      check(qoi ? sfx_qoi_create(h_.get(), p, c, &h) : sfx_form_create(h_.get(), p, c, &h));
+    }
+    return h;
+  }
   int nx = 0, ny = 0, nz = 0;
 
  private:
+  struct Table {
+    int order = 0;
+    int64_t num_elements = 0, num_nodes = 0;
+    std::vector<int32_t> nodes;
+    std::vector<double> vertices;
+  };
   std::shared_ptr<sfx_mesh_s> h_;
+  std::shared_ptr<Table> table_;
 };
 
 /// Quadrature-point state (quadrature_data.hpp:111-144): one State per point,
@@ -152,6 +190,23 @@ struct UserMaker {
   static constexpr bool value_input = true;
   SFX_HD QF operator()(const double*) const { return qf; }
 };
+
+/// fn(graph) with the CSR column locator of the form behind the layout: the
+/// analytic structured grid or the table form's scalar adjacency
+template <typename Fn>
+void with_graph(const sfx_form_layout& L, int p, Fn&& fn) {
+  if (L.general) {
+    fn(kernels::TableGraph{L.graph_ptr, L.graph_col, L.num_nodes});
+    return;
+  }
+  kernels::GridShape g{};
+  g.p = p;
+  g.ne[0] = L.nx;
+  g.ne[1] = L.ny;
+  g.ne[2] = L.nz;
+  for (int d = 0; d < 3; d++) g.N[d] = int64_t(p) * g.ne[d] + 1;
+  fn(g);
+}
 
 inline unsigned warp_blocks(int64_t ne, int epw) {
   const int64_t warps = (ne + epw - 1) / epw;
@@ -326,14 +381,10 @@ struct BoundaryIntegral {
       kernels::face_diag_kernel<C, NQ><<<scatter_blocks(), 256, 0, s>>>(F.node_ptr, F.node_ids, F.node_ent, K.p, diag,
                                                                          F.num_face_nodes, L.num_nodes);
     if (values) {
-      kernels::GridShape g{};
-      g.p = P;
-      g.ne[0] = L.nx;
-      g.ne[1] = L.ny;
-      g.ne[2] = L.nz;
-      for (int d = 0; d < 3; d++) g.N[d] = int64_t(P) * g.ne[d] + 1;
-      kernels::face_csr_kernel<P, C><<<unsigned((F.num_face_nodes * C + 127) / 128), 128, 0, s>>>(
-          g, L.row_ptr, F.fconn, F.node_ptr, F.node_ids, F.node_ent, K.p, values, F.num_face_nodes);
+      with_graph(L, P, [&](auto g) {
+        kernels::face_csr_kernel<P, C><<<unsigned((F.num_face_nodes * C + 127) / 128), 128, 0, s>>>(
+            g, L.row_ptr, F.fconn, F.node_ptr, F.node_ids, F.node_ent, K.p, values, F.num_face_nodes);
+      });
     }
     check_cuda(cudaGetLastError(), "boundary matrix kernels");
   }
@@ -417,8 +468,7 @@ class Functional<H1<p, c>(H1<p, c>)> {
   };
 
   explicit Functional(const Mesh& mesh) : mesh_(mesh), grad_(this) {
-    sfx_form h = nullptr;
-    check(sfx_form_create(mesh.handle(), p, c, &h));
+    sfx_form h = mesh.create(p, c, false);
     form_ = std::shared_ptr<sfx_form_s>(h, [](sfx_form x) { sfx_form_destroy(x); });
     check(sfx_form_get_layout(h, &L_));
     out_.resize(size_t(L_.num_dofs));
@@ -467,6 +517,19 @@ class Functional<H1<p, c>(H1<p, c>)> {
   template <typename QF>
   void AddSurfaceIntegral(DependsOn<0> d, const QF& qf, int side_mask) {
     AddBoundaryIntegral(Dimension<2>{}, d, qf, side_mask);
+  }
+  /// the same over a face list: face_elem[k] an element, face_side[k] its
+  /// local side (1..6, the box-side numbering in the element's own frame)
+  template <typename QF>
+  void AddBoundaryIntegral(Dimension<2>, DependsOn<0>, const QF& qf, const std::vector<int32_t>& face_elem,
+                           const std::vector<int32_t>& face_side) {
+    if (face_elem.size() != face_side.size()) throw std::runtime_error("sfx: face lists differ in length");
+    auto h = std::make_unique<detail::BoundaryHolder<p, c, QF>>();
+    h->b.qf = qf;
+    check(sfx_form_add_face_set_faces(form_.get(), int64_t(face_elem.size()), face_elem.data(), face_side.data(),
+                                      &h->b.face_set));
+    check(sfx_form_get_face_layout(form_.get(), h->b.face_set, &h->b.F));
+    boundary_.push_back(std::move(h));
   }
 
   /// updateQdata(bool) (functional.hpp:523): commit quadrature state on residual calls
@@ -584,19 +647,15 @@ class Functional<H1<p, c>(H1<p, c>)> {
     constexpr int NDOF = c * points_per_element;
     const int64_t chunk = std::min<int64_t>(L_.num_elements, 16384);
     DeviceArray<double> K(size_t(chunk) * NDOF * NDOF);
-    kernels::GridShape g{};
-    g.p = p;
-    g.ne[0] = L_.nx;
-    g.ne[1] = L_.ny;
-    g.ne[2] = L_.nz;
-    for (int d = 0; d < 3; d++) g.N[d] = int64_t(p) * g.ne[d] + 1;
     bool first = true;
     for (auto& in : integrals_) {
       for (int64_t e0 = 0; e0 < L_.num_elements; e0 += chunk) {
         const int64_t e1 = std::min(L_.num_elements, e0 + chunk);
         in->element_matrices(L_, t_lin_, u_lin_.p, K.p, e0, e1, nullptr);
-        kernels::csr_assemble_kernel<p, c><<<unsigned((L_.num_dofs + 127) / 128), 128>>>(
-            g, L_.row_ptr, L_.conn, L_.node_ptr, L_.node_ent, K.p, e0, e1, A.values->p, !first);
+        detail::with_graph(L_, p, [&](auto g) {
+          kernels::csr_assemble_kernel<p, c><<<unsigned((L_.num_dofs + 127) / 128), 128>>>(
+              g, L_.row_ptr, L_.conn, L_.node_ptr, L_.node_ent, K.p, e0, e1, A.values->p, !first);
+        });
         check_cuda(cudaGetLastError(), "assembly kernel");
         first = false;
       }
@@ -716,8 +775,7 @@ class Functional<double(H1<p, c>)> {
   };
 
   explicit Functional(const Mesh& mesh) : mesh_(mesh), grad_(this) {
-    sfx_form h = nullptr;
-    check(sfx_qoi_create(mesh.handle(), p, c, &h));
+    sfx_form h = mesh.create(p, c, true);
     form_ = std::shared_ptr<sfx_form_s>(h, [](sfx_form x) { sfx_form_destroy(x); });
     check(sfx_form_get_layout(h, &L_));
     g_.resize(size_t(L_.num_dofs));
@@ -738,6 +796,17 @@ class Functional<double(H1<p, c>)> {
   void AddBoundaryIntegral(Dimension<2>, DependsOn<0>, const QF& qf, int side_mask) {
     auto h = std::make_unique<detail::QoiFaces<p, c, QF>>(qf);
     check(sfx_form_add_face_set(form_.get(), side_mask, &h->face_set));
+    check(sfx_form_get_face_layout(form_.get(), h->face_set, &h->F));
+    integrals_.push_back(std::move(h));
+  }
+  /// the same over a face list (element, local side 1..6)
+  template <typename QF>
+  void AddBoundaryIntegral(Dimension<2>, DependsOn<0>, const QF& qf, const std::vector<int32_t>& face_elem,
+                           const std::vector<int32_t>& face_side) {
+    if (face_elem.size() != face_side.size()) throw std::runtime_error("sfx: face lists differ in length");
+    auto h = std::make_unique<detail::QoiFaces<p, c, QF>>(qf);
+    check(sfx_form_add_face_set_faces(form_.get(), int64_t(face_elem.size()), face_elem.data(), face_side.data(),
+                                      &h->face_set));
     check(sfx_form_get_face_layout(form_.get(), h->face_set, &h->F));
     integrals_.push_back(std::move(h));
   }

@@ -506,6 +506,9 @@ int sfx_form_get_layout(sfx_form form, sfx_form_layout* out) {
   L.nx = form->mesh.nx;
   L.ny = form->mesh.ny;
   L.nz = form->mesh.nz;
+  L.general = form->general ? 1 : 0;
+  L.graph_ptr = form->sptr.p;
+  L.graph_col = form->scol.p;
   *out = L;
   return SFX_OK;
 }

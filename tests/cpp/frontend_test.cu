@@ -4,6 +4,7 @@
 // tests/test_gpu_frontend.py and called through ctypes; host arrays in/out.
 #include <cuda_runtime.h>
 
+#include <type_traits>
 #include <vector>
 
 #include "sfx/functional.hpp"
@@ -99,10 +100,9 @@ struct Buffers {
 
 // outputs: residual, residual at linearisation, jv, jv (FP32, as double), diagonal, CSR values
 template <typename FunctionalT, typename Setup>
-int run(int nx, int ny, int nz, const double* V, const double* u, const double* du, double* out_r, double* out_r2,
-        double* out_jv, double* out_jv32, double* out_diag, double* out_csr, int64_t* out_nnz, Setup&& setup) {
+int run_on(const sfx::Mesh& mesh, const double* u, const double* du, double* out_r, double* out_r2, double* out_jv,
+           double* out_jv32, double* out_diag, double* out_csr, int64_t* out_nnz, Setup&& setup) {
   try {
-    auto mesh = sfx::Mesh::StructuredHex(nx, ny, nz, V);
     FunctionalT f(mesh);
     setup(f);
     const size_t n = size_t(f.num_dofs());
@@ -127,6 +127,17 @@ int run(int nx, int ny, int nz, const double* V, const double* u, const double* 
     if (out_csr) cudaMemcpy(out_csr, A.values->p, size_t(A.nnz) * 8, cudaMemcpyDeviceToHost);
     *out_nnz = A.nnz;
     return cudaDeviceSynchronize() == cudaSuccess ? 0 : -2;
+  } catch (const std::exception&) {
+    return -1;
+  }
+}
+
+template <typename FunctionalT, typename Setup>
+int run(int nx, int ny, int nz, const double* V, const double* u, const double* du, double* out_r, double* out_r2,
+        double* out_jv, double* out_jv32, double* out_diag, double* out_csr, int64_t* out_nnz, Setup&& setup) {
+  try {
+    auto mesh = sfx::Mesh::StructuredHex(nx, ny, nz, V);
+    return run_on<FunctionalT>(mesh, u, du, out_r, out_r2, out_jv, out_jv32, out_diag, out_csr, out_nnz, setup);
   } catch (const std::exception&) {
     return -1;
   }
@@ -367,6 +378,60 @@ extern "C" int frontend_neohookean_pressure_transpose(double K, double G, double
     cudaMemcpy(out32.data(), b.jv32, n * 4, cudaMemcpyDeviceToHost);
     for (size_t i = 0; i < n; i++) jt32[i] = out32[i];
     return cudaDeviceSynchronize() == cudaSuccess ? 0 : -2;
+  } catch (const std::exception&) {
+    return -1;
+  }
+}
+
+// Neo-Hookean with a user follower pressure over a face list, on an imported
+// element table (Q2): residual, linearisation, actions, diagonal and CSR
+extern "C" int frontend_table_neohookean_pressure(double K, double G, double pressure, int64_t ne, int64_t nn,
+                                                  const int32_t* table, const double* corners, int64_t nf,
+                                                  const int32_t* face_elem, const int32_t* face_side, const double* u,
+                                                  const double* du, double* r, double* r2, double* jv, double* jv32,
+                                                  double* diag, double* csr, int64_t* nnz) {
+  try {
+    auto mesh = sfx::Mesh::FromTable(2, ne, nn, table, corners);
+    std::vector<int32_t> fe(face_elem, face_elem + nf), fs(face_side, face_side + nf);
+    auto setup = [&](auto& f) {
+      f.AddDomainIntegral(sfx::Dimension<3>{}, sfx::DependsOn<0>{}, UserNeoHookean{K, G});
+      f.AddBoundaryIntegral(sfx::Dimension<2>{}, sfx::DependsOn<0>{}, UserPressure{pressure}, fe, fs);
+    };
+    return run_on<sfx::Functional<sfx::H1<2, 3>(sfx::H1<2, 3>)>>(mesh, u, du, r, r2, jv, jv32, diag, csr, nnz, setup);
+  } catch (const std::exception&) {
+    return -1;
+  }
+}
+
+// scalar QoI (user domain and face integrands) on an imported element table
+extern "C" int frontend_table_qoi_poly(int p, int64_t ne, int64_t nn, const int32_t* table, const double* corners,
+                                       int64_t nf, const int32_t* face_elem, const int32_t* face_side, const double* u,
+                                       const double* du, double* value, double* value2, double* action,
+                                       double* grad) {
+  try {
+    auto mesh = sfx::Mesh::FromTable(p, ne, nn, table, corners);
+    std::vector<int32_t> fe(face_elem, face_elem + nf), fs(face_side, face_side + nf);
+    auto setup = [&](auto& q) {
+      q.AddDomainIntegral(sfx::Dimension<3>{}, sfx::DependsOn<0>{}, UserPolyQoI{});
+      q.AddBoundaryIntegral(sfx::Dimension<2>{}, sfx::DependsOn<0>{}, UserPolyFaceQoI{}, fe, fs);
+    };
+    auto go = [&](auto order) -> int {
+      using QoIT = sfx::Functional<double(sfx::H1<decltype(order)::value, 1>)>;
+      QoIT q(mesh);
+      setup(q);
+      const size_t n = size_t(q.num_dofs());
+      Buffers b(n);
+      cudaMemcpy(b.u, u, n * 8, cudaMemcpyHostToDevice);
+      cudaMemcpy(b.du, du, n * 8, cudaMemcpyHostToDevice);
+      *value = q(0.0, b.u);
+      auto [v2, g] = q(0.0, sfx::differentiate_wrt(b.u));
+      *value2 = v2;
+      *action = g(b.du);
+      cudaMemcpy(grad, assemble(g), n * 8, cudaMemcpyDeviceToHost);
+      return cudaDeviceSynchronize() == cudaSuccess ? 0 : -2;
+    };
+    if (p == 1) return go(std::integral_constant<int, 1>{});
+    return go(std::integral_constant<int, 2>{});
   } catch (const std::exception&) {
     return -1;
   }

@@ -263,3 +263,74 @@ def test_user_transpose_action(cuda, felib):
     assert rel(jt, ref) <= 1e-12
     assert rel(jt32, ref) <= 1e-5
     assert rel(ref, orc.jvp(u, v)) > 1e-6  # the follower pressure makes J non-symmetric
+
+
+_i32p = ctypes.POINTER(ctypes.c_int32)
+
+
+def _ip(a):
+    return a.ctypes.data_as(_i32p)
+
+
+def test_user_qfunctions_on_element_table(cuda, felib):
+    """sfx::Mesh::FromTable (an imported element table: scrambled node ids,
+    element order and element frames) with a user Neo-Hookean domain
+    integral and a user follower pressure over a face list, against the
+    oracle's table path."""
+    from tests.problems import ScrambledTable
+
+    m = mesh(3, 2, 2, perturb=0.1, seed=2)
+    st = ScrambledTable(m, 2, seed=5)
+    tm = O.TableHexMesh(2, st.table, st.corners, st.nn)
+    fe, fs = st.faces_of_sides([3, 6])
+    orc = O.OracleFunctional(tm, 2, 3)
+    orc.add_domain_integral(O.MAT_NEOHOOKEAN, PARAMS[O.MAT_NEOHOOKEAN])
+    orc.add_boundary_integral(O.BMAT_PRESSURE, (fe, fs), [0.7])
+    u, du = fields(orc.ndofs, O.MAT_NEOHOOKEAN, seed=8)
+    outs = [np.zeros(orc.ndofs) for _ in range(5)]
+    A = orc.assemble(u)
+    csr = np.zeros(A.nnz)
+    nnz = ctypes.c_int64()
+    table = np.ascontiguousarray(st.table, dtype=np.int32)
+    corners = np.ascontiguousarray(st.corners)
+    fe32, fs32 = np.ascontiguousarray(fe, dtype=np.int32), np.ascontiguousarray(fs, dtype=np.int32)
+    fn = felib.frontend_table_neohookean_pressure
+    fn.argtypes = ([ctypes.c_double] * 3 + [ctypes.c_int64] * 2 + [_i32p, _dp, ctypes.c_int64, _i32p, _i32p]
+                   + [_dp] * 8 + [ctypes.POINTER(ctypes.c_int64)])
+    K, G = PARAMS[O.MAT_NEOHOOKEAN]
+    rc = fn(K, G, 0.7, m.ne, st.nn, _ip(table), _p(corners), len(fe32), _ip(fe32), _ip(fs32), _p(u), _p(du),
+            *[_p(o) for o in outs], _p(csr), ctypes.byref(nnz))
+    assert rc == 0
+    _check_all(orc, u, du, outs, csr, nnz, A)
+
+
+@pytest.mark.parametrize("p", [1, 2])
+def test_user_qoi_on_element_table(cuda, felib, p):
+    from tests.problems import ScrambledTable
+
+    m = mesh(3, 2, 2, perturb=0.1, seed=4)
+    st = ScrambledTable(m, p, seed=6)
+    tm = O.TableHexMesh(p, st.table, st.corners, st.nn)
+    fe, fs = st.faces_of_sides([1, 3, 6])
+    orc = O.OracleQoI(tm, p, 1)
+    orc.add_domain_integral(O.QOI_POLY_TEST)
+    orc.add_boundary_integral(O.QOI_POLY_TEST, (fe, fs))
+    rng = np.random.default_rng(50 + p)
+    u = rng.standard_normal(orc.ndofs) * 0.1
+    du = rng.standard_normal(orc.ndofs)
+    grad = np.zeros(orc.ndofs)
+    value, value2, action = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    table = np.ascontiguousarray(st.table, dtype=np.int32)
+    corners = np.ascontiguousarray(st.corners)
+    fe32, fs32 = np.ascontiguousarray(fe, dtype=np.int32), np.ascontiguousarray(fs, dtype=np.int32)
+    fn = felib.frontend_table_qoi_poly
+    fn.argtypes = ([ctypes.c_int, ctypes.c_int64, ctypes.c_int64, _i32p, _dp, ctypes.c_int64, _i32p, _i32p, _dp, _dp]
+                   + [ctypes.POINTER(ctypes.c_double)] * 3 + [_dp])
+    rc = fn(p, m.ne, st.nn, _ip(table), _p(corners), len(fe32), _ip(fe32), _ip(fs32), _p(u), _p(du),
+            ctypes.byref(value), ctypes.byref(value2), ctypes.byref(action), _p(grad))
+    assert rc == 0
+    ref_v, ref_g = orc.evaluate(u)
+    assert abs(value.value - ref_v) <= 1e-12 * abs(ref_v)
+    assert value2.value == value.value
+    assert rel(grad, ref_g) <= 1e-12
+    assert abs(action.value - ref_g @ du) <= 1e-12 * np.abs(ref_g).sum() * np.abs(du).max()
