@@ -240,6 +240,8 @@ typedef struct {
   int general;             /* 1 for forms built by sfx_form_create_from_table */
   const int64_t* graph_ptr; /* table forms: sorted scalar adjacency [num_nodes + 1] (NULL until the CSR graph is built) */
   const int32_t* graph_col;
+  const double* elem_vertices; /* [e][3][8] reference corner coordinates */
+  const double* shape;     /* shape displacement [3][num_nodes], NULL when none is set */
 } sfx_form_layout;
 int sfx_form_get_layout(sfx_form form, sfx_form_layout* out);
 
@@ -258,6 +260,7 @@ typedef struct {
   const int32_t* node_ptr;  /* [num_face_nodes + 1] entries per distinct node */
   const int32_t* node_ids;  /* global node of each distinct node */
   const int32_t* node_ent;  /* face * nodes_per_face + local, face order */
+  const double* face_vertices; /* [face][3][4] reference corner coordinates, outward (s, t) order */
 } sfx_face_layout;
 int sfx_form_add_face_set(sfx_form form, int side_mask, int* face_set);
 int sfx_form_add_face_set_faces(sfx_form form, int64_t num_faces, const int32_t* face_elem, const int32_t* face_side,

@@ -38,6 +38,7 @@
 #include "sfx/boundary.cuh"
 #include "sfx/kernels.cuh"
 #include "sfx/qoi.cuh"
+#include "sfx/sensitivity.cuh"
 
 namespace sfx {
 
@@ -208,6 +209,15 @@ void with_graph(const sfx_form_layout& L, int p, Fn&& fn) {
   fn(g);
 }
 
+/// out (+)= node-owner scatter of a 3-component E-vector [e][3][node] (shape space)
+template <int NPE>
+void scatter3(const sfx_form_layout& L, const double* E3, double* out, bool accumulate, cudaStream_t s) {
+  if (L.num_nodes == 0) return;
+  kernels::scatter_kernel<3, NPE, double><<<unsigned((L.num_nodes + 255) / 256), 256, 0, s>>>(
+      E3, L.node_ptr, L.node_ent, out, L.num_nodes, accumulate);
+  check_cuda(cudaGetLastError(), "shape-space scatter");
+}
+
 inline unsigned warp_blocks(int64_t ne, int epw) {
   const int64_t warps = (ne + epw - 1) / epw;
   return unsigned((warps * 32 + 127) / 128);
@@ -225,6 +235,11 @@ struct IntegralBase {
   virtual void diagonal(const sfx_form_layout& L, double* E, cudaStream_t s) = 0;
   virtual void element_matrices(const sfx_form_layout& L, double t, const double* u, double* K, int64_t e0,
                                 int64_t e1, cudaStream_t s) = 0;
+  // shape derivatives: dR_e/dp dshape into E [e][c][node]; (dR_e/dp)^T lam into E3 [e][3][node]
+  virtual void shape_jvp(const sfx_form_layout& L, double t, const double* u, const double* dshape, double* E,
+                         cudaStream_t s) = 0;
+  virtual void shape_vjp(const sfx_form_layout& L, double t, const double* u, const double* lam, double* E3,
+                         cudaStream_t s) = 0;
 };
 
 template <int P, int C, typename QF, typename State>
@@ -297,6 +312,20 @@ struct DomainIntegral : IntegralBase {
         <<<warp_blocks(e1 - e0, EPW), 128, 0, s>>>(a, maker, e0, e1);
     check_cuda(cudaGetLastError(), "element matrix kernel");
   }
+  void shape_jvp(const sfx_form_layout& L, double t, const double* u, const double* dshape, double* E,
+                 cudaStream_t s) override {
+    auto a = args(L, t, u, nullptr, E);
+    kernels::shape_jvp_kernel<P, C, State, Maker>
+        <<<warp_blocks(L.num_elements, EPW), 128, 0, s>>>(a, maker, L.elem_vertices, L.shape, dshape);
+    check_cuda(cudaGetLastError(), "shape jvp kernel");
+  }
+  void shape_vjp(const sfx_form_layout& L, double t, const double* u, const double* lam, double* E3,
+                 cudaStream_t s) override {
+    auto a = args(L, t, u, nullptr, nullptr);
+    kernels::shape_adjoint_kernel<P, C, kernels::SHAPE_VJP, State, Maker>
+        <<<warp_blocks(L.num_elements, EPW), 128, 0, s>>>(a, maker, L.elem_vertices, L.shape, lam, E3);
+    check_cuda(cudaGetLastError(), "shape vjp kernel");
+  }
 };
 
 template <typename T>
@@ -320,6 +349,7 @@ struct BoundaryIntegral {
   int face_set = -1;
   sfx_face_layout F{};
   DeviceArray<double> E;
+  DeviceArray<double> E3;  // shape-space face E-vector
   DeviceArray<float> E32;
   DeviceArray<double> K;
 
@@ -372,6 +402,28 @@ struct BoundaryIntegral {
         e, F.node_ptr, F.node_ids, F.node_ent, out, F.num_face_nodes, L.num_nodes);
     check_cuda(cudaGetLastError(), "boundary transposed jvp kernel");
   }
+  // out += dR_boundary/dp (t, u) dshape
+  void shape_jvp(const sfx_form_layout& L, double t, const double* u, const double* dshape, double* out,
+                 cudaStream_t s) {
+    if (F.num_faces == 0) return;
+    E.resize(size_t(F.num_faces) * C * NQ);
+    kernels::face_shape_jvp_kernel<P, C, QF><<<blocks(), 128, 0, s>>>(args(L, u, (const double*)nullptr, E.p, t), qf,
+                                                                      F.face_vertices, L.shape, dshape);
+    kernels::face_scatter_kernel<C, NQ, double><<<scatter_blocks(), 256, 0, s>>>(
+        E.p, F.node_ptr, F.node_ids, F.node_ent, out, F.num_face_nodes, L.num_nodes);
+    check_cuda(cudaGetLastError(), "boundary shape jvp kernel");
+  }
+  // out3 += (dR_boundary/dp (t, u))^T lam  (3 x num_nodes)
+  void shape_vjp(const sfx_form_layout& L, double t, const double* u, const double* lam, double* out3,
+                 cudaStream_t s) {
+    if (F.num_faces == 0) return;
+    E3.resize(size_t(F.num_faces) * 3 * NQ);
+    kernels::face_shape_adjoint_kernel<P, C, kernels::SHAPE_VJP, QF><<<blocks(), 128, 0, s>>>(
+        args(L, u, (const double*)nullptr, E3.p, t), qf, F.face_vertices, L.shape, lam);
+    kernels::face_scatter_kernel<3, NQ, double><<<scatter_blocks(), 256, 0, s>>>(
+        E3.p, F.node_ptr, F.node_ids, F.node_ent, out3, F.num_face_nodes, L.num_nodes);
+    check_cuda(cudaGetLastError(), "boundary shape vjp kernel");
+  }
   // face element matrices at (t, u), then += into the diagonal and / or the CSR values
   void matrices(const sfx_form_layout& L, double t, const double* u, double* diag, double* values, cudaStream_t s) {
     if (F.num_faces == 0) return;
@@ -399,6 +451,10 @@ struct BoundaryBase {
                        cudaStream_t s) = 0;
   virtual void jvp_transpose(const sfx_form_layout& L, double t, const double* u, const double* v, double* out,
                              cudaStream_t s) = 0;
+  virtual void shape_jvp(const sfx_form_layout& L, double t, const double* u, const double* dshape, double* out,
+                         cudaStream_t s) = 0;
+  virtual void shape_vjp(const sfx_form_layout& L, double t, const double* u, const double* lam, double* out3,
+                         cudaStream_t s) = 0;
   virtual void jvp_transpose_f32(const sfx_form_layout& L, double t, const float* u, const float* v, float* out,
                                  cudaStream_t s) = 0;
   virtual void matrices(const sfx_form_layout& L, double t, const double* u, double* diag, double* values,
@@ -421,6 +477,14 @@ struct BoundaryHolder : BoundaryBase {
   void jvp_transpose(const sfx_form_layout& L, double t, const double* u, const double* v, double* out,
                      cudaStream_t s) override {
     b.template jvp_transpose<double>(L, t, u, v, out, s);
+  }
+  void shape_jvp(const sfx_form_layout& L, double t, const double* u, const double* dshape, double* out,
+                 cudaStream_t s) override {
+    b.shape_jvp(L, t, u, dshape, out, s);
+  }
+  void shape_vjp(const sfx_form_layout& L, double t, const double* u, const double* lam, double* out3,
+                 cudaStream_t s) override {
+    b.shape_vjp(L, t, u, lam, out3, s);
   }
   void jvp_transpose_f32(const sfx_form_layout& L, double t, const float* u, const float* v, float* out,
                          cudaStream_t s) override {
@@ -540,7 +604,33 @@ class Functional<H1<p, c>(H1<p, c>)> {
   /// (shape_aware_functional.hpp:45-172).  Linearise again afterwards.
   void SetShapeDisplacement(const double* shape, cudaStream_t s = nullptr) {
     check(sfx_form_set_shape_displacement(form_.get(), shape, s));
+    check(sfx_form_get_layout(form_.get(), &L_));  // the shape field's device address
     linearized_ = false;
+  }
+
+  /// dr = dR/dp (t, u; p) dshape: the residual differentiated with respect to
+  /// the shape displacement set on the form (ShapeAwareFunctional's argument 0,
+  /// shape_aware_functional.hpp:537-541); dshape: device, 3 * num_nodes doubles
+  void ShapeJvp(double t, const double* u, const double* dshape, double* dr, cudaStream_t s = nullptr) {
+    if (integrals_.empty() && boundary_.empty()) throw std::runtime_error("sfx: no integrals");
+    if (integrals_.empty()) check_cuda(cudaMemsetAsync(dr, 0, sizeof(double) * size_t(L_.num_dofs), s), "memset");
+    for (size_t i = 0; i < integrals_.size(); i++) {
+      integrals_[i]->shape_jvp(L_, t, u, dshape, L_.evector, s);
+      check(sfx_scatter_add(form_.get(), L_.evector, dr, i > 0, s));
+    }
+    for (auto& b : boundary_) b->shape_jvp(L_, t, u, dshape, dr, s);
+  }
+  /// out = (dR/dp (t, u; p))^T lam (3 * num_nodes): the adjoint shape
+  /// sensitivity (computeTimestepShapeSensitivity, solid_mechanics.hpp:1421-1431)
+  void ShapeVjp(double t, const double* u, const double* lam, double* out, cudaStream_t s = nullptr) {
+    if (integrals_.empty() && boundary_.empty()) throw std::runtime_error("sfx: no integrals");
+    e3_.resize(size_t(L_.num_elements) * points_per_element * 3);
+    if (integrals_.empty()) check_cuda(cudaMemsetAsync(out, 0, sizeof(double) * size_t(3 * L_.num_nodes), s), "memset");
+    for (size_t i = 0; i < integrals_.size(); i++) {
+      integrals_[i]->shape_vjp(L_, t, u, lam, e3_.p, s);
+      detail::scatter3<points_per_element>(L_, e3_.p, out, i > 0, s);
+    }
+    for (auto& b : boundary_) b->shape_vjp(L_, t, u, lam, out, s);
   }
 
   /// R(t, u) into a member buffer (functional.hpp:502-513)
@@ -672,7 +762,7 @@ class Functional<H1<p, c>(H1<p, c>)> {
   sfx_form_layout L_{};
   std::vector<std::unique_ptr<detail::IntegralBase>> integrals_;
   std::vector<std::unique_ptr<detail::BoundaryBase>> boundary_;
-  DeviceArray<double> out_, df_, u_lin_;
+  DeviceArray<double> out_, df_, u_lin_, e3_;
   DeviceArray<float> u_lin32_;
   double t_lin_ = 0.0;
   bool linearized_ = false;
@@ -689,6 +779,9 @@ struct QoiBase {
   virtual int64_t count(const sfx_form_layout& L) const = 0;
   virtual void run(int mode, const sfx_form_layout& L, sfx_form form, double t, const double* u, const double* du,
                    double* vals, double* grad, cudaStream_t s) = 0;
+  // out3 += dQ/dp (3 x num_nodes), E3: element scratch [e][3][node]
+  virtual void shape_gradient(const sfx_form_layout& L, double t, const double* u, double* E3, double* out3,
+                              cudaStream_t s) = 0;
 };
 
 template <int P, int C, typename QF>
@@ -702,6 +795,15 @@ struct QoiDomain : QoiBase {
     kernels::DomainArgs<double> a{u, du, L.evector, L.conn, L.geom, nullptr, nullptr, L.num_nodes, L.num_elements, t};
     kernels::qoi_domain_kernel<P, C, MODE, QF><<<warp_blocks(L.num_elements, EPW), 128, 0, s>>>(a, qf, vals);
     check_cuda(cudaGetLastError(), "QoI kernel");
+  }
+  void shape_gradient(const sfx_form_layout& L, double t, const double* u, double* E3, double* out3,
+                      cudaStream_t s) override {
+    if (L.num_elements == 0) return;
+    kernels::DomainArgs<double> a{u, nullptr, nullptr, L.conn, L.geom, nullptr, nullptr, L.num_nodes, L.num_elements, t};
+    kernels::shape_adjoint_kernel<P, C, kernels::SHAPE_QOI, Nothing, UserMaker<QF>>
+        <<<warp_blocks(L.num_elements, EPW), 128, 0, s>>>(a, UserMaker<QF>{qf}, L.elem_vertices, L.shape, nullptr, E3);
+    check_cuda(cudaGetLastError(), "QoI shape kernel");
+    scatter3<(P + 1) * (P + 1) * (P + 1)>(L, E3, out3, true, s);
   }
   void run(int mode, const sfx_form_layout& L, sfx_form form, double t, const double* u, const double* du,
            double* vals, double* grad, cudaStream_t s) override {
@@ -723,6 +825,7 @@ struct QoiFaces : QoiBase {
   int face_set = -1;
   sfx_face_layout F{};
   DeviceArray<double> E;
+  DeviceArray<double> E3;
   explicit QoiFaces(const QF& q) : qf(q) {}
   int64_t count(const sfx_form_layout&) const override { return F.num_faces; }
   template <int MODE>
@@ -730,6 +833,17 @@ struct QoiFaces : QoiBase {
     kernels::FaceArgs<double> a{u, du, E.p, F.fconn, F.fgeom, L.num_nodes, F.num_faces, t};
     kernels::qoi_face_kernel<P, C, MODE, QF><<<warp_blocks(F.num_faces, FPW), 128, 0, s>>>(a, qf, vals);
     check_cuda(cudaGetLastError(), "face QoI kernel");
+  }
+  void shape_gradient(const sfx_form_layout& L, double t, const double* u, double*, double* out3,
+                      cudaStream_t s) override {
+    if (F.num_faces == 0) return;
+    E3.resize(size_t(F.num_faces) * 3 * NQ);
+    kernels::FaceArgs<double> a{u, nullptr, E3.p, F.fconn, F.fgeom, L.num_nodes, F.num_faces, t};
+    kernels::face_shape_adjoint_kernel<P, C, kernels::SHAPE_QOI, QF><<<warp_blocks(F.num_faces, FPW), 128, 0, s>>>(
+        a, qf, F.face_vertices, L.shape, nullptr);
+    kernels::face_scatter_kernel<3, NQ, double><<<unsigned((F.num_face_nodes + 255) / 256), 256, 0, s>>>(
+        E3.p, F.node_ptr, F.node_ids, F.node_ent, out3, F.num_face_nodes, L.num_nodes);
+    check_cuda(cudaGetLastError(), "face QoI shape kernels");
   }
   void run(int mode, const sfx_form_layout& L, sfx_form, double t, const double* u, const double* du, double* vals,
            double* grad, cudaStream_t s) override {
@@ -813,6 +927,14 @@ class Functional<double(H1<p, c>)> {
   /// evaluate on X + shape (device, 3 * num_nodes doubles; nullptr = none)
   void SetShapeDisplacement(const double* shape, cudaStream_t s = nullptr) {
     check(sfx_form_set_shape_displacement(form_.get(), shape, s));
+    check(sfx_form_get_layout(form_.get(), &L_));  // the shape field's device address
+  }
+  /// dQ/dp (t, u; p) into out (device, 3 * num_nodes doubles)
+  void ShapeGradient(double t, const double* u, double* out, cudaStream_t s = nullptr) {
+    if (integrals_.empty()) throw std::runtime_error("sfx: no integrals");
+    e3_.resize(size_t(L_.num_elements) * size_t((p + 1) * (p + 1) * (p + 1)) * 3);
+    check_cuda(cudaMemsetAsync(out, 0, sizeof(double) * size_t(3 * L_.num_nodes), s), "memset");
+    for (auto& in : integrals_) in->shape_gradient(L_, t, u, e3_.p, out, s);
   }
 
   /// Q(t, u) into a device double
@@ -879,7 +1001,7 @@ class Functional<double(H1<p, c>)> {
   std::shared_ptr<sfx_form_s> form_;
   sfx_form_layout L_{};
   std::vector<std::unique_ptr<detail::QoiBase>> integrals_;
-  DeviceArray<double> g_, u_lin_, value_, partial_, vals_;
+  DeviceArray<double> g_, u_lin_, value_, partial_, vals_, e3_;
   double t_lin_ = 0.0;
   bool linearized_ = false;
   Gradient grad_;

@@ -501,6 +501,7 @@ extern "C" int sfx_form_get_face_layout(sfx_form form, int face_set, sfx_face_la
   L.node_ptr = bi.node_ptr.p;
   L.node_ids = bi.node_ids.p;
   L.node_ent = bi.node_ent.p;
+  L.face_vertices = bi.Xf.p;
   *out = L;
   return SFX_OK;
 }

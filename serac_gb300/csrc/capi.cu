@@ -509,6 +509,8 @@ int sfx_form_get_layout(sfx_form form, sfx_form_layout* out) {
   L.general = form->general ? 1 : 0;
   L.graph_ptr = form->sptr.p;
   L.graph_col = form->scol.p;
+  L.elem_vertices = form->Xe.p;
+  L.shape = form->has_shape ? form->shape.p : nullptr;
   *out = L;
   return SFX_OK;
 }

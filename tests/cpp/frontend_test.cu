@@ -436,3 +436,46 @@ extern "C" int frontend_table_qoi_poly(int p, int64_t ne, int64_t nn, const int3
     return -1;
   }
 }
+
+// shape derivatives of user q-functions on a shape-displaced configuration:
+// dR/dp dshape and (dR/dp)^T lam of Neo-Hookean + follower pressure (Q2), and
+// dQ/dp of the user energy + normal-displacement QoI
+extern "C" int frontend_shape_sensitivity(double K, double G, double pressure, int side_mask, int nx, int ny, int nz,
+                                          const double* V, const double* shape_host, const double* u_host,
+                                          const double* dshape_host, const double* lam_host, double* jvp_out,
+                                          double* vjp_out, double* qoi_shape_out) {
+  try {
+    auto mesh = sfx::Mesh::StructuredHex(nx, ny, nz, V);
+    sfx::Functional<sfx::H1<2, 3>(sfx::H1<2, 3>)> f(mesh);
+    f.AddDomainIntegral(sfx::Dimension<3>{}, sfx::DependsOn<0>{}, UserNeoHookean{K, G});
+    f.AddBoundaryIntegral(sfx::Dimension<2>{}, sfx::DependsOn<0>{}, UserPressure{pressure}, side_mask);
+    sfx::Functional<double(sfx::H1<2, 3>)> q(mesh);
+    q.AddDomainIntegral(sfx::Dimension<3>{}, sfx::DependsOn<0>{}, UserEnergyQoI{K, G});
+    q.AddBoundaryIntegral(sfx::Dimension<2>{}, sfx::DependsOn<0>{}, UserNormalQoI{}, side_mask);
+    const size_t n = size_t(f.num_dofs()), ns = n;  // 3 components: the shape space has as many entries
+    double *shape, *u, *dshape, *lam, *a, *b, *c;
+    cudaMalloc(&shape, ns * 8);
+    cudaMalloc(&u, n * 8);
+    cudaMalloc(&dshape, ns * 8);
+    cudaMalloc(&lam, n * 8);
+    cudaMalloc(&a, n * 8);
+    cudaMalloc(&b, ns * 8);
+    cudaMalloc(&c, ns * 8);
+    cudaMemcpy(shape, shape_host, ns * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(u, u_host, n * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(dshape, dshape_host, ns * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(lam, lam_host, n * 8, cudaMemcpyHostToDevice);
+    f.SetShapeDisplacement(shape);
+    q.SetShapeDisplacement(shape);
+    f.ShapeJvp(0.0, u, dshape, a);
+    f.ShapeVjp(0.0, u, lam, b);
+    q.ShapeGradient(0.0, u, c);
+    cudaMemcpy(jvp_out, a, n * 8, cudaMemcpyDeviceToHost);
+    cudaMemcpy(vjp_out, b, ns * 8, cudaMemcpyDeviceToHost);
+    cudaMemcpy(qoi_shape_out, c, ns * 8, cudaMemcpyDeviceToHost);
+    for (double* x : {shape, u, dshape, lam, a, b, c}) cudaFree(x);
+    return cudaDeviceSynchronize() == cudaSuccess ? 0 : -2;
+  } catch (const std::exception&) {
+    return -1;
+  }
+}

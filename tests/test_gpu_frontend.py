@@ -334,3 +334,43 @@ def test_user_qoi_on_element_table(cuda, felib, p):
     assert value2.value == value.value
     assert rel(grad, ref_g) <= 1e-12
     assert abs(action.value - ref_g @ du) <= 1e-12 * np.abs(ref_g).sum() * np.abs(du).max()
+
+
+def test_user_shape_sensitivities(cuda, felib):
+    """Front-end shape derivatives of user q-functions (ShapeJvp, ShapeVjp,
+    and the QoI's ShapeGradient) against the C ABI's built-in Neo-Hookean,
+    follower pressure, stored-energy and normal-displacement integrands on the
+    same shape-displaced configuration."""
+    import torch
+
+    import serac_gb300 as sg
+
+    dims = (3, 2, 2)
+    m = mesh(*dims, perturb=0.1, seed=2)
+    K, G = PARAMS[O.MAT_NEOHOOKEAN]
+    sides = [3, 6]
+    mask = sum(1 << (s - 1) for s in sides)
+    nn = m.num_nodes(2)
+    rng = np.random.default_rng(61)
+    shape = rng.standard_normal(3 * nn) * 0.01
+    u = rng.standard_normal(3 * nn) * 0.01
+    dshape = rng.standard_normal(3 * nn)
+    lam = rng.standard_normal(3 * nn)
+    jvp, vjp, qsh = (np.zeros(3 * nn) for _ in range(3))
+    V = np.ascontiguousarray(m.vertices)
+    rc = felib.frontend_shape_sensitivity(ctypes.c_double(K), ctypes.c_double(G), ctypes.c_double(0.7), mask, *dims,
+                                          _p(V), _p(shape), _p(u), _p(dshape), _p(lam), _p(jvp), _p(vjp), _p(qsh))
+    assert rc == 0
+    M = sg.Mesh.structured_hex(*dims, m.vertices)
+    f = sg.Functional(M, sg.H1(2, 3))
+    f.AddDomainIntegral(sg.NEOHOOKEAN, [K, G])
+    f.AddBoundaryIntegral(sg.PRESSURE, sides, [0.7])
+    f.set_shape_displacement(torch.tensor(shape, device=cuda))
+    g = sg.ShapeGradient(f, 0.0, torch.tensor(u, device=cuda))
+    assert rel(jvp, g(torch.tensor(dshape, device=cuda)).cpu().numpy()) <= 1e-10
+    assert rel(vjp, g.MultTranspose(torch.tensor(lam, device=cuda)).cpu().numpy()) <= 1e-10
+    q = sg.QoI(M, sg.H1(2, 3))
+    q.AddDomainIntegral(sg.QOI_NEOHOOKEAN_ENERGY, [K, G])
+    q.AddBoundaryIntegral(sg.QOI_NORMAL_FIELD, sides)
+    q.set_shape_displacement(torch.tensor(shape, device=cuda))
+    assert rel(qsh, q.shape_gradient(0.0, torch.tensor(u, device=cuda)).cpu().numpy()) <= 1e-9
