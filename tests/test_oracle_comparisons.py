@@ -76,3 +76,56 @@ def test_patch_test_perturbed_mesh(p, mat):
     scale = np.abs(r).max()
     assert scale > 1e-6
     assert np.abs(r[:, interior]).max() <= 1e-13 * scale
+
+
+def _one_d_mixed(p, h):
+    """D[i, j] = int phi_i' phi_j over one 1-D element of length h."""
+    B, G = O.basis_1d(p)
+    _, w = np.polynomial.legendre.leggauss(p + 1)
+    w = 0.5 * w
+    return (G * w[:, None]).T @ B
+
+
+@pytest.mark.parametrize("p", [1, 2])
+def test_neohookean_tangent_at_rest_is_linear_elasticity(p):
+    """The vector half of functional_comparisons.cpp (StressFunctor at
+    1e-14): the Neo-Hookean element stiffness at u = 0 equals isotropic
+    linear elasticity with lambda = K - 2G/3, mu = G, built on an unperturbed
+    box from the 1-D integrals of phi phi, phi' phi' and phi' phi."""
+    nx, ny, nz = 2, 3, 2
+    m = O.StructuredHexMesh(nx, ny, nz, O.box_vertices(nx, ny, nz, perturb=0.0))
+    Kb, G = 5.0, 0.25
+    lam = Kb - 2.0 * G / 3.0
+    hs = (1.0 / nx, 1.0 / ny, 1.0 / nz)
+    one = [_one_d(p, h) for h in hs]  # (M, S) per direction
+    Dm = [_one_d_mixed(p, h) for h in hs]
+    npe = (p + 1) ** 3
+
+    def grad_pair(k, l):
+        """int d_k phi_a d_l phi_b (a: test node, b: trial node), lexicographic."""
+        f = []
+        for d in range(3):
+            M, S = one[d]
+            if d == k and d == l:
+                f.append(S)
+            elif d == k:
+                f.append(Dm[d])
+            elif d == l:
+                f.append(Dm[d].T)
+            else:
+                f.append(M)
+        return np.kron(f[2], np.kron(f[1], f[0]))
+
+    Gkl = [[grad_pair(k, l) for l in range(3)] for k in range(3)]
+    lap = Gkl[0][0] + Gkl[1][1] + Gkl[2][2]
+    A = np.zeros((3 * npe, 3 * npe))  # [test (i, a)][trial (j, b)]
+    for i in range(3):
+        for j in range(3):
+            blk = lam * Gkl[i][j] + G * Gkl[j][i] + (G * lap if i == j else 0.0)
+            A[i * npe:(i + 1) * npe, j * npe:(j + 1) * npe] = blk
+    orc = O.OracleFunctional(m, p, 3)
+    orc.add_domain_integral(O.MAT_NEOHOOKEAN, [Kb, G])
+    uE = np.zeros((m.ne, 3 * npe))
+    K = O.element_kernel(O.MAT_NEOHOOKEAN, p, 2, uE, orc.Xq, orc.Jq, [Kb, G])
+    for e in range(m.ne):
+        assert np.abs(K[e].T - A).max() <= 1e-13 * np.abs(A).max()
