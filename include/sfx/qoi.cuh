@@ -14,7 +14,8 @@
 //                 Gradient::assemble(), functional_qoi.inl:422-475 — plus the
 //                 per-element values
 // Per-element (per-face) values are summed along the lanes in a fixed order,
-// and the host side reduces them with a fixed-shape tree: deterministic.
+// then reduced on the device by a two-pass fixed-shape tree (qoi_sum):
+// deterministic.
 #pragma once
 
 #include "sfx/boundary.cuh"

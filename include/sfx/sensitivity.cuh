@@ -23,9 +23,9 @@
 namespace sfx {
 namespace kernels {
 
-/// Per-lane geometry of one element point for the shape seeds: the reference
-/// trilinear position and Jacobian plus the shape field's value and parent
-/// gradient (the dual parts are set per seed).
+/// Reference (trilinear) position X and Jacobian dX/dxi at the Gauss point
+/// (ix, iy, iz) of an element with vertices Xv [3][8]; the callers add the
+/// shape field's value and parent gradient and set the dual parts per seed.
 template <int Q>
 SFX_HDI void reference_point_geometry(const double* Xv, int ix, int iy, int iz, double X[3], double J[3][3]) {
   const double sp[3] = {gl_point(Q, ix), gl_point(Q, iy), gl_point(Q, iz)};
