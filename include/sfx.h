@@ -30,6 +30,8 @@
  *                                   AddDomainIntegral :159-189, AddBoundaryIntegral :201-228, operator() :379-392,
  *                                   Gradient::operator() :420, Gradient::assemble :422-475
  *   sfx_csr_* / sfx_assemble_csr    numerics/functional/functional.hpp:569-667 assemble(Gradient&)
+ *   sfx_set_param_field             physics/base_physics.hpp:300 BasePhysics::setParameter (a parameter
+ *                                   field of the physics module), as per-element values
  *   sfx_update_qdata                numerics/functional/functional.hpp:523 updateQdata(bool)
  *   sfx_set_qdata / sfx_get_qdata   numerics/functional/quadrature_data.hpp:111-144 QuadratureData<T>
  */
@@ -119,6 +121,12 @@ int sfx_form_num_dofs(sfx_form form, int64_t* out);
  * nparams values used for every element.  At most one domain integral per
  * form in this version. */
 int sfx_form_add_domain_integral(sfx_form form, int material, const double* params, int per_element);
+
+/* Replace the material parameters of domain integral `integral` (0-based, in
+ * the order added; params: host, as for sfx_form_add_domain_integral) without
+ * rebuilding the form: a parameter field updated between evaluations, e.g. in
+ * a design loop.  Synchronous; the form must be linearised again. */
+int sfx_set_param_field(sfx_form form, int integral, const double* params, int per_element);
 
 /* Boundary integral over the faces of the sides in side_mask; params: host. */
 int sfx_form_add_boundary_integral(sfx_form form, int bmaterial, int side_mask, const double* params);

@@ -328,6 +328,21 @@ int sfx_form_add_domain_integral(sfx_form form, int material, const double* para
   return SFX_OK;
 }
 
+int sfx_set_param_field(sfx_form form, int integral, const double* params, int per_element) {
+  if (check_form(form)) return SFX_ERR_INVALID;
+  if (integral < 0 || size_t(integral) >= form->domain.size()) return fail(SFX_ERR_INVALID, "no such domain integral");
+  DomainIntegral& di = form->domain[size_t(integral)];
+  if (di.nparams == 0) return fail(SFX_ERR_INVALID, "the material takes no parameters");
+  if (!params) return fail(SFX_ERR_INVALID, "null parameters");
+  std::vector<double> prm(size_t(form->ne) * size_t(di.nparams));
+  for (int64_t e = 0; e < form->ne; e++)
+    for (int k = 0; k < di.nparams; k++)
+      prm[size_t(e * di.nparams + k)] = per_element ? params[e * di.nparams + k] : params[k];
+  SFX_CUDA_TRY(cudaMemcpy(di.params.p, prm.data(), prm.size() * sizeof(double), cudaMemcpyHostToDevice));
+  form->linearized = false;  // the stored tangent belongs to the old parameters
+  return SFX_OK;
+}
+
 int sfx_residual(sfx_form form, double t, const double* u, double* r, void* stream) {
   if (check_form(form)) return SFX_ERR_INVALID;
   if (!u || !r) return fail(SFX_ERR_INVALID, "null vector");

@@ -269,6 +269,17 @@ class Functional:
     add_domain_integral = AddDomainIntegral
     AddVolumeIntegral = AddDomainIntegral
 
+    def set_parameters(self, params, per_element=False, integral=0):
+        """Replace the material parameters of a domain integral (the order of
+        AddDomainIntegral calls) in place; linearise again afterwards."""
+        material = self._materials[integral]
+        np_ = NPARAMS[material]
+        arr = np.ascontiguousarray(np.asarray(params, dtype=np.float64).ravel())
+        expect = self.mesh.num_elements * np_ if per_element else np_
+        if arr.size != expect:
+            raise ValueError(f"expected {expect} parameters, got {arr.size}")
+        _lib.call("sfx_set_param_field", self._h, int(integral), arr.ctypes.data_as(_lib._dp), int(per_element))
+
     def AddBoundaryIntegral(self, material, sides=None, params=None, faces=None):
         """Over the box sides (structured meshes) or a face list
         faces = (element array, local side array)."""

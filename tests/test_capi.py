@@ -82,5 +82,6 @@ def test_new_entry_points_validate_before_touching_a_device():
                  lambda: lib.sfx_form_set_tangent_storage(None, 1),
                  lambda: lib.sfx_form_add_boundary_integral_faces(None, 0, 0, None, None, None),
                  lambda: lib.sfx_form_add_face_set_faces(None, 0, None, None, None),
-                 lambda: lib.sfx_solver_solve_adjoint(None, 0.0, None, None, None, None)):
+                 lambda: lib.sfx_solver_solve_adjoint(None, 0.0, None, None, None, None),
+                 lambda: lib.sfx_set_param_field(None, 0, None, 0)):
         assert call() == -1
