@@ -22,6 +22,14 @@ Reference semantics followed:
   * Krylov: textbook CG (Saad, Iterative Methods, Alg. 6.18) and restarted
     right-preconditioned GMRES (Alg. 9.5 in its flexible form) with Jacobi
   * Newton without line search (equation_solver.cpp:79-200, max_line_search_iterations = 0)
+  * Quantities of interest (functional_qoi.inl:58-528, finite_element<g, QOI>):
+    q det(J) w summed over points, dQ/du assembled from hand-derived partials
+    (OracleQoI); checked against serac's own QOI element kernels when the
+    reference library is built (OracleQoI.evaluate_reference)
+  * Adjoint operators: J^T from the assembled matrix; shape sensitivities
+    (dR/dp)^T lam and dQ/dp by central differences over the shape dofs
+  * Imported element tables (TableHexMesh): element-node tables of one order
+    with element corners, faces as (element, local side) pairs
 
 Mesh numbering (shared with the product by specification, not by code):
   vertices   v(i,j,k) = i + (nx+1) (j + (ny+1) k), i in [0, nx]
