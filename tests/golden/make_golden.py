@@ -3,9 +3,10 @@ kernels (oracle/_ref/libserac_ref.so, built by ``make -C oracle ref`` from the
 reference sources) plus the oracle's global layer (gather / scatter / CSR).
 
 Run from the repository root where the reference tree is present:
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref && python tests/golden/make_golden.py [qoi]
 Inputs are regenerated from the seeds stored in each file; outputs are the
-reference's numbers.
+reference's numbers.  ``qoi`` writes only the quantity-of-interest fixtures
+(values and gradients from serac's QOI element kernels).
 """
 import os
 import sys
@@ -40,6 +41,32 @@ BOUNDARY_CASES = [
     ("traction_p1", O.BMAT_TRACTION, 1, (2, 1, 2), (2, 5, 6), [0.1, 0.2, 0.3, 0.5, -0.4, 0.2], 12),
     ("pressure_p2", O.BMAT_PRESSURE, 2, (1, 2, 1), (1, 2, 3, 4, 5, 6), [0.7], 13),
 ]
+
+
+QOI_CASES = [
+    # name, order, components, dims, domain integrands, face integrands, seed
+    ("qoi_poly_p1", 1, 1, (2, 2, 2), [(O.QOI_POLY_TEST, None), (O.QOI_FIELD, [1.5])],
+     [(O.QOI_POLY_TEST, [1, 3, 6], None)], 21),
+    ("qoi_poly_p2", 2, 1, (2, 1, 2), [(O.QOI_POLY_TEST, None)], [(O.QOI_POLY_TEST, [2, 5], None),
+                                                              (O.QOI_FIELD, [4], [0.5])], 22),
+    ("qoi_energy_p2", 2, 3, (2, 1, 1), [(O.QOI_NEOHOOKEAN_ENERGY, [5.0, 0.25]), (O.QOI_FIELD, [1.0, 0.0, -2.0])],
+     [(O.QOI_NORMAL_FIELD, [1, 6], None), (O.QOI_POLY_TEST, [3], None)], 23),
+]
+
+
+def qoi_case(name, p, c, dims, domain, faces, seed):
+    m = mesh(*dims, perturb=0.15, seed=seed)
+    q = O.OracleQoI(m, p, c)
+    for kind, params in domain:
+        q.add_domain_integral(kind, params)
+    for kind, sides, params in faces:
+        q.add_boundary_integral(kind, sides, params)
+    rng = np.random.default_rng(seed)
+    u = rng.standard_normal(q.ndofs) * (0.01 if c == 3 else 0.1)
+    value, grad = q.evaluate_reference(u)
+    out = {"dims": np.array(dims), "order": p, "components": c, "seed": seed, "u": u, "value": value,
+           "gradient": grad}
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
 
 
 def domain_case(name, mat, p, dims, perturb, seed):
@@ -80,8 +107,12 @@ def boundary_case(name, bmat, p, dims, sides, params, seed):
 if __name__ == "__main__":
     if O.ref_lib() is None:
         sys.exit("reference checker not built: make -C oracle ref")
-    for case in DOMAIN_CASES:
-        domain_case(*case)
-    for case in BOUNDARY_CASES:
-        boundary_case(*case)
-    print("wrote", len(DOMAIN_CASES) + len(BOUNDARY_CASES), "fixtures")
+    qoi_only = len(sys.argv) > 1 and sys.argv[1] == "qoi"
+    if not qoi_only:
+        for case in DOMAIN_CASES:
+            domain_case(*case)
+        for case in BOUNDARY_CASES:
+            boundary_case(*case)
+    for case in QOI_CASES:
+        qoi_case(*case)
+    print("wrote", len(QOI_CASES) + (0 if qoi_only else len(DOMAIN_CASES) + len(BOUNDARY_CASES)), "fixtures")

@@ -144,3 +144,33 @@ def test_qoi_matches_reference_kernels(p, c):
     rv, rg = q.evaluate_reference(u)
     assert abs(v - rv) <= 1e-13 * abs(v)
     assert rel(g, rg) <= 1e-13
+
+
+def _qoi_cases():
+    import importlib.util
+    import os
+
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "make_golden.py")
+    spec = importlib.util.spec_from_file_location("make_golden", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.QOI_CASES
+
+
+@pytest.mark.parametrize("case", _qoi_cases(), ids=lambda c: c[0])
+def test_qoi_matches_golden_fixtures(case):
+    """Values and gradients against the committed fixtures written from
+    serac's own QOI element kernels (tests/golden/make_golden.py qoi)."""
+    import os
+
+    name, p, c, dims, domain, faces, seed = case
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", f"{name}.npz"))
+    m = mesh(*dims, perturb=0.15, seed=seed)
+    q = O.OracleQoI(m, p, c)
+    for kind, params in domain:
+        q.add_domain_integral(kind, params)
+    for kind, sides, params in faces:
+        q.add_boundary_integral(kind, sides, params)
+    v, grad = q.evaluate(g["u"])
+    assert abs(v - float(g["value"])) <= 1e-13 * abs(float(g["value"]))
+    assert rel(grad, g["gradient"]) <= 1e-13
