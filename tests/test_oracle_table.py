@@ -42,3 +42,48 @@ def test_scrambled_table_matches_structured(p, mat):
     Pm = sp.csr_matrix((np.ones(len(P)), (P, np.arange(len(P)))), shape=(len(P), len(P)))
     A, B = a.assemble(u), b.assemble(un)
     assert abs(Pm @ A @ Pm.T - B).max() <= 1e-13 * abs(A).max()
+
+
+@pytest.mark.parametrize("p", [1, 2])
+def test_every_frame_rotation(p):
+    """All 24 proper rotations of one element's local frame (the other element
+    keeps its frame) leave the residual, Jacobian action and boundary
+    integrals unchanged."""
+    from tests.problems import _SIDE_OF, _DIR_OF, _local_map
+
+    m = mesh(2, 1, 1, perturb=0.0)
+    V = m.vertices.copy()
+    V[:, 2] += 0.05 * V[:, 0] * V[:, 1]  # not a brick
+    m = O.StructuredHexMesh(2, 1, 1, V)
+    n = p + 1
+    conn = m.elem_nodes(p)
+    Xe = m.elem_coords()
+    ref = O.OracleFunctional(m, p, 3)
+    ref.add_domain_integral(O.MAT_NEOHOOKEAN, PARAMS[O.MAT_NEOHOOKEAN])
+    ref.add_boundary_integral(O.BMAT_PRESSURE, [3, 6], [0.7])
+    rng = np.random.default_rng(2)
+    u = rng.standard_normal(ref.ndofs) * 0.02
+    du = rng.standard_normal(ref.ndofs)
+    r0, j0 = ref.residual(u), ref.jvp(u, du)
+    for R in cube_rotations():
+        table = conn.copy()
+        corners = Xe.transpose(0, 2, 1).copy()
+        table[1] = conn[1][_local_map(R, n)]
+        corners[1] = Xe[1].T[_local_map(R, 2)]
+        # faces of box sides 3 (x = 1, element 1 only) and 6 (z = 1, both elements)
+        elems, sides = [], []
+        for e, s in ((1, 3), (0, 6), (1, 6)):
+            ax, hi = _DIR_OF[s]
+            d = np.zeros(3, dtype=np.int64)
+            d[ax] = 1 if hi else -1
+            if e == 1:
+                d = R @ d
+            axn = int(np.flatnonzero(d)[0])
+            elems.append(e)
+            sides.append(_SIDE_OF[(axn, 1 if d[axn] > 0 else 0)])
+        tm = O.TableHexMesh(p, table, corners, m.num_nodes(p))
+        f = O.OracleFunctional(tm, p, 3)
+        f.add_domain_integral(O.MAT_NEOHOOKEAN, PARAMS[O.MAT_NEOHOOKEAN])
+        f.add_boundary_integral(O.BMAT_PRESSURE, (np.array(elems), np.array(sides)), [0.7])
+        assert rel(f.residual(u), r0) <= 1e-13
+        assert rel(f.jvp(u, du), j0) <= 1e-13
