@@ -2,7 +2,9 @@
 // models (include/sfx/dual.hpp, tensor.hpp, materials.hpp: the same headers
 // the device kernels compile), in the manner of serac's test_tensor_ad.cpp:
 // every directional derivative carried by a dual number is compared with a
-// central difference of the value.  Built with g++ by tests/test_ad_host.py;
+// central difference of the value (materials, heat q-functions and the
+// boundary models, including the face-Jacobian derivative of the follower
+// pressure that the shape-sensitivity kernels use).  Built with g++ by tests/test_ad_host.py;
 // prints one line per failed check and exits non-zero on failure.
 #include <cmath>
 #include <cstdio>
@@ -141,6 +143,86 @@ int main() {
         return j2(st, A);
       }, H, dH, 2e-6);
     }
+  }
+
+  // heat q-functions: source and flux as functions of (u, grad u)
+  for (int trial = 0; trial < 5; trial++) {
+    const double u0 = 0.4 * U(gen), du0 = U(gen);
+    tensor<double, 3> g0{}, dg0{};
+    for (int i = 0; i < 3; i++) {
+      g0[i] = U(gen);
+      dg0[i] = U(gen);
+    }
+    heat_transfer::NonlinearHeatIntegrand nl{1.2, 0.7, 0.3};
+    auto flux_at = [&](auto uu, auto gg) {
+      tensor<double, 3> x{};
+      return get<1>(nl(0.0, tuple{x, tensor<double, 3, 3>{}}, tuple{uu, gg}));
+    };
+    tensor<S, 3> gs{};
+    for (int i = 0; i < 3; i++) gs[i] = S{g0[i], dg0[i]};
+    const auto ad = flux_at(S{u0, du0}, gs);
+    const double h = 1e-6;
+    tensor<double, 3> gp{}, gm{};
+    for (int i = 0; i < 3; i++) {
+      gp[i] = g0[i] + h * dg0[i];
+      gm[i] = g0[i] - h * dg0[i];
+    }
+    const auto fp = flux_at(u0 + h * du0, gp), fm = flux_at(u0 - h * du0, gm);
+    for (int i = 0; i < 3; i++) expect_close("nonlinear heat flux", ad[i].gradient, (fp[i] - fm[i]) / (2 * h), 1e-8);
+  }
+
+  // boundary models on a face: follower pressure (value of the deformed normal
+  // as a function of du/d(s,t), and of the face Jacobian for shape
+  // derivatives) and the Robin heat flux
+  for (int trial = 0; trial < 5; trial++) {
+    tensor<double, 3, 2> J0{}, dU0{}, dir{};
+    for (int i = 0; i < 3; i++)
+      for (int k = 0; k < 2; k++) {
+        J0[i][k] = (i == k ? 1.0 : 0.0) + 0.2 * U(gen);
+        dU0[i][k] = 0.05 * U(gen);
+        dir[i][k] = U(gen);
+      }
+    boundary_models::Pressure pr{0.7};
+    auto p_of_du = [&](const auto& du) {
+      tensor<double, 3> x{};
+      using T = std::decay_t<decltype(du[0][0])>;
+      return pr(0.0, tuple{x, J0}, tuple{tensor<T, 3>{}, du});
+    };
+    auto p_of_J = [&](const auto& J) {
+      using T = std::decay_t<decltype(J[0][0])>;
+      return pr(0.0, tuple{tensor<T, 3>{}, J}, tuple{tensor<double, 3>{}, dU0});
+    };
+    const double h = 1e-6;
+    auto shift = [&](const tensor<double, 3, 2>& A, double hh) {
+      tensor<double, 3, 2> out{};
+      for (int i = 0; i < 3; i++)
+        for (int k = 0; k < 2; k++) out[i][k] = A[i][k] + hh * dir[i][k];
+      return out;
+    };
+    auto seed = [&](const tensor<double, 3, 2>& A) {
+      tensor<S, 3, 2> out{};
+      for (int i = 0; i < 3; i++)
+        for (int k = 0; k < 2; k++) out[i][k] = S{A[i][k], dir[i][k]};
+      return out;
+    };
+    {
+      const auto ad = p_of_du(seed(dU0));
+      const auto fp = p_of_du(shift(dU0, h)), fm = p_of_du(shift(dU0, -h));
+      for (int i = 0; i < 3; i++) expect_close("pressure d/d(du)", ad[i].gradient, (fp[i] - fm[i]) / (2 * h), 1e-8);
+    }
+    {
+      const auto ad = p_of_J(seed(J0));
+      const auto fp = p_of_J(shift(J0, h)), fm = p_of_J(shift(J0, -h));
+      for (int i = 0; i < 3; i++) expect_close("pressure d/dJ", ad[i].gradient, (fp[i] - fm[i]) / (2 * h), 1e-8);
+    }
+    boundary_models::HeatFlux hf{0.3, 0.7, 1.1};
+    const double u0 = U(gen);
+    tensor<double, 3> x{};
+    x[0] = 0.4;
+    const auto ad = hf(0.0, tuple{x, J0}, tuple{S{u0, 1.0}, tensor<S, 2>{}});
+    const auto f1 = hf(0.0, tuple{x, J0}, tuple{u0 + h, tensor<double, 2>{}});
+    const auto f2 = hf(0.0, tuple{x, J0}, tuple{u0 - h, tensor<double, 2>{}});
+    expect_close("heat flux d/du", ad.gradient, (f1 - f2) / (2 * h), 1e-8);
   }
 
   if (failures) {
