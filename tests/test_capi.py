@@ -85,3 +85,21 @@ def test_new_entry_points_validate_before_touching_a_device():
                  lambda: lib.sfx_solver_solve_adjoint(None, 0.0, None, None, None, None),
                  lambda: lib.sfx_set_param_field(None, 0, None, 0)):
         assert call() == -1
+
+
+def test_python_side_validation():
+    """QoI parameter counts and face lists are validated in Python before any
+    call into the library."""
+    from serac_gb300 import functional as F
+
+    assert F._qoi_nparams(F.QOI_FIELD, 3, False) == 3
+    assert F._qoi_nparams(F.QOI_NEOHOOKEAN_ENERGY, 3, False) == 2
+    assert F._qoi_nparams(F.QOI_NORMAL_FIELD, 3, True) == 0
+    with pytest.raises(ValueError):
+        F._qoi_nparams(F.QOI_NORMAL_FIELD, 1, True)  # needs 3 components
+    with pytest.raises(ValueError):
+        F._qoi_nparams(F.QOI_NEOHOOKEAN_ENERGY, 3, True)  # domain only
+    with pytest.raises(ValueError):
+        F._face_arrays(([0, 1], [3]))
+    e, s = F._face_arrays(([0, 1], [3, 6]))
+    assert e.dtype.name == "int32" and list(s) == [3, 6]
