@@ -73,8 +73,11 @@ class LearnedPreconditioner:
 # ------------------------------------------------------------- materials
 def gaussian_random_field(n, ell, seed):
     """Unit-variance Gaussian random field on the n^3 element grid (element
-    centroids on the unit cube) with covariance exp(-|r|^2 / ell^2), by
-    spectral filtering of white noise (periodic FFT on a 2n grid, cropped)."""
+    centroids on the unit cube), by spectral filtering of white noise with
+    the Gaussian filter exp(-|k|^2 ell^2 / 8) (periodic FFT on a 2n grid,
+    cropped).  Its correlation is exp(-2 |r|^2 / ell^2), i.e. a Gaussian
+    kernel exp(-|r|^2 / (2 s^2)) with standard length s = ell / 2
+    (tests/test_learned_host.py measures it)."""
     rng = np.random.default_rng(seed)
     m = 2 * n
     w = rng.standard_normal((m, m, m))
