@@ -145,6 +145,28 @@ int main() {
     }
   }
 
+  // J2 return map (the scalar consistency solve, test_newton.cpp's subject):
+  // after a plastic step the stress lies on the yield surface,
+  // sqrt(3/2) |dev sigma| = sigma_y + H eqps, to the solver tolerance
+  int plastic_draws = 0;
+  for (int trial = 0; trial < 20; trial++) {
+    const auto H = rand_tensor(0.05);
+    J2::State st{};
+    const auto sigma = j2(st, H);
+    if (st.accumulated_plastic_strain <= 0.0) continue;  // elastic draw
+    plastic_draws++;
+    const auto s = dev(sigma);
+    const double q = std::sqrt(1.5) * norm(s);
+    const double yield = j2.hardening.sigma_y + j2.hardening.Hi * st.accumulated_plastic_strain;
+    expect_close("J2 consistency", q, yield, 1e-10);
+    // the plastic strain increment is deviatoric and along the flow direction
+    expect_close("J2 plastic incompressibility", tr(st.plastic_strain), 0.0, 1e-13);
+  }
+  if (plastic_draws < 10) {
+    std::printf("FAIL J2 consistency: only %d plastic draws\n", plastic_draws);
+    failures++;
+  }
+
   // heat q-functions: source and flux as functions of (u, grad u)
   for (int trial = 0; trial < 5; trial++) {
     const double u0 = 0.4 * U(gen), du0 = U(gen);
