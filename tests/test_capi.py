@@ -103,3 +103,22 @@ def test_python_side_validation():
         F._face_arrays(([0, 1], [3]))
     e, s = F._face_arrays(([0, 1], [3, 6]))
     assert e.dtype.name == "int32" and list(s) == [3, 6]
+
+
+def test_table_rejects_inverted_elements():
+    """An element whose corners are left-handed in its lexicographic frame
+    (for instance a wrong native -> lexicographic permutation) is rejected on
+    the host."""
+    import numpy as np
+
+    from serac_gb300 import _lib
+
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    table = np.arange(8, dtype=np.int32).reshape(1, 8)
+    corners = np.array([[x, y, z] for z in (0.0, 1.0) for y in (0.0, 1.0) for x in (0.0, 1.0)]).reshape(1, 8, 3)
+    corners[0, :, 0] = 1.0 - corners[0, :, 0]  # mirrored in x
+    rc = lib.sfx_form_create_from_table(1, 1, 1, 8, table.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                        corners.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(h))
+    assert rc == -1
+    assert b"inverted" in lib.sfx_last_error()
