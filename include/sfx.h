@@ -106,8 +106,9 @@ int sfx_form_create(sfx_mesh mesh, int order, int components, sfx_form* out);
  * the caller's own numbering in [0, num_nodes) (vdof = component *
  * num_nodes + node); elem_vertices (host, num_elements x 8 x 3 doubles) the
  * element's corner coordinates in lexicographic corner order (trilinear
- * geometry, positively oriented: an element with a non-positive Jacobian at
- * a corner is rejected with SFX_ERR_INVALID).  Every operator of this header works on
+ * geometry, positively oriented: an element whose Jacobian at its centre
+ * is not positive, as a wrong node or corner permutation gives, is rejected
+ * with SFX_ERR_INVALID).  Every operator of this header works on
  * such a form; boundaries are given as face lists
  * (sfx_form_add_boundary_integral_faces), the CSR graph is the union of the
  * element node sets per node (columns sorted), and results follow the

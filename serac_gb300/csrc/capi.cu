@@ -107,6 +107,34 @@ int compute_geometry(sfx_form_s& f, cudaStream_t s) {
   SFX_CUDA_TRY(cudaGetLastError());
   return SFX_OK;
 }
+// every element of an imported table positively oriented in its
+// lexicographic frame: the trilinear map's Jacobian at the element centre
+// (the mean of the four edges along each of xi, eta, zeta) has a positive
+// determinant.  A wrong node or corner permutation inverts the whole element,
+// which this catches; mildly distorted elements that serac accepts pass.
+// Xe: [e][3][8].
+int check_orientation(const std::vector<double>& Xe, int64_t ne) {
+  for (int64_t e = 0; e < ne; e++) {
+    const double* X = &Xe[size_t(e * 24)];
+    double Jc[3][3] = {};
+    for (int d = 0; d < 3; d++) {
+      const int bit = 1 << d;
+      for (int v = 0; v < 8; v++) {
+        if (v & bit) continue;
+        for (int i = 0; i < 3; i++) Jc[i][d] += 0.25 * (X[i * 8 + (v | bit)] - X[i * 8 + v]);
+      }
+    }
+    const double det = Jc[0][0] * (Jc[1][1] * Jc[2][2] - Jc[1][2] * Jc[2][1]) -
+                       Jc[0][1] * (Jc[1][0] * Jc[2][2] - Jc[1][2] * Jc[2][0]) +
+                       Jc[0][2] * (Jc[1][0] * Jc[2][1] - Jc[1][1] * Jc[2][0]);
+    if (!(det > 0.0))
+      return fail(SFX_ERR_INVALID, "element " + std::to_string(e) +
+                                       " is inverted or degenerate (non-positive Jacobian at its centre; check the "
+                                       "lexicographic node and corner order)");
+  }
+  return SFX_OK;
+}
+
 // sizes, node -> element map, device tables and geometric factors of a new
 // form from its element table conn [e][NPE] and vertex coordinates Xe [e][3][8]
 int init_form(sfx_form_s* f, int order, int components, int64_t ne, int64_t nnodes, const std::vector<int32_t>& conn,
@@ -239,27 +267,7 @@ int sfx_form_create_from_table(int order, int components, int64_t num_elements, 
   for (int64_t e = 0; e < num_elements; e++)
     for (int v = 0; v < 8; v++)
       for (int i = 0; i < 3; i++) Xe[size_t(e * 24 + i * 8 + v)] = elem_vertices[size_t((e * 8 + v) * 3 + i)];
-  // every element positively oriented in its lexicographic frame: the
-  // trilinear map's Jacobian at each corner (the three edges leaving it,
-  // signed towards increasing xi, eta, zeta) has a positive determinant
-  for (int64_t e = 0; e < num_elements; e++) {
-    const double* X = &Xe[size_t(e * 24)];  // [i][corner]
-    for (int v = 0; v < 8; v++) {
-      double Jc[3][3];
-      for (int d = 0; d < 3; d++) {
-        const int bit = 1 << d;
-        const int lo = v & ~bit, hi = v | bit;
-        for (int i = 0; i < 3; i++) Jc[i][d] = X[i * 8 + hi] - X[i * 8 + lo];
-      }
-      const double det = Jc[0][0] * (Jc[1][1] * Jc[2][2] - Jc[1][2] * Jc[2][1]) -
-                         Jc[0][1] * (Jc[1][0] * Jc[2][2] - Jc[1][2] * Jc[2][0]) +
-                         Jc[0][2] * (Jc[1][0] * Jc[2][1] - Jc[1][1] * Jc[2][0]);
-      if (!(det > 0.0))
-        return fail(SFX_ERR_INVALID, "element " + std::to_string(e) +
-                                         " is inverted or degenerate (non-positive Jacobian at a corner; check the "
-                                         "lexicographic node and corner order)");
-    }
-  }
+  if (int rc = sfx_impl::check_orientation(Xe, num_elements)) return rc;
   auto* f = new (std::nothrow) sfx_form_s;
   if (!f) return fail(SFX_ERR_NOMEM, "host allocation failed");
   f->general = true;
