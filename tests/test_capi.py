@@ -122,3 +122,16 @@ def test_table_rejects_inverted_elements():
                                         corners.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(h))
     assert rc == -1
     assert b"inverted" in lib.sfx_last_error()
+
+
+def test_missing_library_fails_loudly(monkeypatch):
+    """No CPU fallback: without the built CUDA library the package refuses to
+    run instead of computing elsewhere."""
+    from serac_gb300 import _lib
+
+    monkeypatch.setattr(_lib, "_LIB", None)
+    monkeypatch.setattr(_lib, "LIB_PATH", "/nonexistent/libsfx_gb300.so")
+    with pytest.raises(ImportError):
+        _lib.load()
+    with pytest.raises(ImportError):
+        _lib.call("sfx_version")
