@@ -53,7 +53,7 @@ def config(n_gpus, flush):
 
 
 def problem():
-    from oracle.oracle import box_vertices
+    from serac_gb300 import box_vertices
 
     V = box_vertices(NX, NX, NX, perturb=0.1, seed=1)
     return V

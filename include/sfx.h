@@ -108,7 +108,10 @@ int sfx_form_create(sfx_mesh mesh, int order, int components, sfx_form* out);
  * element's corner coordinates in lexicographic corner order (trilinear
  * geometry, positively oriented: an element whose Jacobian at its centre
  * is not positive, as a wrong node or corner permutation gives, is rejected
- * with SFX_ERR_INVALID).  Every operator of this header works on
+ * with SFX_ERR_INVALID).  Only the centre is checked: an element that is
+ * valid there but has det J <= 0 at some quadrature point (inverted near a
+ * corner) is accepted, as serac accepts it, and gives wrong or non-finite
+ * results; such meshes are the caller's to reject.  Every operator of this header works on
  * such a form; boundaries are given as face lists
  * (sfx_form_add_boundary_integral_faces), the CSR graph is the union of the
  * element node sets per node (columns sorted), and results follow the
@@ -127,7 +130,9 @@ int sfx_form_add_domain_integral(sfx_form form, int material, const double* para
 /* Replace the material parameters of domain integral `integral` (0-based, in
  * the order added; params: host, as for sfx_form_add_domain_integral) without
  * rebuilding the form: a parameter field updated between evaluations, e.g. in
- * a design loop.  Synchronous; the form must be linearised again. */
+ * a design loop.  Synchronous: it first waits for all work queued on the
+ * device (every stream), so no evaluation in flight sees a mix of old and
+ * new parameters; the form must be linearised again. */
 int sfx_set_param_field(sfx_form form, int integral, const double* params, int per_element);
 
 /* Boundary integral over the faces of the sides in side_mask; params: host. */
@@ -296,7 +301,8 @@ int sfx_scatter_add_f32(sfx_form form, const float* E, float* out, int accumulat
  * (order+1)^3 must not exceed 4,194,304 (SFX_ERR_UNSUPPORTED otherwise).
  * Materials: SFX_MAT_HEAT, SFX_MAT_NEOHOOKEAN; order 1 or 2.  The first call
  * on a device looks up the scratch array's device address (make it before
- * any stream capture).  Every call on a device shares the scratch array:
+ * any stream capture); the address is cached per device and context, so a
+ * device reset or a new context is followed by a fresh lookup.  Every call on a device shares the scratch array:
  * calls that overlap on that device race and must be serialised by the
  * caller.  Results equal sfx_residual's for the same mesh and material. */
 int sfx_residual_structured_noalloc(int nx, int ny, int nz, int order, int material, const double* params,

@@ -54,16 +54,18 @@ typedef struct {
   double krylov_rel_tol;     /* 1e-8 */
   double krylov_abs_tol;     /* 1e-12 */
   int precond;               /* SFX_PREC_* (Jacobi-Chebyshev) */
-  int chebyshev_degree;      /* 3: Chebyshev polynomial degree (degree-1 Jacobian actions); higher degrees
-                                amplify the modes above the power-iteration estimate of lmax */
-  double chebyshev_ratio;    /* 30: interval [lmax / ratio, 1.1 lmax] of D^-1 J */
-  int power_iterations;      /* 10: lmax estimate per linearisation */
+  int chebyshev_degree;      /* 3: Chebyshev polynomial degree (degree-1 Jacobian actions) */
+  double chebyshev_ratio;    /* 30: interval [lmax / ratio, 1.05 lmax] of D^-1 J */
+  int eigen_iterations;      /* 20: Lanczos steps of the lmax estimate per linearisation (largest Ritz value
+                                plus its residual bound, from a pseudo-random start vector) */
   int mixed_precision;       /* 1: FP64 flexible GMRES outside, FP32 GMRES + FP32 Jacobi-Chebyshev inside */
   int inner_iterations;      /* 40: FP32 inner GMRES steps per outer step */
   double inner_rel_tol;      /* 1e-3 */
   int print_level;           /* 0 */
   int learned_cycle;         /* 1: SFX_PREC_LEARNED without mixed precision: 1 Chebyshev, network on
                                 the smoothed residual, Chebyshev (two-level cycle); 0 network, Chebyshev */
+  int inner_chebyshev_degree; /* 0: degree of the FP32 Chebyshev inside the mixed-precision solve
+                                 (0: chebyshev_degree) */
 } sfx_solver_options;
 
 typedef struct {
@@ -76,6 +78,7 @@ typedef struct {
   double last_krylov_rel;
   int learned_applications; /* network preconditioner applications */
   int learned_fallbacks;    /* of which fell back to Jacobi-Chebyshev */
+  double lmax_estimate;     /* the last estimate of the largest eigenvalue of D^-1 J (Chebyshev interval) */
 } sfx_solver_stats;
 
 typedef struct sfx_solver_s* sfx_solver;

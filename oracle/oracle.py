@@ -571,6 +571,53 @@ class OracleFunctional:
         return sp.csr_matrix((vals, col, row_ptr), shape=(n, n))
 
 
+    def assemble_rows(self, u, rows, t=0.0, chunk=2048):
+        """The CSR rows ``rows`` (sorted vdof ids) of dR/du from the domain
+        integrals, for meshes whose full matrix is too large to assemble here:
+        returns (row_ptr, col, val) of the sub-matrix A[rows, :], its graph the
+        sorted unique columns that the elements containing each row's node
+        pair it with, values summed in element order."""
+        rows = np.asarray(rows, dtype=np.int64)
+        n, c, N = self.ndofs, self.c, self.nnodes
+        in_rows = np.zeros(n, dtype=bool)
+        in_rows[rows] = True
+        vd = elem_vdofs(self.conn, c, N)
+        touching = np.nonzero(in_rows[vd].any(axis=1))[0]
+        keys, vals = [], []
+        uE = gather(u, self.conn, c, N)
+        nd = vd.shape[1]
+        for mat, params in self.domain:
+            prm = None if not NPARAMS[mat] else np.asarray(params, dtype=np.float64).reshape(-1, NPARAMS[mat])
+            per_element = prm is not None and prm.shape[0] == self.conn.shape[0] and prm.shape[0] > 1
+            for k0 in range(0, touching.size, chunk):
+                els = touching[k0:k0 + chunk]
+                st = None if self.state is None or mat != MAT_J2 else np.ascontiguousarray(self.state[els])
+                K = element_kernel(mat, self.p, 2, np.ascontiguousarray(uE[els]), np.ascontiguousarray(self.Xq[els]),
+                                   np.ascontiguousarray(self.Jq[els]), prm[els] if per_element else prm, None, st,
+                                   False, t, False, self.nthreads)
+                # K[e][trial j][test i] adds to row vd[e, i], column vd[e, j]
+                v = vd[els]
+                r_ = np.broadcast_to(v[:, None, :], (els.size, nd, nd))
+                c_ = np.broadcast_to(v[:, :, None], (els.size, nd, nd))
+                sel = in_rows[r_]
+                keys.append(r_[sel] * n + c_[sel])
+                vals.append(K[sel])
+        key = np.concatenate(keys)
+        val = np.concatenate(vals)
+        order = np.argsort(key, kind="stable")  # element order kept within a (row, col) pair
+        key, val = key[order], val[order]
+        first = np.ones(key.size, dtype=bool)
+        first[1:] = key[1:] != key[:-1]
+        starts = np.nonzero(first)[0]
+        ukey = key[starts]
+        uval = np.add.reduceat(val, starts)
+        r_of, c_of = ukey // n, ukey % n
+        pos = np.searchsorted(rows, r_of)
+        row_ptr = np.zeros(rows.size + 1, dtype=np.int64)
+        np.add.at(row_ptr, pos + 1, 1)
+        return np.cumsum(row_ptr), c_of, uval
+
+
 QOI_MEASURE, QOI_POSITION, QOI_FIELD, QOI_NEOHOOKEAN_ENERGY, QOI_NORMAL_FIELD, QOI_POLY_TEST = range(6)
 
 
@@ -818,6 +865,157 @@ class OracleQoI:
         return self.evaluate(u)[1]
 
 
+class OracleLinearization:
+    """The stored-derivative Jacobian of an OracleFunctional's domain
+    integrals at u: the q-function derivative D is formed once per point
+    (orc_linearize, evaluation_kernel_impl with differentiation) and each
+    action is gather -> D . interpolate -> integrate -> node-owner scatter in
+    C with OpenMP (orc_gather, orc_apply_linearization, orc_scatter:
+    action_of_gradient_kernel, domain_integral_kernels.hpp:277-304).  Domain
+    integrals only (no boundary integrals)."""
+
+    def __init__(self, f, u, t=0.0, nthreads=None):
+        assert not f.boundary, "domain integrals only"
+        self.f = f
+        self.threads = nthreads or f.nthreads
+        L = lib()
+        dp, i64p = _dp, ctypes.POINTER(ctypes.c_int64)
+        L.orc_linearize.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] + [dp] * 5 + [dp, ctypes.c_int]
+        L.orc_apply_linearization.argtypes = [ctypes.c_int] * 3 + [dp, dp, dp, ctypes.c_int]
+        L.orc_gather.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int64, i64p, dp, dp,
+                                 ctypes.c_int]
+        L.orc_scatter.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, i64p, i64p, dp, dp, ctypes.c_int]
+        self.L = L
+        self.conn = np.ascontiguousarray(f.conn.astype(np.int64))
+        ne, npe = self.conn.shape
+        self.ne, self.npe = ne, npe
+        order = np.argsort(self.conn.ravel(), kind="stable")
+        self.node_ent = np.ascontiguousarray(order.astype(np.int64))
+        node_ptr = np.zeros(f.nnodes + 1, dtype=np.int64)
+        np.add.at(node_ptr, self.conn.ravel() + 1, 1)
+        self.node_ptr = np.cumsum(node_ptr)
+        c, nq = f.c, f.Q ** 3
+        N = 4 * c
+        uE = self.gather(np.ascontiguousarray(u, dtype=np.float64))
+        self.D = []
+        for mat, params in f.domain:
+            prm = None
+            if NPARAMS[mat]:
+                prm = np.ascontiguousarray(np.broadcast_to(
+                    np.asarray(params, dtype=np.float64).reshape(-1, NPARAMS[mat]), (ne, NPARAMS[mat])))
+            st = f.state if mat == MAT_J2 else None
+            D = np.zeros((ne, nq, N, N))
+            rc = L.orc_linearize(mat, f.p, ne, t, _ptr(prm), _ptr(uE), _ptr(f.Xq), _ptr(f.Jq),
+                                 _ptr(None if st is None else np.ascontiguousarray(st)), _ptr(D), self.threads)
+            assert rc == 0, rc
+            self.D.append(D)
+        self._dE = np.zeros_like(uE)
+        self._acc = np.zeros_like(uE)
+
+    def gather(self, x):
+        i64p = ctypes.POINTER(ctypes.c_int64)
+        E = np.empty((self.ne, self.f.c * self.npe))
+        self.L.orc_gather(self.ne, self.npe, self.f.c, self.f.nnodes, self.conn.ctypes.data_as(i64p), _ptr(x),
+                          _ptr(E), self.threads)
+        return E
+
+    def scatter(self, E, out):
+        i64p = ctypes.POINTER(ctypes.c_int64)
+        self.L.orc_scatter(self.f.nnodes, self.npe, self.f.c, self.node_ptr.ctypes.data_as(i64p),
+                           self.node_ent.ctypes.data_as(i64p), _ptr(E), _ptr(out), self.threads)
+        return out
+
+    def apply(self, x, out=None):
+        """J(u) x."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.empty(self.f.ndofs) if out is None else out
+        xE = self.gather(x)
+        if len(self.D) == 1:
+            self.L.orc_apply_linearization(self.f.p, self.f.c, self.ne, _ptr(self.D[0]), _ptr(xE),
+                                           _ptr(self._dE), self.threads)
+            return self.scatter(self._dE, out)
+        self._acc[:] = 0.0
+        for D in self.D:
+            self.L.orc_apply_linearization(self.f.p, self.f.c, self.ne, _ptr(D), _ptr(xE), _ptr(self._dE),
+                                           self.threads)
+            self._acc += self._dE
+        return self.scatter(self._acc, out)
+
+
+def jacobian_diagonal(f, u, t=0.0, chunk=4096):
+    """diag(dR/du) from the element matrices (domain integrals), in element chunks."""
+    c, N = f.c, f.nnodes
+    vd = elem_vdofs(f.conn, c, N)
+    out = np.zeros(f.ndofs)
+    uE = gather(u, f.conn, c, N)
+    for mat, params in f.domain:
+        prm = None if not NPARAMS[mat] else np.asarray(params, dtype=np.float64).reshape(-1, NPARAMS[mat])
+        per_element = prm is not None and prm.shape[0] == f.conn.shape[0] and prm.shape[0] > 1
+        for e0 in range(0, f.conn.shape[0], chunk):
+            e1 = min(e0 + chunk, f.conn.shape[0])
+            p_ch = prm[e0:e1] if per_element else prm
+            st = None if f.state is None or mat != MAT_J2 else np.ascontiguousarray(f.state[e0:e1])
+            K = element_kernel(mat, f.p, 2, uE[e0:e1], np.ascontiguousarray(f.Xq[e0:e1]),
+                               np.ascontiguousarray(f.Jq[e0:e1]), p_ch, None, st, False, t, False, f.nthreads)
+            np.add.at(out, vd[e0:e1].ravel(), np.einsum("eii->ei", K).ravel())
+    return out
+
+
+def newton_matrix_free(f, u0, ess, rel_tol=1e-10, abs_tol=0.0, lin_rtol=None, max_iter=30, t=0.0,
+                       max_lin=50000):
+    """Newton without line search (equation_solver.cpp:79-200) whose linear
+    solves are Jacobi-preconditioned CG (Saad Alg. 6.18) on the
+    Dirichlet-eliminated stored-derivative Jacobian, matrix-free
+    (OracleLinearization): for meshes where a direct solve is out of reach.
+    The converged solution does not depend on the linear solver, so by
+    default each solve is only as tight as the step needs (inexact Newton,
+    Eisenstat and Walker 1996): relative tolerance min(1e-2, 0.1 target / |r|),
+    at least 1e-13; lin_rtol fixes it instead.  Returns (u, Newton
+    iterations, final |r|, |r0|, total CG iterations)."""
+    u = np.array(u0, dtype=np.float64, copy=True)
+    mask = np.ones(f.ndofs)
+    mask[ess] = 0.0
+    r = f.residual(u, t=t)
+    r[ess] = 0.0
+    r0 = np.linalg.norm(r)
+    it, lin_total = 0, 0
+    for it in range(max_iter):
+        if np.linalg.norm(r) <= max(rel_tol * r0, abs_tol):
+            break
+        lin = OracleLinearization(f, u, t)
+        diag = jacobian_diagonal(f, u, t)
+        diag[ess] = 1.0
+        target = max(rel_tol * r0, abs_tol)
+        eta = lin_rtol if lin_rtol is not None else max(1e-13, min(1e-2, 0.1 * target / np.linalg.norm(r)))
+        du, k, _ = cg(lambda x: lin.apply(x * mask) * mask + x * (1.0 - mask), r, diag, rtol=eta,
+                      maxiter=max_lin)
+        lin_total += k
+        u -= du
+        r = f.residual(u, t=t)
+        r[ess] = 0.0
+    else:
+        it = max_iter
+    return u, it, np.linalg.norm(r), r0, lin_total
+
+
+def warm_start_matrix_free(f, u, u_target, ess, t=0.0, lin_rtol=1e-3, max_lin=50000):
+    """warm_start with the matrix-free Jacobi-CG linear solve (the predictor
+    is only a starting point for Newton: its tolerance does not change the
+    converged answer)."""
+    mask = np.ones(f.ndofs)
+    mask[ess] = 0.0
+    d = np.zeros_like(u)
+    d[ess] = u_target[ess] - u[ess]
+    lin = OracleLinearization(f, u, t)
+    rhs = -lin.apply(d)
+    rhs[ess] = 0.0
+    diag = jacobian_diagonal(f, u, t)
+    diag[ess] = 1.0
+    x, k, _ = cg(lambda y: lin.apply(y * mask) * mask + y * (1.0 - mask), rhs, diag, rtol=lin_rtol, maxiter=max_lin)
+    x[ess] = 0.0
+    return u + d + x, k
+
+
 def eliminate_dirichlet(A, ess):
     """Zero the rows and columns of ``ess`` and put 1 on their diagonal."""
     import scipy.sparse as sp
@@ -833,27 +1031,34 @@ def eliminate_dirichlet(A, ess):
     return A2
 
 
+def _dot(a, b):
+    """a . b without the BLAS library: its idle worker threads spin against
+    the oracle's OpenMP threads and slow the matrix-free solves several-fold."""
+    return float(np.einsum("i,i->", a, b))
+
+
 def cg(apply_A, b, diag, rtol=1e-10, maxiter=10000):
     """Jacobi-preconditioned conjugate gradients; returns (x, iterations, ||r||/||b||)."""
     x = np.zeros_like(b)
     r = b.copy()
     z = r / diag
     p = z.copy()
-    rz = r @ z
-    nb = np.linalg.norm(b)
+    rz = _dot(r, z)
+    nb = np.sqrt(_dot(b, b))
     if nb == 0:
         return x, 0, 0.0
     for it in range(1, maxiter + 1):
         Ap = apply_A(p)
-        alpha = rz / (p @ Ap)
+        alpha = rz / _dot(p, Ap)
         x += alpha * p
         r -= alpha * Ap
-        rn = np.linalg.norm(r) / nb
+        rn = np.sqrt(_dot(r, r)) / nb
         if rn < rtol:
             return x, it, rn
-        z = r / diag
-        rz_new = r @ z
-        p = z + (rz_new / rz) * p
+        np.divide(r, diag, out=z)
+        rz_new = _dot(r, z)
+        p *= rz_new / rz
+        p += z
         rz = rz_new
     return x, maxiter, rn
 

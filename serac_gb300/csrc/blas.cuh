@@ -152,6 +152,37 @@ __global__ void cheb_step(int64_t n, T a, T b, const T* __restrict__ rhs, const 
   z[i] += v;
 }
 
+// x = a deterministic pseudo-random vector in [-1, 1) (a 64-bit integer hash
+// of the index), so that every eigenmode of an operator is present in it
+template <typename T>
+__global__ void fill_hash(int64_t n, uint64_t seed, T* __restrict__ x) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t h = uint64_t(i) * 0x9E3779B97F4A7C15ull + seed;
+  h ^= h >> 30;
+  h *= 0xBF58476D1CE4E5B9ull;
+  h ^= h >> 27;
+  h *= 0x94D049BB133111EBull;
+  h ^= h >> 31;
+  x[i] = T(double(h >> 11) * (2.0 / 9007199254740992.0) - 1.0);
+}
+
+// y = x / sqrt(d)
+template <typename T>
+__global__ void scale_rsqrt(int64_t n, const T* __restrict__ x, const T* __restrict__ d, T* __restrict__ y) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = x[i] / sqrt(d[i]);
+}
+
+// Lanczos three-term step: w = w / sqrt(d) - alpha v - beta v_prev is done in
+// two kernels: first w /= sqrt(d) (scale_rsqrt in place), then this one
+template <typename T>
+__global__ void lanczos_orth(int64_t n, T alpha, const T* __restrict__ v, T beta, const T* __restrict__ vp,
+                             T* __restrict__ w) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) w[i] = w[i] - alpha * v[i] - beta * vp[i];
+}
+
 template <typename S, typename T>
 __global__ void convert(int64_t n, const S* __restrict__ x, T* __restrict__ y) {
   int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;

@@ -367,6 +367,9 @@ int sfx_set_param_field(sfx_form form, int integral, const double* params, int p
   for (int64_t e = 0; e < form->ne; e++)
     for (int k = 0; k < di.nparams; k++)
       prm[size_t(e * di.nparams + k)] = per_element ? params[e * di.nparams + k] : params[k];
+  // work queued on any stream (non-blocking ones included) may still read the
+  // old parameters: let it finish before they are overwritten
+  SFX_CUDA_TRY(cudaDeviceSynchronize());
   SFX_CUDA_TRY(cudaMemcpy(di.params.p, prm.data(), prm.size() * sizeof(double), cudaMemcpyHostToDevice));
   form->linearized = false;  // the stored tangent belongs to the old parameters
   return SFX_OK;

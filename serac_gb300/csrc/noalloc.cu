@@ -30,21 +30,49 @@ static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
 constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
 double* g_scratch_ptr[kMaxDevices] = {};
+void* g_scratch_ctx[kMaxDevices] = {};  // the context each cached address belongs to
 
-// Device address of the scratch array on the current device (looked up once
-// per device; the host-side symbol is only a stand-in for it).
+// The driver's current context (cuCtxGetCurrent, reached through the runtime
+// so the library needs no link against the driver library).  A device reset
+// or a new primary context reloads the module, and the array may then sit at
+// another address: the cache is keyed by the context as well as the device.
+int current_context(void** ctx) {
+  using GetCtx = int (*)(void**);
+  static GetCtx fn = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<GetCtx>(p);
+    looked_up = true;
+  }
+  *ctx = nullptr;
+  if (!fn || fn(ctx) != 0) return sfx_impl::fail(SFX_ERR_CUDA, "cuCtxGetCurrent failed");
+  return SFX_OK;
+}
+
+// Device address of the scratch array for the current device and context
+// (looked up once per device and context; the host-side symbol is only a
+// stand-in for it and is never handed to a kernel).
 int scratch_address(double** out) {
   int dev = 0;
   cudaError_t err = cudaGetDevice(&dev);
   if (err != cudaSuccess) return sfx_impl::fail(SFX_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(err));
   if (dev < 0 || dev >= kMaxDevices) return sfx_impl::fail(SFX_ERR_UNSUPPORTED, "device index out of range");
+  // (before the runtime's first use of the device the context is still null:
+  // the lookup below creates it, and the next call caches its real handle)
+  void* ctx = nullptr;
+  if (int rc = current_context(&ctx)) return rc;
   std::lock_guard<std::mutex> lock(g_mutex);
-  if (!g_scratch_ptr[dev]) {
+  if (!g_scratch_ptr[dev] || g_scratch_ctx[dev] != ctx) {
     void* p = nullptr;
     err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (err != cudaSuccess)
       return sfx_impl::fail(SFX_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(err));
     g_scratch_ptr[dev] = static_cast<double*>(p);
+    g_scratch_ctx[dev] = ctx;
   }
   *out = g_scratch_ptr[dev];
   return SFX_OK;
@@ -211,13 +239,22 @@ int run(const Grid& g, const QF& qf, const double* vertices, const double* u, do
                               std::to_string(kScratchDoubles) + " available)");
   double* scratch = nullptr;
   if (int rc = scratch_address(&scratch)) return rc;
+  // an error left by earlier, unrelated work is reported as such and left in
+  // place for its owner; the checks after each launch then describe this call
+  cudaError_t err = cudaPeekAtLastError();
+  if (err != cudaSuccess)
+    return sfx_impl::fail(SFX_ERR_CUDA, std::string("error pending from earlier work: ") + cudaGetErrorString(err));
   const int64_t warps = (ne + EPW - 1) / EPW;
   const unsigned blocks = unsigned((warps * 32 + 127) / 128);
   structured_residual_kernel<P, C, State, QF><<<blocks, 128, 0, s>>>(g, qf, vertices, u, scratch, t);
+  err = cudaGetLastError();
+  if (err != cudaSuccess)
+    return sfx_impl::fail(SFX_ERR_CUDA, std::string("no-alloc element launch: ") + cudaGetErrorString(err));
   const int64_t nn = g.Nx * g.Ny * g.Nz;
   structured_scatter_kernel<P, C><<<unsigned((nn + 255) / 256), 256, 0, s>>>(g, scratch, r);
-  cudaError_t err = cudaGetLastError();
-  if (err != cudaSuccess) return sfx_impl::fail(SFX_ERR_CUDA, std::string("no-alloc launch: ") + cudaGetErrorString(err));
+  err = cudaGetLastError();
+  if (err != cudaSuccess)
+    return sfx_impl::fail(SFX_ERR_CUDA, std::string("no-alloc scatter launch: ") + cudaGetErrorString(err));
   return SFX_OK;
 }
 

@@ -7,7 +7,7 @@
 // Iterative Methods, Alg. 6.9 / 9.5) with classical Gram-Schmidt applied
 // twice, or Jacobi-preconditioned CG (Alg. 6.18) for symmetric problems.
 // Preconditioners: Jacobi, Jacobi-Chebyshev (Chebyshev iteration on D^-1 J
-// over [lmax/ratio, 1.1 lmax], lmax from a power iteration), and, in the
+// over [lmax/ratio, 1.05 lmax], lmax from a Lanczos estimate), and, in the
 // mixed-precision mode, an inner FP32 GMRES(k) on the FP32 stored tangent with
 // FP32 Jacobi-Chebyshev inside FP64 flexible GMRES.
 // Dirichlet rows/columns: J[ess, :] = J[:, ess] = I on the essential set,
@@ -141,46 +141,123 @@ int apply_J32(sfx_solver s, const float* x, float* y, cudaStream_t st) {
   return SFX_OK;
 }
 
-// power iteration for the largest eigenvalue of D^-1 J
+// degree of the FP32 Chebyshev polynomial inside the mixed-precision solve
+int inner_degree(sfx_solver s) {
+  return s->opt.inner_chebyshev_degree > 0 ? s->opt.inner_chebyshev_degree : s->opt.chebyshev_degree;
+}
+
+// Eigenvalues of the symmetric tridiagonal matrix (diagonal a, off-diagonal
+// b[1..m-1]) and the last component of each normalised eigenvector, by cyclic
+// Jacobi rotations on the dense m x m matrix (m is a few tens).
+void tridiagonal_eigen(const std::vector<double>& a, const std::vector<double>& b, std::vector<double>& lam,
+                       std::vector<double>& last) {
+  const int m = int(a.size());
+  std::vector<double> A(size_t(m) * m, 0.0), Vm(size_t(m) * m, 0.0);
+  for (int i = 0; i < m; i++) {
+    A[size_t(i) * m + i] = a[size_t(i)];
+    Vm[size_t(i) * m + i] = 1.0;
+    if (i > 0) A[size_t(i) * m + i - 1] = A[size_t(i - 1) * m + i] = b[size_t(i)];
+  }
+  for (int sweep = 0; sweep < 60; sweep++) {
+    double off = 0.0;
+    for (int p = 0; p < m; p++)
+      for (int q = p + 1; q < m; q++) off += A[size_t(p) * m + q] * A[size_t(p) * m + q];
+    if (off < 1e-30) break;
+    for (int p = 0; p < m; p++)
+      for (int q = p + 1; q < m; q++) {
+        const double apq = A[size_t(p) * m + q];
+        if (apq == 0.0) continue;
+        const double th = 0.5 * (A[size_t(q) * m + q] - A[size_t(p) * m + p]) / apq;
+        const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < m; k++) {  // columns p, q
+          const double akp = A[size_t(k) * m + p], akq = A[size_t(k) * m + q];
+          A[size_t(k) * m + p] = c * akp - sn * akq;
+          A[size_t(k) * m + q] = sn * akp + c * akq;
+        }
+        for (int k = 0; k < m; k++) {  // rows p, q
+          const double apk = A[size_t(p) * m + k], aqk = A[size_t(q) * m + k];
+          A[size_t(p) * m + k] = c * apk - sn * aqk;
+          A[size_t(q) * m + k] = sn * apk + c * aqk;
+        }
+        for (int k = 0; k < m; k++) {
+          const double vkp = Vm[size_t(k) * m + p], vkq = Vm[size_t(k) * m + q];
+          Vm[size_t(k) * m + p] = c * vkp - sn * vkq;
+          Vm[size_t(k) * m + q] = sn * vkp + c * vkq;
+        }
+      }
+  }
+  lam.resize(size_t(m));
+  last.resize(size_t(m));
+  for (int i = 0; i < m; i++) {
+    lam[size_t(i)] = A[size_t(i) * m + i];
+    last[size_t(i)] = Vm[size_t(m - 1) * m + i];
+  }
+}
+
+// Upper estimate of the largest eigenvalue of D^-1 J.  For symmetric J the
+// operator is self-adjoint in the D inner product, so Lanczos runs on
+// A = D^-1/2 J D^-1/2 (Saad, Iterative Methods, Alg. 6.15) from a
+// deterministic pseudo-random start (every mode present: a smooth start
+// would hide the high-frequency modes that set lmax), for
+// opt.eigen_iterations steps; the estimate is the largest Ritz value plus its
+// residual |beta_{m+1} s_m|, which bounds its distance to an eigenvalue.
 template <typename T, typename Acc>
-int estimate_lmax(sfx_solver s, int (*apply)(sfx_solver, const T*, T*, cudaStream_t), const T* D, T* x, T* y,
-                  Reducer<T, Acc>& red, double* lmax, cudaStream_t st) {
+int estimate_lmax(sfx_solver s, int (*apply)(sfx_solver, const T*, T*, cudaStream_t), const T* D, T* v, T* w,
+                  T* vp, T* t, Reducer<T, Acc>& red, double* lmax, cudaStream_t st) {
   const int64_t n = s->n;
-  // deterministic start vector: ones on the free vdofs
-  {
-    std::vector<T> ones(size_t(n), T(1));
-    SFX_CUDA_TRY(cudaMemcpyAsync(x, ones.data(), sizeof(T) * n, cudaMemcpyHostToDevice, st));
-    if (s->n_ess) sfx_blas::set_entries<T><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, T(0), x);
-    SFX_CUDA_TRY(cudaStreamSynchronize(st));
-  }
+  const int m = std::max(2, s->opt.eigen_iterations);
   cudaError_t err;
-  double lam = 0.0;
-  for (int it = 0; it < s->opt.power_iterations; it++) {
-    double nx = std::sqrt(double(red.dot(x, x, n, st, &err)));
+  sfx_blas::fill_hash<T><<<nblocks(n), 256, 0, st>>>(n, 0x5eed5eedull, v);
+  if (s->n_ess) sfx_blas::set_entries<T><<<nblocks(s->n_ess), 256, 0, st>>>(s->n_ess, s->ess.p, T(0), v);
+  SFX_CUDA_TRY(cudaMemsetAsync(vp, 0, sizeof(T) * n, st));
+  {
+    const double nv = std::sqrt(double(red.dot(v, v, n, st, &err)));
     SFX_CUDA_TRY(err);
-    sfx_blas::scale<T><<<nblocks(n), 256, 0, st>>>(n, T(1.0 / nx), x);
-    if (int rc = apply(s, x, y, st)) return rc;
-    sfx_blas::diag_solve<T><<<nblocks(n), 256, 0, st>>>(n, y, D, y);
-    lam = double(red.dot(x, y, n, st, &err));
-    SFX_CUDA_TRY(err);
-    std::swap(x, y);
+    sfx_blas::scale<T><<<nblocks(n), 256, 0, st>>>(n, T(1.0 / nv), v);
   }
-  *lmax = lam;
+  std::vector<double> alpha, beta(1, 0.0);
+  double beta_next = 0.0;
+  for (int j = 0; j < m; j++) {
+    sfx_blas::scale_rsqrt<T><<<nblocks(n), 256, 0, st>>>(n, v, D, t);
+    if (int rc = apply(s, t, w, st)) return rc;
+    sfx_blas::scale_rsqrt<T><<<nblocks(n), 256, 0, st>>>(n, w, D, w);
+    const double a = double(red.dot(w, v, n, st, &err));
+    SFX_CUDA_TRY(err);
+    if (!std::isfinite(a)) return fail(SFX_ERR_NONFINITE, "non-finite Lanczos coefficient");
+    alpha.push_back(a);
+    sfx_blas::lanczos_orth<T><<<nblocks(n), 256, 0, st>>>(n, T(a), v, T(beta.back()), vp, w);
+    beta_next = std::sqrt(double(red.dot(w, w, n, st, &err)));
+    SFX_CUDA_TRY(err);
+    if (!(beta_next > 1e-14 * std::fabs(a)) || j == m - 1) break;  // invariant subspace found, or done
+    beta.push_back(beta_next);
+    std::swap(vp, v);  // vp <- v
+    std::swap(v, w);   // v <- w / beta
+    sfx_blas::scale<T><<<nblocks(n), 256, 0, st>>>(n, T(1.0 / beta_next), v);
+  }
+  std::vector<double> lam, last;
+  tridiagonal_eigen(alpha, beta, lam, last);
+  size_t imax = 0;
+  for (size_t i = 1; i < lam.size(); i++)
+    if (lam[i] > lam[imax]) imax = i;
+  *lmax = lam[imax] + std::fabs(beta_next * last[imax]);
+  s->stats.lmax_estimate = *lmax;
+  SFX_CUDA_TRY(cudaGetLastError());
   return SFX_OK;
 }
 
 // z = Chebyshev(D^-1 J) approximation of J^-1 b, degree k, starting from 0
 template <typename T, typename Acc>
 int chebyshev(sfx_solver s, int (*apply)(sfx_solver, const T*, T*, cudaStream_t), const T* D, double lmax,
-              const T* b, T* z, T* d, T* res, cudaStream_t st) {
+              int degree, double ratio, const T* b, T* z, T* d, T* res, cudaStream_t st) {
   const int64_t n = s->n;
-  const double hi = 1.1 * lmax, lo = lmax / s->opt.chebyshev_ratio;
+  const double hi = 1.05 * lmax, lo = lmax / ratio;
   const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo);
   const double sigma = theta / delta;
   double rho = 1.0 / sigma;
   // d = D^-1 b / theta ; z = d
   sfx_blas::cheb_start<T><<<nblocks(n), 256, 0, st>>>(n, T(1.0 / theta), b, D, d, z);
-  for (int k = 1; k < s->opt.chebyshev_degree; k++) {
+  for (int k = 1; k < degree; k++) {
     if (int rc = apply(s, z, res, st)) return rc;  // res = J z
     double rho_new = 1.0 / (2.0 * sigma - rho);
     sfx_blas::cheb_step<T><<<nblocks(n), 256, 0, st>>>(n, T(rho_new * rho), T(2.0 * rho_new / delta), b, res, D, d, z);
@@ -415,8 +492,8 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
         (o.mixed_precision && (ensure(s->V32, size_t(k + 1) * n) || ensure(s->y32, size_t(k + 1)))))
       return fail(SFX_ERR_NOMEM, "FP32 workspace allocation failed");
     sfx_blas::convert<double, float><<<nblocks(n), 256, 0, st>>>(n, s->diag.p, s->diag32.p);
-    if (int rc = estimate_lmax<float, float>(s, apply_J32, s->diag32.p, s->tmp32.p, s->cheb_r32.p, s->red32,
-                                             &s->lmax32, st))
+    if (int rc = estimate_lmax<float, float>(s, apply_J32, s->diag32.p, s->tmp32.p, s->cheb_r32.p, s->cheb_d32.p,
+                                             s->tmp32b.p, s->red32, &s->lmax32, st))
       return rc;
     // Network step on the residual res: z += a NN(res) with a minimising
     // |res - a J NN(res)|, kept only when it takes at least 1 % off the
@@ -448,7 +525,8 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
       return SFX_OK;
     };
     auto cheb32 = [=](const float* b, float* z, cudaStream_t ss) -> int {
-      return chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, b, z, s->cheb_d32.p, s->cheb_r32.p, ss);
+      return chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, inner_degree(s), s->opt.chebyshev_ratio, b, z,
+                                     s->cheb_d32.p, s->cheb_r32.p, ss);
     };
     if (o.mixed_precision) {
       // network step, then inner FP32 GMRES(k) + Jacobi-Chebyshev on what it leaves
@@ -499,15 +577,16 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
         ensure(s->tmp32b, n))
       return fail(SFX_ERR_NOMEM, "FP32 workspace allocation failed");
     sfx_blas::convert<double, float><<<nblocks(n), 256, 0, st>>>(n, s->diag.p, s->diag32.p);
-    if (int rc = estimate_lmax<float, float>(s, apply_J32, s->diag32.p, s->tmp32.p, s->cheb_r32.p, s->red32,
-                                             &s->lmax32, st))
+    if (int rc = estimate_lmax<float, float>(s, apply_J32, s->diag32.p, s->tmp32.p, s->cheb_r32.p, s->cheb_d32.p,
+                                             s->tmp32b.p, s->red32, &s->lmax32, st))
       return rc;
     prec = [=](const double* v, double* z, cudaStream_t) -> int {
       sfx_blas::convert<double, float><<<nblocks(n), 256, 0, st>>>(n, v, s->b32.p);
       SFX_CUDA_TRY(cudaMemsetAsync(s->x32.p, 0, sizeof(float) * n, st));
       std::function<int(const float*, float*, cudaStream_t)> inner_prec = [=](const float* a, float* b,
                                                                                cudaStream_t ss) -> int {
-        return chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, a, b, s->cheb_d32.p, s->cheb_r32.p, ss);
+        return chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, inner_degree(s), s->opt.chebyshev_ratio, a,
+                                       b, s->cheb_d32.p, s->cheb_r32.p, ss);
       };
       int it = 0;
       double rel_in = 0.0;
@@ -521,10 +600,12 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
     };
   } else {
     if (ensure(s->cheb_d, n) || ensure(s->cheb_r, n)) return fail(SFX_ERR_NOMEM, "workspace allocation failed");
-    if (int rc = estimate_lmax<double, double>(s, apply_J64, s->diag.p, s->tmp.p, s->cheb_r.p, s->red, &s->lmax, st))
+    if (int rc = estimate_lmax<double, double>(s, apply_J64, s->diag.p, s->tmp.p, s->cheb_r.p, s->cheb_d.p, s->tmp2.p,
+                                               s->red, &s->lmax, st))
       return rc;
     prec = [=](const double* v, double* z, cudaStream_t) -> int {
-      return chebyshev<double, double>(s, apply_J64, s->diag.p, s->lmax, v, z, s->cheb_d.p, s->cheb_r.p, st);
+      return chebyshev<double, double>(s, apply_J64, s->diag.p, s->lmax, s->opt.chebyshev_degree,
+                                       s->opt.chebyshev_ratio, v, z, s->cheb_d.p, s->cheb_r.p, st);
     };
   }
   SFX_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
@@ -559,12 +640,13 @@ int sfx_solver_default_options(sfx_solver_options* o) {
   o->precond = SFX_PREC_JACOBI_CHEBYSHEV;
   o->chebyshev_degree = 3;
   o->chebyshev_ratio = 30.0;
-  o->power_iterations = 10;
+  o->eigen_iterations = 20;
   o->mixed_precision = 0;
   o->inner_iterations = 40;
   o->inner_rel_tol = 1e-3;
   o->print_level = 0;
   o->learned_cycle = 1;
+  o->inner_chebyshev_degree = 0;
   return SFX_OK;
 }
 
@@ -577,6 +659,7 @@ int sfx_solver_create(sfx_form form, const sfx_solver_options* opt, sfx_solver* 
   if (opt) s->opt = *opt;
   else sfx_solver_default_options(&s->opt);
   if (s->opt.restart < 1 || s->opt.chebyshev_degree < 1 || s->opt.inner_iterations < 1 ||
+      s->opt.inner_chebyshev_degree < 0 || s->opt.eigen_iterations < 2 || !(s->opt.chebyshev_ratio > 1.0) ||
       s->opt.learned_cycle < 0 || s->opt.learned_cycle > 1) {
     delete s;
     return fail(SFX_ERR_INVALID, "bad solver options");

@@ -73,17 +73,18 @@ class LearnedPreconditioner:
 # ------------------------------------------------------------- materials
 def gaussian_random_field(n, ell, seed):
     """Unit-variance Gaussian random field on the n^3 element grid (element
-    centroids on the unit cube), by spectral filtering of white noise with
-    the Gaussian filter exp(-|k|^2 ell^2 / 8) (periodic FFT on a 2n grid,
-    cropped).  Its correlation is exp(-2 |r|^2 / ell^2), i.e. a Gaussian
-    kernel exp(-|r|^2 / (2 s^2)) with standard length s = ell / 2
-    (tests/test_learned_host.py measures it)."""
+    centroids on the unit cube) with Gaussian covariance exp(-|r|^2 / (2 ell^2))
+    (correlation length ell), by spectral filtering of white noise: the
+    covariance's spectral density is proportional to exp(-|k|^2 ell^2 / 2), so
+    the noise is multiplied by its square root exp(-|k|^2 ell^2 / 4) (periodic
+    FFT on a 2n grid, cropped to n).  tests/test_learned_host.py measures
+    the correlation."""
     rng = np.random.default_rng(seed)
     m = 2 * n
     w = rng.standard_normal((m, m, m))
     k = 2 * np.pi * np.fft.fftfreq(m, d=1.0 / n)
     KZ, KY, KX = np.meshgrid(k, k, k, indexing="ij")
-    S = np.exp(-(KX ** 2 + KY ** 2 + KZ ** 2) * ell ** 2 / 8.0)
+    S = np.exp(-(KX ** 2 + KY ** 2 + KZ ** 2) * ell ** 2 / 2.0)
     g = np.real(np.fft.ifftn(np.fft.fftn(w) * np.sqrt(S)))[:n, :n, :n]
     g = (g - g.mean()) / (g.std() + 1e-30)
     return g  # [z][y][x]
@@ -204,10 +205,11 @@ def solve_load_steps(setup, solver, u=None):
     return u, tot
 
 
-def smooth_fields(grid, count, rng, ell_range=(0.05, 0.5)):
+def smooth_fields(grid, count, rng, ell_range=(0.025, 0.25)):
     """count random 3-component displacement fields on the node grid: unit
-    Gaussian random fields with a correlation length drawn from ell_range,
-    byNODES float64 [count, 3 * nodes]."""
+    Gaussian random fields with a correlation length (Gaussian covariance
+    exp(-r^2 / (2 ell^2)), unit cube) drawn from ell_range, byNODES float64
+    [count, 3 * nodes]."""
     nx = grid[0]
     out = np.empty((count, 3 * nx ** 3))
     for i in range(count):

@@ -36,12 +36,13 @@ class SolverOptions(ctypes.Structure):
         ("precond", ctypes.c_int),
         ("chebyshev_degree", ctypes.c_int),
         ("chebyshev_ratio", ctypes.c_double),
-        ("power_iterations", ctypes.c_int),
+        ("eigen_iterations", ctypes.c_int),
         ("mixed_precision", ctypes.c_int),
         ("inner_iterations", ctypes.c_int),
         ("inner_rel_tol", ctypes.c_double),
         ("print_level", ctypes.c_int),
         ("learned_cycle", ctypes.c_int),
+        ("inner_chebyshev_degree", ctypes.c_int),
     ]
 
     @classmethod
@@ -66,6 +67,7 @@ class SolverStats(ctypes.Structure):
         ("last_krylov_rel", ctypes.c_double),
         ("learned_applications", ctypes.c_int),
         ("learned_fallbacks", ctypes.c_int),
+        ("lmax_estimate", ctypes.c_double),
     ]
 
     def as_dict(self):

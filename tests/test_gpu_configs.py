@@ -1,0 +1,230 @@
+"""Parity with the oracle at the configurations' own sizes.
+
+* 32^3 Q2 Neo-Hookean (823,875 DOF, perturbed mesh, K = 5, G = 0.25) at a
+  load-step-1 state: residual and Jacobian action (FP64 1e-12, FP32 1e-5) and
+  every CSR row of five node planes (graph identical, values 1e-12);
+* 64^3 Q2 heterogeneous Neo-Hookean (6,440,067 DOF, lognormal shear modulus
+  of correlation length 0.1, K = 20 G): residual and Jacobian action, 1e-12;
+* 16^3 Q2 heat (35,937 DOF, k = 1, f = 1, u = 0 on x = 0): the Jacobi-CG
+  solve to 1e-10 satisfies the oracle's system to that tolerance, and to
+  1e-12 lands within 1e-9 of the oracle's direct solution;
+* the 32^3 Neo-Hookean compression, load step 1 (u_z = -0.005 on z = 1):
+  the device warm start + Newton (GMRES(50), Jacobi-Chebyshev) against the
+  oracle's warm start + Newton with textbook Jacobi-CG linear solves on its
+  own matrix-free Jacobian, within 1e-9;
+* all 10 load steps of that ramp (to u_z = -0.05) on an 8^3 mesh against the
+  oracle's Newton with direct solves, within 1e-9 at every step.
+
+Reference semantics: functional.hpp:446-498 (residual), :406-432 (Jv),
+:569-667 (assemble), equation_solver.cpp:79-200 (Newton),
+solid_mechanics.hpp:1727-1770 (warm start).
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from tests.problems import rel
+
+pytestmark = pytest.mark.gpu
+
+THREADS = None  # all host cores
+
+
+def _threads():
+    import os
+
+    return THREADS or os.cpu_count() or 1
+
+
+def _load_step1_state(mesh_nodes_xyz, seed=2):
+    """u_z = -0.005 z plus a seeded 1e-4 N(0, 1) perturbation (load step 1 of
+    the compression, away from the exact solution)."""
+    X = mesh_nodes_xyz
+    u = np.zeros((3, X.shape[0]))
+    u[2] = -0.005 * X[:, 2]
+    u += 1e-4 * np.random.default_rng(seed).standard_normal(u.shape)
+    return u.ravel()
+
+
+def _neohookean_pair(n, params, perturb_seed=1):
+    import serac_gb300 as sg
+
+    V = sg.box_vertices(n, n, n, 0.1, perturb_seed)
+    mesh = sg.Mesh.structured_hex(n, n, n, V)
+    per_element = np.ndim(params) == 2
+    f = sg.Functional(mesh, sg.H1(2, 3))
+    f.AddDomainIntegral(sg.NEOHOOKEAN, params, per_element=per_element)
+    orc = O.OracleFunctional(O.StructuredHexMesh(n, n, n, V), 2, 3, nthreads=_threads())
+    orc.add_domain_integral(O.MAT_NEOHOOKEAN, params)
+    return mesh, f, orc
+
+
+def _residual_and_jvp(cuda, f, orc, u, du):
+    import serac_gb300 as sg
+
+    ut = torch.tensor(u, device=cuda)
+    r, J = f(0.0, sg.differentiate_wrt(ut))
+    r = r.cpu().numpy()
+    jv = J(torch.tensor(du, device=cuda)).cpu().numpy()
+    jv32 = J(torch.tensor(du, device=cuda, dtype=torch.float32)).double().cpu().numpy()
+    return r, jv, jv32, J
+
+
+def test_c2_residual_and_jacobian_action_match_oracle(cuda):
+    mesh, f, orc = _neohookean_pair(32, [5.0, 0.25])
+    assert f.ndofs == 823_875
+    u = _load_step1_state(mesh.node_coordinates(2))
+    du = np.random.default_rng(0).standard_normal(f.ndofs)
+    r, jv, jv32, _ = _residual_and_jvp(cuda, f, orc, u, du)
+    assert rel(r, orc.residual(u)) <= 1e-12
+    jv_ref = orc.jvp(u, du)
+    assert rel(jv, jv_ref) <= 1e-12
+    assert rel(jv32, jv_ref) <= 1e-5
+
+
+def test_c2_csr_rows_match_oracle(cuda):
+    """Five node planes (bottom, first mid-edge plane, a middle vertex plane
+    and its neighbour, top) of all three components: 63,375 rows."""
+    import serac_gb300 as sg
+
+    n = 32
+    mesh, f, orc = _neohookean_pair(n, [5.0, 0.25])
+    u = _load_step1_state(mesh.node_coordinates(2))
+    ut = torch.tensor(u, device=cuda)
+    _, J = f(0.0, sg.differentiate_wrt(ut))
+    row_ptr, col, val = sg.assemble(J)
+    assert int(row_ptr[-1]) == 152_771_337
+    N1 = 2 * n + 1
+    plane = N1 * N1
+    N = N1 ** 3
+    blocks = [(comp * N + k * plane, comp * N + (k + 1) * plane) for comp in range(3) for k in (0, 1, n, n + 1, 2 * n)]
+    rows = np.concatenate([np.arange(a, b) for a, b in blocks])
+    rp_ref, col_ref, val_ref = orc.assemble_rows(u, rows)
+    rp = row_ptr.cpu().numpy()
+    got_ptr, got_col, got_val = [np.zeros(1, dtype=np.int64)], [], []
+    for a, b in blocks:
+        lo, hi = int(rp[a]), int(rp[b])
+        got_ptr.append(rp[a + 1:b + 1] - lo + got_ptr[-1][-1])
+        got_col.append(col[lo:hi].cpu().numpy())
+        got_val.append(val[lo:hi].cpu().numpy())
+    got_ptr = np.concatenate(got_ptr)
+    assert np.array_equal(got_ptr, rp_ref)
+    assert np.array_equal(np.concatenate(got_col).astype(np.int64), col_ref)
+    assert rel(np.concatenate(got_val), val_ref) <= 1e-12
+
+
+def test_c3_residual_and_jacobian_action_match_oracle(cuda):
+    from serac_gb300 import learned as LP
+
+    prob = LP.neohookean_problem(64, 2, sigma_log=1.0, ell=0.1, strain=0.05, steps=10, bulk_ratio=20.0)
+    mesh, f, orc = _neohookean_pair(64, prob.params)
+    assert f.ndofs == 6_440_067
+    u = _load_step1_state(mesh.node_coordinates(2))
+    du = np.random.default_rng(1).standard_normal(f.ndofs)
+    r, jv, jv32, _ = _residual_and_jvp(cuda, f, orc, u, du)
+    assert rel(r, orc.residual(u)) <= 1e-12
+    jv_ref = orc.jvp(u, du)
+    assert rel(jv, jv_ref) <= 1e-12
+    assert rel(jv32, jv_ref) <= 1e-5
+
+
+def _heat16():
+    import serac_gb300 as sg
+
+    n = 16
+    V = sg.box_vertices(n, n, n)
+    mesh = sg.Mesh.structured_hex(n, n, n, V)
+    f = sg.Functional(mesh, sg.H1(2, 1))
+    f.AddDomainIntegral(sg.HEAT, [1.0, 1.0])
+    orc = O.OracleFunctional(O.StructuredHexMesh(n, n, n, V), 2, 1, nthreads=_threads())
+    orc.add_domain_integral(O.MAT_HEAT, [1.0, 1.0])
+    return mesh, f, orc, mesh.boundary_nodes(2, [5])
+
+
+def test_c1_cg_jacobi_solve_matches_oracle(cuda):
+    import serac_gb300 as sg
+
+    mesh, f, orc, ess = _heat16()
+    assert f.ndofs == 35_937
+    ref, _, _ = O.newton(orc, np.zeros(f.ndofs), ess, rel_tol=1e-12, abs_tol=0.0)
+    A = O.eliminate_dirichlet(orc.assemble(np.zeros(f.ndofs)), ess)
+    b = -orc.residual(np.zeros(f.ndofs))
+    b[ess] = 0.0
+    for tol, check in ((1e-10, "residual"), (1e-12, "solution")):
+        opts = sg.SolverOptions.defaults(krylov=sg.CG, precond=sg.JACOBI, krylov_rel_tol=tol, krylov_abs_tol=0.0,
+                                         newton_rel_tol=tol, newton_abs_tol=0.0, max_krylov_iterations=20000)
+        s = sg.NewtonSolver(f, opts)
+        s.set_essential(ess)
+        u = torch.zeros(f.ndofs, dtype=torch.float64, device=cuda)
+        st = s.solve(0.0, u)
+        assert st["converged"] == 1 and st["newton_iterations"] == 1
+        x = u.cpu().numpy()
+        if check == "residual":
+            # the device solution satisfies the oracle's linear system to the solve's tolerance
+            assert np.linalg.norm(b - A @ x) <= 1.05 * tol * np.linalg.norm(b)
+        else:
+            assert rel(x, ref) <= 1e-9
+
+
+def _compression(n, uz):
+    import serac_gb300 as sg
+
+    mesh, f, orc = _neohookean_pair(n, [5.0, 0.25])
+    N = f.num_nodes
+    bottom = mesh.boundary_nodes(2, [1])
+    top = mesh.boundary_nodes(2, [6])
+    ess = np.concatenate([bottom, N + bottom, 2 * N + bottom, 2 * N + top])
+    return mesh, f, orc, ess, 2 * N + top
+
+
+def _device_step(f, solver, u, top_dofs, uz):
+    target = u.clone()
+    target[torch.as_tensor(top_dofs, device=u.device)] = uz
+    solver.warm_start(0.0, u, target)
+    return solver.solve(0.0, u)
+
+
+def test_c2_newton_load_step1_matches_oracle_newton(cuda):
+    import serac_gb300 as sg
+
+    n, uz = 32, -0.005
+    mesh, f, orc, ess, top = _compression(n, uz)
+    opts = sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, restart=50, newton_rel_tol=1e-10,
+                                     newton_abs_tol=0.0, krylov_rel_tol=1e-10, krylov_abs_tol=0.0,
+                                     max_krylov_iterations=20000)
+    solver = sg.NewtonSolver(f, opts)
+    solver.set_essential(ess)
+    u = torch.zeros(f.ndofs, dtype=torch.float64, device=cuda)
+    st = _device_step(f, solver, u, top, uz)
+    assert st["converged"] == 1
+    target = np.zeros(f.ndofs)
+    target[top] = uz
+    u0, _ = O.warm_start_matrix_free(orc, np.zeros(f.ndofs), target, ess)
+    ref, it, rn, r0, _ = O.newton_matrix_free(orc, u0, ess, rel_tol=1e-12)
+    assert rn <= 1e-12 * r0
+    assert rel(u.cpu().numpy(), ref) <= 1e-9
+
+
+def test_compression_ramp_all_load_steps_match_oracle(cuda):
+    """The 10-step ramp to u_z = -0.05 on an 8^3 mesh (the 32^3 problem's
+    material and boundary conditions), every converged step within 1e-9."""
+    import serac_gb300 as sg
+
+    n, steps, final = 8, 10, -0.05
+    mesh, f, orc, ess, top = _compression(n, final)
+    opts = sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, newton_rel_tol=1e-10, newton_abs_tol=0.0,
+                                     krylov_rel_tol=1e-11, krylov_abs_tol=0.0, max_krylov_iterations=20000)
+    solver = sg.NewtonSolver(f, opts)
+    solver.set_essential(ess)
+    u = torch.zeros(f.ndofs, dtype=torch.float64, device=cuda)
+    ref = np.zeros(f.ndofs)
+    for step in range(1, steps + 1):
+        uz = final * step / steps
+        st = _device_step(f, solver, u, top, uz)
+        assert st["converged"] == 1, step
+        target = ref.copy()
+        target[top] = uz
+        ref = O.warm_start(orc, ref, target, ess)
+        ref, _, rn = O.newton(orc, ref, ess, rel_tol=1e-12, abs_tol=1e-14)
+        assert rel(u.cpu().numpy(), ref) <= 1e-9, step

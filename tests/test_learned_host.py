@@ -8,8 +8,8 @@ from serac_gb300.learned import gaussian_random_field, node_features
 
 def test_random_field_statistics():
     """Unit variance, zero mean, reproducible by seed, and correlation
-    exp(-2 r^2 / ell^2) along a grid axis (averaged over seeds)."""
-    n, ell = 48, 0.2
+    exp(-r^2 / (2 ell^2)) along a grid axis (averaged over seeds)."""
+    n, ell = 48, 0.1
     g = gaussian_random_field(n, ell, 3)
     assert g.shape == (n, n, n)
     assert abs(g.mean()) < 1e-12 and abs(g.std() - 1.0) < 1e-12
@@ -22,9 +22,9 @@ def test_random_field_statistics():
         for i, lag in enumerate(lags):
             acc[i] += np.mean(f[:, :, :n - lag] * f[:, :, lag:])
     emp = acc / len(seeds)
-    model = np.exp(-2.0 * (lags / n) ** 2 / ell ** 2)
+    model = np.exp(-0.5 * (lags / n) ** 2 / ell ** 2)
     assert np.abs(emp - model).max() < 0.06
-    assert np.abs(emp - np.exp(-((lags / n) ** 2) / ell ** 2)).max() > 0.1  # not the other convention
+    assert np.abs(emp - np.exp(-2.0 * (lags / n) ** 2 / ell ** 2)).max() > 0.1  # not a length of ell / 2
 
 
 def test_node_features():

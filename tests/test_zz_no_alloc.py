@@ -4,9 +4,9 @@ It exists for callers that cannot allocate device memory: the caller brings
 the vertex coordinates, the field and the output vector, and the library's
 element-residual scratch is a fixed device array.  This test calls it through
 the C ABI, twice in a row on the same inputs, and checks each result against
-the regular entry point (sfx_residual, whose scratch comes from the form) at
-the tolerance of the other FP64 parity tests (1e-12 relative), plus the
-size limit.  Collected last so that a failure here stops a -x run only after
+the regular entry point (sfx_residual, whose scratch comes from the form) and
+against the CPU oracle, at the tolerance of the other FP64 parity tests
+(1e-12 relative), plus the size limit.  Collected last so that a failure here stops a -x run only after
 every other test has run; it also passes alone in a fresh process.
 """
 import ctypes
@@ -58,6 +58,35 @@ def test_noalloc_residual_matches_regular_entry_point(cuda, material, order, com
         torch.cuda.synchronize()
         assert torch.isfinite(r).all()
         err = (torch.linalg.norm(r - expected) / torch.linalg.norm(expected)).item()
+        assert err <= TOL64, (call, err)
+
+
+def test_noalloc_residual_matches_oracle(cuda):
+    """The same entry point against the CPU oracle (serac's residual
+    restated), Neo-Hookean Q2 on a perturbed mesh, two calls in a row."""
+    import serac_gb300 as sg
+    from oracle import oracle as O
+    from serac_gb300 import _lib
+
+    lib = _lib.load()
+    lib.sfx_residual_structured_noalloc.restype = ctypes.c_int
+    lib.sfx_residual_structured_noalloc.argtypes = [ctypes.c_int] * 5 + [
+        ctypes.POINTER(ctypes.c_double), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
+        ctypes.c_void_p]
+    dims, params = (6, 5, 4), [5.0, 0.25]
+    V = sg.box_vertices(*dims, perturb=0.1, seed=5)
+    orc = O.OracleFunctional(O.StructuredHexMesh(*dims, V), 2, 3)
+    orc.add_domain_integral(O.MAT_NEOHOOKEAN, params)
+    V_dev = torch.tensor(V, device=cuda)
+    rng = np.random.default_rng(23)
+    for call in range(2):
+        u = rng.standard_normal(orc.ndofs) * 0.02
+        u_dev = torch.tensor(u, device=cuda)
+        r = torch.full_like(u_dev, float("nan"))
+        assert _noalloc(lib, dims, 2, 1, params, V_dev, u_dev, r) == 0, lib.sfx_last_error()
+        torch.cuda.synchronize()
+        ref = orc.residual(u)
+        err = np.linalg.norm(r.cpu().numpy() - ref) / np.linalg.norm(ref)
         assert err <= TOL64, (call, err)
 
 
