@@ -959,12 +959,22 @@ constexpr bool tangent_has_source() {
 /// Shape of the stored q-function derivative per quadrature point:
 /// rows = parent-space outputs (source components if the source depends on the
 /// trial field, then the C x 3 flux), cols = parent-space inputs (values if the
-/// q-function reads them, then the C x 3 gradient).
-template <int C, bool HS, bool VI>
+/// q-function reads them, then the C x 3 gradient).  SYM: the block is
+/// symmetric (a hyperelastic or associative-plastic tangent, whose flux is
+/// the gradient of a potential in the trial gradient; det(J) w and the
+/// parent-space map J^-1 (.) J^-T keep that symmetry), so only its upper
+/// triangle is stored, row-major (packed): 45 entries instead of 81 for the
+/// vector 9 x 9 block, 6 instead of 9 for the scalar 3 x 3 one.
+template <int C, bool HS, bool VI, bool SYM = false>
 struct TangentShape {
   static constexpr int rows = (HS ? C : 0) + 3 * C;
   static constexpr int cols = (VI ? C : 0) + 3 * C;
-  static constexpr int size = rows * cols;
+  static constexpr bool packed = SYM && rows == cols;
+  static constexpr int size = packed ? rows * (rows + 1) / 2 : rows * cols;
+  /// position of entry (r, k) in the per-point block (packed: r <= k)
+  static SFX_HDI constexpr int index(int r, int k) {
+    return packed ? r * cols - r * (r - 1) / 2 + (k - r) : r * cols + k;
+  }
   /// entries of one element's block (size x NQ) rounded up to a multiple of
   /// 4, so that every block starts on a 16-byte (FP32) / 32-byte (FP64)
   /// boundary and can be moved by a bulk copy
@@ -978,6 +988,43 @@ struct TangentShape {
   static constexpr int64_t stride_of = sizeof(TS) == 2 ? stride16<NQ> : stride<NQ>;
 };
 
+/// out = D in (TRANSPOSE: D^T in) for one point's block, read with stride NQ
+/// from Dq (this lane's point).  A packed symmetric block is read once per
+/// stored entry and used for both (r, k) and (k, r): 45 loads and 81 FMA for
+/// the vector 9 x 9 block; D^T = D there.
+template <typename Shape, int NQ, bool TRANSPOSE, typename Real, typename TS>
+SFX_HDI void apply_block(const TS* Dq, const Real* in, Real* out, bool valid) {
+  if constexpr (Shape::packed) {
+#pragma unroll
+    for (int r = 0; r < Shape::rows; r++) out[r] = Real(0);
+#pragma unroll
+    for (int r = 0; r < Shape::rows; r++) {
+#pragma unroll
+      for (int k = r; k < Shape::cols; k++) {
+        const Real d = valid ? Real(Dq[Shape::index(r, k) * NQ]) : Real(0);
+        out[r] += d * in[k];
+        if (k != r) out[k] += d * in[r];
+      }
+    }
+  } else if constexpr (TRANSPOSE) {
+#pragma unroll
+    for (int k = 0; k < Shape::cols; k++) {
+      Real acc = 0;
+#pragma unroll
+      for (int r = 0; r < Shape::rows; r++) acc += (valid ? Real(Dq[Shape::index(r, k) * NQ]) : Real(0)) * in[r];
+      out[k] = acc;
+    }
+  } else {
+#pragma unroll
+    for (int r = 0; r < Shape::rows; r++) {
+      Real acc = 0;
+#pragma unroll
+      for (int k = 0; k < Shape::cols; k++) acc += (valid ? Real(Dq[Shape::index(r, k) * NQ]) : Real(0)) * in[k];
+      out[r] = acc;
+    }
+  }
+}
+
 /// storage -> FP32 for the tangent copies of the FP32 Jacobian action
 SFX_HDI float tangent_to_f32(float x) { return x; }
 SFX_HDI float tangent_to_f32(__half x) { return __half2float(x); }
@@ -989,7 +1036,7 @@ SFX_HDI float tangent_to_f32(__half x) { return __half2float(x); }
 /// D[e * stride + (row * cols + col) * NQ + q] (stride = TangentShape::stride),
 /// in FP64 and FP32 (or FP16 with its own stride16), so that one element's
 /// tangent is one contiguous block; D32 / D16 may be null.
-template <int P, int C, typename State, typename QFMaker>
+template <int P, int C, typename State, typename QFMaker, bool SYM = false>
 __global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QFMaker make_qf, double* __restrict__ D64,
                                                         float* __restrict__ D32, __half* __restrict__ D16,
                                                         double* __restrict__ res_e) {
@@ -1093,14 +1140,14 @@ __global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QF
     using SrcT = std::decay_t<decltype(get<0>(out))>;
     using FluxT = std::decay_t<decltype(get<1>(out))>;
     constexpr bool HS = has_part<JVP, SrcT>();
-    using Shape = TangentShape<C, HS, VI>;
+    using Shape = TangentShape<C, HS, VI, SYM>;
     int row = 0;
 #pragma unroll
     for (int ci = 0; ci < C; ci++) {
       if constexpr (HS) {
         Real v = dvol * part<JVP, Real>(source_comp<C>(get<0>(out), ci));
-        if (valid) {
-          const int64_t in_block = (int64_t(ci) * Shape::cols + k) * NQ + qi;
+        if (valid && (!Shape::packed || ci <= k)) {
+          const int64_t in_block = int64_t(Shape::index(ci, k)) * NQ + qi;
           D64[e * Shape::template stride<NQ> + in_block] = v;
           if (D32) D32[e * Shape::template stride<NQ> + in_block] = float(v);
           if (D16) D16[e * Shape::template stride16<NQ> + in_block] = __float2half_rn(float(v));
@@ -1124,8 +1171,8 @@ __global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QF
 #pragma unroll
       for (int kd = 0; kd < 3; kd++) {
         Real v = dvol * (fp[0] * Ji[kd][0] + fp[1] * Ji[kd][1] + fp[2] * Ji[kd][2]);
-        if (valid) {
-          const int64_t in_block = (int64_t(row + 3 * ci + kd) * Shape::cols + k) * NQ + qi;
+        if (valid && (!Shape::packed || row + 3 * ci + kd <= k)) {
+          const int64_t in_block = int64_t(Shape::index(row + 3 * ci + kd, k)) * NQ + qi;
           D64[e * Shape::template stride<NQ> + in_block] = v;
           if (D32) D32[e * Shape::template stride<NQ> + in_block] = float(v);
           if (D16) D16[e * Shape::template stride16<NQ> + in_block] = __float2half_rn(float(v));
@@ -1151,14 +1198,14 @@ __global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QF
 
 /// Jacobian action from the stored derivative (serac's action_of_gradient_kernel,
 /// domain_integral_kernels.hpp:277-304): interpolate du, apply D, integrate.
-template <int P, int C, bool HS, bool VI, typename Real>
+template <int P, int C, bool HS, bool VI, typename Real, bool SYM = false>
 __global__ void __launch_bounds__(128) jvp_stored_kernel(const Real* __restrict__ du, const Real* __restrict__ D,
                                                          const int32_t* __restrict__ conn, Real* __restrict__ out_e,
                                                          int64_t num_nodes, int64_t num_elements) {
   constexpr int Q = P + 1;
   constexpr int NQ = Q * Q * Q;
   constexpr int EPW = 32 / NQ;
-  using Shape = TangentShape<C, HS, VI>;
+  using Shape = TangentShape<C, HS, VI, SYM>;
   const int lane = threadIdx.x & 31;
   const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const int sub = lane / NQ;
@@ -1196,13 +1243,7 @@ __global__ void __launch_bounds__(128) jvp_stored_kernel(const Real* __restrict_
   }
   Real dout[Shape::rows];
   const Real* Dq = D + (valid ? e * Shape::template stride<NQ> + qi : 0);
-#pragma unroll
-  for (int r = 0; r < Shape::rows; r++) {
-    Real acc = 0;
-#pragma unroll
-    for (int k = 0; k < Shape::cols; k++) acc += (valid ? Dq[(r * Shape::cols + k) * NQ] : Real(0)) * din[k];
-    dout[r] = acc;
-  }
+  apply_block<Shape, NQ, false>(Dq, din, dout, valid);
   constexpr int roff = HS ? C : 0;
 #pragma unroll
   for (int c = 0; c < C; c++) {
@@ -1221,7 +1262,7 @@ __global__ void __launch_bounds__(128) jvp_stored_kernel(const Real* __restrict_
 /// interpolated onto the output side (values if the source depends on the
 /// field, then the gradient), D^T is applied, and the result is integrated
 /// on the input side (values if the q-function reads them, then the flux).
-template <int P, int C, bool HS, bool VI, typename Real>
+template <int P, int C, bool HS, bool VI, typename Real, bool SYM = false>
 __global__ void __launch_bounds__(128) jvp_stored_transpose_kernel(const Real* __restrict__ v,
                                                                    const Real* __restrict__ D,
                                                                    const int32_t* __restrict__ conn,
@@ -1230,7 +1271,7 @@ __global__ void __launch_bounds__(128) jvp_stored_transpose_kernel(const Real* _
   constexpr int Q = P + 1;
   constexpr int NQ = Q * Q * Q;
   constexpr int EPW = 32 / NQ;
-  using Shape = TangentShape<C, HS, VI>;
+  using Shape = TangentShape<C, HS, VI, SYM>;
   const int lane = threadIdx.x & 31;
   const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const int sub = lane / NQ;
@@ -1265,13 +1306,7 @@ __global__ void __launch_bounds__(128) jvp_stored_transpose_kernel(const Real* _
   }
   Real vout[Shape::cols];
   const Real* Dq = D + (valid ? e * Shape::template stride<NQ> + qi : 0);
-#pragma unroll
-  for (int k = 0; k < Shape::cols; k++) {
-    Real acc = 0;
-#pragma unroll
-    for (int r = 0; r < Shape::rows; r++) acc += (valid ? Dq[(r * Shape::cols + k) * NQ] : Real(0)) * vin[r];
-    vout[k] = acc;
-  }
+  apply_block<Shape, NQ, true>(Dq, vin, vout, valid);
   constexpr int coff = VI ? C : 0;
 #pragma unroll
   for (int c = 0; c < C; c++) {
@@ -1292,14 +1327,15 @@ __global__ void __launch_bounds__(128) jvp_stored_transpose_kernel(const Real* _
 /// does not complete sets *err and the warp drains its outstanding copies
 /// (again bounded) before returning.  TRANSPOSE applies the block transposed
 /// (J^T v, as jvp_stored_transpose_kernel) with the same staging.
-template <int C, bool HS, bool VI, int WARPS, int STAGES, bool TRANSPOSE = false, typename TS = float>
+template <int C, bool HS, bool VI, int WARPS, int STAGES, bool TRANSPOSE = false, typename TS = float,
+          bool SYM = false>
 __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float* __restrict__ du,
                                                                     const TS* __restrict__ D,
                                                                     const int32_t* __restrict__ conn,
                                                                     float* __restrict__ out_e, int64_t num_nodes,
                                                                     int64_t num_elements, int* __restrict__ err) {
   constexpr int P = 2, Q = 3, NQ = 27;
-  using Shape = TangentShape<C, HS, VI>;
+  using Shape = TangentShape<C, HS, VI, SYM>;
   // input side (interpolated direction) and output side (integrated) of the
   // block: D[out][in] for J, D^T for J^T
   constexpr bool IN_VALUE = TRANSPOSE ? HS : VI;
@@ -1385,13 +1421,27 @@ __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float*
     }
     const TS* Dq = my_ring + s * ES + qi;
     float dout[NOUT];
+    if constexpr (Shape::packed) {
 #pragma unroll
-    for (int r = 0; r < NOUT; r++) {
-      float acc = 0.f;
+      for (int r = 0; r < NOUT; r++) dout[r] = 0.f;
 #pragma unroll
-      for (int k = 0; k < NIN; k++)
-        acc += tangent_to_f32(Dq[(TRANSPOSE ? k * Shape::cols + r : r * Shape::cols + k) * NQ]) * din[k];
-      dout[r] = acc;
+      for (int r = 0; r < NOUT; r++) {
+#pragma unroll
+        for (int k = r; k < NIN; k++) {
+          const float d = tangent_to_f32(Dq[Shape::index(r, k) * NQ]);
+          dout[r] += d * din[k];
+          if (k != r) dout[k] += d * din[r];
+        }
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < NOUT; r++) {
+        float acc = 0.f;
+#pragma unroll
+        for (int k = 0; k < NIN; k++)
+          acc += tangent_to_f32(Dq[(TRANSPOSE ? Shape::index(k, r) : Shape::index(r, k)) * NQ]) * din[k];
+        dout[r] = acc;
+      }
     }
     __syncwarp();  // every lane has read stage s
     if (lane == 0) {
@@ -1436,14 +1486,14 @@ namespace kernels {
 /// with Psi_0 = phi and Psi_{1..3} = d phi / d xi_k.  Each (a, b) term is a
 /// product of 1-D factors, so the sum over the points runs as three
 /// sum-factorised passes (x, y, z) of 3 FMA per lane.
-template <int P, int C, bool HS, bool VI>
+template <int P, int C, bool HS, bool VI, bool SYM = false>
 __global__ void __launch_bounds__(128) diag_from_tangent_kernel(const double* __restrict__ D, double* __restrict__ out_e,
                                                                 int64_t num_elements) {
   using Real = double;
   constexpr int Q = P + 1;
   constexpr int NQ = Q * Q * Q;
   constexpr int EPW = 32 / NQ;
-  using Shape = TangentShape<C, HS, VI>;
+  using Shape = TangentShape<C, HS, VI, SYM>;
   const int lane = threadIdx.x & 31;
   const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const int sub = lane / NQ;
@@ -1474,7 +1524,9 @@ __global__ void __launch_bounds__(128) diag_from_tangent_kernel(const double* __
       for (int b = (VI ? 0 : 1); b < 4; b++) {
         const int row = (a == 0) ? c : (HS ? C : 0) + 3 * c + (a - 1);
         const int col = (b == 0) ? c : (VI ? C : 0) + 3 * c + (b - 1);
-        Real d = valid ? D[e * Shape::template stride<NQ> + (int64_t(row) * Shape::cols + col) * NQ + qi] : Real(0);
+        const int ent = Shape::packed ? Shape::index(row < col ? row : col, row < col ? col : row)
+                                      : Shape::index(row, col);
+        Real d = valid ? D[e * Shape::template stride<NQ> + int64_t(ent) * NQ + qi] : Real(0);
         // x-pass: T1(ix', qy, qz) = sum_qx d(qx,qy,qz) fa_x(qx,ix') fb_x(qx,ix')
         Real t1 = 0;
 #pragma unroll

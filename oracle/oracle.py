@@ -998,6 +998,24 @@ def newton_matrix_free(f, u0, ess, rel_tol=1e-10, abs_tol=0.0, lin_rtol=None, ma
     return u, it, np.linalg.norm(r), r0, lin_total
 
 
+def newton_correction(f, u, ess, t=0.0, lin_rtol=1e-2, max_lin=50000):
+    """One step of the oracle's own Newton iteration from u: the correction
+    du = J(u)^-1 R(u) on the free rows (Dirichlet-eliminated, Jacobi-CG on
+    the matrix-free stored-derivative Jacobian, to relative accuracy
+    lin_rtol).  Near the solution Newton converges quadratically, so
+    u - du is the oracle's converged solution up to O(|du|^2) + lin_rtol |du|:
+    |du| measures how far u is from it.  Returns (du, |R(u)|, CG iterations)."""
+    mask = np.ones(f.ndofs)
+    mask[ess] = 0.0
+    r = f.residual(u, t=t)
+    r[ess] = 0.0
+    lin = OracleLinearization(f, u, t)
+    diag = jacobian_diagonal(f, u, t)
+    diag[ess] = 1.0
+    du, k, _ = cg(lambda x: lin.apply(x * mask) * mask + x * (1.0 - mask), r, diag, rtol=lin_rtol, maxiter=max_lin)
+    return du, float(np.linalg.norm(r)), k
+
+
 def warm_start_matrix_free(f, u, u_target, ess, t=0.0, lin_rtol=1e-3, max_lin=50000):
     """warm_start with the matrix-free Jacobi-CG linear solve (the predictor
     is only a starting point for Newton: its tolerance does not change the

@@ -18,9 +18,12 @@ namespace {
 using namespace sfx;
 using J2 = solid_mechanics::J2SmallStrain<solid_mechanics::LinearHardening>;
 
+// symmetric_tangent: the stored derivative block is symmetric (the flux is
+// the gradient of a potential in the trial gradient), so it is stored packed
 struct HeatMaker {
   static constexpr int nparams = 2;
   static constexpr bool value_input = false;
+  static constexpr bool symmetric_tangent = true;
   SFX_HD heat_transfer::HeatIntegrand operator()(const double* p) const {
     heat_transfer::HeatIntegrand q{};
     q.material.conductivity = p[0];
@@ -38,6 +41,7 @@ struct NonlinearHeatMaker {
 struct NeoHookeanMaker {
   static constexpr int nparams = 2;
   static constexpr bool value_input = false;
+  static constexpr bool symmetric_tangent = true;  // first Piola stress = dW/dF
   SFX_HD solid_mechanics::MaterialStressFunctor<solid_mechanics::NeoHookean, true> operator()(const double* p) const {
     return {solid_mechanics::NeoHookean{1.0, p[0], p[1]}};
   }
@@ -45,6 +49,7 @@ struct NeoHookeanMaker {
 struct J2Maker {
   static constexpr int nparams = 4;
   static constexpr bool value_input = false;
+  static constexpr bool symmetric_tangent = true;  // associative flow, linear isotropic hardening
   SFX_HD solid_mechanics::MaterialStressFunctor<J2, false> operator()(const double* p) const {
     J2 m{};
     m.E = p[0];
@@ -65,6 +70,12 @@ struct ElasticTestMaker {
   static constexpr bool value_input = true;
   SFX_HD test_models::ElasticModel operator()(const double*) const { return {}; }
 };
+
+// Maker::symmetric_tangent where declared, false otherwise
+template <typename M, typename = void>
+struct sym_of : std::false_type {};
+template <typename M>
+struct sym_of<M, std::void_t<decltype(M::symmetric_tangent)>> : std::bool_constant<M::symmetric_tangent> {};
 
 // Calls fn.template operator()<C, State, Maker>() for the form's material.
 template <typename Fn>
@@ -163,7 +174,8 @@ struct LinearizeFn {
     constexpr int EPW = 32 / NQ;
     using QF = decltype(Maker{}(nullptr));
     constexpr bool HS = kernels::tangent_has_source<C, State, QF>();
-    using Shape = kernels::TangentShape<C, HS, Maker::value_input>;
+    constexpr bool SYM = sym_of<Maker>::value;
+    using Shape = kernels::TangentShape<C, HS, Maker::value_input, SYM>;
     const size_t n = size_t(f.ne) * size_t(Shape::template stride<NQ>);
     const size_t n16 = size_t(f.ne) * size_t(Shape::template stride16<NQ>);
     cudaError_t err = cudaSuccess;
@@ -185,8 +197,8 @@ struct LinearizeFn {
                                   f.nnodes, f.ne, f.t_lin};
     int64_t warps = (f.ne + EPW - 1) / EPW;
     int64_t blocks = (warps * 32 + 127) / 128;
-    kernels::linearize_kernel<P, C, State, Maker><<<unsigned(blocks), 128, 0, s>>>(a, Maker{}, di.D64.p, di.D32.p,
-                                                                                   di.D16.p, res_e);
+    kernels::linearize_kernel<P, C, State, Maker, SYM><<<unsigned(blocks), 128, 0, s>>>(a, Maker{}, di.D64.p, di.D32.p,
+                                                                                        di.D16.p, res_e);
     err = cudaGetLastError();
     if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("linearize launch: ") + cudaGetErrorString(err));
     return SFX_OK;
@@ -196,10 +208,10 @@ struct LinearizeFn {
 // Bulk-copy staged FP32 action for Q2 (J, or J^T when TRANSPOSE): one
 // persistent block per SM with as many warps as fit two-deep rings in 220 KB
 // of shared memory, rings up to 4 deep.
-template <int C, bool HS, bool VI, bool TRANSPOSE, typename TS>
+template <int C, bool HS, bool VI, bool TRANSPOSE, typename TS, bool SYM>
 int launch_tma(const sfx_form_s& f, const float* du, const TS* D, float* E, cudaStream_t s) {
   constexpr int NQ = 27;
-  using Shape = kernels::TangentShape<C, HS, VI>;
+  using Shape = kernels::TangentShape<C, HS, VI, SYM>;
   constexpr size_t kSmemBudget = 220 * 1024;
   constexpr size_t stage_bytes = size_t(Shape::template stride_of<NQ, TS>) * sizeof(TS) + 8;
   constexpr int WARPS = 16 * 2 * stage_bytes <= kSmemBudget   ? 16
@@ -209,7 +221,7 @@ int launch_tma(const sfx_form_s& f, const float* du, const TS* D, float* E, cuda
   constexpr int STAGES = int(std::min<size_t>(4, kSmemBudget / (WARPS * stage_bytes)));
   static_assert(STAGES >= 2, "tangent block too large for a two-stage ring");
   constexpr size_t smem = size_t(WARPS) * STAGES * stage_bytes;
-  auto kern = kernels::jvp_stored_tma_kernel<C, HS, VI, WARPS, STAGES, TRANSPOSE, TS>;
+  auto kern = kernels::jvp_stored_tma_kernel<C, HS, VI, WARPS, STAGES, TRANSPOSE, TS, SYM>;
   static bool configured = false;  // per instantiation
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
@@ -242,14 +254,15 @@ struct StoredJvpFn {
     using QF = decltype(Maker{}(nullptr));
     constexpr bool HS = kernels::tangent_has_source<C, State, QF>();
     if (f.ne == 0) return SFX_OK;
+    constexpr bool SYM = sym_of<Maker>::value;
     if constexpr (P == 2 && std::is_same<Real, float>::value) {
-      const int rc = f.tangent16 ? launch_tma<C, HS, Maker::value_input, false, __half>(f, du, di.D16.p, E, s)
-                                 : launch_tma<C, HS, Maker::value_input, false, float>(f, du, D, E, s);
+      const int rc = f.tangent16 ? launch_tma<C, HS, Maker::value_input, false, __half, SYM>(f, du, di.D16.p, E, s)
+                                 : launch_tma<C, HS, Maker::value_input, false, float, SYM>(f, du, D, E, s);
       if (rc) return rc;
     } else {
       int64_t warps = (f.ne + EPW - 1) / EPW;
       int64_t blocks = (warps * 32 + 127) / 128;
-      kernels::jvp_stored_kernel<P, C, HS, Maker::value_input, Real>
+      kernels::jvp_stored_kernel<P, C, HS, Maker::value_input, Real, SYM>
           <<<unsigned(blocks), 128, 0, s>>>(du, D, f.conn.p, E, f.nnodes, f.ne);
     }
     cudaError_t err = cudaGetLastError();
@@ -273,14 +286,15 @@ struct StoredJvpTransposeFn {
     using QF = decltype(Maker{}(nullptr));
     constexpr bool HS = kernels::tangent_has_source<C, State, QF>();
     if (f.ne == 0) return SFX_OK;
+    constexpr bool SYM = sym_of<Maker>::value;
     if constexpr (P == 2 && std::is_same<Real, float>::value) {
-      const int rc = f.tangent16 ? launch_tma<C, HS, Maker::value_input, true, __half>(f, v, di.D16.p, E, s)
-                                 : launch_tma<C, HS, Maker::value_input, true, float>(f, v, D, E, s);
+      const int rc = f.tangent16 ? launch_tma<C, HS, Maker::value_input, true, __half, SYM>(f, v, di.D16.p, E, s)
+                                 : launch_tma<C, HS, Maker::value_input, true, float, SYM>(f, v, D, E, s);
       if (rc) return rc;
     } else {
       const int64_t warps = (f.ne + EPW - 1) / EPW;
       const int64_t blocks = (warps * 32 + 127) / 128;
-      kernels::jvp_stored_transpose_kernel<P, C, HS, Maker::value_input, Real>
+      kernels::jvp_stored_transpose_kernel<P, C, HS, Maker::value_input, Real, SYM>
           <<<unsigned(blocks), 128, 0, s>>>(v, D, f.conn.p, E, f.nnodes, f.ne);
     }
     cudaError_t err = cudaGetLastError();
@@ -304,7 +318,8 @@ struct DiagFn {
     if (f.ne == 0) return SFX_OK;
     int64_t warps = (f.ne + EPW - 1) / EPW;
     int64_t blocks = (warps * 32 + 127) / 128;
-    kernels::diag_from_tangent_kernel<P, C, HS, Maker::value_input><<<unsigned(blocks), 128, 0, s>>>(di.D64.p, E, f.ne);
+    kernels::diag_from_tangent_kernel<P, C, HS, Maker::value_input, sym_of<Maker>::value>
+        <<<unsigned(blocks), 128, 0, s>>>(di.D64.p, E, f.ne);
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("diagonal launch: ") + cudaGetErrorString(err));
     return SFX_OK;

@@ -22,7 +22,7 @@ def test_reference_arm_json_line():
         assert key in d, key
     assert d["metric"] == "Jv GDOF/s" and d["unit"] == "GDOF/s" and d["higher_is_better"] is True
     assert d["steps"] == 3 and d["warmup"] == 3 and d["value"] > 0
-    assert d["config"]["workload"] == "neohookean_q2_vector_32cubed_jvp"
+    assert d["config"]["workload"] == "neohookean_heterogeneous_q2_vector_96cubed_jvp"
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}

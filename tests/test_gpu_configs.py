@@ -9,9 +9,9 @@
   solve to 1e-10 satisfies the oracle's system to that tolerance, and to
   1e-12 lands within 1e-9 of the oracle's direct solution;
 * the 32^3 Neo-Hookean compression, load step 1 (u_z = -0.005 on z = 1):
-  the device warm start + Newton (GMRES(50), Jacobi-Chebyshev) against the
-  oracle's warm start + Newton with textbook Jacobi-CG linear solves on its
-  own matrix-free Jacobian, within 1e-9;
+  the device warm start + Newton (GMRES(50), Jacobi-Chebyshev) lands within
+  1e-9 of the oracle's Newton solution (one oracle Newton step from it, on
+  the oracle's own residual and matrix-free Jacobian, moves it by < 1e-9);
 * all 10 load steps of that ramp (to u_z = -0.05) on an 8^3 mesh against the
   oracle's Newton with direct solves, within 1e-9 at every step.
 
@@ -186,24 +186,35 @@ def _device_step(f, solver, u, top_dofs, uz):
 
 
 def test_c2_newton_load_step1_matches_oracle_newton(cuda):
+    """The device solution is a fixed point of the oracle's Newton map: one
+    oracle Newton step from it (its own residual and matrix-free Jacobian,
+    Jacobi-CG to 1e-2) moves it by less than 1e-9 relative, so it lies within
+    1e-9 of the oracle's converged solution (the remainder is O(|du|^2)).
+    A full oracle solve from rest at this size takes tens of thousands of
+    matrix-free CG iterations; the ramp test below runs the oracle's full
+    Newton (direct solves) at every load step on a smaller mesh."""
     import serac_gb300 as sg
 
     n, uz = 32, -0.005
     mesh, f, orc, ess, top = _compression(n, uz)
     opts = sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, restart=50, newton_rel_tol=1e-10,
                                      newton_abs_tol=0.0, krylov_rel_tol=1e-10, krylov_abs_tol=0.0,
-                                     max_krylov_iterations=20000)
+                                     max_krylov_iterations=40000)
     solver = sg.NewtonSolver(f, opts)
     solver.set_essential(ess)
     u = torch.zeros(f.ndofs, dtype=torch.float64, device=cuda)
     st = _device_step(f, solver, u, top, uz)
     assert st["converged"] == 1
-    target = np.zeros(f.ndofs)
-    target[top] = uz
-    u0, _ = O.warm_start_matrix_free(orc, np.zeros(f.ndofs), target, ess)
-    ref, it, rn, r0, _ = O.newton_matrix_free(orc, u0, ess, rel_tol=1e-12)
-    assert rn <= 1e-12 * r0
-    assert rel(u.cpu().numpy(), ref) <= 1e-9
+    x = u.cpu().numpy()
+    # the device solution carries the load step's boundary values exactly
+    assert np.all(x[top] == uz) and np.all(x[ess[: ess.size - top.size]] == 0.0)
+    du, rnorm, _ = O.newton_correction(orc, x, ess)
+    r0 = np.zeros(f.ndofs)
+    r0[top] = uz
+    rest = orc.residual(r0)
+    rest[ess] = 0.0
+    assert rnorm <= 1e-9 * np.linalg.norm(rest)
+    assert np.linalg.norm(du) <= 1e-9 * np.linalg.norm(x)
 
 
 def test_compression_ramp_all_load_steps_match_oracle(cuda):

@@ -80,7 +80,7 @@ def test_noalloc_residual_matches_oracle(cuda):
     V_dev = torch.tensor(V, device=cuda)
     rng = np.random.default_rng(23)
     for call in range(2):
-        u = rng.standard_normal(orc.ndofs) * 0.02
+        u = rng.standard_normal(orc.ndofs) * 0.005  # keeps det F > 0 at every point
         u_dev = torch.tensor(u, device=cuda)
         r = torch.full_like(u_dev, float("nan"))
         assert _noalloc(lib, dims, 2, 1, params, V_dev, u_dev, r) == 0, lib.sfx_last_error()
