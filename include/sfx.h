@@ -67,6 +67,13 @@ extern "C" {
 #define SFX_MAT_THERMAL_TEST 3
 #define SFX_MAT_ELASTIC_TEST 4
 #define SFX_MAT_NONLINEAR_HEAT 5
+/* Multi-field material (sfx_mform_add_domain_integral), per-element
+ * parameters {density, K0, G0}, arguments (displacement 3, acceleration 3,
+ * bulk modulus offset 1, shear modulus offset 1):
+ *   SFX_MAT_PARAM_NEOHOOKEAN  {density a, P(grad u; K0 + dK, G0 + dG)}
+ *   (ParameterizedNeoHookeanSolid, parameterized_solid_material.hpp:68-110, in
+ *   SolidMechanics' material integrand with acceleration, solid_mechanics.hpp:809-850) */
+#define SFX_MAT_PARAM_NEOHOOKEAN 16
 
 /* Boundary materials: SFX_BMAT_HEAT_FLUX {q0, q1, alpha}: -(q0 + q1 x + alpha u);
  * SFX_BMAT_TRACTION {t0[3], t1[3]}: -(t0 + t1 x); SFX_BMAT_PRESSURE {p}:
@@ -80,6 +87,7 @@ extern "C" {
 
 typedef struct sfx_mesh_s* sfx_mesh;
 typedef struct sfx_form_s* sfx_form;
+typedef struct sfx_mform_s* sfx_mform;
 
 const char* sfx_last_error(void);
 int sfx_version(void);
@@ -355,6 +363,36 @@ int sfx_update_qdata(sfx_form form, int flag);
 int sfx_qdata_size(sfx_form form, int64_t* num_doubles);
 int sfx_set_qdata(sfx_form form, const double* host_state);
 int sfx_get_qdata(sfx_form form, double* host_state);
+
+/* Multi-field forms: Functional<test(trial_0, ..., trial_{n-1})>
+ * (functional.hpp:189-317), the form SolidMechanics builds as
+ * test(displacement, acceleration, parameters...) (solid_mechanics.hpp:243).
+ * Every field is H1 of the form's order on the mesh's node grid (an H1 field
+ * of lower order is represented exactly by its values there), byNODES
+ * ([component][node]); field_components[i] is 1 or 3; the test space has 3
+ * components.  Fields are passed as a host array of num_fields device
+ * pointers. */
+int sfx_mform_create(sfx_mesh mesh, int order, int test_components, int num_fields, const int* field_components,
+                     sfx_mform* out);
+int sfx_mform_destroy(sfx_mform form);
+int sfx_mform_num_nodes(sfx_mform form, int64_t* out);
+/* AddDomainIntegral(Dimension<3>, DependsOn<depends_on...>, material): the
+ * material's arguments, in order, are the form fields depends_on[0..num_args);
+ * params: host, as for sfx_form_add_domain_integral. */
+int sfx_mform_add_domain_integral(sfx_mform form, int material, const int* depends_on, int num_args,
+                                  const double* params, int per_element);
+/* r = R(t, fields...) (test space, 3 x num_nodes). */
+int sfx_mform_residual(sfx_mform form, double t, const double* const* fields, double* r, void* stream);
+/* operator()(t, ..., differentiate_wrt(field wrt), ...): stores, per
+ * quadrature point, the derivative of every integral that depends on field
+ * `wrt` with respect to it (an integral that does not contributes zero). */
+int sfx_mform_linearize(sfx_mform form, double t, const double* const* fields, int wrt, void* stream);
+/* dr = dR/d(field wrt) d_field (Gradient::Mult for that argument); wrt must
+ * be the field of the last sfx_mform_linearize. */
+int sfx_mform_jvp(sfx_mform form, int wrt, const double* d_field, double* dr, void* stream);
+/* out_field = (dR/d(field wrt))^T v: the test-space vector v mapped onto the
+ * field (what a sensitivity with respect to a parameter field needs). */
+int sfx_mform_jvp_transpose(sfx_mform form, int wrt, const double* v, double* out_field, void* stream);
 
 #ifdef __cplusplus
 }

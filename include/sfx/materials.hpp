@@ -7,6 +7,8 @@
 //   NeoHookean                      physics/materials/solid_material.hpp:98-127
 //   J2SmallStrain<LinearHardening>  physics/materials/solid_material.hpp:132-148, 199-258
 //   MaterialStressFunctor           physics/solid_mechanics.hpp:809-850
+//   ParameterizedNeoHookean         physics/materials/parameterized_solid_material.hpp:68-110
+//   MultiFieldStressFunctor         physics/solid_mechanics.hpp:809-850, 880-893 (acceleration, parameters)
 // The q-function call convention is serac's: qf(t, tuple{X, dX_dxi}, [state&,] tuple{value, gradient}).
 #pragma once
 
@@ -168,6 +170,48 @@ struct MaterialStressFunctor {
       return tuple{zero{}, flux};
     } else {
       return tuple{zero{}, stress};
+    }
+  }
+};
+
+/// parameterized_solid_material.hpp:68-110 (ParameterizedNeoHookeanSolid):
+/// Neo-Hookean Cauchy stress with bulk and shear moduli K0 + dK, G0 + dG,
+/// where dK and dG are parameter fields passed as (value, gradient) pairs.
+struct ParameterizedNeoHookean {
+  using State = Empty;
+  double density = 1.0, K0 = 1.0, G0 = 1.0;
+  template <typename T, typename PK, typename PG>
+  SFX_HDI auto operator()(State&, const tensor<T, 3, 3>& du_dX, const PK& dK, const PG& dG) const {
+    using std::log1p;
+    const auto I = Identity<3>();
+    auto K = K0 + get<0>(dK);
+    auto G = G0 + get<0>(dG);
+    auto lambda = K - (2.0 / 3.0) * G;
+    auto B_minus_I = dot(du_dX, transpose(du_dX)) + transpose(du_dX) + du_dX;
+    auto J_minus_1 = detApIm1(du_dX);
+    auto J = J_minus_1 + 1.0;
+    return (lambda * log1p(J_minus_1) * I + G * B_minus_I) / J;
+  }
+};
+
+/// solid_mechanics.hpp:809-850 with the acceleration field and parameter
+/// fields, as SolidMechanics adds it (DependsOn<0, 1, parameters...>,
+/// :880-893): {density * acceleration, sigma . F^{-T} det F}.
+template <typename Material, bool geometric_nonlinearity = true>
+struct MultiFieldStressFunctor {
+  Material material;
+  template <typename X, typename State, typename D, typename A, typename... P>
+  SFX_HDI auto operator()(double, const X&, State& state, const D& displacement, const A& acceleration,
+                          const P&... params) const {
+    auto du_dX = get<1>(displacement);
+    auto d2u_dt2 = get<0>(acceleration);
+    auto stress = material(state, du_dX, params...);
+    if constexpr (geometric_nonlinearity) {
+      auto dx_dX = du_dX + Identity<3>();
+      auto flux = dot(stress, transpose(inv(dx_dX))) * det(dx_dX);
+      return tuple{material.density * d2u_dt2, flux};
+    } else {
+      return tuple{material.density * d2u_dt2, stress};
     }
   }
 };

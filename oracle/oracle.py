@@ -618,6 +618,81 @@ class OracleFunctional:
         return np.cumsum(row_ptr), c_of, uval
 
 
+MAT_PARAM_NEOHOOKEAN = 16
+MULTI_COMPONENTS = (3, 3, 1, 1)  # displacement, acceleration, bulk and shear modulus offsets
+
+
+class OracleMultiFunctional:
+    """Functional<test(displacement, acceleration, dK, dG)> on a structured hex
+    mesh with the parameterized Neo-Hookean integrand of SolidMechanics
+    (parameterized_solid_material.hpp:68-110 in solid_mechanics.hpp:809-850):
+    every field byNODES on the order-p node grid, per-element parameters
+    {density, K0, G0}.  residual(fields), jvp(fields, wrt, d),
+    jvp_transpose(fields, wrt, v); ``use_ref`` evaluates residual and Jv with
+    serac's own kernels (oracle/_ref)."""
+
+    def __init__(self, mesh: StructuredHexMesh, p: int, params, nthreads: int = 1):
+        self.mesh, self.p, self.nthreads = mesh, p, nthreads
+        self.Q = p + 1
+        self.nnodes = mesh.num_nodes(p)
+        self.conn = mesh.elem_nodes(p)
+        self.Xq, self.Jq = geometric_factors(mesh.elem_coords(), self.Q)
+        ne = self.conn.shape[0]
+        self.params = np.ascontiguousarray(np.broadcast_to(np.asarray(params, dtype=np.float64).reshape(-1, 3), (ne, 3)))
+        L = lib()
+        dp = _dp
+        L.orc_domain_multi.argtypes = [ctypes.c_int] * 5 + [ctypes.c_double] + [dp] * 8 + [dp, ctypes.c_int]
+        L.orc_domain_multi.restype = ctypes.c_int
+        R = ref_lib()
+        if R is not None:
+            R.ref_domain_multi.argtypes = [ctypes.c_int] * 5 + [ctypes.c_double] + [dp] * 8 + [dp]
+            R.ref_domain_multi.restype = ctypes.c_int
+
+    def _gather(self, fields):
+        return [np.ascontiguousarray(gather(np.asarray(f, dtype=np.float64), self.conn, c, self.nnodes))
+                for f, c in zip(fields, MULTI_COMPONENTS)]
+
+    def _call(self, mode, wrt, fields, dE, out_shape, use_ref=False, t=0.0):
+        E = self._gather(fields)
+        out = np.zeros(out_shape)
+        ne = self.conn.shape[0]
+        d = None if dE is None else np.ascontiguousarray(dE)
+        if use_ref:
+            rc = ref_lib().ref_domain_multi(MAT_PARAM_NEOHOOKEAN, self.p, mode, wrt, ne, t, _ptr(self.params), *map(_ptr, E),
+                                            _ptr(d), _ptr(self.Xq), _ptr(self.Jq), _ptr(out))
+        else:
+            rc = lib().orc_domain_multi(MAT_PARAM_NEOHOOKEAN, self.p, mode, wrt, ne, t, _ptr(self.params), *map(_ptr, E),
+                                        _ptr(d), _ptr(self.Xq), _ptr(self.Jq), _ptr(out), self.nthreads)
+        assert rc == 0, rc
+        return out
+
+    def element_residuals(self, fields, use_ref=False):
+        ne, nd = self.conn.shape
+        return self._call(0, 0, fields, None, (ne, 3 * nd), use_ref)
+
+    def residual(self, fields, use_ref=False):
+        return scatter_add(self.element_residuals(fields, use_ref), self.conn, 3, self.nnodes)
+
+    def jvp(self, fields, wrt, d, use_ref=False):
+        c = MULTI_COMPONENTS[wrt]
+        dE = gather(np.asarray(d, dtype=np.float64), self.conn, c, self.nnodes)
+        ne, nd = self.conn.shape
+        return scatter_add(self._call(1, wrt, fields, dE, (ne, 3 * nd), use_ref), self.conn, 3, self.nnodes)
+
+    def element_matrices(self, fields, wrt, use_ref=False):
+        """K_e with respect to argument wrt: [e][trial dof of wrt][test dof] (restatement); the
+        reference's element_gradient_kernel layout for use_ref."""
+        c = MULTI_COMPONENTS[wrt]
+        ne, nd = self.conn.shape
+        return self._call(2, wrt, fields, None, (ne, c * nd, 3 * nd), use_ref)
+
+    def jvp_transpose(self, fields, wrt, v):
+        c = MULTI_COMPONENTS[wrt]
+        vE = gather(np.asarray(v, dtype=np.float64), self.conn, 3, self.nnodes)
+        ne, nd = self.conn.shape
+        return scatter_add(self._call(3, wrt, fields, vE, (ne, c * nd)), self.conn, c, self.nnodes)
+
+
 QOI_MEASURE, QOI_POSITION, QOI_FIELD, QOI_NEOHOOKEAN_ENERGY, QOI_NORMAL_FIELD, QOI_POLY_TEST = range(6)
 
 

@@ -22,6 +22,7 @@
 #include "serac/numerics/functional/domain_integral_kernels.hpp"
 #include "serac/numerics/functional/boundary_integral_kernels.hpp"
 #include "serac/physics/materials/solid_material.hpp"
+#include "serac/physics/materials/parameterized_solid_material.hpp"
 #include "serac/physics/materials/thermal_material.hpp"
 
 using namespace serac;
@@ -641,6 +642,106 @@ void face_geometric_factors_q(int nf, const double* Xf, double* Xq, double* Jq)
 
 }  // namespace
 
+// ------------------------------------------------------ multi-field domain
+// SolidMechanics' material integrand with the acceleration and parameter
+// fields (solid_mechanics.hpp:809-850 with GeometricNonlinearities::On,
+// restated because it is nested in the physics class), evaluated by serac's
+// own evaluation_kernel_impl over four trial spaces
+// (displacement H1<p,3>, acceleration H1<p,3>, two parameter fields
+// H1<p,1>) and differentiated with respect to one of them.
+template <typename Material>
+struct MultiStressQF {
+  Material material;
+  template <typename X, typename D, typename A, typename... P>
+  auto operator()(double, X, D displacement, A acceleration, P... params) const
+  {
+    auto  du_dX   = get<1>(displacement);
+    auto  d2u_dt2 = get<0>(acceleration);
+    Empty state{};
+    auto  stress = material(state, du_dX, params...);
+    auto  dx_dX  = 0.0 * du_dX + Identity<3>();
+    dx_dX += du_dX;
+    auto flux = dot(stress, transpose(inv(dx_dX))) * det(dx_dX);
+    return serac::tuple{material.density * d2u_dt2, flux};
+  }
+};
+
+template <int p, uint32_t wrt>
+struct MultiRunner {
+  using S3 = H1<p, 3>;
+  using S1 = H1<p, 1>;
+  using E3 = finite_element<CUBE, S3>;
+  using E1 = finite_element<CUBE, S1>;
+  using QF = MultiStressQF<solid_mechanics::ParameterizedNeoHookeanSolid>;
+  static constexpr int Q  = p + 1;
+  static constexpr int nq = Q * Q * Q;
+  static constexpr int n3 = E3::ndof * 3, n1 = E1::ndof;
+  using trial_w           = std::conditional_t<(wrt < 2), S3, S1>;
+  static constexpr int nw = wrt < 2 ? n3 : n1;
+  using deriv_t           = decltype(domain_integral::get_derivative_type<int(wrt), 3, S3, S3, S1, S1>(QF{}, Nothing{}));
+
+  // mode 0 residual [3 n][e]; 1 Jv wrt; 2 K_e wrt ([e][nw][n3] as the kernel writes it)
+  static void run(int mode, int ne, double t, const double* params, const double* uE, const double* aE,
+                  const double* kE, const double* gE, const double* dE, const double* X, const double* J, double* out)
+  {
+    std::vector<deriv_t>        derivs(nq);
+    std::vector<double>         scratch(n3);
+    axom::Array<Nothing, 2>     arr;
+    axom::ArrayView<Nothing, 2> view(arr);
+    tuple<E3, E3, E1, E1>       trial_elements{};
+    int                         elements[1] = {0};
+    for (int e = 0; e < ne; e++) {
+      const double* prm = params + size_t(e) * 3;
+      QF            qf{solid_mechanics::ParameterizedNeoHookeanSolid{prm[0], prm[1], prm[2]}};
+      std::vector<const double*> inputs{uE + size_t(e) * n3, aE + size_t(e) * n3, kE + size_t(e) * n1,
+                                        gE + size_t(e) * n1};
+      const double* Xe = X + size_t(e) * 3 * nq;
+      const double* Je = J + size_t(e) * 9 * nq;
+      if (mode == 0) {
+        double* re = out + size_t(e) * n3;
+        std::memset(re, 0, sizeof(double) * n3);
+        domain_integral::evaluation_kernel_impl<NO_DIFFERENTIATION, Q, CUBE>(
+            trial_elements, E3{}, t, inputs, re, Xe, Je, qf, view, derivs.data(), elements, 1, false,
+            camp::int_seq<int, 0, 1, 2, 3>{});
+        continue;
+      }
+      std::fill(scratch.begin(), scratch.end(), 0.0);
+      domain_integral::evaluation_kernel_impl<wrt, Q, CUBE>(trial_elements, E3{}, t, inputs, scratch.data(), Xe, Je,
+                                                            qf, view, derivs.data(), elements, 1, false,
+                                                            camp::int_seq<int, 0, 1, 2, 3>{});
+      if (mode == 1) {
+        double* re = out + size_t(e) * n3;
+        std::memset(re, 0, sizeof(double) * n3);
+        domain_integral::action_of_gradient_kernel<Q, CUBE, S3, trial_w>(dE + size_t(e) * nw, re, derivs.data(),
+                                                                         elements, 1);
+      } else {
+        double* ke = out + size_t(e) * nw * n3;
+        std::memset(ke, 0, sizeof(double) * nw * n3);
+        ExecArrayView<double, 3, ExecutionSpace::CPU> kview(ke, {1, nw, n3});
+        domain_integral::element_gradient_kernel<CUBE, S3, trial_w, Q>(kview, derivs.data(), elements, 1);
+      }
+    }
+  }
+};
+
+template <int p>
+int dispatch_multi(int mode, int wrt, int ne, double t, const double* params, const double* uE, const double* aE,
+                   const double* kE, const double* gE, const double* dE, const double* X, const double* J,
+                   double* out)
+{
+  if (mode == 0) {
+    MultiRunner<p, 0>::run(0, ne, t, params, uE, aE, kE, gE, dE, X, J, out);
+    return 0;
+  }
+  switch (wrt) {
+    case 0: MultiRunner<p, 0>::run(mode, ne, t, params, uE, aE, kE, gE, dE, X, J, out); return 0;
+    case 1: MultiRunner<p, 1>::run(mode, ne, t, params, uE, aE, kE, gE, dE, X, J, out); return 0;
+    case 2: MultiRunner<p, 2>::run(mode, ne, t, params, uE, aE, kE, gE, dE, X, J, out); return 0;
+    case 3: MultiRunner<p, 3>::run(mode, ne, t, params, uE, aE, kE, gE, dE, X, J, out); return 0;
+  }
+  return -1;
+}
+
 extern "C" {
 
 // Quadrature-point positions and Jacobians of trilinear hexes.
@@ -712,3 +813,20 @@ int ref_qoi(int kind, int boundary, int p, int c, int mode, int n, double t, con
 }
 
 }  // extern "C"
+
+// The parameterized Neo-Hookean integrand over (u, a, dK, dG) (material 16):
+// mode 0 residual -> [e][3 nd]; 1 J_wrt dE -> [e][3 nd]; 2 K_e wrt -> [e][nw][3 nd]
+// as element_gradient_kernel writes it.
+extern "C" int ref_domain_multi(int mat, int p, int mode, int wrt, int ne, double t, const double* params,
+                                const double* uE, const double* aE, const double* kE, const double* gE,
+                                const double* dE, const double* Xq, const double* Jq, double* out)
+{
+  if (mat != 16) return -1;
+  try {
+    if (p == 1) return dispatch_multi<1>(mode, wrt, ne, t, params, uE, aE, kE, gE, dE, Xq, Jq, out);
+    if (p == 2) return dispatch_multi<2>(mode, wrt, ne, t, params, uE, aE, kE, gE, dE, Xq, Jq, out);
+  } catch (const std::exception&) {
+    return -2;
+  }
+  return -1;
+}

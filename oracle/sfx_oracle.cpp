@@ -893,6 +893,233 @@ int orc_domain(int mat, int p, int mode, int ne, double t, const double* params,
   return 0;
 }
 
+}  // extern "C"
+
+// ------------------------------------------------------ multi-field domain
+// ParameterizedNeoHookeanSolid (parameterized_solid_material.hpp:68-110) in
+// SolidMechanics' material integrand with an acceleration field
+// (solid_mechanics.hpp:809-850): arguments (u 3, a 3, dK 1, dG 1), per-element
+// parameters {density, K0, G0}; source = density a, flux = sigma F^{-T} det F
+// with sigma = (lambda ln J I + G (B - I)) / J, K = K0 + dK, G = G0 + dG.
+// The derivative with respect to one argument is taken by full forward-mode
+// duals over that argument's inputs (values, parent gradients).
+
+constexpr int MAT_PARAM_NEOHOOKEAN = 16;
+
+template <typename S>
+void qf_param_neohookean(const double* prm, const S (*grad_u)[3], const S* acc, const S& dK, const S& dG, S* src,
+                         S (*flux)[3]) {
+  const double rho = prm[0], K0 = prm[1], G0 = prm[2];
+  S K = dK + K0, G = dG + G0;
+  S lambda = K - G * (2.0 / 3.0);
+  M3<S> H;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) H.a[i][j] = grad_u[i][j];
+  M3<S> BmI;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      S hh = Z<S>();
+      for (int k = 0; k < 3; k++) hh = hh + H.a[i][k] * H.a[j][k];
+      BmI.a[i][j] = hh + H.a[j][i] + H.a[i][j];
+    }
+  S Jm1 = det_ap_im1(H);
+  S Jd = Jm1 + 1.0;
+  S lg = log1p(Jm1);
+  M3<S> F = H;
+  for (int i = 0; i < 3; i++) F.a[i][i] = F.a[i][i] + 1.0;
+  M3<S> Fi = inv3(F);
+  S dF = det3(F);
+  for (int i = 0; i < 3; i++) {
+    src[i] = acc[i] * rho;
+    for (int j = 0; j < 3; j++) {
+      S acc_ij = Z<S>();
+      for (int k = 0; k < 3; k++) {
+        S sig = (lambda * lg * (i == k ? 1.0 : 0.0) + G * BmI.a[i][k]) / Jd;
+        acc_ij = acc_ij + sig * Fi.a[j][k];
+      }
+      flux[i][j] = acc_ij * dF;
+    }
+  }
+}
+
+// values and physical gradients of the four arguments at point q; the
+// argument `wrt` (>= 0) carries duals of width N seeded on its inputs
+template <int N>
+struct MultiPoint {
+  Dual<N> gu[3][3], a[3], dK, dG;
+};
+
+template <int N>
+void multi_point(int wrt, const Basis3& b, int q, const double* const* fe, const M3<double>& Ji, MultiPoint<N>& mp) {
+  const int nd = b.nd;
+  const int comps[4] = {3, 3, 1, 1};
+  const double* phi = &b.phi[size_t(q * nd)];
+  const double* dphi = &b.dphi[size_t(q * nd * 3)];
+  Dual<N> val[4][3], gpar[4][3][3];
+  for (int f = 0; f < 4; f++)
+    for (int c = 0; c < comps[f]; c++) {
+      double v = 0.0, g[3] = {0, 0, 0};
+      for (int a = 0; a < nd; a++) {
+        const double x = fe[f][c * nd + a];
+        v += x * phi[a];
+        for (int j = 0; j < 3; j++) g[j] += x * dphi[a * 3 + j];
+      }
+      val[f][c] = mk<N>(v);
+      if (f == wrt) val[f][c].g[c] = 1.0;
+      for (int j = 0; j < 3; j++) {
+        gpar[f][c][j] = mk<N>(g[j]);
+        if (f == wrt) gpar[f][c][j].g[comps[f] + 3 * c + j] = 1.0;
+      }
+    }
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      Dual<N> s = mk<N>(0.0);
+      for (int k = 0; k < 3; k++) s = s + gpar[0][i][k] * Ji.a[k][j];
+      mp.gu[i][j] = s;
+    }
+  for (int i = 0; i < 3; i++) mp.a[i] = val[1][i];
+  mp.dK = val[2][0];
+  mp.dG = val[3][0];
+}
+
+// one element: mode 0 residual, 1 Jv wrt, 2 K_e wrt ([trial][test]), 3 J^T v wrt
+template <int N>
+void multi_element(int mode, int wrt, const double* prm, const Basis3& b, const double* const* fe, const double* dE,
+                   const double* Xq, const double* Jq, double* out) {
+  const int nd = b.nd, nq = b.nq;
+  const int cw = N / 4;
+  const int test_dofs = 3 * nd;
+  if (mode == 0 || mode == 1) std::memset(out, 0, sizeof(double) * size_t(test_dofs));
+  if (mode == 2) std::memset(out, 0, sizeof(double) * size_t(cw * nd) * size_t(test_dofs));
+  if (mode == 3) std::memset(out, 0, sizeof(double) * size_t(cw * nd));
+  (void)Xq;
+  for (int q = 0; q < nq; q++) {
+    M3<double> Jm;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) Jm.a[i][j] = Jq[(j * 3 + i) * nq + q];
+    M3<double> Ji = inv3(Jm);
+    const double dv = det3(Jm), w = b.w[size_t(q)];
+    MultiPoint<N> mp;
+    multi_point<N>(mode == 0 ? -1 : wrt, b, q, fe, Ji, mp);
+    Dual<N> src[3], flux[3][3];
+    qf_param_neohookean<Dual<N>>(prm, mp.gu, mp.a, mp.dK, mp.dG, src, flux);
+    // parent-space outputs [source 3][flux 3 x 3] with det J folded in: value and derivative
+    double outv[12], D[12][N];
+    for (int i = 0; i < 3; i++) {
+      Dual<N> sv = src[i] * dv;
+      outv[i] = sv.v;
+      for (int n = 0; n < N; n++) D[i][n] = sv.g[n];
+      for (int k = 0; k < 3; k++) {
+        Dual<N> acc = mk<N>(0.0);
+        for (int m = 0; m < 3; m++) acc = acc + flux[i][m] * Ji.a[k][m];
+        acc = acc * dv;
+        outv[3 + 3 * i + k] = acc.v;
+        for (int n = 0; n < N; n++) D[3 + 3 * i + k][n] = acc.g[n];
+      }
+    }
+    const double* phi = &b.phi[size_t(q * nd)];
+    const double* dphi = &b.dphi[size_t(q * nd * 3)];
+    auto integrate_test = [&](const double* o, double* dst) {
+      for (int i = 0; i < 3; i++)
+        for (int a = 0; a < nd; a++)
+          dst[i * nd + a] += w * (o[i] * phi[a] + o[3 + 3 * i] * dphi[a * 3] + o[3 + 3 * i + 1] * dphi[a * 3 + 1] +
+                                  o[3 + 3 * i + 2] * dphi[a * 3 + 2]);
+    };
+    if (mode == 0) {
+      integrate_test(outv, out);
+      continue;
+    }
+    if (mode == 1 || mode == 2) {
+      const int ncol = mode == 1 ? 1 : cw * nd;
+      for (int col = 0; col < ncol; col++) {
+        double din[N];
+        for (int i = 0; i < N; i++) din[i] = 0.0;
+        if (mode == 1) {
+          for (int c = 0; c < cw; c++)
+            for (int a = 0; a < nd; a++) {
+              const double da = dE[c * nd + a];
+              din[c] += da * phi[a];
+              for (int j = 0; j < 3; j++) din[cw + 3 * c + j] += da * dphi[a * 3 + j];
+            }
+        } else {
+          const int c = col / nd, a = col % nd;
+          din[c] = phi[a];
+          for (int j = 0; j < 3; j++) din[cw + 3 * c + j] = dphi[a * 3 + j];
+        }
+        double dout[12];
+        for (int r = 0; r < 12; r++) {
+          double acc = 0.0;
+          for (int k = 0; k < N; k++) acc += D[r][k] * din[k];
+          dout[r] = acc;
+        }
+        integrate_test(dout, mode == 1 ? out : out + size_t(col) * size_t(test_dofs));
+      }
+      continue;
+    }
+    // mode 3: v on the test side, D^T, integrated on field wrt
+    double vin[12];
+    for (int r = 0; r < 12; r++) vin[r] = 0.0;
+    for (int i = 0; i < 3; i++)
+      for (int a = 0; a < nd; a++) {
+        const double va = dE[i * nd + a];
+        vin[i] += va * phi[a];
+        for (int j = 0; j < 3; j++) vin[3 + 3 * i + j] += va * dphi[a * 3 + j];
+      }
+    for (int c = 0; c < cw; c++) {
+      double s0 = 0.0, g[3] = {0, 0, 0};
+      for (int r = 0; r < 12; r++) {
+        s0 += D[r][c] * vin[r];
+        for (int j = 0; j < 3; j++) g[j] += D[r][cw + 3 * c + j] * vin[r];
+      }
+      for (int a = 0; a < nd; a++)
+        out[c * nd + a] += w * (s0 * phi[a] + g[0] * dphi[a * 3] + g[1] * dphi[a * 3 + 1] + g[2] * dphi[a * 3 + 2]);
+    }
+  }
+}
+
+extern "C" {
+
+// Multi-field material MAT_PARAM_NEOHOOKEAN on E-vectors: uE, aE [e][3][nd],
+// kE, gE [e][1][nd]; mode 0 residual -> out [e][3][nd]; 1 Jv with respect to
+// argument wrt (dE: that field's E-vector) -> [e][3][nd]; 2 K_e with respect
+// to wrt -> [e][cw nd][3 nd]; 3 J^T v (dE: test-space E-vector) -> [e][cw][nd].
+int orc_domain_multi(int mat, int p, int mode, int wrt, int ne, double t, const double* params, const double* uE,
+                     const double* aE, const double* kE, const double* gE, const double* dE, const double* Xq,
+                     const double* Jq, double* out, int nthreads) {
+  (void)t;
+  if (mat != MAT_PARAM_NEOHOOKEAN || p < 1 || p > 3 || mode < 0 || mode > 3) return -1;
+  if (mode > 0 && (wrt < 0 || wrt > 3)) return -1;
+  Basis3 b(p);
+  const int nd = b.nd, nq = b.nq;
+  const int comps[4] = {3, 3, 1, 1};
+  const int cw = mode == 0 ? 3 : comps[wrt];
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+#endif
+  for (int e = 0; e < ne; e++) {
+    const double* fe[4] = {uE + size_t(e) * 3 * nd, aE + size_t(e) * 3 * nd, kE + size_t(e) * nd, gE + size_t(e) * nd};
+    const double* prm = params + size_t(e) * 3;
+    const double* X = Xq + size_t(e) * 3 * nq;
+    const double* J = Jq + size_t(e) * 9 * nq;
+    const double* d = nullptr;
+    double* o = nullptr;
+    if (mode == 0) o = out + size_t(e) * 3 * nd;
+    if (mode == 1) {
+      d = dE + size_t(e) * cw * nd;
+      o = out + size_t(e) * 3 * nd;
+    }
+    if (mode == 2) o = out + size_t(e) * size_t(cw * nd) * size_t(3 * nd);
+    if (mode == 3) {
+      d = dE + size_t(e) * 3 * nd;
+      o = out + size_t(e) * cw * nd;
+    }
+    if (cw == 3) multi_element<12>(mode, wrt, prm, b, fe, d, X, J, o);
+    else multi_element<4>(mode, wrt, prm, b, fe, d, X, J, o);
+  }
+  return 0;
+}
+
 // Boundary-face kernels on face E-vectors ([f][comp][node], node
 // lexicographic on the face).  params: HEAT_FLUX {q0,q1,alpha}; TRACTION
 // {t0[3], t1[3]}; PRESSURE {p}.

@@ -80,6 +80,14 @@ SIGNATURES = {
     "sfx_qdata_size": (_c.c_int, [_vp, _i64p]),
     "sfx_set_qdata": (_c.c_int, [_vp, _dp]),
     "sfx_get_qdata": (_c.c_int, [_vp, _dp]),
+    "sfx_mform_create": (_c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int, _c.POINTER(_c.c_int), _c.POINTER(_vp)]),
+    "sfx_mform_destroy": (_c.c_int, [_vp]),
+    "sfx_mform_num_nodes": (_c.c_int, [_vp, _i64p]),
+    "sfx_mform_add_domain_integral": (_c.c_int, [_vp, _c.c_int, _c.POINTER(_c.c_int), _c.c_int, _dp, _c.c_int]),
+    "sfx_mform_residual": (_c.c_int, [_vp, _c.c_double, _c.POINTER(_vp), _vp, _vp]),
+    "sfx_mform_linearize": (_c.c_int, [_vp, _c.c_double, _c.POINTER(_vp), _c.c_int, _vp]),
+    "sfx_mform_jvp": (_c.c_int, [_vp, _c.c_int, _vp, _vp, _vp]),
+    "sfx_mform_jvp_transpose": (_c.c_int, [_vp, _c.c_int, _vp, _vp, _vp]),
     # include/sfx_learned.h
     "sfx_lnet_create": (_c.c_int, [_c.c_uint64, _c.POINTER(_vp)]),
     "sfx_lnet_destroy": (_c.c_int, [_vp]),

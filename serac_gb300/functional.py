@@ -603,6 +603,109 @@ class QoI:
         return float(self.value(t, arg).item())
 
 
+PARAM_NEOHOOKEAN = 16  # multi-field: (displacement 3, acceleration 3, dK 1, dG 1), params {density, K0, G0}
+_MULTI_ARGS = {PARAM_NEOHOOKEAN: (3, 3, 1, 1)}
+
+
+class MultiGradient:
+    """dR/d(field wrt) at the linearisation point of a MultiFunctional:
+    mult(d) applies it to a direction of that field, mult_transpose(v) maps a
+    test-space vector onto the field (functional.hpp:534-708 for one argument)."""
+
+    def __init__(self, form, wrt):
+        self.form, self.wrt = form, wrt
+
+    def mult(self, d, out=None, stream=None):
+        f = self.form
+        _require(d, torch.float64, f.components[self.wrt] * f.num_nodes, "direction")
+        out = torch.empty(f.ndofs, dtype=torch.float64, device=d.device) if out is None else out
+        _lib.call("sfx_mform_jvp", f._h, self.wrt, _dptr(d), _dptr(out), _stream(stream))
+        return out
+
+    Mult = mult
+    __call__ = mult
+
+    def mult_transpose(self, v, out=None, stream=None):
+        f = self.form
+        _require(v, torch.float64, f.ndofs, "v")
+        n = f.components[self.wrt] * f.num_nodes
+        out = torch.empty(n, dtype=torch.float64, device=v.device) if out is None else out
+        _lib.call("sfx_mform_jvp_transpose", f._h, self.wrt, _dptr(v), _dptr(out), _stream(stream))
+        return out
+
+    MultTranspose = mult_transpose
+
+
+class MultiFunctional:
+    """Functional<test(trial_0, ..., trial_{n-1})> (functional.hpp:189-317) on a
+    structured hex mesh: every trial space H1 of the test space's order on the
+    same node grid, with its own component count; SolidMechanics' residual is
+    MultiFunctional(mesh, H1(p, 3), [H1(p, 3), H1(p, 3), H1(p, 1), H1(p, 1)])
+    for (displacement, acceleration, two parameter fields).
+
+        f.AddDomainIntegral(PARAM_NEOHOOKEAN, depends_on=[0, 1, 2, 3], params=[rho, K0, G0])
+        r = f(t, u, a, dK, dG)
+        r, dR_ddK = f(t, u, a, differentiate_wrt(dK), dG)
+        dR_ddK.mult(ddK); dR_ddK.mult_transpose(lam)
+    """
+
+    def __init__(self, mesh, test: H1, trials):
+        self.mesh = mesh
+        self.test = test
+        self.trials = list(trials)
+        if any(t.order != test.order for t in self.trials):
+            raise ValueError("every trial space must have the test space's order")
+        self.components = [t.components for t in self.trials]
+        comps = (ctypes.c_int * len(self.components))(*self.components)
+        h = ctypes.c_void_p()
+        _lib.call("sfx_mform_create", mesh._h, test.order, test.components, len(self.components), comps,
+                  ctypes.byref(h))
+        self._h = h
+        n = ctypes.c_int64()
+        _lib.call("sfx_mform_num_nodes", h, ctypes.byref(n))
+        self.num_nodes = n.value
+        self.ndofs = self.num_nodes * test.components
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib._LIB is not None:
+            _lib.load().sfx_mform_destroy(self._h)
+            self._h = None
+
+    def AddDomainIntegral(self, material, depends_on, params, per_element=False):
+        dep = (ctypes.c_int * len(depends_on))(*depends_on)
+        arr = np.ascontiguousarray(np.asarray(params, dtype=np.float64).ravel())
+        _lib.call("sfx_mform_add_domain_integral", self._h, int(material), dep, len(depends_on),
+                  arr.ctypes.data_as(_lib._dp), int(bool(per_element)))
+
+    def _fields(self, fields):
+        if len(fields) != len(self.components):
+            raise ValueError(f"expected {len(self.components)} fields")
+        ptrs = (ctypes.c_void_p * len(fields))()
+        for i, (u, c) in enumerate(zip(fields, self.components)):
+            _require(u, torch.float64, c * self.num_nodes, f"field {i}")
+            ptrs[i] = u.data_ptr()
+        return ptrs
+
+    def residual(self, t, fields, out=None, stream=None):
+        out = torch.empty(self.ndofs, dtype=torch.float64, device=fields[0].device) if out is None else out
+        _lib.call("sfx_mform_residual", self._h, float(t), self._fields(fields), _dptr(out), _stream(stream))
+        return out
+
+    def linearize(self, t, fields, wrt, stream=None):
+        _lib.call("sfx_mform_linearize", self._h, float(t), self._fields(fields), int(wrt), _stream(stream))
+        return MultiGradient(self, wrt)
+
+    def __call__(self, t, *args):
+        wrt = [i for i, a in enumerate(args) if isinstance(a, differentiate_wrt)]
+        fields = [a.u if isinstance(a, differentiate_wrt) else a for a in args]
+        r = self.residual(t, fields)
+        if not wrt:
+            return r
+        if len(wrt) > 1:
+            raise ValueError("differentiate with respect to one argument at a time")
+        return r, self.linearize(t, fields, wrt[0])
+
+
 def assemble(gradient):
     """CSR of dR/du at the linearisation point, (row_ptr int64, col int32,
     values float64); for a QoI gradient, the vector dQ/du."""

@@ -3,10 +3,13 @@ kernels (oracle/_ref/libserac_ref.so, built by ``make -C oracle ref`` from the
 reference sources) plus the oracle's global layer (gather / scatter / CSR).
 
 Run from the repository root where the reference tree is present:
-    make -C oracle ref && python tests/golden/make_golden.py [qoi]
+    make -C oracle ref && python tests/golden/make_golden.py [qoi|multi]
 Inputs are regenerated from the seeds stored in each file; outputs are the
 reference's numbers.  ``qoi`` writes only the quantity-of-interest fixtures
-(values and gradients from serac's QOI element kernels).
+(values and gradients from serac's QOI element kernels); ``multi`` only the
+multi-field fixtures (the parameterized Neo-Hookean integrand over
+displacement, acceleration and two parameter fields, evaluated and
+differentiated with respect to each argument by serac's own kernels).
 """
 import os
 import sys
@@ -104,9 +107,42 @@ def boundary_case(name, bmat, p, dims, sides, params, seed):
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
 
 
+MULTI_CASES = [
+    # name, order, dims, perturb, params {density, K0, G0}, seed
+    ("param_neohookean_p2", 2, (2, 2, 1), 0.1, [1.3, 5.0, 0.25], 31),
+    ("param_neohookean_p1", 1, (2, 2, 2), 0.1, [0.7, 3.0, 0.4], 32),
+]
+
+
+def multi_fields(nnodes, seed):
+    """Seeded (displacement, acceleration, bulk and shear modulus offsets)."""
+    rng = np.random.default_rng(seed)
+    return [rng.standard_normal(3 * nnodes) * 0.02, rng.standard_normal(3 * nnodes),
+            0.5 * rng.standard_normal(nnodes), 0.05 * rng.standard_normal(nnodes)]
+
+
+def multi_case(name, p, dims, perturb, params, seed):
+    m = mesh(*dims, perturb=perturb, seed=seed)
+    f = O.OracleMultiFunctional(m, p, params)
+    flds = multi_fields(f.nnodes, seed)
+    rng = np.random.default_rng(seed + 1000)
+    out = {"dims": np.array(dims), "order": p, "perturb": perturb, "params": np.array(params), "seed": seed,
+           "residual": f.residual(flds, use_ref=True)}
+    for w, c in enumerate(O.MULTI_COMPONENTS):
+        d = rng.standard_normal(c * f.nnodes)
+        out[f"dir{w}"] = d
+        out[f"jvp{w}"] = f.jvp(flds, w, d, use_ref=True)
+        out[f"ke{w}"] = f.element_matrices(flds, w, use_ref=True)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+
+
 if __name__ == "__main__":
     if O.ref_lib() is None:
         sys.exit("reference checker not built: make -C oracle ref")
+    if len(sys.argv) > 1 and sys.argv[1] == "multi":
+        for case in MULTI_CASES:
+            multi_case(*case)
+        sys.exit(print("wrote", len(MULTI_CASES), "fixtures"))
     qoi_only = len(sys.argv) > 1 and sys.argv[1] == "qoi"
     if not qoi_only:
         for case in DOMAIN_CASES:
@@ -115,4 +151,8 @@ if __name__ == "__main__":
             boundary_case(*case)
     for case in QOI_CASES:
         qoi_case(*case)
-    print("wrote", len(QOI_CASES) + (0 if qoi_only else len(DOMAIN_CASES) + len(BOUNDARY_CASES)), "fixtures")
+    if not qoi_only:
+        for case in MULTI_CASES:
+            multi_case(*case)
+    print("wrote", len(QOI_CASES) + (0 if qoi_only else len(DOMAIN_CASES) + len(BOUNDARY_CASES) + len(MULTI_CASES)),
+          "fixtures")
