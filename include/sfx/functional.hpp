@@ -19,10 +19,12 @@
 // sfx/kernels.cuh; mesh tables, geometric factors and the scatter-add come
 // from the C ABI.
 //
-// Scope of this version: one trial space equal to the test space (DependsOn<0>),
-// domain integrals over the whole mesh and boundary integrals over box sides,
-// both with user q-functions (the C ABI material library,
-// sfx_form_add_boundary_integral, serves callers without a compiler).
+// Scope of this version: Functional<H1<p,c>(H1<p,c>)> with domain integrals
+// over the whole mesh and boundary integrals over box sides or face lists;
+// Functional<H1<p,3>(H1<p,c0>, H1<p,c1>, ...)> with domain integrals under
+// DependsOn<i...> (several trial fields, derivatives and transposed actions
+// with respect to any of them); quantities of interest; all with user
+// q-functions (the C ABI material library serves callers without a compiler).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -37,6 +39,7 @@
 #include "sfx.h"
 #include "sfx/boundary.cuh"
 #include "sfx/kernels.cuh"
+#include "sfx/multifield.cuh"
 #include "sfx/qoi.cuh"
 #include "sfx/sensitivity.cuh"
 
@@ -861,6 +864,238 @@ struct QoiFaces : QoiBase {
 };
 
 }  // namespace detail
+
+namespace detail {
+
+/// out (+)= node-owner scatter of a C-component E-vector [e][C][node]
+template <int C, int NPE>
+void scatter_c(const sfx_form_layout& L, const double* E, double* out, bool accumulate, cudaStream_t s) {
+  if (L.num_nodes == 0) return;
+  kernels::scatter_kernel<C, NPE, double><<<unsigned((L.num_nodes + 255) / 256), 256, 0, s>>>(
+      E, L.node_ptr, L.node_ent, out, L.num_nodes, accumulate);
+  check_cuda(cudaGetLastError(), "multi-field scatter");
+}
+
+/// one multi-field domain integral (type-erased over the q-function and its
+/// DependsOn arguments)
+struct MultiIntegralBase {
+  virtual ~MultiIntegralBase() = default;
+  virtual void residual(const sfx_form_layout& L, double t, const double* const* fields, double* E,
+                        cudaStream_t s) = 0;
+  /// stores the derivative with respect to form field `field`; false if the integral does not read it
+  virtual bool linearize(const sfx_form_layout& L, double t, const double* const* fields, int field,
+                         cudaStream_t s) = 0;
+  virtual void jvp(const sfx_form_layout& L, const double* d, double* E, cudaStream_t s) = 0;
+  virtual void jvp_transpose(const sfx_form_layout& L, const double* v, double* E, cudaStream_t s) = 0;
+};
+
+template <int P, int CT, typename QF, typename State, typename Comps, int... I>
+struct MultiIntegral;
+
+template <int P, int CT, typename QF, typename State, int... C, int... I>
+struct MultiIntegral<P, CT, QF, State, std::integer_sequence<int, C...>, I...> : MultiIntegralBase {
+  static constexpr int NQ = (P + 1) * (P + 1) * (P + 1);
+  static constexpr int EPW = 32 / NQ;
+  static constexpr int form_comps[] = {C...};
+  using FL = kernels::FieldList<form_comps[I]...>;
+  static constexpr int args[] = {I...};
+  struct Maker {
+    QF qf;
+    static constexpr int nparams = 0;
+    SFX_HD QF operator()(const double*) const { return qf; }
+  };
+  Maker maker;
+  DeviceArray<double> D;
+  int W = -1;  // argument of the stored derivative
+
+  explicit MultiIntegral(const QF& qf) : maker{qf} {}
+
+  kernels::MultiArgs<double> margs(const sfx_form_layout& L, double t, const double* const* fields, const double* dir,
+                                   double* E) const {
+    kernels::MultiArgs<double> a{};
+    for (int k = 0; k < int(sizeof...(I)); k++) a.u[k] = fields ? fields[args[k]] : nullptr;
+    a.dir = dir;
+    a.out_e = E;
+    a.conn = L.conn;
+    a.geom = L.geom;
+    a.num_nodes = L.num_nodes;
+    a.num_elements = L.num_elements;
+    a.t = t;
+    return a;
+  }
+  template <int w>
+  void launch(const sfx_form_layout& L, double t, const double* const* fields, double* E, cudaStream_t s) {
+    if constexpr (w >= 0) {
+      constexpr int CW = FL::template comps<w>();
+      D.resize(size_t(L.num_elements) * size_t(kernels::MultiTangentShape<CT, CW>::template stride<NQ>));
+    }
+    kernels::multi_domain_kernel<P, CT, FL, w, State, Maker>
+        <<<warp_blocks(L.num_elements, EPW), 128, 0, s>>>(margs(L, t, fields, nullptr, E), maker, D.p);
+    check_cuda(cudaGetLastError(), "multi-field kernel");
+  }
+  void residual(const sfx_form_layout& L, double t, const double* const* fields, double* E, cudaStream_t s) override {
+    launch<-1>(L, t, fields, E, s);
+  }
+  bool linearize(const sfx_form_layout& L, double t, const double* const* fields, int field, cudaStream_t s) override {
+    W = -1;
+    for (int k = 0; k < int(sizeof...(I)); k++)
+      if (args[k] == field) W = k;
+    switch (W) {
+      case 0: launch<0>(L, t, fields, nullptr, s); break;
+      case 1: if constexpr (sizeof...(I) > 1) launch<1>(L, t, fields, nullptr, s); break;
+      case 2: if constexpr (sizeof...(I) > 2) launch<2>(L, t, fields, nullptr, s); break;
+      case 3: if constexpr (sizeof...(I) > 3) launch<3>(L, t, fields, nullptr, s); break;
+      default: return false;
+    }
+    return true;
+  }
+  template <bool TRANSPOSE>
+  void action(const sfx_form_layout& L, const double* dir, double* E, cudaStream_t s) {
+    auto run = [&](auto cw) {
+      constexpr int CW = decltype(cw)::value;
+      kernels::multi_jvp_kernel<P, CT, CW, TRANSPOSE>
+          <<<warp_blocks(L.num_elements, EPW), 128, 0, s>>>(margs(L, 0.0, nullptr, dir, E), D.p);
+    };
+    const int cw = comps_of(W);
+    if (cw == 1) run(std::integral_constant<int, 1>{});
+    else if (cw == 3) run(std::integral_constant<int, 3>{});
+    else throw std::runtime_error("sfx: field components must be 1 or 3");
+    check_cuda(cudaGetLastError(), "multi-field action");
+  }
+  static int comps_of(int w) {
+    constexpr int a[] = {form_comps[I]...};
+    return (w >= 0 && w < int(sizeof...(I))) ? a[w] : 0;
+  }
+  void jvp(const sfx_form_layout& L, const double* d, double* E, cudaStream_t s) override { action<false>(L, d, E, s); }
+  void jvp_transpose(const sfx_form_layout& L, const double* v, double* E, cudaStream_t s) override {
+    action<true>(L, v, E, s);
+  }
+};
+
+}  // namespace detail
+
+/// Functional<H1<p,c>(H1<p,c0>, H1<p,c1>, ...)> (functional.hpp:189-317): a
+/// residual of several trial fields, each H1 of the test space's order on the
+/// same node grid, as SolidMechanics builds test(displacement, acceleration,
+/// parameters...) (solid_mechanics.hpp:243).  AddDomainIntegral(Dimension<3>,
+/// DependsOn<i...>, qf) passes the fields i... to qf(t, tuple{X, dX/dxi},
+/// tuple{value, gradient}...) in that order; operator()(t, fields...) with one
+/// field wrapped in differentiate_wrt returns (R, dR/d(that field)).
+template <int p, int c, int c0, int c1, int... cs>
+class Functional<H1<p, c>(H1<p, c0>, H1<p, c1>, H1<p, cs>...)> {
+  static constexpr int nfields = 2 + int(sizeof...(cs));
+  using Comps = std::integer_sequence<int, c0, c1, cs...>;
+  static constexpr int comps_[] = {c0, c1, cs...};
+  static constexpr int NPE = (p + 1) * (p + 1) * (p + 1);
+
+ public:
+  /// dR/d(field wrt) at the linearisation point
+  class Gradient {
+   public:
+    explicit Gradient(Functional* f) : f_(f) {}
+    /// df = dR/d(field) d (test space)
+    void Mult(const double* d, double* df, cudaStream_t s = nullptr) const { f_->jvp(d, df, s); }
+    /// out = dR/d(field)^T v (field space)
+    void MultTranspose(const double* v, double* out, cudaStream_t s = nullptr) const { f_->jvp_transpose(v, out, s); }
+    int wrt() const { return f_->wrt_; }
+
+   private:
+    Functional* f_;
+  };
+
+  explicit Functional(const Mesh& mesh) : mesh_(mesh), grad_(this) {
+    static_assert(c == 3, "multi-field residuals have a 3-component test space");
+    sfx_form h = mesh.create(p, c, false);
+    form_ = std::shared_ptr<sfx_form_s>(h, [](sfx_form x) { sfx_form_destroy(x); });
+    check(sfx_form_get_layout(h, &L_));
+    out_.resize(size_t(L_.num_dofs));
+    int cmax = c;
+    for (int k = 0; k < nfields; k++) cmax = std::max(cmax, comps_[k]);
+    e_.resize(size_t(L_.num_elements) * NPE * size_t(cmax));
+  }
+  int64_t num_nodes() const { return L_.num_nodes; }
+
+  template <int... i, typename QF>
+  void AddDomainIntegral(Dimension<3>, DependsOn<i...>, const QF& qf) {
+    static_assert(sizeof...(i) >= 1 && sizeof...(i) <= 4, "one to four arguments");
+    static_assert(((i >= 0 && i < nfields) && ...), "DependsOn index out of range");
+    using Pos = tuple<tensor<double, 3>, tensor<double, 3, 3>>;
+    if constexpr (std::is_invocable<const QF&, double, Pos,
+                                    tuple<kernels::value_t<comps_[i], double>, kernels::grad_t<comps_[i], double>>...>::value)
+      integrals_.emplace_back(new detail::MultiIntegral<p, c, QF, Nothing, Comps, i...>(qf));
+    else
+      integrals_.emplace_back(new detail::MultiIntegral<p, c, QF, Empty, Comps, i...>(qf));
+  }
+
+  /// R(t, fields...) into a member buffer
+  template <typename... F>
+  auto operator()(double t, const F&... fields) {
+    static_assert(sizeof...(F) == size_t(nfields), "one argument per trial field");
+    const double* ptr[nfields] = {field_ptr(fields)...};
+    residual(t, ptr, out_.p, nullptr);
+    constexpr int nwrt = (0 + ... + int(std::is_same<F, differentiate_wrt_this>::value));
+    static_assert(nwrt <= 1, "differentiate with respect to one argument at a time");
+    if constexpr (nwrt == 0) {
+      return static_cast<const double*>(out_.p);
+    } else {
+      int k = 0, w = -1;
+      ((std::is_same<F, differentiate_wrt_this>::value ? (w = k, k++) : k++), ...);
+      linearize(t, ptr, w, nullptr);
+      return std::tuple<const double*, Gradient&>{out_.p, grad_};
+    }
+  }
+  void residual(double t, const double* const* fields, double* r, cudaStream_t s) {
+    if (integrals_.empty()) throw std::runtime_error("sfx: no integrals");
+    for (size_t n = 0; n < integrals_.size(); n++) {
+      integrals_[n]->residual(L_, t, fields, e_.p, s);
+      detail::scatter_c<c, NPE>(L_, e_.p, r, n > 0, s);
+    }
+  }
+  void linearize(double t, const double* const* fields, int wrt, cudaStream_t s) {
+    if (wrt < 0 || wrt >= nfields) throw std::runtime_error("sfx: no such trial field");
+    depends_.assign(integrals_.size(), false);
+    for (size_t n = 0; n < integrals_.size(); n++) depends_[n] = integrals_[n]->linearize(L_, t, fields, wrt, s);
+    wrt_ = wrt;
+  }
+
+ private:
+  friend class Gradient;
+  static const double* field_ptr(const double* u) { return u; }
+  static const double* field_ptr(const differentiate_wrt_this& w) { return w.u; }
+  void jvp(const double* d, double* df, cudaStream_t s) {
+    if (wrt_ < 0) throw std::runtime_error("sfx: linearise first");
+    bool first = true;
+    for (size_t n = 0; n < integrals_.size(); n++) {
+      if (!depends_[n]) continue;
+      integrals_[n]->jvp(L_, d, e_.p, s);
+      detail::scatter_c<c, NPE>(L_, e_.p, df, !first, s);
+      first = false;
+    }
+    if (first) check_cuda(cudaMemsetAsync(df, 0, sizeof(double) * size_t(L_.num_dofs), s), "memset");
+  }
+  void jvp_transpose(const double* v, double* out, cudaStream_t s) {
+    if (wrt_ < 0) throw std::runtime_error("sfx: linearise first");
+    const int cw = comps_[wrt_];
+    bool first = true;
+    for (size_t n = 0; n < integrals_.size(); n++) {
+      if (!depends_[n]) continue;
+      integrals_[n]->jvp_transpose(L_, v, e_.p, s);
+      if (cw == 1) detail::scatter_c<1, NPE>(L_, e_.p, out, !first, s);
+      else detail::scatter_c<3, NPE>(L_, e_.p, out, !first, s);
+      first = false;
+    }
+    if (first) check_cuda(cudaMemsetAsync(out, 0, sizeof(double) * size_t(L_.num_nodes * cw), s), "memset");
+  }
+
+  Mesh mesh_;
+  std::shared_ptr<sfx_form_s> form_;
+  sfx_form_layout L_{};
+  Gradient grad_;
+  DeviceArray<double> out_, e_;
+  std::vector<std::unique_ptr<detail::MultiIntegralBase>> integrals_;
+  std::vector<bool> depends_;
+  int wrt_ = -1;
+};
 
 /// Functional<double(H1<p,c>)>: a quantity of interest (functional_qoi.inl:58-528)
 /// over user q-functions qf(t, tuple{X, dX/dxi}, tuple{u, du/dX}) -> scalar

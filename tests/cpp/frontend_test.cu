@@ -479,3 +479,82 @@ extern "C" int frontend_shape_sensitivity(double K, double G, double pressure, i
     return -1;
   }
 }
+
+// --------------------------------------------------------------- multi-field
+namespace {
+
+// a user q-function of four fields, written out by hand: SolidMechanics'
+// material integrand with acceleration and bulk / shear modulus offset fields
+// around a compressible Neo-Hookean solid
+struct UserParamNeoHookean {
+  double rho, K0, G0;
+  template <typename X, typename U, typename A, typename PK, typename PG>
+  SFX_HD auto operator()(double, const X&, const U& displacement, const A& acceleration, const PK& dK,
+                         const PG& dG) const {
+    using namespace sfx;
+    using std::log1p;
+    auto H = get<1>(displacement);
+    auto K = K0 + get<0>(dK);
+    auto G = G0 + get<0>(dG);
+    auto lambda = K - (2.0 / 3.0) * G;
+    auto F = H + Identity<3>();
+    auto Jm1 = detApIm1(H);
+    auto J = Jm1 + 1.0;
+    auto BmI = dot(H, transpose(H)) + transpose(H) + H;
+    auto sigma = (lambda * log1p(Jm1) * Identity<3>() + G * BmI) / J;
+    return tuple{rho * get<0>(acceleration), dot(sigma, transpose(inv(F))) * J};
+  }
+};
+
+template <int P>
+int run_multi(int nx, int ny, int nz, const double* V, const double* const* host_fields, int wrt, const double* d,
+              const double* v, double rho, double K0, double G0, double* r, double* jv, double* jt) {
+  try {
+    auto mesh = sfx::Mesh::StructuredHex(nx, ny, nz, V);
+    sfx::Functional<sfx::H1<P, 3>(sfx::H1<P, 3>, sfx::H1<P, 3>, sfx::H1<P, 1>, sfx::H1<P, 1>)> f(mesh);
+    f.AddDomainIntegral(sfx::Dimension<3>{}, sfx::DependsOn<0, 1, 2, 3>{}, UserParamNeoHookean{rho, K0, G0});
+    const int64_t N = f.num_nodes();
+    const int comps[4] = {3, 3, 1, 1};
+    sfx::DeviceArray<double> fld[4], dd(size_t(comps[wrt] * N)), vv(size_t(3 * N)), out(size_t(3 * N)),
+        outw(size_t(comps[wrt] * N));
+    for (int k = 0; k < 4; k++) {
+      fld[k].resize(size_t(comps[k] * N));
+      cudaMemcpy(fld[k].p, host_fields[k], sizeof(double) * size_t(comps[k] * N), cudaMemcpyHostToDevice);
+    }
+    cudaMemcpy(dd.p, d, sizeof(double) * size_t(comps[wrt] * N), cudaMemcpyHostToDevice);
+    cudaMemcpy(vv.p, v, sizeof(double) * size_t(3 * N), cudaMemcpyHostToDevice);
+    const double* R = f(0.0, fld[0].p, fld[1].p, fld[2].p, fld[3].p);
+    cudaMemcpy(r, R, sizeof(double) * size_t(3 * N), cudaMemcpyDeviceToHost);
+    auto grad_of = [&](auto& self) -> decltype(auto) {
+      using sfx::differentiate_wrt;
+      switch (wrt) {
+        case 0: return std::get<1>(self(0.0, differentiate_wrt(fld[0].p), fld[1].p, fld[2].p, fld[3].p));
+        case 1: return std::get<1>(self(0.0, fld[0].p, differentiate_wrt(fld[1].p), fld[2].p, fld[3].p));
+        case 2: return std::get<1>(self(0.0, fld[0].p, fld[1].p, differentiate_wrt(fld[2].p), fld[3].p));
+        default: return std::get<1>(self(0.0, fld[0].p, fld[1].p, fld[2].p, differentiate_wrt(fld[3].p)));
+      }
+    };
+    auto& J = grad_of(f);
+    J.Mult(dd.p, out.p);
+    J.MultTranspose(vv.p, outw.p);
+    cudaMemcpy(jv, out.p, sizeof(double) * size_t(3 * N), cudaMemcpyDeviceToHost);
+    cudaMemcpy(jt, outw.p, sizeof(double) * size_t(comps[wrt] * N), cudaMemcpyDeviceToHost);
+    return cudaDeviceSynchronize() == cudaSuccess ? 0 : -2;
+  } catch (const std::exception&) {
+    return -1;
+  }
+}
+
+}  // namespace
+
+// Functional<H1<p,3>(H1<p,3>, H1<p,3>, H1<p,1>, H1<p,1>)> with a user
+// q-function under DependsOn<0, 1, 2, 3>: residual, and the derivative with
+// respect to field wrt applied to d and, transposed, to v (host arrays)
+extern "C" int frontend_multi(int p, int nx, int ny, int nz, const double* V, const double* u, const double* a,
+                              const double* dK, const double* dG, int wrt, const double* d, const double* v,
+                              double rho, double K0, double G0, double* r, double* jv, double* jt) {
+  const double* fields[4] = {u, a, dK, dG};
+  if (wrt < 0 || wrt > 3) return -1;
+  return p == 1 ? run_multi<1>(nx, ny, nz, V, fields, wrt, d, v, rho, K0, G0, r, jv, jt)
+                : run_multi<2>(nx, ny, nz, V, fields, wrt, d, v, rho, K0, G0, r, jv, jt);
+}

@@ -374,3 +374,31 @@ def test_user_shape_sensitivities(cuda, felib):
     q.AddBoundaryIntegral(sg.QOI_NORMAL_FIELD, sides)
     q.set_shape_displacement(torch.tensor(shape, device=cuda))
     assert rel(qsh, q.shape_gradient(0.0, torch.tensor(u, device=cuda)).cpu().numpy()) <= 1e-9
+
+
+@pytest.mark.parametrize("p", [1, 2])
+def test_user_multi_field_qfunction(cuda, felib, p):
+    """Functional<H1<p,3>(H1<p,3>, H1<p,3>, H1<p,1>, H1<p,1>)> with a user
+    q-function (displacement, acceleration, two modulus-offset fields) under
+    DependsOn<0, 1, 2, 3>: residual, derivative and transposed derivative
+    with respect to every field against the oracle, 1e-12."""
+    from tests.golden.make_golden import multi_fields
+
+    dims = (3, 2, 2)
+    V = O.box_vertices(*dims, 0.1, 9)
+    rho, K0, G0 = 1.3, 5.0, 0.25
+    orc = O.OracleMultiFunctional(O.StructuredHexMesh(*dims, V), p, [rho, K0, G0])
+    N = orc.nnodes
+    flds = multi_fields(N, 90 + p)
+    rng = np.random.default_rng(p)
+    felib.frontend_multi.restype = ctypes.c_int
+    for w, c in enumerate(O.MULTI_COMPONENTS):
+        d = rng.standard_normal(c * N)
+        v = rng.standard_normal(3 * N)
+        r, jv, jt = np.zeros(3 * N), np.zeros(3 * N), np.zeros(c * N)
+        rc = felib.frontend_multi(p, *dims, _p(V), *[_p(f) for f in flds], w, _p(d), _p(v), ctypes.c_double(rho),
+                                  ctypes.c_double(K0), ctypes.c_double(G0), _p(r), _p(jv), _p(jt))
+        assert rc == 0
+        assert rel(r, orc.residual(flds)) <= 1e-12
+        assert rel(jv, orc.jvp(flds, w, d)) <= 1e-12, w
+        assert rel(jt, orc.jvp_transpose(flds, w, v)) <= 1e-12, w
