@@ -416,12 +416,13 @@ def run_sfx(args, rank, world):
     fp64_peak = measure_fp64_peak(dev)
 
     # ---- rooflines of the dominant kernels.  Element kernel I/O: du read
-    # once (8 B per DOF), the packed symmetric tangent (45 entries per point),
-    # the element vector written (81 entries per element).
+    # once (8 B per DOF), the stored tangent (FP64: the full 81 entries per
+    # point; FP32: the packed symmetric 45), the element vector written (81
+    # entries per element).
     t_k = statistics.mean(t_elem)
-    alg64 = 8 * ndofs + 45 * 8 * nq + 8 * 81 * ne
-    roof64 = roofline_hbm("sfx::kernels::jvp_stored_kernel<2,3,false,false,double,true> (FP64, packed symmetric "
-                          "tangent)", alg64, t_k, hbm_peak, peak_src, traffic.get("jvp_stored_f64"),
+    alg64 = 8 * ndofs + 81 * 8 * nq + 8 * 81 * ne
+    roof64 = roofline_hbm("sfx::kernels::jvp_stored_kernel<2,3,false,false,double,false> (FP64, full tangent)",
+                          alg64, t_k, hbm_peak, peak_src, traffic.get("jvp_stored_f64"),
                           "FP64-pipe bound: see compute_roofline")
     # FP64 work per element: interpolate grad du (3 x 3 x 24 FMA per point),
     # the 9 x 9 tangent (81 FMA), integrate (3 x 3 x 27 FMA); idle lanes excluded
@@ -456,8 +457,8 @@ def run_sfx(args, rank, world):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded mesh perturbation, material field and linearisation state)",
-        "config": config(world, "working set (8.6 GB packed FP64 tangent) far above L2; L2 also flushed (256 MB "
-                                "write) before every timed step"),
+        "config": config(world, "working set (15.5 GB FP64 tangent) far above L2; L2 also flushed (256 MB write) "
+                                "before every timed step"),
         "e2e": {"value": ndofs * args.steps / sum(t_e2e) / 1e9, "unit": UNIT, "h2d_bytes_per_step": 8 * ndofs,
                 "d2h_bytes_per_step": 8 * ndofs},
         "roofline": roof64,
@@ -550,8 +551,8 @@ def c2_leg(dev, timed, hbm_peak, fp64_peak, K):
 NEWTON_VARIANTS = "plain_fp64,mixed,learned_mixed"
 WEIGHTS = os.path.join(ROOT, "serac_gb300", "weights", "lnet_j2_q2.npy")
 # Jacobi-Chebyshev settings (degree, interval ratio) of each method
-PLAIN_CHEBYSHEV = (16, 256.0)
-INNER_CHEBYSHEV = (10, 100.0)
+PLAIN_CHEBYSHEV = (48, 2304.0)
+INNER_CHEBYSHEV = (16, 256.0)
 
 
 def solver_options(name, **extra):
@@ -639,6 +640,41 @@ def newton_leg(steps, variants, n=NX):
     return out
 
 
+def profile_ops(n, reps):
+    """Every hot operator of the Neo-Hookean Q2 problem on an n^3 mesh (the
+    32^3 configuration: 823,875 DOF, K = 5, G = 0.25, perturbed mesh seed 1),
+    `reps` times each, for profiler captures: residual, linearisation, FP64 and
+    FP32 Jacobian actions, the transposed action and the CSR assembly."""
+    import torch
+
+    import serac_gb300 as sg
+
+    V = sg.box_vertices(n, n, n, perturb=0.1, seed=1)
+    mesh = sg.Mesh.structured_hex(n, n, n, V)
+    f = sg.Functional(mesh, sg.H1(ORDER, 3))
+    f.AddDomainIntegral(sg.NEOHOOKEAN, [5.0, 0.25])
+    X = mesh.node_coordinates(ORDER)
+    u = np.zeros((3, X.shape[0]))
+    u[2] = -0.005 * X[:, 2]
+    u += 1e-4 * np.random.default_rng(2).standard_normal(u.shape)
+    u = torch.tensor(u.ravel(), device="cuda")
+    du = torch.tensor(np.random.default_rng(0).standard_normal(f.ndofs), device="cuda")
+    r = torch.empty_like(du)
+    du32, r32 = du.float(), torch.empty(f.ndofs, dtype=torch.float32, device="cuda")
+    grad = f.linearize(0.0, u)
+    row_ptr, col = f.csr_graph()
+    vals = torch.empty(col.numel(), dtype=torch.float64, device="cuda")
+    for _ in range(reps):
+        f.residual(0.0, u, r)
+        f.linearize(0.0, u)
+        grad.mult(du, r)
+        grad.mult(du32, r32)
+        grad.mult_transpose(du, r)
+        f.assemble_values(vals)
+    torch.cuda.synchronize()
+    return {"profile_ops": n, "reps": reps, "finite": bool(torch.isfinite(vals).all())}
+
+
 def lnet_leg():
     """The learned preconditioner's kernels: one inference pass and one
     training step (batch 8) on the node grids of the 16^3 and 32^3 Q2 meshes."""
@@ -719,8 +755,9 @@ def main():
                     help="load steps of the Newton time-to-1e-8 leg (0 = skip)")
     ap.add_argument("--newton-variants", default=NEWTON_VARIANTS)
     ap.add_argument("--skip-c2", action="store_true", help="skip the 32^3 configuration leg")
-    ap.add_argument("--extra", choices=["newton", "lnet"], default=None,
-                    help="run only the Newton leg (at --extra-n hexes per direction) or the network kernels")
+    ap.add_argument("--extra", choices=["newton", "lnet", "ops"], default=None,
+                    help="run only the Newton leg (at --extra-n hexes per direction), the network kernels, or every "
+                         "hot operator of the Neo-Hookean problem at --extra-n (profiler captures)")
     ap.add_argument("--extra-n", type=int, default=NX)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -736,6 +773,8 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         if args.extra == "newton":
             rec = newton_leg(args.newton_steps, args.newton_variants.split(","), n=args.extra_n)
+        elif args.extra == "ops":
+            rec = profile_ops(args.extra_n, args.steps)
         else:
             rec = lnet_leg()
         if rank == 0:

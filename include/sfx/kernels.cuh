@@ -1035,7 +1035,11 @@ SFX_HDI float tangent_to_f32(__half x) { return __half2float(x); }
 /// element residuals of the same evaluation.  D is stored element-major,
 /// D[e * stride + (row * cols + col) * NQ + q] (stride = TangentShape::stride),
 /// in FP64 and FP32 (or FP16 with its own stride16), so that one element's
-/// tangent is one contiguous block; D32 / D16 may be null.
+/// tangent is one contiguous block; D32 / D16 may be null.  SYM: the FP32 /
+/// FP16 copies (streamed by the HBM-bound inner action) keep only the upper
+/// triangle of a symmetric block; the FP64 copy stays full, because its
+/// action is bound by the FP64 pipe, not by the bytes it reads, and the full
+/// block keeps one independent accumulation chain per output.
 template <int P, int C, typename State, typename QFMaker, bool SYM = false>
 __global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QFMaker make_qf, double* __restrict__ D64,
                                                         float* __restrict__ D32, __half* __restrict__ D16,
@@ -1140,17 +1144,20 @@ __global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QF
     using SrcT = std::decay_t<decltype(get<0>(out))>;
     using FluxT = std::decay_t<decltype(get<1>(out))>;
     constexpr bool HS = has_part<JVP, SrcT>();
-    using Shape = TangentShape<C, HS, VI, SYM>;
+    using Shape = TangentShape<C, HS, VI>;         // FP64 copy: full block
+    using ShapeP = TangentShape<C, HS, VI, SYM>;   // FP32 / FP16 copies: packed when symmetric
     int row = 0;
 #pragma unroll
     for (int ci = 0; ci < C; ci++) {
       if constexpr (HS) {
         Real v = dvol * part<JVP, Real>(source_comp<C>(get<0>(out), ci));
-        if (valid && (!Shape::packed || ci <= k)) {
-          const int64_t in_block = int64_t(Shape::index(ci, k)) * NQ + qi;
-          D64[e * Shape::template stride<NQ> + in_block] = v;
-          if (D32) D32[e * Shape::template stride<NQ> + in_block] = float(v);
-          if (D16) D16[e * Shape::template stride16<NQ> + in_block] = __float2half_rn(float(v));
+        if (valid) {
+          D64[e * Shape::template stride<NQ> + int64_t(Shape::index(ci, k)) * NQ + qi] = v;
+          if (!ShapeP::packed || ci <= k) {
+            const int64_t in_block = int64_t(ShapeP::index(ci, k)) * NQ + qi;
+            if (D32) D32[e * ShapeP::template stride<NQ> + in_block] = float(v);
+            if (D16) D16[e * ShapeP::template stride16<NQ> + in_block] = __float2half_rn(float(v));
+          }
         }
       }
     }
@@ -1171,11 +1178,14 @@ __global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QF
 #pragma unroll
       for (int kd = 0; kd < 3; kd++) {
         Real v = dvol * (fp[0] * Ji[kd][0] + fp[1] * Ji[kd][1] + fp[2] * Ji[kd][2]);
-        if (valid && (!Shape::packed || row + 3 * ci + kd <= k)) {
-          const int64_t in_block = int64_t(Shape::index(row + 3 * ci + kd, k)) * NQ + qi;
-          D64[e * Shape::template stride<NQ> + in_block] = v;
-          if (D32) D32[e * Shape::template stride<NQ> + in_block] = float(v);
-          if (D16) D16[e * Shape::template stride16<NQ> + in_block] = __float2half_rn(float(v));
+        if (valid) {
+          const int rr = row + 3 * ci + kd;
+          D64[e * Shape::template stride<NQ> + int64_t(Shape::index(rr, k)) * NQ + qi] = v;
+          if (!ShapeP::packed || rr <= k) {
+            const int64_t in_block = int64_t(ShapeP::index(rr, k)) * NQ + qi;
+            if (D32) D32[e * ShapeP::template stride<NQ> + in_block] = float(v);
+            if (D16) D16[e * ShapeP::template stride16<NQ> + in_block] = __float2half_rn(float(v));
+          }
         }
         if (!have_res) res_f[ci][kd] = dvol * (fv[0] * Ji[kd][0] + fv[1] * Ji[kd][1] + fv[2] * Ji[kd][2]);
       }

@@ -59,7 +59,7 @@ typedef struct {
   int eigen_iterations;      /* 20: Lanczos steps of the lmax estimate per linearisation (largest Ritz value
                                 plus its residual bound, from a pseudo-random start vector) */
   int mixed_precision;       /* 1: FP64 flexible GMRES outside, FP32 GMRES + FP32 Jacobi-Chebyshev inside */
-  int inner_iterations;      /* 40: FP32 inner GMRES steps per outer step */
+  int inner_iterations;      /* 40: FP32 inner GMRES steps per outer step (at most 256; one cycle, run as one CUDA graph) */
   double inner_rel_tol;      /* 1e-3 */
   int print_level;           /* 0 */
   int learned_cycle;         /* 1: SFX_PREC_LEARNED without mixed precision: 1 Chebyshev, network on

@@ -183,6 +183,84 @@ __global__ void lanczos_orth(int64_t n, T alpha, const T* __restrict__ v, T beta
   if (i < n) w[i] = w[i] - alpha * v[i] - beta * vp[i];
 }
 
+// ------------------------------------------------ device-side GMRES(m) state
+// Least-squares state of one GMRES cycle kept on the device, so that a whole
+// cycle can run as one CUDA graph without reading anything back:
+//   st[0] beta = |r0|, st[1] target, st[2] steps taken (k_done, as a double),
+//   g[m + 1], cs[m], sn[m], H column-major [m][m + 1].
+struct GmresLayout {
+  int m;
+  __host__ __device__ int64_t size() const { return 3 + (m + 1) + 2 * m + int64_t(m + 1) * m; }
+  __host__ __device__ double* g(double* st) const { return st + 3; }
+  __host__ __device__ double* cs(double* st) const { return st + 3 + (m + 1); }
+  __host__ __device__ double* sn(double* st) const { return st + 3 + (m + 1) + m; }
+  __host__ __device__ double* H(double* st) const { return st + 3 + (m + 1) + 2 * m; }
+};
+
+// beta = sqrt(*nrm2), g = beta e_1, target = max(rel beta, abs); no step taken yet
+template <typename Acc>
+__global__ void gmres_init(GmresLayout L, const Acc* __restrict__ nrm2, double rel, double abs_tol,
+                           double* __restrict__ st) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double beta = sqrt(double(*nrm2) > 0.0 ? double(*nrm2) : 0.0);
+  st[0] = beta;
+  st[1] = fmax(rel * beta, abs_tol);
+  st[2] = beta > 0.0 ? -1.0 : 0.0;  // -1: running; >= 0: steps kept
+  double* g = L.g(st);
+  for (int i = 0; i <= L.m; i++) g[i] = 0.0;
+  g[0] = beta;
+}
+
+// Arnoldi column k from the two Gram-Schmidt passes (c1, c2: k + 1
+// coefficients each) and the new vector's squared norm c3, then the Givens
+// rotations (Saad, Alg. 6.9): previous rotations applied, a new one formed,
+// the residual estimate |g[k+1]| updated.  The cycle stops counting once the
+// estimate reaches the target (or the new vector vanishes, or k = m - 1).
+template <typename Acc>
+__global__ void gmres_step(GmresLayout L, int k, const Acc* __restrict__ c1, const Acc* __restrict__ c2,
+                           const Acc* __restrict__ c3, double* __restrict__ st) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (st[2] >= 0.0) return;  // converged earlier (or zero right-hand side)
+  double* Hk = L.H(st) + int64_t(k) * (L.m + 1);
+  double* cs = L.cs(st);
+  double* sn = L.sn(st);
+  double* g = L.g(st);
+  for (int j = 0; j <= k; j++) Hk[j] = double(c1[j]) + double(c2[j]);
+  const double hn = sqrt(double(*c3) > 0.0 ? double(*c3) : 0.0);
+  Hk[k + 1] = hn;
+  for (int j = 0; j < k; j++) {
+    const double t = cs[j] * Hk[j] + sn[j] * Hk[j + 1];
+    Hk[j + 1] = -sn[j] * Hk[j] + cs[j] * Hk[j + 1];
+    Hk[j] = t;
+  }
+  double d = hypot(Hk[k], Hk[k + 1]);
+  if (d == 0.0) d = 1e-300;
+  cs[k] = Hk[k] / d;
+  sn[k] = Hk[k + 1] / d;
+  Hk[k] = d;
+  Hk[k + 1] = 0.0;
+  g[k + 1] = -sn[k] * g[k];
+  g[k] = cs[k] * g[k];
+  if (fabs(g[k + 1]) <= st[1] || hn == 0.0 || k == L.m - 1) st[2] = double(k + 1);
+}
+
+// y = H^-1 g over the steps kept (zero beyond them); adds them to *count
+template <typename T>
+__global__ void gmres_solve(GmresLayout L, double* __restrict__ st, T* __restrict__ y, int* __restrict__ count) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int k = st[2] > 0.0 ? int(st[2]) : 0;
+  const double* H = L.H(st);
+  const double* g = L.g(st);
+  double yv[256];
+  for (int i = k - 1; i >= 0; i--) {
+    double acc = g[i];
+    for (int j = i + 1; j < k; j++) acc -= H[int64_t(j) * (L.m + 1) + i] * yv[j];
+    yv[i] = acc / H[int64_t(i) * (L.m + 1) + i];
+  }
+  for (int i = 0; i < L.m; i++) y[i] = i < k ? T(yv[i]) : T(0);
+  *count += k;
+}
+
 template <typename S, typename T>
 __global__ void convert(int64_t n, const S* __restrict__ x, T* __restrict__ y) {
   int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;

@@ -175,11 +175,13 @@ struct LinearizeFn {
     using QF = decltype(Maker{}(nullptr));
     constexpr bool HS = kernels::tangent_has_source<C, State, QF>();
     constexpr bool SYM = sym_of<Maker>::value;
-    using Shape = kernels::TangentShape<C, HS, Maker::value_input, SYM>;
-    const size_t n = size_t(f.ne) * size_t(Shape::template stride<NQ>);
-    const size_t n16 = size_t(f.ne) * size_t(Shape::template stride16<NQ>);
+    using Shape = kernels::TangentShape<C, HS, Maker::value_input>;         // FP64: full
+    using ShapeP = kernels::TangentShape<C, HS, Maker::value_input, SYM>;  // FP32 / FP16: packed when symmetric
+    const size_t n64 = size_t(f.ne) * size_t(Shape::template stride<NQ>);
+    const size_t n = size_t(f.ne) * size_t(ShapeP::template stride<NQ>);
+    const size_t n16 = size_t(f.ne) * size_t(ShapeP::template stride16<NQ>);
     cudaError_t err = cudaSuccess;
-    if (di.D64.n != n) err = di.D64.alloc(n);
+    if (di.D64.n != n64) err = di.D64.alloc(n64);
     if (err == cudaSuccess) {
       if (f.tangent16) {
         di.D32.reset();
@@ -260,9 +262,11 @@ struct StoredJvpFn {
                                  : launch_tma<C, HS, Maker::value_input, false, float, SYM>(f, du, D, E, s);
       if (rc) return rc;
     } else {
+      // the FP64 copy is stored full; the FP32 copy packed when symmetric
+      constexpr bool SYMR = SYM && std::is_same<Real, float>::value;
       int64_t warps = (f.ne + EPW - 1) / EPW;
       int64_t blocks = (warps * 32 + 127) / 128;
-      kernels::jvp_stored_kernel<P, C, HS, Maker::value_input, Real, SYM>
+      kernels::jvp_stored_kernel<P, C, HS, Maker::value_input, Real, SYMR>
           <<<unsigned(blocks), 128, 0, s>>>(du, D, f.conn.p, E, f.nnodes, f.ne);
     }
     cudaError_t err = cudaGetLastError();
@@ -292,9 +296,10 @@ struct StoredJvpTransposeFn {
                                  : launch_tma<C, HS, Maker::value_input, true, float, SYM>(f, v, D, E, s);
       if (rc) return rc;
     } else {
+      constexpr bool SYMR = SYM && std::is_same<Real, float>::value;
       const int64_t warps = (f.ne + EPW - 1) / EPW;
       const int64_t blocks = (warps * 32 + 127) / 128;
-      kernels::jvp_stored_transpose_kernel<P, C, HS, Maker::value_input, Real, SYM>
+      kernels::jvp_stored_transpose_kernel<P, C, HS, Maker::value_input, Real, SYMR>
           <<<unsigned(blocks), 128, 0, s>>>(v, D, f.conn.p, E, f.nnodes, f.ne);
     }
     cudaError_t err = cudaGetLastError();
@@ -318,8 +323,8 @@ struct DiagFn {
     if (f.ne == 0) return SFX_OK;
     int64_t warps = (f.ne + EPW - 1) / EPW;
     int64_t blocks = (warps * 32 + 127) / 128;
-    kernels::diag_from_tangent_kernel<P, C, HS, Maker::value_input, sym_of<Maker>::value>
-        <<<unsigned(blocks), 128, 0, s>>>(di.D64.p, E, f.ne);
+    kernels::diag_from_tangent_kernel<P, C, HS, Maker::value_input>
+        <<<unsigned(blocks), 128, 0, s>>>(di.D64.p, E, f.ne);  // from the full FP64 copy
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("diagonal launch: ") + cudaGetErrorString(err));
     return SFX_OK;

@@ -107,15 +107,16 @@ struct sfx_solver_s {
   int grid[3] = {0, 0, 0};
   const float* features = nullptr;
   DeviceBuf<float> nn_z, nn_res, nn_x, x32b;
-  // CUDA graphs of the inner FP32 GMRES steps (one per step index), captured
-  // on a private stream and valid for one linear solve (they hold that
-  // solve's Chebyshev coefficients)
+  // the inner FP32 GMRES cycle as one CUDA graph, captured on a private
+  // stream and valid for one linear solve (it holds that solve's Chebyshev
+  // coefficients); its least-squares state and iteration count stay on the device
   cudaStream_t capture = nullptr;
-  std::vector<cudaGraphExec_t> inner_graphs;
+  cudaGraphExec_t inner_graph = nullptr;
+  DeviceBuf<double> gstate;
+  DeviceBuf<int> inner_count;
   void drop_graphs() {
-    for (auto& g : inner_graphs)
-      if (g) cudaGraphExecDestroy(g);
-    inner_graphs.assign(inner_graphs.size(), nullptr);
+    if (inner_graph) cudaGraphExecDestroy(inner_graph);
+    inner_graph = nullptr;
   }
   ~sfx_solver_s() {
     drop_graphs();
@@ -273,7 +274,7 @@ template <typename T, typename Acc>
 int gmres(sfx_solver s, int (*apply)(sfx_solver, const T*, T*, cudaStream_t),
           const std::function<int(const T*, T*, cudaStream_t)>& precond, bool flexible, const T* b, T* x, T* V,
           T* Zs, T* w, T* ydev, Reducer<T, Acc>& red, int restart, int max_iters, double rel_tol, double abs_tol,
-          int* iters_out, double* rel_out, cudaStream_t st, std::vector<cudaGraphExec_t>* graphs = nullptr) {
+          int* iters_out, double* rel_out, cudaStream_t st) {
   const int64_t n = s->n;
   cudaError_t err;
   const double nb = std::sqrt(double(red.dot(b, b, n, st, &err)));
@@ -328,28 +329,7 @@ int gmres(sfx_solver s, int (*apply)(sfx_solver, const T*, T*, cudaStream_t),
         SFX_CUDA_TRY(cudaGetLastError());
         return SFX_OK;
       };
-      if (graphs && size_t(k) < graphs->size()) {
-        cudaGraphExec_t& ge = (*graphs)[size_t(k)];
-        if (!ge) {
-          SFX_CUDA_TRY(cudaStreamBeginCapture(s->capture, cudaStreamCaptureModeThreadLocal));
-          const int rc = step(s->capture);
-          cudaGraph_t graph = nullptr;
-          const cudaError_t e = cudaStreamEndCapture(s->capture, &graph);
-          if (rc || e != cudaSuccess) {
-            if (graph) cudaGraphDestroy(graph);
-            return rc ? rc : fail(SFX_ERR_CUDA, std::string("inner step capture: ") + cudaGetErrorString(e));
-          }
-          const cudaError_t ei = cudaGraphInstantiate(&ge, graph, 0);
-          cudaGraphDestroy(graph);
-          if (ei != cudaSuccess) {
-            ge = nullptr;
-            return fail(SFX_ERR_CUDA, std::string("inner step graph: ") + cudaGetErrorString(ei));
-          }
-        }
-        SFX_CUDA_TRY(cudaGraphLaunch(ge, st));
-      } else {
-        if (int rc = step(st)) return rc;
-      }
+      if (int rc = step(st)) return rc;
       SFX_CUDA_TRY(cudaStreamSynchronize(st));
       double* Hk = &H[size_t(k) * (restart + 1)];
       for (int j = 0; j <= k; j++) Hk[j] = double(red.pinned[size_t(j)]) + double(red.pinned[size_t(k + 1 + j)]);
@@ -401,6 +381,72 @@ int gmres(sfx_solver s, int (*apply)(sfx_solver, const T*, T*, cudaStream_t),
   }
   *iters_out = total;
   *rel_out = beta / nb;
+  return SFX_OK;
+}
+
+// One cycle of the inner FP32 GMRES(m) with x0 = 0 (right-preconditioned by
+// FP32 Jacobi-Chebyshev), x = M V y: Arnoldi with classical Gram-Schmidt
+// applied twice and the Givens least-squares update on the device
+// (gmres_step), so the whole cycle - m preconditioner and operator
+// applications - is captured once per linear solve as one CUDA graph and
+// replayed by every outer step without a host round trip.  The residual
+// estimate ends the counting of steps at inner_rel_tol; the steps after it
+// still run (their coefficients are not used).
+int inner_gmres(sfx_solver s, const float* b, float* x, cudaStream_t st) {
+  const int64_t n = s->n;
+  const int m = s->opt.inner_iterations;
+  const sfx_blas::GmresLayout L{m};
+  if (!s->inner_graph) {
+    auto body = [&](cudaStream_t ss) -> int {
+      float* V = s->V32.p;
+      float* c1 = s->red32.coef.p;
+      SFX_CUDA_TRY(cudaMemcpyAsync(V, b, sizeof(float) * n, cudaMemcpyDeviceToDevice, ss));
+      s->red32.multi_dot_to(V, 0, 1, V, n, c1, ss);
+      sfx_blas::gmres_init<float><<<1, 1, 0, ss>>>(L, c1, s->opt.inner_rel_tol, 0.0, s->gstate.p);
+      sfx_blas::scale_inv_sqrt<float, float><<<nblocks(n), 256, 0, ss>>>(n, c1, V);
+      for (int k = 0; k < m; k++) {
+        float* vk = V + int64_t(k) * n;
+        float* vnext = V + int64_t(k + 1) * n;
+        float* k1 = s->red32.coef.p;
+        float* k2 = k1 + (k + 1);
+        float* k3 = k1 + 2 * (k + 1);
+        if (int rc = chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, inner_degree(s),
+                                             s->opt.chebyshev_ratio, vk, s->tmp32.p, s->cheb_d32.p, s->cheb_r32.p, ss))
+          return rc;
+        if (int rc = apply_J32(s, s->tmp32.p, vnext, ss)) return rc;
+        s->red32.multi_dot_to(V, n, k + 1, vnext, n, k1, ss);
+        sfx_blas::multi_axpy_sub<float><<<nblocks(n), 256, 0, ss>>>(n, k + 1, V, n, k1, vnext);
+        s->red32.multi_dot_to(V, n, k + 1, vnext, n, k2, ss);
+        sfx_blas::multi_axpy_sub<float><<<nblocks(n), 256, 0, ss>>>(n, k + 1, V, n, k2, vnext);
+        s->red32.multi_dot_to(vnext, 0, 1, vnext, n, k3, ss);
+        sfx_blas::scale_inv_sqrt<float, float><<<nblocks(n), 256, 0, ss>>>(n, k3, vnext);
+        sfx_blas::gmres_step<float><<<1, 1, 0, ss>>>(L, k, k1, k2, k3, s->gstate.p);
+      }
+      sfx_blas::gmres_solve<float><<<1, 1, 0, ss>>>(L, s->gstate.p, s->y32.p, s->inner_count.p);
+      SFX_CUDA_TRY(cudaMemsetAsync(s->tmp32b.p, 0, sizeof(float) * n, ss));
+      sfx_blas::multi_axpy_add<float><<<nblocks(n), 256, 0, ss>>>(n, m, V, n, s->y32.p, s->tmp32b.p);
+      if (int rc = chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, inner_degree(s),
+                                           s->opt.chebyshev_ratio, s->tmp32b.p, x, s->cheb_d32.p, s->cheb_r32.p, ss))
+        return rc;
+      SFX_CUDA_TRY(cudaGetLastError());
+      return SFX_OK;
+    };
+    SFX_CUDA_TRY(cudaStreamBeginCapture(s->capture, cudaStreamCaptureModeThreadLocal));
+    const int rc = body(s->capture);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(s->capture, &graph);
+    if (rc || e != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc ? rc : fail(SFX_ERR_CUDA, std::string("inner cycle capture: ") + cudaGetErrorString(e));
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&s->inner_graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+      s->inner_graph = nullptr;
+      return fail(SFX_ERR_CUDA, std::string("inner cycle graph: ") + cudaGetErrorString(ei));
+    }
+  }
+  SFX_CUDA_TRY(cudaGraphLaunch(s->inner_graph, st));
   return SFX_OK;
 }
 
@@ -535,15 +581,10 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
         SFX_CUDA_TRY(cudaMemsetAsync(s->x32b.p, 0, sizeof(float) * n, st));
         const float* left = nullptr;
         if (int rc = nn_step(s->b32.p, s->x32b.p, &left)) return rc;
-        SFX_CUDA_TRY(cudaMemsetAsync(s->x32.p, 0, sizeof(float) * n, st));
-        std::function<int(const float*, float*, cudaStream_t)> inner_prec = cheb32;
-        int it = 0;
-        double rel_in = 0.0;
-        if (int rc = gmres<float, float>(s, apply_J32, inner_prec, false, left, s->x32.p, s->V32.p, nullptr,
-                                         s->tmp32.p, s->y32.p, s->red32, k, k, o.inner_rel_tol, 0.0, &it, &rel_in, st,
-                                         &s->inner_graphs))
-          return rc;
-        s->stats.inner_iterations += it;
+        // the captured inner cycle reads its right-hand side from b32
+        if (left != s->b32.p)
+          SFX_CUDA_TRY(cudaMemcpyAsync(s->b32.p, left, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+        if (int rc = inner_gmres(s, s->b32.p, s->x32.p, st)) return rc;
         sfx_blas::axpby<float><<<nblocks(n), 256, 0, st>>>(n, 1.0f, s->x32.p, 1.0f, s->x32b.p);
         sfx_blas::convert<float, double><<<nblocks(n), 256, 0, st>>>(n, s->x32b.p, z);
         return SFX_OK;
@@ -582,19 +623,7 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
       return rc;
     prec = [=](const double* v, double* z, cudaStream_t) -> int {
       sfx_blas::convert<double, float><<<nblocks(n), 256, 0, st>>>(n, v, s->b32.p);
-      SFX_CUDA_TRY(cudaMemsetAsync(s->x32.p, 0, sizeof(float) * n, st));
-      std::function<int(const float*, float*, cudaStream_t)> inner_prec = [=](const float* a, float* b,
-                                                                               cudaStream_t ss) -> int {
-        return chebyshev<float, float>(s, apply_J32, s->diag32.p, s->lmax32, inner_degree(s), s->opt.chebyshev_ratio, a,
-                                       b, s->cheb_d32.p, s->cheb_r32.p, ss);
-      };
-      int it = 0;
-      double rel_in = 0.0;
-      if (int rc = gmres<float, float>(s, apply_J32, inner_prec, false, s->b32.p, s->x32.p, s->V32.p, nullptr,
-                                       s->tmp32.p, s->y32.p, s->red32, k, k, o.inner_rel_tol, 0.0, &it, &rel_in, st,
-                                       &s->inner_graphs))
-        return rc;
-      s->stats.inner_iterations += it;
+      if (int rc = inner_gmres(s, s->b32.p, s->x32.p, st)) return rc;
       sfx_blas::convert<float, double><<<nblocks(n), 256, 0, st>>>(n, s->x32.p, z);
       return SFX_OK;
     };
@@ -609,11 +638,18 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
     };
   }
   SFX_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
+  SFX_CUDA_TRY(cudaMemsetAsync(s->inner_count.p, 0, sizeof(int), st));
   const bool flexible = o.mixed_precision != 0 || o.krylov == SFX_KRYLOV_FGMRES || o.precond == SFX_PREC_LEARNED;
   int rc = gmres<double, double>(s, apply_J64, prec, flexible, rhs, x, s->V.p, s->Z.p, s->tmp.p, s->y.p, s->red, m,
                                  o.max_krylov_iterations, o.krylov_rel_tol, o.krylov_abs_tol, &iters, &rel, st);
   s->stats.krylov_iterations += iters;
   s->stats.last_krylov_rel = rel;
+  if (rc == SFX_OK && o.mixed_precision) {
+    int inner = 0;  // inner steps counted on the device by the captured cycles
+    SFX_CUDA_TRY(cudaMemcpyAsync(&inner, s->inner_count.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SFX_CUDA_TRY(cudaStreamSynchronize(st));
+    s->stats.inner_iterations += inner;
+  }
   if (rc == SFX_OK && s->form->wait_error.raised()) {
     // a bounded wait inside a replayed FP32 action expired
     s->form->wait_error.clear();
@@ -659,6 +695,7 @@ int sfx_solver_create(sfx_form form, const sfx_solver_options* opt, sfx_solver* 
   if (opt) s->opt = *opt;
   else sfx_solver_default_options(&s->opt);
   if (s->opt.restart < 1 || s->opt.chebyshev_degree < 1 || s->opt.inner_iterations < 1 ||
+      s->opt.inner_iterations > 256 ||
       s->opt.inner_chebyshev_degree < 0 || s->opt.eigen_iterations < 2 || !(s->opt.chebyshev_ratio > 1.0) ||
       s->opt.learned_cycle < 0 || s->opt.learned_cycle > 1) {
     delete s;
@@ -677,7 +714,11 @@ int sfx_solver_create(sfx_form form, const sfx_solver_options* opt, sfx_solver* 
     delete s;
     return fail(SFX_ERR_CUDA, "capture stream creation failed");
   }
-  s->inner_graphs.assign(size_t(s->opt.inner_iterations), nullptr);
+  if (s->gstate.alloc(size_t(sfx_blas::GmresLayout{s->opt.inner_iterations}.size())) != cudaSuccess ||
+      s->inner_count.alloc(1) != cudaSuccess || cudaMemset(s->inner_count.p, 0, sizeof(int)) != cudaSuccess) {
+    delete s;
+    return fail(SFX_ERR_NOMEM, "solver workspace allocation failed");
+  }
   *out = s;
   return SFX_OK;
 }
@@ -718,7 +759,7 @@ int sfx_solver_solve_adjoint(sfx_solver s, double t, const double* u_lin, const 
   s->transpose = true;
   const int rc = linear_solve(s, s->r.p, x, st);
   s->transpose = false;
-  s->drop_graphs();  // the captured inner steps apply J^T
+  s->drop_graphs();  // the captured inner cycle applies J^T
   return rc;
 }
 
