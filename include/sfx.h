@@ -229,6 +229,12 @@ int sfx_jvp_transpose_f32(sfx_form form, const float* v, float* dr, void* stream
  * that nothing completes; returns SFX_ERR_TIMEOUT when the bound worked, as it
  * must, and leaves the context usable. */
 int sfx_selftest_bounded_wait(unsigned polls);
+/* Self-test of the tensor-core (tcgen05) path used by the learned
+ * preconditioner's convolutions: D = A B^T on one 128-row tile, A [128][K] and
+ * B [N][K] BF16 row-major, D [128][N] FP32 (device pointers), N in
+ * {16, 32, 48, 64, 128}, K a multiple of 16 up to 256.  No counterpart in
+ * serac. */
+int sfx_selftest_umma_tile(const void* A, const void* B, int N, int K, float* D);
 
 /* Sparsity of dR/du: every (test vdof, trial vdof) pair of every element,
  * rows sorted, columns sorted within a row (dof_numbering.hpp:290-351).

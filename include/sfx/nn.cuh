@@ -1,7 +1,9 @@
 // sfx — kernels of the learned multilevel preconditioner: 3x3x3 convolutions
 // on node grids (channels-last BF16 activations, FP32 accumulation on the
-// tensor cores through mma.sync m16n8k16), grid transfer between levels, and
-// the backward passes used to train the network.
+// 5th-generation tensor cores through tcgen05.mma with tensor-memory
+// accumulators for the forward and data-gradient convolutions, mma.sync
+// m16n8k16 for the weight gradient), grid transfer between levels, and the
+// backward passes used to train the network.
 //
 // A volume is an nx x ny x nz node grid with C channels (C a multiple of 16),
 // stored [z][y][x][C].  Convolutions use zero padding, stride 1:
@@ -14,6 +16,8 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+
+#include "sfx/umma.cuh"
 
 namespace sfx {
 namespace nn {
@@ -38,146 +42,157 @@ __device__ inline void mma_bf16_16816(float (&d)[4], const uint32_t (&a)[4], con
 
 enum Act : int { ACT_NONE = 0, ACT_RELU = 1 };
 
-/// Shared-memory layout of conv3_fwd for CIN input and COUT output channels:
-/// the input rows of the block's 64 output nodes for each of the 9 (dy, dz)
-/// neighbour offsets (66 consecutive nodes each, a row stride of CIN + 8 bf16)
-/// and the whole weight tensor (per output channel 27 * CIN + 8 bf16).  The
-/// padding makes the mma fragment loads of 8 rows x 4 lanes hit 32 banks.
+/// Shared-memory layout of conv3_fwd_umma: every weight as K-major core
+/// matrices, one B chunk of COUT rows x 16 input channels per (tap, channel
+/// chunk), and two A buffers of 128 nodes x CIN for the tap being computed
+/// and the next one.
 template <int CIN, int COUT>
-struct ConvSmem {
-  static constexpr int NODES = 64;         // output nodes per block (4 warps x 16)
-  static constexpr int SEG = NODES + 2;    // staged source nodes per (dy, dz) offset
-  static constexpr int RS = CIN + 8;       // input row stride (bf16)
-  static constexpr int WS = 27 * CIN + 8;  // weight row stride per output channel (bf16)
-  static constexpr size_t x_elems = size_t(9) * SEG * RS;
-  static constexpr size_t w_elems = size_t(COUT) * WS;
-  static constexpr size_t bytes = (x_elems + w_elems) * 2;
+struct UmmaConvSmem {
+  static constexpr int KC = CIN / 16;                      // K-steps per tap
+  static constexpr uint32_t B_CHUNK = uint32_t(COUT) * 32;  // bytes per (tap, K-step)
+  static constexpr uint32_t A_CHUNK = 128 * 32;
+  static constexpr uint32_t A_BUF = A_CHUNK * KC;
+  static constexpr size_t w_bytes = size_t(27) * KC * B_CHUNK;
+  static constexpr size_t bytes = w_bytes + 2 * size_t(A_BUF);
+  static constexpr uint32_t NCOLS = COUT <= 32 ? 32 : 64;  // TMEM columns of the FP32 accumulator
 };
 
-/// Forward 3x3x3 convolution as an implicit GEMM on mma.sync m16n8k16 (BF16 in,
-/// FP32 accumulate).  A block of 4 warps computes 64 consecutive output nodes
-/// (16 per warp) for all COUT channels; the input rows they touch and the
-/// weights are first staged in shared memory (16-byte vector loads), then the
-/// K loop runs over the 27 taps and the input channels in chunks of 16.
-/// x: [node][CIN] bf16, W: [COUT][27][CIN] bf16, bias: [COUT] f32 (may be
-/// null), y: [node][COUT] bf16.  If `y_f32` is non-null the pre-cast FP32
-/// result is written there instead.  blockIdx.y selects the sample of a batch
-/// (volumes stored one after another).  Dynamic shared memory:
-/// ConvSmem<CIN, COUT>::bytes.
+/// Forward 3x3x3 convolution on the 5th-generation tensor cores: an implicit
+/// GEMM with the 128 output nodes of the block as M, the output channels as
+/// N and K = 27 taps x CIN, accumulated in tensor memory (FP32) by tcgen05.mma
+/// kind::f16 (BF16 operands in shared memory).  The block stages all weights
+/// once; for each tap its 128 threads gather the shifted input rows (16-byte
+/// loads, zero outside the grid) into one of two A buffers while the MMAs of
+/// the previous tap run; one thread issues the tap's CIN / 16 MMAs and commits
+/// them to that buffer's mbarrier, which the gather two taps later waits on.
+/// The epilogue reads the accumulator with tcgen05.ld (warp w: rows
+/// 32w..32w+31), adds the bias, applies the activation and stores BF16 (or
+/// FP32 into y_f32).  x: [node][CIN] bf16, W: [COUT][27][CIN] bf16, bias:
+/// [COUT] f32 (may be null), y: [node][COUT] bf16; blockIdx.y selects the
+/// sample of a batch (volumes stored one after another).  Every wait is
+/// bounded: on a timeout the block sets *err, waits (bounded) for its issued
+/// MMAs and frees its tensor memory.
 template <int CIN, int COUT, int ACT>
-__global__ void __launch_bounds__(128) conv3_fwd(Grid3 g, const __nv_bfloat16* __restrict__ x,
-                                                 const __nv_bfloat16* __restrict__ W, const float* __restrict__ bias,
-                                                 __nv_bfloat16* __restrict__ y, float* __restrict__ y_f32) {
-  static_assert(CIN % 16 == 0 && COUT % 8 == 0, "channel counts");
-  using L = ConvSmem<CIN, COUT>;
-  constexpr int NT = COUT / 8;
-  extern __shared__ __align__(16) unsigned char sfx_conv_smem[];
-  __nv_bfloat16* sx = reinterpret_cast<__nv_bfloat16*>(sfx_conv_smem);
-  __nv_bfloat16* sw = sx + L::x_elems;
+__global__ void __launch_bounds__(128, 1) conv3_fwd_umma(Grid3 g, const __nv_bfloat16* __restrict__ x,
+                                                      const __nv_bfloat16* __restrict__ W,
+                                                      const float* __restrict__ bias, __nv_bfloat16* __restrict__ y,
+                                                      float* __restrict__ y_f32, int* __restrict__ err) {
+  static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 64, "channel counts");
+  using L = UmmaConvSmem<CIN, COUT>;
+  extern __shared__ __align__(128) unsigned char sfx_conv_smem[];
+  unsigned char* sw = sfx_conv_smem;
+  unsigned char* sa = sfx_conv_smem + L::w_bytes;
+  __shared__ uint64_t bars[2];
+  __shared__ uint32_t tmem_base;
+  __shared__ int node_xyz[128][3];
   const int64_t N = g.nodes();
-  const int64_t n0 = int64_t(blockIdx.x) * L::NODES;
+  const int64_t n0 = int64_t(blockIdx.x) * 128;
   x += int64_t(blockIdx.y) * N * CIN;
   if (y) y += int64_t(blockIdx.y) * N * COUT;
   if (y_f32) y_f32 += int64_t(blockIdx.y) * N * COUT;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-  // stage the weights: W[co][tap][ci] -> sw[co * WS + tap * CIN + ci]
+  // weights: W[co][tap][ci] -> chunk (tap, ci / 16), core-matrix slot of (co, ci % 16)
   {
     constexpr int VPR = 27 * CIN / 8;  // 16-byte vectors per output channel
     const uint4* src = reinterpret_cast<const uint4*>(W);
     for (int i = threadIdx.x; i < COUT * VPR; i += blockDim.x) {
       const int co = i / VPR, v = i % VPR;
-      *reinterpret_cast<uint4*>(sw + co * L::WS + v * 8) = src[i];
+      const int tap = v / (CIN / 8), g8 = v % (CIN / 8);
+      const uint32_t off = uint32_t(tap * L::KC + g8 / 2) * L::B_CHUNK + umma::kmajor_offset(co, (g8 & 1) * 8, 128, 256);
+      *reinterpret_cast<uint4*>(sw + off) = src[i];
     }
   }
-  // stage the input rows: segment k = (dz + 1) * 3 + (dy + 1) holds nodes
-  // n0 - 1 + dy nx + dz nx ny + [0, SEG) (zeros outside [0, N))
   {
-    constexpr int VPN = CIN / 8;  // 16-byte vectors per node
-    const uint4* src = reinterpret_cast<const uint4*>(x);
-    const int64_t plane = int64_t(g.nx) * g.ny;
-    for (int i = threadIdx.x; i < 9 * L::SEG * VPN; i += blockDim.x) {
-      const int k = i / (L::SEG * VPN), rem = i % (L::SEG * VPN);
-      const int j = rem / VPN, v = rem % VPN;
-      const int dy = k % 3 - 1, dz = k / 3 - 1;
-      const int64_t node = n0 - 1 + dy * int64_t(g.nx) + dz * plane + j;
-      uint4 val = make_uint4(0u, 0u, 0u, 0u);
-      if (node >= 0 && node < N) val = src[node * VPN + v];
-      *reinterpret_cast<uint4*>(sx + (size_t(k) * L::SEG + j) * L::RS + v * 8) = val;
-    }
+    const int r = threadIdx.x;  // one row per thread
+    const int64_t n = n0 + r;
+    const int64_t nn = n < N ? n : 0;
+    node_xyz[r][0] = n < N ? int(nn % g.nx) : -1000000;  // rows past the grid read zeros
+    node_xyz[r][1] = int((nn / g.nx) % g.ny);
+    node_xyz[r][2] = int(nn / (int64_t(g.nx) * g.ny));
   }
+  if (threadIdx.x == 0) {
+    bulk::mbar_init(&bars[0], 1);
+    bulk::mbar_init(&bars[1], 1);
+    bulk::fence_mbar_init();
+  }
+  if (warp == 0) {
+    umma::tmem_alloc(&tmem_base, L::NCOLS);
+    umma::tmem_relinquish();
+  }
+  umma::fence_before_sync();
   __syncthreads();
-
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int gid = lane >> 2, tig = lane & 3;
-  // the two rows (output nodes) this lane feeds into the A fragment
-  int ln[2] = {warp * 16 + gid, warp * 16 + gid + 8};  // local index in [0, 64)
-  int rx[2], ry[2], rz[2];
-  bool rv[2];
-#pragma unroll
-  for (int h = 0; h < 2; h++) {
-    const int64_t n = n0 + ln[h];
-    rv[h] = n < N;
-    const int64_t nn = rv[h] ? n : 0;
-    rx[h] = int(nn % g.nx);
-    ry[h] = int((nn / g.nx) % g.ny);
-    rz[h] = int(nn / (int64_t(g.nx) * g.ny));
-  }
-  float acc[NT][4];
-#pragma unroll
-  for (int j = 0; j < NT; j++)
-#pragma unroll
-    for (int k = 0; k < 4; k++) acc[j][k] = 0.f;
-
-#pragma unroll 1
-  for (int tap = 0; tap < 27; tap++) {
+  umma::fence_after_sync();
+  const uint32_t tmem = tmem_base;
+  constexpr uint32_t idesc = umma::idesc_bf16_f32(128, COUT);
+  constexpr int GPN = CIN / 8;  // 16-byte groups per node
+  const uint4* src = reinterpret_cast<const uint4*>(x);
+  bool ok = true;
+  for (int tap = 0; tap < 27 && ok; tap++) {
+    const int buf = tap & 1;
+    if (tap >= 2) ok = __syncthreads_and(bulk::mbar_wait(&bars[buf], uint32_t((tap - 2) >> 1) & 1u));
+    if (!ok) break;
+    umma::fence_after_sync();
     const int dx = tap % 3 - 1, dy = (tap / 3) % 3 - 1, dz = tap / 9 - 1;
-    const int seg = (dz + 1) * 3 + (dy + 1);
-    const __nv_bfloat16* rowp[2];
-    bool sv[2];
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const int xx = rx[h] + dx, yy = ry[h] + dy, zz = rz[h] + dz;
-      sv[h] = rv[h] && xx >= 0 && xx < g.nx && yy >= 0 && yy < g.ny && zz >= 0 && zz < g.nz;
-      rowp[h] = sx + (size_t(seg) * L::SEG + (ln[h] + 1 + dx)) * L::RS;
+    unsigned char* A = sa + size_t(buf) * L::A_BUF;
+    for (int i = threadIdx.x; i < 128 * GPN; i += blockDim.x) {
+      const int r = i / GPN, g8 = i % GPN;
+      const int xx = node_xyz[r][0] + dx, yy = node_xyz[r][1] + dy, zz = node_xyz[r][2] + dz;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (xx >= 0 && xx < g.nx && yy >= 0 && yy < g.ny && zz >= 0 && zz < g.nz)
+        v = src[((int64_t(zz) * g.ny + yy) * g.nx + xx) * GPN + g8];
+      *reinterpret_cast<uint4*>(A + uint32_t(g8 / 2) * L::A_CHUNK + umma::kmajor_offset(r, (g8 & 1) * 8, 128, 256)) = v;
     }
+    bulk::fence_proxy_async_smem();  // the gathered rows are read by the tensor core
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    if (threadIdx.x == 0) {
 #pragma unroll
-    for (int kc = 0; kc < CIN / 16; kc++) {
-      const int c0 = kc * 16 + tig * 2;
-      uint32_t a[4];
-      a[0] = sv[0] ? *reinterpret_cast<const uint32_t*>(rowp[0] + c0) : 0u;
-      a[1] = sv[1] ? *reinterpret_cast<const uint32_t*>(rowp[1] + c0) : 0u;
-      a[2] = sv[0] ? *reinterpret_cast<const uint32_t*>(rowp[0] + c0 + 8) : 0u;
-      a[3] = sv[1] ? *reinterpret_cast<const uint32_t*>(rowp[1] + c0 + 8) : 0u;
-#pragma unroll
-      for (int j = 0; j < NT; j++) {
-        const __nv_bfloat16* wr = sw + (j * 8 + gid) * L::WS + tap * CIN + c0;
-        uint32_t b[2] = {*reinterpret_cast<const uint32_t*>(wr), *reinterpret_cast<const uint32_t*>(wr + 8)};
-        mma_bf16_16816(acc[j], a, b);
-      }
+      for (int kc = 0; kc < L::KC; kc++)
+        umma::mma_bf16(tmem, umma::smem_desc(A + uint32_t(kc) * L::A_CHUNK, 128, 256),
+                       umma::smem_desc(sw + uint32_t(tap * L::KC + kc) * L::B_CHUNK, 128, 256), idesc,
+                       tap > 0 || kc > 0);
+      umma::commit(&bars[buf]);
     }
   }
-  // epilogue: rows gid / gid+8, columns j*8 + tig*2 + {0,1}
+  // the last commit (tap 26, buffer 0, its 14th completion) covers every MMA
+  if (ok) ok = __syncthreads_and(bulk::mbar_wait(&bars[0], 1u));
+  umma::fence_after_sync();
+  if (ok) {
+    const int r = 32 * warp + lane;
+    const int64_t n = n0 + r;
 #pragma unroll
-  for (int j = 0; j < NT; j++) {
-    const int co = j * 8 + tig * 2;
-    const float b0 = bias ? bias[co] : 0.f, b1 = bias ? bias[co + 1] : 0.f;
+    for (int c = 0; c < COUT; c += 8) {
+      float v[8];
+      umma::ld_x8(tmem + (uint32_t(32 * warp) << 16) + uint32_t(c), v);
+      if (n < N) {
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-      if (!rv[h]) continue;
-      const int64_t n = n0 + ln[h];
-      float v0 = acc[j][2 * h] + b0, v1 = acc[j][2 * h + 1] + b1;
-      if (ACT == ACT_RELU) {
-        v0 = v0 > 0.f ? v0 : 0.f;
-        v1 = v1 > 0.f ? v1 : 0.f;
-      }
-      if (y_f32) {
-        y_f32[n * COUT + co] = v0;
-        y_f32[n * COUT + co + 1] = v1;
-      } else {
-        reinterpret_cast<uint32_t*>(y)[(n * COUT + co) >> 1] = pack_bf16x2(v0, v1);
+        for (int i = 0; i < 8; i++) {
+          float t = v[i] + (bias ? bias[c + i] : 0.f);
+          if (ACT == ACT_RELU) t = t > 0.f ? t : 0.f;
+          v[i] = t;
+        }
+        if (y_f32) {
+#pragma unroll
+          for (int i = 0; i < 8; i++) y_f32[n * COUT + c + i] = v[i];
+        } else {
+          uint4 pk = make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]),
+                                pack_bf16x2(v[6], v[7]));
+          *reinterpret_cast<uint4*>(y + n * COUT + c) = pk;
+        }
       }
     }
+  } else {
+    if (threadIdx.x == 0) atomicExch(err, 1);
+    // the MMAs already issued (bounded) before the tensor memory is released
+    (void)bulk::mbar_wait(&bars[0], 0u);
+    (void)bulk::mbar_wait(&bars[1], 0u);
   }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  if (warp == 0) umma::tmem_dealloc(tmem, L::NCOLS);
 }
 
 /// Weights of the data-gradient convolution: Wt[ci][tap][co] = W[co][26 - tap][ci].

@@ -66,6 +66,7 @@ SIGNATURES = {
     "sfx_jvp_element": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "sfx_jvp_element_f32": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "sfx_selftest_bounded_wait": (_c.c_int, [_c.c_uint]),
+    "sfx_selftest_umma_tile": (_c.c_int, [_vp, _vp, _c.c_int, _c.c_int, _vp]),
     "sfx_csr_nnz": (_c.c_int, [_vp, _i64p]),
     "sfx_csr_graph": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "sfx_assemble_csr": (_c.c_int, [_vp, _vp, _vp]),

@@ -170,26 +170,28 @@ __global__ void adam(float* __restrict__ p, const float* __restrict__ g, float* 
 
 // launch one staged convolution (the dynamic shared-memory limit is raised
 // once per instantiation)
+// the tensor-core (tcgen05) convolution: one block per 128 output nodes and sample
 template <int CI, int CO, int ACT>
-void launch_conv(Grid3 g, int batch, const bf16* x, const bf16* W, const float* b, bf16* y, float* y32,
+void launch_conv(Grid3 g, int batch, const bf16* x, const bf16* W, const float* b, bf16* y, float* y32, int* err,
                  cudaStream_t s) {
-  using L = sfx::nn::ConvSmem<CI, CO>;
+  using L = sfx::nn::UmmaConvSmem<CI, CO>;
   static bool configured = false;
   if (!configured) {
-    cudaFuncSetAttribute(sfx::nn::conv3_fwd<CI, CO, ACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(L::bytes));
+    cudaFuncSetAttribute(sfx::nn::conv3_fwd_umma<CI, CO, ACT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(L::bytes));
     configured = true;
   }
-  const dim3 blocks(unsigned((g.nodes() + L::NODES - 1) / L::NODES), unsigned(batch));
-  sfx::nn::conv3_fwd<CI, CO, ACT><<<blocks, 128, L::bytes, s>>>(g, x, W, b, y, y32);
+  const dim3 blocks(unsigned((g.nodes() + 127) / 128), unsigned(batch));
+  sfx::nn::conv3_fwd_umma<CI, CO, ACT><<<blocks, 128, L::bytes, s>>>(g, x, W, b, y, y32, err);
 }
 
 void conv_fwd(int ci, int co, bool relu, Grid3 g, int batch, const bf16* x, const bf16* W, const float* b, bf16* y,
-              float* y32, cudaStream_t s) {
-#define SFX_CONV(CI, CO)                                                           \
-  if (ci == CI && co == CO) {                                                      \
-    if (relu) launch_conv<CI, CO, sfx::nn::ACT_RELU>(g, batch, x, W, b, y, y32, s); \
-    else launch_conv<CI, CO, sfx::nn::ACT_NONE>(g, batch, x, W, b, y, y32, s);      \
-    return;                                                                        \
+              float* y32, int* err, cudaStream_t s) {
+#define SFX_CONV(CI, CO)                                                                \
+  if (ci == CI && co == CO) {                                                           \
+    if (relu) launch_conv<CI, CO, sfx::nn::ACT_RELU>(g, batch, x, W, b, y, y32, err, s); \
+    else launch_conv<CI, CO, sfx::nn::ACT_NONE>(g, batch, x, W, b, y, y32, err, s);      \
+    return;                                                                             \
   }
   SFX_PAIRS(SFX_CONV)
 #undef SFX_CONV
@@ -248,6 +250,7 @@ struct Work {
 }  // namespace
 
 struct sfx_lnet_s {
+  sfx_impl::MappedFlag wait_error;  // set by a convolution whose bounded wait expired
   Conv layers[NLAYERS];
   int64_t nparams = 0;
   DeviceBuf<float> P, G, M, V;  // master parameters, gradient, Adam moments
@@ -330,30 +333,30 @@ void input_scale(Work* w, int B, const float* r, cudaStream_t s) {
 void forward(sfx_lnet net, Work* w, int B, cudaStream_t s) {
   const Grid3* g = w->g;
   const int64_t N0 = g[0].nodes(), N1 = g[1].nodes(), N2 = g[2].nodes(), N3 = g[3].nodes();
-  conv_fwd(16, 16, true, g[0], B, w->X0.p, net->W16[A0].p, bias_of(net, A0), w->A0b.p, nullptr, s);
-  conv_fwd(16, 16, true, g[0], B, w->A0b.p, net->W16[B0L].p, bias_of(net, B0L), w->B0b.p, nullptr, s);
+  conv_fwd(16, 16, true, g[0], B, w->X0.p, net->W16[A0].p, bias_of(net, A0), w->A0b.p, nullptr, net->wait_error.dev, s);
+  conv_fwd(16, 16, true, g[0], B, w->A0b.p, net->W16[B0L].p, bias_of(net, B0L), w->B0b.p, nullptr, net->wait_error.dev, s);
   sfx::nn::restrict_to<bf16, bf16><<<grid2(N1 * 16, B), 256, 0, s>>>(g[0], g[1], 16, w->B0b.p, w->C1.p, 0.125f);
-  conv_fwd(16, 32, true, g[1], B, w->C1.p, net->W16[A1].p, bias_of(net, A1), w->A1b.p, nullptr, s);
-  conv_fwd(32, 32, true, g[1], B, w->A1b.p, net->W16[B1L].p, bias_of(net, B1L), w->B1b.p, nullptr, s);
+  conv_fwd(16, 32, true, g[1], B, w->C1.p, net->W16[A1].p, bias_of(net, A1), w->A1b.p, nullptr, net->wait_error.dev, s);
+  conv_fwd(32, 32, true, g[1], B, w->A1b.p, net->W16[B1L].p, bias_of(net, B1L), w->B1b.p, nullptr, net->wait_error.dev, s);
   sfx::nn::restrict_to<bf16, bf16><<<grid2(N2 * 32, B), 256, 0, s>>>(g[1], g[2], 32, w->B1b.p, w->C2.p, 0.125f);
-  conv_fwd(32, 48, true, g[2], B, w->C2.p, net->W16[A2].p, bias_of(net, A2), w->A2b.p, nullptr, s);
-  conv_fwd(48, 48, true, g[2], B, w->A2b.p, net->W16[B2L].p, bias_of(net, B2L), w->B2b.p, nullptr, s);
+  conv_fwd(32, 48, true, g[2], B, w->C2.p, net->W16[A2].p, bias_of(net, A2), w->A2b.p, nullptr, net->wait_error.dev, s);
+  conv_fwd(48, 48, true, g[2], B, w->A2b.p, net->W16[B2L].p, bias_of(net, B2L), w->B2b.p, nullptr, net->wait_error.dev, s);
   sfx::nn::restrict_to<bf16, bf16><<<grid2(N3 * 48, B), 256, 0, s>>>(g[2], g[3], 48, w->B2b.p, w->C3.p, 0.125f);
-  conv_fwd(48, 48, true, g[3], B, w->C3.p, net->W16[A3].p, bias_of(net, A3), w->A3b.p, nullptr, s);
+  conv_fwd(48, 48, true, g[3], B, w->C3.p, net->W16[A3].p, bias_of(net, A3), w->A3b.p, nullptr, net->wait_error.dev, s);
   // D2 = P A3 + B2 ; E2 = relu(conv(D2))
   cudaMemsetAsync(w->D2.p, 0, sizeof(float) * N2 * 48 * B, s);
   sfx::nn::prolong_add<bf16><<<grid2(N2 * 48, B), 256, 0, s>>>(g[2], g[3], 48, w->A3b.p, w->D2.p, 1.f);
   add_bf16_into<<<nb(N2 * 48 * B), 256, 0, s>>>(w->B2b.p, w->D2.p, w->D2b.p, N2 * 48 * B);
-  conv_fwd(48, 32, true, g[2], B, w->D2b.p, net->W16[U2].p, bias_of(net, U2), w->E2.p, nullptr, s);
+  conv_fwd(48, 32, true, g[2], B, w->D2b.p, net->W16[U2].p, bias_of(net, U2), w->E2.p, nullptr, net->wait_error.dev, s);
   cudaMemsetAsync(w->D1.p, 0, sizeof(float) * N1 * 32 * B, s);
   sfx::nn::prolong_add<bf16><<<grid2(N1 * 32, B), 256, 0, s>>>(g[1], g[2], 32, w->E2.p, w->D1.p, 1.f);
   add_bf16_into<<<nb(N1 * 32 * B), 256, 0, s>>>(w->B1b.p, w->D1.p, w->D1b.p, N1 * 32 * B);
-  conv_fwd(32, 16, true, g[1], B, w->D1b.p, net->W16[U1].p, bias_of(net, U1), w->E1.p, nullptr, s);
+  conv_fwd(32, 16, true, g[1], B, w->D1b.p, net->W16[U1].p, bias_of(net, U1), w->E1.p, nullptr, net->wait_error.dev, s);
   cudaMemsetAsync(w->D0.p, 0, sizeof(float) * N0 * 16 * B, s);
   sfx::nn::prolong_add<bf16><<<grid2(N0 * 16, B), 256, 0, s>>>(g[0], g[1], 16, w->E1.p, w->D0.p, 1.f);
   add_bf16_into<<<nb(N0 * 16 * B), 256, 0, s>>>(w->B0b.p, w->D0.p, w->D0b.p, N0 * 16 * B);
-  conv_fwd(16, 16, true, g[0], B, w->D0b.p, net->W16[U0].p, bias_of(net, U0), w->E0.p, nullptr, s);
-  conv_fwd(16, 16, false, g[0], B, w->E0.p, net->W16[OUTL].p, bias_of(net, OUTL), nullptr, w->OUT.p, s);
+  conv_fwd(16, 16, true, g[0], B, w->D0b.p, net->W16[U0].p, bias_of(net, U0), w->E0.p, nullptr, net->wait_error.dev, s);
+  conv_fwd(16, 16, false, g[0], B, w->E0.p, net->W16[OUTL].p, bias_of(net, OUTL), nullptr, w->OUT.p, net->wait_error.dev, s);
 }
 
 // backward through one convolution: given the gradient of its output (post
@@ -370,7 +373,7 @@ void conv_bwd(sfx_lnet net, Work* w, int l, Grid3 g, int B, const bf16* x, const
   add_into<<<nb(c.nw()), 256, 0, s>>>(w->red.p, net->G.p + c.off, c.nw());
   bias_grad(c.co, w->gpre.p, rows, w->red.p, s);
   add_into<<<1, 64, 0, s>>>(w->red.p, net->G.p + c.off + c.nw(), c.co);
-  if (gx) conv_fwd(c.co, c.ci, false, g, B, w->gpre16.p, net->Wt16[l].p, nullptr, nullptr, gx, s);
+  if (gx) conv_fwd(c.co, c.ci, false, g, B, w->gpre16.p, net->Wt16[l].p, nullptr, nullptr, gx, net->wait_error.dev, s);
 }
 
 void backward(sfx_lnet net, Work* w, int B, cudaStream_t s) {
@@ -446,6 +449,13 @@ int lnet_apply(sfx_lnet net, int nx, int ny, int nz, const float* r, const float
   return SFX_OK;
 }
 
+// a convolution of an earlier (completed) call gave up a bounded wait
+int check_waits(sfx_lnet net) {
+  if (!net->wait_error.raised()) return SFX_OK;
+  net->wait_error.clear();
+  return fail(SFX_ERR_TIMEOUT, "a tensor-core wait of the network's convolution expired");
+}
+
 }  // namespace sfx_impl
 
 extern "C" {
@@ -470,7 +480,8 @@ int sfx_lnet_create(uint64_t seed, sfx_lnet* out) {
     std::normal_distribution<double> nd(0.0, std::sqrt(2.0 / (27.0 * c.ci)) * (c.relu ? 1.0 : 0.1));
     for (int64_t i = 0; i < c.nw(); i++) p[size_t(c.off + i)] = float(nd(rng));
   }
-  bool ok = net->P.upload(p.data(), p.size()) == cudaSuccess && net->G.alloc(p.size()) == cudaSuccess &&
+  bool ok = net->wait_error.init() == cudaSuccess && net->P.upload(p.data(), p.size()) == cudaSuccess &&
+            net->G.alloc(p.size()) == cudaSuccess &&
             net->M.alloc(p.size()) == cudaSuccess && net->V.alloc(p.size()) == cudaSuccess;
   for (int l = 0; l < NLAYERS && ok; l++)
     ok = net->W16[l].alloc(size_t(net->layers[l].nw())) == cudaSuccess &&
@@ -512,12 +523,14 @@ int sfx_lnet_set_params(sfx_lnet net, const float* host, int64_t n) {
 int sfx_lnet_apply(sfx_lnet net, int nx, int ny, int nz, const float* r, const float* features, float* z,
                    void* stream) {
   if (!net || !r || !features || !z) return fail(SFX_ERR_INVALID, "null argument");
+  if (int rc = check_waits(net)) return rc;
   return lnet_apply(net, nx, ny, nz, r, features, z, static_cast<cudaStream_t>(stream));
 }
 
 int sfx_lnet_gradient(sfx_lnet net, int nx, int ny, int nz, const float* r, const float* target,
                       const float* features, float* loss, float* grad_host, void* stream) {
   if (!net || !r || !target || !features || !loss || !grad_host) return fail(SFX_ERR_INVALID, "null argument");
+  if (int rc = check_waits(net)) return rc;
   auto s = static_cast<cudaStream_t>(stream);
   Work* w = nullptr;
   if (int rc = get_work(net, nx, ny, nz, 1, &w)) return rc;
@@ -530,6 +543,7 @@ int sfx_lnet_gradient(sfx_lnet net, int nx, int ny, int nz, const float* r, cons
 int sfx_lnet_train_step(sfx_lnet net, int nx, int ny, int nz, int batch, const float* r, const float* target,
                         const float* features, float lr, float* mean_loss, void* stream) {
   if (!net || !r || !target || !features || batch < 1) return fail(SFX_ERR_INVALID, "bad argument");
+  if (int rc = check_waits(net)) return rc;
   auto s = static_cast<cudaStream_t>(stream);
   Work* w = nullptr;
   if (int rc = get_work(net, nx, ny, nz, batch, &w)) return rc;
@@ -544,7 +558,7 @@ int sfx_lnet_train_step(sfx_lnet net, int nx, int ny, int nz, int batch, const f
   float l = 0.f;
   if (int rc = read_mean_loss(w, batch, s, &l)) return rc;
   if (mean_loss) *mean_loss = l;
-  return SFX_OK;
+  return check_waits(net);
 }
 
 }  // extern "C"

@@ -650,6 +650,10 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
     SFX_CUDA_TRY(cudaStreamSynchronize(st));
     s->stats.inner_iterations += inner;
   }
+  if (rc == SFX_OK && s->net && o.precond == SFX_PREC_LEARNED) {
+    SFX_CUDA_TRY(cudaStreamSynchronize(st));
+    if (int rw = check_waits(s->net)) return rw;
+  }
   if (rc == SFX_OK && s->form->wait_error.raised()) {
     // a bounded wait inside a replayed FP32 action expired
     s->form->wait_error.clear();
