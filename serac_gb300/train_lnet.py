@@ -4,9 +4,12 @@ parameters (the file bench.py and the solver load):
     python -m serac_gb300.train_lnet --n 16 --seeds 1000:1032 --epochs 40 \\
         --out serac_gb300/weights/lnet_j2_q2.npy
 
-Training problems: small-strain J2 with linear hardening on n^3 Q2 meshes,
-per-element lognormal Young's modulus (sigma_log in [0.5, 1.5], correlation
-length in [0.05, 0.3], drawn per seed), compression in load steps.  Pairs:
+Training problems (--material): small-strain J2 with linear hardening on
+n^3 Q2 meshes, per-element lognormal Young's modulus (sigma_log in
+[0.5, 1.5], correlation length in [0.05, 0.3], drawn per seed), compression
+in load steps; or the heterogeneous Neo-Hookean solid of the large
+configurations (shear modulus 0.25 exp(g), sigma_log 1, correlation length
+0.1, bulk modulus 20 G), its first load steps (--strain per --steps).  Pairs:
 every Newton (residual, correction) of the mixed-precision solve plus probe
 pairs (smooth random x, r = J x) at each converged step.  Runs on the GPU with
 the library's own BF16 training kernels.
@@ -29,6 +32,9 @@ def main(argv=None):
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--init-seed", type=int, default=0)
     ap.add_argument("--steps", type=int, default=4, help="load steps per training problem")
+    ap.add_argument("--material", choices=["j2", "neohookean"], default="j2")
+    ap.add_argument("--strain", type=float, default=None,
+                    help="compression reached after --steps (default: 0.02 for J2, 0.005 for Neo-Hookean)")
     ap.add_argument("--eval-seeds", default=None,
                     help="first:last held-out seeds: after training, solve them with and without the network")
     ap.add_argument("--out", required=True)
@@ -40,7 +46,8 @@ def main(argv=None):
 
     lo, hi = (int(x) for x in args.seeds.split(":"))
     t0 = time.time()
-    problems = [L.j2_problem(args.n, s, steps=args.steps) for s in range(lo, hi)]
+    make = problem_factory(args.material, args.strain, args.steps)
+    problems = [make(args.n, s) for s in range(lo, hi)]
     R, T, F = L.harvest(problems, probes_per_step=args.probes)
     torch.cuda.synchronize()
     t_harvest = time.time() - t0
@@ -52,17 +59,30 @@ def main(argv=None):
     torch.cuda.synchronize()
     os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
     net.save(args.out)
-    info = {"pairs": int(R.shape[0]), "seeds": args.seeds, "n": args.n, "epochs": args.epochs, "batch": args.batch,
+    info = {"material": args.material, "pairs": int(R.shape[0]), "seeds": args.seeds, "n": args.n,
+            "steps": args.steps, "epochs": args.epochs, "batch": args.batch,
             "lr": args.lr, "harvest_s": round(t_harvest, 1), "train_s": round(time.time() - t0, 1),
             "final_loss": hist[-1], "loss_history": [round(h, 4) for h in hist]}
     if args.eval_seeds:
-        info["evaluation"] = evaluate(net, args.n, args.eval_seeds, args.steps)
+        info["evaluation"] = evaluate(net, args.n, args.eval_seeds, make)
     with open(os.path.splitext(args.out)[0] + ".json", "w") as fh:
         json.dump(info, fh, indent=1)
     print(json.dumps(info))
 
 
-def evaluate(net, n, seeds, steps):
+def problem_factory(material, strain, steps):
+    """(n, seed) -> SolidProblem of the chosen family."""
+    from . import learned as L
+
+    if material == "neohookean":
+        st = 0.005 if strain is None else strain
+        return lambda n, seed: L.neohookean_problem(n, seed, sigma_log=1.0, ell=0.1, strain=st, steps=steps,
+                                                    bulk_ratio=20.0)
+    st = 0.02 if strain is None else strain
+    return lambda n, seed: L.j2_problem(n, seed, strain=st, steps=steps)
+
+
+def evaluate(net, n, seeds, make):
     """Held-out seeds: Krylov iterations and seconds of flexible GMRES with
     Jacobi-Chebyshev alone against the network's two-level step
     (Chebyshev, network, Chebyshev), and of mixed precision against learned +
@@ -84,7 +104,7 @@ def evaluate(net, n, seeds, steps):
     totals = {k: {"krylov_iterations": 0, "seconds": 0.0} for k in variants}
     worst_diff = 0.0
     for seed in range(lo, hi):
-        prob = L.j2_problem(n, seed, steps=steps)
+        prob = make(n, seed)
         sols = {}
         for name, (opts, use_net) in variants.items():
             S = L.SolidSetup(prob)

@@ -183,7 +183,8 @@ def test_corrupted_weights_fall_back_and_keep_the_answer(cuda, mixed):
 def test_trained_network_gain(cuda):
     """What the trained network gains over the method without it.  The network
     is trained on the GPU by the library's own kernels (pairs harvested from
-    the solver on 12 seeded J2 problems at 8^3 Q2 hexes, 40 epochs), then used
+    the solver on 12 seeded J2 problems at 8^3 Q2 hexes, compression to 0.01
+    in two load steps, 40 epochs), then used
     on two held-out seeds inside flexible GMRES as the two-level step
     Chebyshev -> network -> Chebyshev.  Against flexible GMRES with
     Jacobi-Chebyshev alone it must cut the Krylov iterations by at least a
@@ -192,14 +193,16 @@ def test_trained_network_gain(cuda):
     from serac_gb300 import learned as LP
 
     n = 8
-    R, T, F = LP.harvest([LP.j2_problem(n, 1000 + i, steps=2) for i in range(12)], probes_per_step=8)
+    # compression to 0.01 in two steps (at 0.02 the plain Newton iteration
+    # itself diverges on the second step of some held-out seeds)
+    R, T, F = LP.harvest([LP.j2_problem(n, 1000 + i, strain=0.01, steps=2) for i in range(12)], probes_per_step=8)
     net = LP.LearnedPreconditioner(seed=0)
     hist = LP.train(net, (2 * n + 1,) * 3, R, T, F, epochs=40, batch=8, lr=1e-3)
     assert hist[-1] < 0.97 * hist[0]
     base = dict(_TIGHT, krylov=sg.FGMRES)
     plain_its = learned_its = 0
     for seed in (2000, 2001):
-        prob = LP.j2_problem(n, seed, steps=2)
+        prob = LP.j2_problem(n, seed, strain=0.01, steps=2)
         u0, st0 = _solve_steps(prob, sg.SolverOptions.defaults(precond=sg.JACOBI_CHEBYSHEV, **base))
         u1, st1 = _solve_steps(prob, sg.SolverOptions.defaults(precond=sg.LEARNED, learned_cycle=1, **base), net)
         assert float(torch.linalg.norm(u1 - u0) / torch.linalg.norm(u0)) <= 1e-9
