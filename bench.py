@@ -549,7 +549,7 @@ def c2_leg(dev, timed, hbm_peak, fp64_peak, K):
 
 
 NEWTON_VARIANTS = "plain_fp64,mixed,learned_mixed"
-WEIGHTS = os.path.join(ROOT, "serac_gb300", "weights", "lnet_j2_q2.npy")
+WEIGHTS = os.path.join(ROOT, "serac_gb300", "weights", "lnet_neohookean_q2.npy")
 # Jacobi-Chebyshev settings (degree, interval ratio) of each method
 PLAIN_CHEBYSHEV = (48, 2304.0)
 INNER_CHEBYSHEV = (16, 256.0)
@@ -635,8 +635,10 @@ def newton_leg(steps, variants, n=NX):
             out[f"speedup_{name}_vs_plain"] = out["plain_fp64"]["seconds"] / out[name]["seconds"]
     if net is not None:
         out["weights"] = {"file": os.path.relpath(WEIGHTS, ROOT),
-                          "trained_on": "J2 16^3 Q2, seeds 1000-1031 (python -m serac_gb300.train_lnet), applied "
-                                        "fully convolutionally on this problem's node grid"}
+                          "trained_on": "heterogeneous Neo-Hookean (this material distribution) at 32^3 Q2, first two "
+                                        "load steps of seeds 3000-3031, 1152 pairs, 20 epochs (python -m "
+                                        "serac_gb300.train_lnet --material neohookean --n 32), applied fully "
+                                        "convolutionally on this problem's node grid"}
     return out
 
 

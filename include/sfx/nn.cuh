@@ -42,29 +42,30 @@ __device__ inline void mma_bf16_16816(float (&d)[4], const uint32_t (&a)[4], con
 
 enum Act : int { ACT_NONE = 0, ACT_RELU = 1 };
 
-/// Shared-memory layout of conv3_fwd_umma: every weight as K-major core
-/// matrices, one B chunk of COUT rows x 16 input channels per (tap, channel
-/// chunk), and two A buffers of 128 nodes x CIN for the tap being computed
-/// and the next one.
+/// Shared-memory layout of conv3_fwd_umma: two stages, each holding one
+/// tap's A operand (128 nodes x CIN) and B operand (COUT x CIN weights) as
+/// K-major core matrices, one chunk per 16 input channels.  About 34 KB for
+/// the widest layer, so several blocks share an SM and hide each other's
+/// gather latency.
 template <int CIN, int COUT>
 struct UmmaConvSmem {
   static constexpr int KC = CIN / 16;                      // K-steps per tap
-  static constexpr uint32_t B_CHUNK = uint32_t(COUT) * 32;  // bytes per (tap, K-step)
+  static constexpr uint32_t B_CHUNK = uint32_t(COUT) * 32;  // bytes per K-step
   static constexpr uint32_t A_CHUNK = 128 * 32;
-  static constexpr uint32_t A_BUF = A_CHUNK * KC;
-  static constexpr size_t w_bytes = size_t(27) * KC * B_CHUNK;
-  static constexpr size_t bytes = w_bytes + 2 * size_t(A_BUF);
+  static constexpr uint32_t A_STAGE = A_CHUNK * KC;
+  static constexpr uint32_t B_STAGE = B_CHUNK * KC;
+  static constexpr size_t bytes = 2 * size_t(A_STAGE + B_STAGE);
   static constexpr uint32_t NCOLS = COUT <= 32 ? 32 : 64;  // TMEM columns of the FP32 accumulator
 };
 
 /// Forward 3x3x3 convolution on the 5th-generation tensor cores: an implicit
 /// GEMM with the 128 output nodes of the block as M, the output channels as
 /// N and K = 27 taps x CIN, accumulated in tensor memory (FP32) by tcgen05.mma
-/// kind::f16 (BF16 operands in shared memory).  The block stages all weights
-/// once; for each tap its 128 threads gather the shifted input rows (16-byte
-/// loads, zero outside the grid) into one of two A buffers while the MMAs of
-/// the previous tap run; one thread issues the tap's CIN / 16 MMAs and commits
-/// them to that buffer's mbarrier, which the gather two taps later waits on.
+/// kind::f16 (BF16 operands in shared memory).  For each tap the block's 128
+/// threads gather the shifted input rows (16-byte loads, zero outside the
+/// grid) and the tap's weights into one of two stages while the MMAs of the
+/// previous tap run; one thread issues the tap's CIN / 16 MMAs and commits
+/// them to that stage's mbarrier, which the gather two taps later waits on.
 /// The epilogue reads the accumulator with tcgen05.ld (warp w: rows
 /// 32w..32w+31), adds the bias, applies the activation and stores BF16 (or
 /// FP32 into y_f32).  x: [node][CIN] bf16, W: [COUT][27][CIN] bf16, bias:
@@ -73,15 +74,13 @@ struct UmmaConvSmem {
 /// bounded: on a timeout the block sets *err, waits (bounded) for its issued
 /// MMAs and frees its tensor memory.
 template <int CIN, int COUT, int ACT>
-__global__ void __launch_bounds__(128, 1) conv3_fwd_umma(Grid3 g, const __nv_bfloat16* __restrict__ x,
+__global__ void __launch_bounds__(128, 4) conv3_fwd_umma(Grid3 g, const __nv_bfloat16* __restrict__ x,
                                                       const __nv_bfloat16* __restrict__ W,
                                                       const float* __restrict__ bias, __nv_bfloat16* __restrict__ y,
                                                       float* __restrict__ y_f32, int* __restrict__ err) {
   static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 64, "channel counts");
   using L = UmmaConvSmem<CIN, COUT>;
   extern __shared__ __align__(128) unsigned char sfx_conv_smem[];
-  unsigned char* sw = sfx_conv_smem;
-  unsigned char* sa = sfx_conv_smem + L::w_bytes;
   __shared__ uint64_t bars[2];
   __shared__ uint32_t tmem_base;
   __shared__ int node_xyz[128][3];
@@ -91,18 +90,6 @@ __global__ void __launch_bounds__(128, 1) conv3_fwd_umma(Grid3 g, const __nv_bfl
   if (y) y += int64_t(blockIdx.y) * N * COUT;
   if (y_f32) y_f32 += int64_t(blockIdx.y) * N * COUT;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-
-  // weights: W[co][tap][ci] -> chunk (tap, ci / 16), core-matrix slot of (co, ci % 16)
-  {
-    constexpr int VPR = 27 * CIN / 8;  // 16-byte vectors per output channel
-    const uint4* src = reinterpret_cast<const uint4*>(W);
-    for (int i = threadIdx.x; i < COUT * VPR; i += blockDim.x) {
-      const int co = i / VPR, v = i % VPR;
-      const int tap = v / (CIN / 8), g8 = v % (CIN / 8);
-      const uint32_t off = uint32_t(tap * L::KC + g8 / 2) * L::B_CHUNK + umma::kmajor_offset(co, (g8 & 1) * 8, 128, 256);
-      *reinterpret_cast<uint4*>(sw + off) = src[i];
-    }
-  }
   {
     const int r = threadIdx.x;  // one row per thread
     const int64_t n = n0 + r;
@@ -125,8 +112,9 @@ __global__ void __launch_bounds__(128, 1) conv3_fwd_umma(Grid3 g, const __nv_bfl
   umma::fence_after_sync();
   const uint32_t tmem = tmem_base;
   constexpr uint32_t idesc = umma::idesc_bf16_f32(128, COUT);
-  constexpr int GPN = CIN / 8;  // 16-byte groups per node
+  constexpr int GPN = CIN / 8;  // 16-byte groups per node (and per output channel of one tap's weights)
   const uint4* src = reinterpret_cast<const uint4*>(x);
+  const uint4* wsrc = reinterpret_cast<const uint4*>(W);
   bool ok = true;
   for (int tap = 0; tap < 27 && ok; tap++) {
     const int buf = tap & 1;
@@ -134,7 +122,8 @@ __global__ void __launch_bounds__(128, 1) conv3_fwd_umma(Grid3 g, const __nv_bfl
     if (!ok) break;
     umma::fence_after_sync();
     const int dx = tap % 3 - 1, dy = (tap / 3) % 3 - 1, dz = tap / 9 - 1;
-    unsigned char* A = sa + size_t(buf) * L::A_BUF;
+    unsigned char* A = sfx_conv_smem + size_t(buf) * (L::A_STAGE + L::B_STAGE);
+    unsigned char* Bm = A + L::A_STAGE;
     for (int i = threadIdx.x; i < 128 * GPN; i += blockDim.x) {
       const int r = i / GPN, g8 = i % GPN;
       const int xx = node_xyz[r][0] + dx, yy = node_xyz[r][1] + dy, zz = node_xyz[r][2] + dz;
@@ -143,7 +132,13 @@ __global__ void __launch_bounds__(128, 1) conv3_fwd_umma(Grid3 g, const __nv_bfl
         v = src[((int64_t(zz) * g.ny + yy) * g.nx + xx) * GPN + g8];
       *reinterpret_cast<uint4*>(A + uint32_t(g8 / 2) * L::A_CHUNK + umma::kmajor_offset(r, (g8 & 1) * 8, 128, 256)) = v;
     }
-    bulk::fence_proxy_async_smem();  // the gathered rows are read by the tensor core
+    // this tap's weights W[co][tap][ci] -> chunk ci / 16, core-matrix slot of (co, ci % 16)
+    for (int i = threadIdx.x; i < COUT * GPN; i += blockDim.x) {
+      const int co = i / GPN, g8 = i % GPN;
+      *reinterpret_cast<uint4*>(Bm + uint32_t(g8 / 2) * L::B_CHUNK + umma::kmajor_offset(co, (g8 & 1) * 8, 128, 256)) =
+          wsrc[(int64_t(co) * 27 + tap) * GPN + g8];
+    }
+    bulk::fence_proxy_async_smem();  // the gathered operands are read by the tensor core
     umma::fence_before_sync();
     __syncthreads();
     umma::fence_after_sync();
@@ -151,8 +146,7 @@ __global__ void __launch_bounds__(128, 1) conv3_fwd_umma(Grid3 g, const __nv_bfl
 #pragma unroll
       for (int kc = 0; kc < L::KC; kc++)
         umma::mma_bf16(tmem, umma::smem_desc(A + uint32_t(kc) * L::A_CHUNK, 128, 256),
-                       umma::smem_desc(sw + uint32_t(tap * L::KC + kc) * L::B_CHUNK, 128, 256), idesc,
-                       tap > 0 || kc > 0);
+                       umma::smem_desc(Bm + uint32_t(kc) * L::B_CHUNK, 128, 256), idesc, tap > 0 || kc > 0);
       umma::commit(&bars[buf]);
     }
   }
