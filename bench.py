@@ -482,6 +482,7 @@ def run_sfx(args, rank, world):
     torch.cuda.synchronize()
     if rank == 0 and not args.skip_c2:
         result["c2"] = c2_leg(dev, timed, hbm_peak, fp64_peak, max(3, args.steps // 4))
+        result["c5a"] = c5a_leg(dev, timed, max(3, args.steps // 4))
     if args.newton_steps > 0 and rank == 0:
         result["newton"] = newton_leg(args.newton_steps, args.newton_variants.split(","))
     result["clocks"] = clocks.stop()
@@ -545,6 +546,36 @@ def c2_leg(dev, timed, hbm_peak, fp64_peak, K):
                                 "matrices in chunks of 32,768 elements, then one thread per CSR row sums its "
                                 "entries in element order"}}
     del grad, f, vals, col, row_ptr
+    return out
+
+
+def c5a_leg(dev, timed, K):
+    """The large combined run's Q1 mesh: 128^3 hexahedra, H1 Q1 vector
+    (6,440,067 DOF, 2x2x2 Gauss), the same heterogeneous Neo-Hookean
+    material and load-step-1 state: FP64 and FP32 Jacobian actions."""
+    import torch
+
+    import serac_gb300 as sg
+
+    n = 128
+    V = vertices(n)
+    mesh = sg.Mesh.structured_hex(n, n, n, V)
+    f = sg.Functional(mesh, sg.H1(1, 3))
+    f.AddDomainIntegral(sg.NEOHOOKEAN, material(n).params, per_element=True)
+    u = torch.tensor(linearisation_state(mesh.node_coordinates(1)), device=dev)
+    grad = f.linearize(0.0, u)
+    du = torch.tensor(np.random.default_rng(0).standard_normal(f.ndofs), device=dev)
+    dr = torch.empty_like(du)
+    du32, dr32 = du.float(), torch.empty(f.ndofs, dtype=torch.float32, device=dev)
+    for _ in range(3):
+        grad.mult(du, dr)
+        grad.mult(du32, dr32)
+    t64 = timed(lambda: grad.mult(du, dr), K)
+    t32 = timed(lambda: grad.mult(du32, dr32), K)
+    out = {"workload": "neohookean_heterogeneous_q1_vector_128cubed (6,440,067 DOF, 2x2x2 Gauss)",
+           "jv_f64": f.ndofs * K / sum(t64) / 1e9, "jv_f32": f.ndofs * K / sum(t32) / 1e9, "unit": UNIT,
+           "ms_f64": statistics.mean(t64) * 1e3, "ms_f32": statistics.mean(t32) * 1e3}
+    del grad, f
     return out
 
 

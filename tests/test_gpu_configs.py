@@ -13,7 +13,12 @@
   1e-9 of the oracle's Newton solution (one oracle Newton step from it, on
   the oracle's own residual and matrix-free Jacobian, moves it by < 1e-9);
 * all 10 load steps of that ramp (to u_z = -0.05) on an 8^3 mesh against the
-  oracle's Newton with direct solves, within 1e-9 at every step.
+  oracle's Newton with direct solves, within 1e-9 at every step;
+* 32^3 Q2 J2 plasticity with a per-element lognormal Young's modulus (the
+  learned preconditioner's training configuration), after committing a
+  plastic state: residual and Jacobian action, 1e-12;
+* 128^3 Q1 heterogeneous Neo-Hookean (6,440,067 DOF, 2x2x2 Gauss; the large
+  combined run's Q1 mesh): residual and Jacobian action, 1e-12.
 
 Reference semantics: functional.hpp:446-498 (residual), :406-432 (Jv),
 :569-667 (assemble), equation_solver.cpp:79-200 (Newton),
@@ -239,3 +244,58 @@ def test_compression_ramp_all_load_steps_match_oracle(cuda):
         ref = O.warm_start(orc, ref, target, ess)
         ref, _, rn = O.newton(orc, ref, ess, rel_tol=1e-12, abs_tol=1e-14)
         assert rel(u.cpu().numpy(), ref) <= 1e-9, step
+
+
+def test_c4_j2_with_plastic_state_matches_oracle(cuda):
+    """Commit the state at u (updateQdata), then compare residual and Jv at
+    1.5 u, where the committed plastic strain matters."""
+    import serac_gb300 as sg
+    from serac_gb300 import learned as LP
+
+    n = 32
+    prob = LP.j2_problem(n, 2000)
+    V = sg.box_vertices(n, n, n, 0.1, 1)
+    mesh = sg.Mesh.structured_hex(n, n, n, V)
+    f = sg.Functional(mesh, sg.H1(2, 3))
+    f.AddDomainIntegral(sg.J2, prob.params, per_element=True)
+    orc = O.OracleFunctional(O.StructuredHexMesh(n, n, n, V), 2, 3, nthreads=_threads())
+    orc.add_domain_integral(O.MAT_J2, prob.params)
+    X = mesh.node_coordinates(2)
+    u = np.zeros((3, X.shape[0]))
+    u[2] = -0.02 * X[:, 2]  # into the plastic range of the soft elements
+    u = (u + 1e-4 * np.random.default_rng(3).standard_normal(u.shape)).ravel()
+    ut = torch.tensor(u, device=cuda)
+    f.updateQdata(True)
+    f.residual(0.0, ut)
+    f.updateQdata(False)
+    orc.residual(u, update_state=True)
+    assert orc.state[..., 9].max() > 0.0  # some points yielded
+    u2 = 1.5 * u
+    du = np.random.default_rng(4).standard_normal(f.ndofs)
+    r, jv, jv32, _ = _residual_and_jvp(cuda, f, orc, u2, du)
+    assert rel(r, orc.residual(u2)) <= 1e-12
+    jv_ref = orc.jvp(u2, du)
+    assert rel(jv, jv_ref) <= 1e-12
+    assert rel(jv32, jv_ref) <= 1e-5
+
+
+def test_c5a_q1_128cubed_matches_oracle(cuda):
+    import serac_gb300 as sg
+    from serac_gb300 import learned as LP
+
+    n = 128
+    prob = LP.neohookean_problem(n, 2, sigma_log=1.0, ell=0.1, strain=0.05, steps=20, bulk_ratio=20.0)
+    V = sg.box_vertices(n, n, n, 0.1, 1)
+    mesh = sg.Mesh.structured_hex(n, n, n, V)
+    f = sg.Functional(mesh, sg.H1(1, 3))
+    f.AddDomainIntegral(sg.NEOHOOKEAN, prob.params, per_element=True)
+    assert f.ndofs == 6_440_067
+    orc = O.OracleFunctional(O.StructuredHexMesh(n, n, n, V), 1, 3, nthreads=_threads())
+    orc.add_domain_integral(O.MAT_NEOHOOKEAN, prob.params)
+    u = _load_step1_state(mesh.node_coordinates(1))
+    du = np.random.default_rng(5).standard_normal(f.ndofs)
+    r, jv, jv32, _ = _residual_and_jvp(cuda, f, orc, u, du)
+    assert rel(r, orc.residual(u)) <= 1e-12
+    jv_ref = orc.jvp(u, du)
+    assert rel(jv, jv_ref) <= 1e-12
+    assert rel(jv32, jv_ref) <= 1e-5

@@ -1,5 +1,6 @@
-"""Size-independent properties at the configurations' full sizes, where the
-oracle is too slow to run: the Neo-Hookean 32^3 Q2 problem (823,875 DOF) and
+"""Size-independent properties at the configurations' full sizes, alongside
+the direct comparisons with the oracle at those sizes in
+tests/test_gpu_configs.py: the Neo-Hookean 32^3 Q2 problem (823,875 DOF) and
 the heterogeneous 64^3 Q2 problem (6,440,067 DOF).
 
 * the assembled CSR matrix applied to a vector equals the Jacobian action;
