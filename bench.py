@@ -10,9 +10,9 @@ One step = one Jacobian action over the whole mesh (sfx_jvp: fused element
 kernel + deterministic node-owner scatter), linearised at a load-step-1
 state.  `value` is timed with CUDA events around each step with the inputs
 resident in HBM (the FP64 tangent and the vectors are far larger than L2;
-the L2 is also flushed between steps).  `e2e` runs the same call through
-the C ABI with the direction copied from pinned host memory and the result
-copied back inside the timed region.  The `newton` leg is the metric's
+the L2 is also flushed between steps).  `e2e` runs the same action as one
+C ABI call on host buffers (sfx_jvp_host: pinned du in, dr out, the copies
+inside the timed region, overlapped with the kernels slab by slab).  The `newton` leg is the metric's
 second half: time to a 1e-8 relative Newton residual for load step 1
 (warm-start predictor + Newton) with plain FP64 GMRES(50) +
 Jacobi-Chebyshev, FP32-inner mixed precision, and the learned
@@ -404,13 +404,23 @@ def run_sfx(args, rank, world):
     d_du = torch.empty(ndofs, dtype=torch.float64, device=dev)
 
     def e2e_step():
+        # one call with host buffers (sfx_jvp_host): copies in, kernels and
+        # copies out pipelined over slabs of element layers
+        grad.mult(h_du, out=h_dr)
+
+    def e2e_serial_step():
         d_du.copy_(h_du, non_blocking=True)
         grad.mult(d_du, dr)
         h_dr.copy_(dr, non_blocking=True)
 
     for _ in range(max(1, args.warmup)):
         e2e_step()
+        e2e_serial_step()
     t_e2e = timed(e2e_step, args.steps)
+    t_e2e_serial = timed(e2e_serial_step, args.steps)
+    host_e2e = grad.mult(h_du).clone()
+    grad.mult(d_du.copy_(h_du), dr)
+    e2e_bitwise = bool(torch.equal(host_e2e, dr.cpu()))
     ok = bool(torch.isfinite(dr).all().item()) and bool(torch.isfinite(h_dr).all().item())
     torch.cuda.synchronize()
     fp64_peak = measure_fp64_peak(dev)
@@ -424,9 +434,11 @@ def run_sfx(args, rank, world):
     roof64 = roofline_hbm("sfx::kernels::jvp_stored_kernel<2,3,false,false,double,false> (FP64, full tangent)",
                           alg64, t_k, hbm_peak, peak_src, traffic.get("jvp_stored_f64"),
                           "FP64-pipe bound: see compute_roofline")
-    # FP64 work per element: interpolate grad du (3 x 3 x 24 FMA per point),
-    # the 9 x 9 tangent (81 FMA), integrate (3 x 3 x 27 FMA); idle lanes excluded
-    flops_per_elem = 2 * (72 + 81 + 81) * (ORDER + 1) ** 3
+    # FP64 work per element, as the kernel does it (collocated sum
+    # factorisation): interpolate du to the points and differentiate there
+    # (3 components x 18 FMA per point), the 9 x 9 tangent (81 FMA), integrate
+    # (3 x 18 FMA); idle lanes excluded
+    flops_per_elem = 2 * (54 + 81 + 54) * (ORDER + 1) ** 3
     ach = flops_per_elem * ne / t_k / 1e12
     compute = {"bound": "fp64", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach / fp64_peak,
                "flops_per_element": flops_per_elem, "peak_source": "cuBLAS DGEMM 4096^3 measured in this run"}
@@ -460,7 +472,12 @@ def run_sfx(args, rank, world):
         "config": config(world, "working set (15.5 GB FP64 tangent) far above L2; L2 also flushed (256 MB write) "
                                 "before every timed step"),
         "e2e": {"value": ndofs * args.steps / sum(t_e2e) / 1e9, "unit": UNIT, "h2d_bytes_per_step": 8 * ndofs,
-                "d2h_bytes_per_step": 8 * ndofs},
+                "d2h_bytes_per_step": 8 * ndofs, "ms_per_step": statistics.mean(t_e2e) * 1e3,
+                "call": "sfx_jvp_host (pinned host du and dr; H2D, kernels and D2H pipelined over 8 slabs of "
+                        "element layers)", "bitwise_equal_to_device_call": e2e_bitwise,
+                "serial_copies": {"value": ndofs * args.steps / sum(t_e2e_serial) / 1e9,
+                                  "ms_per_step": statistics.mean(t_e2e_serial) * 1e3,
+                                  "note": "H2D copy, sfx_jvp, D2H copy one after another on one stream"}},
         "roofline": roof64,
         "compute_roofline": compute,
         "jv_fp32": {"value": ndofs * args.steps / sum(t_fp32) / 1e9, "unit": UNIT, "dtype": "f32",

@@ -21,6 +21,8 @@
  *   sfx_residual                    numerics/functional/functional.hpp:502-513 operator()(t, u)
  *   sfx_linearize                   numerics/functional/functional.hpp:481-489 operator()(t, differentiate_wrt(u))
  *   sfx_jvp / sfx_jvp_f32           numerics/functional/functional.hpp:556-566 Gradient::Mult / operator()
+ *   sfx_jvp_host                    the same Gradient::Mult on host-resident mfem::Vectors (mfem moves them to
+ *                                   and from the device around the action)
  *   sfx_jvp_element(_f32)           numerics/functional/integral.hpp:93-103 Integral::GradientMult
  *   sfx_jvp_transpose(_f32)         physics/solid_mechanics.hpp:1343-1501 (the adjoint solves' transposed
  *                                   Jacobian, formed there as the transpose of assemble(Gradient&))
@@ -207,6 +209,19 @@ int sfx_form_set_tangent_storage(sfx_form form, int storage);
 /* dr = dR/du(t_lin, u_lin) du, in FP64, and in FP32 (FP32 accumulation). */
 int sfx_jvp(sfx_form form, const double* du, double* dr, void* stream);
 int sfx_jvp_f32(sfx_form form, const float* du, float* dr, void* stream);
+
+/* dr = dR/du(t_lin, u_lin) du in FP64 with du and dr in HOST memory (ndofs
+ * doubles each; page-locked memory lets the copies overlap the kernels).  On
+ * a structured mesh with one domain integral, no boundary integral and the
+ * stored tangent, the copies in, the element kernels, the scatter and the
+ * copies out are pipelined over (up to 8) slabs of element layers in z, on
+ * two internal copy streams and `stream`: slab k's elements need the node
+ * planes up to the slab's top, and the node planes below it are complete
+ * once slab k is done.  Other forms copy in, run sfx_jvp and copy out.  The
+ * result is bitwise that of sfx_jvp.  Blocks until dr is written; two
+ * device vectors of ndofs doubles are allocated on the first call and kept
+ * with the form. */
+int sfx_jvp_host(sfx_form form, const double* du, double* dr, void* stream);
 
 /* Element-level Jacobian action before the scatter-add (Integral::GradientMult,
  * integral.hpp:93-103): dE[e][component][node] (device, num_elements *

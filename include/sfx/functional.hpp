@@ -217,7 +217,7 @@ template <int NPE>
 void scatter3(const sfx_form_layout& L, const double* E3, double* out, bool accumulate, cudaStream_t s) {
   if (L.num_nodes == 0) return;
   kernels::scatter_kernel<3, NPE, double><<<unsigned((L.num_nodes + 255) / 256), 256, 0, s>>>(
-      E3, L.node_ptr, L.node_ent, out, L.num_nodes, accumulate);
+      E3, L.node_ptr, L.node_ent, out, L.num_nodes, accumulate, int64_t(0), L.num_nodes);
   check_cuda(cudaGetLastError(), "shape-space scatter");
 }
 
@@ -872,7 +872,7 @@ template <int C, int NPE>
 void scatter_c(const sfx_form_layout& L, const double* E, double* out, bool accumulate, cudaStream_t s) {
   if (L.num_nodes == 0) return;
   kernels::scatter_kernel<C, NPE, double><<<unsigned((L.num_nodes + 255) / 256), 256, 0, s>>>(
-      E, L.node_ptr, L.node_ent, out, L.num_nodes, accumulate);
+      E, L.node_ptr, L.node_ent, out, L.num_nodes, accumulate, int64_t(0), L.num_nodes);
   check_cuda(cudaGetLastError(), "multi-field scatter");
 }
 

@@ -16,6 +16,7 @@
 
 #include <cstdint>
 #include <type_traits>
+#include <utility>
 
 #include "sfx/dual.hpp"
 #include "sfx/materials.hpp"
@@ -210,6 +211,62 @@ SFX_HDI Real integrate_lane(Real s, Real f0, Real f1, Real f2, int base, int ix,
   return r;
 }
 
+/// interpolate_lane by collocation: the nodal field is first interpolated to
+/// the quadrature points (B along x, y, z: 3Q multiply-adds), then the point
+/// values are differentiated with the collocated derivative matrix Dq = G B^-1
+/// (3Q more).  Same result as interpolate_lane to rounding with 6Q instead of
+/// 8Q (gradient only) or 9Q (value and gradient) multiply-adds per lane — the
+/// cost that bounds the FP64 Jacobian action.
+template <int Q, typename Real>
+SFX_HDI void interpolate_colloc(Real U, int base, int ix, int iy, int iz, const Real (*B)[Q], const Real (*Dq)[Q],
+                                Real& val, Real& g0, Real& g1, Real& g2) {
+  Real a = 0;
+#pragma unroll
+  for (int k = 0; k < Q; k++) a += B[ix][k] * shfl(U, base + k + Q * (iy + Q * iz));
+  Real b = 0;
+#pragma unroll
+  for (int k = 0; k < Q; k++) b += B[iy][k] * shfl(a, base + ix + Q * (k + Q * iz));
+  Real w = 0;
+#pragma unroll
+  for (int k = 0; k < Q; k++) w += B[iz][k] * shfl(b, base + ix + Q * (iy + Q * k));
+  Real d0 = 0, d1 = 0, d2 = 0;
+#pragma unroll
+  for (int k = 0; k < Q; k++) {
+    d0 += Dq[ix][k] * shfl(w, base + k + Q * (iy + Q * iz));
+    d1 += Dq[iy][k] * shfl(w, base + ix + Q * (k + Q * iz));
+    d2 += Dq[iz][k] * shfl(w, base + ix + Q * (iy + Q * k));
+  }
+  val = w;
+  g0 = d0;
+  g1 = d1;
+  g2 = d2;
+}
+
+/// integrate_lane by collocation, the transpose of interpolate_colloc: the
+/// flux is taken back through Dq^T at the points and added to the source,
+/// then B^T is applied along x, y, z.
+template <int Q, bool HS, bool HF, typename Real>
+SFX_HDI Real integrate_colloc(Real s, Real f0, Real f1, Real f2, int base, int ix, int iy, int iz, const Real (*B)[Q],
+                              const Real (*Dq)[Q]) {
+  Real t = HS ? s : Real(0);
+#pragma unroll
+  for (int k = 0; k < (HF ? Q : 0); k++) {
+    t += Dq[k][ix] * shfl(f0, base + k + Q * (iy + Q * iz));
+    t += Dq[k][iy] * shfl(f1, base + ix + Q * (k + Q * iz));
+    t += Dq[k][iz] * shfl(f2, base + ix + Q * (iy + Q * k));
+  }
+  Real a = 0;
+#pragma unroll
+  for (int k = 0; k < Q; k++) a += B[k][ix] * shfl(t, base + k + Q * (iy + Q * iz));
+  Real b = 0;
+#pragma unroll
+  for (int k = 0; k < Q; k++) b += B[k][iy] * shfl(a, base + ix + Q * (k + Q * iz));
+  Real r = 0;
+#pragma unroll
+  for (int k = 0; k < Q; k++) r += B[k][iz] * shfl(b, base + ix + Q * (iy + Q * k));
+  return r;
+}
+
 template <typename State>
 SFX_HDI void load_state(State& s, const double* state, int64_t gq, int64_t nq_total) {
   constexpr int n = sizeof(State) / sizeof(double);
@@ -243,11 +300,11 @@ __global__ void __launch_bounds__(128) domain_kernel(DomainArgs<Real> a, QFMaker
   const bool valid = slot && e < a.num_elements;
   const int ix = qi % Q, iy = (qi / Q) % Q, iz = qi / (Q * Q);
 
-  __shared__ Real sB[Q][Q], sG[Q][Q];
+  __shared__ Real sB[Q][Q], sD[Q][Q];
   if (threadIdx.x < Q * Q) {
     int i = threadIdx.x / Q, j = threadIdx.x % Q;
     sB[i][j] = Real(basis_table<P>().B[i][j]);
-    sG[i][j] = Real(basis_table<P>().G[i][j]);
+    sD[i][j] = Real(basis_table<P>().D[i][j]);
   }
   __syncthreads();
 
@@ -262,11 +319,11 @@ __global__ void __launch_bounds__(128) domain_kernel(DomainArgs<Real> a, QFMaker
   for (int c = 0; c < C; c++) {
     Real U = valid ? a.u[c * a.num_nodes + node] : Real(0);
     Real g[3];
-    interpolate_lane<Q, Real>(U, base, ix, iy, iz, sB, sG, comp<C>(uv, c), g[0], g[1], g[2]);
+    interpolate_colloc<Q, Real>(U, base, ix, iy, iz, sB, sD, comp<C>(uv, c), g[0], g[1], g[2]);
     for (int j = 0; j < 3; j++) comp<C>(ug, c)[j] = g[j];
     if constexpr (MODE == JVP) {
       Real dU = valid ? a.du[c * a.num_nodes + node] : Real(0);
-      interpolate_lane<Q, Real>(dU, base, ix, iy, iz, sB, sG, comp<C>(dv, c), g[0], g[1], g[2]);
+      interpolate_colloc<Q, Real>(dU, base, ix, iy, iz, sB, sD, comp<C>(dv, c), g[0], g[1], g[2]);
       for (int j = 0; j < 3; j++) comp<C>(dg, c)[j] = g[j];
     }
   }
@@ -351,7 +408,7 @@ __global__ void __launch_bounds__(128) domain_kernel(DomainArgs<Real> a, QFMaker
 #pragma unroll
       for (int k = 0; k < 3; k++) f[k] = dvol * (fp[0] * Ji[k][0] + fp[1] * Ji[k][1] + fp[2] * Ji[k][2]);
     }
-    Real r = integrate_lane<Q, HS, HF, Real>(s, f[0], f[1], f[2], base, ix, iy, iz, sB, sG);
+    Real r = integrate_colloc<Q, HS, HF, Real>(s, f[0], f[1], f[2], base, ix, iy, iz, sB, sD);
     if (valid) out_e[c * NQ + qi] = r;
   }
 }
@@ -494,13 +551,15 @@ __global__ void __launch_bounds__(128) shape_jvp_kernel(DomainArgs<double> a, QF
 }
 
 /// L[c * N + node] (+)= sum over the node's (element, local node) pairs, in
-/// element order, of E[(e * C + c) * NPE + local].  One thread per node.
+/// element order, of E[(e * C + c) * NPE + local], for the nodes
+/// [node_begin, node_end).  One thread per node.
 template <int C, int NPE, typename Real>
 __global__ void __launch_bounds__(256) scatter_kernel(const Real* __restrict__ E, const int32_t* __restrict__ node_ptr,
                                                       const int32_t* __restrict__ node_ent, Real* __restrict__ out,
-                                                      int64_t num_nodes, bool accumulate) {
-  int64_t n = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (n >= num_nodes) return;
+                                                      int64_t num_nodes, bool accumulate, int64_t node_begin,
+                                                      int64_t node_end) {
+  const int64_t n = node_begin + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (n >= node_end) return;
   int32_t b = node_ptr[n], end = node_ptr[n + 1];
   Real acc[C];
 #pragma unroll
@@ -980,13 +1039,69 @@ struct TangentShape {
   /// boundary and can be moved by a bulk copy
   template <int NQ>
   static constexpr int64_t stride = (int64_t(size) * NQ + 3) / 4 * 4;
-  /// the same for the FP16 copy (multiples of 8 halves = 16 bytes)
+  /// row and column of entry m of the per-point block (the inverse of index)
+  static SFX_HDI constexpr int row_of(int m) {
+    if (!packed) return m / cols;
+    int r = 0;
+    while (m >= cols - r) {
+      m -= cols - r;
+      r++;
+    }
+    return r;
+  }
+  static SFX_HDI constexpr int col_of(int m) {
+    if (!packed) return m % cols;
+    int r = 0;
+    while (m >= cols - r) {
+      m -= cols - r;
+      r++;
+    }
+    return r + m;
+  }
+  /// entry pairs per point of the FP16 copy
+  static constexpr int pairs = (size + 1) / 2;
+  /// the FP16 copy stores entries (2j, 2j + 1) of a point next to each other
+  /// (one half2 per lane and pair): position of entry m of point q in an
+  /// element's block
   template <int NQ>
-  static constexpr int64_t stride16 = (int64_t(size) * NQ + 7) / 8 * 8;
+  static SFX_HDI constexpr int64_t pos16(int m, int q) {
+    return (int64_t(m / 2) * NQ + q) * 2 + (m & 1);
+  }
+  /// the same for the FP16 copy (pairs x NQ half2, multiples of 8 halves = 16 bytes)
+  template <int NQ>
+  static constexpr int64_t stride16 = (int64_t(pairs) * 2 * NQ + 7) / 8 * 8;
   /// entries per element block in storage type TS
   template <int NQ, typename TS>
   static constexpr int64_t stride_of = sizeof(TS) == 2 ? stride16<NQ> : stride<NQ>;
 };
+
+/// accumulate entry M (value d) of a point's block into out = D in
+/// (TRANSPOSE: D^T in); a packed symmetric entry counts for (r, k) and (k, r)
+template <typename Shape, bool TRANSPOSE, int M>
+SFX_HDI void tangent_entry(float d, const float* in, float* out) {
+  constexpr int r = Shape::row_of(M), k = Shape::col_of(M);
+  if constexpr (Shape::packed) {
+    out[r] += d * in[k];
+    if constexpr (k != r) out[k] += d * in[r];
+  } else if constexpr (TRANSPOSE) {
+    out[k] += d * in[r];
+  } else {
+    out[r] += d * in[k];
+  }
+}
+
+/// out (+)= D in (TRANSPOSE: D^T in) from the FP16 copy, one half2 load per
+/// entry pair (entries 2J, 2J + 1 of this point, pair stride NQ)
+template <typename Shape, bool TRANSPOSE, int NQ, int... J>
+SFX_HDI void apply_pairs16(const __half2* D2, const float* in, float* out, std::integer_sequence<int, J...>) {
+  auto pair = [&](auto j) {
+    constexpr int jj = decltype(j)::value;
+    const float2 d = __half22float2(D2[jj * NQ]);
+    tangent_entry<Shape, TRANSPOSE, 2 * jj>(d.x, in, out);
+    if constexpr (2 * jj + 1 < Shape::size) tangent_entry<Shape, TRANSPOSE, 2 * jj + 1>(d.y, in, out);
+  };
+  (pair(std::integral_constant<int, J>{}), ...);
+}
 
 /// out = D in (TRANSPOSE: D^T in) for one point's block, read with stride NQ
 /// from Dq (this lane's point).  A packed symmetric block is read once per
@@ -1156,7 +1271,9 @@ __global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QF
           if (!ShapeP::packed || ci <= k) {
             const int64_t in_block = int64_t(ShapeP::index(ci, k)) * NQ + qi;
             if (D32) D32[e * ShapeP::template stride<NQ> + in_block] = float(v);
-            if (D16) D16[e * ShapeP::template stride16<NQ> + in_block] = __float2half_rn(float(v));
+            if (D16)
+              D16[e * ShapeP::template stride16<NQ> + ShapeP::template pos16<NQ>(ShapeP::index(ci, k), qi)] =
+                  __float2half_rn(float(v));
           }
         }
       }
@@ -1184,7 +1301,9 @@ __global__ void __launch_bounds__(128) linearize_kernel(DomainArgs<double> a, QF
           if (!ShapeP::packed || rr <= k) {
             const int64_t in_block = int64_t(ShapeP::index(rr, k)) * NQ + qi;
             if (D32) D32[e * ShapeP::template stride<NQ> + in_block] = float(v);
-            if (D16) D16[e * ShapeP::template stride16<NQ> + in_block] = __float2half_rn(float(v));
+            if (D16)
+              D16[e * ShapeP::template stride16<NQ> + ShapeP::template pos16<NQ>(ShapeP::index(rr, k), qi)] =
+                  __float2half_rn(float(v));
           }
         }
         if (!have_res) res_f[ci][kd] = dvol * (fv[0] * Ji[kd][0] + fv[1] * Ji[kd][1] + fv[2] * Ji[kd][2]);
@@ -1227,11 +1346,11 @@ __global__ void __launch_bounds__(128) jvp_stored_kernel(const Real* __restrict_
   const bool valid = slot && e < num_elements;
   const int ix = qi % Q, iy = (qi / Q) % Q, iz = qi / (Q * Q);
 
-  __shared__ Real sB[Q][Q], sG[Q][Q];
+  __shared__ Real sB[Q][Q], sD[Q][Q];
   if (threadIdx.x < Q * Q) {
     int i = threadIdx.x / Q, j = threadIdx.x % Q;
     sB[i][j] = Real(basis_table<P>().B[i][j]);
-    sG[i][j] = Real(basis_table<P>().G[i][j]);
+    sD[i][j] = Real(basis_table<P>().D[i][j]);
   }
   __syncthreads();
 
@@ -1244,7 +1363,7 @@ __global__ void __launch_bounds__(128) jvp_stored_kernel(const Real* __restrict_
   for (int c = 0; c < C; c++) {
     Real U = valid ? du[c * num_nodes + node] : Real(0);
     Real v, g0, g1, g2;
-    interpolate_lane<Q, Real>(U, base, ix, iy, iz, sB, sG, v, g0, g1, g2);
+    interpolate_colloc<Q, Real>(U, base, ix, iy, iz, sB, sD, v, g0, g1, g2);
     if constexpr (VI) din[c] = v;
     constexpr int off = VI ? C : 0;
     din[off + 3 * c + 0] = g0;
@@ -1258,8 +1377,8 @@ __global__ void __launch_bounds__(128) jvp_stored_kernel(const Real* __restrict_
 #pragma unroll
   for (int c = 0; c < C; c++) {
     Real s = HS ? dout[HS ? c : 0] : Real(0);
-    Real r = integrate_lane<Q, HS, true, Real>(s, dout[roff + 3 * c], dout[roff + 3 * c + 1], dout[roff + 3 * c + 2],
-                                               base, ix, iy, iz, sB, sG);
+    Real r = integrate_colloc<Q, HS, true, Real>(s, dout[roff + 3 * c], dout[roff + 3 * c + 1], dout[roff + 3 * c + 2],
+                                               base, ix, iy, iz, sB, sD);
     if (valid) out_e[(e * C + c) * NQ + qi] = r;
   }
 }
@@ -1293,11 +1412,11 @@ __global__ void __launch_bounds__(128) jvp_stored_transpose_kernel(const Real* _
   const bool valid = slot && e < num_elements;
   const int ix = qi % Q, iy = (qi / Q) % Q, iz = qi / (Q * Q);
 
-  __shared__ Real sB[Q][Q], sG[Q][Q];
+  __shared__ Real sB[Q][Q], sD[Q][Q];
   if (threadIdx.x < Q * Q) {
     int i = threadIdx.x / Q, j = threadIdx.x % Q;
     sB[i][j] = Real(basis_table<P>().B[i][j]);
-    sG[i][j] = Real(basis_table<P>().G[i][j]);
+    sD[i][j] = Real(basis_table<P>().D[i][j]);
   }
   __syncthreads();
 
@@ -1308,7 +1427,7 @@ __global__ void __launch_bounds__(128) jvp_stored_transpose_kernel(const Real* _
   for (int c = 0; c < C; c++) {
     Real V = valid ? v[c * num_nodes + node] : Real(0);
     Real val, g0, g1, g2;
-    interpolate_lane<Q, Real>(V, base, ix, iy, iz, sB, sG, val, g0, g1, g2);
+    interpolate_colloc<Q, Real>(V, base, ix, iy, iz, sB, sD, val, g0, g1, g2);
     if constexpr (HS) vin[c] = val;
     vin[roff + 3 * c + 0] = g0;
     vin[roff + 3 * c + 1] = g1;
@@ -1321,8 +1440,8 @@ __global__ void __launch_bounds__(128) jvp_stored_transpose_kernel(const Real* _
 #pragma unroll
   for (int c = 0; c < C; c++) {
     Real s = VI ? vout[VI ? c : 0] : Real(0);
-    Real r = integrate_lane<Q, VI, true, Real>(s, vout[coff + 3 * c], vout[coff + 3 * c + 1], vout[coff + 3 * c + 2],
-                                               base, ix, iy, iz, sB, sG);
+    Real r = integrate_colloc<Q, VI, true, Real>(s, vout[coff + 3 * c], vout[coff + 3 * c + 1], vout[coff + 3 * c + 2],
+                                               base, ix, iy, iz, sB, sD);
     if (valid) out_e[(e * C + c) * NQ + qi] = r;
   }
 }
@@ -1358,12 +1477,12 @@ __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float*
   extern __shared__ __align__(128) unsigned char sfx_dyn_smem[];
   TS* ring = reinterpret_cast<TS*>(sfx_dyn_smem);                                       // [WARPS][STAGES][ES]
   uint64_t* bars = reinterpret_cast<uint64_t*>(sfx_dyn_smem + size_t(WARPS) * STAGES * BYTES);  // [WARPS][STAGES]
-  __shared__ float sB[Q][Q], sG[Q][Q];
+  __shared__ float sB[Q][Q], sD[Q][Q];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (threadIdx.x < Q * Q) {
     const int i = threadIdx.x / Q, j = threadIdx.x % Q;
     sB[i][j] = float(basis_table<P>().B[i][j]);
-    sG[i][j] = float(basis_table<P>().G[i][j]);
+    sD[i][j] = float(basis_table<P>().D[i][j]);
   }
   TS* my_ring = ring + size_t(wid) * STAGES * ES;
   uint64_t* my_bars = bars + wid * STAGES;
@@ -1417,7 +1536,7 @@ __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float*
 #pragma unroll
     for (int c = 0; c < C; c++) {
       float v, g0, g1, g2;
-      interpolate_lane<Q, float>(du_cur[c], 0, ix, iy, iz, sB, sG, v, g0, g1, g2);
+      interpolate_colloc<Q, float>(du_cur[c], 0, ix, iy, iz, sB, sD, v, g0, g1, g2);
       if constexpr (IN_VALUE) din[c] = v;
       constexpr int off = IN_VALUE ? C : 0;
       din[off + 3 * c + 0] = g0;
@@ -1431,7 +1550,13 @@ __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float*
     }
     const TS* Dq = my_ring + s * ES + qi;
     float dout[NOUT];
-    if constexpr (Shape::packed) {
+    if constexpr (std::is_same<TS, __half>::value) {
+      // FP16 copy: one half2 (entries 2j, 2j + 1 of this point) per load
+      const __half2* D2 = reinterpret_cast<const __half2*>(my_ring + s * ES) + qi;
+#pragma unroll
+      for (int r = 0; r < NOUT; r++) dout[r] = 0.f;
+      apply_pairs16<Shape, TRANSPOSE, NQ>(D2, din, dout, std::make_integer_sequence<int, Shape::pairs>{});
+    } else if constexpr (Shape::packed) {
 #pragma unroll
       for (int r = 0; r < NOUT; r++) dout[r] = 0.f;
 #pragma unroll
@@ -1466,8 +1591,8 @@ __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float*
 #pragma unroll
     for (int c = 0; c < C; c++) {
       const float src = OUT_VALUE ? dout[OUT_VALUE ? c : 0] : 0.f;
-      const float r = integrate_lane<Q, OUT_VALUE, true, float>(src, dout[roff + 3 * c], dout[roff + 3 * c + 1],
-                                                                dout[roff + 3 * c + 2], 0, ix, iy, iz, sB, sG);
+      const float r = integrate_colloc<Q, OUT_VALUE, true, float>(src, dout[roff + 3 * c], dout[roff + 3 * c + 1],
+                                                                dout[roff + 3 * c + 2], 0, ix, iy, iz, sB, sD);
       if (lane_ok) out_e[(e * C + c) * NQ + qi] = r;
     }
     // rotate the gather pipeline (its loads had this element's work to land)

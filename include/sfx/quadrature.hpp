@@ -54,6 +54,23 @@ SFX_HDI constexpr void gll_basis(int n, int k, double x, double& phi, double& dp
   dphi = d;
 }
 
+/// Derivative at Gauss point i of the Lagrange polynomial j on the n Gauss
+/// points (the collocated derivative matrix, equal to G B^-1: a degree n-1
+/// field is fixed by its n point values, so differentiating those values is
+/// exact).
+SFX_HDI constexpr double gl_lagrange_dphi(int n, int i, int j) {
+  double v = 1.0, d = 0.0;
+  const double x = gl_point(n, i), xj = gl_point(n, j);
+  for (int m = 0; m < n; m++) {
+    if (m == j) continue;
+    const double xm = gl_point(n, m);
+    const double term = (x - xm) / (xj - xm);
+    d = d * term + v / (xj - xm);
+    v = v * term;
+  }
+  return d;
+}
+
 /// B[q][k] = phi_k(x_q), G[q][k] = phi_k'(x_q) on the (p+1)-point rule.
 SFX_HDI constexpr double basis_B(int p, int q, int k) {
   double phi = 0, dphi = 0;
@@ -71,6 +88,7 @@ template <int P>
 struct BasisTable {
   double B[P + 1][P + 1];
   double G[P + 1][P + 1];
+  double D[P + 1][P + 1];  // collocated derivative at the Gauss points, D[q][j] = l_j'(x_q)
 };
 
 template <int P>
@@ -82,6 +100,7 @@ constexpr BasisTable<P> make_basis_table() {
       gll_basis(P + 1, k, gl_point(P + 1, q), phi, dphi);
       t.B[q][k] = phi;
       t.G[q][k] = dphi;
+      t.D[q][k] = gl_lagrange_dphi(P + 1, q, k);
     }
   return t;
 }

@@ -45,6 +45,7 @@ SIGNATURES = {
     "sfx_linearize": (_c.c_int, [_vp, _c.c_double, _vp, _vp, _vp]),
     "sfx_form_set_jvp_mode": (_c.c_int, [_vp, _c.c_int]),
     "sfx_jvp": (_c.c_int, [_vp, _vp, _vp, _vp]),
+    "sfx_jvp_host": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "sfx_set_param_field": (_c.c_int, [_vp, _c.c_int, _vp, _c.c_int]),
     "sfx_form_set_tangent_storage": (_c.c_int, [_vp, _c.c_int]),
     "sfx_jvp_transpose": (_c.c_int, [_vp, _vp, _vp, _vp]),

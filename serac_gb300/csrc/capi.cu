@@ -25,11 +25,13 @@ int fail(int code, const std::string& msg) {
 namespace {
 
 template <int C, int NPE, typename Real>
-int scatter(const sfx_form_s& f, const Real* E, Real* out, bool accumulate, cudaStream_t s) {
-  if (f.nnodes == 0) return SFX_OK;
-  unsigned blocks = unsigned((f.nnodes + 255) / 256);
+int scatter(const sfx_form_s& f, const Real* E, Real* out, bool accumulate, cudaStream_t s, int64_t n0 = 0,
+            int64_t n1 = -1) {
+  if (n1 < 0) n1 = f.nnodes;
+  if (n1 <= n0) return SFX_OK;
+  unsigned blocks = unsigned((n1 - n0 + 255) / 256);
   sfx::kernels::scatter_kernel<C, NPE, Real>
-      <<<blocks, 256, 0, s>>>(E, f.node_ptr.p, f.node_ent.p, out, f.nnodes, accumulate);
+      <<<blocks, 256, 0, s>>>(E, f.node_ptr.p, f.node_ent.p, out, f.nnodes, accumulate, n0, n1);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("scatter launch: ") + cudaGetErrorString(err));
   return SFX_OK;
@@ -58,6 +60,15 @@ int check_form(sfx_form f) {
 
 int scatter_evector(const sfx_form_s& f, const double* E, double* out, bool accumulate, cudaStream_t s) {
   return scatter_dispatch<double>(f, E, out, accumulate, s);
+}
+
+int scatter_evector_range(const sfx_form_s& f, const double* E, double* out, int64_t n0, int64_t n1,
+                          cudaStream_t s) {
+  if (f.p == 1 && f.c == 1) return scatter<1, 8, double>(f, E, out, false, s, n0, n1);
+  if (f.p == 1 && f.c == 3) return scatter<3, 8, double>(f, E, out, false, s, n0, n1);
+  if (f.p == 2 && f.c == 1) return scatter<1, 27, double>(f, E, out, false, s, n0, n1);
+  if (f.p == 2 && f.c == 3) return scatter<3, 27, double>(f, E, out, false, s, n0, n1);
+  return fail(SFX_ERR_UNSUPPORTED, "unsupported (order, components)");
 }
 
 int scatter_evector3(const sfx_form_s& f, const double* E, double* out, bool accumulate, cudaStream_t s) {

@@ -18,10 +18,16 @@ int launch_element_matrix(const sfx_form_s& f, const DomainIntegral& di, bool di
                           int64_t e1, cudaStream_t s);
 // scatter-add of an E-vector [e][c][node] into an L-vector
 int scatter_evector(const sfx_form_s& f, const double* E, double* out, bool accumulate, cudaStream_t s);
+/// out[c * N + n] = the element sum of E for the nodes [n0, n1) only (no accumulate)
+int scatter_evector_range(const sfx_form_s& f, const double* E, double* out, int64_t n0, int64_t n1,
+                          cudaStream_t s);
 
 // stored-tangent path: linearise (store D, optionally element residuals) and apply D
 int launch_linearize(const sfx_form_s& f, DomainIntegral& di, double* res_e, cudaStream_t s);
 int launch_jvp_stored(const sfx_form_s& f, const DomainIntegral& di, const double* du, double* E, cudaStream_t s);
+/// the FP64 stored-tangent action over the elements [e0, e1) only (E indexed globally)
+int launch_jvp_stored_range(const sfx_form_s& f, const DomainIntegral& di, const double* du, double* E, int64_t e0,
+                            int64_t e1, cudaStream_t s);
 // boundary integrals: add face contributions to out (mode 0 residual at u, 2 action on du)
 int launch_boundary(const sfx_form_s& f, int mode, const double* u, const double* du, double* out, double t,
                     cudaStream_t s);

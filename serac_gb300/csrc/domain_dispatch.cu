@@ -249,25 +249,30 @@ struct StoredJvpFn {
   const Real* D;
   Real* E;
   cudaStream_t s;
+  int64_t e0 = 0, e1 = -1;  // element range [e0, e1) of the FP64 action (default: all)
   template <int C, typename State, typename Maker>
   int operator()() {
     constexpr int NQ = (P + 1) * (P + 1) * (P + 1);
     constexpr int EPW = 32 / NQ;
     using QF = decltype(Maker{}(nullptr));
     constexpr bool HS = kernels::tangent_has_source<C, State, QF>();
-    if (f.ne == 0) return SFX_OK;
+    const int64_t first = e0, last = e1 < 0 ? f.ne : e1;
+    if (last <= first) return SFX_OK;
     constexpr bool SYM = sym_of<Maker>::value;
     if constexpr (P == 2 && std::is_same<Real, float>::value) {
+      if (first != 0 || last != f.ne) return fail(SFX_ERR_UNSUPPORTED, "element ranges are FP64 only");
       const int rc = f.tangent16 ? launch_tma<C, HS, Maker::value_input, false, __half, SYM>(f, du, di.D16.p, E, s)
                                  : launch_tma<C, HS, Maker::value_input, false, float, SYM>(f, du, D, E, s);
       if (rc) return rc;
     } else {
       // the FP64 copy is stored full; the FP32 copy packed when symmetric
       constexpr bool SYMR = SYM && std::is_same<Real, float>::value;
-      int64_t warps = (f.ne + EPW - 1) / EPW;
+      using Shape = kernels::TangentShape<C, HS, Maker::value_input, SYMR>;
+      const int64_t n = last - first;
+      int64_t warps = (n + EPW - 1) / EPW;
       int64_t blocks = (warps * 32 + 127) / 128;
-      kernels::jvp_stored_kernel<P, C, HS, Maker::value_input, Real, SYMR>
-          <<<unsigned(blocks), 128, 0, s>>>(du, D, f.conn.p, E, f.nnodes, f.ne);
+      kernels::jvp_stored_kernel<P, C, HS, Maker::value_input, Real, SYMR><<<unsigned(blocks), 128, 0, s>>>(
+          du, D + first * Shape::template stride<NQ>, f.conn.p + first * NQ, E + first * C * NQ, f.nnodes, n);
     }
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("stored jvp launch: ") + cudaGetErrorString(err));
@@ -416,6 +421,13 @@ int launch_linearize(const sfx_form_s& f, DomainIntegral& di, double* res_e, cud
 int launch_jvp_stored(const sfx_form_s& f, const DomainIntegral& di, const double* du, double* E, cudaStream_t s) {
   if (f.p == 1) return visit_material(di.material, StoredJvpFn<1, double>{f, di, du, di.D64.p, E, s});
   if (f.p == 2) return visit_material(di.material, StoredJvpFn<2, double>{f, di, du, di.D64.p, E, s});
+  return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
+}
+
+int launch_jvp_stored_range(const sfx_form_s& f, const DomainIntegral& di, const double* du, double* E, int64_t e0,
+                            int64_t e1, cudaStream_t s) {
+  if (f.p == 1) return visit_material(di.material, StoredJvpFn<1, double>{f, di, du, di.D64.p, E, s, e0, e1});
+  if (f.p == 2) return visit_material(di.material, StoredJvpFn<2, double>{f, di, du, di.D64.p, E, s, e0, e1});
   return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
 }
 

@@ -126,6 +126,29 @@ struct MappedFlag {
     if (host) *static_cast<volatile int*>(host) = 0;
   }
 };
+/// Streams, events and device vectors of the Jacobian action between host
+/// buffers (sfx_jvp_host), created on its first call.
+struct HostPipe {
+  static constexpr int kMaxChunks = 8;
+  cudaStream_t h2d = nullptr, d2h = nullptr;
+  cudaEvent_t entry = nullptr;  // the caller's stream at the call: the copies start after its earlier work
+  cudaEvent_t in_ready[kMaxChunks] = {};
+  cudaEvent_t out_ready[kMaxChunks] = {};
+  int nevents = 0;
+  DeviceBuf<double> du, dr;
+  HostPipe() = default;
+  HostPipe(const HostPipe&) = delete;
+  HostPipe& operator=(const HostPipe&) = delete;
+  ~HostPipe() {
+    for (int i = 0; i < nevents; i++) {
+      cudaEventDestroy(in_ready[i]);
+      cudaEventDestroy(out_ready[i]);
+    }
+    if (entry) cudaEventDestroy(entry);
+    if (h2d) cudaStreamDestroy(h2d);
+    if (d2h) cudaStreamDestroy(d2h);
+  }
+};
 }  // namespace sfx_impl
 
 struct sfx_form_s {
@@ -179,4 +202,5 @@ struct sfx_form_s {
   sfx_impl::DeviceBuf<int32_t> col;
   sfx_impl::DeviceBuf<double> ke;  // element matrices scratch
   sfx_impl::DeviceBuf<double> kf;  // face matrices scratch
+  sfx_impl::HostPipe host_pipe;    // sfx_jvp_host
 };

@@ -65,7 +65,7 @@ template <int C, int NPE>
 int scatter_c(const sfx_form_s& f, const double* E, double* out, bool accumulate, cudaStream_t s) {
   if (f.nnodes == 0) return SFX_OK;
   sfx::kernels::scatter_kernel<C, NPE, double><<<unsigned((f.nnodes + 255) / 256), 256, 0, s>>>(
-      E, f.node_ptr.p, f.node_ent.p, out, f.nnodes, accumulate);
+      E, f.node_ptr.p, f.node_ent.p, out, f.nnodes, accumulate, int64_t(0), f.nnodes);
   const cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("scatter launch: ") + cudaGetErrorString(err));
   return SFX_OK;

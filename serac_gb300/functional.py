@@ -46,6 +46,13 @@ def _require(t, dtype, n, name):
         raise ValueError(f"{name} must be a contiguous {dtype} tensor with {n} entries")
 
 
+def _require_host(t, n, name):
+    if not isinstance(t, torch.Tensor) or t.device.type != "cpu":
+        raise TypeError(f"{name} must be a CPU tensor")
+    if t.dtype != torch.float64 or not t.is_contiguous() or t.numel() != n:
+        raise ValueError(f"{name} must be a contiguous float64 tensor with {n} entries")
+
+
 @dataclass(frozen=True)
 class H1:
     order: int
@@ -179,7 +186,16 @@ class Gradient:
         self.form = form
 
     def mult(self, du, out=None, stream=None):
+        """J du.  A CPU float64 du (and out) runs sfx_jvp_host: the copies to
+        and from the device are made inside, overlapped with the kernels
+        when the tensors are pinned."""
         f = self.form
+        if isinstance(du, torch.Tensor) and du.device.type == "cpu":
+            _require_host(du, f.ndofs, "du")
+            out = torch.empty_like(du) if out is None else out
+            _require_host(out, f.ndofs, "out")
+            _lib.call("sfx_jvp_host", f._h, _dptr(du), _dptr(out), _stream(stream))
+            return out
         if du.dtype == torch.float32:
             _require(du, torch.float32, f.ndofs, "du")
             out = torch.empty_like(du) if out is None else out

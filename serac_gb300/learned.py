@@ -234,19 +234,21 @@ def probe_pairs(setup, u, count, rng):
     return R.float(), X.float()
 
 
-def harvest(problems, order=2, options=None, probes_per_step=8, newton_pairs=True, max_newton_pairs=64, seed=0):
+def harvest(problems, order=2, options=None, probes_per_step=8, newton_pairs=True, max_newton_pairs=64, seed=0,
+            log=None):
     """Training pairs from the solver on each problem's load steps (warm
     start, Newton with the FP32-inner mixed-precision solve, state commit):
     every Newton step's (residual, correction) pair, and probes_per_step
     probe pairs at each converged step.  Returns float32 CUDA tensors
-    R, T [pairs, 3N] and F [pairs, 2N]."""
+    R, T [pairs, 3N] and F [pairs, 2N].  log(problems_done, pairs) is called
+    after every problem when given."""
     from .solver import SolverOptions as _SO
 
     opts = options or _SO.defaults(precond=JACOBI_CHEBYSHEV, mixed_precision=1, krylov_rel_tol=1e-6,
                                    max_krylov_iterations=1000)
     rng = np.random.default_rng(seed)
     Rs, Ts, Fs = [], [], []
-    for prob in problems:
+    for done, prob in enumerate(problems, 1):
         S = SolidSetup(prob, order)
         solver = NewtonSolver(S.f, opts)
         solver.set_essential(S.ess)
@@ -277,6 +279,8 @@ def harvest(problems, order=2, options=None, probes_per_step=8, newton_pairs=Tru
                 Ts.extend(X)
                 Fs.extend([S.features] * probes_per_step)
             S.commit(u)
+        if log is not None:
+            log(done, len(Rs))
     return torch.stack(Rs), torch.stack(Ts), torch.stack(Fs)
 
 

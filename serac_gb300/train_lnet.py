@@ -37,6 +37,9 @@ def main(argv=None):
                     help="compression reached after --steps (default: 0.02 for J2, 0.005 for Neo-Hookean)")
     ap.add_argument("--eval-seeds", default=None,
                     help="first:last held-out seeds: after training, solve them with and without the network")
+    ap.add_argument("--eval-fp64-seeds", default=None,
+                    help="first:last subset of the held-out seeds also solved by the FP64 methods (Chebyshev "
+                         "alone and the two-level step); default: all of --eval-seeds")
     ap.add_argument("--out", required=True)
     args = ap.parse_args(argv)
 
@@ -48,7 +51,13 @@ def main(argv=None):
     t0 = time.time()
     make = problem_factory(args.material, args.strain, args.steps)
     problems = [make(args.n, s) for s in range(lo, hi)]
-    R, T, F = L.harvest(problems, probes_per_step=args.probes)
+    n_prob = len(problems)
+
+    def progress(done, pairs):
+        if done % 32 == 0 or done == n_prob:
+            print(f"harvest {done}/{n_prob} problems, {pairs} pairs, {time.time() - t0:.0f} s", flush=True)
+
+    R, T, F = L.harvest(problems, probes_per_step=args.probes, log=progress)
     torch.cuda.synchronize()
     t_harvest = time.time() - t0
     grid = (2 * args.n + 1,) * 3
@@ -64,7 +73,7 @@ def main(argv=None):
             "lr": args.lr, "harvest_s": round(t_harvest, 1), "train_s": round(time.time() - t0, 1),
             "final_loss": hist[-1], "loss_history": [round(h, 4) for h in hist]}
     if args.eval_seeds:
-        info["evaluation"] = evaluate(net, args.n, args.eval_seeds, make)
+        info["evaluation"] = evaluate(net, args.n, args.eval_seeds, make, args.eval_fp64_seeds)
     with open(os.path.splitext(args.out)[0] + ".json", "w") as fh:
         json.dump(info, fh, indent=1)
     print(json.dumps(info))
@@ -82,11 +91,12 @@ def problem_factory(material, strain, steps):
     return lambda n, seed: L.j2_problem(n, seed, strain=st, steps=steps)
 
 
-def evaluate(net, n, seeds, make):
+def evaluate(net, n, seeds, make, fp64_seeds=None):
     """Held-out seeds: Krylov iterations and seconds of flexible GMRES with
     Jacobi-Chebyshev alone against the network's two-level step
-    (Chebyshev, network, Chebyshev), and of mixed precision against learned +
-    mixed precision; every pair must reach the same answer."""
+    (Chebyshev, network, Chebyshev) on the fp64_seeds subset (default: all),
+    and of mixed precision against learned + mixed precision on every seed;
+    every solve of a seed must reach the same answer."""
     import torch
 
     from . import learned as L
@@ -101,12 +111,17 @@ def evaluate(net, n, seeds, make):
         "learned_mixed": (SolverOptions.defaults(precond=LEARNED, mixed_precision=1, **tol), True),
     }
     lo, hi = (int(x) for x in seeds.split(":"))
-    totals = {k: {"krylov_iterations": 0, "seconds": 0.0} for k in variants}
+    flo, fhi = (int(x) for x in fp64_seeds.split(":")) if fp64_seeds else (lo, hi)
+    totals = {k: {"krylov_iterations": 0, "seconds": 0.0, "seeds": 0} for k in variants}
+    per_seed = []
     worst_diff = 0.0
     for seed in range(lo, hi):
         prob = make(n, seed)
         sols = {}
+        row = {"seed": seed}
         for name, (opts, use_net) in variants.items():
+            if name in ("chebyshev", "learned_two_level") and not flo <= seed < fhi:
+                continue
             S = L.SolidSetup(prob)
             solver = NewtonSolver(S.f, opts)
             solver.set_essential(S.ess)
@@ -116,17 +131,29 @@ def evaluate(net, n, seeds, make):
             t0 = time.perf_counter()
             u, tot = L.solve_load_steps(S, solver)
             torch.cuda.synchronize()
-            totals[name]["seconds"] += time.perf_counter() - t0
-            totals[name]["krylov_iterations"] += tot["krylov_iterations"] + tot["predictor_krylov_iterations"]
+            dt = time.perf_counter() - t0
+            its = tot["krylov_iterations"] + tot["predictor_krylov_iterations"]
+            totals[name]["seconds"] += dt
+            totals[name]["krylov_iterations"] += its
+            totals[name]["seeds"] += 1
+            row[name] = {"krylov_iterations": its, "seconds": round(dt, 3),
+                         "learned_fallbacks": tot.get("learned_fallbacks", 0),
+                         "learned_applications": tot.get("learned_applications", 0)}
             sols[name] = u
-        ref = sols["chebyshev"]
+        per_seed.append(row)
+        ref = sols.get("chebyshev", sols["mixed"])
         for u in sols.values():
             worst_diff = max(worst_diff, float(torch.linalg.norm(u - ref) / torch.linalg.norm(ref)))
-    return {"seeds": seeds, "n": n, "totals": totals, "max_rel_diff": worst_diff,
-            "iteration_ratio_two_level": totals["learned_two_level"]["krylov_iterations"]
-            / max(1, totals["chebyshev"]["krylov_iterations"]),
-            "time_ratio_two_level": totals["learned_two_level"]["seconds"] / totals["chebyshev"]["seconds"],
-            "time_ratio_learned_mixed": totals["learned_mixed"]["seconds"] / totals["mixed"]["seconds"]}
+    out = {"seeds": seeds, "fp64_seeds": f"{flo}:{fhi}", "n": n, "totals": totals, "max_rel_diff": worst_diff,
+           "time_ratio_learned_mixed": totals["learned_mixed"]["seconds"] / totals["mixed"]["seconds"],
+           "iteration_ratio_learned_mixed": totals["learned_mixed"]["krylov_iterations"]
+           / max(1, totals["mixed"]["krylov_iterations"]),
+           "per_seed": per_seed}
+    if totals["chebyshev"]["seeds"]:
+        out["iteration_ratio_two_level"] = (totals["learned_two_level"]["krylov_iterations"]
+                                            / max(1, totals["chebyshev"]["krylov_iterations"]))
+        out["time_ratio_two_level"] = totals["learned_two_level"]["seconds"] / totals["chebyshev"]["seconds"]
+    return out
 
 
 if __name__ == "__main__":
