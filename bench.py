@@ -396,6 +396,14 @@ def run_sfx(args, rank, world):
     t_rec = timed(lambda: grad.mult(du, dr), k_rec)
     t_rec32 = timed(lambda: grad.mult(du32, dr32), k_rec)
     f.set_jvp_mode(f.STORED_TANGENT)
+    # ---- the FP32 action on the FP16 copy of the tangent (entry pairs, FP32 accumulation)
+    f.set_tangent_storage(f.TANGENT_F16)
+    f.linearize(0.0, u)
+    for _ in range(max(1, args.warmup)):
+        grad.mult(du32, dr32)
+    t_fp16 = timed(lambda: grad.mult(du32, dr32), args.steps)
+    t_elem16 = timed(lambda: grad.element_action(du32, dE32), args.steps)
+    f.set_tangent_storage(f.TANGENT_F32)
     f.linearize(0.0, u)
 
     # ---- end to end through the C ABI with host buffers
@@ -447,6 +455,11 @@ def run_sfx(args, rank, world):
     roof32 = roofline_hbm("sfx::kernels::jvp_stored_tma_kernel<3,false,false,16,2,false,float,true> (FP32, packed "
                           "symmetric tangent, bulk-copy staged)", alg32, t_k32, hbm_peak, peak_src,
                           traffic.get("jvp_stored_tma_f32"))
+    t_k16 = statistics.mean(t_elem16)
+    alg16 = 4 * ndofs + 46 * 2 * nq + 4 * 81 * ne
+    roof16 = roofline_hbm("sfx::kernels::jvp_stored_tma_kernel<3,false,false,16,4,false,__half,true> (FP32 action, "
+                          "FP16 packed symmetric tangent as entry pairs, bulk-copy staged)", alg16, t_k16, hbm_peak,
+                          peak_src, None)
     # residual: compulsory traffic (read u, write r: 16 B per DOF; vertices
     # 24 B; two parameters per element 16 B) as the algorithmic bytes
     t_r = statistics.mean(t_res)
@@ -482,6 +495,8 @@ def run_sfx(args, rank, world):
         "compute_roofline": compute,
         "jv_fp32": {"value": ndofs * args.steps / sum(t_fp32) / 1e9, "unit": UNIT, "dtype": "f32",
                     "ms_per_step": statistics.mean(t_fp32) * 1e3, "roofline": roof32},
+        "jv_fp16_tangent": {"value": ndofs * args.steps / sum(t_fp16) / 1e9, "unit": UNIT, "dtype": "f32 (f16 tangent)",
+                            "ms_per_step": statistics.mean(t_fp16) * 1e3, "roofline": roof16},
         "residual": {"value": ndofs * args.steps / sum(t_res) / 1e9, "unit": UNIT, "dtype": "f64",
                      "ms_per_step": t_r * 1e3, "roofline": roof_res,
                      "note": "R(u): fused element kernel (Neo-Hookean q-function, FP64) + node-owner scatter"},
