@@ -1,4 +1,5 @@
-// sfx — bulk asynchronous copies (cp.async.bulk, the untiled TMA path) and
+// sfx — bulk asynchronous copies (cp.async.bulk: the untiled TMA path, and
+// cp.async.bulk.tensor: tiled loads through a tensor map) and
 // shared-memory mbarriers for sm_90+ / sm_103a, as inline PTX.  Every wait is
 // bounded: mbar_wait gives up after kMaxMbarPolls polls and reports failure,
 // so a kernel can record an error and return instead of spinning forever.
@@ -32,6 +33,19 @@ __device__ inline void copy_g2s(void* dst, const void* src, uint32_t bytes, uint
   asm volatile(
       "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
       "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+/// tiled tensor load (cp.async.bulk.tensor, 5-D, the TMA tile path) of the
+/// box at coordinates (c0..c4) of the tensor map `map` (a __grid_constant__
+/// kernel parameter or global memory) into shared memory, completing on
+/// `bar`.  c0 * element size must be a multiple of 16 bytes; the other
+/// coordinates may lie outside the tensor (those elements read zero).
+__device__ inline void tma_load_5d(void* dst, const void* map, int c0, int c1, int c2, int c3, int c4,
+                                   uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+      "%6}], [%7];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(smem_addr(bar))
       : "memory");
 }
 /// one poll: whether the phase of parity `parity` has completed

@@ -12,6 +12,7 @@
 // nodes per direction (the Q2 node grid of an n^3 mesh is (2n+1)^3).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -182,6 +183,165 @@ __global__ void __launch_bounds__(128, 4) conv3_fwd_umma(Grid3 g, const __nv_bfl
     // the MMAs already issued (bounded) before the tensor memory is released
     (void)bulk::mbar_wait(&bars[0], 0u);
     (void)bulk::mbar_wait(&bars[1], 0u);
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  if (warp == 0) umma::tmem_dealloc(tmem, L::NCOLS);
+}
+
+/// Brick of input nodes staged by conv3_fwd_brick: the 8 x 16 x BZ output
+/// nodes of a block plus a one-node halo, (10 x 18 x (BZ + 2)) nodes, stored
+/// as 2 * CIN / 16 slabs of 8 channels, each slab [z][y][x] x 16 bytes (what
+/// one tiled TMA load of an 8-channel box writes).
+template <int CIN, int BZ>
+struct BrickLayout {
+  static constexpr int BX = 8, BY = 16;
+  static constexpr int XP = BX + 2, YP = BY + 2, ZP = BZ + 2;
+  static constexpr int NODES = XP * YP * ZP;
+  static constexpr int KC = CIN / 16;                      // 16-channel K-steps
+  static constexpr uint32_t SLAB = uint32_t(NODES) * 16;    // bytes of one 8-channel slab
+  static constexpr uint32_t BRICK = SLAB * 2 * KC;
+};
+
+/// output planes per block: 4 for the 16-channel inputs of the finest level,
+/// 2 for the wider (coarser) layers, so the brick and the weights of all 27
+/// taps fit in shared memory
+__host__ __device__ constexpr int brick_bz(int cin) { return cin == 16 ? 4 : 2; }
+
+template <int CIN, int COUT>
+struct BrickConvSmem {
+  static constexpr int BZ = brick_bz(CIN);
+  using Brick = BrickLayout<CIN, BZ>;
+  static constexpr uint32_t W_BYTES = 27u * COUT * CIN * 2;  // all taps, [tap][kc][half][co] x 16 bytes
+  static constexpr size_t bytes = size_t(Brick::BRICK) + W_BYTES;
+  static constexpr uint32_t cols = uint32_t(BZ) * COUT;       // BZ accumulators of COUT FP32 columns
+  static constexpr uint32_t NCOLS = cols <= 32 ? 32 : cols <= 64 ? 64 : cols <= 128 ? 128 : 256;
+};
+
+/// Forward 3x3x3 convolution as an implicit GEMM on the 5th-generation tensor
+/// cores with a shared-memory brick: each block owns 8 x 16 x BZ output nodes
+/// of one sample.  One thread loads the brick with its halo by tiled TMA
+/// (2 CIN / 16 loads of an 8-channel box through the tensor map `xmap` of the
+/// activations [sample][z][y][x][CIN]; halo nodes outside the grid read
+/// zero), while the block copies the weights of all 27 taps into K-major core
+/// matrices.  For a tap (dx, dy, dz) the A operand of output plane zt (128
+/// rows = 8 x by 16 y nodes) is then the brick itself read through a shifted
+/// descriptor: row group y starts at node ((zt + dz + 1) 18 + y + dy + 1) 10 +
+/// dx + 1 (leading byte offset = one slab between channel halves, stride
+/// byte offset = one brick row of 10 nodes between row groups), so no tap
+/// is ever gathered.  One thread issues the 27 x BZ x CIN / 16 MMAs into BZ
+/// tensor-memory accumulators and commits them; the epilogue reads them with
+/// tcgen05.ld (warp w: rows 32w..32w+31 of each plane), adds the bias,
+/// applies the activation and stores BF16 (or FP32 into y_f32).  W: [COUT]
+/// [27][CIN] bf16, bias: [COUT] f32 (may be null), y: [node][COUT] per sample.
+/// Every wait is bounded: on a timeout the block sets *err, waits (bounded)
+/// for its copies and MMAs in flight and frees its tensor memory.
+template <int CIN, int COUT, int ACT>
+__global__ void __launch_bounds__(128, 1) conv3_fwd_brick(const __grid_constant__ CUtensorMap xmap, Grid3 g,
+                                                       const __nv_bfloat16* __restrict__ W,
+                                                       const float* __restrict__ bias, __nv_bfloat16* __restrict__ y,
+                                                       float* __restrict__ y_f32, int* __restrict__ err) {
+  static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 64, "channel counts");
+  using L = BrickConvSmem<CIN, COUT>;
+  using Bk = typename L::Brick;
+  constexpr int BZ = L::BZ;
+  extern __shared__ __align__(128) unsigned char sfx_conv_smem[];
+  __shared__ uint64_t bar_load, bar_mma;
+  __shared__ uint32_t tmem_base;
+  unsigned char* brick = sfx_conv_smem;
+  unsigned char* wsm = sfx_conv_smem + Bk::BRICK;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nbx = (g.nx + Bk::BX - 1) / Bk::BX, nby = (g.ny + Bk::BY - 1) / Bk::BY;
+  const int bx = int(blockIdx.x % unsigned(nbx)), by = int((blockIdx.x / unsigned(nbx)) % unsigned(nby));
+  const int bz = int(blockIdx.x / unsigned(nbx * nby));
+  const int sample = int(blockIdx.y);
+  const int64_t N = g.nodes();
+  if (threadIdx.x == 0) {
+    bulk::mbar_init(&bar_load, 1);
+    bulk::mbar_init(&bar_mma, 1);
+    bulk::fence_mbar_init();
+  }
+  if (warp == 0) {
+    umma::tmem_alloc(&tmem_base, L::NCOLS);
+    umma::tmem_relinquish();
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = tmem_base;
+  if (threadIdx.x == 0) {
+    bulk::mbar_arrive_expect_tx(&bar_load, Bk::BRICK);
+#pragma unroll
+    for (int sl = 0; sl < 2 * Bk::KC; sl++)
+      bulk::tma_load_5d(brick + uint32_t(sl) * Bk::SLAB, &xmap, sl * 8, bx * Bk::BX - 1, by * Bk::BY - 1, bz * BZ - 1,
+                        sample, &bar_load);
+  }
+  // weights W[co][tap][ci] -> [tap][ci / 8][co] x 16 bytes (K-major core matrices per tap and K-step)
+  constexpr int GPN = CIN / 8;
+  const uint4* wsrc = reinterpret_cast<const uint4*>(W);
+  for (int i = threadIdx.x; i < COUT * 27 * GPN; i += blockDim.x) {
+    const int g8 = i % GPN, tap = (i / GPN) % 27, co = i / (GPN * 27);
+    *reinterpret_cast<uint4*>(wsm + ((uint32_t(tap) * GPN + g8) * COUT + co) * 16u) = wsrc[i];
+  }
+  bulk::fence_proxy_async_smem();  // the weights are read by the tensor core (async proxy)
+  bool ok = __syncthreads_and(bulk::mbar_wait(&bar_load, 0u));
+  umma::fence_after_sync();
+  if (ok && threadIdx.x == 0) {
+    constexpr uint32_t idesc = umma::idesc_bf16_f32(128, COUT);
+    for (int tap = 0; tap < 27; tap++) {
+      const int dx = tap % 3 - 1, dy = (tap / 3) % 3 - 1, dz = tap / 9 - 1;
+#pragma unroll
+      for (int zt = 0; zt < BZ; zt++) {
+        const uint32_t n0 = uint32_t(((zt + dz + 1) * Bk::YP + (dy + 1)) * Bk::XP + (dx + 1));
+#pragma unroll
+        for (int kc = 0; kc < Bk::KC; kc++) {
+          const uint64_t adesc = umma::smem_desc(brick + uint32_t(2 * kc) * Bk::SLAB + n0 * 16u, Bk::SLAB, Bk::XP * 16);
+          const uint64_t bdesc = umma::smem_desc(wsm + (uint32_t(tap) * GPN + 2 * kc) * COUT * 16u, COUT * 16, 128);
+          umma::mma_bf16(tmem + uint32_t(zt * COUT), adesc, bdesc, idesc, tap > 0 || kc > 0);
+        }
+      }
+    }
+    umma::commit(&bar_mma);
+  }
+  const bool issued = ok;
+  if (ok) ok = __syncthreads_and(bulk::mbar_wait(&bar_mma, 0u));
+  umma::fence_after_sync();
+  if (ok) {
+    const int r = 32 * warp + lane;  // row of every plane's tile: 8 x by 16 y
+    const int ox = bx * Bk::BX + (r & 7), oy = by * Bk::BY + (r >> 3);
+#pragma unroll
+    for (int zt = 0; zt < BZ; zt++) {
+      const int oz = bz * BZ + zt;
+      const bool inside = ox < g.nx && oy < g.ny && oz < g.nz;
+      const int64_t n = int64_t(sample) * N + (int64_t(oz) * g.ny + oy) * g.nx + ox;
+#pragma unroll
+      for (int c = 0; c < COUT; c += 8) {
+        float v[8];
+        umma::ld_x8(tmem + (uint32_t(32 * warp) << 16) + uint32_t(zt * COUT + c), v);
+        if (inside) {
+#pragma unroll
+          for (int i = 0; i < 8; i++) {
+            float t = v[i] + (bias ? bias[c + i] : 0.f);
+            if (ACT == ACT_RELU) t = t > 0.f ? t : 0.f;
+            v[i] = t;
+          }
+          if (y_f32) {
+#pragma unroll
+            for (int i = 0; i < 8; i++) y_f32[n * COUT + c + i] = v[i];
+          } else {
+            const uint4 pk = make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]),
+                                        pack_bf16x2(v[6], v[7]));
+            *reinterpret_cast<uint4*>(y + n * COUT + c) = pk;
+          }
+        }
+      }
+    }
+  } else {
+    if (threadIdx.x == 0) atomicExch(err, 1);
+    // the copies and MMAs in flight (bounded) before the tensor memory is released
+    (void)bulk::mbar_wait(&bar_load, 0u);
+    if (issued) (void)bulk::mbar_wait(&bar_mma, 0u);
   }
   umma::fence_before_sync();
   __syncthreads();

@@ -4,6 +4,8 @@
 // selects the sample); per-sample scales and losses stay on the device, so a
 // training step synchronises with the host once (to report the loss) and an
 // inference pass not at all.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -29,6 +31,11 @@ using sfx::nn::Grid3;
 using bf16 = __nv_bfloat16;
 
 namespace {
+
+#define SFX_TRY(call)                  \
+  do {                                 \
+    if (int rc_ = (call)) return rc_;  \
+  } while (0)
 
 inline unsigned nb(int64_t n, int b = 256) { return unsigned((n + b - 1) / b); }
 inline dim3 grid2(int64_t n, int batch, int b = 256) { return dim3(nb(n, b), unsigned(batch)); }
@@ -168,33 +175,71 @@ __global__ void adam(float* __restrict__ p, const float* __restrict__ g, float* 
 // --------------------------------------------------------- conv dispatch
 #define SFX_PAIRS(X) X(16, 16) X(16, 32) X(32, 32) X(32, 48) X(48, 48) X(48, 32) X(32, 16)
 
-// launch one staged convolution (the dynamic shared-memory limit is raised
-// once per instantiation)
-// the tensor-core (tcgen05) convolution: one block per 128 output nodes and sample
-template <int CI, int CO, int ACT>
-void launch_conv(Grid3 g, int batch, const bf16* x, const bf16* W, const float* b, bf16* y, float* y32, int* err,
-                 cudaStream_t s) {
-  using L = sfx::nn::UmmaConvSmem<CI, CO>;
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(sfx::nn::conv3_fwd_umma<CI, CO, ACT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         int(L::bytes));
-    configured = true;
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
+// (no link-time dependency on libcuda)
+PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    looked_up = true;
   }
-  const dim3 blocks(unsigned((g.nodes() + 127) / 128), unsigned(batch));
-  sfx::nn::conv3_fwd_umma<CI, CO, ACT><<<blocks, 128, L::bytes, s>>>(g, x, W, b, y, y32, err);
+  return fn;
 }
 
-void conv_fwd(int ci, int co, bool relu, Grid3 g, int batch, const bf16* x, const bf16* W, const float* b, bf16* y,
-              float* y32, int* err, cudaStream_t s) {
-#define SFX_CONV(CI, CO)                                                                \
-  if (ci == CI && co == CO) {                                                           \
-    if (relu) launch_conv<CI, CO, sfx::nn::ACT_RELU>(g, batch, x, W, b, y, y32, err, s); \
-    else launch_conv<CI, CO, sfx::nn::ACT_NONE>(g, batch, x, W, b, y, y32, err, s);      \
-    return;                                                                             \
+// tensor map of `batch` activation volumes [z][y][x][C] (BF16) with the brick
+// convolution's box: 8 channels x (8 + 2) x (16 + 2) x (BZ + 2) nodes x 1 sample
+int activation_map(CUtensorMap* map, const bf16* x, int C, Grid3 g, int batch, int bz) {
+  auto fn = encode_tiled();
+  if (!fn) return fail(SFX_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  const cuuint64_t dims[5] = {cuuint64_t(C), cuuint64_t(g.nx), cuuint64_t(g.ny), cuuint64_t(g.nz), cuuint64_t(batch)};
+  const cuuint64_t row = cuuint64_t(C) * 2;
+  const cuuint64_t strides[4] = {row, row * g.nx, row * g.nx * g.ny, row * g.nx * g.ny * g.nz};
+  const cuuint32_t box[5] = {8, 10, 18, cuuint32_t(bz + 2), 1};
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16*>(x), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(SFX_ERR_CUDA, "cuTensorMapEncodeTiled failed for an activation volume");
+  return SFX_OK;
+}
+
+// the tensor-core (tcgen05) brick convolution: one block per 8 x 16 x BZ
+// output nodes and sample (the dynamic shared-memory limit is raised once per
+// instantiation)
+template <int CI, int CO, int ACT>
+int launch_conv(Grid3 g, int batch, const bf16* x, const bf16* W, const float* b, bf16* y, float* y32, int* err,
+                cudaStream_t s) {
+  using L = sfx::nn::BrickConvSmem<CI, CO>;
+  static bool configured = false;
+  if (!configured) {
+    SFX_CUDA_TRY(cudaFuncSetAttribute(sfx::nn::conv3_fwd_brick<CI, CO, ACT>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, int(L::bytes)));
+    configured = true;
+  }
+  CUtensorMap map;
+  if (int rc = activation_map(&map, x, CI, g, batch, L::BZ)) return rc;
+  const int64_t bricks = int64_t((g.nx + 7) / 8) * ((g.ny + 15) / 16) * ((g.nz + L::BZ - 1) / L::BZ);
+  const dim3 blocks{unsigned(bricks), unsigned(batch)};
+  sfx::nn::conv3_fwd_brick<CI, CO, ACT><<<blocks, 128, L::bytes, s>>>(map, g, W, b, y, y32, err);
+  SFX_CUDA_TRY(cudaGetLastError());
+  return SFX_OK;
+}
+
+int conv_fwd(int ci, int co, bool relu, Grid3 g, int batch, const bf16* x, const bf16* W, const float* b, bf16* y,
+             float* y32, int* err, cudaStream_t s) {
+#define SFX_CONV(CI, CO)                                                                       \
+  if (ci == CI && co == CO) {                                                                  \
+    if (relu) return launch_conv<CI, CO, sfx::nn::ACT_RELU>(g, batch, x, W, b, y, y32, err, s); \
+    return launch_conv<CI, CO, sfx::nn::ACT_NONE>(g, batch, x, W, b, y, y32, err, s);           \
   }
   SFX_PAIRS(SFX_CONV)
 #undef SFX_CONV
+  return fail(SFX_ERR_UNSUPPORTED, "no convolution for these channel counts");
 }
 // blocks of the weight-gradient kernel for a grid and batch (at most 4 per SM)
 int wgrad_blocks(Grid3 g, int batch) {
@@ -330,39 +375,40 @@ void input_scale(Work* w, int B, const float* r, cudaStream_t s) {
   make_scale<<<1, 64, 0, s>>>(w->ss.p, 3 * N, B, w->scale.p);
 }
 
-void forward(sfx_lnet net, Work* w, int B, cudaStream_t s) {
+int forward(sfx_lnet net, Work* w, int B, cudaStream_t s) {
   const Grid3* g = w->g;
   const int64_t N0 = g[0].nodes(), N1 = g[1].nodes(), N2 = g[2].nodes(), N3 = g[3].nodes();
-  conv_fwd(16, 16, true, g[0], B, w->X0.p, net->W16[A0].p, bias_of(net, A0), w->A0b.p, nullptr, net->wait_error.dev, s);
-  conv_fwd(16, 16, true, g[0], B, w->A0b.p, net->W16[B0L].p, bias_of(net, B0L), w->B0b.p, nullptr, net->wait_error.dev, s);
+  SFX_TRY(conv_fwd(16, 16, true, g[0], B, w->X0.p, net->W16[A0].p, bias_of(net, A0), w->A0b.p, nullptr, net->wait_error.dev, s));
+  SFX_TRY(conv_fwd(16, 16, true, g[0], B, w->A0b.p, net->W16[B0L].p, bias_of(net, B0L), w->B0b.p, nullptr, net->wait_error.dev, s));
   sfx::nn::restrict_to<bf16, bf16><<<grid2(N1 * 16, B), 256, 0, s>>>(g[0], g[1], 16, w->B0b.p, w->C1.p, 0.125f);
-  conv_fwd(16, 32, true, g[1], B, w->C1.p, net->W16[A1].p, bias_of(net, A1), w->A1b.p, nullptr, net->wait_error.dev, s);
-  conv_fwd(32, 32, true, g[1], B, w->A1b.p, net->W16[B1L].p, bias_of(net, B1L), w->B1b.p, nullptr, net->wait_error.dev, s);
+  SFX_TRY(conv_fwd(16, 32, true, g[1], B, w->C1.p, net->W16[A1].p, bias_of(net, A1), w->A1b.p, nullptr, net->wait_error.dev, s));
+  SFX_TRY(conv_fwd(32, 32, true, g[1], B, w->A1b.p, net->W16[B1L].p, bias_of(net, B1L), w->B1b.p, nullptr, net->wait_error.dev, s));
   sfx::nn::restrict_to<bf16, bf16><<<grid2(N2 * 32, B), 256, 0, s>>>(g[1], g[2], 32, w->B1b.p, w->C2.p, 0.125f);
-  conv_fwd(32, 48, true, g[2], B, w->C2.p, net->W16[A2].p, bias_of(net, A2), w->A2b.p, nullptr, net->wait_error.dev, s);
-  conv_fwd(48, 48, true, g[2], B, w->A2b.p, net->W16[B2L].p, bias_of(net, B2L), w->B2b.p, nullptr, net->wait_error.dev, s);
+  SFX_TRY(conv_fwd(32, 48, true, g[2], B, w->C2.p, net->W16[A2].p, bias_of(net, A2), w->A2b.p, nullptr, net->wait_error.dev, s));
+  SFX_TRY(conv_fwd(48, 48, true, g[2], B, w->A2b.p, net->W16[B2L].p, bias_of(net, B2L), w->B2b.p, nullptr, net->wait_error.dev, s));
   sfx::nn::restrict_to<bf16, bf16><<<grid2(N3 * 48, B), 256, 0, s>>>(g[2], g[3], 48, w->B2b.p, w->C3.p, 0.125f);
-  conv_fwd(48, 48, true, g[3], B, w->C3.p, net->W16[A3].p, bias_of(net, A3), w->A3b.p, nullptr, net->wait_error.dev, s);
+  SFX_TRY(conv_fwd(48, 48, true, g[3], B, w->C3.p, net->W16[A3].p, bias_of(net, A3), w->A3b.p, nullptr, net->wait_error.dev, s));
   // D2 = P A3 + B2 ; E2 = relu(conv(D2))
   cudaMemsetAsync(w->D2.p, 0, sizeof(float) * N2 * 48 * B, s);
   sfx::nn::prolong_add<bf16><<<grid2(N2 * 48, B), 256, 0, s>>>(g[2], g[3], 48, w->A3b.p, w->D2.p, 1.f);
   add_bf16_into<<<nb(N2 * 48 * B), 256, 0, s>>>(w->B2b.p, w->D2.p, w->D2b.p, N2 * 48 * B);
-  conv_fwd(48, 32, true, g[2], B, w->D2b.p, net->W16[U2].p, bias_of(net, U2), w->E2.p, nullptr, net->wait_error.dev, s);
+  SFX_TRY(conv_fwd(48, 32, true, g[2], B, w->D2b.p, net->W16[U2].p, bias_of(net, U2), w->E2.p, nullptr, net->wait_error.dev, s));
   cudaMemsetAsync(w->D1.p, 0, sizeof(float) * N1 * 32 * B, s);
   sfx::nn::prolong_add<bf16><<<grid2(N1 * 32, B), 256, 0, s>>>(g[1], g[2], 32, w->E2.p, w->D1.p, 1.f);
   add_bf16_into<<<nb(N1 * 32 * B), 256, 0, s>>>(w->B1b.p, w->D1.p, w->D1b.p, N1 * 32 * B);
-  conv_fwd(32, 16, true, g[1], B, w->D1b.p, net->W16[U1].p, bias_of(net, U1), w->E1.p, nullptr, net->wait_error.dev, s);
+  SFX_TRY(conv_fwd(32, 16, true, g[1], B, w->D1b.p, net->W16[U1].p, bias_of(net, U1), w->E1.p, nullptr, net->wait_error.dev, s));
   cudaMemsetAsync(w->D0.p, 0, sizeof(float) * N0 * 16 * B, s);
   sfx::nn::prolong_add<bf16><<<grid2(N0 * 16, B), 256, 0, s>>>(g[0], g[1], 16, w->E1.p, w->D0.p, 1.f);
   add_bf16_into<<<nb(N0 * 16 * B), 256, 0, s>>>(w->B0b.p, w->D0.p, w->D0b.p, N0 * 16 * B);
-  conv_fwd(16, 16, true, g[0], B, w->D0b.p, net->W16[U0].p, bias_of(net, U0), w->E0.p, nullptr, net->wait_error.dev, s);
-  conv_fwd(16, 16, false, g[0], B, w->E0.p, net->W16[OUTL].p, bias_of(net, OUTL), nullptr, w->OUT.p, net->wait_error.dev, s);
+  SFX_TRY(conv_fwd(16, 16, true, g[0], B, w->D0b.p, net->W16[U0].p, bias_of(net, U0), w->E0.p, nullptr, net->wait_error.dev, s));
+  SFX_TRY(conv_fwd(16, 16, false, g[0], B, w->E0.p, net->W16[OUTL].p, bias_of(net, OUTL), nullptr, w->OUT.p, net->wait_error.dev, s));
+  return SFX_OK;
 }
 
 // backward through one convolution: given the gradient of its output (post
 // activation) gy, accumulate dW, db (summed over the batch) into G and write
 // the input gradient to gx (fp32, overwritten) unless gx is null.
-void conv_bwd(sfx_lnet net, Work* w, int l, Grid3 g, int B, const bf16* x, const bf16* y, const float* gy, float* gx,
+int conv_bwd(sfx_lnet net, Work* w, int l, Grid3 g, int B, const bf16* x, const bf16* y, const float* gy, float* gx,
               cudaStream_t s) {
   const Conv& c = net->layers[l];
   const int64_t rows = g.nodes() * B;
@@ -373,34 +419,36 @@ void conv_bwd(sfx_lnet net, Work* w, int l, Grid3 g, int B, const bf16* x, const
   add_into<<<nb(c.nw()), 256, 0, s>>>(w->red.p, net->G.p + c.off, c.nw());
   bias_grad(c.co, w->gpre.p, rows, w->red.p, s);
   add_into<<<1, 64, 0, s>>>(w->red.p, net->G.p + c.off + c.nw(), c.co);
-  if (gx) conv_fwd(c.co, c.ci, false, g, B, w->gpre16.p, net->Wt16[l].p, nullptr, nullptr, gx, net->wait_error.dev, s);
+  if (gx) SFX_TRY(conv_fwd(c.co, c.ci, false, g, B, w->gpre16.p, net->Wt16[l].p, nullptr, nullptr, gx, net->wait_error.dev, s));
+  return SFX_OK;
 }
 
-void backward(sfx_lnet net, Work* w, int B, cudaStream_t s) {
+int backward(sfx_lnet net, Work* w, int B, cudaStream_t s) {
   const Grid3* g = w->g;
   const int64_t N0 = g[0].nodes(), N1 = g[1].nodes(), N2 = g[2].nodes(), N3 = g[3].nodes();
   // output and up path
-  conv_bwd(net, w, OUTL, g[0], B, w->E0.p, nullptr, w->gOUT.p, w->gE0.p, s);
-  conv_bwd(net, w, U0, g[0], B, w->D0b.p, w->E0.p, w->gE0.p, w->gD0.p, s);
+  SFX_TRY(conv_bwd(net, w, OUTL, g[0], B, w->E0.p, nullptr, w->gOUT.p, w->gE0.p, s));
+  SFX_TRY(conv_bwd(net, w, U0, g[0], B, w->D0b.p, w->E0.p, w->gE0.p, w->gD0.p, s));
   cudaMemcpyAsync(w->gB0.p, w->gD0.p, sizeof(float) * N0 * 16 * B, cudaMemcpyDeviceToDevice, s);
   sfx::nn::restrict_to<float, float><<<grid2(N1 * 16, B), 256, 0, s>>>(g[0], g[1], 16, w->gD0.p, w->gE1.p, 1.f);
-  conv_bwd(net, w, U1, g[1], B, w->D1b.p, w->E1.p, w->gE1.p, w->gD1.p, s);
+  SFX_TRY(conv_bwd(net, w, U1, g[1], B, w->D1b.p, w->E1.p, w->gE1.p, w->gD1.p, s));
   cudaMemcpyAsync(w->gB1.p, w->gD1.p, sizeof(float) * N1 * 32 * B, cudaMemcpyDeviceToDevice, s);
   sfx::nn::restrict_to<float, float><<<grid2(N2 * 32, B), 256, 0, s>>>(g[1], g[2], 32, w->gD1.p, w->gE2.p, 1.f);
-  conv_bwd(net, w, U2, g[2], B, w->D2b.p, w->E2.p, w->gE2.p, w->gD2.p, s);
+  SFX_TRY(conv_bwd(net, w, U2, g[2], B, w->D2b.p, w->E2.p, w->gE2.p, w->gD2.p, s));
   cudaMemcpyAsync(w->gB2.p, w->gD2.p, sizeof(float) * N2 * 48 * B, cudaMemcpyDeviceToDevice, s);
   sfx::nn::restrict_to<float, float><<<grid2(N3 * 48, B), 256, 0, s>>>(g[2], g[3], 48, w->gD2.p, w->gA3.p, 1.f);
   // coarsest and down path
-  conv_bwd(net, w, A3, g[3], B, w->C3.p, w->A3b.p, w->gA3.p, w->gC3.p, s);
+  SFX_TRY(conv_bwd(net, w, A3, g[3], B, w->C3.p, w->A3b.p, w->gA3.p, w->gC3.p, s));
   sfx::nn::prolong_add<float><<<grid2(N2 * 48, B), 256, 0, s>>>(g[2], g[3], 48, w->gC3.p, w->gB2.p, 0.125f);
-  conv_bwd(net, w, B2L, g[2], B, w->A2b.p, w->B2b.p, w->gB2.p, w->gA2.p, s);
-  conv_bwd(net, w, A2, g[2], B, w->C2.p, w->A2b.p, w->gA2.p, w->gC2.p, s);
+  SFX_TRY(conv_bwd(net, w, B2L, g[2], B, w->A2b.p, w->B2b.p, w->gB2.p, w->gA2.p, s));
+  SFX_TRY(conv_bwd(net, w, A2, g[2], B, w->C2.p, w->A2b.p, w->gA2.p, w->gC2.p, s));
   sfx::nn::prolong_add<float><<<grid2(N1 * 32, B), 256, 0, s>>>(g[1], g[2], 32, w->gC2.p, w->gB1.p, 0.125f);
-  conv_bwd(net, w, B1L, g[1], B, w->A1b.p, w->B1b.p, w->gB1.p, w->gA1.p, s);
-  conv_bwd(net, w, A1, g[1], B, w->C1.p, w->A1b.p, w->gA1.p, w->gC1.p, s);
+  SFX_TRY(conv_bwd(net, w, B1L, g[1], B, w->A1b.p, w->B1b.p, w->gB1.p, w->gA1.p, s));
+  SFX_TRY(conv_bwd(net, w, A1, g[1], B, w->C1.p, w->A1b.p, w->gA1.p, w->gC1.p, s));
   sfx::nn::prolong_add<float><<<grid2(N0 * 16, B), 256, 0, s>>>(g[0], g[1], 16, w->gC1.p, w->gB0.p, 0.125f);
-  conv_bwd(net, w, B0L, g[0], B, w->A0b.p, w->B0b.p, w->gB0.p, w->gA0.p, s);
-  conv_bwd(net, w, A0, g[0], B, w->X0.p, w->A0b.p, w->gA0.p, nullptr, s);
+  SFX_TRY(conv_bwd(net, w, B0L, g[0], B, w->A0b.p, w->B0b.p, w->gB0.p, w->gA0.p, s));
+  SFX_TRY(conv_bwd(net, w, A0, g[0], B, w->X0.p, w->A0b.p, w->gA0.p, nullptr, s));
+  return SFX_OK;
 }
 
 // a batch: forward, loss, backward (gradient summed over the samples into
@@ -409,13 +457,13 @@ int batch_grad(sfx_lnet net, Work* w, int B, const float* r, const float* t, con
   const int64_t N = w->g[0].nodes();
   input_scale(w, B, r, s);
   pack_input<<<grid2(N, B), 256, 0, s>>>(r, feat, N, w->scale.p, w->X0.p);
-  forward(net, w, B, s);
+  SFX_TRY(forward(net, w, B, s));
   target_sq<<<grid2(N, B), 256, 0, s>>>(t, feat, N, w->scale.p, w->tmpf.p);
   segment_sums<<<B, 256, 0, s>>>(w->tmpf.p, N, w->tt.p);
   make_inverse<<<1, 64, 0, s>>>(w->tt.p, B, w->inv_tt.p);
   loss_grad<<<grid2(N, B), 256, 0, s>>>(w->OUT.p, t, feat, N, w->scale.p, w->inv_tt.p, w->gOUT.p, w->err.p);
   segment_sums<<<B, 256, 0, s>>>(w->err.p, N, w->esum.p);
-  backward(net, w, B, s);
+  SFX_TRY(backward(net, w, B, s));
   SFX_CUDA_TRY(cudaGetLastError());
   return SFX_OK;
 }
@@ -443,7 +491,7 @@ int lnet_apply(sfx_lnet net, int nx, int ny, int nz, const float* r, const float
   const int64_t N = w->g[0].nodes();
   input_scale(w, 1, r, s);
   pack_input<<<grid2(N, 1), 256, 0, s>>>(r, features, N, w->scale.p, w->X0.p);
-  forward(net, w, 1, s);
+  if (int rc = forward(net, w, 1, s)) return rc;
   unpack_output<<<grid2(N, 1), 256, 0, s>>>(w->OUT.p, features, N, w->scale.p, z);
   SFX_CUDA_TRY(cudaGetLastError());
   return SFX_OK;
