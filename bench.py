@@ -683,7 +683,7 @@ def newton_leg(steps, variants, n=NX):
             pre = S.predictor(solver, u, step)
             st = solver.solve(0.0, u, raise_on_failure=False)
             for k in ("newton_iterations", "krylov_iterations", "inner_iterations", "learned_applications",
-                      "learned_fallbacks"):
+                      "learned_fallbacks", "learned_skipped"):
                 tot[k] = tot.get(k, 0) + st[k]
             tot["predictor_krylov_iterations"] = tot.get("predictor_krylov_iterations", 0) + pre["krylov_iterations"]
             tot["converged"] = min(tot.get("converged", 1), st["converged"])

@@ -66,6 +66,9 @@ typedef struct {
                                 the smoothed residual, Chebyshev (two-level cycle); 0 network, Chebyshev */
   int inner_chebyshev_degree; /* 0: degree of the FP32 Chebyshev inside the mixed-precision solve
                                  (0: chebyshev_degree) */
+  int learned_max_rejections; /* 3: after this many network steps in a row are skipped (each taking less
+                                 than 1 % off the residual), the rest of the linear solve runs without the
+                                 network (counted in learned_skipped); 0: always try the network */
 } sfx_solver_options;
 
 typedef struct {
@@ -79,6 +82,7 @@ typedef struct {
   int learned_applications; /* network preconditioner applications */
   int learned_fallbacks;    /* of which fell back to Jacobi-Chebyshev */
   double lmax_estimate;     /* the last estimate of the largest eigenvalue of D^-1 J (Chebyshev interval) */
+  int learned_skipped;      /* preconditioner applications that did not try the network (learned_max_rejections) */
 } sfx_solver_stats;
 
 typedef struct sfx_solver_s* sfx_solver;

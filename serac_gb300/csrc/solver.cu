@@ -102,6 +102,7 @@ struct sfx_solver_s {
   Reducer<double, double> red;
   Reducer<float, float> red32;
   double lmax = 0.0, lmax32 = 0.0;
+  int nn_rejected_run = 0;  // network steps skipped in a row in the current linear solve
   // learned preconditioner
   sfx_lnet net = nullptr;
   int grid[3] = {0, 0, 0};
@@ -548,6 +549,10 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
     auto nn_step = [=](const float* res, float* z, const float** left) -> int {
       cudaError_t err;
       *left = res;
+      if (o.learned_max_rejections > 0 && s->nn_rejected_run >= o.learned_max_rejections) {
+        s->stats.learned_skipped++;  // the network kept failing in this linear solve
+        return SFX_OK;
+      }
       const double nv = double(s->red32.dot(res, res, n, st, &err));
       SFX_CUDA_TRY(err);
       if (int rc = lnet_apply(s->net, s->grid[0], s->grid[1], s->grid[2], res, s->features, s->nn_z.p, st)) return rc;
@@ -565,8 +570,10 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
         SFX_CUDA_TRY(cudaMemcpyAsync(s->nn_res.p, res, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
         sfx_blas::axpby<float><<<nblocks(n), 256, 0, st>>>(n, float(-a), s->nn_x.p, 1.0f, s->nn_res.p);
         *left = s->nn_res.p;
+        s->nn_rejected_run = 0;
       } else {
         s->stats.learned_fallbacks++;
+        s->nn_rejected_run++;
       }
       return SFX_OK;
     };
@@ -639,6 +646,7 @@ int linear_solve(sfx_solver s, const double* rhs, double* x, cudaStream_t st) {
   }
   SFX_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
   SFX_CUDA_TRY(cudaMemsetAsync(s->inner_count.p, 0, sizeof(int), st));
+  s->nn_rejected_run = 0;
   const bool flexible = o.mixed_precision != 0 || o.krylov == SFX_KRYLOV_FGMRES || o.precond == SFX_PREC_LEARNED;
   int rc = gmres<double, double>(s, apply_J64, prec, flexible, rhs, x, s->V.p, s->Z.p, s->tmp.p, s->y.p, s->red, m,
                                  o.max_krylov_iterations, o.krylov_rel_tol, o.krylov_abs_tol, &iters, &rel, st);
@@ -687,6 +695,7 @@ int sfx_solver_default_options(sfx_solver_options* o) {
   o->print_level = 0;
   o->learned_cycle = 1;
   o->inner_chebyshev_degree = 0;
+  o->learned_max_rejections = 3;
   return SFX_OK;
 }
 
@@ -701,7 +710,7 @@ int sfx_solver_create(sfx_form form, const sfx_solver_options* opt, sfx_solver* 
   if (s->opt.restart < 1 || s->opt.chebyshev_degree < 1 || s->opt.inner_iterations < 1 ||
       s->opt.inner_iterations > 256 ||
       s->opt.inner_chebyshev_degree < 0 || s->opt.eigen_iterations < 2 || !(s->opt.chebyshev_ratio > 1.0) ||
-      s->opt.learned_cycle < 0 || s->opt.learned_cycle > 1) {
+      s->opt.learned_cycle < 0 || s->opt.learned_cycle > 1 || s->opt.learned_max_rejections < 0) {
     delete s;
     return fail(SFX_ERR_INVALID, "bad solver options");
   }

@@ -43,6 +43,7 @@ class SolverOptions(ctypes.Structure):
         ("print_level", ctypes.c_int),
         ("learned_cycle", ctypes.c_int),
         ("inner_chebyshev_degree", ctypes.c_int),
+        ("learned_max_rejections", ctypes.c_int),
     ]
 
     @classmethod
@@ -68,6 +69,7 @@ class SolverStats(ctypes.Structure):
         ("learned_applications", ctypes.c_int),
         ("learned_fallbacks", ctypes.c_int),
         ("lmax_estimate", ctypes.c_double),
+        ("learned_skipped", ctypes.c_int),
     ]
 
     def as_dict(self):

@@ -138,6 +138,7 @@ def evaluate(net, n, seeds, make, fp64_seeds=None):
             totals[name]["seeds"] += 1
             row[name] = {"krylov_iterations": its, "seconds": round(dt, 3),
                          "learned_fallbacks": tot.get("learned_fallbacks", 0),
+                         "learned_skipped": tot.get("learned_skipped", 0),
                          "learned_applications": tot.get("learned_applications", 0)}
             sols[name] = u
         per_seed.append(row)
