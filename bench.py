@@ -19,8 +19,10 @@ Jacobi-Chebyshev, FP32-inner mixed precision, and the learned
 preconditioner on top of mixed precision.  Extra legs: the FP32 inner
 action, the residual, the transposed action, the recomputed-tangent action,
 and the 32^3 Q2 configuration with its CSR assembly.  `--impl reference`
-times the CPU path (serac's stored-derivative Jacobian action, as restated
-by the oracle) on the host cores over a slab of the same mesh.
+(and the `cpu_baseline` leg) times the CPU path (serac's stored-derivative
+Jacobian action, as restated by the oracle) on the whole mesh laid out as
+serac runs without a GPU: one single-threaded process per host core, each
+owning a z-slab of element layers, all at once.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl sfx|reference]
 """
@@ -48,7 +50,6 @@ SIGMA_LOG, ELL, BULK_RATIO = 1.0, 0.1, 20.0
 LOAD_STEPS, FINAL_UZ = 20, -0.05
 MESH_SEED, MATERIAL_SEED = 1, 2
 WORKLOAD = "neohookean_heterogeneous_q2_vector_96cubed_jvp"
-SLAB = 4  # element layers of the CPU sample (a z-slab of the same mesh)
 
 
 def config(n_gpus, flush):
@@ -170,44 +171,60 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ CPU baseline
-def cpu_slab_rate(seconds=10.0, threads=None, min_reps=1, max_reps=None):
-    """The oracle's stored-derivative Jacobian action (serac's
-    action_of_gradient_kernel restated, sum-factorised, gather and node-owner
-    scatter in C, OpenMP over elements) on a z-slab of SLAB element layers of
-    the benchmark mesh, with the same material and linearisation state.
-    Returns (GDOF/s of the whole mesh at the slab's median per-element rate,
-    repetitions, threads, seconds, per-repetition times)."""
+def _slab_worker(z0, z1, reps, warmup, barrier, queue):
+    """One 'rank' of the CPU baseline: element layers [z0, z1) of the
+    benchmark mesh, its derivative formed (untimed), then `warmup` + `reps`
+    single-threaded Jacobian actions timed after all ranks are ready."""
     from oracle import oracle as O
 
-    threads = threads or os.cpu_count() or 1
     V = vertices()
     nv = NX + 1
-    Vs = np.ascontiguousarray(V.reshape(nv, nv * nv, 3)[:SLAB + 1].reshape(-1, 3))
+    layers = z1 - z0
+    Vs = np.ascontiguousarray(V.reshape(nv, nv * nv, 3)[z0:z1 + 1].reshape(-1, 3))
     prob = material()
-    ne_slab = NX * NX * SLAB
-    params = np.ascontiguousarray(prob.params[:ne_slab])
-    f = O.OracleFunctional(O.StructuredHexMesh(NX, NX, SLAB, Vs), ORDER, 3, nthreads=threads)
+    params = np.ascontiguousarray(prob.params[z0 * NX * NX:z1 * NX * NX])
+    f = O.OracleFunctional(O.StructuredHexMesh(NX, NX, layers, Vs), ORDER, 3, nthreads=1)
     f.add_domain_integral(O.MAT_NEOHOOKEAN, params)
     N1 = ORDER * NX + 1
-    planes = ORDER * SLAB + 1
     u_full = linearisation_state(node_coordinates(NX, V)).reshape(3, N1, N1 * N1)
-    u = np.ascontiguousarray(u_full[:, :planes].reshape(-1))
-    lin = O.OracleLinearization(f, u, nthreads=threads)
-    du = np.random.default_rng(0).standard_normal(f.ndofs)
+    u = np.ascontiguousarray(u_full[:, ORDER * z0:ORDER * z1 + 1].reshape(-1))
+    lin = O.OracleLinearization(f, u, nthreads=1)
+    du = np.random.default_rng(z0).standard_normal(f.ndofs)
     out = np.empty(f.ndofs)
-    lin.apply(du, out)
+    barrier.wait()
     times = []
-    t0 = time.perf_counter()
-    while True:
+    for k in range(warmup + reps):
         t1 = time.perf_counter()
         lin.apply(du, out)
-        times.append(time.perf_counter() - t1)
-        el = time.perf_counter() - t0
-        if (len(times) >= min_reps and el >= seconds) or (max_reps and len(times) >= max_reps):
-            break
-    t_full = statistics.median(times) * NX ** 3 / ne_slab
+        if k >= warmup:
+            times.append(time.perf_counter() - t1)
+    queue.put((z0, times))
+
+
+def cpu_slab_processes(reps=5, warmup=1, procs=None):
+    """The CPU path laid out as serac runs it without a GPU, one MPI rank per
+    core: P independent single-threaded processes (P = host cores), each owning
+    a contiguous z-slab of element layers of the benchmark mesh with its own
+    derivative, all timing the oracle's stored-derivative Jacobian action
+    (serac's action_of_gradient_kernel restated: gather, sum factorisation,
+    node-owner scatter in C) at once.  A run's time is its slowest slab's;
+    the baseline is the median over `reps` runs after `warmup`.  Returns
+    (GDOF/s of the whole mesh, processes, per-run times)."""
+    import multiprocessing as mp
+
+    procs = max(1, min(procs or os.cpu_count() or 1, NX))
+    ctx = mp.get_context("spawn")  # the parent may hold a CUDA context
+    barrier, queue = ctx.Barrier(procs), ctx.Queue()
+    bounds = [(NX * k // procs, NX * (k + 1) // procs) for k in range(procs)]
+    workers = [ctx.Process(target=_slab_worker, args=(z0, z1, reps, warmup, barrier, queue)) for z0, z1 in bounds]
+    for w in workers:
+        w.start()
+    results = dict(queue.get() for _ in workers)
+    for w in workers:
+        w.join()
+    runs = [max(results[z0][k] for z0, _ in bounds) for k in range(reps)]
     dofs = 3 * (ORDER * NX + 1) ** 3
-    return dofs / t_full / 1e9, len(times), threads, el, times
+    return dofs / statistics.median(runs) / 1e9, procs, runs
 
 
 # ----------------------------------------------------------------- GPU arm
@@ -523,12 +540,15 @@ def run_sfx(args, rank, world):
     if args.newton_steps > 0 and rank == 0:
         result["newton"] = newton_leg(args.newton_steps, args.newton_variants.split(","))
     result["clocks"] = clocks.stop()
+    if rank == 0 and args.cpu_seconds > 0:
+        gd, procs, runs = cpu_slab_processes(reps=5, warmup=1)
+        result["cpu_baseline"] = {"value": gd, "unit": UNIT, "cores": procs, "kind": "port",
+                                  "sample": f"the whole {NX}^3 mesh as {procs} z-slabs, one single-threaded process "
+                                            f"per slab and core (serac's MPI layout without a GPU), all slabs at "
+                                            f"once; a run's time is the slowest slab's; median of 5 runs after 1 "
+                                            f"warm-up ({statistics.median(runs) * 1e3:.0f} ms); derivative formed "
+                                            f"once per slab, untimed"}
     if rank == 0:
-        gd, reps, thr, el, _ = cpu_slab_rate(seconds=args.cpu_seconds)
-        result["cpu_baseline"] = {"value": gd, "unit": UNIT, "cores": thr, "kind": "port",
-                                  "sample": f"{NX}x{NX}x{SLAB}-element z-slab of the same mesh, material and state; "
-                                            f"median of {reps} Jacobian actions ({el:.1f} s), scaled to the "
-                                            f"{NX}^3 mesh by element count (derivative formed once, untimed)"}
         print(json.dumps(result))
 
 
@@ -781,10 +801,8 @@ def lnet_leg():
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    threads = os.cpu_count() or 1
-    # each step is one Jacobian action over the slab sample, scaled to the mesh
-    cpu_slab_rate(seconds=0.0, threads=threads, min_reps=max(1, args.warmup), max_reps=max(1, args.warmup))
-    gd, reps, thr, el, times = cpu_slab_rate(seconds=0.0, threads=threads, min_reps=args.steps, max_reps=args.steps)
+    # each step is one Jacobian action over the whole mesh, one z-slab per host core
+    gd, thr, runs = cpu_slab_processes(reps=max(1, args.steps), warmup=max(1, args.warmup))
     dofs = 3 * (ORDER * NX + 1) ** 3
     result = {
         "impl": "reference",
@@ -802,8 +820,9 @@ def run_reference(args, rank, world):
         "data": "synthetic (seeded mesh perturbation, material field and linearisation state)",
         "config": config(1, "host memory (CPU path)"),
         "cpu_baseline": {"value": gd, "unit": UNIT, "cores": thr, "kind": "port",
-                         "sample": f"{NX}x{NX}x{SLAB}-element z-slab of the same mesh, material and state; median "
-                                   f"of {reps} Jacobian actions, scaled to the {NX}^3 mesh by element count"},
+                         "sample": f"the whole {NX}^3 mesh as {thr} z-slabs, one single-threaded process per slab "
+                                   f"and core, all at once; a step's time is the slowest slab's; median of "
+                                   f"{len(runs)} steps after {max(1, args.warmup)} warm-up"},
         "e2e": {"value": gd, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "serac's own build needs mfem/hypre/axom (absent) and its element kernels compile only where its "
                 "sources are (not on the benchmark host); the oracle's restatement of action_of_gradient_kernel "
@@ -818,7 +837,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["sfx", "reference"], default="sfx")
-    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0,
+                    help="0 skips the CPU baseline leg of the GPU arm (profiler runs); otherwise it runs in full")
     ap.add_argument("--kernels-only", action="store_true", help="run only the Jacobian actions (profiling)")
     ap.add_argument("--precision", choices=["f64", "f32"], default="f64", help="precision of --kernels-only")
     ap.add_argument("--newton-steps", type=int, default=1,
