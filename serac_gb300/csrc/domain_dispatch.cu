@@ -208,8 +208,8 @@ struct LinearizeFn {
 };
 
 // Bulk-copy staged FP32 action for Q2 (J, or J^T when TRANSPOSE): one
-// persistent block per SM with as many warps as fit two-deep rings in 220 KB
-// of shared memory, rings up to 4 deep.  Without `colored` the kernel writes
+// persistent block per SM with as many warps (up to 24) as fit two-deep rings
+// in 220 KB of shared memory, rings up to 4 deep.  Without `colored` the kernel writes
 // the E-vector E (scattered by the caller); with it the eight colour sets of
 // the structured mesh run one after another, each adding its element
 // vectors into the global vector E in place (zeroed first unless
@@ -221,7 +221,10 @@ int launch_tma_kernel(const sfx_form_s& f, const float* du, const TS* D, float* 
   using Shape = kernels::TangentShape<C, HS, VI, SYM>;
   constexpr size_t kSmemBudget = 220 * 1024;
   constexpr size_t stage_bytes = size_t(Shape::template stride_of<NQ, TS>) * sizeof(TS) + 8;
-  constexpr int WARPS = 16 * 2 * stage_bytes <= kSmemBudget   ? 16
+  // 24 warps (the FP16 copy: 768 threads, at most 85 registers each) when
+  // two stages of them fit; the FP32 copy gets 16
+  constexpr int WARPS = 24 * 2 * stage_bytes <= kSmemBudget   ? 24
+                        : 16 * 2 * stage_bytes <= kSmemBudget ? 16
                         : 12 * 2 * stage_bytes <= kSmemBudget ? 12
                         : 8 * 2 * stage_bytes <= kSmemBudget  ? 8
                                                               : 4;
