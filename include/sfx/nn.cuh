@@ -43,153 +43,6 @@ __device__ inline void mma_bf16_16816(float (&d)[4], const uint32_t (&a)[4], con
 
 enum Act : int { ACT_NONE = 0, ACT_RELU = 1 };
 
-/// Shared-memory layout of conv3_fwd_umma: two stages, each holding one
-/// tap's A operand (128 nodes x CIN) and B operand (COUT x CIN weights) as
-/// K-major core matrices, one chunk per 16 input channels.  About 34 KB for
-/// the widest layer, so several blocks share an SM and hide each other's
-/// gather latency.
-template <int CIN, int COUT>
-struct UmmaConvSmem {
-  static constexpr int KC = CIN / 16;                      // K-steps per tap
-  static constexpr uint32_t B_CHUNK = uint32_t(COUT) * 32;  // bytes per K-step
-  static constexpr uint32_t A_CHUNK = 128 * 32;
-  static constexpr uint32_t A_STAGE = A_CHUNK * KC;
-  static constexpr uint32_t B_STAGE = B_CHUNK * KC;
-  static constexpr size_t bytes = 2 * size_t(A_STAGE + B_STAGE);
-  static constexpr uint32_t NCOLS = COUT <= 32 ? 32 : 64;  // TMEM columns of the FP32 accumulator
-};
-
-/// Forward 3x3x3 convolution on the 5th-generation tensor cores: an implicit
-/// GEMM with the 128 output nodes of the block as M, the output channels as
-/// N and K = 27 taps x CIN, accumulated in tensor memory (FP32) by tcgen05.mma
-/// kind::f16 (BF16 operands in shared memory).  For each tap the block's 128
-/// threads gather the shifted input rows (16-byte loads, zero outside the
-/// grid) and the tap's weights into one of two stages while the MMAs of the
-/// previous tap run; one thread issues the tap's CIN / 16 MMAs and commits
-/// them to that stage's mbarrier, which the gather two taps later waits on.
-/// The epilogue reads the accumulator with tcgen05.ld (warp w: rows
-/// 32w..32w+31), adds the bias, applies the activation and stores BF16 (or
-/// FP32 into y_f32).  x: [node][CIN] bf16, W: [COUT][27][CIN] bf16, bias:
-/// [COUT] f32 (may be null), y: [node][COUT] bf16; blockIdx.y selects the
-/// sample of a batch (volumes stored one after another).  Every wait is
-/// bounded: on a timeout the block sets *err, waits (bounded) for its issued
-/// MMAs and frees its tensor memory.
-template <int CIN, int COUT, int ACT>
-__global__ void __launch_bounds__(128, 4) conv3_fwd_umma(Grid3 g, const __nv_bfloat16* __restrict__ x,
-                                                      const __nv_bfloat16* __restrict__ W,
-                                                      const float* __restrict__ bias, __nv_bfloat16* __restrict__ y,
-                                                      float* __restrict__ y_f32, int* __restrict__ err) {
-  static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 64, "channel counts");
-  using L = UmmaConvSmem<CIN, COUT>;
-  extern __shared__ __align__(128) unsigned char sfx_conv_smem[];
-  __shared__ uint64_t bars[2];
-  __shared__ uint32_t tmem_base;
-  __shared__ int node_xyz[128][3];
-  const int64_t N = g.nodes();
-  const int64_t n0 = int64_t(blockIdx.x) * 128;
-  x += int64_t(blockIdx.y) * N * CIN;
-  if (y) y += int64_t(blockIdx.y) * N * COUT;
-  if (y_f32) y_f32 += int64_t(blockIdx.y) * N * COUT;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  {
-    const int r = threadIdx.x;  // one row per thread
-    const int64_t n = n0 + r;
-    const int64_t nn = n < N ? n : 0;
-    node_xyz[r][0] = n < N ? int(nn % g.nx) : -1000000;  // rows past the grid read zeros
-    node_xyz[r][1] = int((nn / g.nx) % g.ny);
-    node_xyz[r][2] = int(nn / (int64_t(g.nx) * g.ny));
-  }
-  if (threadIdx.x == 0) {
-    bulk::mbar_init(&bars[0], 1);
-    bulk::mbar_init(&bars[1], 1);
-    bulk::fence_mbar_init();
-  }
-  if (warp == 0) {
-    umma::tmem_alloc(&tmem_base, L::NCOLS);
-    umma::tmem_relinquish();
-  }
-  umma::fence_before_sync();
-  __syncthreads();
-  umma::fence_after_sync();
-  const uint32_t tmem = tmem_base;
-  constexpr uint32_t idesc = umma::idesc_bf16_f32(128, COUT);
-  constexpr int GPN = CIN / 8;  // 16-byte groups per node (and per output channel of one tap's weights)
-  const uint4* src = reinterpret_cast<const uint4*>(x);
-  const uint4* wsrc = reinterpret_cast<const uint4*>(W);
-  bool ok = true;
-  for (int tap = 0; tap < 27 && ok; tap++) {
-    const int buf = tap & 1;
-    if (tap >= 2) ok = __syncthreads_and(bulk::mbar_wait(&bars[buf], uint32_t((tap - 2) >> 1) & 1u));
-    if (!ok) break;
-    umma::fence_after_sync();
-    const int dx = tap % 3 - 1, dy = (tap / 3) % 3 - 1, dz = tap / 9 - 1;
-    unsigned char* A = sfx_conv_smem + size_t(buf) * (L::A_STAGE + L::B_STAGE);
-    unsigned char* Bm = A + L::A_STAGE;
-    for (int i = threadIdx.x; i < 128 * GPN; i += blockDim.x) {
-      const int r = i / GPN, g8 = i % GPN;
-      const int xx = node_xyz[r][0] + dx, yy = node_xyz[r][1] + dy, zz = node_xyz[r][2] + dz;
-      uint4 v = make_uint4(0u, 0u, 0u, 0u);
-      if (xx >= 0 && xx < g.nx && yy >= 0 && yy < g.ny && zz >= 0 && zz < g.nz)
-        v = src[((int64_t(zz) * g.ny + yy) * g.nx + xx) * GPN + g8];
-      *reinterpret_cast<uint4*>(A + uint32_t(g8 / 2) * L::A_CHUNK + umma::kmajor_offset(r, (g8 & 1) * 8, 128, 256)) = v;
-    }
-    // this tap's weights W[co][tap][ci] -> chunk ci / 16, core-matrix slot of (co, ci % 16)
-    for (int i = threadIdx.x; i < COUT * GPN; i += blockDim.x) {
-      const int co = i / GPN, g8 = i % GPN;
-      *reinterpret_cast<uint4*>(Bm + uint32_t(g8 / 2) * L::B_CHUNK + umma::kmajor_offset(co, (g8 & 1) * 8, 128, 256)) =
-          wsrc[(int64_t(co) * 27 + tap) * GPN + g8];
-    }
-    bulk::fence_proxy_async_smem();  // the gathered operands are read by the tensor core
-    umma::fence_before_sync();
-    __syncthreads();
-    umma::fence_after_sync();
-    if (threadIdx.x == 0) {
-#pragma unroll
-      for (int kc = 0; kc < L::KC; kc++)
-        umma::mma_bf16(tmem, umma::smem_desc(A + uint32_t(kc) * L::A_CHUNK, 128, 256),
-                       umma::smem_desc(Bm + uint32_t(kc) * L::B_CHUNK, 128, 256), idesc, tap > 0 || kc > 0);
-      umma::commit(&bars[buf]);
-    }
-  }
-  // the last commit (tap 26, buffer 0, its 14th completion) covers every MMA
-  if (ok) ok = __syncthreads_and(bulk::mbar_wait(&bars[0], 1u));
-  umma::fence_after_sync();
-  if (ok) {
-    const int r = 32 * warp + lane;
-    const int64_t n = n0 + r;
-#pragma unroll
-    for (int c = 0; c < COUT; c += 8) {
-      float v[8];
-      umma::ld_x8(tmem + (uint32_t(32 * warp) << 16) + uint32_t(c), v);
-      if (n < N) {
-#pragma unroll
-        for (int i = 0; i < 8; i++) {
-          float t = v[i] + (bias ? bias[c + i] : 0.f);
-          if (ACT == ACT_RELU) t = t > 0.f ? t : 0.f;
-          v[i] = t;
-        }
-        if (y_f32) {
-#pragma unroll
-          for (int i = 0; i < 8; i++) y_f32[n * COUT + c + i] = v[i];
-        } else {
-          uint4 pk = make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]),
-                                pack_bf16x2(v[6], v[7]));
-          *reinterpret_cast<uint4*>(y + n * COUT + c) = pk;
-        }
-      }
-    }
-  } else {
-    if (threadIdx.x == 0) atomicExch(err, 1);
-    // the MMAs already issued (bounded) before the tensor memory is released
-    (void)bulk::mbar_wait(&bars[0], 0u);
-    (void)bulk::mbar_wait(&bars[1], 0u);
-  }
-  umma::fence_before_sync();
-  __syncthreads();
-  umma::fence_after_sync();
-  if (warp == 0) umma::tmem_dealloc(tmem, L::NCOLS);
-}
-
 /// Brick of input nodes staged by conv3_fwd_brick: the 8 x 16 x BZ output
 /// nodes of a block plus a one-node halo, (10 x 18 x (BZ + 2)) nodes, stored
 /// as 2 * CIN / 16 slabs of 8 channels, each slab [z][y][x] x 16 bytes (what

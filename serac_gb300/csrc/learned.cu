@@ -139,19 +139,39 @@ __global__ void square(const float* __restrict__ a, float* __restrict__ b, int64
   int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i < n) b[i] = a[i] * a[i];
 }
-// out[b] = sum of a[b * len .. (b + 1) * len) in double, fixed order (one block per segment)
-__global__ void __launch_bounds__(256) segment_sums(const float* __restrict__ a, int64_t len, float* __restrict__ out) {
+// out[b] = sum of a[b * len .. (b + 1) * len) in double, fixed order, in two
+// passes: block (g, b) sums chunk g of segment b into part[b][g]; then one
+// block per segment sums its kSegChunks partials
+constexpr int kSegChunks = 64;
+__global__ void __launch_bounds__(256) segment_partials(const float* __restrict__ a, int64_t len,
+                                                        double* __restrict__ part) {
   __shared__ double sh[256];
-  const float* seg = a + int64_t(blockIdx.x) * len;
+  const int64_t chunk = (len + kSegChunks - 1) / kSegChunks;
+  const int64_t b0 = int64_t(blockIdx.x) * chunk, b1 = b0 + chunk < len ? b0 + chunk : len;
+  const float* seg = a + int64_t(blockIdx.y) * len;
   double acc = 0.0;
-  for (int64_t i = threadIdx.x; i < len; i += 256) acc += seg[i];
+  for (int64_t i = b0 + threadIdx.x; i < b1; i += 256) acc += seg[i];
   sh[threadIdx.x] = acc;
   __syncthreads();
   for (int s = 128; s > 0; s >>= 1) {
     if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
     __syncthreads();
   }
+  if (threadIdx.x == 0) part[int64_t(blockIdx.y) * kSegChunks + blockIdx.x] = sh[0];
+}
+__global__ void segment_finish(const double* __restrict__ part, float* __restrict__ out) {
+  __shared__ double sh[kSegChunks];
+  sh[threadIdx.x] = part[int64_t(blockIdx.x) * kSegChunks + threadIdx.x];
+  __syncthreads();
+  for (int s = kSegChunks / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
   if (threadIdx.x == 0) out[blockIdx.x] = float(sh[0]);
+}
+void segment_sums(const float* a, int64_t len, int nseg, double* part, float* out, cudaStream_t s) {
+  segment_partials<<<dim3(kSegChunks, unsigned(nseg)), 256, 0, s>>>(a, len, part);
+  segment_finish<<<unsigned(nseg), kSegChunks, 0, s>>>(part, out);
 }
 // scale[b] = RMS of the residual (1 for a zero residual)
 __global__ void make_scale(const float* __restrict__ ss, int64_t len, int batch, float* __restrict__ scale) {
@@ -290,6 +310,7 @@ struct Work {
   DeviceBuf<bf16> gpre16;
   DeviceBuf<float> part, red, err;
   DeviceBuf<float> ss, scale, tt, inv_tt, esum;  // per sample
+  DeviceBuf<double> seg;                         // partial sums of segment_sums [sample][kSegChunks]
 };
 
 }  // namespace
@@ -359,6 +380,7 @@ int get_work(sfx_lnet net, int nx, int ny, int nz, int batch, Work** out) {
   ok = ok && w->part.alloc(npart) == cudaSuccess && w->red.alloc(size_t(48) * 27 * 48) == cudaSuccess &&
        w->err.alloc(N0 * B) == cudaSuccess;
   for (auto* b : {&w->ss, &w->scale, &w->tt, &w->inv_tt, &w->esum}) ok = ok && b->alloc(B) == cudaSuccess;
+  ok = ok && w->seg.alloc(B * kSegChunks) == cudaSuccess;
   if (!ok) return fail(SFX_ERR_NOMEM, "network workspace allocation failed");
   *out = w.get();
   net->work[key] = std::move(w);
@@ -371,7 +393,7 @@ const float* bias_of(sfx_lnet net, int l) { return net->P.p + net->layers[l].off
 void input_scale(Work* w, int B, const float* r, cudaStream_t s) {
   const int64_t N = w->g[0].nodes();
   square<<<nb(int64_t(B) * 3 * N), 256, 0, s>>>(r, w->tmpf.p, int64_t(B) * 3 * N);
-  segment_sums<<<B, 256, 0, s>>>(w->tmpf.p, 3 * N, w->ss.p);
+  segment_sums(w->tmpf.p, 3 * N, B, w->seg.p, w->ss.p, s);
   make_scale<<<1, 64, 0, s>>>(w->ss.p, 3 * N, B, w->scale.p);
 }
 
@@ -459,10 +481,10 @@ int batch_grad(sfx_lnet net, Work* w, int B, const float* r, const float* t, con
   pack_input<<<grid2(N, B), 256, 0, s>>>(r, feat, N, w->scale.p, w->X0.p);
   SFX_TRY(forward(net, w, B, s));
   target_sq<<<grid2(N, B), 256, 0, s>>>(t, feat, N, w->scale.p, w->tmpf.p);
-  segment_sums<<<B, 256, 0, s>>>(w->tmpf.p, N, w->tt.p);
+  segment_sums(w->tmpf.p, N, B, w->seg.p, w->tt.p, s);
   make_inverse<<<1, 64, 0, s>>>(w->tt.p, B, w->inv_tt.p);
   loss_grad<<<grid2(N, B), 256, 0, s>>>(w->OUT.p, t, feat, N, w->scale.p, w->inv_tt.p, w->gOUT.p, w->err.p);
-  segment_sums<<<B, 256, 0, s>>>(w->err.p, N, w->esum.p);
+  segment_sums(w->err.p, N, B, w->seg.p, w->esum.p, s);
   SFX_TRY(backward(net, w, B, s));
   SFX_CUDA_TRY(cudaGetLastError());
   return SFX_OK;

@@ -40,12 +40,30 @@ def main(argv=None):
     ap.add_argument("--eval-fp64-seeds", default=None,
                     help="first:last subset of the held-out seeds also solved by the FP64 methods (Chebyshev "
                          "alone and the two-level step); default: all of --eval-seeds")
+    ap.add_argument("--eval-steps", type=int, default=None,
+                    help="load steps of the held-out problems (default: --steps)")
+    ap.add_argument("--eval-strain", type=float, default=None,
+                    help="compression of the held-out problems after their load steps (default: --strain)")
+    ap.add_argument("--load", default=None,
+                    help="evaluate these trained parameters (.npy) instead of harvesting and training")
     ap.add_argument("--out", required=True)
     args = ap.parse_args(argv)
 
     import torch
 
     from . import learned as L
+
+    make_eval = problem_factory(args.material, args.strain if args.eval_strain is None else args.eval_strain,
+                                args.steps if args.eval_steps is None else args.eval_steps)
+    if args.load:
+        net = L.LearnedPreconditioner(seed=args.init_seed)
+        net.load(args.load)
+        info = {"material": args.material, "weights": args.load, "n": args.n,
+                "evaluation": evaluate(net, args.n, args.eval_seeds, make_eval, args.eval_fp64_seeds)}
+        with open(args.out, "w") as fh:
+            json.dump(info, fh, indent=1)
+        print(json.dumps(info))
+        return
 
     lo, hi = (int(x) for x in args.seeds.split(":"))
     t0 = time.time()
@@ -73,7 +91,7 @@ def main(argv=None):
             "lr": args.lr, "harvest_s": round(t_harvest, 1), "train_s": round(time.time() - t0, 1),
             "final_loss": hist[-1], "loss_history": [round(h, 4) for h in hist]}
     if args.eval_seeds:
-        info["evaluation"] = evaluate(net, args.n, args.eval_seeds, make, args.eval_fp64_seeds)
+        info["evaluation"] = evaluate(net, args.n, args.eval_seeds, make_eval, args.eval_fp64_seeds)
     with open(os.path.splitext(args.out)[0] + ".json", "w") as fh:
         json.dump(info, fh, indent=1)
     print(json.dumps(info))
@@ -136,16 +154,22 @@ def evaluate(net, n, seeds, make, fp64_seeds=None):
             totals[name]["seconds"] += dt
             totals[name]["krylov_iterations"] += its
             totals[name]["seeds"] += 1
-            row[name] = {"krylov_iterations": its, "seconds": round(dt, 3),
+            row[name] = {"krylov_iterations": its, "seconds": round(dt, 3), "converged": int(tot.get("converged", 0)),
+                         "newton_iterations": tot.get("newton_iterations", 0),
                          "learned_fallbacks": tot.get("learned_fallbacks", 0),
                          "learned_skipped": tot.get("learned_skipped", 0),
                          "learned_applications": tot.get("learned_applications", 0)}
             sols[name] = u
-        per_seed.append(row)
         ref = sols.get("chebyshev", sols["mixed"])
-        for u in sols.values():
-            worst_diff = max(worst_diff, float(torch.linalg.norm(u - ref) / torch.linalg.norm(ref)))
-    out = {"seeds": seeds, "fp64_seeds": f"{flo}:{fhi}", "n": n, "totals": totals, "max_rel_diff": worst_diff,
+        for name, u in sols.items():
+            d = float(torch.linalg.norm(u - ref) / torch.linalg.norm(ref))
+            row[name]["rel_diff"] = d
+            if all(row[k]["converged"] for k in sols):
+                worst_diff = max(worst_diff, d)
+        per_seed.append(row)
+    converged = sum(all(v["converged"] for k, v in r.items() if k != "seed") for r in per_seed)
+    out = {"seeds": seeds, "fp64_seeds": f"{flo}:{fhi}", "n": n, "totals": totals,
+           "seeds_all_converged": converged, "max_rel_diff_converged": worst_diff,
            "time_ratio_learned_mixed": totals["learned_mixed"]["seconds"] / totals["mixed"]["seconds"],
            "iteration_ratio_learned_mixed": totals["learned_mixed"]["krylov_iterations"]
            / max(1, totals["mixed"]["krylov_iterations"]),
