@@ -519,12 +519,7 @@ def run_sfx(args, rank, world):
         "roofline": roof64,
         "compute_roofline": compute,
         "jv_fp32": {"value": ndofs * args.steps / sum(t_fp32) / 1e9, "unit": UNIT, "dtype": "f32",
-                    "ms_per_step": statistics.mean(t_fp32) * 1e3, "roofline": roof32,
-                    "action_roofline": roofline_hbm(
-                        "sfx_jvp_f32: the bulk-copy kernel over the eight colour sets, element vectors added into "
-                        "dr in place (zeroing dr included)", 4 * ndofs + 45 * 4 * nq + 2 * 4 * ndofs,
-                        statistics.mean(t_fp32), hbm_peak, peak_src, None,
-                        "algorithmic bytes: du read, packed tangent, dr zeroed and written once")},
+                    "ms_per_step": statistics.mean(t_fp32) * 1e3, "roofline": roof32},
         "jv_fp16_tangent": {"value": ndofs * args.steps / sum(t_fp16) / 1e9, "unit": UNIT, "dtype": "f32 (f16 tangent)",
                             "ms_per_step": statistics.mean(t_fp16) * 1e3, "roofline": roof16},
         "residual": {"value": ndofs * args.steps / sum(t_res) / 1e9, "unit": UNIT, "dtype": "f64",

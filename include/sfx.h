@@ -206,11 +206,7 @@ int sfx_form_set_jvp_mode(sfx_form form, int mode);
 #define SFX_TANGENT_F16 1
 int sfx_form_set_tangent_storage(sfx_form form, int storage);
 
-/* dr = dR/du(t_lin, u_lin) du, in FP64, and in FP32 (FP32 accumulation).
- * On structured order-2 forms the FP32 action adds the element vectors of
- * the eight element colours (elements of one colour share no node) straight
- * into dr, one colour after another (deterministic, no atomics, no E-vector
- * pass); du and dr must not overlap (SFX_ERR_INVALID). */
+/* dr = dR/du(t_lin, u_lin) du, in FP64, and in FP32 (FP32 accumulation). */
 int sfx_jvp(sfx_form form, const double* du, double* dr, void* stream);
 int sfx_jvp_f32(sfx_form form, const float* du, float* dr, void* stream);
 

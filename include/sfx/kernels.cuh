@@ -1446,21 +1446,6 @@ __global__ void __launch_bounds__(128) jvp_stored_transpose_kernel(const Real* _
   }
 }
 
-/// The elements of one colour of a structured mesh: (ex, ey, ez) =
-/// 2 (ix, iy, iz) + (bx, by, bz) with ix < cx, iy < cy, iz < cz (count
-/// items).  Two Q2 (or Q1) elements of one colour share no node, so their
-/// element vectors can be added into the global vector in place, the eight
-/// colours one after another.
-struct ColorSet {
-  int64_t nx = 0, ny = 0;  // elements per direction of the mesh in x and y
-  int bx = 0, by = 0, bz = 0;
-  int64_t cx = 0, cy = 0, count = 0;
-  SFX_HDI int64_t element(int64_t i) const {
-    const int64_t ix = i % cx, iy = (i / cx) % cy, iz = i / (cx * cy);
-    return (2 * ix + bx) + nx * ((2 * iy + by) + ny * (2 * iz + bz));
-  }
-};
-
 /// FP32 Jacobian action from the stored tangent for Q2 elements, with each
 /// element's tangent block (81 x 27 floats for the vector Neo-Hookean case,
 /// 8.7 KB, contiguous) staged into shared memory by bulk asynchronous copies
@@ -1470,19 +1455,14 @@ struct ColorSet {
 /// Elements are dealt to warps round-robin (persistent grid).  A wait that
 /// does not complete sets *err and the warp drains its outstanding copies
 /// (again bounded) before returning.  TRANSPOSE applies the block transposed
-/// (J^T v, as jvp_stored_transpose_kernel) with the same staging.  COLORED
-/// processes the elements of one colour set and adds each element vector
-/// into the global vector `out` (byNODES) in place, which replaces the
-/// E-vector write and the node-owner scatter; otherwise `out` is the E-vector
-/// [e][c][node].
+/// (J^T v, as jvp_stored_transpose_kernel) with the same staging.
 template <int C, bool HS, bool VI, int WARPS, int STAGES, bool TRANSPOSE = false, typename TS = float,
-          bool SYM = false, bool COLORED = false>
+          bool SYM = false>
 __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float* __restrict__ du,
                                                                     const TS* __restrict__ D,
                                                                     const int32_t* __restrict__ conn,
-                                                                    float* __restrict__ out, int64_t num_nodes,
-                                                                    int64_t num_elements, int* __restrict__ err,
-                                                                    ColorSet cs) {
+                                                                    float* __restrict__ out_e, int64_t num_nodes,
+                                                                    int64_t num_elements, int* __restrict__ err) {
   constexpr int P = 2, Q = 3, NQ = 27;
   using Shape = TangentShape<C, HS, VI, SYM>;
   // input side (interpolated direction) and output side (integrated) of the
@@ -1512,18 +1492,15 @@ __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float*
   }
   __syncthreads();
 
-  // work items: the elements, or those of one colour (COLORED)
-  const int64_t items = COLORED ? cs.count : num_elements;
-  auto element_of = [&](int64_t i) { return COLORED ? cs.element(i) : i; };
   const int64_t first = int64_t(blockIdx.x) * WARPS + wid;
   const int64_t step = int64_t(gridDim.x) * WARPS;
   // prologue: the first STAGES elements of this warp
   if (lane == 0) {
     for (int s = 0; s < STAGES; s++) {
-      const int64_t i = first + s * step;
-      if (i < items) {
+      const int64_t e = first + s * step;
+      if (e < num_elements) {
         bulk::mbar_arrive_expect_tx(&my_bars[s], BYTES);
-        bulk::copy_g2s(my_ring + s * ES, D + element_of(i) * ES, BYTES, &my_bars[s]);
+        bulk::copy_g2s(my_ring + s * ES, D + e * ES, BYTES, &my_bars[s]);
       }
     }
   }
@@ -1535,26 +1512,25 @@ __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float*
   // gather pipeline: du of the current element and the node id of the next
   // one are already in registers; each iteration issues the next element's du
   // and the node id two elements ahead before computing
-  int32_t node_cur = 0, node_next = 0;
+  int32_t node_next = 0;
   float du_cur[C];
   {
-    node_cur = (lane_ok && first < items) ? conn[element_of(first) * NQ + qi] : 0;
+    const int32_t node0 = (lane_ok && first < num_elements) ? conn[first * NQ + qi] : 0;
 #pragma unroll
-    for (int c = 0; c < C; c++) du_cur[c] = (lane_ok && first < items) ? du[c * num_nodes + node_cur] : 0.f;
-    const int64_t i1 = first + step;
-    node_next = (lane_ok && i1 < items) ? conn[element_of(i1) * NQ + qi] : 0;
+    for (int c = 0; c < C; c++) du_cur[c] = (lane_ok && first < num_elements) ? du[c * num_nodes + node0] : 0.f;
+    const int64_t e1 = first + step;
+    node_next = (lane_ok && e1 < num_elements) ? conn[e1 * NQ + qi] : 0;
   }
   int it = 0;
   bool failed = false;
-  for (int64_t i = first; i < items; i += step, it++) {
-    const int64_t e = element_of(i);
+  for (int64_t e = first; e < num_elements; e += step, it++) {
     const int s = it % STAGES;
     const uint32_t parity = uint32_t(it / STAGES) & 1u;
-    const int64_t i1 = i + step, i2 = i + 2 * step;
+    const int64_t e1 = e + step, e2 = e + 2 * step;
     float du_next[C];
 #pragma unroll
-    for (int c = 0; c < C; c++) du_next[c] = (lane_ok && i1 < items) ? du[c * num_nodes + node_next] : 0.f;
-    const int32_t node_after = (lane_ok && i2 < items) ? conn[element_of(i2) * NQ + qi] : 0;
+    for (int c = 0; c < C; c++) du_next[c] = (lane_ok && e1 < num_elements) ? du[c * num_nodes + node_next] : 0.f;
+    const int32_t node_after = (lane_ok && e2 < num_elements) ? conn[e2 * NQ + qi] : 0;
     // interpolate du while the tangent is in flight
     float din[NIN];
 #pragma unroll
@@ -1604,11 +1580,11 @@ __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float*
     }
     __syncwarp();  // every lane has read stage s
     if (lane == 0) {
-      const int64_t in = i + int64_t(STAGES) * step;
-      if (in < items) {
+      const int64_t en = e + int64_t(STAGES) * step;
+      if (en < num_elements) {
         bulk::fence_proxy_async_smem();
         bulk::mbar_arrive_expect_tx(&my_bars[s], BYTES);
-        bulk::copy_g2s(my_ring + s * ES, D + element_of(in) * ES, BYTES, &my_bars[s]);
+        bulk::copy_g2s(my_ring + s * ES, D + en * ES, BYTES, &my_bars[s]);
       }
     }
     constexpr int roff = OUT_VALUE ? C : 0;
@@ -1617,17 +1593,11 @@ __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float*
       const float src = OUT_VALUE ? dout[OUT_VALUE ? c : 0] : 0.f;
       const float r = integrate_colloc<Q, OUT_VALUE, true, float>(src, dout[roff + 3 * c], dout[roff + 3 * c + 1],
                                                                 dout[roff + 3 * c + 2], 0, ix, iy, iz, sB, sD);
-      if (lane_ok) {
-        // COLORED: no other element of this colour touches this node, so the
-        // global vector is updated in place (fixed colour order, no atomics)
-        if constexpr (COLORED) out[c * num_nodes + node_cur] += r;
-        else out[(e * C + c) * NQ + qi] = r;
-      }
+      if (lane_ok) out_e[(e * C + c) * NQ + qi] = r;
     }
     // rotate the gather pipeline (its loads had this element's work to land)
 #pragma unroll
     for (int c = 0; c < C; c++) du_cur[c] = du_next[c];
-    node_cur = node_next;
     node_next = node_after;
   }
   if (failed) {
@@ -1635,7 +1605,7 @@ __global__ void __launch_bounds__(WARPS * 32) jvp_stored_tma_kernel(const float*
     // drain: the copies issued for iterations it .. it + STAGES - 1
     for (int j = 0; j < STAGES; j++) {
       const int k = it + j;
-      if (first + int64_t(k) * step < items) (void)bulk::mbar_wait(&my_bars[k % STAGES], uint32_t(k / STAGES) & 1u);
+      if (first + int64_t(k) * step < num_elements) (void)bulk::mbar_wait(&my_bars[k % STAGES], uint32_t(k / STAGES) & 1u);
     }
   }
 }

@@ -56,17 +56,6 @@ int check_form(sfx_form f) {
   return SFX_OK;
 }
 
-// the FP32 stored-tangent actions of structured order-2 forms add the element
-// vectors into the result by colour sets (no E-vector and no scatter pass)
-bool colour_sets(const sfx_form_s& f) { return !f.general && f.p == 2 && f.mesh.nx > 0; }
-
-// the colour-set actions update the result while later colours still read
-// the direction: the two vectors must not overlap
-bool overlap(const void* a, const void* b, size_t bytes) {
-  const auto x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
-  return x < y + bytes && y < x + bytes;
-}
-
 }  // namespace
 
 int scatter_evector(const sfx_form_s& f, const double* E, double* out, bool accumulate, cudaStream_t s) {
@@ -482,7 +471,6 @@ int sfx_jvp_f32(sfx_form form, const float* du, float* dr, void* stream) {
   if (check_form(form)) return SFX_ERR_INVALID;
   if (!du || !dr) return fail(SFX_ERR_INVALID, "null vector");
   if (!form->linearized) return fail(SFX_ERR_INVALID, "sfx_linearize must be called before sfx_jvp_f32");
-  if (overlap(du, dr, sizeof(float) * size_t(form->ndofs))) return fail(SFX_ERR_INVALID, "du and dr overlap");
   if (form->wait_error.raised()) {
     form->wait_error.clear();
     return fail(SFX_ERR_TIMEOUT, "a bulk-copy wait of an earlier FP32 Jacobian action expired");
@@ -490,10 +478,6 @@ int sfx_jvp_f32(sfx_form form, const float* du, float* dr, void* stream) {
   auto s = static_cast<cudaStream_t>(stream);
   if (form->domain.empty()) SFX_CUDA_TRY(cudaMemsetAsync(dr, 0, sizeof(float) * size_t(form->ndofs), s));
   for (size_t i = 0; i < form->domain.size(); i++) {
-    if (form->jvp_mode == SFX_JVP_STORED_TANGENT && colour_sets(*form)) {
-      if (int rc = launch_jvp_stored_f32_direct(*form, form->domain[i], du, dr, i > 0, s)) return rc;
-      continue;
-    }
     int rc = form->jvp_mode == SFX_JVP_STORED_TANGENT
                  ? launch_jvp_stored_f32(*form, form->domain[i], du, form->e32.p, s)
                  : launch_domain_jvp_f32(*form, form->domain[i], form->u_lin32.p, du, form->e32.p, form->t_lin, s);
@@ -522,7 +506,6 @@ int sfx_jvp_transpose_f32(sfx_form form, const float* v, float* dr, void* stream
   if (check_form(form)) return SFX_ERR_INVALID;
   if (!v || !dr) return fail(SFX_ERR_INVALID, "null vector");
   if (!form->linearized) return fail(SFX_ERR_INVALID, "sfx_linearize must be called before sfx_jvp_transpose_f32");
-  if (overlap(v, dr, sizeof(float) * size_t(form->ndofs))) return fail(SFX_ERR_INVALID, "v and dr overlap");
   if (!form->domain.empty() && form->jvp_mode != SFX_JVP_STORED_TANGENT)
     return fail(SFX_ERR_UNSUPPORTED, "the transposed action needs the stored tangent (SFX_JVP_STORED_TANGENT)");
   if (form->wait_error.raised()) {
@@ -532,10 +515,6 @@ int sfx_jvp_transpose_f32(sfx_form form, const float* v, float* dr, void* stream
   auto s = static_cast<cudaStream_t>(stream);
   if (form->domain.empty()) SFX_CUDA_TRY(cudaMemsetAsync(dr, 0, sizeof(float) * size_t(form->ndofs), s));
   for (size_t i = 0; i < form->domain.size(); i++) {
-    if (colour_sets(*form)) {
-      if (int rc = launch_jvp_transpose_f32_direct(*form, form->domain[i], v, dr, i > 0, s)) return rc;
-      continue;
-    }
     if (int rc = launch_jvp_transpose_f32(*form, form->domain[i], v, form->e32.p, s)) return rc;
     if (int rc2 = scatter_dispatch<float>(*form, form->e32.p, dr, i > 0, s)) return rc2;
   }

@@ -71,13 +71,6 @@ int launch_boundary_transpose_f32(const sfx_form_s& f, const float* v, float* ou
 // diagonal of the element Jacobians from the stored tangent (E-vector)
 int launch_diag_from_tangent(const sfx_form_s& f, const DomainIntegral& di, double* E, cudaStream_t s);
 int launch_jvp_stored_f32(const sfx_form_s& f, const DomainIntegral& di, const float* du, float* E, cudaStream_t s);
-/// the FP32 stored-tangent action (or its transpose) of a structured order-2
-/// form added straight into the global vector dr by the eight colour sets
-/// (no E-vector, no scatter); dr is zeroed first unless `accumulate`
-int launch_jvp_stored_f32_direct(const sfx_form_s& f, const DomainIntegral& di, const float* du, float* dr,
-                                 bool accumulate, cudaStream_t s);
-int launch_jvp_transpose_f32_direct(const sfx_form_s& f, const DomainIntegral& di, const float* v, float* dr,
-                                    bool accumulate, cudaStream_t s);
 
 int launch_domain_jvp_f32(const sfx_form_s& f, const DomainIntegral& di, const float* u, const float* du, float* E,
                           double t, cudaStream_t s);

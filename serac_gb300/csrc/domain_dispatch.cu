@@ -209,14 +209,9 @@ struct LinearizeFn {
 
 // Bulk-copy staged FP32 action for Q2 (J, or J^T when TRANSPOSE): one
 // persistent block per SM with as many warps (up to 24) as fit two-deep rings
-// in 220 KB of shared memory, rings up to 4 deep.  Without `colored` the kernel writes
-// the E-vector E (scattered by the caller); with it the eight colour sets of
-// the structured mesh run one after another, each adding its element
-// vectors into the global vector E in place (zeroed first unless
-// `accumulate`).
-template <int C, bool HS, bool VI, bool TRANSPOSE, typename TS, bool SYM, bool COLORED>
-int launch_tma_kernel(const sfx_form_s& f, const float* du, const TS* D, float* out, int64_t items,
-                      const kernels::ColorSet& cs, cudaStream_t s) {
+// in 220 KB of shared memory, rings up to 4 deep.
+template <int C, bool HS, bool VI, bool TRANSPOSE, typename TS, bool SYM>
+int launch_tma(const sfx_form_s& f, const float* du, const TS* D, float* E, cudaStream_t s) {
   constexpr int NQ = 27;
   using Shape = kernels::TangentShape<C, HS, VI, SYM>;
   constexpr size_t kSmemBudget = 220 * 1024;
@@ -231,7 +226,7 @@ int launch_tma_kernel(const sfx_form_s& f, const float* du, const TS* D, float* 
   constexpr int STAGES = int(std::min<size_t>(4, kSmemBudget / (WARPS * stage_bytes)));
   static_assert(STAGES >= 2, "tangent block too large for a two-stage ring");
   constexpr size_t smem = size_t(WARPS) * STAGES * stage_bytes;
-  auto kern = kernels::jvp_stored_tma_kernel<C, HS, VI, WARPS, STAGES, TRANSPOSE, TS, SYM, COLORED>;
+  auto kern = kernels::jvp_stored_tma_kernel<C, HS, VI, WARPS, STAGES, TRANSPOSE, TS, SYM>;
   static bool configured = false;  // per instantiation
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
@@ -244,31 +239,8 @@ int launch_tma_kernel(const sfx_form_s& f, const float* du, const TS* D, float* 
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   }
-  if (items <= 0) return SFX_OK;
-  const int64_t blocks = std::min<int64_t>((items + WARPS - 1) / WARPS, std::max(sms, 1));
-  kern<<<unsigned(blocks), WARPS * 32, smem, s>>>(du, D, f.conn.p, out, f.nnodes, f.ne, f.wait_error.dev, cs);
-  return SFX_OK;
-}
-
-template <int C, bool HS, bool VI, bool TRANSPOSE, typename TS, bool SYM>
-int launch_tma(const sfx_form_s& f, const float* du, const TS* D, float* out, cudaStream_t s, bool colored = false,
-               bool accumulate = false) {
-  if (!colored)
-    return launch_tma_kernel<C, HS, VI, TRANSPOSE, TS, SYM, false>(f, du, D, out, f.ne, kernels::ColorSet{}, s);
-  if (!accumulate) SFX_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * size_t(f.ndofs), s));
-  const int64_t nx = f.mesh.nx, ny = f.mesh.ny, nz = f.mesh.nz;
-  for (int color = 0; color < 8; color++) {
-    kernels::ColorSet cs;
-    cs.nx = nx;
-    cs.ny = ny;
-    cs.bx = color & 1;
-    cs.by = (color >> 1) & 1;
-    cs.bz = (color >> 2) & 1;
-    cs.cx = (nx - cs.bx + 1) / 2;
-    cs.cy = (ny - cs.by + 1) / 2;
-    cs.count = cs.cx * cs.cy * ((nz - cs.bz + 1) / 2);
-    if (int rc = launch_tma_kernel<C, HS, VI, TRANSPOSE, TS, SYM, true>(f, du, D, out, cs.count, cs, s)) return rc;
-  }
+  const int64_t blocks = std::min<int64_t>((f.ne + WARPS - 1) / WARPS, std::max(sms, 1));
+  kern<<<unsigned(blocks), WARPS * 32, smem, s>>>(du, D, f.conn.p, E, f.nnodes, f.ne, f.wait_error.dev);
   return SFX_OK;
 }
 
@@ -281,8 +253,6 @@ struct StoredJvpFn {
   Real* E;
   cudaStream_t s;
   int64_t e0 = 0, e1 = -1;  // element range [e0, e1) of the FP64 action (default: all)
-  bool colored = false;     // FP32 Q2: add into the global vector E by colour sets
-  bool accumulate = false;  // ... keeping what E holds
   template <int C, typename State, typename Maker>
   int operator()() {
     constexpr int NQ = (P + 1) * (P + 1) * (P + 1);
@@ -294,10 +264,8 @@ struct StoredJvpFn {
     constexpr bool SYM = sym_of<Maker>::value;
     if constexpr (P == 2 && std::is_same<Real, float>::value) {
       if (first != 0 || last != f.ne) return fail(SFX_ERR_UNSUPPORTED, "element ranges are FP64 only");
-      const int rc =
-          f.tangent16
-              ? launch_tma<C, HS, Maker::value_input, false, __half, SYM>(f, du, di.D16.p, E, s, colored, accumulate)
-              : launch_tma<C, HS, Maker::value_input, false, float, SYM>(f, du, D, E, s, colored, accumulate);
+      const int rc = f.tangent16 ? launch_tma<C, HS, Maker::value_input, false, __half, SYM>(f, du, di.D16.p, E, s)
+                                 : launch_tma<C, HS, Maker::value_input, false, float, SYM>(f, du, D, E, s);
       if (rc) return rc;
     } else {
       // the FP64 copy is stored full; the FP32 copy packed when symmetric
@@ -323,7 +291,6 @@ struct StoredJvpTransposeFn {
   const Real* D;
   Real* E;
   cudaStream_t s;
-  bool colored = false, accumulate = false;  // as StoredJvpFn
   template <int C, typename State, typename Maker>
   int operator()() {
     constexpr int NQ = (P + 1) * (P + 1) * (P + 1);
@@ -333,10 +300,8 @@ struct StoredJvpTransposeFn {
     if (f.ne == 0) return SFX_OK;
     constexpr bool SYM = sym_of<Maker>::value;
     if constexpr (P == 2 && std::is_same<Real, float>::value) {
-      const int rc =
-          f.tangent16
-              ? launch_tma<C, HS, Maker::value_input, true, __half, SYM>(f, v, di.D16.p, E, s, colored, accumulate)
-              : launch_tma<C, HS, Maker::value_input, true, float, SYM>(f, v, D, E, s, colored, accumulate);
+      const int rc = f.tangent16 ? launch_tma<C, HS, Maker::value_input, true, __half, SYM>(f, v, di.D16.p, E, s)
+                                 : launch_tma<C, HS, Maker::value_input, true, float, SYM>(f, v, D, E, s);
       if (rc) return rc;
     } else {
       constexpr bool SYMR = SYM && std::is_same<Real, float>::value;
@@ -479,18 +444,6 @@ int launch_jvp_transpose(const sfx_form_s& f, const DomainIntegral& di, const do
   if (f.p == 1) return visit_material(di.material, StoredJvpTransposeFn<1, double>{f, di, v, di.D64.p, E, s});
   if (f.p == 2) return visit_material(di.material, StoredJvpTransposeFn<2, double>{f, di, v, di.D64.p, E, s});
   return fail(SFX_ERR_UNSUPPORTED, "order must be 1 or 2");
-}
-
-int launch_jvp_stored_f32_direct(const sfx_form_s& f, const DomainIntegral& di, const float* du, float* dr,
-                                 bool accumulate, cudaStream_t s) {
-  if (f.p != 2 || f.general) return fail(SFX_ERR_UNSUPPORTED, "colour sets need a structured order-2 form");
-  return visit_material(di.material, StoredJvpFn<2, float>{f, di, du, di.D32.p, dr, s, 0, -1, true, accumulate});
-}
-
-int launch_jvp_transpose_f32_direct(const sfx_form_s& f, const DomainIntegral& di, const float* v, float* dr,
-                                    bool accumulate, cudaStream_t s) {
-  if (f.p != 2 || f.general) return fail(SFX_ERR_UNSUPPORTED, "colour sets need a structured order-2 form");
-  return visit_material(di.material, StoredJvpTransposeFn<2, float>{f, di, v, di.D32.p, dr, s, true, accumulate});
 }
 
 int launch_jvp_transpose_f32(const sfx_form_s& f, const DomainIntegral& di, const float* v, float* E,

@@ -72,30 +72,3 @@ def test_host_jvp_rejects_wrong_buffers(cuda):
         grad.mult(torch.tensor(du, dtype=torch.float32))
     with pytest.raises(ValueError):
         grad.mult(torch.tensor(du[:-1]))
-
-
-def test_fp32_colour_set_action_matches_element_scatter(cuda):
-    """The FP32 action of a structured Q2 form adds the element vectors by
-    colour sets straight into the result; it must agree with the element
-    vectors scattered node by node (sfx_jvp_element_f32 + the node-owner sum
-    in float64) to FP32 rounding, on a mesh with a single layer in y (colour
-    sets with no element) and odd counts elsewhere; overlapping du and dr
-    are rejected."""
-    import serac_gb300 as sg
-
-    orc, f = _form(O.MAT_NEOHOOKEAN, 2, (5, 1, 3))
-    u, du = fields(orc.ndofs, O.MAT_NEOHOOKEAN, seed=4, scale=0.1)
-    _, grad = f(0.0, sg.differentiate_wrt(torch.tensor(u, device=cuda)))
-    du32 = torch.tensor(du, device=cuda, dtype=torch.float32)
-    out = grad.mult(du32).double().cpu().numpy()
-    conn = np.asarray(orc.conn)
-    E = grad.element_action(du32).double().cpu().numpy().reshape(conn.shape[0], 3, 27)
-    ref = np.zeros((3, f.num_nodes))
-    for c in range(3):
-        np.add.at(ref[c], conn.ravel(), E[:, c, :].ravel())
-    assert rel(out, ref.ravel()) <= 1e-6
-    assert rel(out, orc.jvp(u, du)) <= 1e-5
-    from serac_gb300._lib import SfxError
-
-    with pytest.raises(SfxError):
-        grad.mult(du32, out=du32)
