@@ -219,9 +219,21 @@ def cpu_slab_processes(reps=5, warmup=1, procs=None):
     workers = [ctx.Process(target=_slab_worker, args=(z0, z1, reps, warmup, barrier, queue)) for z0, z1 in bounds]
     for w in workers:
         w.start()
-    results = dict(queue.get() for _ in workers)
-    for w in workers:
-        w.join()
+    results = {}
+    try:
+        while len(results) < len(workers):
+            try:
+                z0, times = queue.get(timeout=5.0)
+                results[z0] = times
+            except Exception:  # queue.Empty: check that no worker died before reporting
+                dead = [w.exitcode for w in workers if w.exitcode not in (None, 0)]
+                if dead:
+                    raise RuntimeError(f"CPU baseline worker failed (exit codes {dead})")
+    finally:
+        for w in workers:
+            w.join(timeout=60.0)
+            if w.is_alive():
+                w.terminate()
     runs = [max(results[z0][k] for z0, _ in bounds) for k in range(reps)]
     dofs = 3 * (ORDER * NX + 1) ** 3
     return dofs / statistics.median(runs) / 1e9, procs, runs
