@@ -72,13 +72,26 @@ struct BrickConvSmem {
   static constexpr uint32_t NCOLS = cols <= 32 ? 32 : cols <= 64 ? 64 : cols <= 128 ? 128 : 256;
 };
 
+/// The weights W[co][tap][ci] of a brick convolution in its shared-memory
+/// order, [tap][ci / 8][co] x 8 BF16 (K-major core matrices per tap and
+/// K-step), so that one bulk copy stages all 27 taps.  One thread per
+/// 16-byte group of W.
+template <int CIN, int COUT>
+__global__ void pack_brick_weights(const __nv_bfloat16* __restrict__ W, __nv_bfloat16* __restrict__ Wp) {
+  constexpr int GPN = CIN / 8;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= COUT * 27 * GPN) return;
+  const int g8 = i % GPN, tap = (i / GPN) % 27, co = i / (GPN * 27);
+  reinterpret_cast<uint4*>(Wp)[(tap * GPN + g8) * COUT + co] = reinterpret_cast<const uint4*>(W)[i];
+}
+
 /// Forward 3x3x3 convolution as an implicit GEMM on the 5th-generation tensor
 /// cores with a shared-memory brick: each block owns 8 x 16 x BZ output nodes
 /// of one sample.  One thread loads the brick with its halo by tiled TMA
 /// (2 CIN / 16 loads of an 8-channel box through the tensor map `xmap` of the
 /// activations [sample][z][y][x][CIN]; halo nodes outside the grid read
-/// zero), while the block copies the weights of all 27 taps into K-major core
-/// matrices.  For a tap (dx, dy, dz) the A operand of output plane zt (128
+/// zero) and the weights of all 27 taps, pre-packed as K-major core matrices
+/// (pack_brick_weights), by one bulk copy, all on one mbarrier.  For a tap (dx, dy, dz) the A operand of output plane zt (128
 /// rows = 8 x by 16 y nodes) is then the brick itself read through a shifted
 /// descriptor: row group y starts at node ((zt + dz + 1) 18 + y + dy + 1) 10 +
 /// dx + 1 (leading byte offset = one slab between channel halves, stride
@@ -86,13 +99,14 @@ struct BrickConvSmem {
 /// is ever gathered.  One thread issues the 27 x BZ x CIN / 16 MMAs into BZ
 /// tensor-memory accumulators and commits them; the epilogue reads them with
 /// tcgen05.ld (warp w: rows 32w..32w+31 of each plane), adds the bias,
-/// applies the activation and stores BF16 (or FP32 into y_f32).  W: [COUT]
-/// [27][CIN] bf16, bias: [COUT] f32 (may be null), y: [node][COUT] per sample.
+/// applies the activation and stores BF16 (or FP32 into y_f32).  Wp: the
+/// packed weights (27 COUT CIN bf16, 16-byte aligned), bias: [COUT] f32 (may
+/// be null), y: [node][COUT] per sample.
 /// Every wait is bounded: on a timeout the block sets *err, waits (bounded)
 /// for its copies and MMAs in flight and frees its tensor memory.
 template <int CIN, int COUT, int ACT>
 __global__ void __launch_bounds__(128, 1) conv3_fwd_brick(const __grid_constant__ CUtensorMap xmap, Grid3 g,
-                                                       const __nv_bfloat16* __restrict__ W,
+                                                       const __nv_bfloat16* __restrict__ Wp,
                                                        const float* __restrict__ bias, __nv_bfloat16* __restrict__ y,
                                                        float* __restrict__ y_f32, int* __restrict__ err) {
   static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 64, "channel counts");
@@ -123,21 +137,15 @@ __global__ void __launch_bounds__(128, 1) conv3_fwd_brick(const __grid_constant_
   __syncthreads();
   umma::fence_after_sync();
   const uint32_t tmem = tmem_base;
+  constexpr int GPN = CIN / 8;
   if (threadIdx.x == 0) {
-    bulk::mbar_arrive_expect_tx(&bar_load, Bk::BRICK);
+    bulk::mbar_arrive_expect_tx(&bar_load, Bk::BRICK + L::W_BYTES);
 #pragma unroll
     for (int sl = 0; sl < 2 * Bk::KC; sl++)
       bulk::tma_load_5d(brick + uint32_t(sl) * Bk::SLAB, &xmap, sl * 8, bx * Bk::BX - 1, by * Bk::BY - 1, bz * BZ - 1,
                         sample, &bar_load);
+    bulk::copy_g2s(wsm, Wp, L::W_BYTES, &bar_load);
   }
-  // weights W[co][tap][ci] -> [tap][ci / 8][co] x 16 bytes (K-major core matrices per tap and K-step)
-  constexpr int GPN = CIN / 8;
-  const uint4* wsrc = reinterpret_cast<const uint4*>(W);
-  for (int i = threadIdx.x; i < COUT * 27 * GPN; i += blockDim.x) {
-    const int g8 = i % GPN, tap = (i / GPN) % 27, co = i / (GPN * 27);
-    *reinterpret_cast<uint4*>(wsm + ((uint32_t(tap) * GPN + g8) * COUT + co) * 16u) = wsrc[i];
-  }
-  bulk::fence_proxy_async_smem();  // the weights are read by the tensor core (async proxy)
   bool ok = __syncthreads_and(bulk::mbar_wait(&bar_load, 0u));
   umma::fence_after_sync();
   if (ok && threadIdx.x == 0) {

@@ -284,6 +284,15 @@ void flip(int ci, int co, const bf16* W, bf16* Wt, cudaStream_t s) {
   SFX_PAIRS(SFX_FL)
 #undef SFX_FL
 }
+void pack(int ci, int co, const bf16* W, bf16* Wp, cudaStream_t s) {
+#define SFX_PK(CI, CO)                                                                      \
+  if (ci == CI && co == CO) {                                                               \
+    sfx::nn::pack_brick_weights<CI, CO><<<nb(CO * 27 * CI / 8), 256, 0, s>>>(W, Wp);        \
+    return;                                                                                 \
+  }
+  SFX_PAIRS(SFX_PK)
+#undef SFX_PK
+}
 void bias_grad(int co, const float* dy, int64_t rows, float* db, cudaStream_t s) {
   if (co == 16) sfx::nn::bias_grad<16><<<16, 256, 0, s>>>(dy, rows, db);
   else if (co == 32) sfx::nn::bias_grad<32><<<32, 256, 0, s>>>(dy, rows, db);
@@ -320,7 +329,8 @@ struct sfx_lnet_s {
   Conv layers[NLAYERS];
   int64_t nparams = 0;
   DeviceBuf<float> P, G, M, V;  // master parameters, gradient, Adam moments
-  DeviceBuf<bf16> W16[NLAYERS], Wt16[NLAYERS];
+  DeviceBuf<bf16> W16[NLAYERS], Wt16[NLAYERS];    // [co][tap][ci], and flipped for the data gradient
+  DeviceBuf<bf16> Wp16[NLAYERS], Wtp16[NLAYERS];  // the same packed for the brick convolution
   int64_t step = 0;
   std::map<std::tuple<int, int, int>, std::unique_ptr<Work>> work;
 };
@@ -332,6 +342,8 @@ int sync_weights(sfx_lnet net, cudaStream_t s) {
     const Conv& c = net->layers[l];
     f32_to_bf16<<<nb(c.nw()), 256, 0, s>>>(net->P.p + c.off, net->W16[l].p, c.nw());
     flip(c.ci, c.co, net->W16[l].p, net->Wt16[l].p, s);
+    pack(c.ci, c.co, net->W16[l].p, net->Wp16[l].p, s);
+    pack(c.co, c.ci, net->Wt16[l].p, net->Wtp16[l].p, s);
   }
   SFX_CUDA_TRY(cudaGetLastError());
   return SFX_OK;
@@ -400,30 +412,30 @@ void input_scale(Work* w, int B, const float* r, cudaStream_t s) {
 int forward(sfx_lnet net, Work* w, int B, cudaStream_t s) {
   const Grid3* g = w->g;
   const int64_t N0 = g[0].nodes(), N1 = g[1].nodes(), N2 = g[2].nodes(), N3 = g[3].nodes();
-  SFX_TRY(conv_fwd(16, 16, true, g[0], B, w->X0.p, net->W16[A0].p, bias_of(net, A0), w->A0b.p, nullptr, net->wait_error.dev, s));
-  SFX_TRY(conv_fwd(16, 16, true, g[0], B, w->A0b.p, net->W16[B0L].p, bias_of(net, B0L), w->B0b.p, nullptr, net->wait_error.dev, s));
+  SFX_TRY(conv_fwd(16, 16, true, g[0], B, w->X0.p, net->Wp16[A0].p, bias_of(net, A0), w->A0b.p, nullptr, net->wait_error.dev, s));
+  SFX_TRY(conv_fwd(16, 16, true, g[0], B, w->A0b.p, net->Wp16[B0L].p, bias_of(net, B0L), w->B0b.p, nullptr, net->wait_error.dev, s));
   sfx::nn::restrict_to<bf16, bf16><<<grid2(N1 * 16, B), 256, 0, s>>>(g[0], g[1], 16, w->B0b.p, w->C1.p, 0.125f);
-  SFX_TRY(conv_fwd(16, 32, true, g[1], B, w->C1.p, net->W16[A1].p, bias_of(net, A1), w->A1b.p, nullptr, net->wait_error.dev, s));
-  SFX_TRY(conv_fwd(32, 32, true, g[1], B, w->A1b.p, net->W16[B1L].p, bias_of(net, B1L), w->B1b.p, nullptr, net->wait_error.dev, s));
+  SFX_TRY(conv_fwd(16, 32, true, g[1], B, w->C1.p, net->Wp16[A1].p, bias_of(net, A1), w->A1b.p, nullptr, net->wait_error.dev, s));
+  SFX_TRY(conv_fwd(32, 32, true, g[1], B, w->A1b.p, net->Wp16[B1L].p, bias_of(net, B1L), w->B1b.p, nullptr, net->wait_error.dev, s));
   sfx::nn::restrict_to<bf16, bf16><<<grid2(N2 * 32, B), 256, 0, s>>>(g[1], g[2], 32, w->B1b.p, w->C2.p, 0.125f);
-  SFX_TRY(conv_fwd(32, 48, true, g[2], B, w->C2.p, net->W16[A2].p, bias_of(net, A2), w->A2b.p, nullptr, net->wait_error.dev, s));
-  SFX_TRY(conv_fwd(48, 48, true, g[2], B, w->A2b.p, net->W16[B2L].p, bias_of(net, B2L), w->B2b.p, nullptr, net->wait_error.dev, s));
+  SFX_TRY(conv_fwd(32, 48, true, g[2], B, w->C2.p, net->Wp16[A2].p, bias_of(net, A2), w->A2b.p, nullptr, net->wait_error.dev, s));
+  SFX_TRY(conv_fwd(48, 48, true, g[2], B, w->A2b.p, net->Wp16[B2L].p, bias_of(net, B2L), w->B2b.p, nullptr, net->wait_error.dev, s));
   sfx::nn::restrict_to<bf16, bf16><<<grid2(N3 * 48, B), 256, 0, s>>>(g[2], g[3], 48, w->B2b.p, w->C3.p, 0.125f);
-  SFX_TRY(conv_fwd(48, 48, true, g[3], B, w->C3.p, net->W16[A3].p, bias_of(net, A3), w->A3b.p, nullptr, net->wait_error.dev, s));
+  SFX_TRY(conv_fwd(48, 48, true, g[3], B, w->C3.p, net->Wp16[A3].p, bias_of(net, A3), w->A3b.p, nullptr, net->wait_error.dev, s));
   // D2 = P A3 + B2 ; E2 = relu(conv(D2))
   cudaMemsetAsync(w->D2.p, 0, sizeof(float) * N2 * 48 * B, s);
   sfx::nn::prolong_add<bf16><<<grid2(N2 * 48, B), 256, 0, s>>>(g[2], g[3], 48, w->A3b.p, w->D2.p, 1.f);
   add_bf16_into<<<nb(N2 * 48 * B), 256, 0, s>>>(w->B2b.p, w->D2.p, w->D2b.p, N2 * 48 * B);
-  SFX_TRY(conv_fwd(48, 32, true, g[2], B, w->D2b.p, net->W16[U2].p, bias_of(net, U2), w->E2.p, nullptr, net->wait_error.dev, s));
+  SFX_TRY(conv_fwd(48, 32, true, g[2], B, w->D2b.p, net->Wp16[U2].p, bias_of(net, U2), w->E2.p, nullptr, net->wait_error.dev, s));
   cudaMemsetAsync(w->D1.p, 0, sizeof(float) * N1 * 32 * B, s);
   sfx::nn::prolong_add<bf16><<<grid2(N1 * 32, B), 256, 0, s>>>(g[1], g[2], 32, w->E2.p, w->D1.p, 1.f);
   add_bf16_into<<<nb(N1 * 32 * B), 256, 0, s>>>(w->B1b.p, w->D1.p, w->D1b.p, N1 * 32 * B);
-  SFX_TRY(conv_fwd(32, 16, true, g[1], B, w->D1b.p, net->W16[U1].p, bias_of(net, U1), w->E1.p, nullptr, net->wait_error.dev, s));
+  SFX_TRY(conv_fwd(32, 16, true, g[1], B, w->D1b.p, net->Wp16[U1].p, bias_of(net, U1), w->E1.p, nullptr, net->wait_error.dev, s));
   cudaMemsetAsync(w->D0.p, 0, sizeof(float) * N0 * 16 * B, s);
   sfx::nn::prolong_add<bf16><<<grid2(N0 * 16, B), 256, 0, s>>>(g[0], g[1], 16, w->E1.p, w->D0.p, 1.f);
   add_bf16_into<<<nb(N0 * 16 * B), 256, 0, s>>>(w->B0b.p, w->D0.p, w->D0b.p, N0 * 16 * B);
-  SFX_TRY(conv_fwd(16, 16, true, g[0], B, w->D0b.p, net->W16[U0].p, bias_of(net, U0), w->E0.p, nullptr, net->wait_error.dev, s));
-  SFX_TRY(conv_fwd(16, 16, false, g[0], B, w->E0.p, net->W16[OUTL].p, bias_of(net, OUTL), nullptr, w->OUT.p, net->wait_error.dev, s));
+  SFX_TRY(conv_fwd(16, 16, true, g[0], B, w->D0b.p, net->Wp16[U0].p, bias_of(net, U0), w->E0.p, nullptr, net->wait_error.dev, s));
+  SFX_TRY(conv_fwd(16, 16, false, g[0], B, w->E0.p, net->Wp16[OUTL].p, bias_of(net, OUTL), nullptr, w->OUT.p, net->wait_error.dev, s));
   return SFX_OK;
 }
 
@@ -441,7 +453,7 @@ int conv_bwd(sfx_lnet net, Work* w, int l, Grid3 g, int B, const bf16* x, const 
   add_into<<<nb(c.nw()), 256, 0, s>>>(w->red.p, net->G.p + c.off, c.nw());
   bias_grad(c.co, w->gpre.p, rows, w->red.p, s);
   add_into<<<1, 64, 0, s>>>(w->red.p, net->G.p + c.off + c.nw(), c.co);
-  if (gx) SFX_TRY(conv_fwd(c.co, c.ci, false, g, B, w->gpre16.p, net->Wt16[l].p, nullptr, nullptr, gx, net->wait_error.dev, s));
+  if (gx) SFX_TRY(conv_fwd(c.co, c.ci, false, g, B, w->gpre16.p, net->Wtp16[l].p, nullptr, nullptr, gx, net->wait_error.dev, s));
   return SFX_OK;
 }
 
@@ -555,7 +567,9 @@ int sfx_lnet_create(uint64_t seed, sfx_lnet* out) {
             net->M.alloc(p.size()) == cudaSuccess && net->V.alloc(p.size()) == cudaSuccess;
   for (int l = 0; l < NLAYERS && ok; l++)
     ok = net->W16[l].alloc(size_t(net->layers[l].nw())) == cudaSuccess &&
-         net->Wt16[l].alloc(size_t(net->layers[l].nw())) == cudaSuccess;
+         net->Wt16[l].alloc(size_t(net->layers[l].nw())) == cudaSuccess &&
+         net->Wp16[l].alloc(size_t(net->layers[l].nw())) == cudaSuccess &&
+         net->Wtp16[l].alloc(size_t(net->layers[l].nw())) == cudaSuccess;
   if (ok) ok = cudaMemset(net->M.p, 0, p.size() * 4) == cudaSuccess && cudaMemset(net->V.p, 0, p.size() * 4) == cudaSuccess;
   if (!ok || sync_weights(net, nullptr) != SFX_OK || cudaDeviceSynchronize() != cudaSuccess) {
     delete net;
