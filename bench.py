@@ -672,6 +672,29 @@ def solver_options(name, **extra):
     return sg.SolverOptions.defaults(precond=prec, mixed_precision=1, chebyshev_degree=d, chebyshev_ratio=r, **base)
 
 
+def warm_up_variant(name, net):
+    """One load step of the same method on a 4^3 mesh before the timed solve,
+    so that the first use of its kernels in the process (module loading,
+    graph instantiation) stays out of the timed region."""
+    import torch
+
+    import serac_gb300 as sg
+    from serac_gb300 import learned as LP
+
+    S = LP.SolidSetup(LP.neohookean_problem(4, MATERIAL_SEED, sigma_log=SIGMA_LOG, ell=ELL, strain=-FINAL_UZ,
+                                            steps=LOAD_STEPS, bulk_ratio=BULK_RATIO), ORDER)
+    if name.endswith("f16"):
+        S.f.set_tangent_storage(S.f.TANGENT_F16)
+    solver = sg.NewtonSolver(S.f, solver_options(name))
+    solver.set_essential(S.ess)
+    if name.startswith("learned"):
+        solver.set_learned(net, S.grid, S.features)
+    u = torch.zeros(S.f.ndofs, dtype=torch.float64, device="cuda")
+    S.predictor(solver, u, 1)
+    solver.solve(0.0, u, raise_on_failure=False)
+    torch.cuda.synchronize()
+
+
 def newton_leg(steps, variants, n=NX):
     """Newton time-to-1e-8 relative residual on the benchmark problem over the
     first `steps` of its 20 load steps (warm-start predictor, Newton): plain
@@ -701,6 +724,7 @@ def newton_leg(steps, variants, n=NX):
         if name == "learned_mixed" and net is None:
             out[name] = {"unavailable": f"no trained weights at {os.path.relpath(WEIGHTS, ROOT)}"}
             continue
+        warm_up_variant(name, net)
         torch.cuda.synchronize()
         free0 = torch.cuda.mem_get_info()[0]
         S = LP.SolidSetup(prob, ORDER)
