@@ -550,6 +550,59 @@ __global__ void __launch_bounds__(128) shape_jvp_kernel(DomainArgs<double> a, QF
   }
 }
 
+/// The node-owner scatter of a structured mesh (elements e = ex + nx (ey +
+/// ny ez), nodes x + Nx (y + Ny z), Nx = P nx + 1): the elements containing
+/// a node and its local index follow from its grid position, so no node ->
+/// element table is read, and blocks of 32 x 8 nodes of one node plane read
+/// the element vectors of a compact patch.  Sums in increasing element order,
+/// as scatter_kernel, so the result is bitwise that of scatter_kernel.
+/// Node planes [z0, z1) (blockIdx.z + z0).
+template <int P, int C, typename Real>
+__global__ void __launch_bounds__(256) grid_scatter_kernel(const Real* __restrict__ E, Real* __restrict__ out,
+                                                           int nx, int ny, int nz, bool accumulate, int z0) {
+  constexpr int n = P + 1;
+  constexpr int NPE = n * n * n;
+  const int Nx = P * nx + 1, Ny = P * ny + 1;
+  const int x = int(blockIdx.x) * 32 + int(threadIdx.x & 31), y = int(blockIdx.y) * 8 + int(threadIdx.x >> 5);
+  const int z = z0 + int(blockIdx.z);
+  if (x >= Nx || y >= Ny) return;
+  const int64_t num_nodes = int64_t(Nx) * Ny * (int64_t(P) * nz + 1);
+  const int64_t node = x + int64_t(Nx) * (y + int64_t(Ny) * z);
+  // per direction: the (element, local index) pairs containing the node,
+  // lower element first (slot 0 below slot 1; a node inside an element has
+  // slot 0 only)
+  const int I[3] = {x, y, z}, dims[3] = {nx, ny, nz};
+  int el[3][2], lo[3][2];
+  bool ok[3][2];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const int e = I[d] / P, r = I[d] - e * P;
+    el[d][0] = r == 0 ? e - 1 : e;
+    lo[d][0] = r == 0 ? P : r;
+    ok[d][0] = r != 0 || e > 0;
+    el[d][1] = e;
+    lo[d][1] = 0;
+    ok[d][1] = r == 0 && e < dims[d];
+  }
+  Real acc[C];
+#pragma unroll
+  for (int c = 0; c < C; c++) acc[c] = accumulate ? out[c * num_nodes + node] : Real(0);
+#pragma unroll
+  for (int a = 0; a < 2; a++)
+#pragma unroll
+    for (int b = 0; b < 2; b++)
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        if (!(ok[2][a] && ok[1][b] && ok[0][k])) continue;
+        const int64_t e = el[0][k] + int64_t(nx) * (el[1][b] + int64_t(ny) * el[2][a]);
+        const int loc = lo[0][k] + n * (lo[1][b] + n * lo[2][a]);
+#pragma unroll
+        for (int c = 0; c < C; c++) acc[c] += E[(e * C + c) * NPE + loc];
+      }
+#pragma unroll
+  for (int c = 0; c < C; c++) out[c * num_nodes + node] = acc[c];
+}
+
 /// L[c * N + node] (+)= sum over the node's (element, local node) pairs, in
 /// element order, of E[(e * C + c) * NPE + local], for the nodes
 /// [node_begin, node_end).  One thread per node.

@@ -29,6 +29,20 @@ int scatter(const sfx_form_s& f, const Real* E, Real* out, bool accumulate, cuda
             int64_t n1 = -1) {
   if (n1 < 0) n1 = f.nnodes;
   if (n1 <= n0) return SFX_OK;
+  constexpr int P = NPE == 8 ? 1 : 2;
+  if (!f.general && f.mesh.nx > 0) {
+    // structured mesh: whole node planes through the grid scatter (no node -> element table)
+    const int Nx = P * f.mesh.nx + 1, Ny = P * f.mesh.ny + 1;
+    const int64_t plane = int64_t(Nx) * Ny;
+    if (n0 % plane == 0 && n1 % plane == 0) {
+      const dim3 grid{unsigned((Nx + 31) / 32), unsigned((Ny + 7) / 8), unsigned((n1 - n0) / plane)};
+      sfx::kernels::grid_scatter_kernel<P, C, Real>
+          <<<grid, 256, 0, s>>>(E, out, f.mesh.nx, f.mesh.ny, f.mesh.nz, accumulate, int(n0 / plane));
+      cudaError_t err = cudaGetLastError();
+      if (err != cudaSuccess) return fail(SFX_ERR_CUDA, std::string("scatter launch: ") + cudaGetErrorString(err));
+      return SFX_OK;
+    }
+  }
   unsigned blocks = unsigned((n1 - n0 + 255) / 256);
   sfx::kernels::scatter_kernel<C, NPE, Real>
       <<<blocks, 256, 0, s>>>(E, f.node_ptr.p, f.node_ent.p, out, f.nnodes, accumulate, n0, n1);
